@@ -1,0 +1,314 @@
+"""Traversal microbenchmark of the Salty hot path on GB300.
+
+Workload (one step): closest-hit queries for 16,777,216 seeded rays against a
+1,000,000-triangle soup (centroids uniform in [0,1]^3, vertices within +-0.005), BVH
+built on the device with 32-bin SAH and collapsed to 8-wide quantised nodes.  Rays start
+on a radius-2 sphere about (0.5,0.5,0.5) and aim at uniform points of the cube; tmin
+1e-4, tmax inf.  Metric: Mrays/s (rays traced per second), whole job.
+
+  value  device-resident rays and hits (torch CUDA tensors), one salty_trace per step
+  e2e    the same call with rays in pinned host memory and hits written back to it:
+         host->device and device->host copies inside every step
+Rays (512 MiB) and hits (256 MiB) are larger than L2, so no flush is needed between steps;
+the BVH (nodes + leaf triangles) stays resident, as in any traversal.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TRIS = 1_000_000
+N_RAYS = 16_777_216
+SOUP_SEED, RAY_SEED = 20260001, 20260002
+TMIN = 1e-4
+METRIC = "Mrays/s"
+CPU_SAMPLE = 131_072        # rays of the same stream timed on the host cores
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        if shutil.which("nvidia-smi"):
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.out.close()
+
+    def summary(self) -> dict | None:
+        if not self.path or not os.path.exists(self.path):
+            return None
+        rows = [l.strip().split(", ") for l in open(self.path) if l.strip()]
+        os.unlink(self.path)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("SALTY_BENCH_GLOO") is None else "gloo")
+        pg = dist
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x: float, device) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_port_rays_per_s(tris: np.ndarray, rays: np.ndarray) -> tuple[float, int, float]:
+    """The oracle restatement of the reference traversal (the reference's triangle test,
+    no t-culling) on all host cores.  Returns (rays/s, threads, seconds)."""
+    from oracle.oracle import Oracle, build
+    build(with_reference=False)
+    o = Oracle()
+    threads = os.cpu_count() or 1
+    import ctypes as C
+    h = o.L.oracle_bvh_create(np.ascontiguousarray(tris), tris.shape[0])
+    try:
+        n = rays.shape[0]
+        ids = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        u = np.empty(n, np.float32)
+        v = np.empty(n, np.float32)
+        t0 = time.perf_counter()
+        o.L.oracle_trace(h, np.ascontiguousarray(rays), n, 0, 0, threads, ids, t, u, v)
+        dt = time.perf_counter() - t0
+    finally:
+        o.L.oracle_bvh_destroy(h)
+    return n / dt, threads, dt
+
+
+def run_reference(args, ws, rank, local, pg):
+    """The reference's CPU implementation of the path, timed on the host cores."""
+    if rank != 0:
+        return
+    import salty_gb300
+    tris = salty_gb300.microbench_soup(SOUP_SEED, N_TRIS)
+    sample = 16384
+    rays = salty_gb300.microbench_rays(RAY_SEED, sample, TMIN)
+    from oracle.oracle import Oracle, build
+    build(with_reference=False)
+    o = Oracle()
+    threads = os.cpu_count() or 1
+    h = o.L.oracle_bvh_create(tris, N_TRIS)
+    ids = np.empty(sample, np.int32)
+    t = np.empty(sample, np.float32)
+    u = np.empty(sample, np.float32)
+    v = np.empty(sample, np.float32)
+    for _ in range(args.warmup):
+        o.L.oracle_trace(h, rays, sample, 0, 0, threads, ids, t, u, v)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.L.oracle_trace(h, rays, sample, 0, 0, threads, ids, t, u, v)
+    dt = time.perf_counter() - t0
+    o.L.oracle_bvh_destroy(h)
+    value = sample * args.steps / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded PCG soup and rays)",
+        "config": {"workload": "traversal microbenchmark: 1M-triangle soup, closest hit", "n_tris": N_TRIS,
+                   "rays_per_step": sample, "full_rays": N_RAYS},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"first {sample} rays of the 16,777,216-ray stream per step, 1M triangles"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--any-hit", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    ws, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank, local, pg)
+        return
+
+    import torch
+    import salty_gb300
+    from salty_gb300 import build as b
+    b.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = salty_gb300.Context(local)
+    tris = salty_gb300.microbench_soup(SOUP_SEED, N_TRIS)
+    scene = ctx.upload_scene(tris)
+    info = scene.build()
+    rays_h = ctx.pinned((N_RAYS, 8), np.float32)
+    salty_gb300.microbench_rays(RAY_SEED, N_RAYS, TMIN, out=rays_h)
+    hits_h = ctx.pinned((N_RAYS, 4), np.float32)
+    d_rays = torch.from_numpy(rays_h).to(dev)
+    d_hits = torch.empty((N_RAYS, 4), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()  # the library runs on its own stream
+    any_hit = args.any_hit
+
+    # fetch counts (untimed): algorithmic bytes per ray
+    st = scene.trace_raw(d_rays, d_hits, any_hit=any_hit, counters=True)
+    n_node = st["node_fetches"] / N_RAYS
+    n_tri = st["tri_fetches"] / N_RAYS
+    bytes_per_ray = 32 + 16 + 80 * n_node + 48 * n_tri
+
+    # ---- device-resident steps
+    for _ in range(args.warmup):
+        scene.trace_raw(d_rays, d_hits, any_hit=any_hit)
+    barrier(pg)
+    torch.cuda.synchronize()
+    kernel_ms = 0.0
+    with ClockSampler(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            s = scene.trace_raw(d_rays, d_hits, any_hit=any_hit)
+            kernel_ms += s["kernel_ms"]
+        e1.record()
+        torch.cuda.synchronize()
+    barrier(pg)
+    region_ms = e0.elapsed_time(e1)
+    region_ms = max_over_ranks(pg, region_ms, dev)
+    clocks = clk.summary()
+    value = ws * N_RAYS * args.steps / (region_ms / 1e3) / 1e6
+    launch_ms = kernel_ms / args.steps
+
+    # ---- end to end: pinned host rays in, host hits out, every step
+    for _ in range(args.warmup):
+        scene.trace_raw(rays_h, hits_h, any_hit=any_hit)
+    barrier(pg)
+    torch.cuda.synchronize()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record()
+    h2d = d2h = 0
+    e2e_kernels = 0
+    for _ in range(args.steps):
+        s = scene.trace_raw(rays_h, hits_h, any_hit=any_hit)
+        h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
+        e2e_kernels += math.ceil(N_RAYS / (1 << 21))
+    e3.record()
+    torch.cuda.synchronize()
+    barrier(pg)
+    e2e_ms = max_over_ranks(pg, e2.elapsed_time(e3), dev)
+    e2e_value = ws * N_RAYS * args.steps / (e2e_ms / 1e3) / 1e6
+
+    # check: the last device step's hits equal the host path's
+    same = bool(torch.equal(d_hits.cpu(), torch.from_numpy(hits_h)))
+
+    peaks = measured_peaks()
+    achieved = bytes_per_ray * N_RAYS / (launch_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": region_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded PCG soup and rays, generated on the host)",
+        "config": {"workload": "traversal microbenchmark: 1M-triangle soup, 16,777,216 rays, "
+                               + ("any hit" if any_hit else "closest hit"),
+                   "n_tris": N_TRIS, "rays_per_step": N_RAYS, "bvh": "device 32-bin SAH -> 8-wide, 8-bit planes",
+                   "bvh_nodes": info["n_nodes"], "bvh_depth": info["depth"], "bvh_build_ms": info["build_ms"],
+                   "sah_cost": info["sah_cost"], "triangle_test": "reference-compatible (bit-exact ids)",
+                   "l2": "inputs larger than L2 (rays 512 MiB, hits 256 MiB); BVH resident",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": args.steps + e2e_kernels,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "peak_source": peaks["source"], "kernel_ms": launch_ms,
+                     "bytes_per_ray": bytes_per_ray, "node_fetches_per_ray": n_node, "tri_fetches_per_ray": n_tri},
+        "clocks": clocks,
+        "host_device_hits_equal": same,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        sample = CPU_SAMPLE
+        cps, cores, secs = cpu_port_rays_per_s(tris, rays_h[:sample].copy())
+        line["cpu_baseline"] = {"value": cps / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                                "sample": f"first {sample} rays of the same stream, same 1M triangles "
+                                          f"({secs:.1f} s on {cores} threads)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    scene.close()
+    ctx.close()
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

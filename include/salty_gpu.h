@@ -1,0 +1,224 @@
+/* salty_gpu.h -- C ABI of the GB300-native Salty path-tracing hot path.
+ *
+ * The reference (ProjectAsura/Salty) is one Windows executable with an in-process C++
+ * plugin API; it has no DLL or FFI.  Each entry point below replaces a piece of that
+ * API (paths are relative to the reference project's src/ directory):
+ *
+ *   salty_scene_upload   Scene construction: Mesh::Create(n, Vertex*, IMaterial*)
+ *                        (src/s3d_mesh.cpp:539), material factories
+ *                        (src/s3d_materialfactory.cpp:28-132), PinholeCamera::Update
+ *                        (include/s3d_camera.h:63-90), Scene members
+ *                        (include/s3d_scene.h:98-103)
+ *   salty_bvh_build      BVH8::Create / SplitSAH (src/s3d_bvh8.cpp:254-342,401-479)
+ *   salty_trace          Scene::Intersect -> BVH8::IsHit -> Triangle::IsHit
+ *                        (include/s3d_scene.h:63-75, src/s3d_bvh8.cpp:191-206,
+ *                        src/s3d_triangle.cpp:73-105)
+ *   salty_render         PathTracer::TracePath / Radiance / NextEventEstimation
+ *                        (src/s3d_pt.cpp:182-353)
+ *   salty_tonemap        ToneMapper::Map (src/s3d_tonemapper.cpp:206-353) and the sRGB8
+ *                        conversion of PathTracer::Capture (src/s3d_pt.cpp:145-171)
+ *   salty_denoise_nlm    FilterNLM (src/s3d_denoiser.cpp:19-95)
+ *
+ * Conventions.  Every call returns salty_status (0 = OK) and is synchronous on the
+ * context's own CUDA stream.  Array arguments marked "host or device" may be either;
+ * the library checks with cudaPointerGetAttributes and copies host arrays itself.
+ * The caller keeps ownership of every array it passes.  A context is used by one host
+ * thread at a time; separate contexts may run on separate threads.  Sizes are 64-bit.
+ */
+#ifndef SALTY_GPU_H
+#define SALTY_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SALTY_ABI_VERSION 1
+
+typedef enum salty_status {
+    SALTY_OK = 0,
+    SALTY_ERR_INVALID_ARG = 1,
+    SALTY_ERR_OOM = 2,
+    SALTY_ERR_CUDA = 3,
+    SALTY_ERR_TIMEOUT = 4,        /* a bounded device-side wait gave up */
+    SALTY_ERR_QUEUE_OVERFLOW = 5, /* a device queue or traversal stack ran out of room */
+    SALTY_ERR_CANCELLED = 6,      /* salty_ctx_cancel was called during the render */
+    SALTY_ERR_NOT_BUILT = 7,      /* salty_trace/salty_render before salty_bvh_build */
+    SALTY_ERR_CAPACITY = 8        /* input larger than a documented maximum */
+} salty_status;
+
+typedef struct salty_ctx salty_ctx;
+typedef struct salty_scene salty_scene;
+
+/* ---------------------------------------------------------------- context */
+/* Replaces the process-wide state of PathTracer::Run (src/s3d_pt.cpp:77-132). */
+salty_status salty_ctx_create(salty_ctx** out, int device);
+void salty_ctx_destroy(salty_ctx* ctx);
+/* Last error text of this context ("" if none).  Valid until the next call. */
+const char* salty_last_error(const salty_ctx* ctx);
+int salty_abi_version(void);
+/* Requests that a running salty_render stop at the next sample boundary (any thread). */
+void salty_ctx_cancel(salty_ctx* ctx);
+
+/* Page-locked host memory for fast copies (cudaHostAlloc). */
+salty_status salty_host_alloc(salty_ctx* ctx, size_t bytes, void** out);
+void salty_host_free(salty_ctx* ctx, void* p);
+
+/* ---------------------------------------------------------------- scene */
+enum { SALTY_LAMBERT = 0, SALTY_MIRROR = 1, SALTY_GLASS = 2, SALTY_GGX = 3 };
+
+/* IMaterial (include/s3d_material.h:35-42): Lambert (src/s3d_lambert.cpp), Mirror
+ * (src/s3d_mirror.cpp), Glass (src/s3d_glass.cpp) and a GGX conductor (the reference
+ * only has SampleGGX, include/s3d_math.h:2985-2993). */
+typedef struct salty_material {
+    int32_t type;
+    float color[3];     /* Lambert albedo / mirror, glass, GGX specular colour */
+    float emission[3];
+    float ior;          /* glass */
+    float roughness;    /* GGX: alpha = roughness^2 */
+} salty_material;
+
+/* PinholeCamera (include/s3d_camera.h:63-100).  fov is the reference's linear screen
+ * half-extent factor (a 40 degree field of view is fov = 2 tan 20 deg). */
+typedef struct salty_camera {
+    float pos[3], target[3], up[3];
+    float fov;
+    float near_clip;
+} salty_camera;
+
+typedef struct salty_scene_desc {
+    const float* tri_pos;      /* n_tris * 9: v0, v1, v2 (host or device) */
+    const float* tri_nrm;      /* n_tris * 9 shading normals, or NULL (geometric) */
+    const int32_t* tri_mat;    /* n_tris material indices, or NULL (all 0) */
+    int64_t n_tris;
+    const salty_material* mats;  /* host */
+    int32_t n_mats;
+    /* One-sided parallelogram area light, emitting along cross(edge_a, edge_b).  The
+     * library adds its two triangles to the scene (indices n_tris, n_tris + 1). */
+    int32_t has_light;
+    float light_corner[3], light_edge_a[3], light_edge_b[3], light_emission[3];
+    /* Directional (delta) sun: unit direction towards the sun, irradiance. */
+    int32_t has_sun;
+    float sun_dir[3], sun_radiance[3];
+    float sky[3];              /* constant sky radiance (Scene::SampleIBL) */
+    salty_camera camera;
+} salty_scene_desc;
+
+salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* desc, salty_scene** out);
+void salty_scene_destroy(salty_ctx* ctx, salty_scene* scene);
+
+/* ---------------------------------------------------------------- BVH */
+typedef struct salty_build_opts {
+    int32_t bins;          /* SAH bins per axis, 8..32 (default 32) */
+    int32_t max_leaf;      /* triangles per leaf, 1..3 (default 3) */
+    float   trav_cost;     /* SAH node cost relative to one triangle test (default 1) */
+} salty_build_opts;
+
+typedef struct salty_bvh_info {
+    int64_t n_nodes;       /* BVH8 nodes (80 bytes each) */
+    int64_t n_binary;      /* binary nodes built before the collapse */
+    int32_t depth;         /* BVH8 depth (root = 1) */
+    int32_t binary_depth;
+    double  sah_cost;      /* SAH cost of the BVH8 (node cost 1, triangle cost 1) */
+    float   build_ms;      /* device time of the whole build (CUDA events) */
+} salty_bvh_info;
+
+/* Device binned-SAH build collapsed to 8-wide nodes with 8-bit quantised child boxes.
+ * opts may be NULL (defaults).  info may be NULL. */
+salty_status salty_bvh_build(salty_ctx* ctx, salty_scene* scene, const salty_build_opts* opts,
+                             salty_bvh_info* info);
+
+/* ---------------------------------------------------------------- trace */
+typedef struct salty_ray { float org[3]; float tmin; float dir[3]; float tmax; } salty_ray; /* 32 B */
+typedef struct salty_hit { float t; int32_t id; float u, v; } salty_hit;                    /* 16 B */
+
+enum {
+    SALTY_TRACE_ANY_HIT = 1 << 0,     /* stop at the first hit (occlusion); default closest */
+    SALTY_TRACE_WATERTIGHT = 1 << 1,  /* watertight test; default: the reference's test */
+    SALTY_TRACE_COUNTERS = 1 << 2     /* count node/triangle fetches (slower) */
+};
+
+/* Closest or any hit for n rays.  Closest hit: the smallest t the triangle test accepts
+ * in [tmin, tmax]; equal t goes to the lowest triangle index.  Misses: id = -1, t = +inf.
+ * u, v: barycentric weights of v1, v2.  rays/hits: host or device.  Triangle ids are
+ * scene input indices. */
+salty_status salty_trace(salty_ctx* ctx, salty_scene* scene, const salty_ray* rays, int64_t n,
+                         uint32_t flags, salty_hit* hits);
+
+typedef struct salty_trace_stats {
+    double  kernel_ms;       /* device time of the traversal kernel(s), CUDA events */
+    double  total_ms;        /* device time of the call including copies */
+    int64_t rays;
+    int64_t node_fetches;    /* SALTY_TRACE_COUNTERS only */
+    int64_t tri_fetches;     /* SALTY_TRACE_COUNTERS only */
+    int64_t h2d_bytes, d2h_bytes;
+} salty_trace_stats;
+/* Statistics of the last salty_trace on this context. */
+salty_status salty_last_trace_stats(const salty_ctx* ctx, salty_trace_stats* out);
+
+/* ---------------------------------------------------------------- render */
+enum { SALTY_PROFILE_COMPAT = 0, SALTY_PROFILE_PHYSICAL = 1 };
+enum { SALTY_TM_NONE = -1, SALTY_TM_REINHARD = 0, SALTY_TM_UNCHARTED2 = 1, SALTY_TM_ACES = 2 };
+
+typedef struct salty_render_opts {
+    int32_t width, height;
+    int32_t spp;            /* samples per pixel added by this call */
+    int32_t max_depth;      /* path segments (PathTracer::Config::MaxBounceCount) */
+    int32_t rr_depth;       /* physical profile: Russian roulette from this depth */
+    int32_t profile;        /* SALTY_PROFILE_* */
+    uint64_t seed;
+    int32_t accumulate;     /* 0: clear the film first; 1: add to it (progressive) */
+    int32_t fp64;           /* accumulate in double (converged oracle images) */
+    int32_t tonemap;        /* SALTY_TM_* for srgb8 output */
+    int32_t ref_oetf;       /* 1: the reference's pow(1.055x, 1/2.4) - 0.055 OETF */
+} salty_render_opts;
+
+typedef struct salty_render_stats {
+    double  ms;               /* device time of the render call */
+    int64_t samples;          /* camera samples in the film after the call */
+    int64_t rays;             /* primary + extension + shadow rays traced by the call */
+    int64_t paths;            /* camera paths traced by the call */
+} salty_render_stats;
+
+/* Renders opts->spp samples per pixel into the scene's film (wavefront path tracer), then
+ * writes the film's per-pixel mean (mean_rgb, W*H*3 float), the variance of that mean
+ * (var_rgb) and the tonemapped sRGB8 image (srgb8, W*H*3).  Any output may be NULL;
+ * outputs are host or device. */
+salty_status salty_render(salty_ctx* ctx, salty_scene* scene, const salty_render_opts* opts,
+                          float* mean_rgb, float* var_rgb, uint8_t* srgb8, salty_render_stats* stats);
+
+/* Film sums as stored (W*H*3 each): FP32 sum + Kahan compensation, or FP64 sums when the
+ * film was rendered with fp64.  Arrays host or device; NULL skips. */
+salty_status salty_film_read(salty_ctx* ctx, salty_scene* scene, double* sum, double* sumsq,
+                             int64_t* samples);
+
+/* ---------------------------------------------------------------- post */
+/* ToneMapper::Map on a W*H*3 linear image, optionally followed by the sRGB8 conversion.
+ * out_rgb / out_srgb8 may be NULL.  Arrays host or device. */
+salty_status salty_tonemap(salty_ctx* ctx, int32_t type, int32_t width, int32_t height,
+                           const float* rgb, float* out_rgb, uint8_t* out_srgb8, int32_t ref_oetf,
+                           float* ave_lw, float* max_lw);
+
+/* FilterNLM as the reference defines it: RGBA, 5x5 patch, 13x13 search, h = sigma = coeff. */
+salty_status salty_denoise_nlm_ref(salty_ctx* ctx, int32_t width, int32_t height, float coeff,
+                                   const float* rgba, float* out);
+
+/* Variance-scaled NLM on RGB with per-pixel variance of the mean (W*H*3 each):
+ * search window (2 search_r + 1)^2, patch (2 patch_r + 1)^2, strength k. */
+salty_status salty_denoise_nlm(salty_ctx* ctx, int32_t width, int32_t height, int32_t search_r,
+                               int32_t patch_r, float k, const float* rgb, const float* var,
+                               float* out);
+
+/* ---------------------------------------------------------------- inputs */
+/* The traversal microbenchmark's seeded inputs (host arrays): a triangle soup with
+ * centroids uniform in [0,1]^3 and vertices within +-0.005, and rays from a radius-2
+ * sphere about (0.5,0.5,0.5) towards uniform points of the cube. */
+salty_status salty_microbench_soup(uint64_t seed, int64_t n, float* tri_pos);
+salty_status salty_microbench_rays(uint64_t seed, int64_t n, float tmin, salty_ray* rays);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SALTY_GPU_H */

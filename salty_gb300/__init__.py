@@ -1,0 +1,345 @@
+"""salty_gb300 -- GB300-native path-tracing hot path of ProjectAsura/Salty.
+
+Python host mirror over the C ABI of include/salty_gpu.h (libsalty_gpu.so, built
+in-tree by salty_gb300/build.py).  Every call goes to the CUDA library; if the
+library is missing or has no GPU the calls raise -- there is no CPU fallback.
+
+Mapping to the reference's API (paths relative to the reference project's src/):
+  Context.upload_scene  Scene construction (Mesh::Create, material factories,
+                        PinholeCamera::Update; include/s3d_scene.h:22-109)
+  Scene.build           BVH8::Create (src/s3d_bvh8.cpp:401-479)
+  Scene.trace           Scene::Intersect (include/s3d_scene.h:63-75)
+  Scene.render          PathTracer::TracePath / Radiance (src/s3d_pt.cpp:182-353)
+  Context.tonemap       ToneMapper::Map + the sRGB8 step of PathTracer::Capture
+  Context.nlm_ref       FilterNLM (src/s3d_denoiser.cpp:19-95)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libsalty_gpu.so")
+
+OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_QUEUE_OVERFLOW, ERR_CANCELLED, ERR_NOT_BUILT, ERR_CAPACITY = range(9)
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT", 5: "QUEUE_OVERFLOW",
+                6: "CANCELLED", 7: "NOT_BUILT", 8: "CAPACITY"}
+LAMBERT, MIRROR, GLASS, GGX = 0, 1, 2, 3
+TRACE_ANY_HIT, TRACE_WATERTIGHT, TRACE_COUNTERS = 1, 2, 4
+PROFILE_COMPAT, PROFILE_PHYSICAL = 0, 1
+TM_NONE, TM_REINHARD, TM_UNCHARTED2, TM_ACES = -1, 0, 1, 2
+
+
+class SaltyError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"salty: {STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Material(C.Structure):
+    _fields_ = [("type", C.c_int32), ("color", C.c_float * 3), ("emission", C.c_float * 3),
+                ("ior", C.c_float), ("roughness", C.c_float)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3),
+                ("fov", C.c_float), ("near_clip", C.c_float)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("tri_pos", C.c_void_p), ("tri_nrm", C.c_void_p), ("tri_mat", C.c_void_p),
+                ("n_tris", C.c_int64), ("mats", C.c_void_p), ("n_mats", C.c_int32),
+                ("has_light", C.c_int32), ("light_corner", C.c_float * 3), ("light_edge_a", C.c_float * 3),
+                ("light_edge_b", C.c_float * 3), ("light_emission", C.c_float * 3),
+                ("has_sun", C.c_int32), ("sun_dir", C.c_float * 3), ("sun_radiance", C.c_float * 3),
+                ("sky", C.c_float * 3), ("camera", Camera)]
+
+
+class BuildOpts(C.Structure):
+    _fields_ = [("bins", C.c_int32), ("max_leaf", C.c_int32), ("trav_cost", C.c_float)]
+
+
+class BvhInfo(C.Structure):
+    _fields_ = [("n_nodes", C.c_int64), ("n_binary", C.c_int64), ("depth", C.c_int32),
+                ("binary_depth", C.c_int32), ("sah_cost", C.c_double), ("build_ms", C.c_float)]
+
+
+class TraceStats(C.Structure):
+    _fields_ = [("kernel_ms", C.c_double), ("total_ms", C.c_double), ("rays", C.c_int64),
+                ("node_fetches", C.c_int64), ("tri_fetches", C.c_int64), ("h2d_bytes", C.c_int64),
+                ("d2h_bytes", C.c_int64)]
+
+
+class RenderOpts(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
+                ("rr_depth", C.c_int32), ("profile", C.c_int32), ("seed", C.c_uint64), ("accumulate", C.c_int32),
+                ("fp64", C.c_int32), ("tonemap", C.c_int32), ("ref_oetf", C.c_int32)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("ms", C.c_double), ("samples", C.c_int64), ("rays", C.c_int64), ("paths", C.c_int64)]
+
+
+# Every extern "C" symbol declared in include/salty_gpu.h.
+EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_abi_version", "salty_ctx_cancel",
+           "salty_host_alloc", "salty_host_free", "salty_scene_upload", "salty_scene_destroy", "salty_bvh_build",
+           "salty_trace", "salty_last_trace_stats", "salty_render", "salty_film_read", "salty_tonemap",
+           "salty_denoise_nlm_ref", "salty_denoise_nlm", "salty_microbench_soup", "salty_microbench_rays"]
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libsalty_gpu.so (raises if it was not built: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise SaltyError(ERR_CUDA, f"{LIB_PATH} is missing; run __graft_entry__.build() or salty_gb300/build.py")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, u32, u64, f32 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint32, C.c_uint64, C.c_float
+    sig = {
+        "salty_ctx_create": (i32, [C.POINTER(vp), C.c_int]),
+        "salty_ctx_destroy": (None, [vp]),
+        "salty_last_error": (C.c_char_p, [vp]),
+        "salty_abi_version": (C.c_int, []),
+        "salty_ctx_cancel": (None, [vp]),
+        "salty_host_alloc": (i32, [vp, C.c_size_t, C.POINTER(vp)]),
+        "salty_host_free": (None, [vp, vp]),
+        "salty_scene_upload": (i32, [vp, C.POINTER(SceneDesc), C.POINTER(vp)]),
+        "salty_scene_destroy": (None, [vp, vp]),
+        "salty_bvh_build": (i32, [vp, vp, C.POINTER(BuildOpts), C.POINTER(BvhInfo)]),
+        "salty_trace": (i32, [vp, vp, vp, i64, u32, vp]),
+        "salty_last_trace_stats": (i32, [vp, C.POINTER(TraceStats)]),
+        "salty_render": (i32, [vp, vp, C.POINTER(RenderOpts), vp, vp, vp, C.POINTER(RenderStats)]),
+        "salty_film_read": (i32, [vp, vp, vp, vp, C.POINTER(i64)]),
+        "salty_tonemap": (i32, [vp, i32, i32, i32, vp, vp, vp, i32, C.POINTER(f32), C.POINTER(f32)]),
+        "salty_denoise_nlm_ref": (i32, [vp, i32, i32, f32, vp, vp]),
+        "salty_denoise_nlm": (i32, [vp, i32, i32, i32, i32, f32, vp, vp, vp]),
+        "salty_microbench_soup": (i32, [u64, i64, vp]),
+        "salty_microbench_rays": (i32, [u64, i64, f32, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a) -> int:
+    """Address of a numpy array or a torch tensor (host or CUDA)."""
+    if a is None:
+        return 0
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        if not a.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return a.data_ptr()
+    raise TypeError(f"unsupported buffer {type(a)}")
+
+
+def _f3(v) -> C.Array:
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+def microbench_soup(seed: int, n: int) -> np.ndarray:
+    out = np.empty((n, 9), np.float32)
+    st = lib().salty_microbench_soup(seed, n, _ptr(out))
+    if st:
+        raise SaltyError(st, "microbench_soup")
+    return out
+
+
+def microbench_rays(seed: int, n: int, tmin: float = 1e-4, out: np.ndarray | None = None) -> np.ndarray:
+    if out is None:
+        out = np.empty((n, 8), np.float32)
+    st = lib().salty_microbench_rays(seed, n, tmin, _ptr(out))
+    if st:
+        raise SaltyError(st, "microbench_rays")
+    return out
+
+
+class Context:
+    """A device, its stream and scratch (salty_ctx)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        st = lib().salty_ctx_create(C.byref(h), device)
+        if st:
+            raise SaltyError(st, f"salty_ctx_create(device={device}) failed (is a GPU present?)")
+        self.h = h
+        self._pinned = []
+
+    def check(self, st: int, what: str) -> None:
+        if st:
+            raise SaltyError(st, f"{what}: {lib().salty_last_error(self.h).decode(errors='replace')}")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            for p in self._pinned:
+                lib().salty_host_free(self.h, p)
+            self._pinned = []
+            lib().salty_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def pinned(self, shape, dtype=np.float32) -> np.ndarray:
+        """A numpy array in page-locked host memory owned by this context."""
+        nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        p = C.c_void_p()
+        self.check(lib().salty_host_alloc(self.h, nbytes, C.byref(p)), "host_alloc")
+        self._pinned.append(p)
+        buf = (C.c_char * nbytes).from_address(p.value)
+        return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def upload_scene(self, tri_pos, tri_nrm=None, tri_mat=None, materials=(), light=None, sun=None,
+                     sky=(0.0, 0.0, 0.0), camera=None) -> "Scene":
+        tri_pos = tri_pos if hasattr(tri_pos, "data_ptr") else np.ascontiguousarray(tri_pos, np.float32)
+        n = tri_pos.shape[0] if tri_pos.ndim == 2 else tri_pos.size // 9
+        if tri_nrm is not None and not hasattr(tri_nrm, "data_ptr"):
+            tri_nrm = np.ascontiguousarray(tri_nrm, np.float32)
+        if tri_mat is not None and not hasattr(tri_mat, "data_ptr"):
+            tri_mat = np.ascontiguousarray(tri_mat, np.int32)
+        mats = (Material * max(1, len(materials)))()
+        for i, m in enumerate(materials):
+            mats[i].type = int(m.get("type", LAMBERT))
+            mats[i].color = _f3(m.get("color", (0.75, 0.75, 0.75)))
+            mats[i].emission = _f3(m.get("emission", (0, 0, 0)))
+            mats[i].ior = float(m.get("ior", 1.5))
+            mats[i].roughness = float(m.get("roughness", 0.3))
+        d = SceneDesc()
+        d.tri_pos, d.tri_nrm, d.tri_mat = _ptr(tri_pos), _ptr(tri_nrm), _ptr(tri_mat)
+        d.n_tris = n
+        d.mats = C.addressof(mats) if materials else None
+        d.n_mats = len(materials)
+        if light:
+            d.has_light = 1
+            d.light_corner, d.light_edge_a = _f3(light["corner"]), _f3(light["edge_a"])
+            d.light_edge_b, d.light_emission = _f3(light["edge_b"]), _f3(light["emission"])
+        if sun:
+            d.has_sun = 1
+            d.sun_dir, d.sun_radiance = _f3(sun["dir"]), _f3(sun["radiance"])
+        d.sky = _f3(sky)
+        cam = camera or {"pos": (0, 0, -1), "target": (0, 0, 0), "up": (0, 1, 0), "fov": 1.0}
+        d.camera.pos, d.camera.target, d.camera.up = _f3(cam["pos"]), _f3(cam["target"]), _f3(cam["up"])
+        d.camera.fov = float(cam["fov"])
+        d.camera.near_clip = float(cam.get("near", 1.0))
+        h = C.c_void_p()
+        self.check(lib().salty_scene_upload(self.h, C.byref(d), C.byref(h)), "scene_upload")
+        return Scene(self, h, n)
+
+    def tonemap(self, img, type_: int = TM_REINHARD, srgb: bool = True, ref_oetf: bool = True):
+        img = img if hasattr(img, "data_ptr") else np.ascontiguousarray(img, np.float32)
+        h, w = img.shape[:2]
+        out = np.empty((h, w, 3), np.float32)
+        s8 = np.empty((h, w, 3), np.uint8) if srgb else None
+        ave, mx = C.c_float(), C.c_float()
+        self.check(lib().salty_tonemap(self.h, type_, w, h, _ptr(img), _ptr(out), _ptr(s8), int(ref_oetf),
+                                       C.byref(ave), C.byref(mx)), "tonemap")
+        return out, s8, ave.value, mx.value
+
+    def nlm_ref(self, rgba, coeff: float):
+        rgba = np.ascontiguousarray(rgba, np.float32)
+        h, w = rgba.shape[:2]
+        out = np.empty_like(rgba)
+        self.check(lib().salty_denoise_nlm_ref(self.h, w, h, coeff, _ptr(rgba), _ptr(out)), "nlm_ref")
+        return out
+
+    def nlm(self, rgb, var, search_r: int = 10, patch_r: int = 3, k: float = 0.45):
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        var = np.ascontiguousarray(var, np.float32)
+        h, w = rgb.shape[:2]
+        out = np.empty_like(rgb)
+        self.check(lib().salty_denoise_nlm(self.h, w, h, search_r, patch_r, k, _ptr(rgb), _ptr(var), _ptr(out)),
+                   "nlm")
+        return out
+
+
+@dataclass
+class TraceResult:
+    ids: np.ndarray
+    t: np.ndarray
+    u: np.ndarray
+    v: np.ndarray
+
+
+class Scene:
+    """A device scene (salty_scene): triangles, materials, lights, camera, BVH, film."""
+
+    def __init__(self, ctx: Context, h: C.c_void_p, n_tris: int):
+        self.ctx, self.h, self.n_tris = ctx, h, n_tris
+        self.info = None
+
+    def close(self) -> None:
+        if getattr(self, "h", None) and self.ctx.h:
+            lib().salty_scene_destroy(self.ctx.h, self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build(self, bins: int = 32, max_leaf: int = 3, trav_cost: float = 1.0) -> dict:
+        o = BuildOpts(bins, max_leaf, trav_cost)
+        info = BvhInfo()
+        self.ctx.check(lib().salty_bvh_build(self.ctx.h, self.h, C.byref(o), C.byref(info)), "bvh_build")
+        self.info = {k: getattr(info, k) for k, _ in BvhInfo._fields_}
+        return self.info
+
+    def trace_raw(self, rays, hits, n: int | None = None, any_hit=False, watertight=False, counters=False) -> dict:
+        """rays (n,8) float32 and hits (n,4) 16-byte records; numpy (host) or torch CUDA tensors."""
+        flags = (TRACE_ANY_HIT if any_hit else 0) | (TRACE_WATERTIGHT if watertight else 0) | \
+                (TRACE_COUNTERS if counters else 0)
+        if n is None:
+            n = rays.shape[0]
+        self.ctx.check(lib().salty_trace(self.ctx.h, self.h, _ptr(rays), n, flags, _ptr(hits)), "trace")
+        s = TraceStats()
+        lib().salty_last_trace_stats(self.ctx.h, C.byref(s))
+        return {k: getattr(s, k) for k, _ in TraceStats._fields_}
+
+    def trace(self, rays: np.ndarray, any_hit=False, watertight=False, counters=False) -> TraceResult:
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        hits = np.empty((rays.shape[0], 4), np.float32)
+        self.last_stats = self.trace_raw(rays, hits, any_hit=any_hit, watertight=watertight, counters=counters)
+        return TraceResult(hits[:, 1].copy().view(np.int32), hits[:, 0].copy(), hits[:, 2].copy(), hits[:, 3].copy())
+
+    def render(self, width: int, height: int, spp: int, max_depth: int, rr_depth: int = 3,
+               profile: int = PROFILE_PHYSICAL, seed: int = 1, accumulate: bool = False, fp64: bool = False,
+               tonemap: int = TM_REINHARD, ref_oetf: bool = True, want=("mean", "var", "srgb")) -> dict:
+        o = RenderOpts(width, height, spp, max_depth, rr_depth, profile, seed, int(accumulate), int(fp64),
+                       tonemap, int(ref_oetf))
+        mean = np.empty((height, width, 3), np.float32) if "mean" in want else None
+        var = np.empty((height, width, 3), np.float32) if "var" in want else None
+        s8 = np.empty((height, width, 3), np.uint8) if "srgb" in want else None
+        st = RenderStats()
+        self.ctx.check(lib().salty_render(self.ctx.h, self.h, C.byref(o), _ptr(mean), _ptr(var), _ptr(s8),
+                                          C.byref(st)), "render")
+        return {"mean": mean, "var": var, "srgb": s8, "ms": st.ms, "samples": st.samples, "rays": st.rays,
+                "paths": st.paths}
+
+    def film(self, width: int, height: int):
+        s = np.empty((height, width, 3), np.float64)
+        q = np.empty((height, width, 3), np.float64)
+        n = C.c_int64()
+        self.ctx.check(lib().salty_film_read(self.ctx.h, self.h, _ptr(s), _ptr(q), C.byref(n)), "film_read")
+        return s, q, n.value

@@ -1,0 +1,203 @@
+// internal.h -- shared host/device definitions of libsalty_gpu (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/salty_gpu.h"
+
+namespace salty {
+
+// ------------------------------------------------------------------ BVH8 node
+// 80 bytes, read as five 16-byte loads:
+//   w0: origin p (3 x f32), packed exponents ex|ey<<8|ez<<16 | imask<<24
+//   w1: child_base, tri_base, meta[0..3], meta[4..7]
+//   w2: qlo_x[8], qlo_y[8]      w3: qlo_z[8], qhi_x[8]      w4: qhi_y[8], qhi_z[8]
+// Child slot s covers [p + qlo*2^e, p + qhi*2^e] per axis (e = byte - 127); the
+// quantised box contains the child's exact box.  Slot bit a is 1 when the child lies on
+// the high side of the node centre along axis a, so visiting slots in increasing order
+// of (slot XOR ray-octant) is roughly front to back.  imask bit s: slot s is an inner
+// node, numbered child_base + popc(imask & ((1<<s)-1)).  A leaf slot's meta byte is
+// (count << 5) | offset: triangles tri_base + offset .. + count - 1.  Empty slots have
+// qlo = 255 > qhi = 0, an empty box.
+struct alignas(16) Bvh8Node {
+    uint4 w[5];
+};
+static_assert(sizeof(Bvh8Node) == 80, "node layout");
+
+constexpr int kMaxLeafTris = 3;
+constexpr int kMaxNodeTris = 24;
+
+// Leaf-ordered triangle: three float4, v0.xyz + input id (int bits), v1.xyz, v2.xyz.
+constexpr int kTriFloat4 = 3;
+
+// Binary build node (32 bytes).  count > 0: leaf over prim positions [a, a + count);
+// count == 0: inner node with children a and a + 1.
+struct alignas(16) BNode {
+    float lo[3];
+    int a;
+    float hi[3];
+    int count;
+};
+
+// ------------------------------------------------------------------ errors
+struct ErrorSink {
+    std::string msg;
+    salty_status fail(salty_status s, const char* fmt, ...) {
+        char buf[1024];
+        va_list ap;
+        va_start(ap, fmt);
+        std::vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        msg = buf;
+        return s;
+    }
+};
+
+#define SALTY_TRY_CUDA(sink, expr)                                                              \
+    do {                                                                                        \
+        cudaError_t e__ = (expr);                                                               \
+        if (e__ != cudaSuccess)                                                                 \
+            return (sink).fail(e__ == cudaErrorMemoryAllocation ? SALTY_ERR_OOM : SALTY_ERR_CUDA, \
+                               "%s:%d %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(e__)); \
+    } while (0)
+
+#define SALTY_TRY(expr)                       \
+    do {                                      \
+        salty_status s__ = (expr);            \
+        if (s__ != SALTY_OK) return s__;      \
+    } while (0)
+
+// ------------------------------------------------------------------ device buffers
+// Grow-only device allocation (cudaMalloc); contents are not preserved on growth.
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= cap && p) return cudaSuccess;
+        release();
+        size_t want = n ? n : 1;
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e == cudaSuccess) cap = want;
+        else p = nullptr;
+        return e;
+    }
+};
+
+// ------------------------------------------------------------------ scene
+struct GpuMaterial {
+    int type;
+    float color[3];
+    float emission[3];
+    float ior;
+    float roughness;
+    float rr_threshold;  // compat Lambert dice threshold max(albedo, 0.01)
+};
+
+struct SceneConsts {
+    int has_light;
+    float lc[3], la[3], lb[3], ln[3], le[3];
+    float larea;
+    int light_tri0;      // first light triangle id (n_tris of the input), -1 if none
+    int has_sun;
+    float sun_dir[3], sun_rad[3];
+    float sky[3];
+    float cam_pos[3], cam_cx[3], cam_cy[3], cam_cz[3];
+    float cam_fov, cam_near;
+    float cam_target[3], cam_up[3];
+};
+
+struct Film {
+    int width = 0, height = 0;
+    int fp64 = 0;
+    int64_t samples = 0;
+    DevBuf<float> sum, comp, sumsq;      // FP32 sum with Kahan compensation
+    DevBuf<double> sum64, sumsq64;       // FP64 film
+};
+
+struct Bvh {
+    DevBuf<Bvh8Node> nodes;
+    DevBuf<float4> tris;        // leaf order, kTriFloat4 per triangle
+    int64_t n_nodes = 0;
+    int32_t depth = 0;
+    bool built = false;
+    salty_bvh_info info{};
+};
+
+}  // namespace salty
+
+struct salty_scene {
+    int64_t n_tris = 0;          // including the two light triangles
+    int64_t n_input = 0;         // triangles given by the caller
+    salty::DevBuf<float> pos;    // n_tris * 9
+    salty::DevBuf<float> nrm;    // n_tris * 9
+    salty::DevBuf<int> mat;      // n_tris
+    salty::DevBuf<salty::GpuMaterial> mats;
+    int n_mats = 0;
+    salty::SceneConsts consts{};
+    salty::Bvh bvh;
+    salty::Film film;
+};
+
+struct salty_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev[8] = {};
+    salty::ErrorSink err;
+    salty_trace_stats last_trace{};
+    volatile int cancel = 0;
+    // scratch shared by calls on this context
+    salty::DevBuf<unsigned char> scratch;
+    salty::DevBuf<float4> ray_buf;
+    salty::DevBuf<float4> hit_buf;
+    salty::DevBuf<unsigned long long> counters;
+    salty::DevBuf<int> status;   // device status word(s)
+    void* pinned = nullptr;      // small pinned readback area
+};
+
+namespace salty {
+// bvh_build.cu
+salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& opts);
+// trace.cu
+salty_status trace_launch(salty_ctx* ctx, salty_scene* sc, const float4* d_rays, long long n,
+                          const int* n_dev, uint32_t flags, float4* d_hits,
+                          unsigned long long* d_counters, cudaStream_t st, int* d_status);
+// render.cu
+salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
+                    salty_render_stats* stats);
+salty_status film_outputs(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
+                          float* d_mean, float* d_var, uint8_t* d_srgb);
+// post.cu
+salty_status tonemap_device(salty_ctx* ctx, int type, int w, int h, const float* d_rgb,
+                            float* d_out, uint8_t* d_srgb, int ref_oetf, float* ave, float* mx);
+salty_status nlm_ref_device(salty_ctx* ctx, int w, int h, float coeff, const float* d_in,
+                            float* d_out);
+salty_status nlm_var_device(salty_ctx* ctx, int w, int h, int search_r, int patch_r, float k,
+                            const float* d_rgb, const float* d_var, float* d_out);
+
+inline bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+}  // namespace salty

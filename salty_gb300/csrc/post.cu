@@ -1,0 +1,317 @@
+// post.cu -- tonemapping, sRGB8 and the NLM denoisers.
+//
+//   ToneMapper::Map (src/s3d_tonemapper.cpp:206-353): a log-average / max-luminance
+//   reduction, then a per-pixel curve (Reinhard, Uncharted2, ACES) fused with the clamp,
+//   OETF and 8-bit rounding of PathTracer::Capture (src/s3d_pt.cpp:145-171).  Both passes
+//   stream the image once (HBM bound); per-pixel arithmetic keeps the reference's
+//   operation order with separately rounded products.  The reduction sums log terms in
+//   double, where the reference adds them one by one in single precision.
+//   FilterNLM (src/s3d_denoiser.cpp:19-95): each block stages its tile plus halo in
+//   shared memory and evaluates the reference's weights in the reference's order.
+#include <cfloat>
+#include <cstring>
+
+#include "internal.h"
+
+namespace salty {
+namespace {
+
+__device__ __forceinline__ int f2o(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float o2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+inline int f2o_host(float f) {
+    int i;
+    std::memcpy(&i, &f, 4);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+
+struct LumAcc {
+    double sum;
+    int maxo;
+    int pad;
+};
+
+// RGBToY (src/s3d_tonemapper.cpp:31-33)
+__device__ __forceinline__ float rgb_to_y(float r, float g, float b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(0.299f, r), __fmul_rn(0.587f, g)), __fmul_rn(0.114f, b));
+}
+
+constexpr int kRedBlock = 256;
+
+__global__ void __launch_bounds__(kRedBlock) k_lum_reduce(const float* __restrict__ rgb, long long npx, LumAcc* acc) {
+    const float eps = 0.00001f;
+    double s = 0.0;
+    float mx = -FLT_MAX;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx;
+         i += (long long)gridDim.x * blockDim.x) {
+        float lw = rgb_to_y(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+        if (lw != lw) lw = eps;
+        if (lw < FLT_EPSILON) lw = eps;
+        mx = fmaxf(mx, lw);
+        s += (double)logf(__fadd_rn(eps, lw));
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, off);
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    }
+    __shared__ double ss[kRedBlock / 32];
+    __shared__ float sm[kRedBlock / 32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { ss[w] = s; sm[w] = mx; }
+    __syncthreads();
+    if (w == 0) {
+        s = l < kRedBlock / 32 ? ss[l] : 0.0;
+        mx = l < kRedBlock / 32 ? sm[l] : -FLT_MAX;
+        for (int off = 16; off > 0; off >>= 1) {
+            s += __shfl_xor_sync(0xffffffffu, s, off);
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+        }
+        if (l == 0) {
+            atomicAdd(&acc->sum, s);
+            atomicMax(&acc->maxo, f2o(mx));
+        }
+    }
+}
+
+__device__ __forceinline__ float u2_curve(float x) {
+    const float A = 0.15f, B = 0.50f, C = 0.10f, D = 0.20f, E = 0.01f, F = 0.30f;
+    // ((x*(A*x + C*B) + D*E) / (x*(A*x + B) + D*F)) - E/F
+    float num = __fadd_rn(__fmul_rn(x, __fadd_rn(__fmul_rn(A, x), __fmul_rn(C, B))), __fmul_rn(D, E));
+    float den = __fadd_rn(__fmul_rn(x, __fadd_rn(__fmul_rn(A, x), B)), __fmul_rn(D, F));
+    return __fsub_rn(__fdiv_rn(num, den), __fdiv_rn(E, F));
+}
+
+__device__ __forceinline__ float saturate(float x) { return x < 0.0f ? 0.0f : (x > 1.0f ? 1.0f : x); }
+
+// ACESFilm (src/s3d_tonemapper.cpp:117-130)
+__device__ __forceinline__ float aces_curve(float x) {
+    const float a = 2.51f, b = 0.03f, c = 2.43f, d = 0.59f, e = 0.14f, f = 0.665406f, g = 12.0f;
+    float num = __fmul_rn(x, __fadd_rn(__fdiv_rn(__fmul_rn(__fmul_rn(a, x), f), g), b));
+    float den = __fadd_rn(__fmul_rn(__fdiv_rn(__fmul_rn(x, f), g), __fadd_rn(__fmul_rn(__fmul_rn(c, x), f), d)), e);
+    return saturate(__fdiv_rn(num, den));
+}
+
+__device__ __forceinline__ unsigned char to_srgb8(float x, int ref_oetf) {
+    if (x > 1.0f) x = 1.0f;
+    if (x < 0.0f) x = 0.0f;
+    if (x != x) x = 0.0f;
+    if (ref_oetf)
+        x = (x <= 0.0031308f) ? __fmul_rn(12.92f, x) : __fsub_rn(powf(__fmul_rn(1.055f, x), 1.0f / 2.4f), 0.055f);
+    else
+        x = (x <= 0.0031308f) ? __fmul_rn(12.92f, x) : __fsub_rn(__fmul_rn(1.055f, powf(x, 1.0f / 2.4f)), 0.055f);
+    return (unsigned char)__fadd_rn(__fmul_rn(x, 255.0f), 0.5f);
+}
+
+struct TmParams {
+    int type;
+    float coeff;
+    float m2;      // Reinhard (maxLw * coeff)^2
+    float white;   // Uncharted2 curve at LinearWhite
+    int ref_oetf;
+};
+
+__global__ void k_tonemap(const float* __restrict__ in, long long n, TmParams p, float* __restrict__ out,
+                          unsigned char* __restrict__ srgb) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float x = __fmul_rn(in[i], p.coeff);
+        float y;
+        if (p.type == SALTY_TM_ACES) {
+            y = aces_curve(x);
+        } else if (p.type == SALTY_TM_UNCHARTED2) {
+            y = __fdiv_rn(u2_curve(__fmul_rn(2.0f, x)), p.white);
+        } else {
+            // L * (1 + L / maxLw2) / (1 + L)  (src/s3d_tonemapper.cpp:256-268)
+            y = __fdiv_rn(__fmul_rn(x, __fadd_rn(1.0f, __fdiv_rn(x, p.m2))), __fadd_rn(1.0f, x));
+        }
+        if (out) out[i] = y;
+        if (srgb) srgb[i] = to_srgb8(y, p.ref_oetf);
+    }
+}
+
+// ---------------------------------------------------------------- NLM (reference)
+constexpr int kNlmTile = 16;
+constexpr int kNlmHalo = 8;  // 13x13 search (6) + 5x5 patch (2)
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__global__ void __launch_bounds__(kNlmTile* kNlmTile) k_nlm_ref(const float4* __restrict__ src, int w, int h,
+                                                                  float inv_h2, float two_s2, float4* __restrict__ dst) {
+    constexpr int S = kNlmTile + 2 * kNlmHalo;
+    __shared__ float4 tile[S][S];
+    const int x0 = blockIdx.x * kNlmTile - kNlmHalo, y0 = blockIdx.y * kNlmTile - kNlmHalo;
+    for (int i = threadIdx.y * kNlmTile + threadIdx.x; i < S * S; i += kNlmTile * kNlmTile) {
+        const int ty = i / S, tx = i % S;
+        tile[ty][tx] = src[(size_t)clampi(y0 + ty, 0, h - 1) * w + clampi(x0 + tx, 0, w - 1)];
+    }
+    __syncthreads();
+    const int x = blockIdx.x * kNlmTile + threadIdx.x, y = blockIdx.y * kNlmTile + threadIdx.y;
+    if (x >= w || y >= h) return;
+    // tile coordinate of image pixel (ix, iy) after clamping: clamp first, then offset
+    auto T = [&](int ix, int iy) -> const float4& {
+        return tile[clampi(iy, 0, h - 1) - y0][clampi(ix, 0, w - 1) - x0];
+    };
+    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
+    float sw = 0.0f;
+    for (int sx = x - 6; sx <= x + 6; ++sx) {
+        for (int sy = y - 6; sy <= y + 6; ++sy) {
+            float acc = 0.0f;
+            for (int ax = -2; ax <= 2; ++ax) {
+                for (int ay = -2; ay <= 2; ++ay) {
+                    const float4 a = T(x + ax, y + ay), b = T(sx + ax, sy + ay);
+                    const float d0 = __fsub_rn(a.x, b.x), d1 = __fsub_rn(a.y, b.y), d2 = __fsub_rn(a.z, b.z),
+                                d3 = __fsub_rn(a.w, b.w);
+                    const float q = __fadd_rn(__fadd_rn(__fmul_rn(d3, d3), __fmul_rn(d2, d2)),
+                                              __fadd_rn(__fmul_rn(d1, d1), __fmul_rn(d0, d0)));
+                    acc = __fadd_rn(acc, q);
+                }
+            }
+            const float arg = __fmul_rn(-fmaxf(__fsub_rn(acc, two_s2), 0.0f), inv_h2);
+            const float wt = expf(arg);
+            sw = __fadd_rn(sw, wt);
+            const float4 c = T(sx, sy);
+            sum.x = __fadd_rn(sum.x, __fmul_rn(c.x, wt));
+            sum.y = __fadd_rn(sum.y, __fmul_rn(c.y, wt));
+            sum.z = __fadd_rn(sum.z, __fmul_rn(c.z, wt));
+            sum.w = __fadd_rn(sum.w, __fmul_rn(c.w, wt));
+        }
+    }
+    dst[(size_t)y * w + x] = make_float4(__fdiv_rn(sum.x, sw), __fdiv_rn(sum.y, sw), __fdiv_rn(sum.z, sw),
+                                         __fdiv_rn(sum.w, sw));
+}
+
+// ---------------------------------------------------------------- NLM (variance scaled)
+// Rousselle, Knaus, Zwicker, "Adaptive rendering with non-local means filtering"
+// (SIGGRAPH Asia 2012): patch distance normalised by the pixels' variances.
+constexpr int kVTile = 16;
+
+__global__ void __launch_bounds__(kVTile* kVTile) k_nlm_var(const float* __restrict__ rgb, const float* __restrict__ var,
+                                                            int w, int h, int R, int P, float k2, float norm,
+                                                            float* __restrict__ out) {
+    extern __shared__ float sm[];
+    const int H = R + P;
+    const int S = kVTile + 2 * H;
+    float* tc = sm;                 // S*S*3 colours
+    float* tv = sm + S * S * 3;     // S*S*3 variances
+    const int x0 = blockIdx.x * kVTile - H, y0 = blockIdx.y * kVTile - H;
+    for (int i = threadIdx.y * kVTile + threadIdx.x; i < S * S; i += kVTile * kVTile) {
+        const int ty = i / S, tx = i % S;
+        const size_t g = ((size_t)clampi(y0 + ty, 0, h - 1) * w + clampi(x0 + tx, 0, w - 1)) * 3;
+        for (int c = 0; c < 3; ++c) {
+            tc[i * 3 + c] = rgb[g + c];
+            tv[i * 3 + c] = var[g + c];
+        }
+    }
+    __syncthreads();
+    const int x = blockIdx.x * kVTile + threadIdx.x, y = blockIdx.y * kVTile + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const float eps = 1e-10f;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, sw = 0.f;
+    for (int dy = -R; dy <= R; ++dy) {
+        for (int dx = -R; dx <= R; ++dx) {
+            float d2 = 0.0f;
+            for (int py = -P; py <= P; ++py) {
+                for (int px = -P; px <= P; ++px) {
+                    const int ia = ((clampi(y + py, 0, h - 1) - y0) * S + (clampi(x + px, 0, w - 1) - x0)) * 3;
+                    const int ib = ((clampi(y + dy + py, 0, h - 1) - y0) * S + (clampi(x + dx + px, 0, w - 1) - x0)) * 3;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float a = tc[ia + c], b = tc[ib + c], va = tv[ia + c], vb = tv[ib + c];
+                        const float num = (a - b) * (a - b) - (va + fminf(va, vb));
+                        d2 += num / (eps + k2 * (va + vb));
+                    }
+                }
+            }
+            const float wt = expf(-fmaxf(0.0f, d2 * norm));
+            const int iq = ((clampi(y + dy, 0, h - 1) - y0) * S + (clampi(x + dx, 0, w - 1) - x0)) * 3;
+            sw += wt;
+            s0 += wt * tc[iq];
+            s1 += wt * tc[iq + 1];
+            s2 += wt * tc[iq + 2];
+        }
+    }
+    const size_t o = ((size_t)y * w + x) * 3;
+    out[o] = s0 / sw;
+    out[o + 1] = s1 / sw;
+    out[o + 2] = s2 / sw;
+}
+
+}  // namespace
+
+salty_status tonemap_device(salty_ctx* ctx, int type, int w, int h, const float* d_rgb, float* d_out,
+                            uint8_t* d_srgb, int ref_oetf, float* ave, float* mx) {
+    auto& E = ctx->err;
+    cudaStream_t st = ctx->stream;
+    const long long npx = (long long)w * h;
+    LumAcc* acc = reinterpret_cast<LumAcc*>(ctx->counters.p + 32);
+    LumAcc init{0.0, f2o_host(-FLT_MAX), 0};
+    SALTY_TRY_CUDA(E, cudaMemcpyAsync(acc, &init, sizeof init, cudaMemcpyHostToDevice, st));
+    int grid = ctx->num_sms * 4;
+    long long need = (npx + kRedBlock - 1) / kRedBlock;
+    if (grid > need) grid = (int)need;
+    k_lum_reduce<<<grid, kRedBlock, 0, st>>>(d_rgb, npx, acc);
+    LumAcc res;
+    SALTY_TRY_CUDA(E, cudaMemcpyAsync(&res, acc, sizeof res, cudaMemcpyDeviceToHost, st));
+    SALTY_TRY_CUDA(E, cudaStreamSynchronize(st));
+    // ComputeLogarithmicAverage (src/s3d_tonemapper.cpp:84-94)
+    float mean = (float)(res.sum / (double)npx);
+    float ave_lw = expf(mean);
+    int mo = res.maxo;
+    float max_lw;
+    {
+        int i = mo >= 0 ? mo : mo ^ 0x7fffffff;
+        std::memcpy(&max_lw, &i, 4);
+    }
+    if (ave) *ave = ave_lw;
+    if (mx) *mx = max_lw;
+    TmParams p;
+    p.type = type;
+    p.ref_oetf = ref_oetf;
+    p.coeff = (type == SALTY_TM_ACES ? 0.27f : 0.18f) / ave_lw;
+    float m2 = max_lw * p.coeff;
+    p.m2 = m2 * m2;
+    {
+        // Uncharted2Tonemap(LinearWhite = 11.2), host evaluation in the same order
+        const float A = 0.15f, B = 0.50f, C = 0.10f, D = 0.20f, Ee = 0.01f, F = 0.30f, x = 11.2f;
+        float num = x * (A * x + C * B) + D * Ee;
+        float den = x * (A * x + B) + D * F;
+        p.white = num / den - Ee / F;
+    }
+    if (d_out || d_srgb) {
+        const long long n = npx * 3;
+        int g2 = ctx->num_sms * 8;
+        long long need2 = (n + 255) / 256;
+        if (g2 > need2) g2 = (int)need2;
+        k_tonemap<<<g2, 256, 0, st>>>(d_rgb, n, p, d_out, d_srgb);
+    }
+    SALTY_TRY_CUDA(E, cudaGetLastError());
+    return SALTY_OK;
+}
+
+salty_status nlm_ref_device(salty_ctx* ctx, int w, int h, float coeff, const float* d_in, float* d_out) {
+    // FilterNLM parameters (src/s3d_denoiser.cpp:22-25)
+    float ph = fmaxf(0.0001f, coeff), sigma = fmaxf(0.0001f, coeff);
+    float inv_h2 = 1.0f / (ph * ph);
+    float two_s2 = 2.0f * (sigma * sigma);
+    dim3 blk(kNlmTile, kNlmTile), grd((w + kNlmTile - 1) / kNlmTile, (h + kNlmTile - 1) / kNlmTile);
+    k_nlm_ref<<<grd, blk, 0, ctx->stream>>>((const float4*)d_in, w, h, inv_h2, two_s2, (float4*)d_out);
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+salty_status nlm_var_device(salty_ctx* ctx, int w, int h, int search_r, int patch_r, float k, const float* d_rgb,
+                            const float* d_var, float* d_out) {
+    const int H = search_r + patch_r, S = kVTile + 2 * H;
+    size_t smem = (size_t)S * S * 6 * sizeof(float);
+    if (smem > 200 * 1024) return ctx->err.fail(SALTY_ERR_CAPACITY, "NLM window too large");
+    SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(k_nlm_var, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    float norm = 1.0f / (3.0f * (float)((2 * patch_r + 1) * (2 * patch_r + 1)));
+    dim3 blk(kVTile, kVTile), grd((w + kVTile - 1) / kVTile, (h + kVTile - 1) / kVTile);
+    k_nlm_var<<<grd, blk, smem, ctx->stream>>>(d_rgb, d_var, w, h, search_r, patch_r, k * k, norm, d_out);
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+}  // namespace salty

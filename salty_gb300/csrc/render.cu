@@ -1,0 +1,863 @@
+// render.cu -- wavefront path tracer.
+//
+// Replaces PathTracer::TracePath / Radiance / NextEventEstimation (src/s3d_pt.cpp:182-353),
+// which walk one path at a time per OpenMP thread.  Here the camera samples of a frame are
+// processed in waves of up to `capacity` paths; each bounce of a wave is
+//   extend   closest-hit traversal of every live path         (trace.cu kernel)
+//   shade1   next-event estimation: builds the shadow-ray queue
+//   shadow   traversal of the shadow queue                     (trace.cu kernel)
+//   shade2   adds unoccluded light, samples the BSDF, Russian roulette, and compacts the
+//            surviving paths into the next queue (warp ballot + one atomic per warp)
+// and a final accumulate pass adds each sample's radiance to the film (Kahan-compensated
+// FP32, or FP64).  Queue lengths stay in device memory, so one wave is a fixed sequence of
+// launches, captured once as a CUDA graph and replayed for every wave of the frame.
+//
+// Two estimators:
+//   SALTY_PROFILE_COMPAT reproduces the reference's estimator: pixel-centre rays, uniform
+//     hemisphere Lambert sampling weighted by albedo, dice-based termination without
+//     reweighting (src/s3d_lambert.cpp:64-86), Mirror (src/s3d_mirror.cpp:59-71), the
+//     Schlick Glass with its 1/0.5 branch weights (src/s3d_glass.cpp:60-128), NEE through
+//     a closest-hit shadow ray with the reference's MIS weight (src/s3d_pt.cpp:251-292),
+//     and the reference's triangle test with t in [1e-3, 1e12].
+//   SALTY_PROFILE_PHYSICAL is an unbiased estimator for the same scenes: jittered pixels,
+//     cosine-weighted Lambert, exact-Fresnel dielectric, GGX, balance-heuristic MIS
+//     between BSDF sampling and the one-sided area light, a delta sun, constant sky,
+//     Russian roulette from rr_depth, watertight triangle test, ray epsilon 1e-4.
+// Random numbers: one PCG stream (include/s3d_math.h:2769-2817 step) per (pixel, sample).
+#include <cfloat>
+#include <cmath>
+#include <algorithm>
+#include <cstring>
+
+#include "internal.h"
+
+namespace salty {
+namespace {
+
+constexpr float kPi = 3.1415926535897932384626433832795f;
+constexpr float k2Pi = 6.283185307179586476925286766559f;
+constexpr float kFHitMin = 1e-3f, kFHitMax = 1e12f;  // include/s3d_math.h:44-45
+constexpr float kEps = 1e-4f;
+
+// ---------------------------------------------------------------- RNG
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+struct Rng {
+    unsigned long long s;
+    __device__ __forceinline__ unsigned u32() {
+        unsigned long long old = s;
+        s = old * 6364136223846793005ull + 1442695040888963407ull;
+        unsigned xs = (unsigned)(((old >> 18) ^ old) >> 27);
+        unsigned rot = (unsigned)(old >> 59);
+        return (xs >> rot) | (xs << ((~rot + 1u) & 31u));
+    }
+    __device__ __forceinline__ float f32() { return __fdiv_rn((float)u32(), 4294967296.0f); }
+};
+__device__ __forceinline__ Rng rng_for(unsigned long long seed, unsigned long long pixel, unsigned long long sample) {
+    Rng r;
+    r.s = mix64(seed ^ mix64((pixel << 32) | (sample & 0xffffffffull))) + 1442695040888963407ull;
+    (void)r.u32();
+    return r;
+}
+
+// ---------------------------------------------------------------- vectors
+struct V {
+    float x, y, z;
+};
+__device__ __forceinline__ V mk(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ V operator+(V a, V b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V operator-(V a, V b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V operator*(V a, V b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ V operator*(V a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ V operator-(V a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ float dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V cross(V a, V b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float maxc(V a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
+__device__ __forceinline__ V safe_unit(V v) {
+    float m = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    return m > 0.0f ? mk(v.x / m, v.y / m, v.z / m) : v;
+}
+__device__ __forceinline__ V reflect(V i, V n) {
+    float d2 = 2.0f * dot(n, i);
+    return mk(i.x - d2 * n.x, i.y - d2 * n.y, i.z - d2 * n.z);
+}
+// Duff et al. 2017 (include/s3d_math.h:2875-2886)
+__device__ __forceinline__ void tangent_space(V n, V& t, V& b) {
+    float s = n.z >= 0.0f ? 1.0f : -1.0f;
+    float a = -1.0f / (s + n.z);
+    float bb = n.x * n.y * a;
+    t = mk(1.0f + s * n.x * n.x * a, s * bb, -s * n.x);
+    b = mk(bb, s + n.y * n.y * a, -n.y);
+}
+__device__ __forceinline__ V ld3(const float* p) { return mk(p[0], p[1], p[2]); }
+__device__ __forceinline__ V xyz(float4 v) { return mk(v.x, v.y, v.z); }
+
+// ---------------------------------------------------------------- state
+struct PathSoA {
+    float4* W;      // throughput xyz, w = prev bsdf pdf
+    float4* L;      // radiance xyz, w = unused
+    uint4* meta;    // x,y = rng state, z = wave-local sample slot, w = depth | prev_delta<<16
+};
+
+struct Camera {
+    float pos[3], cx[3], cy[3], cz[3];
+};
+
+struct WaveParams {
+    const float* pos;
+    const float* nrm;
+    const int* mat;
+    const GpuMaterial* mats;
+    SceneConsts k;
+    Camera cam;
+    int width, height, spp, max_depth, rr_depth, profile;
+    unsigned long long seed;
+    long long total_samples;   // width*height*spp
+    int capacity;
+};
+
+struct WaveBuffers {
+    float4* rays[2];
+    PathSoA path[2];
+    float4* hits;
+    float4* nee;       // 2 per path: contribution xyz, w = shadow-queue index (int bits, -1 none)
+    float4* srays;     // shadow queue rays (2 per path)
+    float4* shits;
+    float4* lbuf;      // per wave-local sample: radiance xyz
+    int* counts;       // [0] queue A len, [1] queue B len, [2] shadow len, [3] finished
+    long long* wave;   // [0] first global sample of the current wave
+    unsigned long long* stats;  // [0] rays traced, [1] paths
+};
+
+// ---------------------------------------------------------------- kernels
+// Camera rays for samples [g0, g0 + n) of the frame; sample index g -> (sample s =
+// g / (W*H), pixel p = g % (W*H)).  PinholeCamera::GetRay (include/s3d_camera.h:95-100)
+// with separately rounded operations.
+__global__ void k_generate(WaveParams P, WaveBuffers B) {
+    const long long g0 = B.wave[0];
+    const long long remain = P.total_samples - g0;
+    const int n = (int)(remain < P.capacity ? remain : P.capacity);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        B.counts[0] = n;
+        B.counts[1] = 0;
+        B.counts[2] = 0;
+        atomicAdd(&B.stats[1], (unsigned long long)n);
+        atomicAdd(&B.stats[0], (unsigned long long)n);
+    }
+    const long long npx = (long long)P.width * P.height;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const long long g = g0 + i;
+        const long long s = g / npx, p = g % npx;
+        const int px = (int)(p % P.width), py = (int)(p / P.width);
+        Rng rng = rng_for(P.seed, (unsigned long long)p, (unsigned long long)s);
+        float fx, fy;
+        if (P.profile == SALTY_PROFILE_COMPAT) {
+            fx = __fsub_rn(__fdiv_rn(__fadd_rn(0.5f, (float)px), (float)P.width), 0.5f);
+            fy = __fsub_rn(__fdiv_rn(__fadd_rn(0.5f, (float)py), (float)P.height), 0.5f);
+        } else {
+            float jx = rng.f32(), jy = rng.f32();
+            fx = __fsub_rn(__fdiv_rn(__fadd_rn(jx, (float)px), (float)P.width), 0.5f);
+            fy = __fsub_rn(__fdiv_rn(__fadd_rn(jy, (float)py), (float)P.height), 0.5f);
+        }
+        float q[3], d[3];
+        for (int a = 0; a < 3; ++a) {
+            q[a] = __fadd_rn(__fadd_rn(__fmul_rn(P.cam.cx[a], fx), __fmul_rn(P.cam.cy[a], fy)), P.cam.cz[a]);
+            d[a] = __fsub_rn(q[a], P.cam.pos[a]);
+        }
+        const float mag = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
+        const float tmin = P.profile == SALTY_PROFILE_COMPAT ? kFHitMin : kEps;
+        const float tmax = P.profile == SALTY_PROFILE_COMPAT ? kFHitMax : INFINITY;
+        B.rays[0][2 * i] = make_float4(P.cam.pos[0], P.cam.pos[1], P.cam.pos[2], tmin);
+        B.rays[0][2 * i + 1] = make_float4(__fdiv_rn(d[0], mag), __fdiv_rn(d[1], mag), __fdiv_rn(d[2], mag), tmax);
+        B.path[0].W[i] = make_float4(1.f, 1.f, 1.f, 0.f);
+        B.path[0].L[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        B.path[0].meta[i] = make_uint4((unsigned)rng.s, (unsigned)(rng.s >> 32), (unsigned)i, 1u << 16);
+        B.lbuf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+struct Surf {
+    V p, ng, ngf, ns, nsf;
+    bool into;
+};
+
+__device__ __forceinline__ Surf surface(const WaveParams& P, int id, float t, float u, float v, V o, V d) {
+    Surf s;
+    s.p = o + d * t;
+    const float* tp = P.pos + (size_t)id * 9;
+    V v0 = ld3(tp), v1 = ld3(tp + 3), v2 = ld3(tp + 6);
+    s.ng = safe_unit(cross(v1 - v0, v2 - v0));
+    s.into = dot(s.ng, d) < 0.0f;
+    s.ngf = s.into ? s.ng : -s.ng;
+    // Triangle::CalcParam (src/s3d_triangle.cpp:107-121)
+    const float* np = P.nrm + (size_t)id * 9;
+    float al = 1.0f - u - v;
+    V n = mk(np[0] * al + np[3] * u + np[6] * v, np[1] * al + np[4] * u + np[7] * v, np[2] * al + np[5] * u + np[8] * v);
+    s.ns = safe_unit(n);
+    s.nsf = dot(s.ns, d) < 0.0f ? s.ns : -s.ns;
+    return s;
+}
+
+__device__ __forceinline__ bool is_light(const WaveParams& P, int id) {
+    return P.k.light_tri0 >= 0 && id >= P.k.light_tri0 && id < P.k.light_tri0 + 2;
+}
+
+__device__ __forceinline__ float ggx_d(float nh, float a2) {
+    float k = nh * nh * (a2 - 1.0f) + 1.0f;
+    return a2 / (kPi * k * k);
+}
+__device__ __forceinline__ float ggx_g1(float nv, float a2) { return 2.0f * nv / (nv + sqrtf(a2 + (1.0f - a2) * nv * nv)); }
+__device__ __forceinline__ V schlick(V f0, float c) {
+    float m = 1.0f - c, m2 = m * m, m5 = m2 * m2 * m;
+    return mk(f0.x + (1.0f - f0.x) * m5, f0.y + (1.0f - f0.y) * m5, f0.z + (1.0f - f0.z) * m5);
+}
+// f(wo, wi) without the cosine, and the BSDF-sampling pdf (physical profile)
+__device__ __forceinline__ V phys_eval(const GpuMaterial& m, V n, V wo, V wi, float& pdf) {
+    V col = ld3(m.color);
+    float ni = dot(n, wi);
+    if (m.type == SALTY_GGX) {
+        float a = m.roughness * m.roughness, a2 = a * a;
+        float no = dot(n, wo);
+        V h = safe_unit(wo + wi);
+        float nh = dot(n, h), oh = dot(wo, h);
+        if (no <= 0.0f || ni <= 0.0f || nh <= 0.0f || oh <= 0.0f) { pdf = 0.0f; return mk(0, 0, 0); }
+        float D = ggx_d(nh, a2), G = ggx_g1(no, a2) * ggx_g1(ni, a2);
+        pdf = D * nh / (4.0f * oh);
+        return schlick(col, oh) * (D * G / (4.0f * no * ni));
+    }
+    pdf = ni / kPi;
+    return col * (1.0f / kPi);
+}
+
+// warp-aggregated append: returns this lane's slot in a queue of counter `ctr`
+__device__ __forceinline__ int warp_append(bool want, int* ctr) {
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (!m) return -1;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(ctr, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return want ? base + __popc(m & ((1u << lane) - 1u)) : -1;
+}
+
+// NEE for the live paths of queue `q`: appends shadow rays, stores contributions.
+__global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
+    const int n = B.counts[q];
+    const int stride = gridDim.x * blockDim.x;
+    const int lim = (n + 31) & ~31;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < lim; i += stride) {
+        bool live = i < n;
+        float4 h = live ? B.hits[i] : make_float4(0, 0, 0, 0);
+        int id = __float_as_int(h.y);
+        bool want_l = false, want_s = false;
+        float4 ray_l0, ray_l1, ray_s0, ray_s1;
+        V cl = mk(0, 0, 0), cs = mk(0, 0, 0);
+        if (live && id >= 0 && !is_light(P, id)) {
+            const GpuMaterial m = P.mats[P.mat[id]];
+            const bool delta = (m.type == SALTY_MIRROR || m.type == SALTY_GLASS);
+            uint4 mt = B.path[q].meta[i];
+            Rng rng;
+            rng.s = (unsigned long long)mt.x | ((unsigned long long)mt.y << 32);
+            const float4 r0 = B.rays[q][2 * i], r1 = B.rays[q][2 * i + 1];
+            V o = xyz(r0), d = xyz(r1);
+            if (P.profile == SALTY_PROFILE_COMPAT) {
+                if (!delta && P.k.has_light) {
+                    Surf s;
+                    s.p = mk(__fadd_rn(o.x, __fmul_rn(d.x, h.x)), __fadd_rn(o.y, __fmul_rn(d.y, h.x)),
+                             __fadd_rn(o.z, __fmul_rn(d.z, h.x)));
+                    const float* np = P.nrm + (size_t)id * 9;
+                    float al = 1.0f - h.z - h.w;
+                    V n = safe_unit(mk(np[0] * al + np[3] * h.z + np[6] * h.w, np[1] * al + np[4] * h.z + np[7] * h.w,
+                                       np[2] * al + np[5] * h.z + np[8] * h.w));
+                    (void)rng.u32();  // Scene::GetLight (include/s3d_scene.h:84-90), one light
+                    float u = rng.f32(), w = rng.f32();
+                    V lp = ld3(P.k.lc) + ld3(P.k.la) * u + ld3(P.k.lb) * w;
+                    float pdf = 1.0f / P.k.larea;
+                    V ld = lp - s.p;
+                    float dist2 = dot(ld, ld);
+                    ld = safe_unit(ld);
+                    float cos_s = fabsf(dot(n, ld));
+                    float cos_l = fabsf(dot(ld3(P.k.ln), -ld));
+                    V fs = ld3(m.color) * (1.0f / kPi);
+                    float G = cos_s * cos_l / dist2;
+                    float brdf_pdf = fabsf(ld.z / kPi) * cos_l / dist2;
+                    float mis = pdf / (brdf_pdf + pdf);
+                    cl = ld3(P.k.le) * fs * mis * (G / pdf);
+                    want_l = true;
+                    ray_l0 = make_float4(s.p.x, s.p.y, s.p.z, kFHitMin);
+                    ray_l1 = make_float4(ld.x, ld.y, ld.z, kFHitMax);
+                }
+            } else {
+                if (!delta) {
+                    Surf s = surface(P, id, h.x, h.z, h.w, o, d);
+                    V wo = -d;
+                    if (P.k.has_light) {
+                        float u1 = rng.f32(), u2 = rng.f32();
+                        V lp = ld3(P.k.lc) + ld3(P.k.la) * u1 + ld3(P.k.lb) * u2;
+                        V wi = lp - s.p;
+                        float dist2 = dot(wi, wi), dist = sqrtf(dist2);
+                        wi = wi * (1.0f / dist);
+                        float cos_l = dot(ld3(P.k.ln), -wi);
+                        float cos_s = dot(s.nsf, wi), cos_g = dot(s.ngf, wi);
+                        if (cos_l > 0.0f && cos_s > 0.0f && cos_g > 0.0f) {
+                            float pdf_b;
+                            V f = phys_eval(m, s.nsf, wo, wi, pdf_b);
+                            float pdf_l = dist2 / (cos_l * P.k.larea);
+                            float mis = pdf_l / (pdf_l + pdf_b);
+                            cl = f * ld3(P.k.le) * (cos_s * mis / pdf_l);
+                            want_l = true;
+                            ray_l0 = make_float4(s.p.x, s.p.y, s.p.z, kEps);
+                            ray_l1 = make_float4(wi.x, wi.y, wi.z, dist * (1.0f - 1e-4f));
+                        }
+                    }
+                    if (P.k.has_sun) {
+                        V wi = ld3(P.k.sun_dir);
+                        float cos_s = dot(s.nsf, wi), cos_g = dot(s.ngf, wi);
+                        if (cos_s > 0.0f && cos_g > 0.0f) {
+                            float pdf_b;
+                            V f = phys_eval(m, s.nsf, wo, wi, pdf_b);
+                            cs = f * ld3(P.k.sun_rad) * cos_s;
+                            want_s = true;
+                            ray_s0 = make_float4(s.p.x, s.p.y, s.p.z, kEps);
+                            ray_s1 = make_float4(wi.x, wi.y, wi.z, INFINITY);
+                        }
+                    }
+                }
+            }
+            B.path[q].meta[i] = make_uint4((unsigned)rng.s, (unsigned)(rng.s >> 32), mt.z, mt.w);
+        }
+        const int ql = warp_append(want_l, &B.counts[2]);
+        const int qs = warp_append(want_s, &B.counts[2]);
+        if (want_l) {
+            B.srays[2 * ql] = ray_l0;
+            B.srays[2 * ql + 1] = ray_l1;
+        }
+        if (want_s) {
+            B.srays[2 * qs] = ray_s0;
+            B.srays[2 * qs + 1] = ray_s1;
+        }
+        if (live) {
+            B.nee[2 * i] = make_float4(cl.x, cl.y, cl.z, __int_as_float(want_l ? ql : -1));
+            B.nee[2 * i + 1] = make_float4(cs.x, cs.y, cs.z, __int_as_float(want_s ? qs : -1));
+        }
+    }
+}
+
+// BSDF sampling, Russian roulette, compaction of queue q into queue q^1.
+__global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
+    const int n = B.counts[q];
+    const int stride = gridDim.x * blockDim.x;
+    const int lim = (n + 31) & ~31;
+    const bool compat = P.profile == SALTY_PROFILE_COMPAT;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < lim; i += stride) {
+        const bool live = i < n;
+        bool cont = false;
+        float4 nr0, nr1, nW, nL;
+        uint4 nmeta;
+        if (live) {
+            const float4 h = B.hits[i];
+            const int id = __float_as_int(h.y);
+            float4 W4 = B.path[q].W[i], L4 = B.path[q].L[i];
+            uint4 mt = B.path[q].meta[i];
+            V W = xyz(W4), L = xyz(L4);
+            float prev_pdf = W4.w;
+            const bool prev_delta = (mt.w >> 16) & 1u;
+            Rng rng;
+            rng.s = (unsigned long long)mt.x | ((unsigned long long)mt.y << 32);
+            const float4 r0 = B.rays[q][2 * i], r1 = B.rays[q][2 * i + 1];
+            V o = xyz(r0), d = xyz(r1);
+            // unoccluded light
+            const float4 e0 = B.nee[2 * i], e1 = B.nee[2 * i + 1];
+            const int q0 = __float_as_int(e0.w), q1 = __float_as_int(e1.w);
+            if (q0 >= 0) {
+                const int sid = __float_as_int(B.shits[q0].y);
+                bool vis = compat ? (sid >= 0 && is_light(P, sid)) : (sid < 0);
+                if (vis) L = L + W * xyz(e0);
+            }
+            if (q1 >= 0) {
+                const int sid = __float_as_int(B.shits[q1].y);
+                if (sid < 0) L = L + W * xyz(e1);
+            }
+            if (id < 0) {
+                L = L + W * ld3(P.k.sky);
+            } else if (compat) {
+                const GpuMaterial m = P.mats[P.mat[id]];
+                V pos = mk(__fadd_rn(o.x, __fmul_rn(d.x, h.x)), __fadd_rn(o.y, __fmul_rn(d.y, h.x)),
+                           __fadd_rn(o.z, __fmul_rn(d.z, h.x)));
+                L = L + W * ld3(m.emission);
+                const float* np = P.nrm + (size_t)id * 9;
+                float al = 1.0f - h.z - h.w;
+                V normal = safe_unit(mk(np[0] * al + np[3] * h.z + np[6] * h.w, np[1] * al + np[4] * h.z + np[7] * h.w,
+                                        np[2] * al + np[5] * h.z + np[8] * h.w));
+                V nm = dot(normal, d) < 0.0f ? normal : -normal;
+                V col = ld3(m.color), out, wgt;
+                bool dice = false;
+                if (m.type == SALTY_MIRROR) {
+                    out = safe_unit(reflect(d, nm));
+                    wgt = col;
+                } else if (m.type == SALTY_GLASS) {
+                    V refl = safe_unit(reflect(d, nm));
+                    bool into = dot(normal, nm) > 0.0f;
+                    float nc = 1.0f, nt = m.ior;
+                    float nnt = into ? nc / nt : nt / nc;
+                    float ddn = dot(d, nm);
+                    float cos2t = 1.0f - nnt * nnt * (1.0f - ddn * ddn);
+                    if (cos2t < 0.0f) {
+                        out = refl;
+                        wgt = col;
+                    } else {
+                        V refr = safe_unit(d * nnt - normal * (into ? 1.0f : -1.0f) * (ddn * nnt + sqrtf(cos2t)));
+                        float a = nt - nc, b = nt + nc, R0 = a * a / (b * b);
+                        float c = 1.0f - (into ? -ddn : dot(refr, normal));
+                        float c2 = c * c;
+                        float Re = R0 + (1.0f - R0) * (c2 * c2 * c), Tr = 1.0f - Re;
+                        float Pp = 0.25f + 0.5f * Re;
+                        if (rng.f32() < Pp) { out = refl; wgt = col * (Re / (Pp * 0.5f)); }
+                        else { out = refr; wgt = col * (Tr / ((1.0f - Pp) * 0.5f)); }
+                    }
+                } else {
+                    V t, b;
+                    tangent_space(nm, t, b);
+                    float uu = rng.f32(), vv = rng.f32();
+                    float rr = sqrtf(1.0f - uu * uu), ph = k2Pi * vv;
+                    float sp, cp;
+                    sincosf(ph, &sp, &cp);
+                    out = safe_unit(t * (rr * cp) + b * (rr * sp) + nm * uu);
+                    dice = rng.f32() >= m.rr_threshold;
+                    wgt = col;
+                }
+                W = W * wgt;
+                bool stop = dice || (W.x < FLT_EPSILON && W.y < FLT_EPSILON && W.z < FLT_EPSILON) ||
+                            depth + 1 >= P.max_depth;
+                if (!stop) {
+                    cont = true;
+                    nr0 = make_float4(pos.x, pos.y, pos.z, kFHitMin);
+                    nr1 = make_float4(out.x, out.y, out.z, kFHitMax);
+                    nW = make_float4(W.x, W.y, W.z, 0.0f);
+                }
+            } else if (is_light(P, id)) {
+                float cos_l = dot(ld3(P.k.ln), -d);
+                if (cos_l > 0.0f) {
+                    if (prev_delta) L = L + W * ld3(P.k.le);
+                    else {
+                        float pdf_l = h.x * h.x / (cos_l * P.k.larea);
+                        float mis = prev_pdf / (prev_pdf + pdf_l);
+                        L = L + W * ld3(P.k.le) * mis;
+                    }
+                }
+            } else {
+                const GpuMaterial m = P.mats[P.mat[id]];
+                Surf s = surface(P, id, h.x, h.z, h.w, o, d);
+                L = L + W * ld3(m.emission);
+                V col = ld3(m.color), wi, wgt;
+                float pdf = 0.0f;
+                bool is_delta = false, dead = false;
+                if (m.type == SALTY_MIRROR) {
+                    wi = reflect(d, s.nsf);
+                    wgt = col;
+                    is_delta = true;
+                } else if (m.type == SALTY_GLASS) {
+                    float eta = s.into ? 1.0f / m.ior : m.ior;
+                    float cosi = -dot(d, s.nsf);
+                    float sin2t = eta * eta * (1.0f - cosi * cosi);
+                    float F = 1.0f, cost = 0.0f;
+                    if (sin2t < 1.0f) {
+                        cost = sqrtf(1.0f - sin2t);
+                        float rs = (eta * cosi - cost) / (eta * cosi + cost);
+                        float rp = (cosi - eta * cost) / (cosi + eta * cost);
+                        F = 0.5f * (rs * rs + rp * rp);
+                    }
+                    float xi = rng.f32();
+                    if (xi < F) wi = reflect(d, s.nsf);
+                    else wi = safe_unit(d * eta + s.nsf * (eta * cosi - cost));
+                    wgt = col;
+                    is_delta = true;
+                } else if (m.type == SALTY_GGX) {
+                    float a = m.roughness * m.roughness, a2 = a * a;
+                    float r1 = rng.f32(), r2 = rng.f32();
+                    float ph = k2Pi * r1;
+                    float ct = sqrtf((1.0f - r2) / fmaxf(r2 * (a2 - 1.0f) + 1.0f, 1e-8f));
+                    float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+                    V t, b;
+                    tangent_space(s.nsf, t, b);
+                    float sp, cp;
+                    sincosf(ph, &sp, &cp);
+                    V hh = safe_unit(t * (st * cp) + b * (st * sp) + s.nsf * ct);
+                    wi = reflect(d, hh);
+                    V wo = -d;
+                    float no = dot(s.nsf, wo), ni = dot(s.nsf, wi), nh = dot(s.nsf, hh), oh = dot(wo, hh);
+                    if (ni <= 0.0f || no <= 0.0f || oh <= 0.0f || dot(s.ngf, wi) <= 0.0f) {
+                        dead = true;
+                    } else {
+                        float G = ggx_g1(no, a2) * ggx_g1(ni, a2);
+                        wgt = schlick(col, oh) * (G * oh / (no * nh));
+                        pdf = ggx_d(nh, a2) * nh / (4.0f * oh);
+                    }
+                } else {
+                    float r1 = rng.f32(), r2 = rng.f32();
+                    float rr = sqrtf(r1), ph = k2Pi * r2;
+                    float z = sqrtf(fmaxf(0.0f, 1.0f - r1));
+                    V t, b;
+                    tangent_space(s.nsf, t, b);
+                    float sp, cp;
+                    sincosf(ph, &sp, &cp);
+                    wi = safe_unit(t * (rr * cp) + b * (rr * sp) + s.nsf * z);
+                    if (dot(s.ngf, wi) <= 0.0f) dead = true;
+                    wgt = col;
+                    pdf = dot(s.nsf, wi) / kPi;
+                }
+                if (!dead) {
+                    W = W * wgt;
+                    bool stop = (W.x <= 0.0f && W.y <= 0.0f && W.z <= 0.0f);
+                    if (!stop && depth >= P.rr_depth) {
+                        float qv = fminf(0.95f, maxc(W));
+                        if (rng.f32() >= qv) stop = true;
+                        else W = W * (1.0f / qv);
+                    }
+                    if (depth + 1 >= P.max_depth) stop = true;
+                    if (!stop) {
+                        cont = true;
+                        nr0 = make_float4(s.p.x, s.p.y, s.p.z, kEps);
+                        nr1 = make_float4(wi.x, wi.y, wi.z, INFINITY);
+                        nW = make_float4(W.x, W.y, W.z, pdf);
+                        mt.w = (unsigned)(depth + 1) | ((is_delta ? 1u : 0u) << 16);
+                    }
+                }
+            }
+            nL = make_float4(L.x, L.y, L.z, 0.0f);
+            nmeta = make_uint4((unsigned)rng.s, (unsigned)(rng.s >> 32), mt.z, compat ? (unsigned)(depth + 1) : mt.w);
+            if (!cont) B.lbuf[mt.z] = nL;
+        }
+        const int slot = warp_append(cont, &B.counts[q ^ 1]);
+        if (cont) {
+            B.rays[q ^ 1][2 * slot] = nr0;
+            B.rays[q ^ 1][2 * slot + 1] = nr1;
+            B.path[q ^ 1].W[slot] = nW;
+            B.path[q ^ 1].L[slot] = nL;
+            B.path[q ^ 1].meta[slot] = nmeta;
+        }
+    }
+}
+
+__global__ void k_count_rays(WaveBuffers B, int q) {
+    atomicAdd(&B.stats[0], (unsigned long long)(B.counts[q ^ 1] + B.counts[2]));
+}
+
+__global__ void k_reset_queue(WaveBuffers B, int q) {
+    B.counts[q] = 0;
+    B.counts[2] = 0;
+}
+
+// Adds the wave's samples to the film: one thread per pixel, samples in index order.
+__global__ void k_accumulate(WaveParams P, WaveBuffers B, float* __restrict__ sum, float* __restrict__ comp,
+                             float* __restrict__ sumsq, double* __restrict__ sum64, double* __restrict__ sumsq64) {
+    const long long g0 = B.wave[0];
+    const long long npx = (long long)P.width * P.height;
+    const long long remain = P.total_samples - g0;
+    const long long n = remain < P.capacity ? remain : P.capacity;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
+        // samples s with g0 <= s*npx + p < g0 + n
+        long long s_lo = (g0 - p + npx - 1) / npx;
+        if (g0 - p <= 0) s_lo = 0;
+        long long s_hi = (g0 + n - 1 - p) / npx;  // inclusive
+        if (g0 + n - 1 - p < 0) continue;
+        if (s_lo > s_hi) continue;
+        if (sum64) {
+            double a0 = sum64[3 * p], a1 = sum64[3 * p + 1], a2 = sum64[3 * p + 2];
+            double b0 = sumsq64[3 * p], b1 = sumsq64[3 * p + 1], b2 = sumsq64[3 * p + 2];
+            for (long long s = s_lo; s <= s_hi; ++s) {
+                float4 l = B.lbuf[s * npx + p - g0];
+                a0 += l.x; a1 += l.y; a2 += l.z;
+                b0 += (double)l.x * l.x; b1 += (double)l.y * l.y; b2 += (double)l.z * l.z;
+            }
+            sum64[3 * p] = a0; sum64[3 * p + 1] = a1; sum64[3 * p + 2] = a2;
+            sumsq64[3 * p] = b0; sumsq64[3 * p + 1] = b1; sumsq64[3 * p + 2] = b2;
+        } else {
+            float a[3], c[3], q2[3];
+            for (int k = 0; k < 3; ++k) { a[k] = sum[3 * p + k]; c[k] = comp[3 * p + k]; q2[k] = sumsq[3 * p + k]; }
+            for (long long s = s_lo; s <= s_hi; ++s) {
+                float4 l = B.lbuf[s * npx + p - g0];
+                float v[3] = {l.x, l.y, l.z};
+                for (int k = 0; k < 3; ++k) {
+                    // Kahan-compensated sum
+                    float y = __fsub_rn(v[k], c[k]);
+                    float t = __fadd_rn(a[k], y);
+                    c[k] = __fsub_rn(__fsub_rn(t, a[k]), y);
+                    a[k] = t;
+                    q2[k] = __fadd_rn(q2[k], __fmul_rn(v[k], v[k]));
+                }
+            }
+            for (int k = 0; k < 3; ++k) { sum[3 * p + k] = a[k]; comp[3 * p + k] = c[k]; sumsq[3 * p + k] = q2[k]; }
+        }
+    }
+}
+
+__global__ void k_next_wave(WaveParams P, WaveBuffers B) { B.wave[0] += P.capacity; }
+
+__global__ void k_film_out(const float* sum, const float* sumsq, const double* sum64, const double* sumsq64,
+                           long long n, double count, float* mean, float* var) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double s = sum64 ? sum64[i] : (double)sum[i];
+        double q = sum64 ? sumsq64[i] : (double)sumsq[i];
+        double m = count > 0 ? s / count : 0.0;
+        if (mean) mean[i] = (float)m;
+        if (var) {
+            double v = count > 1 ? (q / count - m * m) * count / (count - 1.0) / count : 0.0;
+            var[i] = (float)(v > 0 ? v : 0.0);
+        }
+    }
+}
+
+struct WaveStore {
+    DevBuf<float4> rays[2], W[2], L[2], hits, nee, srays, shits, lbuf;
+    DevBuf<uint4> meta[2];
+    DevBuf<int> counts;
+    DevBuf<long long> wave;
+    DevBuf<unsigned long long> stats, tc0, tc1;
+};
+
+}  // namespace
+
+salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o, salty_render_stats* stats) {
+    auto& E = ctx->err;
+    cudaStream_t st = ctx->stream;
+    Film& F = sc->film;
+    const long long npx = (long long)o.width * o.height;
+    const bool fresh = !o.accumulate || F.width != o.width || F.height != o.height || F.fp64 != o.fp64;
+    if (fresh) {
+        F.width = o.width;
+        F.height = o.height;
+        F.fp64 = o.fp64;
+        F.samples = 0;
+        if (o.fp64) {
+            SALTY_TRY_CUDA(E, F.sum64.ensure(npx * 3));
+            SALTY_TRY_CUDA(E, F.sumsq64.ensure(npx * 3));
+            SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sum64.p, 0, npx * 3 * sizeof(double), st));
+            SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sumsq64.p, 0, npx * 3 * sizeof(double), st));
+        } else {
+            SALTY_TRY_CUDA(E, F.sum.ensure(npx * 3));
+            SALTY_TRY_CUDA(E, F.comp.ensure(npx * 3));
+            SALTY_TRY_CUDA(E, F.sumsq.ensure(npx * 3));
+            SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sum.p, 0, npx * 3 * sizeof(float), st));
+            SALTY_TRY_CUDA(E, cudaMemsetAsync(F.comp.p, 0, npx * 3 * sizeof(float), st));
+            SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sumsq.p, 0, npx * 3 * sizeof(float), st));
+        }
+    }
+    if (o.spp == 0) {
+        if (stats) { stats->samples = F.samples; }
+        return SALTY_OK;
+    }
+    const long long total = npx * o.spp;
+    long long cap = std::min<long long>(total, 1ll << 22);
+    WaveStore S;
+    for (int i = 0; i < 2; ++i) {
+        SALTY_TRY_CUDA(E, S.rays[i].ensure(cap * 2));
+        SALTY_TRY_CUDA(E, S.W[i].ensure(cap));
+        SALTY_TRY_CUDA(E, S.L[i].ensure(cap));
+        SALTY_TRY_CUDA(E, S.meta[i].ensure(cap));
+    }
+    SALTY_TRY_CUDA(E, S.hits.ensure(cap));
+    SALTY_TRY_CUDA(E, S.nee.ensure(cap * 2));
+    SALTY_TRY_CUDA(E, S.srays.ensure(cap * 4));
+    SALTY_TRY_CUDA(E, S.shits.ensure(cap * 2));
+    SALTY_TRY_CUDA(E, S.lbuf.ensure(cap));
+    SALTY_TRY_CUDA(E, S.counts.ensure(8));
+    SALTY_TRY_CUDA(E, S.wave.ensure(1));
+    SALTY_TRY_CUDA(E, S.stats.ensure(4));
+    SALTY_TRY_CUDA(E, S.tc0.ensure(4));
+    SALTY_TRY_CUDA(E, S.tc1.ensure(4));
+    SALTY_TRY_CUDA(E, cudaMemsetAsync(S.counts.p, 0, 8 * sizeof(int), st));
+    SALTY_TRY_CUDA(E, cudaMemsetAsync(S.wave.p, 0, sizeof(long long), st));
+    SALTY_TRY_CUDA(E, cudaMemsetAsync(S.stats.p, 0, 4 * sizeof(unsigned long long), st));
+
+    WaveParams P;
+    P.pos = sc->pos.p;
+    P.nrm = sc->nrm.p;
+    P.mat = sc->mat.p;
+    P.mats = sc->mats.p;
+    P.k = sc->consts;
+    {
+        // PinholeCamera::Update (include/s3d_camera.h:63-90), host floats
+        const SceneConsts& k = sc->consts;
+        float aspect = (float)o.width / (float)o.height;
+        float dir[3] = {k.cam_target[0] - k.cam_pos[0], k.cam_target[1] - k.cam_pos[1], k.cam_target[2] - k.cam_pos[2]};
+        auto unitv = [](float* v) {
+            float m = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            v[0] /= m; v[1] /= m; v[2] /= m;
+        };
+        auto crossv = [](const float* a, const float* b, float* r) {
+            r[0] = a[1] * b[2] - a[2] * b[1];
+            r[1] = a[2] * b[0] - a[0] * b[2];
+            r[2] = a[0] * b[1] - a[1] * b[0];
+        };
+        unitv(dir);
+        float cx[3], cy[3];
+        crossv(dir, k.cam_up, cx);
+        unitv(cx);
+        for (int a = 0; a < 3; ++a) cx[a] = cx[a] * k.cam_fov * aspect;
+        crossv(dir, cx, cy);
+        unitv(cy);
+        for (int a = 0; a < 3; ++a) {
+            cy[a] = cy[a] * k.cam_fov;
+            P.cam.pos[a] = k.cam_pos[a];
+            P.cam.cx[a] = cx[a];
+            P.cam.cy[a] = cy[a];
+            P.cam.cz[a] = k.cam_pos[a] + dir[a] * k.cam_near;
+        }
+    }
+    P.width = o.width;
+    P.height = o.height;
+    P.spp = o.spp;
+    P.max_depth = o.max_depth;
+    P.rr_depth = o.rr_depth;
+    P.profile = o.profile;
+    P.seed = o.seed + 0x9e3779b97f4a7c15ull * (unsigned long long)F.samples;  // new streams per progressive call
+    P.total_samples = total;
+    P.capacity = (int)cap;
+
+    WaveBuffers B;
+    for (int i = 0; i < 2; ++i) {
+        B.rays[i] = S.rays[i].p;
+        B.path[i] = PathSoA{S.W[i].p, S.L[i].p, S.meta[i].p};
+    }
+    B.hits = S.hits.p;
+    B.nee = S.nee.p;
+    B.srays = S.srays.p;
+    B.shits = S.shits.p;
+    B.lbuf = S.lbuf.p;
+    B.counts = S.counts.p;
+    B.wave = S.wave.p;
+    B.stats = S.stats.p;
+
+    const bool compat = o.profile == SALTY_PROFILE_COMPAT;
+    const uint32_t ext_flags = compat ? 0u : (uint32_t)SALTY_TRACE_WATERTIGHT;
+    const uint32_t sh_flags = compat ? 0u : (uint32_t)(SALTY_TRACE_WATERTIGHT | SALTY_TRACE_ANY_HIT);
+    const int sgrid = ctx->num_sms * 8;
+
+    cudaEvent_t e0 = ctx->ev[0], e1 = ctx->ev[1];
+    SALTY_TRY_CUDA(E, cudaEventRecord(e0, st));
+    // one wave as a CUDA graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    SALTY_TRY_CUDA(E, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    salty_status cap_status = SALTY_OK;
+    do {
+        k_generate<<<sgrid, 256, 0, st>>>(P, B);
+        int q = 0;
+        for (int depth = 0; depth < o.max_depth; ++depth) {
+            cap_status = trace_launch(ctx, sc, B.rays[q], cap, &B.counts[q], ext_flags, B.hits, S.tc0.p, st,
+                                      ctx->status.p);
+            if (cap_status != SALTY_OK) break;
+            k_shade1<<<sgrid, 256, 0, st>>>(P, B, q);
+            cap_status = trace_launch(ctx, sc, B.srays, 2 * cap, &B.counts[2], sh_flags, B.shits, S.tc1.p, st,
+                                      ctx->status.p);
+            if (cap_status != SALTY_OK) break;
+            k_shade2<<<sgrid, 256, 0, st>>>(P, B, q, depth);
+            k_count_rays<<<1, 1, 0, st>>>(B, q);
+            k_reset_queue<<<1, 1, 0, st>>>(B, q);
+            q ^= 1;
+        }
+        if (cap_status != SALTY_OK) break;
+        k_accumulate<<<sgrid, 256, 0, st>>>(P, B, o.fp64 ? nullptr : F.sum.p, o.fp64 ? nullptr : F.comp.p,
+                                            o.fp64 ? nullptr : F.sumsq.p, o.fp64 ? F.sum64.p : nullptr,
+                                            o.fp64 ? F.sumsq64.p : nullptr);
+        k_next_wave<<<1, 1, 0, st>>>(P, B);
+    } while (0);
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (cap_status != SALTY_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return cap_status;
+    }
+    SALTY_TRY_CUDA(E, ce);
+    SALTY_TRY_CUDA(E, cudaGraphInstantiate(&exec, graph, 0));
+    const long long waves = (total + cap - 1) / cap;
+    salty_status rs = SALTY_OK;
+    for (long long w = 0; w < waves; ++w) {
+        if (ctx->cancel) { rs = E.fail(SALTY_ERR_CANCELLED, "render cancelled"); break; }
+        cudaError_t le = cudaGraphLaunch(exec, st);
+        if (le != cudaSuccess) { rs = E.fail(SALTY_ERR_CUDA, "graph launch: %s", cudaGetErrorString(le)); break; }
+        if ((w & 7) == 7) cudaStreamSynchronize(st);
+    }
+    SALTY_TRY_CUDA(E, cudaEventRecord(e1, st));
+    cudaError_t se = cudaEventSynchronize(e1);
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    SALTY_TRY_CUDA(E, se);
+    SALTY_TRY_CUDA(E, cudaGetLastError());
+    if (rs != SALTY_OK) return rs;
+    int status = 0;
+    SALTY_TRY_CUDA(E, cudaMemcpy(&status, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (status) return E.fail(SALTY_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
+    unsigned long long hs[2];
+    SALTY_TRY_CUDA(E, cudaMemcpy(hs, S.stats.p, sizeof hs, cudaMemcpyDeviceToHost));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    F.samples += o.spp;
+    if (stats) {
+        stats->ms = ms;
+        stats->samples = F.samples;
+        stats->rays = (int64_t)hs[0];
+        stats->paths = (int64_t)hs[1];
+    }
+    return SALTY_OK;
+}
+
+salty_status film_outputs(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o, float* d_mean, float* d_var,
+                          uint8_t* d_srgb) {
+    auto& E = ctx->err;
+    Film& F = sc->film;
+    const long long n = (long long)F.width * F.height * 3;
+    DevBuf<float> tmp;
+    float* mean = d_mean;
+    if (!mean && d_srgb) {
+        SALTY_TRY_CUDA(E, tmp.ensure(n));
+        mean = tmp.p;
+    }
+    k_film_out<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(F.fp64 ? nullptr : F.sum.p, F.fp64 ? nullptr : F.sumsq.p,
+                                                         F.fp64 ? F.sum64.p : nullptr, F.fp64 ? F.sumsq64.p : nullptr,
+                                                         n, (double)F.samples, mean, d_var);
+    SALTY_TRY_CUDA(E, cudaGetLastError());
+    if (d_srgb) {
+        int tm = o.tonemap < 0 ? SALTY_TM_REINHARD : o.tonemap;
+        SALTY_TRY(tonemap_device(ctx, tm, F.width, F.height, mean, nullptr, d_srgb, o.ref_oetf, nullptr, nullptr));
+    }
+    return SALTY_OK;
+}
+
+}  // namespace salty
+
+extern "C" salty_status salty_film_read(salty_ctx* ctx, salty_scene* sc, double* sum, double* sumsq,
+                                        int64_t* samples) {
+    using namespace salty;
+    if (!ctx) return SALTY_ERR_INVALID_ARG;
+    if (!sc) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "null scene");
+    Film& F = sc->film;
+    if (samples) *samples = F.samples;
+    const long long n = (long long)F.width * F.height * 3;
+    if (n == 0) return SALTY_OK;
+    cudaSetDevice(ctx->device);
+    auto fetch = [&](double* dst, const double* s64, const float* s32) -> salty_status {
+        if (!dst) return SALTY_OK;
+        DevBuf<double> tmp;
+        const double* src = s64;
+        if (!s64) {
+            SALTY_TRY_CUDA(ctx->err, tmp.ensure(n));
+            // widen on the host side of the copy: copy floats then convert
+            std::vector<float> h(n);
+            SALTY_TRY_CUDA(ctx->err, cudaMemcpy(h.data(), s32, n * sizeof(float), cudaMemcpyDeviceToHost));
+            std::vector<double> hd(h.begin(), h.end());
+            SALTY_TRY_CUDA(ctx->err, cudaMemcpy(dst, hd.data(), n * sizeof(double), cudaMemcpyDefault));
+            return SALTY_OK;
+        }
+        SALTY_TRY_CUDA(ctx->err, cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyDefault));
+        return SALTY_OK;
+    };
+    SALTY_TRY(fetch(sum, F.fp64 ? F.sum64.p : nullptr, F.sum.p));
+    SALTY_TRY(fetch(sumsq, F.fp64 ? F.sumsq64.p : nullptr, F.sumsq.p));
+    return SALTY_OK;
+}

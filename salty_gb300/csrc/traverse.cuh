@@ -1,0 +1,265 @@
+// traverse.cuh -- device-side closest/any-hit traversal of the quantised BVH8.
+//
+// Replaces the recursive virtual walk BVH8::IsHit -> BoundingBox8::IsHit ->
+// Leaf::IsHit -> Triangle::IsHit (src/s3d_bvh8.cpp:191-206, include/s3d_math.h:
+// 2549-2586, src/s3d_leaf.cpp:74-87, src/s3d_triangle.cpp:73-105).  One thread per ray;
+// a node is five 16-byte loads; child boxes are tested against [tmin, best t] (the
+// reference tests the whole line) and visited nearest-octant first; the stack of
+// pending child groups lives in shared memory.  The loop follows the compressed wide
+// BVH traversal published by Ylitie, Karras and Laine (HPG 2017).
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+#include "internal.h"
+
+namespace salty {
+
+// Group stack entry: x = child base index, y = (hit bits in key order << 8) | imask.
+template <int DEPTH>
+struct TravStack {
+    uint2* base;    // shared memory, [DEPTH][blockDim]
+    int stride;     // blockDim.x
+    __device__ __forceinline__ uint2& at(int i) const { return base[i * stride]; }
+};
+
+struct TravRay {
+    float ox, oy, oz, dx, dy, dz;
+    float ix, iy, iz;        // 1/d with zero components replaced by tiny values
+    float tmin, tmax;
+    unsigned oct;            // bit a set when d[a] < 0
+    // watertight shear constants
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+
+struct TravHit {
+    float t, u, v;
+    int id;
+};
+
+struct TravCount {
+    unsigned nodes, tris;
+};
+
+__device__ __forceinline__ float safe_rcp(float d) {
+    float ad = fabsf(d);
+    if (ad < 1e-30f) d = copysignf(1e-30f, d);
+    return __frcp_rn(d);
+}
+
+__device__ __forceinline__ void make_trav_ray(TravRay& r, float ox, float oy, float oz, float tmin, float dx,
+                                              float dy, float dz, float tmax) {
+    r.ox = ox; r.oy = oy; r.oz = oz; r.dx = dx; r.dy = dy; r.dz = dz;
+    r.tmin = tmin; r.tmax = tmax;
+    r.ix = safe_rcp(dx); r.iy = safe_rcp(dy); r.iz = safe_rcp(dz);
+    r.oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
+    float ad[3] = {fabsf(dx), fabsf(dy), fabsf(dz)};
+    int kz = 0;
+    if (ad[1] > ad[kz]) kz = 1;
+    if (ad[2] > ad[kz]) kz = 2;
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    float d[3] = {dx, dy, dz};
+    if (d[kz] < 0.0f) { int t = kx; kx = ky; ky = t; }
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.Sx = __fdiv_rn(d[kx], d[kz]);
+    r.Sy = __fdiv_rn(d[ky], d[kz]);
+    r.Sz = __fdiv_rn(1.0f, d[kz]);
+}
+
+// ---------------------------------------------------------------- triangle tests
+// The reference's test (src/s3d_triangle.cpp:73-105), operation for operation, with
+// every product and sum rounded separately (no fused multiply-add) and IEEE division,
+// so t, beta and gamma equal the reference's bit for bit.  Sign checks on the
+// numerators reject before the divisions where the quotient's sign alone decides.
+__device__ __forceinline__ bool tri_ref(const TravRay& r, float4 a, float4 b, float4 c, float tmin, float tmax,
+                                        float& t, float& u, float& v) {
+    const float e1x = __fsub_rn(b.x, a.x), e1y = __fsub_rn(b.y, a.y), e1z = __fsub_rn(b.z, a.z);
+    const float e2x = __fsub_rn(c.x, a.x), e2y = __fsub_rn(c.y, a.y), e2z = __fsub_rn(c.z, a.z);
+    // s1 = d x e2
+    const float s1x = __fsub_rn(__fmul_rn(r.dy, e2z), __fmul_rn(r.dz, e2y));
+    const float s1y = __fsub_rn(__fmul_rn(r.dz, e2x), __fmul_rn(r.dx, e2z));
+    const float s1z = __fsub_rn(__fmul_rn(r.dx, e2y), __fmul_rn(r.dy, e2x));
+    const float div = __fadd_rn(__fadd_rn(__fmul_rn(s1x, e1x), __fmul_rn(s1y, e1y)), __fmul_rn(s1z, e1z));
+    if (fabsf(div) <= FLT_EPSILON) return false;
+    const float dvx = __fsub_rn(r.ox, a.x), dvy = __fsub_rn(r.oy, a.y), dvz = __fsub_rn(r.oz, a.z);
+    const float nb = __fadd_rn(__fadd_rn(__fmul_rn(dvx, s1x), __fmul_rn(dvy, s1y)), __fmul_rn(dvz, s1z));
+    if (nb == 0.0f || (__float_as_uint(nb) ^ __float_as_uint(div)) >> 31) return false;  // beta <= 0
+    const float beta = __fdiv_rn(nb, div);
+    if (beta <= 0.0f || beta >= 1.0f) return false;
+    // s2 = dv x e1
+    const float s2x = __fsub_rn(__fmul_rn(dvy, e1z), __fmul_rn(dvz, e1y));
+    const float s2y = __fsub_rn(__fmul_rn(dvz, e1x), __fmul_rn(dvx, e1z));
+    const float s2z = __fsub_rn(__fmul_rn(dvx, e1y), __fmul_rn(dvy, e1x));
+    const float ng = __fadd_rn(__fadd_rn(__fmul_rn(r.dx, s2x), __fmul_rn(r.dy, s2y)), __fmul_rn(r.dz, s2z));
+    if (ng == 0.0f || (__float_as_uint(ng) ^ __float_as_uint(div)) >> 31) return false;  // gamma <= 0
+    const float gamma = __fdiv_rn(ng, div);
+    if (gamma <= 0.0f || __fadd_rn(beta, gamma) >= 1.0f) return false;
+    const float nt = __fadd_rn(__fadd_rn(__fmul_rn(e2x, s2x), __fmul_rn(e2y, s2y)), __fmul_rn(e2z, s2z));
+    const float dist = __fdiv_rn(nt, div);
+    if (!(dist >= tmin) || dist > tmax) return false;
+    t = dist; u = beta; v = gamma;
+    return true;
+}
+
+// Watertight test (Woop, Benthin, Wald, JCGT 2013) without fused operations, so an edge
+// shared by two triangles gets the same edge function with opposite sign in both.
+__device__ __forceinline__ bool tri_watertight(const TravRay& r, float4 a, float4 b, float4 c, float tmin,
+                                               float tmax, float& t, float& u, float& v) {
+    const float o[3] = {r.ox, r.oy, r.oz};
+    const float A[3] = {__fsub_rn(a.x, o[0]), __fsub_rn(a.y, o[1]), __fsub_rn(a.z, o[2])};
+    const float B[3] = {__fsub_rn(b.x, o[0]), __fsub_rn(b.y, o[1]), __fsub_rn(b.z, o[2])};
+    const float C[3] = {__fsub_rn(c.x, o[0]), __fsub_rn(c.y, o[1]), __fsub_rn(c.z, o[2])};
+    const float Ax = __fsub_rn(A[r.kx], __fmul_rn(r.Sx, A[r.kz])), Ay = __fsub_rn(A[r.ky], __fmul_rn(r.Sy, A[r.kz]));
+    const float Bx = __fsub_rn(B[r.kx], __fmul_rn(r.Sx, B[r.kz])), By = __fsub_rn(B[r.ky], __fmul_rn(r.Sy, B[r.kz]));
+    const float Cx = __fsub_rn(C[r.kx], __fmul_rn(r.Sx, C[r.kz])), Cy = __fsub_rn(C[r.ky], __fmul_rn(r.Sy, C[r.kz]));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx));
+        V = (float)__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx));
+        W = (float)__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    const float Az = __fmul_rn(r.Sz, A[r.kz]), Bz = __fmul_rn(r.Sz, B[r.kz]), Cz = __fmul_rn(r.Sz, C[r.kz]);
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    if (det > 0.0f) {
+        if (T < __fmul_rn(tmin, det) || T > __fmul_rn(tmax, det)) return false;
+    } else {
+        if (T > __fmul_rn(tmin, det) || T < __fmul_rn(tmax, det)) return false;
+    }
+    const float rcp = __frcp_rn(det);
+    t = __fmul_rn(T, rcp);
+    u = __fmul_rn(V, rcp);
+    v = __fmul_rn(W, rcp);
+    if (!(t >= tmin) || t > tmax) return false;
+    return true;
+}
+
+__device__ __forceinline__ float u8f(unsigned w, int k) { return (float)((w >> (8 * k)) & 0xffu); }
+
+// Relative widening of box intervals: covers the rounding of the decoded planes,
+// of 1/d and of the fused plane evaluation, so the quantised-box test never rejects a
+// box the exact ray segment meets.
+constexpr float kBoxSlack = 1.0f / (1 << 20);
+
+// Intersects the 8 children of node `idx`.  Returns inner-child hits in key order
+// (bit slot^oct) and triangle hits relative to tri_base.
+__device__ __forceinline__ void intersect_node(const Bvh8Node* __restrict__ nodes, unsigned idx, const TravRay& r,
+                                               float tcull, unsigned& child_base, unsigned& imask,
+                                               unsigned& inner_hits, unsigned& tri_base, unsigned& tri_hits) {
+    const uint4* np = reinterpret_cast<const uint4*>(nodes + idx);
+    const uint4 w0 = __ldg(np + 0), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+    const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+    const float sx = __uint_as_float((w0.w & 0xffu) << 23);
+    const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
+    const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+    imask = w0.w >> 24;
+    child_base = w1.x;
+    tri_base = w1.y;
+    const float ax = sx * r.ix, ay = sy * r.iy, az = sz * r.iz;
+    const float bx = (px - r.ox) * r.ix, by = (py - r.oy) * r.iy, bz = (pz - r.oz) * r.iz;
+    // near/far plane words by ray octant
+    const unsigned nlx0 = (r.oct & 1) ? w3.z : w2.x, nlx1 = (r.oct & 1) ? w3.w : w2.y;
+    const unsigned nhx0 = (r.oct & 1) ? w2.x : w3.z, nhx1 = (r.oct & 1) ? w2.y : w3.w;
+    const unsigned nly0 = (r.oct & 2) ? w4.x : w2.z, nly1 = (r.oct & 2) ? w4.y : w2.w;
+    const unsigned nhy0 = (r.oct & 2) ? w2.z : w4.x, nhy1 = (r.oct & 2) ? w2.w : w4.y;
+    const unsigned nlz0 = (r.oct & 4) ? w4.z : w3.x, nlz1 = (r.oct & 4) ? w4.w : w3.y;
+    const unsigned nhz0 = (r.oct & 4) ? w3.x : w4.z, nhz1 = (r.oct & 4) ? w3.y : w4.w;
+    inner_hits = 0;
+    tri_hits = 0;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const unsigned lx = half ? nlx1 : nlx0, hx = half ? nhx1 : nhx0;
+        const unsigned ly = half ? nly1 : nly0, hy = half ? nhy1 : nhy0;
+        const unsigned lz = half ? nlz1 : nlz0, hz = half ? nhz1 : nhz0;
+        const unsigned meta = half ? w1.w : w1.z;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float tnx = fmaf(u8f(lx, k), ax, bx), tfx = fmaf(u8f(hx, k), ax, bx);
+            const float tny = fmaf(u8f(ly, k), ay, by), tfy = fmaf(u8f(hy, k), ay, by);
+            const float tnz = fmaf(u8f(lz, k), az, bz), tfz = fmaf(u8f(hz, k), az, bz);
+            float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+            float tf = fminf(fminf(tfx, tfy), fminf(tfz, tcull));
+            tn = fmaf(-kBoxSlack, fabsf(tn), tn);
+            tf = fmaf(kBoxSlack, fabsf(tf), tf);
+            if (tn <= tf) {
+                const int slot = half * 4 + k;
+                if (imask & (1u << slot)) {
+                    inner_hits |= 1u << (slot ^ r.oct);
+                } else {
+                    const unsigned m = (meta >> (8 * k)) & 0xffu;
+                    const unsigned cnt = m >> 5, off = m & 31u;
+                    tri_hits |= ((1u << cnt) - 1u) << off;
+                }
+            }
+        }
+    }
+}
+
+// Closest hit (ANY = false) or any hit.  CULL_SLACK: a box is kept while its entry is
+// within best_t * (1 + slack) -- a relative margin over the triangle test's rounding, so
+// the closest hit never depends on which nodes were culled.
+template <bool ANY, bool WATERTIGHT, bool COUNT, int DEPTH>
+__device__ __forceinline__ bool traverse(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris,
+                                         const TravRay& r, float cull_slack, TravStack<DEPTH> stack,
+                                         TravHit& hit, TravCount& cnt, int& overflow) {
+    hit.t = INFINITY;
+    hit.id = -1;
+    hit.u = hit.v = 0.0f;
+    float tcull = r.tmax;
+    unsigned ng_base = 0, ng_hits = 1u << r.oct, ng_imask = 1u;  // group holding the root
+    unsigned tg_base = 0, tg_hits = 0;
+    int sp = 0;
+    for (;;) {
+        if (ng_hits) {
+            const unsigned key = __ffs(ng_hits) - 1;
+            ng_hits &= ng_hits - 1;
+            const unsigned slot = key ^ r.oct;
+            const unsigned idx = ng_base + __popc(ng_imask & ((1u << slot) - 1u));
+            if (ng_hits) {
+                if (sp >= DEPTH) { overflow = 1; return hit.id >= 0; }
+                stack.at(sp++) = make_uint2(ng_base, (ng_hits << 8) | ng_imask);
+            }
+            unsigned cb, im, ih, tb, th;
+            intersect_node(nodes, idx, r, tcull, cb, im, ih, tb, th);
+            if (COUNT) ++cnt.nodes;
+            ng_base = cb; ng_imask = im; ng_hits = ih;
+            tg_base = tb; tg_hits = th;
+        }
+        while (tg_hits) {
+            const unsigned k = __ffs(tg_hits) - 1;
+            tg_hits &= tg_hits - 1;
+            const float4* tp = tris + (size_t)(tg_base + k) * kTriFloat4;
+            const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            if (COUNT) ++cnt.tris;
+            float t, u, v;
+            const float tlim = ANY ? r.tmax : hit.t;
+            bool h = WATERTIGHT ? tri_watertight(r, a, b, c, r.tmin, fminf(r.tmax, tlim), t, u, v)
+                                : tri_ref(r, a, b, c, r.tmin, r.tmax, t, u, v);
+            if (h) {
+                const int id = __float_as_int(a.w);
+                if (t < hit.t || (t == hit.t && id < hit.id)) {
+                    hit.t = t; hit.u = u; hit.v = v; hit.id = id;
+                    if (ANY) return true;
+                    tcull = fminf(r.tmax, fmaf(cull_slack, t, t));
+                }
+            }
+        }
+        if (!ng_hits) {
+            if (sp == 0) break;
+            const uint2 e = stack.at(--sp);
+            ng_base = e.x;
+            ng_hits = e.y >> 8;
+            ng_imask = e.y & 0xffu;
+        }
+    }
+    return hit.id >= 0;
+}
+
+}  // namespace salty

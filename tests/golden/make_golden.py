@@ -1,0 +1,150 @@
+"""Generates the committed golden fixtures from the UNMODIFIED reference.
+
+Run in a checkout where the reference sources exist (oracle/Makefile builds
+oracle/_ref/libsalty_ref.so from them):
+
+    python tests/golden/make_golden.py
+
+The reference has no tests, golden vectors or known-answer files of its own, so these
+fixtures are its outputs on seeded inputs, produced through the harness in
+oracle/ref/sref_harness.cpp.  Inputs are regenerated from their seeds by the tests
+(sha256 digests below detect any drift of the generators between hosts).
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import struct
+import sys
+import tempfile
+import zlib
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.oracle import Oracle, Reference, SceneData, build  # noqa: E402
+
+SOUP_SEED, RAY_SEED = 20260001, 20260002
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def decode_png(path: str) -> np.ndarray:
+    """Minimal PNG reader for 8-bit RGB, non-interlaced (what stb_image_write emits)."""
+    data = open(path, "rb").read()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, idat, w, h = 8, b"", 0, 0
+    while pos < len(data):
+        ln, = struct.unpack(">I", data[pos:pos + 4])
+        typ = data[pos + 4:pos + 8]
+        body = data[pos + 8:pos + 8 + ln]
+        if typ == b"IHDR":
+            w, h, depth, ctype = struct.unpack(">IIBB", body[:10])
+            assert depth == 8 and ctype == 2
+        elif typ == b"IDAT":
+            idat += body
+        pos += 12 + ln
+    raw = zlib.decompress(idat)
+    stride = w * 3
+    out = np.zeros((h, stride), np.uint8)
+    prev = np.zeros(stride, np.int32)
+    for y in range(h):
+        f = raw[y * (stride + 1)]
+        line = np.frombuffer(raw[y * (stride + 1) + 1:(y + 1) * (stride + 1)], np.uint8).astype(np.int32)
+        cur = np.zeros(stride, np.int32)
+        for x in range(stride):
+            a = cur[x - 3] if x >= 3 else 0
+            b = prev[x]
+            c = prev[x - 3] if x >= 3 else 0
+            if f == 0:
+                p = 0
+            elif f == 1:
+                p = a
+            elif f == 2:
+                p = b
+            elif f == 3:
+                p = (a + b) // 2
+            else:
+                pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
+                p = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+            cur[x] = (line[x] + p) & 0xFF
+        out[y] = cur
+        prev = cur
+    return out.reshape(h, w, 3)
+
+
+def cornell_scene() -> SceneData:
+    from salty_gb300 import scenes  # noqa: E402  (numpy-only module)
+    sc = scenes.cornell("baseline")
+    return SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], None,
+                     sc["sky"], sc["camera"])
+
+
+def hdr_image(seed: int, w: int, h: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    img = np.exp(rng.normal(-1.0, 1.5, size=(h, w, 3))).astype(np.float32)
+    img[0, 0] = 0.0            # exercises the epsilon floor of the log-average
+    img[1, 1] = (40.0, 35.0, 30.0)
+    return img
+
+
+def main() -> None:
+    build(with_reference=True)
+    o, r = Oracle(), Reference()
+
+    # 1. traversal: 1M-triangle soup, first 65536 rays of the microbenchmark stream
+    tris = o.gen_soup(SOUP_SEED, 1_000_000)
+    rays = o.gen_rays(RAY_SEED, 65536)
+    s = r.soup(tris)
+    ids, t, u, v, _ = s.trace(rays)
+    s.close()
+    np.savez_compressed(os.path.join(HERE, "trace_soup_1m.npz"), ids=ids, t=t,
+                        soup_sha=sha(tris), rays_sha=sha(rays), n_tris=1_000_000, n_rays=65536,
+                        soup_seed=SOUP_SEED, ray_seed=RAY_SEED)
+
+    # 2. traversal, small soup, with barycentrics
+    tris_s = o.gen_soup(7, 30000)
+    rays_s = o.gen_rays(8, 8192)
+    s = r.soup(tris_s)
+    ids, t, u, v, _ = s.trace(rays_s)
+    s.close()
+    np.savez_compressed(os.path.join(HERE, "trace_soup_30k.npz"), ids=ids, t=t, u=u, v=v,
+                        soup_sha=sha(tris_s), rays_sha=sha(rays_s), soup_seed=7, ray_seed=8,
+                        n_tris=30000, n_rays=8192)
+
+    # 3. Cornell box through PathTracer::Radiance (reference estimator)
+    sc = cornell_scene()
+    W = H = 64
+    spp, depth = 1024, 8
+    total, sq, secs = r.render(sc, W, H, spp, depth, seed=12345)
+    mean = total / spp
+    var = (sq / spp - mean * mean) * spp / (spp - 1) / spp
+    np.savez_compressed(os.path.join(HERE, "cornell_ref_64.npz"), mean=mean.astype(np.float32),
+                        var=np.maximum(var, 0).astype(np.float32), spp=spp, max_bounce=depth, width=W, height=H)
+    print(f"cornell reference render: {secs:.2f} s")
+
+    # 4. tonemapping and the sRGB8 capture
+    img = hdr_image(99, 48, 32)
+    out = {f"tm{k}": r.tonemap(k, img) for k in (0, 1, 2)}
+    with tempfile.TemporaryDirectory() as td:
+        p = os.path.join(td, "cap.png")
+        r.capture_png(img, p)
+        png = decode_png(p)
+    np.savez_compressed(os.path.join(HERE, "tonemap_ref.npz"), img=img, srgb_aces_ref=png, **out)
+
+    # 5. NLM
+    rng = np.random.default_rng(5)
+    rgba = rng.random((20, 24, 4), dtype=np.float32)
+    rgba[..., 3] = 1.0
+    nl = r.nlm(rgba, 0.2)
+    np.savez_compressed(os.path.join(HERE, "nlm_ref.npz"), rgba=rgba, coeff=0.2, out=nl)
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,69 @@
+"""The C ABI library: it loads without a GPU and exports every symbol the header declares."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "salty_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(salty_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_python_binding_set(salty_lib):
+    import salty_gb300
+    assert header_symbols() == sorted(salty_gb300.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(salty_lib):
+    import salty_gb300
+    out = subprocess.run(["nm", "-D", "--defined-only", salty_gb300.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (salty_[a-z0-9_]+)", out))
+    missing = [s for s in header_symbols() if s not in exported]
+    assert not missing, missing
+    for s in header_symbols():
+        assert hasattr(salty_lib, s)
+
+
+def test_abi_version(salty_lib):
+    assert salty_lib.salty_abi_version() == 1
+
+
+def test_context_without_gpu_fails_cleanly(salty_lib):
+    import torch
+    import salty_gb300
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(salty_gb300.SaltyError) as e:
+        salty_gb300.Context(0)
+    assert e.value.status == salty_gb300.ERR_CUDA
+
+
+def test_generators_validate_arguments(salty_lib):
+    import ctypes as C
+    assert salty_lib.salty_microbench_soup(1, -1, None) == 1
+    assert salty_lib.salty_microbench_rays(1, 5, C.c_float(1e-4), None) == 1
+    assert salty_lib.salty_microbench_soup(1, 0, None) == 0
+
+
+def test_null_context_is_rejected(salty_lib):
+    assert salty_lib.salty_bvh_build(None, None, None, None) == 1
+    assert salty_lib.salty_trace(None, None, None, 0, 0, None) == 1
+    assert salty_lib.salty_render(None, None, None, None, None, None, None) == 1
+    assert salty_lib.salty_last_error(None) == b"null context"
+
+
+def test_microbench_rays_are_unit_and_aimed_at_the_cube(salty_lib):
+    import salty_gb300
+    r = salty_gb300.microbench_rays(3, 10000, 1e-4)
+    o, d = r[:, 0:3], r[:, 4:7]
+    np.testing.assert_allclose(np.linalg.norm(o - 0.5, axis=1), 2.0, rtol=1e-6)
+    np.testing.assert_allclose(np.linalg.norm(d, axis=1), 1.0, rtol=1e-6)
+    assert np.all(r[:, 3] == np.float32(1e-4)) and np.all(np.isinf(r[:, 7]))
+    # origin on the sphere is uniform: mean near the centre
+    assert np.all(np.abs(o.mean(axis=0) - 0.5) < 0.05)

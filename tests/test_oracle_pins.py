@@ -1,0 +1,142 @@
+"""Pins the oracle restatement (oracle/salty_oracle.c) to the reference.
+
+CPU only.  The reference ships no tests or golden vectors, so the pins are (a) the
+committed fixtures in tests/golden/, made from the unmodified reference by
+tests/golden/make_golden.py, and (b) live comparisons against the reference compiled
+from its sources (oracle/_ref), where that build exists.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+SOUP_SEED, RAY_SEED = 20260001, 20260002
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def zscores(mean_a, var_a, mean_b, var_b):
+    return (mean_a - mean_b) / np.sqrt(np.maximum(var_a + var_b, 1e-30))
+
+
+def test_generators_reproduce_fixture_inputs(oracle):
+    g = np.load(os.path.join(GOLDEN, "trace_soup_1m.npz"))
+    assert sha(oracle.gen_soup(SOUP_SEED, 1_000_000)) == str(g["soup_sha"])
+    assert sha(oracle.gen_rays(RAY_SEED, 65536)) == str(g["rays_sha"])
+
+
+def test_library_generators_equal_oracle(oracle):
+    import salty_gb300
+    from salty_gb300 import build as b
+    b.build()
+    for n in (0, 1, 1000, 12345):
+        assert np.array_equal(salty_gb300.microbench_soup(11, n), oracle.gen_soup(11, n))
+        assert np.array_equal(salty_gb300.microbench_rays(12, n, 1e-4), oracle.gen_rays(12, n, 1e-4))
+
+
+def test_oracle_trace_matches_reference_fixture_small(oracle):
+    g = np.load(os.path.join(GOLDEN, "trace_soup_30k.npz"))
+    tris = oracle.gen_soup(int(g["soup_seed"]), int(g["n_tris"]))
+    rays = oracle.gen_rays(int(g["ray_seed"]), int(g["n_rays"]))
+    assert sha(tris) == str(g["soup_sha"]) and sha(rays) == str(g["rays_sha"])
+    ids, t, u, v = oracle.trace(tris, rays, mode=0)
+    assert np.array_equal(ids, g["ids"])
+    hit = ids >= 0
+    assert hit.sum() > 50
+    assert np.array_equal(t[hit], g["t"][hit])
+    assert np.array_equal(u[hit], g["u"][hit]) and np.array_equal(v[hit], g["v"][hit])
+
+
+def test_oracle_trace_matches_reference_fixture_1m(oracle):
+    g = np.load(os.path.join(GOLDEN, "trace_soup_1m.npz"))
+    tris = oracle.gen_soup(SOUP_SEED, 1_000_000)
+    rays = oracle.gen_rays(RAY_SEED, 65536)
+    ids, t, _, _ = oracle.trace(tris, rays, mode=0)
+    assert np.array_equal(ids, g["ids"]), f"{(ids != g['ids']).sum()} id mismatches"
+    hit = ids >= 0
+    assert hit.mean() > 0.95
+    assert np.array_equal(t[hit], g["t"][hit])
+
+
+def test_oracle_trace_matches_live_reference(oracle, reference):
+    tris = oracle.gen_soup(31, 20000)
+    rays = oracle.gen_rays(32, 4096)
+    s = reference.soup(tris)
+    rid, rt, ru, rv, _ = s.trace(rays)
+    s.close()
+    ids, t, u, v = oracle.trace(tris, rays, mode=0)
+    assert np.array_equal(ids, rid)
+    hit = ids >= 0
+    assert np.array_equal(t[hit], rt[hit]) and np.array_equal(u[hit], ru[hit]) and np.array_equal(v[hit], rv[hit])
+
+
+def test_watertight_differs_only_at_edges(oracle):
+    tris = oracle.gen_soup(41, 200000)
+    rays = oracle.gen_rays(42, 20000)
+    a, ta, _, _ = oracle.trace(tris, rays, mode=0)
+    b, tb, _, _ = oracle.trace(tris, rays, mode=1)
+    assert (a != b).mean() < 2e-3
+    both = (a == b) & (a >= 0)
+    assert np.max(np.abs(ta[both] - tb[both]) / ta[both]) < 1e-5
+
+
+def test_oracle_compat_render_matches_reference_fixture(oracle):
+    from oracle.oracle import PROFILE_COMPAT, SceneData
+    from salty_gb300 import scenes
+    g = np.load(os.path.join(GOLDEN, "cornell_ref_64.npz"))
+    sc = scenes.cornell("baseline")
+    sd = SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], None, sc["sky"],
+                   sc["camera"])
+    spp = int(g["spp"])
+    tot, sq = oracle.render(sd, int(g["width"]), int(g["height"]), spp, int(g["max_bounce"]),
+                            profile=PROFILE_COMPAT, seed=777)
+    m = tot / spp
+    v = np.maximum((sq / spp - m * m) * spp / (spp - 1) / spp, 0)
+    z = zscores(m, v, g["mean"], g["var"])
+    # 3-sigma per pixel: at most ~1% of pixel-channels outside, none beyond 6 sigma
+    assert np.mean(np.abs(z) > 3) < 0.01
+    assert np.max(np.abs(z)) < 6
+    assert abs(m.mean() / g["mean"].mean() - 1) < 0.01
+
+
+def test_oracle_tonemap_matches_reference_fixture(oracle):
+    g = np.load(os.path.join(GOLDEN, "tonemap_ref.npz"))
+    img = g["img"]
+    for k in (0, 1, 2):
+        out, ave, mx = oracle.tonemap(k, img)
+        assert np.array_equal(out, g[f"tm{k}"]), f"tonemap {k}"
+
+
+def test_oracle_srgb_matches_reference_capture(oracle):
+    g = np.load(os.path.join(GOLDEN, "tonemap_ref.npz"))
+    out, _, _ = oracle.tonemap(2, g["img"])
+    s8 = oracle.srgb8(out, ref_oetf=True)
+    assert np.array_equal(s8, g["srgb_aces_ref"])
+
+
+def test_oracle_nlm_matches_reference_fixture(oracle):
+    g = np.load(os.path.join(GOLDEN, "nlm_ref.npz"))
+    out = oracle.nlm_ref(g["rgba"], float(g["coeff"]))
+    np.testing.assert_allclose(out, g["out"], rtol=2e-6, atol=1e-7)
+
+
+def test_oracle_physical_render_is_consistent(oracle):
+    """The physical estimator converges to the same image with and without MIS-relevant
+    sampling changes: two seeds agree within 3 sigma (self-consistency of the checker)."""
+    from oracle.oracle import PROFILE_PHYSICAL, SceneData
+    from salty_gb300 import scenes
+    sc = scenes.cornell("mixed")
+    sd = SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], None, sc["sky"],
+                   sc["camera"])
+    res = []
+    for seed in (1, 2):
+        tot, sq = oracle.render(sd, 32, 32, 256, 8, profile=PROFILE_PHYSICAL, seed=seed)
+        m = tot / 256
+        res.append((m, np.maximum((sq / 256 - m * m) * 256 / 255 / 256, 0)))
+    z = zscores(res[0][0], res[0][1], res[1][0], res[1][1])
+    assert np.mean(np.abs(z) > 3) < 0.02

@@ -1,0 +1,115 @@
+"""Parity of the wavefront path tracer (salty_render) with the reference and the oracle.
+
+Images at equal spp must agree per pixel within a 3-sigma Monte Carlo bound: with
+independent estimates a, b and their variances of the mean, z = (a - b)/sqrt(va + vb);
+the test allows 1% of pixel-channels beyond 3 sigma (a normal variable exceeds it 0.27%
+of the time) and none beyond 6.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def zstats(ma, va, mb, vb):
+    z = (ma - mb) / np.sqrt(np.maximum(va + vb, 1e-30))
+    return np.mean(np.abs(z) > 3), np.max(np.abs(z))
+
+
+def _gpu_scene(ctx, sc):
+    from salty_gb300 import scenes
+    s = scenes.upload(ctx, sc)
+    s.build()
+    return s
+
+
+def _oracle_scene(sc):
+    from oracle.oracle import SceneData
+    return SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], sc["sun"],
+                     sc["sky"], sc["camera"])
+
+
+def test_compat_cornell_matches_reference_fixture(ctx):
+    """The reference's own estimator (PathTracer::Radiance) vs the GPU compat profile."""
+    import salty_gb300
+    from salty_gb300 import scenes
+    g = np.load(os.path.join(GOLDEN, "cornell_ref_64.npz"))
+    s = _gpu_scene(ctx, scenes.cornell("baseline"))
+    r = s.render(int(g["width"]), int(g["height"]), int(g["spp"]), int(g["max_bounce"]),
+                 profile=salty_gb300.PROFILE_COMPAT, seed=4242)
+    frac, zmax = zstats(r["mean"], r["var"], g["mean"], g["var"])
+    assert frac < 0.01 and zmax < 6, (frac, zmax)
+    assert abs(r["mean"].mean() / g["mean"].mean() - 1) < 0.01
+
+
+@pytest.mark.parametrize("variant", ["baseline", "mixed"])
+def test_physical_cornell_matches_oracle(ctx, oracle, variant):
+    import salty_gb300
+    from oracle.oracle import PROFILE_PHYSICAL
+    from salty_gb300 import scenes
+    sc = scenes.cornell(variant)
+    W = H = 48
+    spp = 512
+    s = _gpu_scene(ctx, sc)
+    r = s.render(W, H, spp, 8, rr_depth=3, profile=salty_gb300.PROFILE_PHYSICAL, seed=99)
+    tot, sq = oracle.render(_oracle_scene(sc), W, H, spp, 8, rr_depth=3, profile=PROFILE_PHYSICAL, seed=1234)
+    m = tot / spp
+    v = np.maximum((sq / spp - m * m) * spp / (spp - 1) / spp, 0)
+    frac, zmax = zstats(r["mean"], r["var"], m, v)
+    assert frac < 0.01 and zmax < 6, (frac, zmax)
+    assert r["rays"] > W * H * spp  # primary + extension + shadow rays
+
+
+def test_same_streams_as_oracle_give_nearly_identical_images(ctx, oracle):
+    """Same seed => same per-(pixel, sample) PCG streams: most samples follow the same path,
+    so the images agree far inside the Monte Carlo bound."""
+    import salty_gb300
+    from oracle.oracle import PROFILE_PHYSICAL
+    from salty_gb300 import scenes
+    sc = scenes.cornell("baseline")
+    s = _gpu_scene(ctx, sc)
+    r = s.render(32, 32, 64, 8, profile=salty_gb300.PROFILE_PHYSICAL, seed=7)
+    tot, _ = oracle.render(_oracle_scene(sc), 32, 32, 64, 8, profile=PROFILE_PHYSICAL, seed=7)
+    m = tot / 64
+    assert np.median(np.abs(r["mean"] - m) / np.maximum(m, 1e-3)) < 1e-3
+
+
+def test_progressive_accumulation_and_fp64_film(ctx):
+    import salty_gb300
+    from salty_gb300 import scenes
+    s = _gpu_scene(ctx, scenes.cornell("baseline"))
+    a = s.render(32, 32, 16, 8, seed=5, want=("mean",))
+    b = s.render(32, 32, 16, 8, seed=5, accumulate=True, want=("mean", "var"))
+    assert b["samples"] == 32
+    s64 = s.render(32, 32, 32, 8, seed=5, fp64=True, want=("mean", "var"))
+    assert s64["samples"] == 32
+    frac, zmax = zstats(b["mean"], b["var"], s64["mean"], s64["var"])
+    assert frac < 0.02
+    # the first 16 samples are part of the accumulated film
+    assert np.all(np.isfinite(b["mean"])) and not np.array_equal(a["mean"], b["mean"])
+
+
+def test_srgb8_output_is_tonemapped_film(ctx):
+    import salty_gb300
+    from salty_gb300 import scenes
+    s = _gpu_scene(ctx, scenes.cornell("baseline"))
+    r = s.render(40, 30, 16, 8, seed=3, tonemap=salty_gb300.TM_ACES, ref_oetf=True)
+    _, s8, _, _ = ctx.tonemap(r["mean"], salty_gb300.TM_ACES, srgb=True, ref_oetf=True)
+    assert np.array_equal(r["srgb"], s8)
+    assert r["srgb"].max() <= 247  # the reference OETF maps 1.0 to 247
+
+
+def test_render_rejects_bad_options(ctx):
+    import salty_gb300
+    from salty_gb300 import scenes
+    s = _gpu_scene(ctx, scenes.cornell("baseline"))
+    with pytest.raises(salty_gb300.SaltyError):
+        s.render(0, 10, 1, 8)
+    with pytest.raises(salty_gb300.SaltyError):
+        s.render(10, 10, 1, 0)
+    with pytest.raises(salty_gb300.SaltyError):
+        s.render(10, 10, 1, 8, profile=7)
