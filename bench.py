@@ -198,7 +198,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--any-hit", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (smaller cases for profiling)")
     args = ap.parse_args()
+    n_rays = args.rays
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     ws, rank, local, pg = dist_setup()
     if args.impl == "reference":
@@ -215,18 +217,18 @@ def main():
     tris = salty_gb300.microbench_soup(SOUP_SEED, N_TRIS)
     scene = ctx.upload_scene(tris)
     info = scene.build()
-    rays_h = ctx.pinned((N_RAYS, 8), np.float32)
-    salty_gb300.microbench_rays(RAY_SEED, N_RAYS, TMIN, out=rays_h)
-    hits_h = ctx.pinned((N_RAYS, 4), np.float32)
+    rays_h = ctx.pinned((n_rays, 8), np.float32)
+    salty_gb300.microbench_rays(RAY_SEED, n_rays, TMIN, out=rays_h)
+    hits_h = ctx.pinned((n_rays, 4), np.float32)
     d_rays = torch.from_numpy(rays_h).to(dev)
-    d_hits = torch.empty((N_RAYS, 4), dtype=torch.float32, device=dev)
+    d_hits = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
     torch.cuda.synchronize()  # the library runs on its own stream
     any_hit = args.any_hit
 
     # fetch counts (untimed): algorithmic bytes per ray
     st = scene.trace_raw(d_rays, d_hits, any_hit=any_hit, counters=True)
-    n_node = st["node_fetches"] / N_RAYS
-    n_tri = st["tri_fetches"] / N_RAYS
+    n_node = st["node_fetches"] / n_rays
+    n_tri = st["tri_fetches"] / n_rays
     bytes_per_ray = 32 + 16 + 80 * n_node + 48 * n_tri
 
     # ---- device-resident steps
@@ -247,7 +249,7 @@ def main():
     region_ms = e0.elapsed_time(e1)
     region_ms = max_over_ranks(pg, region_ms, dev)
     clocks = clk.summary()
-    value = ws * N_RAYS * args.steps / (region_ms / 1e3) / 1e6
+    value = ws * n_rays * args.steps / (region_ms / 1e3) / 1e6
     launch_ms = kernel_ms / args.steps
 
     # ---- end to end: pinned host rays in, host hits out, every step
@@ -263,26 +265,27 @@ def main():
     for _ in range(args.steps):
         s = scene.trace_raw(rays_h, hits_h, any_hit=any_hit)
         h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
-        e2e_kernels += math.ceil(N_RAYS / (1 << 21))
+        e2e_kernels += math.ceil(n_rays / (1 << 21))
     e3.record()
     torch.cuda.synchronize()
     barrier(pg)
     e2e_ms = max_over_ranks(pg, e2.elapsed_time(e3), dev)
-    e2e_value = ws * N_RAYS * args.steps / (e2e_ms / 1e3) / 1e6
+    e2e_value = ws * n_rays * args.steps / (e2e_ms / 1e3) / 1e6
 
-    # check: the last device step's hits equal the host path's
-    same = bool(torch.equal(d_hits.cpu(), torch.from_numpy(hits_h)))
+    # check: the last device step's hits equal the host path's, bit for bit (a miss stores
+    # id -1, whose float bit pattern is a NaN, so compare the raw words)
+    same = bool(np.array_equal(d_hits.cpu().numpy().view(np.int32), hits_h.view(np.int32)))
 
     peaks = measured_peaks()
-    achieved = bytes_per_ray * N_RAYS / (launch_ms / 1e3) / 1e9
+    achieved = bytes_per_ray * n_rays / (launch_ms / 1e3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": region_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded PCG soup and rays, generated on the host)",
-        "config": {"workload": "traversal microbenchmark: 1M-triangle soup, 16,777,216 rays, "
+        "config": {"workload": f"traversal microbenchmark: 1M-triangle soup, {n_rays:,} rays, "
                                + ("any hit" if any_hit else "closest hit"),
-                   "n_tris": N_TRIS, "rays_per_step": N_RAYS, "bvh": "device 32-bin SAH -> 8-wide, 8-bit planes",
+                   "n_tris": N_TRIS, "rays_per_step": n_rays, "bvh": "device 32-bin SAH -> 8-wide, 8-bit planes",
                    "bvh_nodes": info["n_nodes"], "bvh_depth": info["depth"], "bvh_build_ms": info["build_ms"],
                    "sah_cost": info["sah_cost"], "triangle_test": "reference-compatible (bit-exact ids)",
                    "l2": "inputs larger than L2 (rays 512 MiB, hits 256 MiB); BVH resident",

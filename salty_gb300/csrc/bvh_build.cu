@@ -531,11 +531,13 @@ __global__ void k_collapse(const BNode* __restrict__ bn, int nwork, const int2* 
         }
         if (c.count == 0) {
             imask |= 1u << s;
+            meta[s] = (unsigned char)((1u << 5) | (24u + s));  // one hit bit at 24 + slot
             int idx = child_base + r_int++;
             int w = atomicAdd(&ctr->next_work, 1);
             work_next[w] = make_int2(set[i], idx);
         } else {
-            meta[s] = (unsigned char)((c.count << 5) | off);
+            // unary triangle count in the top three bits, first triangle in the low five
+            meta[s] = (unsigned char)((((1u << c.count) - 1u) << 5) | off);
             for (int j = 0; j < c.count; ++j) {
                 int q = prim[c.a + j];
                 const float* p = pos + (size_t)q * 9;

@@ -21,8 +21,11 @@ namespace salty {
 // quantised box contains the child's exact box.  Slot bit a is 1 when the child lies on
 // the high side of the node centre along axis a, so visiting slots in increasing order
 // of (slot XOR ray-octant) is roughly front to back.  imask bit s: slot s is an inner
-// node, numbered child_base + popc(imask & ((1<<s)-1)).  A leaf slot's meta byte is
-// (count << 5) | offset: triangles tri_base + offset .. + count - 1.  Empty slots have
+// node, numbered child_base + popc(imask & ((1<<s)-1)); its meta byte is
+// (1 << 5) | (24 + s).  A leaf slot's meta byte is (((1 << count) - 1) << 5) | offset:
+// triangles tri_base + offset .. + count - 1.  So (meta >> 5) << (meta & 31) is the
+// slot's bit pattern in a 32-bit hit mask (triangles 0..23, inner children 24..31,
+// after XOR-ing inner slots with the ray octant).  Empty slots have meta 0 and
 // qlo = 255 > qhi = 0, an empty box.
 struct alignas(16) Bvh8Node {
     uint4 w[5];

@@ -12,6 +12,8 @@ namespace salty {
 namespace {
 
 constexpr int kTraceBlock = 128;
+constexpr int kPool = 128;          // rays taken from the global cursor per refill
+constexpr int kPostponeLanes = 7;   // test triangles only with at least this many lanes
 
 // counters: [0] ray cursor, [1] node fetches, [2] triangle fetches
 template <bool ANY, bool WT, bool COUNT, int DEPTH>
@@ -24,21 +26,56 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
     const int lane = threadIdx.x & 31;
     // queue length from device memory when given (wavefront queues), else the argument
     const long long n = n_dev ? (long long)*n_dev : n_arg;
+    const unsigned lt_mask = (1u << lane) - 1u;
     TravCount cnt{0, 0};
     int overflow = 0;
+    // Warp-uniform pool of ray indices [pool_next, pool_end), refilled kPool at a time
+    // from the global cursor; each lane holds one ray and takes a new one from the pool
+    // as soon as its walk ends.
+    long long pool_next = 0, pool_end = 0;
+    bool drained = false;
+    long long rid = -1;
+    TravRay r;
+    TravState s;
     for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&counters[0], 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= (unsigned long long)n) break;
-        const long long i = (long long)base + lane;
-        if (i < n) {
-            const float4 ra = __ldcs(rays + 2 * i), rb = __ldcs(rays + 2 * i + 1);
-            TravRay r;
-            make_trav_ray(r, ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w);
-            TravHit h;
-            traverse<ANY, WT, COUNT, DEPTH>(nodes, tris, r, cull_slack, st, h, cnt, overflow);
-            __stcs(hits + i, make_float4(h.t, __int_as_float(h.id), h.u, h.v));
+        const bool idle = rid < 0;
+        const unsigned idle_mask = __ballot_sync(0xffffffffu, idle);
+        if (idle_mask) {
+            if (pool_next >= pool_end && !drained) {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(&counters[0], (unsigned long long)kPool);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                pool_next = (long long)base;
+                pool_end = min((long long)base + kPool, n);
+                if ((long long)base + kPool >= n) drained = true;
+            }
+            const long long mine = pool_next + __popc(idle_mask & lt_mask);
+            if (idle && mine < pool_end) {
+                rid = mine;
+                const float4 ra = __ldcs(rays + 2 * rid), rb = __ldcs(rays + 2 * rid + 1);
+                make_trav_ray(r, ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w);
+                trav_init(s, r);
+            }
+            pool_next = min(pool_end, pool_next + __popc(idle_mask));
+        }
+        const bool active = rid >= 0;
+        if (__ballot_sync(0xffffffffu, active) == 0) break;
+        if (active && s.ng_hits) trav_node_step<DEPTH, COUNT>(s, nodes, r, st, cnt, overflow);
+        // Triangle postponing: with too few lanes holding triangles, set the group aside
+        // and keep walking nodes with the rest of the warp.
+        const bool want = active && s.tg_hits != 0;
+        const unsigned want_mask = __ballot_sync(0xffffffffu, want);
+        bool run = want;
+        if (want && __popc(want_mask) < kPostponeLanes && s.ng_hits != 0 && s.sp < DEPTH) {
+            st.at(s.sp++) = make_uint2(s.tg_base, s.tg_hits | kTriGroupFlag);
+            s.tg_hits = 0;
+            run = false;
+        }
+        bool done = false;
+        if (run) done = trav_tri_step<ANY, WT, COUNT>(s, tris, r, cull_slack, cnt);
+        if (active && (done || !trav_pop(s, st))) {
+            __stcs(hits + rid, make_float4(s.hit.t, __int_as_float(s.hit.id), s.hit.u, s.hit.v));
+            rid = -1;
         }
     }
     if (COUNT) {
@@ -95,11 +132,12 @@ salty_status trace_launch(salty_ctx* ctx, salty_scene* sc, const float4* d_rays,
                           uint32_t flags, float4* d_hits, unsigned long long* d_counters, cudaStream_t st,
                           int* d_status) {
     SALTY_TRY_CUDA(ctx->err, cudaMemsetAsync(d_counters, 0, 3 * sizeof(unsigned long long), st));
-    if (sc->bvh.depth <= 16)
-        return dispatch_depth<16>(ctx, sc, d_rays, n, n_dev, flags, d_hits, d_counters, st, d_status);
-    if (sc->bvh.depth <= 40)
-        return dispatch_depth<40>(ctx, sc, d_rays, n, n_dev, flags, d_hits, d_counters, st, d_status);
-    return ctx->err.fail(SALTY_ERR_CAPACITY, "BVH depth %d exceeds the traversal stack (40)", sc->bvh.depth);
+    // Each BVH level can hold one pending node group and one postponed triangle group.
+    if (2 * sc->bvh.depth + 1 <= 24)
+        return dispatch_depth<24>(ctx, sc, d_rays, n, n_dev, flags, d_hits, d_counters, st, d_status);
+    if (2 * sc->bvh.depth + 1 <= 48)
+        return dispatch_depth<48>(ctx, sc, d_rays, n, n_dev, flags, d_hits, d_counters, st, d_status);
+    return ctx->err.fail(SALTY_ERR_CAPACITY, "BVH depth %d exceeds the traversal stack (23 levels)", sc->bvh.depth);
 }
 
 }  // namespace salty

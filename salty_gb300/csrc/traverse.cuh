@@ -52,7 +52,8 @@ __device__ __forceinline__ float safe_rcp(float d) {
 __device__ __forceinline__ void make_trav_ray(TravRay& r, float ox, float oy, float oz, float tmin, float dx,
                                               float dy, float dz, float tmax) {
     r.ox = ox; r.oy = oy; r.oz = oz; r.dx = dx; r.dy = dy; r.dz = dz;
-    r.tmin = tmin; r.tmax = tmax;
+    r.tmin = fmaxf(tmin, 0.0f);  // a negative tmin is treated as 0
+    r.tmax = tmax;
     r.ix = safe_rcp(dx); r.iy = safe_rcp(dy); r.iz = safe_rcp(dz);
     r.oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
     float ad[3] = {fabsf(dx), fabsf(dy), fabsf(dz)};
@@ -72,13 +73,18 @@ __device__ __forceinline__ void make_trav_ray(TravRay& r, float ox, float oy, fl
 // ---------------------------------------------------------------- triangle tests
 // The reference's test (src/s3d_triangle.cpp:73-105), operation for operation, with
 // every product and sum rounded separately (no fused multiply-add) and IEEE division,
-// so t, beta and gamma equal the reference's bit for bit.  Sign checks on the
-// numerators reject before the divisions where the quotient's sign alone decides.
+// so t, beta and gamma equal the reference's bit for bit.  The divisions are the costly
+// part, so candidates are first rejected without them wherever the outcome is already
+// certain: a numerator of the wrong sign (the quotient's sign is exact), or
+// |nb| + |ng| clearly above |div| (beta + gamma >= 1 after every rounding), or
+// |nt| clearly above |div| * tfar (t beyond the farthest useful distance).  "Clearly"
+// is a relative margin of 2^-16, far above the few ulps the roundings can move.
+// Candidates inside the margins take the exact path.  tfar is the current closest hit
+// (or tmax): equal distances still reach the exact path, for the lowest-id tie rule.
 __device__ __forceinline__ bool tri_ref(const TravRay& r, float4 a, float4 b, float4 c, float tmin, float tmax,
-                                        float& t, float& u, float& v) {
+                                        float tfar, float& t, float& u, float& v) {
     const float e1x = __fsub_rn(b.x, a.x), e1y = __fsub_rn(b.y, a.y), e1z = __fsub_rn(b.z, a.z);
     const float e2x = __fsub_rn(c.x, a.x), e2y = __fsub_rn(c.y, a.y), e2z = __fsub_rn(c.z, a.z);
-    // s1 = d x e2
     const float s1x = __fsub_rn(__fmul_rn(r.dy, e2z), __fmul_rn(r.dz, e2y));
     const float s1y = __fsub_rn(__fmul_rn(r.dz, e2x), __fmul_rn(r.dx, e2z));
     const float s1z = __fsub_rn(__fmul_rn(r.dx, e2y), __fmul_rn(r.dy, e2x));
@@ -87,17 +93,20 @@ __device__ __forceinline__ bool tri_ref(const TravRay& r, float4 a, float4 b, fl
     const float dvx = __fsub_rn(r.ox, a.x), dvy = __fsub_rn(r.oy, a.y), dvz = __fsub_rn(r.oz, a.z);
     const float nb = __fadd_rn(__fadd_rn(__fmul_rn(dvx, s1x), __fmul_rn(dvy, s1y)), __fmul_rn(dvz, s1z));
     if (nb == 0.0f || (__float_as_uint(nb) ^ __float_as_uint(div)) >> 31) return false;  // beta <= 0
-    const float beta = __fdiv_rn(nb, div);
-    if (beta <= 0.0f || beta >= 1.0f) return false;
-    // s2 = dv x e1
     const float s2x = __fsub_rn(__fmul_rn(dvy, e1z), __fmul_rn(dvz, e1y));
     const float s2y = __fsub_rn(__fmul_rn(dvz, e1x), __fmul_rn(dvx, e1z));
     const float s2z = __fsub_rn(__fmul_rn(dvx, e1y), __fmul_rn(dvy, e1x));
     const float ng = __fadd_rn(__fadd_rn(__fmul_rn(r.dx, s2x), __fmul_rn(r.dy, s2y)), __fmul_rn(r.dz, s2z));
     if (ng == 0.0f || (__float_as_uint(ng) ^ __float_as_uint(div)) >> 31) return false;  // gamma <= 0
+    const float ad = fabsf(div);
+    constexpr float kMargin = 1.0f + 1.0f / 65536.0f;
+    if (fabsf(nb) + fabsf(ng) > ad * kMargin) return false;                             // beta + gamma >= 1
+    const float nt = __fadd_rn(__fadd_rn(__fmul_rn(e2x, s2x), __fmul_rn(e2y, s2y)), __fmul_rn(e2z, s2z));
+    if (fabsf(nt) > ad * (tfar * kMargin)) return false;                                 // t > tfar
+    const float beta = __fdiv_rn(nb, div);
+    if (beta <= 0.0f || beta >= 1.0f) return false;
     const float gamma = __fdiv_rn(ng, div);
     if (gamma <= 0.0f || __fadd_rn(beta, gamma) >= 1.0f) return false;
-    const float nt = __fadd_rn(__fadd_rn(__fmul_rn(e2x, s2x), __fmul_rn(e2y, s2y)), __fmul_rn(e2z, s2z));
     const float dist = __fdiv_rn(nt, div);
     if (!(dist >= tmin) || dist > tmax) return false;
     t = dist; u = beta; v = gamma;
@@ -141,12 +150,27 @@ __device__ __forceinline__ bool tri_watertight(const TravRay& r, float4 a, float
     return true;
 }
 
-__device__ __forceinline__ float u8f(unsigned w, int k) { return (float)((w >> (8 * k)) & 0xffu); }
+// Byte k of w as a float: the byte is placed under the exponent of 2^23 (one byte
+// permute) and 2^23 is subtracted (one add) -- exact for 0..255.
+__device__ __forceinline__ float u8f(unsigned w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + k)) - 8388608.0f;
+}
 
-// Relative widening of box intervals: covers the rounding of the decoded planes,
-// of 1/d and of the fused plane evaluation, so the quantised-box test never rejects a
-// box the exact ray segment meets.
-constexpr float kBoxSlack = 1.0f / (1 << 20);
+__device__ __forceinline__ float fmax4(float a, float b, float c, float d) {
+    float m;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(m) : "f"(a), "f"(b), "f"(c));
+    return fmaxf(m, d);
+}
+__device__ __forceinline__ float fmin4(float a, float b, float c, float d) {
+    float m;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(m) : "f"(a), "f"(b), "f"(c));
+    return fminf(m, d);
+}
+
+// Widening of the far plane (tn >= tmin >= 0): covers the rounding of the decoded
+// planes, of 1/d and of the fused plane evaluation, so the quantised-box test never
+// rejects a box the exact ray segment meets.
+constexpr float kBoxSlackMul = 1.0f + 1.0f / (1 << 17);
 
 // Intersects the 8 children of node `idx`.  Returns inner-child hits in key order
 // (bit slot^oct) and triangle hits relative to tri_base.
@@ -171,95 +195,134 @@ __device__ __forceinline__ void intersect_node(const Bvh8Node* __restrict__ node
     const unsigned nhy0 = (r.oct & 2) ? w2.z : w4.x, nhy1 = (r.oct & 2) ? w2.w : w4.y;
     const unsigned nlz0 = (r.oct & 4) ? w4.z : w3.x, nlz1 = (r.oct & 4) ? w4.w : w3.y;
     const unsigned nhz0 = (r.oct & 4) ? w3.x : w4.z, nhz1 = (r.oct & 4) ? w3.y : w4.w;
-    inner_hits = 0;
-    tri_hits = 0;
+    // Inner-child meta bytes hold 24 + slot; XOR-ing their low three bits with the ray
+    // octant turns that into 24 + key, so one shift per child places inner hits in bits
+    // 24..31 (key order) and leaf triangles in bits 0..23.
+    const unsigned spread_lo = (((imask & 0x0fu) * 0x00204081u) & 0x01010101u) * r.oct;
+    const unsigned spread_hi = ((((imask >> 4) & 0x0fu) * 0x00204081u) & 0x01010101u) * r.oct;
+    unsigned hits = 0;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
         const unsigned lx = half ? nlx1 : nlx0, hx = half ? nhx1 : nhx0;
         const unsigned ly = half ? nly1 : nly0, hy = half ? nhy1 : nhy0;
         const unsigned lz = half ? nlz1 : nlz0, hz = half ? nhz1 : nhz0;
-        const unsigned meta = half ? w1.w : w1.z;
+        const unsigned meta = half ? (w1.w ^ spread_hi) : (w1.z ^ spread_lo);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const float tnx = fmaf(u8f(lx, k), ax, bx), tfx = fmaf(u8f(hx, k), ax, bx);
             const float tny = fmaf(u8f(ly, k), ay, by), tfy = fmaf(u8f(hy, k), ay, by);
             const float tnz = fmaf(u8f(lz, k), az, bz), tfz = fmaf(u8f(hz, k), az, bz);
-            float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
-            float tf = fminf(fminf(tfx, tfy), fminf(tfz, tcull));
-            tn = fmaf(-kBoxSlack, fabsf(tn), tn);
-            tf = fmaf(kBoxSlack, fabsf(tf), tf);
-            if (tn <= tf) {
-                const int slot = half * 4 + k;
-                if (imask & (1u << slot)) {
-                    inner_hits |= 1u << (slot ^ r.oct);
-                } else {
-                    const unsigned m = (meta >> (8 * k)) & 0xffu;
-                    const unsigned cnt = m >> 5, off = m & 31u;
-                    tri_hits |= ((1u << cnt) - 1u) << off;
-                }
+            const float tn = fmax4(tnx, tny, tnz, r.tmin);
+            const float tf = fmin4(tfx, tfy, tfz, tcull);
+            if (tn <= tf * kBoxSlackMul) {
+                const unsigned m = __byte_perm(meta, 0u, 0x4440u + k);
+                hits |= (m >> 5) << (m & 31u);
             }
         }
     }
+    inner_hits = hits >> 24;
+    tri_hits = hits & 0x00ffffffu;
 }
 
-// Closest hit (ANY = false) or any hit.  CULL_SLACK: a box is kept while its entry is
-// within best_t * (1 + slack) -- a relative margin over the triangle test's rounding, so
-// the closest hit never depends on which nodes were culled.
-template <bool ANY, bool WATERTIGHT, bool COUNT, int DEPTH>
-__device__ __forceinline__ bool traverse(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris,
-                                         const TravRay& r, float cull_slack, TravStack<DEPTH> stack,
-                                         TravHit& hit, TravCount& cnt, int& overflow) {
-    hit.t = INFINITY;
-    hit.id = -1;
-    hit.u = hit.v = 0.0f;
-    float tcull = r.tmax;
-    unsigned ng_base = 0, ng_hits = 1u << r.oct, ng_imask = 1u;  // group holding the root
-    unsigned tg_base = 0, tg_hits = 0;
-    int sp = 0;
-    for (;;) {
-        if (ng_hits) {
-            const unsigned key = __ffs(ng_hits) - 1;
-            ng_hits &= ng_hits - 1;
-            const unsigned slot = key ^ r.oct;
-            const unsigned idx = ng_base + __popc(ng_imask & ((1u << slot) - 1u));
-            if (ng_hits) {
-                if (sp >= DEPTH) { overflow = 1; return hit.id >= 0; }
-                stack.at(sp++) = make_uint2(ng_base, (ng_hits << 8) | ng_imask);
+// ---------------------------------------------------------------- stepwise walk
+// The walk of one ray as explicit state, advanced one node (and its triangles) per step,
+// so a warp can keep every lane busy: finished lanes take new rays while the others
+// continue (k_trace), and triangle groups can be set aside on the stack (postponed)
+// while too few lanes of the warp have triangles to test.
+struct TravState {
+    unsigned ng_base, ng_hits, ng_imask;  // current node group (hits in key order)
+    unsigned tg_base, tg_hits;            // current triangle group
+    int sp;
+    float tcull;                          // far limit for boxes: best t * (1 + slack), or tmax
+    TravHit hit;
+};
+
+// Stack entries with this flag in .y are postponed triangle groups.
+constexpr unsigned kTriGroupFlag = 0x80000000u;
+
+__device__ __forceinline__ void trav_init(TravState& s, const TravRay& r) {
+    s.ng_base = 0;
+    s.ng_hits = 1u << r.oct;  // a group holding only the root, in slot 0
+    s.ng_imask = 1u;
+    s.tg_base = 0;
+    s.tg_hits = 0;
+    s.sp = 0;
+    s.tcull = r.tmax;
+    s.hit.t = INFINITY;
+    s.hit.id = -1;
+    s.hit.u = s.hit.v = 0.0f;
+}
+
+// Visits the nearest pending child of the current node group.  A full stack drops the
+// remaining group and raises `overflow` (reported to the caller as an error).
+template <int DEPTH, bool COUNT>
+__device__ __forceinline__ void trav_node_step(TravState& s, const Bvh8Node* __restrict__ nodes, const TravRay& r,
+                                               TravStack<DEPTH> st, TravCount& cnt, int& overflow) {
+    const unsigned key = __ffs(s.ng_hits) - 1;
+    s.ng_hits &= s.ng_hits - 1;
+    const unsigned slot = key ^ r.oct;
+    const unsigned idx = s.ng_base + __popc(s.ng_imask & ((1u << slot) - 1u));
+    if (s.ng_hits) {
+        if (s.sp < DEPTH) st.at(s.sp++) = make_uint2(s.ng_base, (s.ng_hits << 8) | s.ng_imask);
+        else overflow = 1;
+    }
+    unsigned cb, im, ih, tb, th;
+    intersect_node(nodes, idx, r, s.tcull, cb, im, ih, tb, th);
+    if (COUNT) ++cnt.nodes;
+    s.ng_base = cb;
+    s.ng_imask = im;
+    s.ng_hits = ih;
+    s.tg_base = tb;
+    s.tg_hits = th;
+}
+
+// Tests the triangles of the current group.  Closest hit: smallest t, equal t to the
+// lowest id; boxes are then culled beyond t * (1 + cull_slack), a relative margin over
+// the triangle test's rounding so the answer never depends on what was culled.
+// Returns true when an any-hit query has its answer.
+template <bool ANY, bool WATERTIGHT, bool COUNT>
+__device__ __forceinline__ bool trav_tri_step(TravState& s, const float4* __restrict__ tris, const TravRay& r,
+                                              float cull_slack, TravCount& cnt) {
+    while (s.tg_hits) {
+        const unsigned k = __ffs(s.tg_hits) - 1;
+        s.tg_hits &= s.tg_hits - 1;
+        const float4* tp = tris + (size_t)(s.tg_base + k) * kTriFloat4;
+        const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+        if (COUNT) ++cnt.tris;
+        float t, u, v;
+        const float tlim = ANY ? r.tmax : fminf(r.tmax, s.hit.t);
+        const bool h = WATERTIGHT ? tri_watertight(r, a, b, c, r.tmin, tlim, t, u, v)
+                                  : tri_ref(r, a, b, c, r.tmin, r.tmax, tlim, t, u, v);
+        if (h) {
+            const int id = __float_as_int(a.w);
+            if (t < s.hit.t || (t == s.hit.t && id < s.hit.id)) {
+                s.hit.t = t;
+                s.hit.u = u;
+                s.hit.v = v;
+                s.hit.id = id;
+                if (ANY) return true;
+                s.tcull = fminf(r.tmax, fmaf(cull_slack, t, t));
             }
-            unsigned cb, im, ih, tb, th;
-            intersect_node(nodes, idx, r, tcull, cb, im, ih, tb, th);
-            if (COUNT) ++cnt.nodes;
-            ng_base = cb; ng_imask = im; ng_hits = ih;
-            tg_base = tb; tg_hits = th;
-        }
-        while (tg_hits) {
-            const unsigned k = __ffs(tg_hits) - 1;
-            tg_hits &= tg_hits - 1;
-            const float4* tp = tris + (size_t)(tg_base + k) * kTriFloat4;
-            const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-            if (COUNT) ++cnt.tris;
-            float t, u, v;
-            const float tlim = ANY ? r.tmax : hit.t;
-            bool h = WATERTIGHT ? tri_watertight(r, a, b, c, r.tmin, fminf(r.tmax, tlim), t, u, v)
-                                : tri_ref(r, a, b, c, r.tmin, r.tmax, t, u, v);
-            if (h) {
-                const int id = __float_as_int(a.w);
-                if (t < hit.t || (t == hit.t && id < hit.id)) {
-                    hit.t = t; hit.u = u; hit.v = v; hit.id = id;
-                    if (ANY) return true;
-                    tcull = fminf(r.tmax, fmaf(cull_slack, t, t));
-                }
-            }
-        }
-        if (!ng_hits) {
-            if (sp == 0) break;
-            const uint2 e = stack.at(--sp);
-            ng_base = e.x;
-            ng_hits = e.y >> 8;
-            ng_imask = e.y & 0xffu;
         }
     }
-    return hit.id >= 0;
+    return false;
+}
+
+// Makes a group current when both are exhausted.  Returns false when the walk is over.
+template <int DEPTH>
+__device__ __forceinline__ bool trav_pop(TravState& s, TravStack<DEPTH> st) {
+    if (s.ng_hits || s.tg_hits) return true;
+    if (s.sp == 0) return false;
+    const uint2 e = st.at(--s.sp);
+    if (e.y & kTriGroupFlag) {
+        s.tg_base = e.x;
+        s.tg_hits = e.y & ~kTriGroupFlag;
+    } else {
+        s.ng_base = e.x;
+        s.ng_hits = e.y >> 8;
+        s.ng_imask = e.y & 0xffu;
+    }
+    return true;
 }
 
 }  // namespace salty
