@@ -201,6 +201,27 @@ salty_status salty_tonemap(salty_ctx* ctx, int32_t type, int32_t width, int32_t 
                            const float* rgb, float* out_rgb, uint8_t* out_srgb8, int32_t ref_oetf,
                            float* ave_lw, float* max_lw);
 
+/* salty_tonemap, for callers that must not allocate device memory when they tonemap.
+ * No counterpart in the reference: it exists for hosts such as a real-time viewer that
+ * tonemaps every frame inside its render loop, a CUDA-graph capture (where cudaMalloc is
+ * not allowed), or an engine that owns all GPU memory and forbids allocation after start-up
+ * -- cudaMalloc also synchronises the device, which such loops cannot afford.
+ *   - Arrays are device memory only: d_rgb (W*H*3 float), d_out_rgb and/or d_out_srgb8
+ *     (either may be NULL, not both).  The call allocates nothing and does not wait: it
+ *     enqueues three kernels on `stream` (a cudaStream_t; NULL = the context's stream) and
+ *     returns; synchronise the stream before reading the outputs.
+ *   - Its scratch is a fixed 64 KiB device array inside the library, present on every GPU
+ *     that loads the library until the process exits; images are limited to 16,777,216
+ *     pixels (4096 x 4096).  Larger images return SALTY_ERR_CAPACITY before any launch.
+ *   - The first call on each device looks up that array's device address once (with the
+ *     device current); make that first call before capturing the stream into a graph.
+ *   - Every call reuses the same array and overwrites all of it that it reads, so nothing
+ *     carries over between calls -- but calls that overlap on the GPU (other streams,
+ *     other host threads) race on it: serialise them.
+ * Results equal salty_tonemap's up to the order of the log-luminance sum. */
+salty_status salty_tonemap_noalloc(salty_ctx* ctx, void* stream, int32_t type, int32_t width, int32_t height,
+                                   const float* d_rgb, float* d_out_rgb, uint8_t* d_out_srgb8, int32_t ref_oetf);
+
 /* FilterNLM as the reference defines it: RGBA, 5x5 patch, 13x13 search, h = sigma = coeff. */
 salty_status salty_denoise_nlm_ref(salty_ctx* ctx, int32_t width, int32_t height, float coeff,
                                    const float* rgba, float* out);

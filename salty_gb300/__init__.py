@@ -87,7 +87,8 @@ class RenderStats(C.Structure):
 EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_abi_version", "salty_ctx_cancel",
            "salty_host_alloc", "salty_host_free", "salty_scene_upload", "salty_scene_destroy", "salty_bvh_build",
            "salty_trace", "salty_last_trace_stats", "salty_render", "salty_film_read", "salty_tonemap",
-           "salty_denoise_nlm_ref", "salty_denoise_nlm", "salty_microbench_soup", "salty_microbench_rays"]
+           "salty_denoise_nlm_ref", "salty_denoise_nlm", "salty_microbench_soup", "salty_microbench_rays",
+           "salty_tonemap_noalloc"]
 
 _lib = None
 
@@ -118,6 +119,7 @@ def lib() -> C.CDLL:
         "salty_film_read": (i32, [vp, vp, vp, vp, C.POINTER(i64)]),
         "salty_tonemap": (i32, [vp, i32, i32, i32, vp, vp, vp, i32, C.POINTER(f32), C.POINTER(f32)]),
         "salty_denoise_nlm_ref": (i32, [vp, i32, i32, f32, vp, vp]),
+        "salty_tonemap_noalloc": (i32, [vp, vp, i32, i32, i32, vp, vp, vp, i32]),
         "salty_denoise_nlm": (i32, [vp, i32, i32, i32, i32, f32, vp, vp, vp]),
         "salty_microbench_soup": (i32, [u64, i64, vp]),
         "salty_microbench_rays": (i32, [u64, i64, f32, vp]),

@@ -315,3 +315,172 @@ salty_status nlm_var_device(salty_ctx* ctx, int w, int h, int search_r, int patc
 }
 
 }  // namespace salty
+
+// ---------------------------------------------------------------- no-allocation tonemap
+// salty_tonemap_noalloc: the same tonemap for callers that must not allocate device memory
+// when they tonemap (see include/salty_gpu.h).  Its scratch is the fixed array below,
+// part of the library image, so it exists on every device that loads the library until
+// the process exits.  Layout: kNoAllocPartials partial sums (one per block of
+// kNoAllocPixelsPerBlock pixels), then the tonemap parameters.  Every call overwrites what
+// it reads, so nothing has to be cleared between calls; calls that overlap on the GPU share
+// the array and race.
+namespace salty {
+namespace {
+
+constexpr int kNoAllocPartials = 4096;
+constexpr int kNoAllocPixelsPerBlock = 4096;
+constexpr long long kNoAllocMaxPixels = (long long)kNoAllocPartials * kNoAllocPixelsPerBlock;
+
+struct NoAllocScratch {
+    LumAcc part[kNoAllocPartials];
+    TmParams params;
+    float ave_max[2];
+};
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+// Per-block luminance partials in a fixed pixel-to-block mapping (deterministic).
+__global__ void __launch_bounds__(kRedBlock) k_lum_partials(const float* __restrict__ rgb, long long npx,
+                                                            NoAllocScratch* sc) {
+    const float eps = 0.00001f;
+    const long long b0 = (long long)blockIdx.x * kNoAllocPixelsPerBlock;
+    const long long b1 = min(npx, b0 + kNoAllocPixelsPerBlock);
+    double s = 0.0;
+    float mx = -FLT_MAX;
+    for (long long i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+        float lw = rgb_to_y(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+        if (lw != lw) lw = eps;
+        if (lw < FLT_EPSILON) lw = eps;
+        mx = fmaxf(mx, lw);
+        s += (double)logf(__fadd_rn(eps, lw));
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, off);
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    }
+    __shared__ double ss[kRedBlock / 32];
+    __shared__ float sm[kRedBlock / 32];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { ss[w] = s; sm[w] = mx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        float m = -FLT_MAX;
+        for (int k = 0; k < kRedBlock / 32; ++k) { t += ss[k]; m = fmaxf(m, sm[k]); }
+        sc->part[blockIdx.x].sum = t;
+        sc->part[blockIdx.x].maxo = f2o(m);
+    }
+}
+
+// Reduces the partials in index order and derives the curve parameters on the device, so
+// the three launches need no host round trip.  ComputeLogarithmicAverage and the
+// per-operator constants: src/s3d_tonemapper.cpp:84-94, :246-250, :291-297, :331-335.
+__global__ void __launch_bounds__(kRedBlock) k_lum_finalize(NoAllocScratch* sc, int nparts, long long npx, int type,
+                                                            int ref_oetf) {
+    double s = 0.0;
+    float mx = -FLT_MAX;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+        s += sc->part[i].sum;
+        mx = fmaxf(mx, o2f(sc->part[i].maxo));
+    }
+    __shared__ double ss[kRedBlock];
+    __shared__ float sm[kRedBlock];
+    ss[threadIdx.x] = s;
+    sm[threadIdx.x] = mx;
+    __syncthreads();
+    for (int h = kRedBlock / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            ss[threadIdx.x] += ss[threadIdx.x + h];
+            sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + h]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const float mean = (float)(ss[0] / (double)npx);
+    const float ave = expf(mean);
+    const float max_lw = sm[0];
+    TmParams p;
+    p.type = type;
+    p.ref_oetf = ref_oetf;
+    p.coeff = __fdiv_rn(type == SALTY_TM_ACES ? 0.27f : 0.18f, ave);
+    const float m2 = __fmul_rn(max_lw, p.coeff);
+    p.m2 = __fmul_rn(m2, m2);
+    p.white = u2_curve(11.2f);
+    sc->params = p;
+    sc->ave_max[0] = ave;
+    sc->ave_max[1] = max_lw;
+}
+
+__global__ void k_tonemap_params(const float* __restrict__ in, long long n, const NoAllocScratch* __restrict__ sc,
+                                 float* __restrict__ out, unsigned char* __restrict__ srgb) {
+    const TmParams p = sc->params;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float x = __fmul_rn(in[i], p.coeff);
+        float y;
+        if (p.type == SALTY_TM_ACES) y = aces_curve(x);
+        else if (p.type == SALTY_TM_UNCHARTED2) y = __fdiv_rn(u2_curve(__fmul_rn(2.0f, x)), p.white);
+        else y = __fdiv_rn(__fmul_rn(x, __fadd_rn(1.0f, __fdiv_rn(x, p.m2))), __fadd_rn(1.0f, x));
+        if (out) out[i] = y;
+        if (srgb) srgb[i] = to_srgb8(y, p.ref_oetf);
+    }
+}
+
+// Device address of g_noalloc_scratch per device, looked up once per device with that
+// device current (the array's name is only a host-side stand-in in host code).
+constexpr int kMaxDevices = 64;
+void* g_noalloc_addr[kMaxDevices] = {};
+
+cudaError_t noalloc_scratch(int device, NoAllocScratch** out) {
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    void* p = __atomic_load_n(&g_noalloc_addr[device], __ATOMIC_ACQUIRE);
+    if (!p) {
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        __atomic_store_n(&g_noalloc_addr[device], p, __ATOMIC_RELEASE);
+    }
+    *out = static_cast<NoAllocScratch*>(p);
+    return cudaSuccess;
+}
+
+bool on_device(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+}  // namespace salty
+
+extern "C" salty_status salty_tonemap_noalloc(salty_ctx* ctx, void* stream, int32_t type, int32_t width,
+                                              int32_t height, const float* d_rgb, float* d_out_rgb,
+                                              uint8_t* d_out_srgb8, int32_t ref_oetf) {
+    using namespace salty;
+    if (!ctx) return SALTY_ERR_INVALID_ARG;
+    auto& E = ctx->err;
+    if (width <= 0 || height <= 0) return E.fail(SALTY_ERR_INVALID_ARG, "tonemap_noalloc: bad image size");
+    const long long npx = (long long)width * height;
+    if (npx > kNoAllocMaxPixels)
+        return E.fail(SALTY_ERR_CAPACITY, "tonemap_noalloc: %lld pixels exceed the fixed scratch limit of %lld",
+                      npx, kNoAllocMaxPixels);
+    if (type < SALTY_TM_REINHARD || type > SALTY_TM_ACES) return E.fail(SALTY_ERR_INVALID_ARG, "bad tonemap type");
+    if (!d_out_rgb && !d_out_srgb8) return E.fail(SALTY_ERR_INVALID_ARG, "tonemap_noalloc: no output");
+    SALTY_TRY_CUDA(E, cudaSetDevice(ctx->device));
+    if (!on_device(d_rgb) || (d_out_rgb && !on_device(d_out_rgb)) || (d_out_srgb8 && !on_device(d_out_srgb8)))
+        return E.fail(SALTY_ERR_INVALID_ARG, "tonemap_noalloc: arrays must be device memory");
+    NoAllocScratch* sc = nullptr;
+    SALTY_TRY_CUDA(E, noalloc_scratch(ctx->device, &sc));
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    const int nparts = (int)((npx + kNoAllocPixelsPerBlock - 1) / kNoAllocPixelsPerBlock);
+    k_lum_partials<<<nparts, kRedBlock, 0, st>>>(d_rgb, npx, sc);
+    k_lum_finalize<<<1, kRedBlock, 0, st>>>(sc, nparts, npx, type, ref_oetf);
+    const long long n = npx * 3;
+    long long g = (n + 255) / 256;
+    if (g > (long long)ctx->num_sms * 8) g = (long long)ctx->num_sms * 8;
+    k_tonemap_params<<<(unsigned)g, 256, 0, st>>>(d_rgb, n, sc, d_out_rgb, d_out_srgb8);
+    SALTY_TRY_CUDA(E, cudaGetLastError());
+    return SALTY_OK;
+}
