@@ -99,9 +99,13 @@ typedef struct salty_scene_desc {
      * library adds its two triangles to the scene (indices n_tris, n_tris + 1). */
     int32_t has_light;
     float light_corner[3], light_edge_a[3], light_edge_b[3], light_emission[3];
-    /* Directional (delta) sun: unit direction towards the sun, irradiance. */
+    /* Directional sun: unit direction towards the sun, irradiance on a surface facing it,
+     * and the angular radius of its disk in radians (0: a delta light, reachable only by
+     * next-event estimation; > 0: a uniform disk of that radius, sampled by NEE and hit by
+     * BSDF-sampled rays, the two combined by multiple importance sampling). */
     int32_t has_sun;
     float sun_dir[3], sun_radiance[3];
+    float sun_half_angle;
     float sky[3];              /* constant sky radiance (Scene::SampleIBL) */
     salty_camera camera;
 } salty_scene_desc;
@@ -173,6 +177,11 @@ typedef struct salty_render_opts {
     int32_t fp64;           /* accumulate in double (converged oracle images) */
     int32_t tonemap;        /* SALTY_TM_* for srgb8 output */
     int32_t ref_oetf;       /* 1: the reference's pow(1.055x, 1/2.4) - 0.055 OETF */
+    /* Optional window of the width x height frame (all 0: the whole frame).  Pixels keep
+     * their full-frame rays and random streams, so a window renders exactly the same
+     * samples as the matching pixels of a full render; the film and the outputs are
+     * crop_w x crop_h. */
+    int32_t crop_x, crop_y, crop_w, crop_h;
 } salty_render_opts;
 
 typedef struct salty_render_stats {
@@ -193,6 +202,11 @@ salty_status salty_render(salty_ctx* ctx, salty_scene* scene, const salty_render
  * film was rendered with fp64.  Arrays host or device; NULL skips. */
 salty_status salty_film_read(salty_ctx* ctx, salty_scene* scene, double* sum, double* sumsq,
                              int64_t* samples);
+
+/* Mean first-hit features of the film (the learned denoiser's auxiliary inputs): albedo
+ * (W*H*3), shading normal facing the camera (W*H*3) and 1/(1 + hit distance) (W*H; 0 where
+ * the camera ray escapes).  Arrays host or device; NULL skips. */
+salty_status salty_film_aov(salty_ctx* ctx, salty_scene* scene, float* albedo, float* normal, float* depth);
 
 /* ---------------------------------------------------------------- post */
 /* ToneMapper::Map on a W*H*3 linear image, optionally followed by the sRGB8 conversion.

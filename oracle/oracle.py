@@ -48,7 +48,8 @@ class _Scene(C.Structure):
                 ("has_light", C.c_int), ("light_corner", C.c_float * 3),
                 ("light_edge_a", C.c_float * 3), ("light_edge_b", C.c_float * 3),
                 ("light_emission", C.c_float * 3), ("has_sun", C.c_int),
-                ("sun_dir", C.c_float * 3), ("sun_radiance", C.c_float * 3), ("sky", C.c_float * 3),
+                ("sun_dir", C.c_float * 3), ("sun_radiance", C.c_float * 3), ("sun_half_angle", C.c_float),
+                ("sky", C.c_float * 3),
                 ("cam_pos", C.c_float * 3), ("cam_target", C.c_float * 3), ("cam_up", C.c_float * 3),
                 ("cam_fov", C.c_float), ("cam_near", C.c_float)]
 
@@ -174,6 +175,7 @@ class Oracle:
             s.has_sun = 1
             s.sun_dir = _f3(sc.sun["dir"])
             s.sun_radiance = _f3(sc.sun["radiance"])
+            s.sun_half_angle = float(sc.sun.get("half_angle", 0.0))
         s.sky = _f3(sc.sky)
         cam = sc.camera
         s.cam_pos = _f3(cam["pos"])

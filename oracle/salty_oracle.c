@@ -385,6 +385,10 @@ typedef struct {
     v3 lc, la, lb, ln, le;   /* light corner, edges, unit normal, emission */
     float larea;
     v3 cam_pos, cam_cx, cam_cy, cam_cz;
+    /* sun disk: direction, frame, cos of the angular radius, radiance, 1/solid angle */
+    v3 sun_dir, sun_t, sun_b, sun_L;
+    int sun_disk;
+    float sun_cos_max, sun_pdf;
 } rscene;
 
 /* PinholeCamera::Update (include/s3d_camera.h:63-90) */
@@ -450,6 +454,17 @@ static void rscene_init(rscene* r, const oracle_scene* sc) {
         }
     }
     r->bvh = (obvh*)oracle_bvh_create(r->pos, n);
+    if (sc->has_sun) {
+        r->sun_dir = unit(ld3(sc->sun_dir));
+        r->sun_disk = sc->sun_half_angle > 0.0f;
+        r->sun_cos_max = (float)cos((double)sc->sun_half_angle);
+        double omega = 2.0 * 3.14159265358979323846 * (1.0 - cos((double)sc->sun_half_angle));
+        r->sun_pdf = r->sun_disk ? (float)(1.0 / omega) : 0.0f;
+        r->sun_L = r->sun_disk ? mk((float)(sc->sun_radiance[0] / omega), (float)(sc->sun_radiance[1] / omega),
+                                    (float)(sc->sun_radiance[2] / omega))
+                               : mk(0, 0, 0);
+        tangent_space(r->sun_dir, &r->sun_t, &r->sun_b);
+    }
 }
 
 static void rscene_free(rscene* r) {
@@ -632,6 +647,10 @@ static v3 phys_radiance(const rscene* r, v3 o, v3 d, const oracle_render_opts* o
         ohit h;
         if (!closest(r, o, d, kEps, INFINITY, 1, &h)) {
             L = add(L, mul(W, ld3(sc->sky)));
+            if (sc->has_sun && r->sun_disk && dot(d, r->sun_dir) >= r->sun_cos_max) {
+                float w = prev_delta ? 1.0f : prev_pdf / (prev_pdf + r->sun_pdf);
+                L = add(L, scl(mul(W, r->sun_L), w));
+            }
             break;
         }
         v3 p = add(o, scl(d, h.t));
@@ -675,12 +694,24 @@ static v3 phys_radiance(const rscene* r, v3 o, v3 d, const oracle_render_opts* o
                 }
             }
             if (sc->has_sun) {
-                v3 wi = ld3(sc->sun_dir);
+                v3 wi = r->sun_dir;
+                if (r->sun_disk) {  /* uniform direction in the sun's cone */
+                    float u1 = opcg_f32(rnd), u2 = opcg_f32(rnd);
+                    float ct = 1.0f - u1 * (1.0f - r->sun_cos_max);
+                    float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+                    float ph = k2Pi * u2;
+                    wi = safe_unit(add(add(scl(r->sun_t, st * cosf(ph)), scl(r->sun_b, st * sinf(ph))), scl(wi, ct)));
+                }
                 float cos_s = dot(nsf, wi), cos_g = dot(ngf, wi);
                 if (cos_s > 0.0f && cos_g > 0.0f && !occluded(r, p, wi, kEps, INFINITY)) {
                     float pdf_b;
                     v3 f = phys_eval(m, nsf, wo, wi, &pdf_b);
-                    L = add(L, scl(mul(mul(W, f), ld3(sc->sun_radiance)), cos_s));
+                    if (r->sun_disk) {
+                        float mis = r->sun_pdf / (r->sun_pdf + pdf_b);
+                        L = add(L, scl(mul(mul(W, f), r->sun_L), cos_s * mis / r->sun_pdf));
+                    } else {
+                        L = add(L, scl(mul(mul(W, f), ld3(sc->sun_radiance)), cos_s));
+                    }
                 }
             }
         }

@@ -70,6 +70,7 @@ typedef struct {
     int          has_sun;
     float        sun_dir[3];        /* unit, towards the sun */
     float        sun_radiance[3];   /* irradiance on a surface facing the sun */
+    float        sun_half_angle;    /* radians; 0 = delta light, > 0 = uniform disk with MIS */
     float        sky[3];            /* constant sky radiance */
     float        cam_pos[3], cam_target[3], cam_up[3];
     float        cam_fov, cam_near; /* fov used linearly as in include/s3d_camera.h:85-86 */

@@ -55,7 +55,7 @@ class SceneDesc(C.Structure):
                 ("has_light", C.c_int32), ("light_corner", C.c_float * 3), ("light_edge_a", C.c_float * 3),
                 ("light_edge_b", C.c_float * 3), ("light_emission", C.c_float * 3),
                 ("has_sun", C.c_int32), ("sun_dir", C.c_float * 3), ("sun_radiance", C.c_float * 3),
-                ("sky", C.c_float * 3), ("camera", Camera)]
+                ("sun_half_angle", C.c_float), ("sky", C.c_float * 3), ("camera", Camera)]
 
 
 class BuildOpts(C.Structure):
@@ -76,7 +76,8 @@ class TraceStats(C.Structure):
 class RenderOpts(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
                 ("rr_depth", C.c_int32), ("profile", C.c_int32), ("seed", C.c_uint64), ("accumulate", C.c_int32),
-                ("fp64", C.c_int32), ("tonemap", C.c_int32), ("ref_oetf", C.c_int32)]
+                ("fp64", C.c_int32), ("tonemap", C.c_int32), ("ref_oetf", C.c_int32), ("crop_x", C.c_int32),
+                ("crop_y", C.c_int32), ("crop_w", C.c_int32), ("crop_h", C.c_int32)]
 
 
 class RenderStats(C.Structure):
@@ -88,7 +89,7 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_host_alloc", "salty_host_free", "salty_scene_upload", "salty_scene_destroy", "salty_bvh_build",
            "salty_trace", "salty_last_trace_stats", "salty_render", "salty_film_read", "salty_tonemap",
            "salty_denoise_nlm_ref", "salty_denoise_nlm", "salty_microbench_soup", "salty_microbench_rays",
-           "salty_tonemap_noalloc"]
+           "salty_tonemap_noalloc", "salty_film_aov"]
 
 _lib = None
 
@@ -117,6 +118,7 @@ def lib() -> C.CDLL:
         "salty_last_trace_stats": (i32, [vp, C.POINTER(TraceStats)]),
         "salty_render": (i32, [vp, vp, C.POINTER(RenderOpts), vp, vp, vp, C.POINTER(RenderStats)]),
         "salty_film_read": (i32, [vp, vp, vp, vp, C.POINTER(i64)]),
+        "salty_film_aov": (i32, [vp, vp, vp, vp, vp]),
         "salty_tonemap": (i32, [vp, i32, i32, i32, vp, vp, vp, i32, C.POINTER(f32), C.POINTER(f32)]),
         "salty_denoise_nlm_ref": (i32, [vp, i32, i32, f32, vp, vp]),
         "salty_tonemap_noalloc": (i32, [vp, vp, i32, i32, i32, vp, vp, vp, i32]),
@@ -239,6 +241,7 @@ class Context:
         if sun:
             d.has_sun = 1
             d.sun_dir, d.sun_radiance = _f3(sun["dir"]), _f3(sun["radiance"])
+            d.sun_half_angle = float(sun.get("half_angle", 0.0))
         d.sky = _f3(sky)
         cam = camera or {"pos": (0, 0, -1), "target": (0, 0, 0), "up": (0, 1, 0), "fov": 1.0}
         d.camera.pos, d.camera.target, d.camera.up = _f3(cam["pos"]), _f3(cam["target"]), _f3(cam["up"])
@@ -327,17 +330,32 @@ class Scene:
 
     def render(self, width: int, height: int, spp: int, max_depth: int, rr_depth: int = 3,
                profile: int = PROFILE_PHYSICAL, seed: int = 1, accumulate: bool = False, fp64: bool = False,
-               tonemap: int = TM_REINHARD, ref_oetf: bool = True, want=("mean", "var", "srgb")) -> dict:
+               tonemap: int = TM_REINHARD, ref_oetf: bool = True, want=("mean", "var", "srgb"),
+               crop: tuple | None = None, out: dict | None = None) -> dict:
+        """Adds spp samples per pixel to the film and returns its mean / variance of the mean /
+        tonemapped sRGB8 (host arrays, or the device tensors given in `out`).  crop = (x, y, w, h)
+        renders that window of the width x height frame with the frame's own rays."""
+        cx, cy, cw, ch = crop if crop else (0, 0, 0, 0)
         o = RenderOpts(width, height, spp, max_depth, rr_depth, profile, seed, int(accumulate), int(fp64),
-                       tonemap, int(ref_oetf))
-        mean = np.empty((height, width, 3), np.float32) if "mean" in want else None
-        var = np.empty((height, width, 3), np.float32) if "var" in want else None
-        s8 = np.empty((height, width, 3), np.uint8) if "srgb" in want else None
+                       tonemap, int(ref_oetf), cx, cy, cw, ch)
+        fh, fw = (ch, cw) if crop else (height, width)
+        out = out or {}
+        mean = out.get("mean", np.empty((fh, fw, 3), np.float32) if "mean" in want else None)
+        var = out.get("var", np.empty((fh, fw, 3), np.float32) if "var" in want else None)
+        s8 = out.get("srgb", np.empty((fh, fw, 3), np.uint8) if "srgb" in want else None)
         st = RenderStats()
         self.ctx.check(lib().salty_render(self.ctx.h, self.h, C.byref(o), _ptr(mean), _ptr(var), _ptr(s8),
                                           C.byref(st)), "render")
         return {"mean": mean, "var": var, "srgb": s8, "ms": st.ms, "samples": st.samples, "rays": st.rays,
                 "paths": st.paths}
+
+    def aov(self, width: int, height: int) -> dict:
+        """Mean first-hit features of the film: albedo, normal (H, W, 3), depth = 1/(1+t) (H, W)."""
+        al = np.empty((height, width, 3), np.float32)
+        nr = np.empty((height, width, 3), np.float32)
+        dp = np.empty((height, width), np.float32)
+        self.ctx.check(lib().salty_film_aov(self.ctx.h, self.h, _ptr(al), _ptr(nr), _ptr(dp)), "film_aov")
+        return {"albedo": al, "normal": nr, "depth": dp}
 
     def film(self, width: int, height: int):
         s = np.empty((height, width, 3), np.float64)

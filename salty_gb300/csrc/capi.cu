@@ -254,6 +254,23 @@ salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* d, salty
         k.sun_rad[i] = d->sun_radiance[i];
         k.sky[i] = d->sky[i];
     }
+    if (d->has_sun) {
+        if (!(d->sun_half_angle >= 0.0f) || d->sun_half_angle > 0.5f)
+            return fail(E.fail(SALTY_ERR_INVALID_ARG, "sun_half_angle must be in [0, 0.5] radians"));
+        V3 sd = unit(v3(d->sun_dir));
+        put(k.sun_dir, sd);
+        k.sun_disk = d->sun_half_angle > 0.0f;
+        k.sun_cos_max = std::cos((double)d->sun_half_angle);
+        // solid angle of the cone, in double (1 - cos is tiny for small disks)
+        const double omega = 2.0 * 3.14159265358979323846 * (1.0 - std::cos((double)d->sun_half_angle));
+        k.sun_pdf = k.sun_disk ? (float)(1.0 / omega) : 0.0f;
+        for (int i = 0; i < 3; ++i) k.sun_L[i] = k.sun_disk ? (float)(d->sun_radiance[i] / omega) : 0.0f;
+        // Duff et al. 2017 frame around the sun direction
+        float s = sd.z >= 0.0f ? 1.0f : -1.0f, a = -1.0f / (s + sd.z), b = sd.x * sd.y * a;
+        V3 t{1.0f + s * sd.x * sd.x * a, s * b, -s * sd.x}, bb{b, s + sd.y * sd.y * a, -sd.y};
+        put(k.sun_t, t);
+        put(k.sun_b, bb);
+    }
     // PinholeCamera::Update (include/s3d_camera.h:63-90) minus the aspect, applied per render
     const salty_camera& cam = d->camera;
     for (int i = 0; i < 3; ++i) {
@@ -410,6 +427,10 @@ salty_status salty_render(salty_ctx* ctx, salty_scene* sc, const salty_render_op
     if (o->width <= 0 || o->height <= 0 || o->spp < 0 || o->max_depth < 1)
         return E.fail(SALTY_ERR_INVALID_ARG, "bad render size/spp/depth");
     if ((int64_t)o->width * o->height > (1ll << 28)) return E.fail(SALTY_ERR_CAPACITY, "image too large");
+    const bool cropped = o->crop_w > 0 || o->crop_h > 0 || o->crop_x != 0 || o->crop_y != 0;
+    if (cropped && (o->crop_w <= 0 || o->crop_h <= 0 || o->crop_x < 0 || o->crop_y < 0 ||
+                    (int64_t)o->crop_x + o->crop_w > o->width || (int64_t)o->crop_y + o->crop_h > o->height))
+        return E.fail(SALTY_ERR_INVALID_ARG, "crop window outside the frame");
     if (o->profile != SALTY_PROFILE_COMPAT && o->profile != SALTY_PROFILE_PHYSICAL)
         return E.fail(SALTY_ERR_INVALID_ARG, "bad profile");
     if (!sc->bvh.built) return E.fail(SALTY_ERR_NOT_BUILT, "salty_bvh_build has not been called");
@@ -419,7 +440,7 @@ salty_status salty_render(salty_ctx* ctx, salty_scene* sc, const salty_render_op
     SALTY_TRY(render(ctx, sc, *o, &st));
     if (stats) *stats = st;
     if (!mean_rgb && !var_rgb && !srgb8) return SALTY_OK;
-    const size_t npx = (size_t)o->width * o->height;
+    const size_t npx = cropped ? (size_t)o->crop_w * o->crop_h : (size_t)o->width * o->height;
     const bool dm = !mean_rgb || is_device_ptr(mean_rgb), dv = !var_rgb || is_device_ptr(var_rgb),
                ds = !srgb8 || is_device_ptr(srgb8);
     float *tm = nullptr, *tv = nullptr;

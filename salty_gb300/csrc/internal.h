@@ -118,6 +118,11 @@ struct SceneConsts {
     int light_tri0;      // first light triangle id (n_tris of the input), -1 if none
     int has_sun;
     float sun_dir[3], sun_rad[3];
+    int sun_disk;            // 1: finite disk (sun_cos_max < 1), 0: delta light
+    float sun_cos_max;       // cos of the disk's angular radius
+    float sun_L[3];          // disk radiance = irradiance / solid angle
+    float sun_pdf;           // 1 / solid angle
+    float sun_t[3], sun_b[3];  // tangent frame around sun_dir
     float sky[3];
     float cam_pos[3], cam_cx[3], cam_cy[3], cam_cz[3];
     float cam_fov, cam_near;
@@ -125,11 +130,14 @@ struct SceneConsts {
 };
 
 struct Film {
-    int width = 0, height = 0;
+    int width = 0, height = 0;           // film (window) size
+    int frame_w = 0, frame_h = 0;        // frame the window belongs to
+    int crop_x = 0, crop_y = 0;
     int fp64 = 0;
     int64_t samples = 0;
     DevBuf<float> sum, comp, sumsq;      // FP32 sum with Kahan compensation
     DevBuf<double> sum64, sumsq64;       // FP64 film
+    DevBuf<float> aov;                   // first-hit feature sums, 7 per pixel
 };
 
 struct Bvh {

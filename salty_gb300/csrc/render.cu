@@ -21,8 +21,11 @@
 //     and the reference's triangle test with t in [1e-3, 1e12].
 //   SALTY_PROFILE_PHYSICAL is an unbiased estimator for the same scenes: jittered pixels,
 //     cosine-weighted Lambert, exact-Fresnel dielectric, GGX, balance-heuristic MIS
-//     between BSDF sampling and the one-sided area light, a delta sun, constant sky,
-//     Russian roulette from rr_depth, watertight triangle test, ray epsilon 1e-4.
+//     between BSDF sampling and the one-sided area light, a directional sun (delta, or a
+//     disk sampled by NEE and hit by BSDF rays, combined by MIS), constant sky, Russian
+//     roulette from rr_depth, watertight triangle test, ray epsilon 1e-4.
+// The first bounce of every sample also records the denoiser's features (albedo, shading
+// normal, 1/(1 + distance)), averaged in the film next to the radiance.
 // Random numbers: one PCG stream (include/s3d_math.h:2769-2817 step) per (pixel, sample).
 #include <cfloat>
 #include <cmath>
@@ -116,6 +119,7 @@ struct WaveParams {
     SceneConsts k;
     Camera cam;
     int width, height, spp, max_depth, rr_depth, profile;
+    int crop_x, crop_y, film_w, film_h;   // the film: a film_w x film_h window at (crop_x, crop_y)
     unsigned long long seed;
     long long total_samples;   // width*height*spp
     int capacity;
@@ -129,6 +133,7 @@ struct WaveBuffers {
     float4* srays;     // shadow queue rays (2 per path)
     float4* shits;
     float4* lbuf;      // per wave-local sample: radiance xyz
+    float4* abuf;      // per wave-local sample, first hit: 2 x float4 (albedo, 1/(1+t)) (normal, 0)
     int* counts;       // [0] queue A len, [1] queue B len, [2] shadow len, [3] finished
     long long* wave;   // [0] first global sample of the current wave
     unsigned long long* stats;  // [0] rays traced, [1] paths
@@ -149,11 +154,12 @@ __global__ void k_generate(WaveParams P, WaveBuffers B) {
         atomicAdd(&B.stats[1], (unsigned long long)n);
         atomicAdd(&B.stats[0], (unsigned long long)n);
     }
-    const long long npx = (long long)P.width * P.height;
+    const long long npx = (long long)P.film_w * P.film_h;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const long long g = g0 + i;
-        const long long s = g / npx, p = g % npx;
-        const int px = (int)(p % P.width), py = (int)(p / P.width);
+        const long long s = g / npx, fp = g % npx;
+        const int px = P.crop_x + (int)(fp % P.film_w), py = P.crop_y + (int)(fp / P.film_w);
+        const long long p = (long long)py * P.width + px;  // full-frame pixel: its random stream
         Rng rng = rng_for(P.seed, (unsigned long long)p, (unsigned long long)s);
         float fx, fy;
         if (P.profile == SALTY_PROFILE_COMPAT) {
@@ -178,6 +184,8 @@ __global__ void k_generate(WaveParams P, WaveBuffers B) {
         B.path[0].L[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         B.path[0].meta[i] = make_uint4((unsigned)rng.s, (unsigned)(rng.s >> 32), (unsigned)i, 1u << 16);
         B.lbuf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        B.abuf[2 * i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        B.abuf[2 * i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
@@ -317,11 +325,25 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
                     }
                     if (P.k.has_sun) {
                         V wi = ld3(P.k.sun_dir);
+                        if (P.k.sun_disk) {
+                            // uniform direction in the sun's cone
+                            float u1 = rng.f32(), u2 = rng.f32();
+                            float ct = 1.0f - u1 * (1.0f - P.k.sun_cos_max);
+                            float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+                            float sp, cp;
+                            sincosf(k2Pi * u2, &sp, &cp);
+                            wi = safe_unit(ld3(P.k.sun_t) * (st * cp) + ld3(P.k.sun_b) * (st * sp) + wi * ct);
+                        }
                         float cos_s = dot(s.nsf, wi), cos_g = dot(s.ngf, wi);
                         if (cos_s > 0.0f && cos_g > 0.0f) {
                             float pdf_b;
                             V f = phys_eval(m, s.nsf, wo, wi, pdf_b);
-                            cs = f * ld3(P.k.sun_rad) * cos_s;
+                            if (P.k.sun_disk) {
+                                float mis = P.k.sun_pdf / (P.k.sun_pdf + pdf_b);
+                                cs = f * ld3(P.k.sun_L) * (cos_s * mis / P.k.sun_pdf);
+                            } else {
+                                cs = f * ld3(P.k.sun_rad) * cos_s;
+                            }
                             want_s = true;
                             ray_s0 = make_float4(s.p.x, s.p.y, s.p.z, kEps);
                             ray_s1 = make_float4(wi.x, wi.y, wi.z, INFINITY);
@@ -383,8 +405,27 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                 const int sid = __float_as_int(B.shits[q1].y);
                 if (sid < 0) L = L + W * xyz(e1);
             }
+            if (depth == 0 && id >= 0) {
+                // first-hit features of the sample (denoiser inputs): albedo, 1/(1+t),
+                // shading normal facing the camera
+                const GpuMaterial am = P.mats[P.mat[id]];
+                const float* np = P.nrm + (size_t)id * 9;
+                const float al = 1.0f - h.z - h.w;
+                V n = safe_unit(mk(np[0] * al + np[3] * h.z + np[6] * h.w, np[1] * al + np[4] * h.z + np[7] * h.w,
+                                   np[2] * al + np[5] * h.z + np[8] * h.w));
+                if (dot(n, d) > 0.0f) n = -n;
+                const bool emitter = is_light(P, id);
+                B.abuf[2 * mt.z] = make_float4(emitter ? 1.0f : am.color[0], emitter ? 1.0f : am.color[1],
+                                               emitter ? 1.0f : am.color[2], 1.0f / (1.0f + h.x));
+                B.abuf[2 * mt.z + 1] = make_float4(n.x, n.y, n.z, 0.0f);
+            }
             if (id < 0) {
                 L = L + W * ld3(P.k.sky);
+                // an escaping ray inside the sun's disk (physical profile, finite sun)
+                if (!compat && P.k.has_sun && P.k.sun_disk && dot(d, ld3(P.k.sun_dir)) >= P.k.sun_cos_max) {
+                    const float w = prev_delta ? 1.0f : prev_pdf / (prev_pdf + P.k.sun_pdf);
+                    L = L + W * ld3(P.k.sun_L) * w;
+                }
             } else if (compat) {
                 const GpuMaterial m = P.mats[P.mat[id]];
                 V pos = mk(__fadd_rn(o.x, __fmul_rn(d.x, h.x)), __fadd_rn(o.y, __fmul_rn(d.y, h.x)),
@@ -555,9 +596,10 @@ __global__ void k_reset_queue(WaveBuffers B, int q) {
 
 // Adds the wave's samples to the film: one thread per pixel, samples in index order.
 __global__ void k_accumulate(WaveParams P, WaveBuffers B, float* __restrict__ sum, float* __restrict__ comp,
-                             float* __restrict__ sumsq, double* __restrict__ sum64, double* __restrict__ sumsq64) {
+                             float* __restrict__ sumsq, double* __restrict__ sum64, double* __restrict__ sumsq64,
+                             float* __restrict__ aov) {
     const long long g0 = B.wave[0];
-    const long long npx = (long long)P.width * P.height;
+    const long long npx = (long long)P.film_w * P.film_h;
     const long long remain = P.total_samples - g0;
     const long long n = remain < P.capacity ? remain : P.capacity;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
@@ -594,10 +636,32 @@ __global__ void k_accumulate(WaveParams P, WaveBuffers B, float* __restrict__ su
             }
             for (int k = 0; k < 3; ++k) { sum[3 * p + k] = a[k]; comp[3 * p + k] = c[k]; sumsq[3 * p + k] = q2[k]; }
         }
+        // first-hit features: albedo (3), normal (3), 1/(1+t) (1)
+        float f[7];
+        for (int k = 0; k < 7; ++k) f[k] = aov[7 * p + k];
+        for (long long s = s_lo; s <= s_hi; ++s) {
+            const float4 a0 = B.abuf[2 * (s * npx + p - g0)], a1 = B.abuf[2 * (s * npx + p - g0) + 1];
+            f[0] += a0.x; f[1] += a0.y; f[2] += a0.z; f[6] += a0.w;
+            f[3] += a1.x; f[4] += a1.y; f[5] += a1.z;
+        }
+        for (int k = 0; k < 7; ++k) aov[7 * p + k] = f[k];
     }
 }
 
 __global__ void k_next_wave(WaveParams P, WaveBuffers B) { B.wave[0] += P.capacity; }
+
+// Mean first-hit features of the film: albedo W*H*3, normal W*H*3, 1/(1+t) W*H.
+__global__ void k_aov_out(const float* __restrict__ aov, long long npx, double count, float* albedo, float* normal,
+                          float* depth) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
+        const float inv = count > 0 ? (float)(1.0 / count) : 0.0f;
+        for (int k = 0; k < 3; ++k) {
+            if (albedo) albedo[3 * p + k] = aov[7 * p + k] * inv;
+            if (normal) normal[3 * p + k] = aov[7 * p + 3 + k] * inv;
+        }
+        if (depth) depth[p] = aov[7 * p + 6] * inv;
+    }
+}
 
 __global__ void k_film_out(const float* sum, const float* sumsq, const double* sum64, const double* sumsq64,
                            long long n, double count, float* mean, float* var) {
@@ -614,7 +678,7 @@ __global__ void k_film_out(const float* sum, const float* sumsq, const double* s
 }
 
 struct WaveStore {
-    DevBuf<float4> rays[2], W[2], L[2], hits, nee, srays, shits, lbuf;
+    DevBuf<float4> rays[2], W[2], L[2], hits, nee, srays, shits, lbuf, abuf;
     DevBuf<uint4> meta[2];
     DevBuf<int> counts;
     DevBuf<long long> wave;
@@ -627,13 +691,23 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
     auto& E = ctx->err;
     cudaStream_t st = ctx->stream;
     Film& F = sc->film;
-    const long long npx = (long long)o.width * o.height;
-    const bool fresh = !o.accumulate || F.width != o.width || F.height != o.height || F.fp64 != o.fp64;
+    const bool cropped = o.crop_w > 0 && o.crop_h > 0;
+    const int fw = cropped ? o.crop_w : o.width, fh = cropped ? o.crop_h : o.height;
+    const int cx = cropped ? o.crop_x : 0, cy = cropped ? o.crop_y : 0;
+    const long long npx = (long long)fw * fh;
+    const bool fresh = !o.accumulate || F.width != fw || F.height != fh || F.fp64 != o.fp64 || F.frame_w != o.width ||
+                       F.frame_h != o.height || F.crop_x != cx || F.crop_y != cy;
     if (fresh) {
-        F.width = o.width;
-        F.height = o.height;
+        F.width = fw;
+        F.height = fh;
+        F.frame_w = o.width;
+        F.frame_h = o.height;
+        F.crop_x = cx;
+        F.crop_y = cy;
         F.fp64 = o.fp64;
         F.samples = 0;
+        SALTY_TRY_CUDA(E, F.aov.ensure(npx * 7));
+        SALTY_TRY_CUDA(E, cudaMemsetAsync(F.aov.p, 0, npx * 7 * sizeof(float), st));
         if (o.fp64) {
             SALTY_TRY_CUDA(E, F.sum64.ensure(npx * 3));
             SALTY_TRY_CUDA(E, F.sumsq64.ensure(npx * 3));
@@ -666,6 +740,7 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
     SALTY_TRY_CUDA(E, S.srays.ensure(cap * 4));
     SALTY_TRY_CUDA(E, S.shits.ensure(cap * 2));
     SALTY_TRY_CUDA(E, S.lbuf.ensure(cap));
+    SALTY_TRY_CUDA(E, S.abuf.ensure(cap * 2));
     SALTY_TRY_CUDA(E, S.counts.ensure(8));
     SALTY_TRY_CUDA(E, S.wave.ensure(1));
     SALTY_TRY_CUDA(E, S.stats.ensure(4));
@@ -712,6 +787,10 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
     }
     P.width = o.width;
     P.height = o.height;
+    P.crop_x = cx;
+    P.crop_y = cy;
+    P.film_w = fw;
+    P.film_h = fh;
     P.spp = o.spp;
     P.max_depth = o.max_depth;
     P.rr_depth = o.rr_depth;
@@ -730,6 +809,7 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
     B.srays = S.srays.p;
     B.shits = S.shits.p;
     B.lbuf = S.lbuf.p;
+    B.abuf = S.abuf.p;
     B.counts = S.counts.p;
     B.wave = S.wave.p;
     B.stats = S.stats.p;
@@ -765,7 +845,7 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
         if (cap_status != SALTY_OK) break;
         k_accumulate<<<sgrid, 256, 0, st>>>(P, B, o.fp64 ? nullptr : F.sum.p, o.fp64 ? nullptr : F.comp.p,
                                             o.fp64 ? nullptr : F.sumsq.p, o.fp64 ? F.sum64.p : nullptr,
-                                            o.fp64 ? F.sumsq64.p : nullptr);
+                                            o.fp64 ? F.sumsq64.p : nullptr, F.aov.p);
         k_next_wave<<<1, 1, 0, st>>>(P, B);
     } while (0);
     cudaError_t ce = cudaStreamEndCapture(st, &graph);
@@ -859,5 +939,35 @@ extern "C" salty_status salty_film_read(salty_ctx* ctx, salty_scene* sc, double*
     };
     SALTY_TRY(fetch(sum, F.fp64 ? F.sum64.p : nullptr, F.sum.p));
     SALTY_TRY(fetch(sumsq, F.fp64 ? F.sumsq64.p : nullptr, F.sumsq.p));
+    return SALTY_OK;
+}
+
+extern "C" salty_status salty_film_aov(salty_ctx* ctx, salty_scene* sc, float* albedo, float* normal, float* depth) {
+    using namespace salty;
+    if (!ctx) return SALTY_ERR_INVALID_ARG;
+    if (!sc) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "null scene");
+    Film& F = sc->film;
+    const long long npx = (long long)F.width * F.height;
+    if (npx == 0 || !F.aov.p) return ctx->err.fail(SALTY_ERR_NOT_BUILT, "the film is empty");
+    cudaSetDevice(ctx->device);
+    auto& E = ctx->err;
+    float* outs[3] = {albedo, normal, depth};
+    const long long sizes[3] = {npx * 3, npx * 3, npx};
+    DevBuf<float> tmp[3];
+    float* dev[3];
+    for (int i = 0; i < 3; ++i) {
+        dev[i] = outs[i];
+        if (outs[i] && !is_device_ptr(outs[i])) {
+            SALTY_TRY_CUDA(E, tmp[i].ensure(sizes[i]));
+            dev[i] = tmp[i].p;
+        }
+    }
+    k_aov_out<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(F.aov.p, npx, (double)F.samples, dev[0], dev[1], dev[2]);
+    SALTY_TRY_CUDA(E, cudaGetLastError());
+    for (int i = 0; i < 3; ++i)
+        if (outs[i] && dev[i] != outs[i])
+            SALTY_TRY_CUDA(E, cudaMemcpyAsync(outs[i], dev[i], sizes[i] * sizeof(float), cudaMemcpyDeviceToHost,
+                                              ctx->stream));
+    SALTY_TRY_CUDA(E, cudaStreamSynchronize(ctx->stream));
     return SALTY_OK;
 }

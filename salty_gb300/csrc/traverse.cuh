@@ -117,13 +117,18 @@ __device__ __forceinline__ bool tri_ref(const TravRay& r, float4 a, float4 b, fl
 // shared by two triangles gets the same edge function with opposite sign in both.
 __device__ __forceinline__ bool tri_watertight(const TravRay& r, float4 a, float4 b, float4 c, float tmin,
                                                float tmax, float& t, float& u, float& v) {
-    const float o[3] = {r.ox, r.oy, r.oz};
-    const float A[3] = {__fsub_rn(a.x, o[0]), __fsub_rn(a.y, o[1]), __fsub_rn(a.z, o[2])};
-    const float B[3] = {__fsub_rn(b.x, o[0]), __fsub_rn(b.y, o[1]), __fsub_rn(b.z, o[2])};
-    const float C[3] = {__fsub_rn(c.x, o[0]), __fsub_rn(c.y, o[1]), __fsub_rn(c.z, o[2])};
-    const float Ax = __fsub_rn(A[r.kx], __fmul_rn(r.Sx, A[r.kz])), Ay = __fsub_rn(A[r.ky], __fmul_rn(r.Sy, A[r.kz]));
-    const float Bx = __fsub_rn(B[r.kx], __fmul_rn(r.Sx, B[r.kz])), By = __fsub_rn(B[r.ky], __fmul_rn(r.Sy, B[r.kz]));
-    const float Cx = __fsub_rn(C[r.kx], __fmul_rn(r.Sx, C[r.kz])), Cy = __fsub_rn(C[r.ky], __fmul_rn(r.Sy, C[r.kz]));
+    // vertices relative to the origin, components permuted to (kx, ky, kz) with selects
+    // (no dynamically indexed arrays, which would live in local memory)
+    auto pick = [](float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); };
+    const float a0 = __fsub_rn(a.x, r.ox), a1 = __fsub_rn(a.y, r.oy), a2 = __fsub_rn(a.z, r.oz);
+    const float b0 = __fsub_rn(b.x, r.ox), b1 = __fsub_rn(b.y, r.oy), b2 = __fsub_rn(b.z, r.oz);
+    const float c0 = __fsub_rn(c.x, r.ox), c1 = __fsub_rn(c.y, r.oy), c2 = __fsub_rn(c.z, r.oz);
+    const float aX = pick(a0, a1, a2, r.kx), aY = pick(a0, a1, a2, r.ky), aZ = pick(a0, a1, a2, r.kz);
+    const float bX = pick(b0, b1, b2, r.kx), bY = pick(b0, b1, b2, r.ky), bZ = pick(b0, b1, b2, r.kz);
+    const float cX = pick(c0, c1, c2, r.kx), cY = pick(c0, c1, c2, r.ky), cZ = pick(c0, c1, c2, r.kz);
+    const float Ax = __fsub_rn(aX, __fmul_rn(r.Sx, aZ)), Ay = __fsub_rn(aY, __fmul_rn(r.Sy, aZ));
+    const float Bx = __fsub_rn(bX, __fmul_rn(r.Sx, bZ)), By = __fsub_rn(bY, __fmul_rn(r.Sy, bZ));
+    const float Cx = __fsub_rn(cX, __fmul_rn(r.Sx, cZ)), Cy = __fsub_rn(cY, __fmul_rn(r.Sy, cZ));
     float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
     float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
     float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
@@ -135,7 +140,7 @@ __device__ __forceinline__ bool tri_watertight(const TravRay& r, float4 a, float
     if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
     const float det = __fadd_rn(__fadd_rn(U, V), W);
     if (det == 0.0f) return false;
-    const float Az = __fmul_rn(r.Sz, A[r.kz]), Bz = __fmul_rn(r.Sz, B[r.kz]), Cz = __fmul_rn(r.Sz, C[r.kz]);
+    const float Az = __fmul_rn(r.Sz, aZ), Bz = __fmul_rn(r.Sz, bZ), Cz = __fmul_rn(r.Sz, cZ);
     const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
     if (det > 0.0f) {
         if (T < __fmul_rn(tmin, det) || T > __fmul_rn(tmax, det)) return false;

@@ -97,6 +97,123 @@ def soup(n: int, seed: int = 20260001) -> dict:
             "camera": {"pos": (0.5, 0.5, -1.5), "target": (0.5, 0.5, 0.5), "up": (0, 1, 0), "fov": 1.0}}
 
 
+def value_noise(n: int, octaves: int, seed: int, base: int = 4) -> np.ndarray:
+    """n x n samples over [0,1]^2 of seeded value noise: sum over octaves k of 0.5^k times a
+    smoothstep-interpolated random lattice with base * 2^k cells per side, normalised to [0,1]."""
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0.0, 1.0, n)
+    h = np.zeros((n, n))
+    amp_sum = 0.0
+    for k in range(octaves):
+        f = base * 2 ** k
+        lat = rng.random((f + 1, f + 1))
+        g = x * f
+        i0 = np.minimum(np.floor(g).astype(np.int64), f - 1)
+        t = g - i0
+        s = t * t * (3.0 - 2.0 * t)
+        a = lat[np.ix_(i0, i0)]
+        b = lat[np.ix_(i0, i0 + 1)]
+        c = lat[np.ix_(i0 + 1, i0)]
+        d = lat[np.ix_(i0 + 1, i0 + 1)]
+        sy, sx = s[:, None], s[None, :]
+        h += (0.5 ** k) * ((a * (1 - sx) + b * sx) * (1 - sy) + (c * (1 - sx) + d * sx) * sy)
+        amp_sum += 0.5 ** k
+    return h / amp_sum
+
+
+def _icosphere(subdiv: int) -> np.ndarray:
+    """Unit icosphere triangles (20 * 4^subdiv, 3, 3), outward winding."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+         (8, 6, 7), (9, 8, 1)]
+    tris = np.array([[v[a], v[b], v[c]] for a, b, c in f], np.float64)
+    tris /= np.linalg.norm(tris, axis=2, keepdims=True)
+    for _ in range(subdiv):
+        a, b, c = tris[:, 0], tris[:, 1], tris[:, 2]
+        ab, bc, ca = a + b, b + c, c + a
+        ab /= np.linalg.norm(ab, axis=1, keepdims=True)
+        bc /= np.linalg.norm(bc, axis=1, keepdims=True)
+        ca /= np.linalg.norm(ca, axis=1, keepdims=True)
+        tris = np.concatenate([np.stack([a, ab, ca], 1), np.stack([ab, b, bc], 1), np.stack([ca, bc, c], 1),
+                               np.stack([ab, bc, ca], 1)])
+    n = np.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0])
+    flip = np.einsum("ij,ij->i", n, tris.sum(1)) < 0
+    tris[flip] = tris[flip][:, ::-1]
+    return tris
+
+
+def heightfield(grid: int = 2048, n_spheres: int = 4096, seed: int = 2026, height: float = 0.15,
+                subdiv: int = 3, sun_half_angle: float = math.radians(4.0)) -> dict:
+    """The 1080p heightfield scene: a grid x grid terrain (2 grid^2 triangles) over [0,1]^2
+    with 6-octave value-noise heights (amplitude 0.5^k), n_spheres icospheres (20 * 4^subdiv
+    triangles each) with radii log-uniform in [0.005, 0.05] above it; sphere materials 60%
+    Lambert (albedo U[0.1,0.9]), 20% mirror, 10% dielectric (IOR 1.5), 10% GGX (roughness
+    U[0.05,0.5]); constant sky 1.0 and a directional sun whose disk has a 4 degree angular
+    radius (sampled together with the BSDF by MIS; a delta sun makes the glints of the
+    low-roughness GGX spheres unbounded fireflies)."""
+    rng = np.random.default_rng(seed)
+    n = grid + 1
+    h = value_noise(n, 6, seed) * height
+    xs = np.linspace(0.0, 1.0, n)
+    X, Z = np.meshgrid(xs, xs)
+    P = np.stack([X, h, Z], -1).astype(np.float32)          # [row(z), col(x), 3]
+    dhdx = np.gradient(h, xs, axis=1)
+    dhdz = np.gradient(h, xs, axis=0)
+    N = np.stack([-dhdx, np.ones_like(h), -dhdz], -1)
+    N = (N / np.linalg.norm(N, axis=-1, keepdims=True)).astype(np.float32)
+    a, b = P[:-1, :-1], P[:-1, 1:]        # (i,j), (i,j+1)
+    c, d = P[1:, 1:], P[1:, :-1]          # (i+1,j+1), (i+1,j)
+    na, nb, nc, nd = N[:-1, :-1], N[:-1, 1:], N[1:, 1:], N[1:, :-1]
+    t_pos = np.stack([np.stack([a, d, c], 2), np.stack([a, c, b], 2)], 2).reshape(-1, 9)
+    t_nrm = np.stack([np.stack([na, nd, nc], 2), np.stack([na, nc, nb], 2)], 2).reshape(-1, 9)
+    t_mat = np.zeros(t_pos.shape[0], np.int32)
+
+    mats = [{"type": LAMBERT, "color": (0.45, 0.40, 0.33)}]
+    unit = _icosphere(subdiv).astype(np.float32)             # (m, 3, 3)
+    m = unit.shape[0]
+    cx = rng.uniform(0.05, 0.95, n_spheres)
+    cz = rng.uniform(0.05, 0.95, n_spheres)
+    r = np.exp(rng.uniform(np.log(0.005), np.log(0.05), n_spheres))
+    # terrain height under each centre (bilinear on the grid)
+    gx, gz = cx * grid, cz * grid
+    i0, j0 = np.minimum(gz.astype(int), grid - 1), np.minimum(gx.astype(int), grid - 1)
+    fz, fx = gz - i0, gx - j0
+    ground = (h[i0, j0] * (1 - fx) * (1 - fz) + h[i0, j0 + 1] * fx * (1 - fz) + h[i0 + 1, j0] * (1 - fx) * fz
+              + h[i0 + 1, j0 + 1] * fx * fz)
+    cy = ground + r * (1.0 + rng.uniform(0.0, 1.0, n_spheres))
+    kind = rng.random(n_spheres)
+    s_mat = np.empty(n_spheres, np.int32)
+    for i in range(n_spheres):
+        if kind[i] < 0.6:
+            mats.append({"type": LAMBERT, "color": tuple(rng.uniform(0.1, 0.9, 3))})
+        elif kind[i] < 0.8:
+            mats.append({"type": MIRROR, "color": (0.9, 0.9, 0.9)})
+        elif kind[i] < 0.9:
+            mats.append({"type": GLASS, "color": (1.0, 1.0, 1.0), "ior": 1.5})
+        else:
+            mats.append({"type": GGX, "color": tuple(rng.uniform(0.5, 0.95, 3)), "roughness": rng.uniform(0.05, 0.5)})
+        s_mat[i] = len(mats) - 1
+    centers = np.stack([cx, cy, cz], -1).astype(np.float32)
+    s_pos = (centers[:, None, None, :] + r.astype(np.float32)[:, None, None, None] * unit[None]).reshape(-1, 9)
+    s_nrm = np.broadcast_to(unit[None], (n_spheres, m, 3, 3)).reshape(-1, 9)
+    pos = np.concatenate([t_pos, s_pos]).astype(np.float32)
+    nrm = np.concatenate([t_nrm, s_nrm]).astype(np.float32)
+    mat = np.concatenate([t_mat, np.repeat(s_mat, m)]).astype(np.int32)
+    sun = np.array([-0.4, 0.75, -0.55])
+    sun /= np.linalg.norm(sun)
+    return {
+        "name": f"heightfield-{grid}-{n_spheres}",
+        "tri_pos": pos, "tri_nrm": nrm, "tri_mat": mat, "materials": mats, "light": None,
+        "sun": {"dir": tuple(sun), "radiance": (3.0, 2.9, 2.7), "half_angle": sun_half_angle},
+        "sky": (1.0, 1.0, 1.0),
+        "camera": {"pos": (0.5, 0.42, -0.3), "target": (0.5, 0.05, 0.6), "up": (0.0, 1.0, 0.0),
+                   "fov": 2.0 * math.tan(math.radians(25.0)), "near": 1.0},
+    }
+
+
 def upload(ctx, scene: dict):
     """Context.upload_scene with a scene dict from this module."""
     kw = {k: v for k, v in scene.items() if k != "name"}

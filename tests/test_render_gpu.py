@@ -64,6 +64,54 @@ def test_physical_cornell_matches_oracle(ctx, oracle, variant):
     assert r["rays"] > W * H * spp  # primary + extension + shadow rays
 
 
+@pytest.mark.parametrize("half_angle", [0.0, 0.07])
+def test_sun_sky_heightfield_matches_oracle(ctx, oracle, half_angle):
+    """Sky + sun (delta, and a disk combined with BSDF sampling by MIS) over a small
+    heightfield with spheres of every material."""
+    import salty_gb300
+    from oracle.oracle import PROFILE_PHYSICAL
+    from salty_gb300 import scenes
+    sc = scenes.heightfield(grid=48, n_spheres=24, seed=7, subdiv=2, sun_half_angle=half_angle)
+    W, H, spp = 40, 24, 256
+    s = _gpu_scene(ctx, sc)
+    r = s.render(W, H, spp, 6, rr_depth=3, profile=salty_gb300.PROFILE_PHYSICAL, seed=21)
+    tot, sq = oracle.render(_oracle_scene(sc), W, H, spp, 6, rr_depth=3, profile=PROFILE_PHYSICAL, seed=22)
+    m = tot / spp
+    v = np.maximum((sq / spp - m * m) * spp / (spp - 1) / spp, 0)
+    frac, zmax = zstats(r["mean"], r["var"], m, v)
+    assert frac < 0.015 and zmax < 6, (frac, zmax)
+
+
+def test_crop_window_renders_the_same_samples(ctx):
+    """A window keeps its pixels' full-frame rays and random streams: identical values."""
+    import salty_gb300
+    from salty_gb300 import scenes
+    s = _gpu_scene(ctx, scenes.cornell("mixed"))
+    full = s.render(64, 48, 8, 8, seed=13, want=("mean",))["mean"]
+    win = s.render(64, 48, 8, 8, seed=13, want=("mean",), crop=(10, 7, 30, 20))["mean"]
+    assert win.shape == (20, 30, 3)
+    np.testing.assert_array_equal(win, full[7:27, 10:40])
+
+
+def test_first_hit_features(ctx):
+    """Albedo, normal and 1/(1+t) of the first hit, averaged over the pixel's samples."""
+    from salty_gb300 import scenes
+    s = _gpu_scene(ctx, scenes.cornell("baseline"))
+    s.render(64, 64, 16, 8, seed=1, want=())
+    f = s.aov(64, 64)
+    # a pixel well inside the back wall (grey Lambert 0.75, normal -z, t from z=-1.4 to 1)
+    al, nr, dp = f["albedo"][20, 32], f["normal"][20, 32], f["depth"][20, 32]
+    np.testing.assert_allclose(al, 0.75, rtol=1e-5)
+    np.testing.assert_allclose(nr, (0, 0, -1), atol=1e-5)
+    assert 1.0 / (1.0 + 2.6) < dp < 1.0 / (1.0 + 2.3)
+    # pixels whose samples all escaped past the open front of the box: every feature 0
+    esc = f["depth"] == 0
+    assert esc.any()
+    assert np.all(f["albedo"][esc] == 0) and np.all(f["normal"][esc] == 0)
+    n = np.linalg.norm(f["normal"].reshape(-1, 3), axis=1)
+    assert np.all(n <= 1.0 + 1e-5)
+
+
 def test_same_streams_as_oracle_give_nearly_identical_images(ctx, oracle):
     """Same seed => same per-(pixel, sample) PCG streams: most samples follow the same path,
     so the images agree far inside the Monte Carlo bound."""
