@@ -246,6 +246,36 @@ salty_status salty_denoise_nlm(salty_ctx* ctx, int32_t width, int32_t height, in
                                int32_t patch_r, float k, const float* rgb, const float* var,
                                float* out);
 
+/* ---------------------------------------------------------------- learned denoiser
+ * No reference counterpart: the reference's only denoiser is FilterNLM
+ * (src/s3d_denoiser.cpp:19-95).  A 5-level U-Net (3x3 convolutions, 16->32->48->64->80->96
+ * channels, skip connections, about 566k parameters) whose convolutions run as implicit
+ * GEMMs on the tensor cores in BF16 with FP32 accumulation, trained with Adam on an L1
+ * loss in log(1 + colour) space.
+ *
+ * Features: n images of h x w pixels, 10 floats per pixel in this order: colour (the noisy
+ * mean, linear), first-hit albedo (3), first-hit normal (3), 1/(1 + first-hit distance)
+ * -- salty_film_read's mean followed by salty_film_aov's three planes.  h and w must be
+ * multiples of 16 and n*h*w at most 2^26.  Arrays are host or device. */
+typedef struct salty_unet salty_unet;
+
+/* He-uniform initial weights from `seed`, zero biases. */
+salty_status salty_unet_create(salty_ctx* ctx, uint64_t seed, salty_unet** out);
+void salty_unet_destroy(salty_ctx* ctx, salty_unet* net);
+/* Number of FP32 parameters: per layer, weights [9][cout][cin] then biases [cout]. */
+int64_t salty_unet_param_count(const salty_unet* net);
+/* Copies the FP32 parameters and/or the gradients of the last train step (either may be NULL). */
+salty_status salty_unet_get_params(salty_ctx* ctx, salty_unet* net, float* params, float* grads);
+salty_status salty_unet_set_params(salty_ctx* ctx, salty_unet* net, const float* params);
+/* Denoised linear RGB, n*h*w*3 floats. */
+salty_status salty_unet_forward(salty_ctx* ctx, salty_unet* net, const float* features, int32_t n, int32_t h,
+                                int32_t w, float* out_rgb);
+/* One step on a batch: forward, loss against target_rgb (n*h*w*3 linear), gradients, and,
+ * when lr > 0, an Adam update (beta 0.9, 0.999, eps 1e-8).  With lr == 0 only the loss and
+ * the gradients are computed.  *loss (may be NULL) = mean |out - log(1 + target)|. */
+salty_status salty_unet_train_step(salty_ctx* ctx, salty_unet* net, const float* features, const float* target_rgb,
+                                   int32_t n, int32_t h, int32_t w, float lr, float* loss);
+
 /* ---------------------------------------------------------------- inputs */
 /* The traversal microbenchmark's seeded inputs (host arrays): a triangle soup with
  * centroids uniform in [0,1]^3 and vertices within +-0.005, and rays from a radius-2

@@ -89,7 +89,9 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_host_alloc", "salty_host_free", "salty_scene_upload", "salty_scene_destroy", "salty_bvh_build",
            "salty_trace", "salty_last_trace_stats", "salty_render", "salty_film_read", "salty_tonemap",
            "salty_denoise_nlm_ref", "salty_denoise_nlm", "salty_microbench_soup", "salty_microbench_rays",
-           "salty_tonemap_noalloc", "salty_film_aov"]
+           "salty_tonemap_noalloc", "salty_film_aov", "salty_unet_create", "salty_unet_destroy",
+           "salty_unet_param_count", "salty_unet_get_params", "salty_unet_set_params", "salty_unet_forward",
+           "salty_unet_train_step"]
 
 _lib = None
 
@@ -125,6 +127,13 @@ def lib() -> C.CDLL:
         "salty_denoise_nlm": (i32, [vp, i32, i32, i32, i32, f32, vp, vp, vp]),
         "salty_microbench_soup": (i32, [u64, i64, vp]),
         "salty_microbench_rays": (i32, [u64, i64, f32, vp]),
+        "salty_unet_create": (i32, [vp, u64, C.POINTER(vp)]),
+        "salty_unet_destroy": (None, [vp, vp]),
+        "salty_unet_param_count": (i64, [vp]),
+        "salty_unet_get_params": (i32, [vp, vp, vp, vp]),
+        "salty_unet_set_params": (i32, [vp, vp, vp]),
+        "salty_unet_forward": (i32, [vp, vp, vp, i32, i32, i32, vp]),
+        "salty_unet_train_step": (i32, [vp, vp, vp, vp, i32, i32, i32, f32, C.POINTER(f32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -363,3 +372,82 @@ class Scene:
         n = C.c_int64()
         self.ctx.check(lib().salty_film_read(self.ctx.h, self.h, _ptr(s), _ptr(q), C.byref(n)), "film_read")
         return s, q, n.value
+
+
+# The learned denoiser's layers (cin, cout, relu) in parameter order; every layer is a 3x3
+# convolution with weights [9][cout][cin] followed by biases [cout].
+UNET_LAYERS = [(16, 32, 1), (32, 32, 1), (32, 48, 1), (48, 48, 1), (48, 64, 1), (64, 64, 1), (64, 80, 1),
+               (80, 80, 1), (80, 96, 1), (176, 80, 1), (144, 64, 1), (112, 48, 1), (80, 32, 1), (32, 8, 0)]
+
+
+def unet_features(mean, aov: dict) -> np.ndarray:
+    """(H, W, 10) denoiser input: noisy colour, first-hit albedo, normal, 1/(1 + distance)."""
+    return np.concatenate([np.asarray(mean, np.float32), aov["albedo"], aov["normal"],
+                           aov["depth"][..., None]], axis=-1).astype(np.float32)
+
+
+class Unet:
+    """The learned denoiser (salty_unet): BF16 tensor-core convolutions, FP32 master weights."""
+
+    def __init__(self, ctx: Context, seed: int = 1):
+        self.ctx = ctx
+        h = C.c_void_p()
+        ctx.check(lib().salty_unet_create(ctx.h, seed, C.byref(h)), "unet_create")
+        self.h = h
+        self.n_params = int(lib().salty_unet_param_count(h))
+
+    def close(self) -> None:
+        if getattr(self, "h", None) and self.ctx.h:
+            lib().salty_unet_destroy(self.ctx.h, self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        p = np.empty(self.n_params, np.float32)
+        self.ctx.check(lib().salty_unet_get_params(self.ctx.h, self.h, _ptr(p), None), "unet_get_params")
+        return p
+
+    def grads(self) -> np.ndarray:
+        g = np.empty(self.n_params, np.float32)
+        self.ctx.check(lib().salty_unet_get_params(self.ctx.h, self.h, None, _ptr(g)), "unet_get_params")
+        return g
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        if p.size != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters, got {p.size}")
+        self.ctx.check(lib().salty_unet_set_params(self.ctx.h, self.h, _ptr(p)), "unet_set_params")
+
+    @staticmethod
+    def _batch(a, ch):
+        if not hasattr(a, "data_ptr"):
+            a = np.ascontiguousarray(a, np.float32)
+        if a.ndim == 3:
+            a = a[None]
+        if a.ndim != 4 or a.shape[-1] != ch:
+            raise ValueError(f"expected (N, H, W, {ch}) or (H, W, {ch}), got {tuple(a.shape)}")
+        return a
+
+    def forward(self, features, out=None):
+        f = self._batch(features, 10)
+        n, h, w = f.shape[:3]
+        if out is None:
+            out = np.empty((n, h, w, 3), np.float32)
+        self.ctx.check(lib().salty_unet_forward(self.ctx.h, self.h, _ptr(f), n, h, w, _ptr(out)), "unet_forward")
+        return out[0] if features.ndim == 3 and isinstance(out, np.ndarray) else out
+
+    def train_step(self, features, target, lr: float) -> float:
+        f = self._batch(features, 10)
+        t = self._batch(target, 3)
+        n, h, w = f.shape[:3]
+        if tuple(t.shape[:3]) != (n, h, w):
+            raise ValueError("features and target differ in shape")
+        loss = C.c_float()
+        self.ctx.check(lib().salty_unet_train_step(self.ctx.h, self.h, _ptr(f), _ptr(t), n, h, w, lr,
+                                                   C.byref(loss)), "unet_train_step")
+        return loss.value

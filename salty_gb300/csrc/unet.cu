@@ -1,0 +1,900 @@
+// unet.cu -- the learned denoiser: a 5-level U-Net trained and run by these kernels.
+//
+// The reference has an NLM filter (src/s3d_denoiser.cpp:19-95) and no learned denoiser;
+// this network is new.  Input: 10 features per pixel (log(1 + colour), first-hit albedo,
+// normal, 1/(1 + distance)), padded to 16 channels.  Architecture (NHWC, BF16 activations):
+//   enc: conv 16->32, 32->32 | pool | 32->48, 48->48 | pool | 48->64, 64->64 | pool |
+//        64->80, 80->80 | pool | 80->96
+//   dec: up + concat(96+80) -> 80 | up + concat(80+64) -> 64 | up + concat(64+48) -> 48 |
+//        up + concat(48+32) -> 32 | conv 32->8 (channels 0..2: log(1 + colour))
+// every conv 3x3, stride 1, zero padding, ReLU except the last; 2x2 max-pool; nearest 2x
+// up-sampling.  Loss: mean |out - log(1 + target)| (L1 in log space).  Optimiser: Adam.
+//
+// Convolutions are implicit GEMMs on the tensor cores (mma.sync m16n8k16, BF16 operands,
+// FP32 accumulation):
+//   forward       M = pixels, N = Cout, K = 9*Cin: a CTA stages an 8x16-pixel tile plus halo
+//                 in shared memory; A fragments come from it, B fragments from the weights.
+//   backward data the same kernel on dY with the weights flipped and transposed.
+//   backward wts  M = Cout, N = Cin, K = pixels: ldmatrix.trans turns the NHWC tiles of dY and
+//                 of the shifted input into fragments with pixels along K; each CTA sums its
+//                 pixel tiles in registers and adds the partial into FP32 gradients.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+namespace salty {
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int kTileX = 16, kTileY = 8;          // output tile of one CTA
+constexpr int kHaloX = kTileX + 2, kHaloY = kTileY + 2;
+constexpr int kConvThreads = 128;
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void ldmatrix_x4_trans(unsigned (&r)[4], const void* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+
+// ---------------------------------------------------------------- conv3x3 (forward, backward data)
+// in:  [N][H][W][in_cs] BF16 (channels 0..Cin-1 used, Cin % 16 == 0)
+// wt:  [9][wrows][Cin] BF16 (tap-major, input channel contiguous); output channel co reads row co
+// out: [N][H][W][out_cs] BF16 at channel offset out_co (channels co < Cout written)
+// NT n8-tiles per CTA; blockIdx.y selects output channels [blockIdx.y*NT*8, +NT*8).
+template <int NT>
+__global__ void __launch_bounds__(kConvThreads) k_conv3x3(const bf16* __restrict__ in, int in_cs, int Cin,
+                                                          const bf16* __restrict__ wt, const float* __restrict__ bias,
+                                                          bf16* __restrict__ out, int out_cs, int out_co, int Cout,
+                                                          int N, int H, int W, int relu) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16* tile = reinterpret_cast<bf16*>(smem_raw);
+    const int stride = Cin + 8;  // halves per halo pixel (conflict-free fragment loads)
+    const int tiles_x = (W + kTileX - 1) / kTileX, tiles_y = (H + kTileY - 1) / kTileY;
+    int t = blockIdx.x;
+    const int tx = t % tiles_x;
+    t /= tiles_x;
+    const int ty = t % tiles_y;
+    const int n = t / tiles_y;
+    const int x0 = tx * kTileX, y0 = ty * kTileY;
+    // stage the halo tile
+    const int chunks = Cin / 8;
+    for (int i = threadIdx.x; i < kHaloX * kHaloY * chunks; i += kConvThreads) {
+        const int pix = i / chunks, c = i % chunks;
+        const int gy = y0 - 1 + pix / kHaloX, gx = x0 - 1 + pix % kHaloX;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+            v = *reinterpret_cast<const uint4*>(in + (((size_t)n * H + gy) * W + gx) * in_cs + c * 8);
+        *reinterpret_cast<uint4*>(tile + pix * stride + c * 8) = v;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, tq = lane & 3;
+    const int co_base = blockIdx.y * NT * 8;
+    float acc[2][NT][4];
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int j = 0; j < NT; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[m][j][k] = 0.0f;
+    const int wrows_stride = Cin;  // halves per weight row
+    for (int tap = 0; tap < 9; ++tap) {
+        const int ky = tap / 3, kx = tap % 3;
+        const bf16* wtap = wt + (size_t)tap * gridDim.y * NT * 8 * wrows_stride;
+        for (int cb = 0; cb < Cin; cb += 16) {
+            unsigned b[NT][2];
+#pragma unroll
+            for (int j = 0; j < NT; ++j) {
+                const bf16* wr = wtap + (size_t)(co_base + j * 8 + g) * wrows_stride + cb + 2 * tq;
+                b[j][0] = __ldg(reinterpret_cast<const unsigned*>(wr));
+                b[j][1] = __ldg(reinterpret_cast<const unsigned*>(wr + 8));
+            }
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+                const int row = 2 * warp + m;  // tile row handled by this m16 tile
+                const bf16* p0 = tile + ((row + ky) * kHaloX + (g + kx)) * stride + cb + 2 * tq;
+                const bf16* p1 = p0 + 8 * stride;  // pixel g + 8
+                unsigned a[4];
+                a[0] = *reinterpret_cast<const unsigned*>(p0);
+                a[1] = *reinterpret_cast<const unsigned*>(p1);
+                a[2] = *reinterpret_cast<const unsigned*>(p0 + 8);
+                a[3] = *reinterpret_cast<const unsigned*>(p1 + 8);
+#pragma unroll
+                for (int j = 0; j < NT; ++j) mma_bf16(acc[m][j], a, b[j][0], b[j][1]);
+            }
+        }
+    }
+    // epilogue: bias, ReLU, BF16
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+        const int y = y0 + 2 * warp + m;
+        if (y >= H) continue;
+#pragma unroll
+        for (int j = 0; j < NT; ++j) {
+            const int co = co_base + j * 8 + 2 * tq;
+            if (co >= Cout) continue;
+            const float b0 = bias ? bias[co] : 0.0f, b1 = bias ? bias[co + 1] : 0.0f;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int x = x0 + g + 8 * h;
+                if (x >= W) continue;
+                float v0 = acc[m][j][2 * h] + b0, v1 = acc[m][j][2 * h + 1] + b1;
+                if (relu) { v0 = fmaxf(v0, 0.0f); v1 = fmaxf(v1, 0.0f); }
+                *reinterpret_cast<__nv_bfloat162*>(out + (((size_t)n * H + y) * W + x) * out_cs + out_co + co) =
+                    __floats2bfloat162_rn(v0, v1);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- conv3x3 backward weights
+// dW[tap][co][ci] += sum_p dY[p][co] * X[p + (ky-1, kx-1)][ci] for one tap (blockIdx.y) and a
+// 16-wide input-channel slice (blockIdx.z); CTAs stride over 8x16 pixel tiles (blockIdx.x).
+// dY: [N][H][W][dy_cs] with Cpad = dy_cs channels (multiple of 16, zero beyond the layer's
+// real outputs); rows co >= cout_real are not written.  X: [N][H][W][x_cs], Cin % 16 == 0.
+__global__ void __launch_bounds__(kConvThreads) k_conv3x3_wgrad(const bf16* __restrict__ dy, int Cpad, int cout_real,
+                                                                const bf16* __restrict__ x, int x_cs, int Cin,
+                                                                float* __restrict__ dw, int N, int H, int W) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int dstride = Cpad + 8;
+    constexpr int xstride = 16 + 8;
+    bf16* dys = reinterpret_cast<bf16*>(smem_raw);         // [128][dstride]
+    bf16* xs = dys + kTileX * kTileY * dstride;            // [10*18][xstride]
+    const int tap = blockIdx.y, ky = tap / 3, kx = tap % 3;
+    const int ci0 = blockIdx.z * 16;
+    const int tiles_x = (W + kTileX - 1) / kTileX, tiles_y = (H + kTileY - 1) / kTileY;
+    const int ntiles = N * tiles_x * tiles_y;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mtiles = Cpad / 16;
+    float acc[2][2][4];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[a][j][k] = 0.0f;
+    const int kk = lane & 7, which = lane >> 3;  // ldmatrix: row within matrix, matrix index
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int tt = t;
+        const int tx = tt % tiles_x;
+        tt /= tiles_x;
+        const int ty = tt % tiles_y;
+        const int n = tt / tiles_y;
+        const int x0 = tx * kTileX, y0 = ty * kTileY;
+        __syncthreads();
+        const int dchunks = Cpad / 8;
+        for (int i = threadIdx.x; i < kTileX * kTileY * dchunks; i += kConvThreads) {
+            const int pix = i / dchunks, c = i % dchunks;
+            const int gy = y0 + pix / kTileX, gx = x0 + pix % kTileX;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (gy < H && gx < W) v = *reinterpret_cast<const uint4*>(dy + (((size_t)n * H + gy) * W + gx) * Cpad + c * 8);
+            *reinterpret_cast<uint4*>(dys + pix * dstride + c * 8) = v;
+        }
+        for (int i = threadIdx.x; i < kHaloX * kHaloY * 2; i += kConvThreads) {
+            const int pix = i / 2, c = i % 2;
+            const int gy = y0 - 1 + pix / kHaloX, gx = x0 - 1 + pix % kHaloX;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+                v = *reinterpret_cast<const uint4*>(x + (((size_t)n * H + gy) * W + gx) * x_cs + ci0 + c * 8);
+            *reinterpret_cast<uint4*>(xs + pix * xstride + c * 8) = v;
+        }
+        __syncthreads();
+        // K = the tile's 128 pixels in 8 steps of 16 (one tile row each)
+        for (int s = 0; s < kTileY; ++s) {
+            // B: pixels (row s, cols 0..15) shifted by the tap x 16 input channels.  Matrices:
+            // 0 = (px 0-7, ci 0-7), 1 = (px 8-15, ci 0-7), 2 = (px 0-7, ci 8-15), 3 = (px 8-15, ci 8-15)
+            unsigned bq[4];
+            {
+                const int px = kk + ((which & 1) ? 8 : 0);
+                const int cc = (which & 2) ? 8 : 0;
+                ldmatrix_x4_trans(bq, xs + ((s + ky) * kHaloX + px + kx) * xstride + cc);
+            }
+            for (int mi = 0; mi < 2; ++mi) {
+                const int mt = warp + 4 * mi;
+                if (mt >= mtiles) break;
+                // A: output channels (rows) x pixels (k).  Matrices: 0 = (co 0-7, px 0-7),
+                // 1 = (co 8-15, px 0-7), 2 = (co 0-7, px 8-15), 3 = (co 8-15, px 8-15)
+                unsigned a[4];
+                {
+                    const int px = kk + ((which & 2) ? 8 : 0);
+                    const int co = mt * 16 + ((which & 1) ? 8 : 0);
+                    ldmatrix_x4_trans(a, dys + (s * kTileX + px) * dstride + co);
+                }
+                mma_bf16(acc[mi][0], a, bq[0], bq[1]);
+                mma_bf16(acc[mi][1], a, bq[2], bq[3]);
+            }
+        }
+    }
+    const int g = lane >> 2, tq = lane & 3;
+    for (int mi = 0; mi < 2; ++mi) {
+        const int mt = warp + 4 * mi;
+        if (mt >= mtiles) break;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int ci = ci0 + j * 8 + 2 * tq;
+            const int co0 = mt * 16 + g, co1 = co0 + 8;
+            if (co0 < cout_real) {
+                float* r0 = dw + ((size_t)tap * cout_real + co0) * Cin + ci;
+                atomicAdd(r0, acc[mi][j][0]);
+                atomicAdd(r0 + 1, acc[mi][j][1]);
+            }
+            if (co1 < cout_real) {
+                float* r1 = dw + ((size_t)tap * cout_real + co1) * Cin + ci;
+                atomicAdd(r1, acc[mi][j][2]);
+                atomicAdd(r1 + 1, acc[mi][j][3]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- elementwise / layout
+// features (10 floats per pixel: colour, albedo, normal, 1/(1+t)) -> 16-channel BF16 input
+__global__ void k_prep_input(const float* __restrict__ f, long long npx, bf16* __restrict__ x) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
+        const float* s = f + p * 10;
+        bf16* d = x + p * 16;
+        for (int c = 0; c < 3; ++c) d[c] = __float2bfloat16(log1pf(fmaxf(s[c], 0.0f)));
+        for (int c = 3; c < 10; ++c) d[c] = __float2bfloat16(s[c]);
+        for (int c = 10; c < 16; ++c) d[c] = __float2bfloat16(0.0f);
+    }
+}
+
+// 2x2 max-pool: in [N][H][W][C] -> out [N][H/2][W/2][C]
+__global__ void k_pool(const bf16* __restrict__ in, bf16* __restrict__ out, int N, int H, int W, int C) {
+    const int Ho = H / 2, Wo = W / 2;
+    const long long total = (long long)N * Ho * Wo * C;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        long long p = i / C;
+        const int xo = (int)(p % Wo);
+        p /= Wo;
+        const int yo = (int)(p % Ho);
+        const int n = (int)(p / Ho);
+        const bf16* s = in + (((size_t)n * H + 2 * yo) * W + 2 * xo) * C + c;
+        float m = fmaxf(fmaxf(__bfloat162float(s[0]), __bfloat162float(s[C])),
+                        fmaxf(__bfloat162float(s[(size_t)W * C]), __bfloat162float(s[(size_t)W * C + C])));
+        out[i] = __float2bfloat16(m);
+    }
+}
+
+// max-pool backward: the gradient goes to the first input equal to the max (ties: first)
+__global__ void k_pool_bwd(const bf16* __restrict__ in, const float* __restrict__ dout, float* __restrict__ din, int N,
+                           int H, int W, int C) {
+    const int Ho = H / 2, Wo = W / 2;
+    const long long total = (long long)N * Ho * Wo * C;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        long long p = i / C;
+        const int xo = (int)(p % Wo);
+        p /= Wo;
+        const int yo = (int)(p % Ho);
+        const int n = (int)(p / Ho);
+        const size_t base = (((size_t)n * H + 2 * yo) * W + 2 * xo) * C + c;
+        const size_t off[4] = {0, (size_t)C, (size_t)W * C, (size_t)W * C + C};
+        float m = -INFINITY;
+        int arg = 0;
+        for (int k = 0; k < 4; ++k) {
+            float v = __bfloat162float(in[base + off[k]]);
+            if (v > m) { m = v; arg = k; }
+        }
+        din[base + off[arg]] += dout[i];
+    }
+}
+
+// nearest 2x up-sampling of coarse [N][H/2][W/2][Cc] into channels [0, Cc) of cat [N][H][W][Ccat]
+__global__ void k_upsample(const bf16* __restrict__ coarse, int Cc, bf16* __restrict__ cat, int Ccat, int N, int H,
+                           int W) {
+    const long long total = (long long)N * H * W * Cc;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % Cc);
+        long long p = i / Cc;
+        const int x = (int)(p % W);
+        p /= W;
+        const int y = (int)(p % H);
+        const int n = (int)(p / H);
+        cat[(((size_t)n * H + y) * W + x) * Ccat + c] = coarse[(((size_t)n * (H / 2) + y / 2) * (W / 2) + x / 2) * Cc + c];
+    }
+}
+
+// copy skip [N][H][W][Cs] into channels [off, off + Cs) of cat
+__global__ void k_copy_channels(const bf16* __restrict__ src, int Cs, bf16* __restrict__ dst, int Cd, int off,
+                                long long npx) {
+    const long long total = npx * Cs;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / Cs;
+        const int c = (int)(i % Cs);
+        dst[p * Cd + off + c] = src[i];
+    }
+}
+
+// L1 loss in log space on channels 0..2 of out [npx][8]; grad dout (FP32, zero elsewhere)
+__global__ void k_loss(const bf16* __restrict__ out, const float* __restrict__ target, long long npx,
+                       float* __restrict__ dout, double* __restrict__ loss_sum) {
+    double s = 0.0;
+    const float scale = 1.0f / (3.0f * (float)npx);
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
+        for (int c = 0; c < 8; ++c) {
+            float g = 0.0f;
+            if (c < 3) {
+                const float y = __bfloat162float(out[p * 8 + c]);
+                const float t = log1pf(fmaxf(target[p * 3 + c], 0.0f));
+                const float d = y - t;
+                s += fabsf(d);
+                g = (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) * scale;
+            }
+            dout[p * 8 + c] = g;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss_sum, s);
+}
+
+// network output (log colour) -> linear colour
+__global__ void k_output(const bf16* __restrict__ out, long long npx, float* __restrict__ rgb) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x)
+        for (int c = 0; c < 3; ++c) rgb[p * 3 + c] = fmaxf(expm1f(__bfloat162float(out[p * 8 + c])), 0.0f);
+}
+
+// ReLU backward on a layer's output y: g = dy * (y > 0) in BF16 (the next GEMMs' operand),
+// with g_cs >= C channels per pixel, the extra ones zero.
+__global__ void k_relu_bwd(const bf16* __restrict__ y, int y_cs, const float* __restrict__ dy, int C, int relu,
+                           long long npx, bf16* __restrict__ g, int g_cs) {
+    const long long total = npx * g_cs;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / g_cs;
+        const int c = (int)(i % g_cs);
+        float v = 0.0f;
+        if (c < C) {
+            v = dy[p * C + c];
+            if (relu && !(__bfloat162float(y[p * y_cs + c]) > 0.0f)) v = 0.0f;
+        }
+        g[i] = __float2bfloat16(v);
+    }
+}
+
+// bias gradient: db[c] += sum_p g[p][c] for c < C (g has g_cs channels per pixel)
+__global__ void k_bias_grad(const bf16* __restrict__ g, int g_cs, int C, long long npx, float* __restrict__ db) {
+    extern __shared__ float sb[];
+    for (int c = threadIdx.x; c < C; c += blockDim.x) sb[c] = 0.0f;
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx * C; i += (long long)gridDim.x * blockDim.x)
+        atomicAdd(&sb[i % C], __bfloat162float(g[(i / C) * g_cs + i % C]));
+    __syncthreads();
+    for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&db[c], sb[c]);
+}
+
+// BF16 activation gradient (from a backward-data GEMM) -> FP32, optionally accumulated;
+// channels [off, off + C) of src [npx][Cs]
+__global__ void k_grad_to_f32(const bf16* __restrict__ src, int Cs, int off, int C, long long npx, float* __restrict__ dst,
+                              int accumulate) {
+    const long long total = npx * C;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / C;
+        const int c = (int)(i % C);
+        const float v = __bfloat162float(src[p * Cs + off + c]);
+        dst[i] = accumulate ? dst[i] + v : v;
+    }
+}
+
+// up-sampling backward: coarse grad = sum of its 2x2 children's grads (channels [0, Cc) of dcat)
+__global__ void k_upsample_bwd(const bf16* __restrict__ dcat, int Ccat, float* __restrict__ dcoarse, int Cc, int N,
+                               int H, int W) {
+    const int Hc = H / 2, Wc = W / 2;
+    const long long total = (long long)N * Hc * Wc * Cc;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % Cc);
+        long long p = i / Cc;
+        const int x = (int)(p % Wc);
+        p /= Wc;
+        const int y = (int)(p % Hc);
+        const int n = (int)(p / Hc);
+        float s = 0.0f;
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx)
+                s += __bfloat162float(dcat[(((size_t)n * H + 2 * y + dy) * W + 2 * x + dx) * Ccat + c]);
+        dcoarse[i] = s;
+    }
+}
+
+// Adam on FP32 masters, then the BF16 copies: forward layout [tap][co][ci] and the
+// backward-data layout [tap][ci][co] with taps flipped (8 - tap).
+struct AdamArgs {
+    float lr, b1, b2, eps, c1, c2;  // c1 = 1/(1-b1^t), c2 = 1/(1-b2^t)
+};
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       long long n, AdamArgs a) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = a.b1 * m[i] + (1.0f - a.b1) * gi;
+        const float vi = a.b2 * v[i] + (1.0f - a.b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= a.lr * (mi * a.c1) / (sqrtf(vi * a.c2) + a.eps);
+    }
+}
+
+__global__ void k_weights_to_bf16(const float* __restrict__ w, int Cout, int Cin, int rows_fwd, int rows_bwd,
+                                  int cout_pad, bf16* __restrict__ wf, bf16* __restrict__ wb) {
+    const int total = 9 * Cout * Cin;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int ci = i % Cin, co = (i / Cin) % Cout, tap = i / (Cin * Cout);
+        const bf16 v = __float2bfloat16(w[i]);
+        wf[((size_t)tap * rows_fwd + co) * Cin + ci] = v;
+        if (wb) wb[((size_t)(8 - tap) * rows_bwd + ci) * cout_pad + co] = v;
+    }
+}
+
+inline int gsz(long long n, int block = 256) {
+    long long g = (n + block - 1) / block;
+    return (int)(g > 4096 ? 4096 : (g < 1 ? 1 : g));
+}
+
+// ---------------------------------------------------------------- network
+struct UnetLayer {
+    int cin, cout, relu;  // cin % 16 == 0 (input padded); cout % 8 == 0
+    int cout_pad;         // cout rounded up to 16 (gradient operand channels)
+    long long w_off, b_off;  // parameter vector: w [9][cout][cin], then b [cout]
+    int nt, rows_fwd;     // forward conv: n8 tiles per CTA, BF16 weight rows
+    int nt_b, rows_bwd;   // backward-data conv (outputs cin channels)
+    long long wf_off, wb_off;  // BF16 weight copies
+};
+
+// Layer table: input padded to 16 channels, output 8 channels of which 3 are used.
+const int kLayers[][3] = {
+    {16, 32, 1}, {32, 32, 1},   // enc0 -> e0
+    {32, 48, 1}, {48, 48, 1},   // enc1 -> e1
+    {48, 64, 1}, {64, 64, 1},   // enc2 -> e2
+    {64, 80, 1}, {80, 80, 1},   // enc3 -> e3
+    {80, 96, 1},                // bottleneck -> b
+    {176, 80, 1},               // dec3: up(b) + e3 -> d3
+    {144, 64, 1},               // dec2: up(d3) + e2 -> d2
+    {112, 48, 1},               // dec1: up(d2) + e1 -> d1
+    {80, 32, 1},                // dec0: up(d1) + e0 -> d0
+    {32, 8, 0},                 // output
+};
+constexpr int kNumLayers = 14;
+
+int pick_nt(int c) {
+    if (c <= 64) return c / 8;  // the whole channel count in one CTA
+    for (int nt = 6; nt >= 2; --nt)
+        if (c % (nt * 8) == 0) return nt;
+    return 2;
+}
+
+inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+// Activation workspace (BF16), by name; sizes in elements for N x H x W inputs.
+enum {
+    T_X, T_A0, T_E0, T_P0, T_A1, T_E1, T_P1, T_A2, T_E2, T_P2, T_A3, T_E3, T_P3, T_B,
+    T_C3, T_D3, T_C2, T_D2, T_C1, T_D1, T_C0, T_D0, T_OUT, T_G, T_G2, T_COUNT
+};
+// FP32 gradients, by name.
+enum {
+    G_OUT, G_D0, G_C0S, G_D1, G_D2, G_D3, G_B, G_E0, G_E1, G_E2, G_E3, G_P3, G_A3, G_P2, G_A2, G_P1, G_A1, G_P0,
+    G_A0, G_COUNT
+};
+
+}  // namespace
+
+struct Unet {
+    std::vector<UnetLayer> layers;
+    long long n_params = 0;
+    DevBuf<float> params, grads, adam_m, adam_v;
+    DevBuf<bf16> wf, wb;
+    long long step = 0;
+    int N = 0, H = 0, W = 0;
+    DevBuf<bf16> act;
+    DevBuf<float> gbuf;
+    long long act_off[T_COUNT], g_off[G_COUNT];
+    DevBuf<float> io;       // device copies of host features / targets / outputs
+    DevBuf<double> loss;
+};
+
+namespace {
+
+void init_layers(Unet& u) {
+    u.layers.clear();
+    long long off = 0, wf = 0, wb = 0;
+    for (int i = 0; i < kNumLayers; ++i) {
+        UnetLayer L;
+        L.cin = kLayers[i][0];
+        L.cout = kLayers[i][1];
+        L.relu = kLayers[i][2];
+        L.cout_pad = round_up(L.cout, 16);
+        L.w_off = off;
+        off += 9LL * L.cin * L.cout;
+        L.b_off = off;
+        off += L.cout;
+        L.nt = pick_nt(L.cout);
+        L.rows_fwd = round_up(L.cout, L.nt * 8);
+        L.nt_b = pick_nt(L.cin);
+        L.rows_bwd = round_up(L.cin, L.nt_b * 8);
+        L.wf_off = wf;
+        wf += 9LL * L.rows_fwd * L.cin;
+        L.wb_off = wb;
+        wb += 9LL * L.rows_bwd * L.cout_pad;
+        u.layers.push_back(L);
+    }
+    u.n_params = off;
+}
+
+salty_status launch_conv(salty_ctx* ctx, const bf16* in, int in_cs, int cin, const bf16* w, int rows, int nt,
+                         const float* bias, bf16* out, int out_cs, int cout, int N, int H, int W, int relu) {
+    const int tiles = N * ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
+    dim3 grid(tiles, rows / (nt * 8));
+    const size_t smem = (size_t)kHaloX * kHaloY * (cin + 8) * sizeof(bf16);
+#define SALTY_CONV_CASE(NTV)                                                                                         \
+    case NTV: {                                                                                                     \
+        SALTY_TRY_CUDA(ctx->err,                                                                                    \
+                       cudaFuncSetAttribute(k_conv3x3<NTV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+        k_conv3x3<NTV><<<grid, kConvThreads, smem, ctx->stream>>>(in, in_cs, cin, w, bias, out, out_cs, 0, cout, N, H, \
+                                                                  W, relu);                                         \
+        break;                                                                                                      \
+    }
+    switch (nt) {
+        SALTY_CONV_CASE(1) SALTY_CONV_CASE(2) SALTY_CONV_CASE(4) SALTY_CONV_CASE(5) SALTY_CONV_CASE(6)
+        SALTY_CONV_CASE(8)
+        default:
+            return ctx->err.fail(SALTY_ERR_INVALID_ARG, "unsupported conv tile %d", nt);
+    }
+#undef SALTY_CONV_CASE
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+salty_status launch_wgrad(salty_ctx* ctx, const bf16* dy, int cpad, int cout, const bf16* x, int x_cs, int cin,
+                          float* dw, int N, int H, int W) {
+    const size_t smem = ((size_t)kTileX * kTileY * (cpad + 8) + (size_t)kHaloX * kHaloY * 24) * sizeof(bf16);
+    SALTY_TRY_CUDA(ctx->err,
+                   cudaFuncSetAttribute(k_conv3x3_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int tiles = N * ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
+    int gx = ctx->num_sms * 8 / (9 * (cin / 16));
+    if (gx < 1) gx = 1;
+    if (gx > tiles) gx = tiles;
+    dim3 grid(gx, 9, cin / 16);
+    k_conv3x3_wgrad<<<grid, kConvThreads, smem, ctx->stream>>>(dy, cpad, cout, x, x_cs, cin, dw, N, H, W);
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+salty_status ensure_workspace(salty_ctx* ctx, Unet& u, int N, int H, int W) {
+    if (u.N == N && u.H == H && u.W == W && u.act.p) return SALTY_OK;
+    const long long P0 = (long long)N * H * W, P1 = P0 / 4, P2 = P0 / 16, P3 = P0 / 64, P4 = P0 / 256;
+    const long long asz[T_COUNT] = {P0 * 16, P0 * 32, P0 * 32, P1 * 32, P1 * 48, P1 * 48, P2 * 48, P2 * 64, P2 * 64,
+                                    P3 * 64, P3 * 80, P3 * 80, P4 * 80, P4 * 96, P3 * 176, P3 * 80, P2 * 144, P2 * 64,
+                                    P1 * 112, P1 * 48, P0 * 80, P0 * 32, P0 * 8, P0 * 176, P0 * 176};
+    const long long gsz_[G_COUNT] = {P0 * 8, P0 * 32, P0 * 32, P1 * 48, P2 * 64, P3 * 80, P4 * 96, P0 * 32, P1 * 48,
+                                     P2 * 64, P3 * 80, P4 * 80, P3 * 80, P3 * 64, P2 * 64, P2 * 48, P1 * 48, P1 * 32,
+                                     P0 * 32};
+    long long o = 0;
+    for (int i = 0; i < T_COUNT; ++i) { u.act_off[i] = o; o += (asz[i] + 63) / 64 * 64; }
+    SALTY_TRY_CUDA(ctx->err, u.act.ensure((size_t)o));
+    o = 0;
+    for (int i = 0; i < G_COUNT; ++i) { u.g_off[i] = o; o += (gsz_[i] + 63) / 64 * 64; }
+    SALTY_TRY_CUDA(ctx->err, u.gbuf.ensure((size_t)o));
+    u.N = N; u.H = H; u.W = W;
+    return SALTY_OK;
+}
+
+salty_status refresh_bf16(salty_ctx* ctx, Unet& u) {
+    for (const UnetLayer& L : u.layers)
+        k_weights_to_bf16<<<gsz(9LL * L.cout * L.cin), 256, 0, ctx->stream>>>(
+            u.params.p + L.w_off, L.cout, L.cin, L.rows_fwd, L.rows_bwd, L.cout_pad, u.wf.p + L.wf_off, u.wb.p + L.wb_off);
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+struct Fwd {
+    bf16* t[T_COUNT];
+};
+
+salty_status forward(salty_ctx* ctx, Unet& u, const float* d_feat, int N, int H, int W, Fwd& F) {
+    SALTY_TRY(ensure_workspace(ctx, u, N, H, W));
+    for (int i = 0; i < T_COUNT; ++i) F.t[i] = u.act.p + u.act_off[i];
+    cudaStream_t st = ctx->stream;
+    const long long P0 = (long long)N * H * W;
+    k_prep_input<<<gsz(P0), 256, 0, st>>>(d_feat, P0, F.t[T_X]);
+    auto conv = [&](int li, int in, int in_cs, int out, int h, int w) {
+        const UnetLayer& L = u.layers[li];
+        return launch_conv(ctx, F.t[in], in_cs, L.cin, u.wf.p + L.wf_off, L.rows_fwd, L.nt, u.params.p + L.b_off,
+                           F.t[out], L.cout, L.cout, N, h, w, L.relu);
+    };
+    auto pool = [&](int in, int out, int h, int w, int c) {
+        k_pool<<<gsz((long long)N * (h / 2) * (w / 2) * c), 256, 0, st>>>(F.t[in], F.t[out], N, h, w, c);
+    };
+    auto upcat = [&](int coarse, int cc, int skip, int cs, int cat, int h, int w) {
+        const long long np = (long long)N * h * w;
+        k_upsample<<<gsz(np * cc), 256, 0, st>>>(F.t[coarse], cc, F.t[cat], cc + cs, N, h, w);
+        k_copy_channels<<<gsz(np * cs), 256, 0, st>>>(F.t[skip], cs, F.t[cat], cc + cs, cc, np);
+    };
+    const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8, H4 = H / 16, W4 = W / 16;
+    SALTY_TRY(conv(0, T_X, 16, T_A0, H, W));
+    SALTY_TRY(conv(1, T_A0, 32, T_E0, H, W));
+    pool(T_E0, T_P0, H, W, 32);
+    SALTY_TRY(conv(2, T_P0, 32, T_A1, H1, W1));
+    SALTY_TRY(conv(3, T_A1, 48, T_E1, H1, W1));
+    pool(T_E1, T_P1, H1, W1, 48);
+    SALTY_TRY(conv(4, T_P1, 48, T_A2, H2, W2));
+    SALTY_TRY(conv(5, T_A2, 64, T_E2, H2, W2));
+    pool(T_E2, T_P2, H2, W2, 64);
+    SALTY_TRY(conv(6, T_P2, 64, T_A3, H3, W3));
+    SALTY_TRY(conv(7, T_A3, 80, T_E3, H3, W3));
+    pool(T_E3, T_P3, H3, W3, 80);
+    SALTY_TRY(conv(8, T_P3, 80, T_B, H4, W4));
+    upcat(T_B, 96, T_E3, 80, T_C3, H3, W3);
+    SALTY_TRY(conv(9, T_C3, 176, T_D3, H3, W3));
+    upcat(T_D3, 80, T_E2, 64, T_C2, H2, W2);
+    SALTY_TRY(conv(10, T_C2, 144, T_D2, H2, W2));
+    upcat(T_D2, 64, T_E1, 48, T_C1, H1, W1);
+    SALTY_TRY(conv(11, T_C1, 112, T_D1, H1, W1));
+    upcat(T_D1, 48, T_E0, 32, T_C0, H, W);
+    SALTY_TRY(conv(12, T_C0, 80, T_D0, H, W));
+    SALTY_TRY(conv(13, T_D0, 32, T_OUT, H, W));
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+// One conv layer backward.  dy: FP32 [npx][cout] gradient of the layer output y.  Adds the
+// weight and bias gradients; leaves dL/d(input) in BF16 in F.t[T_G2] ([npx][cin]) when
+// want_dx.
+salty_status conv_backward(salty_ctx* ctx, Unet& u, Fwd& F, int li, int x, int y, const float* dy, int N, int h,
+                           int w, bool want_dx) {
+    const UnetLayer& L = u.layers[li];
+    const long long npx = (long long)N * h * w;
+    cudaStream_t st = ctx->stream;
+    bf16* g = F.t[T_G];
+    k_relu_bwd<<<gsz(npx * L.cout_pad), 256, 0, st>>>(F.t[y], L.cout, dy, L.cout, L.relu, npx, g, L.cout_pad);
+    k_bias_grad<<<gsz(npx * L.cout), 256, L.cout * sizeof(float), st>>>(g, L.cout_pad, L.cout, npx,
+                                                                       u.grads.p + L.b_off);
+    SALTY_TRY(launch_wgrad(ctx, g, L.cout_pad, L.cout, F.t[x], L.cin, L.cin, u.grads.p + L.w_off, N, h, w));
+    if (want_dx)
+        SALTY_TRY(launch_conv(ctx, g, L.cout_pad, L.cout_pad, u.wb.p + L.wb_off, L.rows_bwd, L.nt_b, nullptr,
+                              F.t[T_G2], L.cin, L.cin, N, h, w, 0));
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+// Loss and all gradients for the batch in F (after forward); grads are zeroed first.
+salty_status backward(salty_ctx* ctx, Unet& u, Fwd& F, const float* d_target, int N, int H, int W, double* loss) {
+    cudaStream_t st = ctx->stream;
+    const long long P0 = (long long)N * H * W;
+    float* G[G_COUNT];
+    for (int i = 0; i < G_COUNT; ++i) G[i] = u.gbuf.p + u.g_off[i];
+    SALTY_TRY_CUDA(ctx->err, cudaMemsetAsync(u.grads.p, 0, u.n_params * sizeof(float), st));
+    SALTY_TRY_CUDA(ctx->err, u.loss.ensure(1));
+    SALTY_TRY_CUDA(ctx->err, cudaMemsetAsync(u.loss.p, 0, sizeof(double), st));
+    k_loss<<<gsz(P0), 256, 0, st>>>(F.t[T_OUT], d_target, P0, G[G_OUT], u.loss.p);
+    const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8, H4 = H / 16, W4 = W / 16;
+    const long long P1 = P0 / 4, P2 = P0 / 16, P3 = P0 / 64, P4 = P0 / 256;
+    auto to_f32 = [&](int cs, int off, int c, long long np, float* dst, int acc) {
+        k_grad_to_f32<<<gsz(np * c), 256, 0, st>>>(F.t[T_G2], cs, off, c, np, dst, acc);
+    };
+    // decoder: a conv's input gradient splits into the up-sampled part and the skip part
+    auto split = [&](int cc, int cs, int h, int w, float* g_coarse, float* g_skip) {
+        const long long np = (long long)N * h * w;
+        k_upsample_bwd<<<gsz(np / 4 * cc), 256, 0, st>>>(F.t[T_G2], cc + cs, g_coarse, cc, N, h, w);
+        to_f32(cc + cs, cc, cs, np, g_skip, 0);
+    };
+    SALTY_TRY(conv_backward(ctx, u, F, 13, T_D0, T_OUT, G[G_OUT], N, H, W, true));
+    to_f32(32, 0, 32, P0, G[G_D0], 0);
+    SALTY_TRY(conv_backward(ctx, u, F, 12, T_C0, T_D0, G[G_D0], N, H, W, true));
+    split(48, 32, H, W, G[G_D1], G[G_E0]);
+    SALTY_TRY(conv_backward(ctx, u, F, 11, T_C1, T_D1, G[G_D1], N, H1, W1, true));
+    split(64, 48, H1, W1, G[G_D2], G[G_E1]);
+    SALTY_TRY(conv_backward(ctx, u, F, 10, T_C2, T_D2, G[G_D2], N, H2, W2, true));
+    split(80, 64, H2, W2, G[G_D3], G[G_E2]);
+    SALTY_TRY(conv_backward(ctx, u, F, 9, T_C3, T_D3, G[G_D3], N, H3, W3, true));
+    split(96, 80, H3, W3, G[G_B], G[G_E3]);
+    SALTY_TRY(conv_backward(ctx, u, F, 8, T_P3, T_B, G[G_B], N, H4, W4, true));
+    to_f32(80, 0, 80, P4, G[G_P3], 0);
+    k_pool_bwd<<<gsz(P4 * 80), 256, 0, st>>>(F.t[T_E3], G[G_P3], G[G_E3], N, H3, W3, 80);
+    SALTY_TRY(conv_backward(ctx, u, F, 7, T_A3, T_E3, G[G_E3], N, H3, W3, true));
+    to_f32(80, 0, 80, P3, G[G_A3], 0);
+    SALTY_TRY(conv_backward(ctx, u, F, 6, T_P2, T_A3, G[G_A3], N, H3, W3, true));
+    to_f32(64, 0, 64, P3, G[G_P2], 0);
+    k_pool_bwd<<<gsz(P3 * 64), 256, 0, st>>>(F.t[T_E2], G[G_P2], G[G_E2], N, H2, W2, 64);
+    SALTY_TRY(conv_backward(ctx, u, F, 5, T_A2, T_E2, G[G_E2], N, H2, W2, true));
+    to_f32(64, 0, 64, P2, G[G_A2], 0);
+    SALTY_TRY(conv_backward(ctx, u, F, 4, T_P1, T_A2, G[G_A2], N, H2, W2, true));
+    to_f32(48, 0, 48, P2, G[G_P1], 0);
+    k_pool_bwd<<<gsz(P2 * 48), 256, 0, st>>>(F.t[T_E1], G[G_P1], G[G_E1], N, H1, W1, 48);
+    SALTY_TRY(conv_backward(ctx, u, F, 3, T_A1, T_E1, G[G_E1], N, H1, W1, true));
+    to_f32(48, 0, 48, P1, G[G_A1], 0);
+    SALTY_TRY(conv_backward(ctx, u, F, 2, T_P0, T_A1, G[G_A1], N, H1, W1, true));
+    to_f32(32, 0, 32, P1, G[G_P0], 0);
+    k_pool_bwd<<<gsz(P1 * 32), 256, 0, st>>>(F.t[T_E0], G[G_P0], G[G_E0], N, H, W, 32);
+    SALTY_TRY(conv_backward(ctx, u, F, 1, T_A0, T_E0, G[G_E0], N, H, W, true));
+    to_f32(32, 0, 32, P0, G[G_A0], 0);
+    SALTY_TRY(conv_backward(ctx, u, F, 0, T_X, T_A0, G[G_A0], N, H, W, false));
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    double l = 0.0;
+    SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(&l, u.loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(st));
+    *loss = l / (3.0 * (double)P0);
+    (void)P1; (void)P2; (void)P3; (void)W4; (void)H4;
+    return SALTY_OK;
+}
+
+// Copies n floats of a host-or-device array to the device workspace at `off`.
+salty_status stage(salty_ctx* ctx, Unet& u, const float* src, long long n, long long off, const float** out) {
+    if (is_device_ptr(src)) {
+        *out = src;
+        return SALTY_OK;
+    }
+    SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(u.io.p + off, src, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    *out = u.io.p + off;
+    return SALTY_OK;
+}
+
+salty_status check_shape(salty_ctx* ctx, int n, int h, int w) {
+    if (n <= 0 || h <= 0 || w <= 0 || h % 16 || w % 16)
+        return ctx->err.fail(SALTY_ERR_INVALID_ARG, "unet: n, h, w must be positive and h, w multiples of 16");
+    if ((long long)n * h * w > (1ll << 26)) return ctx->err.fail(SALTY_ERR_CAPACITY, "unet: batch too large");
+    return SALTY_OK;
+}
+
+}  // namespace
+}  // namespace salty
+
+struct salty_unet {
+    salty::Unet net;
+};
+
+extern "C" {
+
+salty_status salty_unet_create(salty_ctx* ctx, uint64_t seed, salty_unet** out) {
+    using namespace salty;
+    if (!ctx || !out) return SALTY_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    auto* h = new (std::nothrow) salty_unet();
+    if (!h) return ctx->err.fail(SALTY_ERR_OOM, "host allocation failed");
+    Unet& u = h->net;
+    init_layers(u);
+    long long wf = 0, wb = 0;
+    for (const UnetLayer& L : u.layers) {
+        wf = L.wf_off + 9LL * L.rows_fwd * L.cin;
+        wb = L.wb_off + 9LL * L.rows_bwd * L.cout_pad;
+    }
+    auto fail = [&](salty_status s) { delete h; return s; };
+    if (u.params.ensure(u.n_params) != cudaSuccess || u.grads.ensure(u.n_params) != cudaSuccess ||
+        u.adam_m.ensure(u.n_params) != cudaSuccess || u.adam_v.ensure(u.n_params) != cudaSuccess ||
+        u.wf.ensure(wf) != cudaSuccess || u.wb.ensure(wb) != cudaSuccess)
+        return fail(ctx->err.fail(SALTY_ERR_OOM, "unet parameters"));
+    // He-uniform weights from a PCG stream (seeded), zero biases
+    std::vector<float> p(u.n_params, 0.0f);
+    uint64_t s = seed + 1442695040888963407ull;
+    auto next = [&]() {
+        uint64_t old = s;
+        s = old * 6364136223846793005ull + 1442695040888963407ull;
+        uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27), rot = (uint32_t)(old >> 59);
+        return (float)((xs >> rot) | (xs << ((~rot + 1u) & 31u))) / 4294967296.0f;
+    };
+    for (size_t li = 0; li < u.layers.size(); ++li) {
+        const UnetLayer& L = u.layers[li];
+        const int real_cin = li == 0 ? 10 : L.cin;
+        const float bound = std::sqrt(6.0f / (9.0f * real_cin)) * (L.relu ? 1.0f : 0.5f);
+        for (long long i = 0; i < 9LL * L.cin * L.cout; ++i) {
+            const int ci = (int)(i % L.cin);
+            p[L.w_off + i] = (li == 0 && ci >= 10) ? 0.0f : (2.0f * next() - 1.0f) * bound;
+        }
+    }
+    cudaStream_t st = ctx->stream;
+    if (cudaMemcpyAsync(u.params.p, p.data(), p.size() * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(u.adam_m.p, 0, u.n_params * sizeof(float), st) != cudaSuccess ||
+        cudaMemsetAsync(u.adam_v.p, 0, u.n_params * sizeof(float), st) != cudaSuccess ||
+        cudaMemsetAsync(u.wf.p, 0, wf * sizeof(bf16), st) != cudaSuccess ||
+        cudaMemsetAsync(u.wb.p, 0, wb * sizeof(bf16), st) != cudaSuccess)
+        return fail(ctx->err.fail(SALTY_ERR_CUDA, "unet init copies"));
+    if (refresh_bf16(ctx, u) != SALTY_OK) return fail(SALTY_ERR_CUDA);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return fail(ctx->err.fail(SALTY_ERR_CUDA, "unet init"));
+    *out = h;
+    return SALTY_OK;
+}
+
+void salty_unet_destroy(salty_ctx* ctx, salty_unet* net) {
+    if (ctx) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    delete net;
+}
+
+int64_t salty_unet_param_count(const salty_unet* net) { return net ? net->net.n_params : 0; }
+
+salty_status salty_unet_get_params(salty_ctx* ctx, salty_unet* net, float* params, float* grads) {
+    using namespace salty;
+    if (!ctx || !net) return SALTY_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Unet& u = net->net;
+    if (params) SALTY_TRY_CUDA(ctx->err, cudaMemcpy(params, u.params.p, u.n_params * sizeof(float), cudaMemcpyDefault));
+    if (grads) SALTY_TRY_CUDA(ctx->err, cudaMemcpy(grads, u.grads.p, u.n_params * sizeof(float), cudaMemcpyDefault));
+    return SALTY_OK;
+}
+
+salty_status salty_unet_set_params(salty_ctx* ctx, salty_unet* net, const float* params) {
+    using namespace salty;
+    if (!ctx || !net || !params) return SALTY_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Unet& u = net->net;
+    SALTY_TRY_CUDA(ctx->err, cudaMemcpy(u.params.p, params, u.n_params * sizeof(float), cudaMemcpyDefault));
+    SALTY_TRY(refresh_bf16(ctx, u));
+    SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(ctx->stream));
+    return SALTY_OK;
+}
+
+salty_status salty_unet_forward(salty_ctx* ctx, salty_unet* net, const float* features, int32_t n, int32_t h,
+                                int32_t w, float* out_rgb) {
+    using namespace salty;
+    if (!ctx || !net || !features || !out_rgb) return SALTY_ERR_INVALID_ARG;
+    SALTY_TRY(check_shape(ctx, n, h, w));
+    cudaSetDevice(ctx->device);
+    Unet& u = net->net;
+    const long long P0 = (long long)n * h * w;
+    SALTY_TRY_CUDA(ctx->err, u.io.ensure((size_t)P0 * 16));
+    const float* df;
+    SALTY_TRY(stage(ctx, u, features, P0 * 10, 0, &df));
+    Fwd F;
+    SALTY_TRY(forward(ctx, u, df, n, h, w, F));
+    const bool dev_out = is_device_ptr(out_rgb);
+    float* dout = dev_out ? out_rgb : u.io.p + P0 * 10;
+    k_output<<<gsz(P0), 256, 0, ctx->stream>>>(F.t[T_OUT], P0, dout);
+    if (!dev_out)
+        SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(out_rgb, dout, P0 * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(ctx->stream));
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+salty_status salty_unet_train_step(salty_ctx* ctx, salty_unet* net, const float* features, const float* target_rgb,
+                                   int32_t n, int32_t h, int32_t w, float lr, float* loss) {
+    using namespace salty;
+    if (!ctx || !net || !features || !target_rgb) return SALTY_ERR_INVALID_ARG;
+    SALTY_TRY(check_shape(ctx, n, h, w));
+    cudaSetDevice(ctx->device);
+    Unet& u = net->net;
+    const long long P0 = (long long)n * h * w;
+    SALTY_TRY_CUDA(ctx->err, u.io.ensure((size_t)P0 * 16));
+    const float *df, *dt;
+    SALTY_TRY(stage(ctx, u, features, P0 * 10, 0, &df));
+    SALTY_TRY(stage(ctx, u, target_rgb, P0 * 3, P0 * 10, &dt));
+    Fwd F;
+    SALTY_TRY(forward(ctx, u, df, n, h, w, F));
+    double l = 0.0;
+    SALTY_TRY(backward(ctx, u, F, dt, n, h, w, &l));
+    if (loss) *loss = (float)l;
+    if (lr > 0.0f) {
+        ++u.step;
+        AdamArgs a;
+        a.lr = lr;
+        a.b1 = 0.9f;
+        a.b2 = 0.999f;
+        a.eps = 1e-8f;
+        a.c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)u.step)));
+        a.c2 = (float)(1.0 / (1.0 - std::pow(0.999, (double)u.step)));
+        k_adam<<<gsz(u.n_params), 256, 0, ctx->stream>>>(u.params.p, u.grads.p, u.adam_m.p, u.adam_v.p, u.n_params, a);
+        SALTY_TRY(refresh_bf16(ctx, u));
+    }
+    SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(ctx->stream));
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+}  // extern "C"
+

@@ -1,0 +1,115 @@
+"""The learned denoiser's CUDA path (salty_unet_*) against the float64 oracle with BF16
+rounding at the same points (oracle/unet_oracle.py).
+
+Tolerances: the two differ only by FP32 (tensor-core) vs FP64 accumulation order, which
+now and then moves a BF16 rounding by one step (2^-8 relative); those differences
+propagate, so outputs are compared at 2% relative L2 and gradients per layer at 5%
+relative L2 with a cosine similarity above 0.998.
+"""
+import numpy as np
+import pytest
+
+from test_unet_oracle import _features
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def net(ctx):
+    import salty_gb300
+    n = salty_gb300.Unet(ctx, seed=11)
+    yield n
+    n.close()
+
+
+def _batch(seed, n=2, h=32, w=32):
+    rng = np.random.default_rng(seed)
+    f = _features(rng, n, h, w)
+    t = (f[..., :3] * rng.uniform(0.6, 1.4, f[..., :3].shape)).astype(np.float32)
+    return f, t
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+def test_parameter_count_and_init(net):
+    from oracle.unet_oracle import param_count, split_params
+    assert net.n_params == param_count()
+    p = net.params()
+    assert np.all(np.isfinite(p))
+    w0, b0 = split_params(p)[0]
+    assert np.all(w0[..., 10:] == 0) and np.all(b0 == 0)  # padded input channels unused
+
+
+def test_forward_matches_oracle(net):
+    from oracle.unet_oracle import UnetOracle
+    f, _ = _batch(1)
+    out = net.forward(f)
+    want, _ = UnetOracle(net.params()).forward(f)
+    assert out.shape == (2, 32, 32, 3)
+    assert _rel(out, want) < 0.02, _rel(out, want)
+
+
+def test_gradients_match_oracle(net):
+    from oracle.unet_oracle import LAYERS, UnetOracle
+    f, t = _batch(2)
+    p0 = net.params()
+    loss = net.train_step(f, t, lr=0.0)
+    np.testing.assert_array_equal(net.params(), p0)  # lr = 0: no update
+    g = net.grads()
+    lo, go = UnetOracle(p0).loss_and_grads(f, t)
+    assert abs(loss / lo - 1) < 1e-2, (loss, lo)
+    o = 0
+    for i, (ci, co, _) in enumerate(LAYERS):
+        n = 9 * ci * co + co
+        a, b = g[o:o + n], go[o:o + n]
+        cos = a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
+        assert _rel(a, b) < 0.05 and cos > 0.998, (i, _rel(a, b), cos)
+        o += n
+
+
+def test_adam_first_step(ctx):
+    """First Adam step moves every parameter with a clear gradient by lr against its sign."""
+    import salty_gb300
+    net = salty_gb300.Unet(ctx, seed=5)
+    f, t = _batch(3, n=1, h=16, w=16)
+    p0 = net.params()
+    net.train_step(f, t, lr=0.0)
+    g = net.grads()
+    net.train_step(f, t, lr=1e-3)
+    d = net.params() - p0
+    big = np.abs(g) > 1e-5
+    np.testing.assert_allclose(d[big], -1e-3 * np.sign(g[big]), rtol=1e-3, atol=1e-7)
+    net.close()
+
+
+def test_training_reduces_loss(ctx):
+    import salty_gb300
+    net = salty_gb300.Unet(ctx, seed=6)
+    f, t = _batch(4, n=4, h=64, w=64)
+    l0 = net.train_step(f, t, lr=0.0)
+    for _ in range(60):
+        l = net.train_step(f, t, lr=2e-3)
+    assert l < 0.6 * l0, (l0, l)
+    net.close()
+
+
+def test_device_arrays_and_batching(ctx, net):
+    import torch
+    f, _ = _batch(5, n=3, h=16, w=48)
+    host = net.forward(f)
+    dev = torch.empty((3, 16, 48, 3), dtype=torch.float32, device="cuda")
+    net.forward(torch.from_numpy(f).cuda(), out=dev)
+    np.testing.assert_array_equal(dev.cpu().numpy(), host)
+    # images of a batch are independent
+    np.testing.assert_array_equal(net.forward(f[1]), host[1])
+
+
+def test_rejects_bad_shapes(net):
+    import salty_gb300
+    f, t = _batch(6, n=1, h=16, w=16)
+    with pytest.raises(salty_gb300.SaltyError):
+        net.forward(np.zeros((1, 20, 16, 10), np.float32))
+    with pytest.raises(ValueError):
+        net.train_step(f, t[:, :8], lr=0.0)
