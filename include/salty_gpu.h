@@ -112,6 +112,10 @@ typedef struct salty_scene_desc {
 
 salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* desc, salty_scene** out);
 void salty_scene_destroy(salty_ctx* ctx, salty_scene* scene);
+/* Replaces the scene's camera (Scene::m_pCamera / PinholeCamera::Update,
+ * include/s3d_camera.h:63-90) without touching geometry or BVH.  Render the next frame
+ * with accumulate = 0: the film's samples belong to the old view. */
+salty_status salty_scene_set_camera(salty_ctx* ctx, salty_scene* scene, const salty_camera* camera);
 
 /* ---------------------------------------------------------------- BVH */
 typedef struct salty_build_opts {
@@ -253,10 +257,12 @@ salty_status salty_denoise_nlm(salty_ctx* ctx, int32_t width, int32_t height, in
  * GEMMs on the tensor cores in BF16 with FP32 accumulation, trained with Adam on an L1
  * loss in log(1 + colour) space.
  *
- * Features: n images of h x w pixels, 10 floats per pixel in this order: colour (the noisy
+ * Features: n images of h x w pixels, 11 floats per pixel in this order: colour (the noisy
  * mean, linear), first-hit albedo (3), first-hit normal (3), 1/(1 + first-hit distance)
- * -- salty_film_read's mean followed by salty_film_aov's three planes.  h and w must be
- * multiples of 16 and n*h*w at most 2^26.  Arrays are host or device. */
+ * -- salty_film_read's mean followed by salty_film_aov's three planes -- and the colour's
+ * noise level in log space, mean over channels of sqrt(var_c) / (1 + colour_c) with var the
+ * variance of the mean.  h and w must be multiples of 16 and n*h*w at most 2^26.  Arrays
+ * are host or device. */
 typedef struct salty_unet salty_unet;
 
 /* He-uniform initial weights from `seed`, zero biases. */
@@ -272,9 +278,15 @@ salty_status salty_unet_forward(salty_ctx* ctx, salty_unet* net, const float* fe
                                 int32_t w, float* out_rgb);
 /* One step on a batch: forward, loss against target_rgb (n*h*w*3 linear), gradients, and,
  * when lr > 0, an Adam update (beta 0.9, 0.999, eps 1e-8).  With lr == 0 only the loss and
- * the gradients are computed.  *loss (may be NULL) = mean |out - log(1 + target)|. */
+ * the gradients are computed.  *loss (may be NULL) = mean |y - log(1 + target)| over pixels
+ * and colour channels, y = log(1 + input colour) + the network's correction. */
 salty_status salty_unet_train_step(salty_ctx* ctx, salty_unet* net, const float* features, const float* target_rgb,
                                    int32_t n, int32_t h, int32_t w, float lr, float* loss);
+/* Denoises the scene's film (the frame or window of the last salty_render) in one device
+ * pass: film mean, variance and first-hit features -> features (borders reflected up to
+ * multiples of 16) -> network.  out_rgb: film width * height * 3 floats, host or device.
+ * NLM (salty_denoise_nlm) is the fallback where no trained weights exist. */
+salty_status salty_denoise_unet(salty_ctx* ctx, salty_unet* net, salty_scene* scene, float* out_rgb);
 
 /* ---------------------------------------------------------------- inputs */
 /* The traversal microbenchmark's seeded inputs (host arrays): a triangle soup with

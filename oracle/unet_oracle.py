@@ -109,7 +109,7 @@ class UnetOracle:
         feat = np.asarray(feat, np.float32)
         x = np.zeros(feat.shape[:3] + (16,))
         x[..., :3] = np.log1p(np.maximum(feat[..., :3], 0.0)).astype(np.float32)
-        x[..., 3:10] = feat[..., 3:10]
+        x[..., 3:11] = feat[..., 3:11]
         return self.r(x)
 
     # ---------------------------------------------------------------- passes
@@ -137,14 +137,15 @@ class UnetOracle:
         S["c1"] = np.concatenate([self._up(S["d2"]), S["e1"]], -1); S["d1"] = conv(11, S["c1"])
         S["c0"] = np.concatenate([self._up(S["d1"]), S["e0"]], -1); S["d0"] = conv(12, S["c0"])
         S["out"] = conv(13, S["d0"])
-        return np.maximum(np.expm1(S["out"][..., :3]), 0.0), S
+        S["pred"] = S["out"][..., :3] + S["x"][..., :3]  # correction of the input's log colour
+        return np.maximum(np.expm1(S["pred"]), 0.0), S
 
     def loss_and_grads(self, feat, target):
         """Mean |out - log(1 + target)| and the gradient of every parameter (flat vector)."""
         _, S = self.forward(feat)
         t = np.log1p(np.maximum(np.asarray(target, np.float32 if self.bf16 else np.float64), 0.0)).astype(np.float64)
         npx = t.shape[0] * t.shape[1] * t.shape[2]
-        d = S["out"][..., :3] - t
+        d = S["pred"] - t
         loss = np.abs(d).sum() / (3.0 * npx)
         scale = float(np.float32(1.0) / np.float32(3.0 * npx)) if self.bf16 else 1.0 / (3.0 * npx)
         dout = np.zeros(S["out"].shape)
@@ -189,4 +190,4 @@ class UnetOracle:
     def loss(self, feat, target):
         out, S = self.forward(feat)
         t = np.log1p(np.maximum(np.asarray(target, np.float64), 0.0))
-        return np.abs(S["out"][..., :3] - t).mean()
+        return np.abs(S["pred"] - t).mean()

@@ -91,7 +91,7 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_denoise_nlm_ref", "salty_denoise_nlm", "salty_microbench_soup", "salty_microbench_rays",
            "salty_tonemap_noalloc", "salty_film_aov", "salty_unet_create", "salty_unet_destroy",
            "salty_unet_param_count", "salty_unet_get_params", "salty_unet_set_params", "salty_unet_forward",
-           "salty_unet_train_step"]
+           "salty_unet_train_step", "salty_scene_set_camera", "salty_denoise_unet"]
 
 _lib = None
 
@@ -115,6 +115,7 @@ def lib() -> C.CDLL:
         "salty_host_free": (None, [vp, vp]),
         "salty_scene_upload": (i32, [vp, C.POINTER(SceneDesc), C.POINTER(vp)]),
         "salty_scene_destroy": (None, [vp, vp]),
+        "salty_scene_set_camera": (i32, [vp, vp, C.POINTER(Camera)]),
         "salty_bvh_build": (i32, [vp, vp, C.POINTER(BuildOpts), C.POINTER(BvhInfo)]),
         "salty_trace": (i32, [vp, vp, vp, i64, u32, vp]),
         "salty_last_trace_stats": (i32, [vp, C.POINTER(TraceStats)]),
@@ -134,6 +135,7 @@ def lib() -> C.CDLL:
         "salty_unet_set_params": (i32, [vp, vp, vp]),
         "salty_unet_forward": (i32, [vp, vp, vp, i32, i32, i32, vp]),
         "salty_unet_train_step": (i32, [vp, vp, vp, vp, i32, i32, i32, f32, C.POINTER(f32)]),
+        "salty_denoise_unet": (i32, [vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -277,11 +279,15 @@ class Context:
         self.check(lib().salty_denoise_nlm_ref(self.h, w, h, coeff, _ptr(rgba), _ptr(out)), "nlm_ref")
         return out
 
-    def nlm(self, rgb, var, search_r: int = 10, patch_r: int = 3, k: float = 0.45):
-        rgb = np.ascontiguousarray(rgb, np.float32)
-        var = np.ascontiguousarray(var, np.float32)
+    def nlm(self, rgb, var, search_r: int = 10, patch_r: int = 3, k: float = 0.45, out=None):
+        """Variance-scaled NLM of an (H, W, 3) image; numpy arrays or device tensors."""
+        if not hasattr(rgb, "data_ptr"):
+            rgb = np.ascontiguousarray(rgb, np.float32)
+        if not hasattr(var, "data_ptr"):
+            var = np.ascontiguousarray(var, np.float32)
         h, w = rgb.shape[:2]
-        out = np.empty_like(rgb)
+        if out is None:
+            out = rgb.new_empty(rgb.shape) if hasattr(rgb, "data_ptr") else np.empty_like(rgb)
         self.check(lib().salty_denoise_nlm(self.h, w, h, search_r, patch_r, k, _ptr(rgb), _ptr(var), _ptr(out)),
                    "nlm")
         return out
@@ -301,6 +307,8 @@ class Scene:
     def __init__(self, ctx: Context, h: C.c_void_p, n_tris: int):
         self.ctx, self.h, self.n_tris = ctx, h, n_tris
         self.info = None
+        self.film_shape = (0, 0)
+        self.film_samples = 0
 
     def close(self) -> None:
         if getattr(self, "h", None) and self.ctx.h:
@@ -348,6 +356,7 @@ class Scene:
         o = RenderOpts(width, height, spp, max_depth, rr_depth, profile, seed, int(accumulate), int(fp64),
                        tonemap, int(ref_oetf), cx, cy, cw, ch)
         fh, fw = (ch, cw) if crop else (height, width)
+        self.film_shape = (fh, fw)
         out = out or {}
         mean = out.get("mean", np.empty((fh, fw, 3), np.float32) if "mean" in want else None)
         var = out.get("var", np.empty((fh, fw, 3), np.float32) if "var" in want else None)
@@ -355,8 +364,15 @@ class Scene:
         st = RenderStats()
         self.ctx.check(lib().salty_render(self.ctx.h, self.h, C.byref(o), _ptr(mean), _ptr(var), _ptr(s8),
                                           C.byref(st)), "render")
+        self.film_samples = int(st.samples)
         return {"mean": mean, "var": var, "srgb": s8, "ms": st.ms, "samples": st.samples, "rays": st.rays,
                 "paths": st.paths}
+
+    def set_camera(self, pos, target, up=(0.0, 1.0, 0.0), fov: float = 1.0, near: float = 1.0) -> None:
+        c = Camera()
+        c.pos, c.target, c.up = _f3(pos), _f3(target), _f3(up)
+        c.fov, c.near_clip = float(fov), float(near)
+        self.ctx.check(lib().salty_scene_set_camera(self.ctx.h, self.h, C.byref(c)), "scene_set_camera")
 
     def aov(self, width: int, height: int) -> dict:
         """Mean first-hit features of the film: albedo, normal (H, W, 3), depth = 1/(1+t) (H, W)."""
@@ -374,16 +390,22 @@ class Scene:
         return s, q, n.value
 
 
+UNET_FEATURES = 11  # input floats per pixel
+
 # The learned denoiser's layers (cin, cout, relu) in parameter order; every layer is a 3x3
 # convolution with weights [9][cout][cin] followed by biases [cout].
 UNET_LAYERS = [(16, 32, 1), (32, 32, 1), (32, 48, 1), (48, 48, 1), (48, 64, 1), (64, 64, 1), (64, 80, 1),
                (80, 80, 1), (80, 96, 1), (176, 80, 1), (144, 64, 1), (112, 48, 1), (80, 32, 1), (32, 8, 0)]
 
 
-def unet_features(mean, aov: dict) -> np.ndarray:
-    """(H, W, 10) denoiser input: noisy colour, first-hit albedo, normal, 1/(1 + distance)."""
-    return np.concatenate([np.asarray(mean, np.float32), aov["albedo"], aov["normal"],
-                           aov["depth"][..., None]], axis=-1).astype(np.float32)
+def unet_features(mean, var, aov: dict) -> np.ndarray:
+    """(H, W, 11) denoiser input: noisy colour, first-hit albedo, normal, 1/(1 + distance) and
+    the colour's noise level in log space, mean_c sqrt(var_c) / (1 + colour_c), from the mean
+    and the variance of the mean of a film."""
+    mean = np.asarray(mean, np.float32)
+    noise = (np.sqrt(np.maximum(np.asarray(var, np.float32), 0.0)) / (1.0 + np.maximum(mean, 0.0))).mean(-1)
+    return np.concatenate([mean, aov["albedo"], aov["normal"], aov["depth"][..., None], noise[..., None]],
+                          axis=-1).astype(np.float32)
 
 
 class Unet:
@@ -434,15 +456,23 @@ class Unet:
         return a
 
     def forward(self, features, out=None):
-        f = self._batch(features, 10)
+        f = self._batch(features, UNET_FEATURES)
         n, h, w = f.shape[:3]
         if out is None:
             out = np.empty((n, h, w, 3), np.float32)
         self.ctx.check(lib().salty_unet_forward(self.ctx.h, self.h, _ptr(f), n, h, w, _ptr(out)), "unet_forward")
         return out[0] if features.ndim == 3 and isinstance(out, np.ndarray) else out
 
+    def denoise_film(self, scene: "Scene", out=None):
+        """Denoised image of the scene's film (H, W, 3), computed on the device."""
+        h, w = scene.film_shape
+        if out is None:
+            out = np.empty((h, w, 3), np.float32)
+        self.ctx.check(lib().salty_denoise_unet(self.ctx.h, self.h, scene.h, _ptr(out)), "denoise_unet")
+        return out
+
     def train_step(self, features, target, lr: float) -> float:
-        f = self._batch(features, 10)
+        f = self._batch(features, UNET_FEATURES)
         t = self._batch(target, 3)
         n, h, w = f.shape[:3]
         if tuple(t.shape[:3]) != (n, h, w):

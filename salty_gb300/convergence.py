@@ -1,4 +1,4 @@
-"""Time-to-RMSE measurement: plain progressive rendering vs a denoised path.
+"""Time-to-RMSE measurement: plain progressive rendering vs denoised paths.
 
 Error metric (relative MSE, used throughout the denoising literature):
     relMSE = mean over pixels and channels of (x - r)^2 / (r^2 + 0.01),  relRMSE = sqrt(relMSE)
@@ -7,11 +7,18 @@ At 1080p that reference would cost ~1.4e11 camera paths, so it is rendered for a
 (crop) of the frame; the window's pixels keep their full-frame rays, so the methods render
 the whole frame and are scored on the window.
 
+The reference is itself a Monte Carlo estimate: against it, an image's measured relMSE is
+its true relMSE plus the reference's own, E = mean(var_r / (r^2 + 0.01)) with var_r the
+variance of the reference's mean (independent samples).  At relRMSE 0.01 the two are of
+the same size, so every error reported here is the measured relMSE minus E (an unbiased
+estimate of the error against the exact image), and E is reported beside it.
+
 A method's time to reach a target relRMSE is measured with a doubling sample schedule:
 the frame is rendered progressively (each pass doubles the samples), after each pass the
-method's image is scored, and the time at which the curve crosses the target is
-interpolated in log(error) against time between the two passes that bracket it.  Times are
-host wall-clock around the library calls (which are synchronous), excluding scoring.
+method's image is formed on the device and scored, and the time at which the curve crosses
+the target is interpolated in log(error) against time between the two passes that bracket
+it.  Times are host wall-clock around the synchronous library calls of each pass (render
+plus the method's own post-processing), excluding the scoring read-back.
 """
 from __future__ import annotations
 
@@ -34,52 +41,87 @@ def rel_rmse(x: np.ndarray, ref: np.ndarray) -> float:
 
 
 def reference_image(scene, width: int, height: int, crop: tuple, max_depth: int, spp: int = 65536,
-                    chunk: int = 2048, seed: int = 987654321, rr_depth: int = 3) -> tuple[np.ndarray, float]:
-    """FP64-accumulated mean of the crop window at `spp` samples; returns (image, seconds)."""
+                    chunk: int = 4096, seed: int = 987654321, rr_depth: int = 3) -> dict:
+    """FP64-accumulated crop window at `spp` samples: {"mean", "var" (of the mean), "noise"
+    (the relMSE its own noise adds, E above), "spp", "seconds"}."""
     t0 = time.perf_counter()
     done = 0
     out = None
     while done < spp:
         k = min(chunk, spp - done)
         out = scene.render(width, height, k, max_depth, rr_depth=rr_depth, profile=PROFILE_PHYSICAL, seed=seed,
-                           accumulate=done > 0, fp64=True, want=("mean",), crop=crop)
+                           accumulate=done > 0, fp64=True, want=("mean", "var"), crop=crop)
         done += k
-    return out["mean"], time.perf_counter() - t0
+    m, v = out["mean"].astype(np.float64), out["var"].astype(np.float64)
+    return {"mean": out["mean"], "var": out["var"], "noise": float(np.mean(v / (m * m + 1e-2))), "spp": spp,
+            "seconds": time.perf_counter() - t0}
 
 
-def crop_of(img: np.ndarray, crop: tuple) -> np.ndarray:
+def corrected_rel_mse(x: np.ndarray, ref: dict) -> float:
+    """relMSE against the exact image, estimated as measured minus the reference's noise."""
+    return rel_mse(x, ref["mean"]) - ref["noise"]
+
+
+def crop_of(img, crop: tuple):
     x, y, w, h = crop
     return img[y:y + h, x:x + w]
 
 
-def converge(scene, width: int, height: int, crop: tuple, ref: np.ndarray, max_depth: int, target: float,
-             denoise=None, spp0: int = 4, max_spp: int = 1 << 16, seed: int = 1, rr_depth: int = 3) -> dict:
-    """Progressive full-frame rendering with doubling spp; denoise(mean, var) -> image (or None
-    for the plain path).  Returns the error curve and the interpolated time to `target`."""
+def converge(scene, width: int, height: int, crop: tuple, ref: dict, max_depth: int, target: float,
+             method: str = "plain", ctx=None, denoiser=None, spp0: int = 4, max_spp: int = 1 << 16, seed: int = 1,
+             rr_depth: int = 3, nlm_k: float = 0.45) -> dict:
+    """Progressive full-frame rendering with doubling spp until the method's image reaches
+    relRMSE <= target on the crop.  method: "plain" (the film mean), "nlm" (salty_denoise_nlm
+    of mean and variance) or "unet" (salty_denoise_unet of the film through `denoiser`, a
+    salty_gb300.denoiser.Denoiser, which picks its network by the film's samples)."""
+    import torch
+    dev = torch.device("cuda")
+    mean = torch.empty((height, width, 3), dtype=torch.float32, device=dev)
+    var = torch.empty_like(mean)
+    img = torch.empty_like(mean)
     curve = []
     spent = 0.0
     total = 0
     step = spp0
+    target_mse = target * target
     while total < max_spp:
+        step = min(step, max_spp - total)
         t0 = time.perf_counter()
-        r = scene.render(width, height, step, max_depth, rr_depth=rr_depth, profile=PROFILE_PHYSICAL, seed=seed,
-                         accumulate=total > 0, want=("mean", "var") if denoise else ("mean",))
-        img = denoise(r["mean"], r["var"]) if denoise else r["mean"]
+        if method == "plain":
+            scene.render(width, height, step, max_depth, rr_depth=rr_depth, profile=PROFILE_PHYSICAL, seed=seed,
+                         accumulate=total > 0, want=("mean",), out={"mean": mean})
+            out = mean
+        elif method == "nlm":
+            scene.render(width, height, step, max_depth, rr_depth=rr_depth, profile=PROFILE_PHYSICAL, seed=seed,
+                         accumulate=total > 0, want=("mean", "var"), out={"mean": mean, "var": var})
+            ctx.nlm(mean, var, 10, 3, nlm_k, out=img)
+            out = img
+        elif method == "unet":
+            scene.render(width, height, step, max_depth, rr_depth=rr_depth, profile=PROFILE_PHYSICAL, seed=seed,
+                         accumulate=total > 0, want=())
+            denoiser.film(scene, out=img)
+            out = img
+        else:
+            raise ValueError(f"unknown method {method}")
+        torch.cuda.synchronize()
         spent += time.perf_counter() - t0
         total += step
-        err = rel_rmse(crop_of(img, crop), ref)
-        curve.append({"spp": total, "seconds": spent, "rel_rmse": err})
-        if err <= target:
+        err = corrected_rel_mse(crop_of(out, crop).cpu().numpy(), ref)
+        curve.append({"spp": total, "seconds": spent, "rel_mse": err})
+        if err <= target_mse:
             break
         step = total  # doubles the film each pass
-    hit = next((i for i, c in enumerate(curve) if c["rel_rmse"] <= target), None)
+    hit = next((i for i, c in enumerate(curve) if c["rel_mse"] <= target_mse), None)
     if hit is None:
         t_target = None
     elif hit == 0:
         t_target = curve[0]["seconds"]
     else:
         a, b = curve[hit - 1], curve[hit]
-        la, lb, lt = math.log(a["rel_rmse"]), math.log(b["rel_rmse"]), math.log(target)
+        la = math.log(max(a["rel_mse"], 1e-30))
+        lb = math.log(max(b["rel_mse"], 1e-30))
+        lt = math.log(target_mse)
         f = (la - lt) / (la - lb) if la != lb else 1.0
         t_target = a["seconds"] + f * (b["seconds"] - a["seconds"])
-    return {"curve": curve, "seconds_to_target": t_target, "target": target}
+    return {"method": method, "curve": curve, "seconds_to_target": t_target, "target": target,
+            "ref_noise": ref["noise"]}

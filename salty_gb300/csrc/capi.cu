@@ -288,6 +288,25 @@ salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* d, salty
     return SALTY_OK;
 }
 
+salty_status salty_scene_set_camera(salty_ctx* ctx, salty_scene* scene, const salty_camera* cam) {
+    if (!ctx) return SALTY_ERR_INVALID_ARG;
+    if (!scene || !cam) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "null scene or camera");
+    for (int i = 0; i < 3; ++i)
+        if (!std::isfinite(cam->pos[i]) || !std::isfinite(cam->target[i]) || !std::isfinite(cam->up[i]))
+            return ctx->err.fail(SALTY_ERR_INVALID_ARG, "camera has a non-finite component");
+    if (!(cam->fov > 0.0f) || !std::isfinite(cam->fov))
+        return ctx->err.fail(SALTY_ERR_INVALID_ARG, "camera fov must be positive");
+    salty::SceneConsts& k = scene->consts;
+    for (int i = 0; i < 3; ++i) {
+        k.cam_pos[i] = cam->pos[i];
+        k.cam_target[i] = cam->target[i];
+        k.cam_up[i] = cam->up[i];
+    }
+    k.cam_fov = cam->fov;
+    k.cam_near = cam->near_clip > 0 ? cam->near_clip : 1.0f;
+    return SALTY_OK;
+}
+
 void salty_scene_destroy(salty_ctx* ctx, salty_scene* scene) {
     if (ctx) {
         cudaSetDevice(ctx->device);

@@ -194,6 +194,8 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
                     salty_render_stats* stats);
 salty_status film_outputs(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
                           float* d_mean, float* d_var, uint8_t* d_srgb);
+salty_status film_features(salty_ctx* ctx, salty_scene* sc, float* d_mean, float* d_var, float* d_albedo,
+                           float* d_normal, float* d_depth);
 // post.cu
 salty_status tonemap_device(salty_ctx* ctx, int type, int w, int h, const float* d_rgb,
                             float* d_out, uint8_t* d_srgb, int ref_oetf, float* ave, float* mx);

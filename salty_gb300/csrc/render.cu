@@ -909,6 +909,24 @@ salty_status film_outputs(salty_ctx* ctx, salty_scene* sc, const salty_render_op
     return SALTY_OK;
 }
 
+// Mean, variance of the mean and mean first-hit features of the film, all on the device
+// (any output may be null).  The film must hold samples.
+salty_status film_features(salty_ctx* ctx, salty_scene* sc, float* d_mean, float* d_var, float* d_albedo,
+                           float* d_normal, float* d_depth) {
+    Film& F = sc->film;
+    const long long npx = (long long)F.width * F.height;
+    if (npx == 0 || F.samples == 0 || !F.aov.p) return ctx->err.fail(SALTY_ERR_NOT_BUILT, "the film is empty");
+    if (d_mean || d_var)
+        k_film_out<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(
+            F.fp64 ? nullptr : F.sum.p, F.fp64 ? nullptr : F.sumsq.p, F.fp64 ? F.sum64.p : nullptr,
+            F.fp64 ? F.sumsq64.p : nullptr, npx * 3, (double)F.samples, d_mean, d_var);
+    if (d_albedo || d_normal || d_depth)
+        k_aov_out<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(F.aov.p, npx, (double)F.samples, d_albedo, d_normal,
+                                                            d_depth);
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
 }  // namespace salty
 
 extern "C" salty_status salty_film_read(salty_ctx* ctx, salty_scene* sc, double* sum, double* sumsq,

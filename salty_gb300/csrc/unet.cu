@@ -1,14 +1,15 @@
 // unet.cu -- the learned denoiser: a 5-level U-Net trained and run by these kernels.
 //
 // The reference has an NLM filter (src/s3d_denoiser.cpp:19-95) and no learned denoiser;
-// this network is new.  Input: 10 features per pixel (log(1 + colour), first-hit albedo,
-// normal, 1/(1 + distance)), padded to 16 channels.  Architecture (NHWC, BF16 activations):
+// this network is new.  Input: 11 features per pixel (log(1 + colour), first-hit albedo,
+// normal, 1/(1 + distance), the colour's noise level), padded to 16 channels.  Architecture (NHWC, BF16 activations):
 //   enc: conv 16->32, 32->32 | pool | 32->48, 48->48 | pool | 48->64, 64->64 | pool |
 //        64->80, 80->80 | pool | 80->96
 //   dec: up + concat(96+80) -> 80 | up + concat(80+64) -> 64 | up + concat(64+48) -> 48 |
-//        up + concat(48+32) -> 32 | conv 32->8 (channels 0..2: log(1 + colour))
+//        up + concat(48+32) -> 32 | conv 32->8 (channels 0..2: a correction r of the input's
+//        log colour; the prediction is log(1 + colour) = x + r)
 // every conv 3x3, stride 1, zero padding, ReLU except the last; 2x2 max-pool; nearest 2x
-// up-sampling.  Loss: mean |out - log(1 + target)| (L1 in log space).  Optimiser: Adam.
+// up-sampling.  Loss: mean |x + r - log(1 + target)| (L1 in log space).  Optimiser: Adam.
 //
 // Convolutions are implicit GEMMs on the tensor cores (mma.sync m16n8k16, BF16 operands,
 // FP32 accumulation):
@@ -34,6 +35,7 @@ using bf16 = __nv_bfloat16;
 constexpr int kTileX = 16, kTileY = 8;          // output tile of one CTA
 constexpr int kHaloX = kTileX + 2, kHaloY = kTileY + 2;
 constexpr int kConvThreads = 128;
+constexpr int kFeatures = 11;                   // input floats per pixel
 
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
     asm volatile(
@@ -245,14 +247,15 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_wgrad(const bf16* __re
 }
 
 // ---------------------------------------------------------------- elementwise / layout
-// features (10 floats per pixel: colour, albedo, normal, 1/(1+t)) -> 16-channel BF16 input
+// features (kFeatures floats per pixel: colour, albedo, normal, 1/(1+t), noise level)
+// -> 16-channel BF16 input, colour as log(1 + colour)
 __global__ void k_prep_input(const float* __restrict__ f, long long npx, bf16* __restrict__ x) {
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
-        const float* s = f + p * 10;
+        const float* s = f + p * kFeatures;
         bf16* d = x + p * 16;
         for (int c = 0; c < 3; ++c) d[c] = __float2bfloat16(log1pf(fmaxf(s[c], 0.0f)));
-        for (int c = 3; c < 10; ++c) d[c] = __float2bfloat16(s[c]);
-        for (int c = 10; c < 16; ++c) d[c] = __float2bfloat16(0.0f);
+        for (int c = 3; c < kFeatures; ++c) d[c] = __float2bfloat16(s[c]);
+        for (int c = kFeatures; c < 16; ++c) d[c] = __float2bfloat16(0.0f);
     }
 }
 
@@ -324,16 +327,18 @@ __global__ void k_copy_channels(const bf16* __restrict__ src, int Cs, bf16* __re
     }
 }
 
-// L1 loss in log space on channels 0..2 of out [npx][8]; grad dout (FP32, zero elsewhere)
-__global__ void k_loss(const bf16* __restrict__ out, const float* __restrict__ target, long long npx,
-                       float* __restrict__ dout, double* __restrict__ loss_sum) {
+// L1 loss in log space on channels 0..2 of the prediction y = out + x (the network predicts
+// a correction of the input's log colour x, channels 0..2 of the 16-channel input [npx][16]);
+// grad dout [npx][8] (FP32, zero beyond channel 2)
+__global__ void k_loss(const bf16* __restrict__ out, const bf16* __restrict__ x, const float* __restrict__ target,
+                       long long npx, float* __restrict__ dout, double* __restrict__ loss_sum) {
     double s = 0.0;
     const float scale = 1.0f / (3.0f * (float)npx);
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
         for (int c = 0; c < 8; ++c) {
             float g = 0.0f;
             if (c < 3) {
-                const float y = __bfloat162float(out[p * 8 + c]);
+                const float y = __bfloat162float(out[p * 8 + c]) + __bfloat162float(x[p * 16 + c]);
                 const float t = log1pf(fmaxf(target[p * 3 + c], 0.0f));
                 const float d = y - t;
                 s += fabsf(d);
@@ -346,10 +351,13 @@ __global__ void k_loss(const bf16* __restrict__ out, const float* __restrict__ t
     if ((threadIdx.x & 31) == 0) atomicAdd(loss_sum, s);
 }
 
-// network output (log colour) -> linear colour
-__global__ void k_output(const bf16* __restrict__ out, long long npx, float* __restrict__ rgb) {
+// prediction (input log colour + network correction) -> linear colour
+__global__ void k_output(const bf16* __restrict__ out, const bf16* __restrict__ x, long long npx,
+                         float* __restrict__ rgb) {
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x)
-        for (int c = 0; c < 3; ++c) rgb[p * 3 + c] = fmaxf(expm1f(__bfloat162float(out[p * 8 + c])), 0.0f);
+        for (int c = 0; c < 3; ++c)
+            rgb[p * 3 + c] =
+                fmaxf(expm1f(__bfloat162float(out[p * 8 + c]) + __bfloat162float(x[p * 16 + c])), 0.0f);
 }
 
 // ReLU backward on a layer's output y: g = dy * (y > 0) in BF16 (the next GEMMs' operand),
@@ -441,6 +449,30 @@ __global__ void k_weights_to_bf16(const float* __restrict__ w, int Cout, int Cin
     }
 }
 
+// Film planes (W x H) -> network input (Wp x Hp, multiples of 16) with reflected borders:
+// colour, albedo, normal, 1/(1+t), noise level mean_c sqrt(var_c) / (1 + colour_c).
+__global__ void k_pack_features(const float* __restrict__ mean, const float* __restrict__ var,
+                                const float* __restrict__ albedo, const float* __restrict__ normal,
+                                const float* __restrict__ depth, int W, int H, int Wp, int Hp, float* __restrict__ f) {
+    const long long total = (long long)Wp * Hp;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % Wp), y = (int)(i / Wp);
+        const int sx = x < W ? x : max(2 * W - 2 - x, 0), sy = y < H ? y : max(2 * H - 2 - y, 0);
+        const long long p = (long long)sy * W + sx;
+        float* d = f + i * kFeatures;
+        float noise = 0.0f;
+        for (int c = 0; c < 3; ++c) {
+            const float m = mean[3 * p + c];
+            d[c] = m;
+            d[3 + c] = albedo[3 * p + c];
+            d[6 + c] = normal[3 * p + c];
+            noise += sqrtf(fmaxf(var[3 * p + c], 0.0f)) / (1.0f + fmaxf(m, 0.0f));
+        }
+        d[9] = depth[p];
+        d[10] = noise * (1.0f / 3.0f);
+    }
+}
+
 inline int gsz(long long n, int block = 256) {
     long long g = (n + block - 1) / block;
     return (int)(g > 4096 ? 4096 : (g < 1 ? 1 : g));
@@ -504,6 +536,7 @@ struct Unet {
     DevBuf<float> gbuf;
     long long act_off[T_COUNT], g_off[G_COUNT];
     DevBuf<float> io;       // device copies of host features / targets / outputs
+    DevBuf<float> film_ws;  // film planes, packed features and padded output of salty_denoise_unet
     DevBuf<double> loss;
 };
 
@@ -680,7 +713,7 @@ salty_status backward(salty_ctx* ctx, Unet& u, Fwd& F, const float* d_target, in
     SALTY_TRY_CUDA(ctx->err, cudaMemsetAsync(u.grads.p, 0, u.n_params * sizeof(float), st));
     SALTY_TRY_CUDA(ctx->err, u.loss.ensure(1));
     SALTY_TRY_CUDA(ctx->err, cudaMemsetAsync(u.loss.p, 0, sizeof(double), st));
-    k_loss<<<gsz(P0), 256, 0, st>>>(F.t[T_OUT], d_target, P0, G[G_OUT], u.loss.p);
+    k_loss<<<gsz(P0), 256, 0, st>>>(F.t[T_OUT], F.t[T_X], d_target, P0, G[G_OUT], u.loss.p);
     const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8, H4 = H / 16, W4 = W / 16;
     const long long P1 = P0 / 4, P2 = P0 / 16, P3 = P0 / 64, P4 = P0 / 256;
     auto to_f32 = [&](int cs, int off, int c, long long np, float* dst, int acc) {
@@ -788,11 +821,12 @@ salty_status salty_unet_create(salty_ctx* ctx, uint64_t seed, salty_unet** out) 
     };
     for (size_t li = 0; li < u.layers.size(); ++li) {
         const UnetLayer& L = u.layers[li];
-        const int real_cin = li == 0 ? 10 : L.cin;
-        const float bound = std::sqrt(6.0f / (9.0f * real_cin)) * (L.relu ? 1.0f : 0.5f);
+        const int real_cin = li == 0 ? kFeatures : L.cin;
+        // the output layer starts small: the initial prediction is close to the input
+        const float bound = std::sqrt(6.0f / (9.0f * real_cin)) * (L.relu ? 1.0f : 0.1f);
         for (long long i = 0; i < 9LL * L.cin * L.cout; ++i) {
             const int ci = (int)(i % L.cin);
-            p[L.w_off + i] = (li == 0 && ci >= 10) ? 0.0f : (2.0f * next() - 1.0f) * bound;
+            p[L.w_off + i] = (li == 0 && ci >= kFeatures) ? 0.0f : (2.0f * next() - 1.0f) * bound;
         }
     }
     cudaStream_t st = ctx->stream;
@@ -849,12 +883,12 @@ salty_status salty_unet_forward(salty_ctx* ctx, salty_unet* net, const float* fe
     const long long P0 = (long long)n * h * w;
     SALTY_TRY_CUDA(ctx->err, u.io.ensure((size_t)P0 * 16));
     const float* df;
-    SALTY_TRY(stage(ctx, u, features, P0 * 10, 0, &df));
+    SALTY_TRY(stage(ctx, u, features, P0 * kFeatures, 0, &df));
     Fwd F;
     SALTY_TRY(forward(ctx, u, df, n, h, w, F));
     const bool dev_out = is_device_ptr(out_rgb);
-    float* dout = dev_out ? out_rgb : u.io.p + P0 * 10;
-    k_output<<<gsz(P0), 256, 0, ctx->stream>>>(F.t[T_OUT], P0, dout);
+    float* dout = dev_out ? out_rgb : u.io.p + P0 * kFeatures;
+    k_output<<<gsz(P0), 256, 0, ctx->stream>>>(F.t[T_OUT], F.t[T_X], P0, dout);
     if (!dev_out)
         SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(out_rgb, dout, P0 * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(ctx->stream));
@@ -872,8 +906,8 @@ salty_status salty_unet_train_step(salty_ctx* ctx, salty_unet* net, const float*
     const long long P0 = (long long)n * h * w;
     SALTY_TRY_CUDA(ctx->err, u.io.ensure((size_t)P0 * 16));
     const float *df, *dt;
-    SALTY_TRY(stage(ctx, u, features, P0 * 10, 0, &df));
-    SALTY_TRY(stage(ctx, u, target_rgb, P0 * 3, P0 * 10, &dt));
+    SALTY_TRY(stage(ctx, u, features, P0 * kFeatures, 0, &df));
+    SALTY_TRY(stage(ctx, u, target_rgb, P0 * 3, P0 * kFeatures, &dt));
     Fwd F;
     SALTY_TRY(forward(ctx, u, df, n, h, w, F));
     double l = 0.0;
@@ -893,6 +927,39 @@ salty_status salty_unet_train_step(salty_ctx* ctx, salty_unet* net, const float*
     }
     SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(ctx->stream));
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+salty_status salty_denoise_unet(salty_ctx* ctx, salty_unet* net, salty_scene* scene, float* out_rgb) {
+    using namespace salty;
+    if (!ctx || !net || !scene || !out_rgb) return SALTY_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Unet& u = net->net;
+    const Film& Fm = scene->film;
+    const int W = Fm.width, H = Fm.height;
+    if ((long long)W * H == 0 || Fm.samples == 0) return ctx->err.fail(SALTY_ERR_NOT_BUILT, "the film is empty");
+    const int Wp = (W + 15) / 16 * 16, Hp = (H + 15) / 16 * 16;
+    SALTY_TRY(check_shape(ctx, 1, Hp, Wp));
+    const long long npx = (long long)W * H, npp = (long long)Wp * Hp;
+    // [mean 3 | var 3 | albedo 3 | normal 3 | depth 1] per film pixel, then features, then output
+    SALTY_TRY_CUDA(ctx->err, u.film_ws.ensure((size_t)(npx * 13 + npp * (kFeatures + 3))));
+    float* mean = u.film_ws.p;
+    float* var = mean + npx * 3;
+    float* alb = var + npx * 3;
+    float* nrm = alb + npx * 3;
+    float* dep = nrm + npx * 3;
+    float* feat = dep + npx;
+    float* outp = feat + npp * kFeatures;
+    SALTY_TRY(film_features(ctx, scene, mean, var, alb, nrm, dep));
+    k_pack_features<<<gsz(npp), 256, 0, ctx->stream>>>(mean, var, alb, nrm, dep, W, H, Wp, Hp, feat);
+    Fwd F;
+    SALTY_TRY(forward(ctx, u, feat, 1, Hp, Wp, F));
+    k_output<<<gsz(npp), 256, 0, ctx->stream>>>(F.t[T_OUT], F.t[T_X], npp, outp);
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    SALTY_TRY_CUDA(ctx->err, cudaMemcpy2DAsync(out_rgb, (size_t)W * 3 * sizeof(float), outp,
+                                               (size_t)Wp * 3 * sizeof(float), (size_t)W * 3 * sizeof(float), H,
+                                               cudaMemcpyDefault, ctx->stream));
+    SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(ctx->stream));
     return SALTY_OK;
 }
 

@@ -1,0 +1,242 @@
+"""Denoising front end: the learned U-Net (salty_unet_*) with NLM as its fallback, the
+renderer-generated training set, the training loop and the weight files.
+
+The reference's only denoiser is FilterNLM (src/s3d_denoiser.cpp:19-95), which
+salty_denoise_nlm extends with a 21x21 search window, 7x7 patches and a per-pixel
+variance-scaled filter strength.  The U-Net is new: it is trained here, on the GPU, by
+the library's own forward and backward kernels, on pairs the renderer generates --
+a crop window of a 1920x1080 frame of a seeded heightfield scene rendered at a few
+samples per pixel (input, with first-hit albedo, normal and depth) and, independently,
+at many (target).
+
+Training runs as a module:
+    python -m salty_gb300.denoiser train --out weights.npz [--scenes 16 --cams 4 ...]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+from . import PROFILE_PHYSICAL, Context, Unet, unet_features
+from . import scenes as _scenes
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_WEIGHTS = os.path.join(HERE, "weights", "unet_heightfield.npz")
+# the same network trained only on inputs of >= 1024 samples per pixel
+DEFAULT_HQ_WEIGHTS = os.path.join(HERE, "weights", "unet_heightfield_hq.npz")
+
+FRAME = (1920, 1080)
+MAX_DEPTH = 12
+
+
+# ---------------------------------------------------------------- weights
+def save_weights(net: Unet, path: str, meta: dict | None = None) -> None:
+    from . import UNET_LAYERS
+    os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    np.savez_compressed(path, params=net.params(), layers=np.array(UNET_LAYERS, np.int32),
+                        meta=np.array(json.dumps(meta or {})))
+
+
+def load_weights(net: Unet, path: str) -> dict:
+    from . import UNET_LAYERS
+    z = np.load(path)
+    if not np.array_equal(z["layers"], np.array(UNET_LAYERS, np.int32)):
+        raise ValueError(f"{path} holds weights of another architecture")
+    net.set_params(z["params"])
+    return json.loads(str(z["meta"]))
+
+
+# ---------------------------------------------------------------- inference
+def _pad16(a: np.ndarray) -> np.ndarray:
+    h, w = a.shape[:2]
+    ph, pw = (-h) % 16, (-w) % 16
+    if ph == 0 and pw == 0:
+        return np.ascontiguousarray(a)
+    return np.pad(a, ((0, ph), (0, pw), (0, 0)), mode="reflect")
+
+
+class Denoiser:
+    """denoise(mean, var, aov, spp) -> image.  Uses the U-Net when weights are available and
+    NLM (salty_denoise_nlm, 21x21 search, 7x7 patch) otherwise, or when method="nlm".  With
+    high-spp weights too, films of at least hq_from_spp samples per pixel use those."""
+
+    def __init__(self, ctx: Context, weights: str | None = DEFAULT_WEIGHTS, method: str = "auto",
+                 nlm_k: float = 0.45, hq_weights: str | None = DEFAULT_HQ_WEIGHTS, hq_from_spp: int = 1024):
+        self.ctx = ctx
+        self.nlm_k = nlm_k
+        self.net = self.hq = None
+        self.meta = self.hq_meta = {}
+        self.hq_from_spp = hq_from_spp
+        if method not in ("auto", "unet", "nlm"):
+            raise ValueError(f"unknown method {method}")
+        if method != "nlm" and weights and os.path.exists(weights):
+            self.net = Unet(ctx)
+            self.meta = load_weights(self.net, weights)
+            if hq_weights and os.path.exists(hq_weights):
+                self.hq = Unet(ctx)
+                self.hq_meta = load_weights(self.hq, hq_weights)
+        elif method == "unet":
+            raise FileNotFoundError(f"no U-Net weights at {weights}")
+        self.method = "unet" if self.net is not None else "nlm"
+
+    def pick(self, spp: int | None) -> Unet:
+        return self.hq if self.hq is not None and spp is not None and spp >= self.hq_from_spp else self.net
+
+    def __call__(self, mean, var=None, aov=None, spp: int | None = None):
+        h, w = mean.shape[:2]
+        if self.method == "nlm" or aov is None:
+            if var is None:
+                raise ValueError("NLM needs the per-pixel variance of the mean")
+            return self.ctx.nlm(mean, var, 10, 3, self.nlm_k)
+        if var is None:
+            raise ValueError("the U-Net needs the per-pixel variance of the mean")
+        f = _pad16(unet_features(mean, var, aov))
+        return self.pick(spp).forward(f)[:h, :w]
+
+    def film(self, scene, out=None):
+        """Denoised film of `scene` (the frame or window of its last render), on the device
+        when `out` is a device tensor."""
+        if self.method == "nlm":
+            raise RuntimeError("film denoising needs U-Net weights; use __call__ for NLM")
+        return self.pick(scene.film_samples).denoise_film(scene, out=out)
+
+    def close(self):
+        for n in (self.net, self.hq):
+            if n is not None:
+                n.close()
+        self.net = self.hq = None
+
+
+# ---------------------------------------------------------------- training data
+def random_view(rng: np.random.Generator) -> dict:
+    """A camera above the [0,1]^2 terrain looking down at a random azimuth."""
+    pos = np.array([rng.uniform(0.15, 0.85), rng.uniform(0.3, 0.55), rng.uniform(0.15, 0.85)])
+    az = rng.uniform(0.0, 2.0 * math.pi)
+    dist = rng.uniform(0.3, 0.8)
+    target = np.array([pos[0] + dist * math.sin(az), rng.uniform(0.0, 0.1), pos[2] + dist * math.cos(az)])
+    return {"pos": tuple(pos), "target": tuple(target), "up": (0.0, 1.0, 0.0),
+            "fov": 2.0 * math.tan(math.radians(rng.uniform(18.0, 32.0)))}
+
+
+def random_sun(rng: np.random.Generator) -> tuple:
+    el = math.radians(rng.uniform(15.0, 70.0))
+    az = rng.uniform(0.0, 2.0 * math.pi)
+    return (math.cos(el) * math.sin(az), math.sin(el), math.cos(el) * math.cos(az))
+
+
+def make_training_set(ctx: Context, seeds, cams: int = 4, crop: int = 256, levels=(4, 16, 64, 256, 1024, 4096),
+                      target_spp: int = 16384, grid: int = 2048, n_spheres: int = 4096, log=print):
+    """Returns (features (M, crop, crop, 11), targets (M, crop, crop, 3)) as float32 host arrays,
+    M = len(seeds) * cams * len(levels).  Each view renders the target film first (its own
+    seed), then one progressive input film whose mean and features are read at every level."""
+    W, H = FRAME
+    feats, targets = [], []
+    t0 = time.perf_counter()
+    for sd in seeds:
+        rng = np.random.default_rng(1_000_003 * int(sd) + 17)
+        sc = _scenes.heightfield(grid=grid, n_spheres=n_spheres, seed=int(sd))
+        sc["sun"]["dir"] = random_sun(rng)
+        s = _scenes.upload(ctx, sc)
+        s.build()
+        for _ in range(cams):
+            s.set_camera(**random_view(rng))
+            cr = (int(rng.integers(0, W - crop + 1)), int(rng.integers(0, H - crop + 1)), crop, crop)
+            tgt = s.render(W, H, target_spp, MAX_DEPTH, profile=PROFILE_PHYSICAL, seed=int(rng.integers(1 << 30)),
+                           want=("mean",), crop=cr)["mean"]
+            done, seed = 0, int(rng.integers(1 << 30))
+            for lv in levels:
+                r = s.render(W, H, lv - done, MAX_DEPTH, profile=PROFILE_PHYSICAL, seed=seed, accumulate=done > 0,
+                             want=("mean", "var"), crop=cr)
+                done = lv
+                feats.append(unet_features(r["mean"], r["var"], s.aov(crop, crop)))
+                targets.append(tgt)
+        s.close()
+        if log:
+            log(f"scene {sd}: {len(feats)} pairs, {time.perf_counter() - t0:.1f} s")
+    return np.stack(feats), np.stack(targets).astype(np.float32)
+
+
+# ---------------------------------------------------------------- training
+def train(net: Unet, feats, targets, steps: int, batch: int = 16, patch: int = 128, lr: float = 1e-3,
+          seed: int = 0, log=print, log_every: int = 250) -> list:
+    """Adam on random patches (with flips) of a device-resident training set; the learning
+    rate follows a cosine from lr to lr/20.  Returns the loss history."""
+    import torch
+    dev = torch.device("cuda")
+    F = torch.as_tensor(feats, device=dev)
+    T = torch.as_tensor(targets, device=dev)
+    M, S = F.shape[0], F.shape[1]
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    fb = torch.empty((batch, patch, patch, F.shape[-1]), device=dev)
+    tb = torch.empty((batch, patch, patch, 3), device=dev)
+    hist = []
+    t0 = time.perf_counter()
+    for it in range(steps):
+        idx = torch.randint(0, M, (batch,), generator=g)
+        oy = torch.randint(0, S - patch + 1, (batch,), generator=g)
+        ox = torch.randint(0, S - patch + 1, (batch,), generator=g)
+        flips = torch.randint(0, 4, (batch,), generator=g)
+        for b in range(batch):
+            i, y, x, fl = int(idx[b]), int(oy[b]), int(ox[b]), int(flips[b])
+            fp, tp = F[i, y:y + patch, x:x + patch], T[i, y:y + patch, x:x + patch]
+            dims = [d for d, bit in ((0, 1), (1, 2)) if fl & bit]
+            if dims:
+                fp, tp = fp.flip(dims), tp.flip(dims)
+            fb[b].copy_(fp)
+            tb[b].copy_(tp)
+        lr_t = lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * it / max(1, steps))))
+        hist.append(net.train_step(fb, tb, lr_t))
+        if log and (it + 1) % log_every == 0:
+            log(f"step {it + 1}: loss {np.mean(hist[-log_every:]):.5f} lr {lr_t:.2e} "
+                f"{time.perf_counter() - t0:.1f} s")
+    return hist
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description="Train the U-Net denoiser on renderer-generated pairs.")
+    ap.add_argument("cmd", choices=["train"])
+    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--hq-out", default=None, help="also train a network on inputs of >= --hq-min-level spp")
+    ap.add_argument("--hq-min-level", type=int, default=1024)
+    ap.add_argument("--scenes", type=int, default=16)
+    ap.add_argument("--cams", type=int, default=4)
+    ap.add_argument("--crop", type=int, default=256)
+    ap.add_argument("--target-spp", type=int, default=16384)
+    ap.add_argument("--levels", default="4,16,64,256,1024,4096,16384")
+    ap.add_argument("--steps", type=int, default=16000)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--patch", type=int, default=128)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=1)
+    a = ap.parse_args(argv)
+    levels = tuple(int(x) for x in a.levels.split(","))
+    ctx = Context(0)
+    # training scenes use seeds 1..n; the benchmark scene's seed (2026) stays held out
+    seeds = [s for s in range(1, a.scenes + 2) if s != 2026][:a.scenes]
+    t0 = time.perf_counter()
+    feats, targets = make_training_set(ctx, seeds, a.cams, a.crop, levels, a.target_spp)
+    t_data = time.perf_counter() - t0
+    runs = [(a.out, levels)]
+    if a.hq_out:
+        runs.append((a.hq_out, tuple(lv for lv in levels if lv >= a.hq_min_level)))
+    for path, lv in runs:
+        keep = np.array([levels[i % len(levels)] in lv for i in range(feats.shape[0])])
+        net = Unet(ctx, seed=a.seed)
+        t0 = time.perf_counter()
+        hist = train(net, feats[keep], targets[keep], a.steps, a.batch, a.patch, a.lr, seed=a.seed)
+        meta = {"scenes": seeds, "cams": a.cams, "crop": a.crop, "levels": lv, "target_spp": a.target_spp,
+                "pairs": int(keep.sum()), "steps": a.steps, "batch": a.batch, "patch": a.patch, "lr": a.lr,
+                "final_loss": float(np.mean(hist[-100:])), "data_seconds": round(t_data, 1),
+                "train_seconds": round(time.perf_counter() - t0, 1)}
+        save_weights(net, path, meta)
+        net.close()
+        print(json.dumps(meta))
+
+
+if __name__ == "__main__":
+    main()

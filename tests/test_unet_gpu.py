@@ -39,7 +39,7 @@ def test_parameter_count_and_init(net):
     p = net.params()
     assert np.all(np.isfinite(p))
     w0, b0 = split_params(p)[0]
-    assert np.all(w0[..., 10:] == 0) and np.all(b0 == 0)  # padded input channels unused
+    assert np.all(w0[..., 11:] == 0) and np.all(b0 == 0)  # padded input channels unused
 
 
 def test_forward_matches_oracle(net):
@@ -87,9 +87,10 @@ def test_adam_first_step(ctx):
 def test_training_reduces_loss(ctx):
     import salty_gb300
     net = salty_gb300.Unet(ctx, seed=6)
-    f, t = _batch(4, n=4, h=64, w=64)
+    f, _ = _batch(4, n=4, h=64, w=64)
+    t = np.ascontiguousarray(2.0 * f[..., 3:6])  # a function of the features the net can learn
     l0 = net.train_step(f, t, lr=0.0)
-    for _ in range(60):
+    for _ in range(400):
         l = net.train_step(f, t, lr=2e-3)
     assert l < 0.6 * l0, (l0, l)
     net.close()
@@ -110,6 +111,6 @@ def test_rejects_bad_shapes(net):
     import salty_gb300
     f, t = _batch(6, n=1, h=16, w=16)
     with pytest.raises(salty_gb300.SaltyError):
-        net.forward(np.zeros((1, 20, 16, 10), np.float32))
+        net.forward(np.zeros((1, 20, 16, 11), np.float32))
     with pytest.raises(ValueError):
         net.train_step(f, t[:, :8], lr=0.0)

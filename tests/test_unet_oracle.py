@@ -22,12 +22,13 @@ def _init(seed):
 
 
 def _features(rng, n, h, w):
-    f = np.empty((n, h, w, 10), np.float32)
+    f = np.empty((n, h, w, 11), np.float32)
     f[..., :3] = rng.lognormal(-1.0, 1.0, (n, h, w, 3))
     f[..., 3:6] = rng.uniform(0, 1, (n, h, w, 3))
     nr = rng.normal(size=(n, h, w, 3))
     f[..., 6:9] = nr / np.linalg.norm(nr, axis=-1, keepdims=True)
     f[..., 9] = rng.uniform(0.2, 1, (n, h, w))
+    f[..., 10] = rng.uniform(0.0, 0.5, (n, h, w))
     return f
 
 
