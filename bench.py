@@ -38,6 +38,11 @@ SOUP_SEED, RAY_SEED = 20260001, 20260002
 TMIN = 1e-4
 METRIC = "Mrays/s"
 CPU_SAMPLE = 131_072        # rays of the same stream timed on the host cores
+# DRAM bytes (read + write) per ray of the closest-hit k_trace launch, from the ncu capture
+# of the same kernel on the same soup at 4,194,304 rays (profiles/trace_closest_soup1m_4Mrays.md);
+# rays in and hits out dominate and scale with the ray count, so traffic per launch is this
+# figure times the rays of the launch.
+NCU_DRAM_BYTES_PER_RAY = (485.8e6 + 69.9e6) / 4_194_304
 
 
 def measured_peaks() -> dict:
@@ -190,6 +195,143 @@ def run_reference(args, ws, rank, local, pg):
     print(json.dumps(line), flush=True)
 
 
+def run_time_to_rmse(args):
+    """The 1080p heightfield scene (13.6M triangles, sky + sun disk, depth 12): seconds until
+    the image of each method reaches relRMSE <= target on a 256x256 window against an FP64
+    render of that window at --ref-spp samples (its own noise subtracted).  Methods: plain
+    progressive rendering, the U-Net on the film (salty_denoise_unet), NLM."""
+    import torch
+    import salty_gb300
+    from salty_gb300 import build as b
+    from salty_gb300 import convergence as cv
+    from salty_gb300 import denoiser as dn
+    from salty_gb300 import scenes
+    b.build()
+    W, H, D = 1920, 1080, 12
+    crop = (832, 412, 256, 256)
+    ctx = salty_gb300.Context(0)
+    t0 = time.perf_counter()
+    sc = scenes.heightfield()
+    s = scenes.upload(ctx, sc)
+    info = s.build()
+    setup_s = time.perf_counter() - t0
+    ref = cv.reference_image(s, W, H, crop, D, spp=args.ref_spp)
+    den = dn.Denoiser(ctx)
+    for _ in range(args.warmup):
+        s.render(W, H, 4, D, seed=3, want=())
+    # the C3 render configuration on its own: 1080p, 64 spp, depth 12
+    torch.cuda.synchronize()
+    r = s.render(W, H, 64, D, seed=5, want=())
+    render = {"spp": 64, "ms": r["ms"], "Mrays_s": r["rays"] / r["ms"] / 1e3, "Mpaths_s": r["paths"] / r["ms"] / 1e3,
+              "rays_per_path": r["rays"] / max(r["paths"], 1)}
+    res = {}
+    with ClockSampler(0) as clk:
+        for m in args.methods.split(","):
+            res[m] = cv.converge(s, W, H, crop, ref, D, args.target, method=m, ctx=ctx, denoiser=den,
+                                 max_spp=args.max_spp)
+    clocks = clk.summary()
+    plain = res.get("plain", {}).get("seconds_to_target")
+    best = res.get("unet", {}).get("seconds_to_target")
+    line = {
+        "metric": f"seconds to relRMSE <= {args.target} (1080p heightfield, 256x256 window vs FP64 {args.ref_spp}-spp)",
+        "value": best, "unit": "s", "n_gpus": 1, "higher_is_better": False, "dtype": "f32",
+        "data": "synthetic (seeded heightfield scene generated on the host)",
+        "config": {"workload": "1920x1080 heightfield: 2048^2 terrain + 4096 icospheres (13.6M triangles), sky 1.0 + "
+                               "sun disk, max depth 12, physical profile",
+                   "n_tris": int(sc["tri_pos"].shape[0]), "bvh_nodes": info["n_nodes"], "bvh_build_ms": info["build_ms"],
+                   "window": crop, "ref_spp": args.ref_spp, "ref_noise_rel_mse": ref["noise"],
+                   "ref_seconds": ref["seconds"], "setup_seconds": setup_s,
+                   "denoiser": {"method": den.method, "hq_from_spp": den.hq_from_spp,
+                                "weights": {k: v for k, v in den.meta.items() if k != "scenes"}}},
+        "plain_seconds": plain, "speedup_vs_plain": (plain / best) if plain and best else None,
+        "methods": {m: {"seconds_to_target": v["seconds_to_target"], "curve": v["curve"]} for m, v in res.items()},
+        "render_c3": render, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    den.close()
+    s.close()
+    ctx.close()
+
+
+def run_batch(args):
+    """256 seeded scenes of uneven size (soups and heightfields, 1e3..1e6 triangles,
+    64^2..512^2 pixels, 4/16/64 spp, depth 8, physical profile): one salty_render_batch per
+    step (tuning from salty_autotune) against one salty_render call per scene per step."""
+    import torch
+    import salty_gb300
+    from salty_gb300 import build as b
+    from salty_gb300 import scenes
+    b.build()
+    ctx = salty_gb300.Context(0)
+    t0 = time.perf_counter()
+    ss, opts, tris = [], [], 0
+    build_ms = 0.0
+    for i in range(args.scenes):
+        d, o = scenes.batch_scene(20260100 + i)
+        o["profile"] = salty_gb300.PROFILE_PHYSICAL
+        s = scenes.upload(ctx, d)
+        build_ms += s.build()["build_ms"]
+        tris += int(d["tri_pos"].shape[0])
+        ss.append(s)
+        opts.append(o)
+    setup_s = time.perf_counter() - t0
+    samples = sum(o["width"] * o["height"] * o["spp"] for o in opts)
+    default = ctx.tuning
+    t0 = time.perf_counter()
+    tuned, trial_ms = ctx.autotune(ss, opts, trial_spp=1)
+    tune_s = time.perf_counter() - t0
+
+    def batched():
+        return ctx.render_batch(ss, opts)
+
+    def per_scene():
+        tot = {"ms": 0.0, "rays": 0, "paths": 0}
+        for s, o in zip(ss, opts):
+            o2 = dict(o)
+            r = s.render(o2.pop("width"), o2.pop("height"), o2.pop("spp"), o2.pop("max_depth"), want=(), **o2)
+            for k in tot:
+                tot[k] += r[k]
+        return tot
+
+    res = {}
+    with ClockSampler(0) as clk:
+        for name, fn in (("batched", batched), ("per_scene", per_scene)):
+            for _ in range(args.warmup):
+                fn()
+            torch.cuda.synchronize()
+            rays = 0
+            t0 = time.perf_counter()
+            dev_ms = 0.0
+            for _ in range(args.steps):
+                r = fn()
+                rays += r["rays"]
+                dev_ms += r["ms"]
+            wall = time.perf_counter() - t0
+            res[name] = {"Mrays_s": rays / wall / 1e6, "wall_ms_per_step": wall * 1e3 / args.steps,
+                         "device_ms_per_step": dev_ms / args.steps, "rays_per_step": rays // args.steps,
+                         "wall_ms_per_scene": wall * 1e3 / args.steps / len(ss)}
+    clocks = clk.summary()
+    line = {
+        "metric": "Mrays/s (batched uneven renders)", "value": res["batched"]["Mrays_s"], "unit": "Mrays/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
+        "ms_per_step": res["batched"]["wall_ms_per_step"],
+        "data": "synthetic (seeded soups and heightfields generated on the host)",
+        "config": {"workload": f"{len(ss)} scenes, soup or heightfield, 1e3..1e6 triangles, 64^2..512^2 px, "
+                               "4/16/64 spp, depth 8, physical profile, one salty_render_batch per step",
+                   "scenes": len(ss), "triangles": tris, "samples_per_step": samples,
+                   "bvh_build_ms_total": build_ms, "setup_seconds": setup_s,
+                   "tuning": tuned, "default_tuning": default, "autotune_seconds": tune_s,
+                   "autotune_trial_ms": trial_ms},
+        "batched": res["batched"], "per_scene": res["per_scene"],
+        "speedup_vs_per_scene": res["batched"]["Mrays_s"] / res["per_scene"]["Mrays_s"],
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    for s in ss:
+        s.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -199,7 +341,19 @@ def main():
     ap.add_argument("--any-hit", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (smaller cases for profiling)")
+    ap.add_argument("--workload", default="traversal", choices=["traversal", "time-to-rmse", "batch"])
+    ap.add_argument("--scenes", type=int, default=256, help="batch: number of scenes")
+    ap.add_argument("--target", type=float, default=0.01, help="time-to-rmse: relRMSE target")
+    ap.add_argument("--ref-spp", type=int, default=65536, help="time-to-rmse: samples of the FP64 reference")
+    ap.add_argument("--max-spp", type=int, default=1 << 17, help="time-to-rmse: give up beyond this")
+    ap.add_argument("--methods", default="plain,unet", help="time-to-rmse: plain,unet,nlm")
     args = ap.parse_args()
+    if args.workload == "time-to-rmse":
+        run_time_to_rmse(args)
+        return
+    if args.workload == "batch":
+        run_batch(args)
+        return
     n_rays = args.rays
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     ws, rank, local, pg = dist_setup()
@@ -293,7 +447,9 @@ def main():
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": args.steps + e2e_kernels,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "frac": achieved / peaks["hbm_gbs"],
+                     "traffic": None if any_hit else NCU_DRAM_BYTES_PER_RAY * n_rays,
+                     "traffic_source": "ncu dram bytes per ray at 4,194,304 rays, scaled to the launch",
                      "peak_source": peaks["source"], "kernel_ms": launch_ms,
                      "bytes_per_ray": bytes_per_ray, "node_fetches_per_ray": n_node, "tri_fetches_per_ray": n_tri},
         "clocks": clocks,

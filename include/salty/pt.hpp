@@ -77,6 +77,18 @@ struct Material {
         return make(SALTY_GLASS, specular, emissive, ior, 0.f);
     }
     static Material GGX(Color3 specular, float roughness) { return make(SALTY_GGX, specular, {}, 1.5f, roughness); }
+    // MaterialFactory::CreatePhong / CreatePlastic (src/s3d_materialfactory.cpp:28-132)
+    static Material Phong(Color3 specular, float power, Color3 emissive = {}) {
+        Material r = make(SALTY_PHONG, specular, emissive, 1.5f, 0.f);
+        r.m.power = power;
+        return r;
+    }
+    static Material Plastic(Color3 diffuse, Color3 specular, float power, Color3 emissive = {}) {
+        Material r = make(SALTY_PLASTIC, diffuse, emissive, 1.5f, 0.f);
+        r.m.specular[0] = specular.x; r.m.specular[1] = specular.y; r.m.specular[2] = specular.z;
+        r.m.power = power;
+        return r;
+    }
 
 private:
     static Material make(int type, Color3 c, Color3 e, float ior, float rough) {

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define SALTY_ABI_VERSION 1
+#define SALTY_ABI_VERSION 2
 
 typedef enum salty_status {
     SALTY_OK = 0,
@@ -67,17 +67,20 @@ salty_status salty_host_alloc(salty_ctx* ctx, size_t bytes, void** out);
 void salty_host_free(salty_ctx* ctx, void* p);
 
 /* ---------------------------------------------------------------- scene */
-enum { SALTY_LAMBERT = 0, SALTY_MIRROR = 1, SALTY_GLASS = 2, SALTY_GGX = 3 };
+enum { SALTY_LAMBERT = 0, SALTY_MIRROR = 1, SALTY_GLASS = 2, SALTY_GGX = 3, SALTY_PHONG = 4, SALTY_PLASTIC = 5 };
 
 /* IMaterial (include/s3d_material.h:35-42): Lambert (src/s3d_lambert.cpp), Mirror
- * (src/s3d_mirror.cpp), Glass (src/s3d_glass.cpp) and a GGX conductor (the reference
- * only has SampleGGX, include/s3d_math.h:2985-2993). */
+ * (src/s3d_mirror.cpp), Glass (src/s3d_glass.cpp), Phong (src/s3d_phong.cpp: color is the
+ * specular colour), Plastic (src/s3d_plastic.cpp: color diffuse, specular, power) and a GGX
+ * conductor (the reference only has SampleGGX, include/s3d_math.h:2985-2993). */
 typedef struct salty_material {
     int32_t type;
     float color[3];     /* Lambert albedo / mirror, glass, GGX specular colour */
     float emission[3];
     float ior;          /* glass */
     float roughness;    /* GGX: alpha = roughness^2 */
+    float specular[3];  /* Plastic: specular colour (color is its diffuse colour) */
+    float power;        /* Phong, Plastic: lobe exponent (> 0) */
 } salty_material;
 
 /* PinholeCamera (include/s3d_camera.h:63-100).  fov is the reference's linear screen
@@ -201,6 +204,37 @@ typedef struct salty_render_stats {
  * outputs are host or device. */
 salty_status salty_render(salty_ctx* ctx, salty_scene* scene, const salty_render_opts* opts,
                           float* mean_rgb, float* var_rgb, uint8_t* srgb8, salty_render_stats* stats);
+
+/* Renders several scenes in one pass: their samples share the wavefront queues of one
+ * CUDA graph per wave, their BVHs are walked from one concatenated arena (built on the
+ * first call for a set of scenes and kept while none of them is rebuilt), and each scene's
+ * own film receives its samples exactly as salty_render with the same options would add
+ * them (identical values).  PathTracer::Run (src/s3d_pt.cpp:77-132) renders one scene per
+ * process; this is the batched form of it.  opts[i] belongs to scenes[i]; all scenes share
+ * one profile; a scene may appear once.  total (may be NULL): device time, samples, rays
+ * and paths of the whole batch.  Read each film with salty_render (spp = 0, accumulate = 1)
+ * or salty_film_read. */
+salty_status salty_render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salty_render_opts* opts,
+                                int32_t n, salty_render_stats* total);
+
+/* Launch shapes of the renderer and the traversal kernel (per context). */
+typedef struct salty_tuning {
+    int32_t trace_block;     /* traversal threads per block: 64, 128 or 256 */
+    int32_t trace_pool;      /* rays a warp takes from the queue per refill, 32..4096 */
+    int32_t trace_postpone;  /* fewest lanes that test a triangle group together, 1..32 */
+    int32_t shade_block;     /* shading threads per block, a multiple of 32 in 64..1024 */
+    int64_t wave_paths;      /* paths in flight per wave (queue capacity), 2^16..2^26 */
+} salty_tuning;
+salty_status salty_get_tuning(salty_ctx* ctx, salty_tuning* out);
+salty_status salty_set_tuning(salty_ctx* ctx, const salty_tuning* t);
+/* Picks the tuning for a render: trial renders of the batch with at most trial_spp samples
+ * per pixel, timed with CUDA events, one pass of coordinate descent over wave_paths,
+ * shade_block, trace_block, trace_pool and trace_postpone.  Leaves the best tuning set on
+ * the context (also copied to out and its trial time to best_ms; either may be NULL) and
+ * each film holding its last trial render: render with accumulate = 0 afterwards.  BVH node
+ * width (8) and traversal stack depth (from the BVH depth) are fixed by the build. */
+salty_status salty_autotune(salty_ctx* ctx, salty_scene* const* scenes, const salty_render_opts* opts, int32_t n,
+                            int32_t trial_spp, salty_tuning* out, float* best_ms);
 
 /* Film sums as stored (W*H*3 each): FP32 sum + Kahan compensation, or FP64 sums when the
  * film was rendered with fp64.  Arrays host or device; NULL skips. */

@@ -26,7 +26,7 @@ _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 _u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 
-LAMBERT, MIRROR, GLASS, GGX = 0, 1, 2, 3
+LAMBERT, MIRROR, GLASS, GGX, PHONG, PLASTIC = 0, 1, 2, 3, 4, 5
 PROFILE_COMPAT, PROFILE_PHYSICAL = 0, 1
 TM_REINHARD, TM_UNCHARTED2, TM_ACES = 0, 1, 2
 
@@ -39,7 +39,7 @@ def build(with_reference: bool | None = None) -> None:
 
 class _Mat(C.Structure):
     _fields_ = [("type", C.c_int), ("color", C.c_float * 3), ("emission", C.c_float * 3),
-                ("ior", C.c_float), ("roughness", C.c_float)]
+                ("ior", C.c_float), ("roughness", C.c_float), ("specular", C.c_float * 3), ("power", C.c_float)]
 
 
 class _Scene(C.Structure):
@@ -61,7 +61,8 @@ class _Opts(C.Structure):
 
 
 class _RefMat(C.Structure):
-    _fields_ = [("type", C.c_int), ("color", C.c_float * 3), ("emission", C.c_float * 3), ("ior", C.c_float)]
+    _fields_ = [("type", C.c_int), ("color", C.c_float * 3), ("emission", C.c_float * 3), ("ior", C.c_float),
+                ("specular", C.c_float * 3), ("power", C.c_float)]
 
 
 class _RefScene(C.Structure):
@@ -158,6 +159,8 @@ class Oracle:
             mats[i].emission = _f3(m.get("emission", (0, 0, 0)))
             mats[i].ior = m.get("ior", 1.5)
             mats[i].roughness = m.get("roughness", 0.3)
+            mats[i].specular = _f3(m.get("specular", (0.0, 0.0, 0.0)))
+            mats[i].power = m.get("power", 32.0)
         s = _Scene()
         s.tri_pos = pos.ctypes.data
         s.tri_nrm = nrm.ctypes.data if nrm is not None else None
@@ -284,10 +287,12 @@ class Reference:
         mat = np.ascontiguousarray(sc.tri_mat, np.int32)
         mats = (_RefMat * max(1, len(sc.materials)))()
         for i, m in enumerate(sc.materials):
-            mats[i].type = min(m.get("type", LAMBERT), GLASS) if m.get("type", 0) != GGX else LAMBERT
+            mats[i].type = LAMBERT if m.get("type", LAMBERT) == GGX else m.get("type", LAMBERT)
             mats[i].color = _f3(m.get("color", (0.75, 0.75, 0.75)))
             mats[i].emission = _f3(m.get("emission", (0, 0, 0)))
             mats[i].ior = m.get("ior", 1.5)
+            mats[i].specular = _f3(m.get("specular", (0.0, 0.0, 0.0)))
+            mats[i].power = m.get("power", 32.0)
         s = _RefScene()
         s.tri_pos, s.tri_nrm, s.tri_mat = pos.ctypes.data, nrm.ctypes.data, mat.ctypes.data
         s.n_tris = pos.shape[0]

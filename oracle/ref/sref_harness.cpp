@@ -40,6 +40,8 @@
 #include <s3d_bvh8.h>
 #include <s3d_mesh.h>
 #include <s3d_lambert.h>
+#include <s3d_phong.h>
+#include <s3d_plastic.h>
 #include <s3d_mirror.h>
 #include <s3d_glass.h>
 #include <s3d_camera.h>
@@ -148,10 +150,12 @@ private:
 extern "C" {
 
 struct sref_material {
-    int type;            // 0 Lambert, 1 Mirror, 2 Glass
-    float color[3];
+    int type;            // 0 Lambert, 1 Mirror, 2 Glass, 4 Phong, 5 Plastic
+    float color[3];      // Plastic: diffuse
     float emission[3];
     float ior;
+    float specular[3];   // Plastic
+    float power;         // Phong, Plastic
 };
 
 struct sref_scene_desc {
@@ -256,6 +260,9 @@ void* sref_scene_create(const sref_scene_desc* d, int width, int height) {
         IMaterial* mat = nullptr;
         if (sm.type == 1) mat = Mirror::Create(c, e);
         else if (sm.type == 2) mat = Glass::Create(c, sm.ior, e);
+        else if (sm.type == 4) mat = Phong::Create(c, sm.power, e);
+        else if (sm.type == 5)
+            mat = Plastic::Create(c, Color3(sm.specular[0], sm.specular[1], sm.specular[2]), sm.power, e);
         else mat = Lambert::Create(c, e);
         sc.mats.push_back(mat);
     }

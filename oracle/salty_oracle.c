@@ -528,6 +528,14 @@ static v3 compat_nee(const rscene* r, v3 pos, v3 n, const oracle_material* m, op
     return mk(0, 0, 0);
 }
 
+/* SamplePhong (include/s3d_math.h:2976-2982): cos(theta) = (1 - v)^(1 / (n + 1)) */
+static v3 sample_phong(float u, float v, float n) {
+    float p = k2Pi * u;
+    float ct = powf(1.0f - v, 1.0f / (n + 1.0f));
+    float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+    return mk(st * cosf(p), st * sinf(p), ct);
+}
+
 /* Lambert::Shade (src/s3d_lambert.cpp:64-86), Mirror::Shade (src/s3d_mirror.cpp:59-71),
  * Glass::Shade (src/s3d_glass.cpp:60-128). */
 static v3 compat_shade(const oracle_material* m, v3 in, v3 normal, opcg* rnd, v3* out, int* dice) {
@@ -560,6 +568,52 @@ static v3 compat_shade(const oracle_material* m, v3 in, v3 normal, opcg* rnd, v3
         if (opcg_f32(rnd) < P) { *out = refl; return scl(col, Re / (P * prob)); }
         *out = refr;
         return scl(col, Tr / ((1.0f - P) * prob));
+    }
+    if (m->type == ORACLE_PHONG) {
+        /* Phong::Shade (src/s3d_phong.cpp:65-88): a lobe around the mirror direction,
+         * weight specular * cos(out, n), dice against max(specular, 0.01) */
+        float u = opcg_f32(rnd), v = opcg_f32(rnd);
+        v3 s = sample_phong(u, v, m->power);
+        v3 w = safe_unit(reflect(in, nm));
+        v3 t, b;
+        tangent_space(w, &t, &b);
+        v3 dir = safe_unit(add(add(scl(t, s.x), scl(b, s.y)), scl(w, s.z)));
+        float cosine = fabsf(dot(dir, nm));
+        *out = dir;
+        float thr = fmaxf(fmaxf(fmaxf(m->color[0], m->color[1]), m->color[2]), 0.01f);
+        *dice = opcg_f32(rnd) >= thr;
+        return scl(col, cosine);
+    }
+    if (m->type == ORACLE_PLASTIC) {
+        /* Plastic::Shade (src/s3d_plastic.cpp:71-142): Schlick R with R0 = 0.5 picks the
+         * diffuse branch with P = (R + 0.5) / 2 and weights it R / P (uniform hemisphere),
+         * the Phong branch (1 - R) / (1 - P) * cos; the specular dice threshold is derived
+         * from the diffuse one (src/s3d_plastic.cpp:34-37) */
+        float cosine = fabsf(dot(normal, in));
+        float t1 = 1.0f - cosine;
+        float R = 0.5f + 0.5f * t1 * t1 * t1 * t1 * t1;
+        float P = (R + 0.5f) / 2.0f;
+        float thr0 = fmaxf(fmaxf(fmaxf(m->color[0], m->color[1]), m->color[2]), 0.01f);
+        if (opcg_f32(rnd) <= P) {
+            v3 t, b;
+            tangent_space(nm, &t, &b);
+            float u = opcg_f32(rnd), v = opcg_f32(rnd);
+            float rr = sqrtf(1.0f - u * u), p = k2Pi * v;
+            v3 s = mk(rr * cosf(p), rr * sinf(p), u);
+            *out = safe_unit(add(add(scl(t, s.x), scl(b, s.y)), scl(nm, s.z)));
+            *dice = opcg_f32(rnd) >= thr0;
+            return scl(col, R / P);
+        }
+        float u = opcg_f32(rnd), v = opcg_f32(rnd);
+        v3 s = sample_phong(u, v, m->power);
+        v3 w = safe_unit(reflect(in, nm));
+        v3 t, b;
+        tangent_space(w, &t, &b);
+        v3 dir = safe_unit(add(add(scl(t, s.x), scl(b, s.y)), scl(w, s.z)));
+        float dots = dot(dir, nm);
+        *out = dir;
+        *dice = opcg_f32(rnd) >= fmaxf(thr0, 0.01f);
+        return scl(ld3(m->specular), dots * (1.0f - R) / (1.0f - P));
     }
     /* Lambert (GGX falls back to Lambert in the compat profile: the reference has no GGX
      * material) */
@@ -604,7 +658,8 @@ static v3 compat_radiance(const rscene* r, v3 o, v3 d, int max_bounce, opcg* rnd
  * MIS, NEE to a delta sun, constant sky on escape, Russian roulette from rr_depth with
  * survival min(0.95, max W).  Ray epsilon 1e-4.  Random numbers per (pixel, sample) stream,
  * consumed in this order: jitter x, y; per vertex: light point u, v (non-delta, light
- * present); BSDF (Lambert 2, glass 1, GGX 2, mirror 0); RR 1 (depth >= rr_depth). */
+ * present); BSDF (Lambert 2, glass 1, GGX 2, mirror 0, Phong 2, plastic 3); RR 1
+ * (depth >= rr_depth). */
 static const float kEps = 1e-4f;
 
 static float ggx_d(float nh, float a2) {
@@ -619,10 +674,42 @@ static v3 schlick(v3 f0, float c) {
     return mk(f0.x + (1.0f - f0.x) * m5, f0.y + (1.0f - f0.y) * m5, f0.z + (1.0f - f0.z) * m5);
 }
 
+/* Normalised Phong lobe around the mirror direction r of wo (physical profile):
+ * f = (n + 2) / (2 pi) cos^n(r, wi); sampled with pdf (n + 1) / (2 pi) cos^n(r, wi). */
+static float phong_lobe(v3 n, v3 wo, v3 wi, float power, float* pdf) {
+    v3 r = reflect(neg(wo), n);
+    float c = dot(r, wi);
+    if (c <= 0.0f) { *pdf = 0.0f; return 0.0f; }
+    float cn = powf(c, power);
+    *pdf = (power + 1.0f) / k2Pi * cn;
+    return (power + 2.0f) / k2Pi * cn;
+}
+/* Plastic (physical profile): Schlick F with R0 = 0.04 at the outgoing angle splits
+ * F * specular * Phong lobe + (1 - F) * diffuse / pi; sampled as a one-sample mixture that
+ * takes the lobe with probability Ps = clamp(F, 0.1, 0.9). */
+static float plastic_fresnel(float cos_o) {
+    float m = 1.0f - fmaxf(cos_o, 0.0f), m2 = m * m;
+    return 0.04f + 0.96f * m2 * m2 * m;
+}
+static float plastic_ps(float F) { return fminf(0.9f, fmaxf(0.1f, F)); }
+
 /* f(wo, wi) without the cosine and the BSDF-sampling pdf, for NEE. */
 static v3 phys_eval(const oracle_material* m, v3 n, v3 wo, v3 wi, float* pdf) {
     v3 col = mk(m->color[0], m->color[1], m->color[2]);
     float ni = dot(n, wi);
+    if (m->type == ORACLE_PHONG) {
+        float lp;
+        float f = phong_lobe(n, wo, wi, m->power, &lp);
+        *pdf = lp;
+        return scl(col, f);
+    }
+    if (m->type == ORACLE_PLASTIC) {
+        float lp;
+        float fl = phong_lobe(n, wo, wi, m->power, &lp);
+        float F = plastic_fresnel(dot(n, wo)), ps = plastic_ps(F);
+        *pdf = ps * lp + (1.0f - ps) * fmaxf(ni, 0.0f) / kPi;
+        return add(scl(ld3(m->specular), F * fl), scl(col, (1.0f - F) / kPi));
+    }
     if (m->type == ORACLE_GGX) {
         float a = m->roughness * m->roughness, a2 = a * a;
         float no = dot(n, wo);
@@ -749,6 +836,33 @@ static v3 phys_radiance(const rscene* r, v3 o, v3 d, const oracle_render_opts* o
             v3 F = schlick(col, oh);
             weight = scl(F, G * oh / (no * nh));
             pdf = ggx_d(nh, a2) * nh / (4.0f * oh);
+        } else if (m->type == ORACLE_PHONG || m->type == ORACLE_PLASTIC) {
+            /* random numbers: branch 1 (plastic only), direction 2 */
+            int lobe = 1;
+            float F = 0.0f, ps = 1.0f;
+            if (m->type == ORACLE_PLASTIC) {
+                F = plastic_fresnel(dot(nsf, wo));
+                ps = plastic_ps(F);
+                lobe = opcg_f32(rnd) < ps;
+            }
+            float r1 = opcg_f32(rnd), r2 = opcg_f32(rnd);
+            v3 t, b;
+            if (lobe) {
+                v3 s = sample_phong(r1, r2, m->power);
+                v3 rdir = reflect(d, nsf);
+                tangent_space(rdir, &t, &b);
+                wi = safe_unit(add(add(scl(t, s.x), scl(b, s.y)), scl(rdir, s.z)));
+            } else {
+                float rr = sqrtf(r1), ph = k2Pi * r2;
+                float z = sqrtf(fmaxf(0.0f, 1.0f - r1));
+                tangent_space(nsf, &t, &b);
+                wi = safe_unit(add(add(scl(t, rr * cosf(ph)), scl(b, rr * sinf(ph))), scl(nsf, z)));
+            }
+            float ni = dot(nsf, wi);
+            if (ni <= 0.0f || dot(ngf, wi) <= 0.0f) break;
+            v3 f = phys_eval(m, nsf, wo, wi, &pdf);
+            if (!(pdf > 0.0f)) break;
+            weight = scl(f, ni / pdf);
         } else {
             float r1 = opcg_f32(rnd), r2 = opcg_f32(rnd);
             float rr = sqrtf(r1), ph = k2Pi * r2;

@@ -47,7 +47,8 @@ void  oracle_trace(void* bvh, const float* rays8, long n, int mode, int any_hit,
                    int32_t* ids, float* t, float* u, float* v);
 
 /* ---- rendering ---- */
-enum { ORACLE_LAMBERT = 0, ORACLE_MIRROR = 1, ORACLE_GLASS = 2, ORACLE_GGX = 3 };
+enum { ORACLE_LAMBERT = 0, ORACLE_MIRROR = 1, ORACLE_GLASS = 2, ORACLE_GGX = 3, ORACLE_PHONG = 4,
+       ORACLE_PLASTIC = 5 };
 enum { ORACLE_PROFILE_COMPAT = 0, ORACLE_PROFILE_PHYSICAL = 1 };
 
 typedef struct {
@@ -56,6 +57,8 @@ typedef struct {
     float emission[3];
     float ior;
     float roughness;
+    float specular[3];  /* Plastic: specular colour (color is the diffuse one) */
+    float power;        /* Phong / Plastic: lobe exponent */
 } oracle_material;
 
 typedef struct {

@@ -27,7 +27,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libsalty_gpu.so")
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_QUEUE_OVERFLOW, ERR_CANCELLED, ERR_NOT_BUILT, ERR_CAPACITY = range(9)
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT", 5: "QUEUE_OVERFLOW",
                 6: "CANCELLED", 7: "NOT_BUILT", 8: "CAPACITY"}
-LAMBERT, MIRROR, GLASS, GGX = 0, 1, 2, 3
+LAMBERT, MIRROR, GLASS, GGX, PHONG, PLASTIC = 0, 1, 2, 3, 4, 5
 TRACE_ANY_HIT, TRACE_WATERTIGHT, TRACE_COUNTERS = 1, 2, 4
 PROFILE_COMPAT, PROFILE_PHYSICAL = 0, 1
 TM_NONE, TM_REINHARD, TM_UNCHARTED2, TM_ACES = -1, 0, 1, 2
@@ -41,7 +41,7 @@ class SaltyError(RuntimeError):
 
 class Material(C.Structure):
     _fields_ = [("type", C.c_int32), ("color", C.c_float * 3), ("emission", C.c_float * 3),
-                ("ior", C.c_float), ("roughness", C.c_float)]
+                ("ior", C.c_float), ("roughness", C.c_float), ("specular", C.c_float * 3), ("power", C.c_float)]
 
 
 class Camera(C.Structure):
@@ -84,6 +84,14 @@ class RenderStats(C.Structure):
     _fields_ = [("ms", C.c_double), ("samples", C.c_int64), ("rays", C.c_int64), ("paths", C.c_int64)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("trace_block", C.c_int32), ("trace_pool", C.c_int32), ("trace_postpone", C.c_int32),
+                ("shade_block", C.c_int32), ("wave_paths", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # Every extern "C" symbol declared in include/salty_gpu.h.
 EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_abi_version", "salty_ctx_cancel",
            "salty_host_alloc", "salty_host_free", "salty_scene_upload", "salty_scene_destroy", "salty_bvh_build",
@@ -91,7 +99,8 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_denoise_nlm_ref", "salty_denoise_nlm", "salty_microbench_soup", "salty_microbench_rays",
            "salty_tonemap_noalloc", "salty_film_aov", "salty_unet_create", "salty_unet_destroy",
            "salty_unet_param_count", "salty_unet_get_params", "salty_unet_set_params", "salty_unet_forward",
-           "salty_unet_train_step", "salty_scene_set_camera", "salty_denoise_unet"]
+           "salty_unet_train_step", "salty_scene_set_camera", "salty_denoise_unet", "salty_render_batch",
+           "salty_get_tuning", "salty_set_tuning", "salty_autotune"]
 
 _lib = None
 
@@ -136,6 +145,10 @@ def lib() -> C.CDLL:
         "salty_unet_forward": (i32, [vp, vp, vp, i32, i32, i32, vp]),
         "salty_unet_train_step": (i32, [vp, vp, vp, vp, i32, i32, i32, f32, C.POINTER(f32)]),
         "salty_denoise_unet": (i32, [vp, vp, vp, vp]),
+        "salty_render_batch": (i32, [vp, vp, vp, i32, C.POINTER(RenderStats)]),
+        "salty_get_tuning": (i32, [vp, C.POINTER(Tuning)]),
+        "salty_set_tuning": (i32, [vp, C.POINTER(Tuning)]),
+        "salty_autotune": (i32, [vp, vp, vp, i32, i32, C.POINTER(Tuning), C.POINTER(f32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -179,6 +192,14 @@ def microbench_rays(seed: int, n: int, tmin: float = 1e-4, out: np.ndarray | Non
     if st:
         raise SaltyError(st, "microbench_rays")
     return out
+
+
+def render_opts(width: int, height: int, spp: int, max_depth: int, rr_depth: int = 3,
+                profile: int = PROFILE_PHYSICAL, seed: int = 1, accumulate: bool = False, fp64: bool = False,
+                tonemap: int = TM_REINHARD, ref_oetf: bool = True, crop: tuple | None = None) -> RenderOpts:
+    cx, cy, cw, ch = crop if crop else (0, 0, 0, 0)
+    return RenderOpts(width, height, spp, max_depth, rr_depth, profile, seed, int(accumulate), int(fp64), tonemap,
+                      int(ref_oetf), cx, cy, cw, ch)
 
 
 class Context:
@@ -240,6 +261,8 @@ class Context:
             mats[i].emission = _f3(m.get("emission", (0, 0, 0)))
             mats[i].ior = float(m.get("ior", 1.5))
             mats[i].roughness = float(m.get("roughness", 0.3))
+            mats[i].specular = _f3(m.get("specular", (0.0, 0.0, 0.0)))
+            mats[i].power = float(m.get("power", 32.0))
         d = SceneDesc()
         d.tri_pos, d.tri_nrm, d.tri_mat = _ptr(tri_pos), _ptr(tri_nrm), _ptr(tri_mat)
         d.n_tris = n
@@ -261,6 +284,50 @@ class Context:
         h = C.c_void_p()
         self.check(lib().salty_scene_upload(self.h, C.byref(d), C.byref(h)), "scene_upload")
         return Scene(self, h, n)
+
+    @staticmethod
+    def _batch_args(scenes, opts):
+        if len(scenes) != len(opts) or not scenes:
+            raise ValueError("one options dict per scene")
+        arr = (C.c_void_p * len(scenes))(*[sc.h.value for sc in scenes])
+        ro = (RenderOpts * len(scenes))(*[render_opts(**o) for o in opts])
+        return arr, ro
+
+    def render_batch(self, scenes, opts) -> dict:
+        """One salty_render_batch over scenes (Scene objects) with per-scene options (dicts of
+        render_opts' arguments).  Each scene's film receives its samples; returns the batch's
+        device time, samples, rays and paths."""
+        arr, ro = self._batch_args(scenes, opts)
+        st = RenderStats()
+        self.check(lib().salty_render_batch(self.h, arr, ro, len(scenes), C.byref(st)), "render_batch")
+        for sc, o in zip(scenes, opts):
+            n = C.c_int64()
+            self.check(lib().salty_film_read(self.h, sc.h, None, None, C.byref(n)), "film_read")
+            sc.film_samples = n.value
+            crop = o.get("crop")
+            sc.film_shape = (crop[3], crop[2]) if crop else (o["height"], o["width"])
+        return {"ms": st.ms, "samples": st.samples, "rays": st.rays, "paths": st.paths}
+
+    @property
+    def tuning(self) -> dict:
+        t = Tuning()
+        self.check(lib().salty_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return t.as_dict()
+
+    @tuning.setter
+    def tuning(self, d: dict) -> None:
+        t = Tuning()
+        lib().salty_get_tuning(self.h, C.byref(t))
+        for k, v in d.items():
+            setattr(t, k, int(v))
+        self.check(lib().salty_set_tuning(self.h, C.byref(t)), "set_tuning")
+
+    def autotune(self, scenes, opts, trial_spp: int = 1) -> tuple[dict, float]:
+        """salty_autotune: sets and returns the fastest tuning for this batch and its trial ms."""
+        arr, ro = self._batch_args(scenes, opts)
+        t, ms = Tuning(), C.c_float()
+        self.check(lib().salty_autotune(self.h, arr, ro, len(scenes), trial_spp, C.byref(t), C.byref(ms)), "autotune")
+        return t.as_dict(), ms.value
 
     def tonemap(self, img, type_: int = TM_REINHARD, srgb: bool = True, ref_oetf: bool = True):
         img = img if hasattr(img, "data_ptr") else np.ascontiguousarray(img, np.float32)
@@ -353,8 +420,8 @@ class Scene:
         tonemapped sRGB8 (host arrays, or the device tensors given in `out`).  crop = (x, y, w, h)
         renders that window of the width x height frame with the frame's own rays."""
         cx, cy, cw, ch = crop if crop else (0, 0, 0, 0)
-        o = RenderOpts(width, height, spp, max_depth, rr_depth, profile, seed, int(accumulate), int(fp64),
-                       tonemap, int(ref_oetf), cx, cy, cw, ch)
+        o = render_opts(width, height, spp, max_depth, rr_depth, profile, seed, accumulate, fp64, tonemap, ref_oetf,
+                        crop)
         fh, fw = (ch, cw) if crop else (height, width)
         self.film_shape = (fh, fw)
         out = out or {}
@@ -367,6 +434,13 @@ class Scene:
         self.film_samples = int(st.samples)
         return {"mean": mean, "var": var, "srgb": s8, "ms": st.ms, "samples": st.samples, "rays": st.rays,
                 "paths": st.paths}
+
+    def read(self, width: int, height: int, crop: tuple | None = None, fp64: bool = False,
+             want=("mean", "var"), out: dict | None = None, **kw) -> dict:
+        """The film's mean / variance / sRGB8 without adding samples (salty_render with spp 0);
+        width, height, crop and fp64 must be those the film was rendered with."""
+        return self.render(width, height, 0, kw.pop("max_depth", 1), accumulate=True, fp64=fp64, crop=crop,
+                           want=want, out=out, **kw)
 
     def set_camera(self, pos, target, up=(0.0, 1.0, 0.0), fov: float = 1.0, near: float = 1.0) -> None:
         c = Camera()

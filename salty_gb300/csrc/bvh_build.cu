@@ -16,6 +16,8 @@
 #include <cfloat>
 #include <cmath>
 
+#include <atomic>
+
 #include "internal.h"
 
 namespace salty {
@@ -681,8 +683,11 @@ salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& 
     cudaEventElapsedTime(&ms, e0, e1);
     if (hc->ntris != n) return E.fail(SALTY_ERR_CUDA, "collapse wrote %d of %d triangles", hc->ntris, n);
     sc->bvh.n_nodes = hc->n8;
+    sc->bvh.n_tris = n;
     sc->bvh.depth = depth8;
     sc->bvh.built = true;
+    static std::atomic<uint64_t> builds{0};
+    sc->bvh.generation = ++builds;  // unique in the process
     sc->bvh.info.n_nodes = hc->n8;
     sc->bvh.info.n_binary = n_binary;
     sc->bvh.info.depth = depth8;

@@ -81,6 +81,24 @@ struct Pcg {
 
 }  // namespace
 
+namespace salty {
+salty_status check_render_opts(salty_ctx* ctx, const salty_scene* sc, const salty_render_opts* o) {
+    auto& E = ctx->err;
+    if (!sc || !o) return E.fail(SALTY_ERR_INVALID_ARG, "null scene or options");
+    if (o->width <= 0 || o->height <= 0 || o->spp < 0 || o->max_depth < 1 || o->max_depth > 0xffff)
+        return E.fail(SALTY_ERR_INVALID_ARG, "bad render size/spp/depth");
+    if ((int64_t)o->width * o->height > (1ll << 28)) return E.fail(SALTY_ERR_CAPACITY, "image too large");
+    const bool cropped = o->crop_w > 0 || o->crop_h > 0 || o->crop_x != 0 || o->crop_y != 0;
+    if (cropped && (o->crop_w <= 0 || o->crop_h <= 0 || o->crop_x < 0 || o->crop_y < 0 ||
+                    (int64_t)o->crop_x + o->crop_w > o->width || (int64_t)o->crop_y + o->crop_h > o->height))
+        return E.fail(SALTY_ERR_INVALID_ARG, "crop window outside the frame");
+    if (o->profile != SALTY_PROFILE_COMPAT && o->profile != SALTY_PROFILE_PHYSICAL)
+        return E.fail(SALTY_ERR_INVALID_ARG, "bad profile");
+    if (!sc->bvh.built) return E.fail(SALTY_ERR_NOT_BUILT, "salty_bvh_build has not been called");
+    return SALTY_OK;
+}
+}  // namespace salty
+
 extern "C" {
 
 int salty_abi_version(void) { return SALTY_ABI_VERSION; }
@@ -186,13 +204,19 @@ salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* d, salty
     std::vector<GpuMaterial> mats(d->n_mats + 1);
     for (int i = 0; i < d->n_mats; ++i) {
         const salty_material& m = d->mats[i];
-        if (m.type < SALTY_LAMBERT || m.type > SALTY_GGX) return fail(E.fail(SALTY_ERR_INVALID_ARG, "material %d: bad type", i));
-        GpuMaterial g;
+        if (m.type < SALTY_LAMBERT || m.type > SALTY_PLASTIC)
+            return fail(E.fail(SALTY_ERR_INVALID_ARG, "material %d: bad type", i));
+        if ((m.type == SALTY_PHONG || m.type == SALTY_PLASTIC) && !(m.power > 0.0f && m.power < 1e6f))
+            return fail(E.fail(SALTY_ERR_INVALID_ARG, "material %d: power must be in (0, 1e6)", i));
+        GpuMaterial g{};
         g.type = m.type;
         for (int c = 0; c < 3; ++c) { g.color[c] = m.color[c]; g.emission[c] = m.emission[c]; }
         g.ior = m.ior > 0 ? m.ior : 1.5f;
         g.roughness = m.roughness;
-        // Lambert::Lambert (src/s3d_lambert.cpp:22-31)
+        for (int c = 0; c < 3; ++c) g.specular[c] = m.specular[c];
+        g.power = m.power;
+        // Lambert::Lambert (src/s3d_lambert.cpp:22-31), Phong::Phong (src/s3d_phong.cpp:22-31),
+        // Plastic::Plastic (src/s3d_plastic.cpp:22-37): max(colour, 0.01)
         g.rr_threshold = std::max(std::max(std::max(m.color[0], m.color[1]), m.color[2]), 0.01f);
         mats[i] = g;
     }
@@ -438,21 +462,13 @@ salty_status salty_last_trace_stats(const salty_ctx* ctx, salty_trace_stats* out
 }
 
 // ---------------------------------------------------------------- render / post
+
 salty_status salty_render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts* o, float* mean_rgb,
                           float* var_rgb, uint8_t* srgb8, salty_render_stats* stats) {
     if (!ctx) return SALTY_ERR_INVALID_ARG;
     auto& E = ctx->err;
-    if (!sc || !o) return E.fail(SALTY_ERR_INVALID_ARG, "null scene or options");
-    if (o->width <= 0 || o->height <= 0 || o->spp < 0 || o->max_depth < 1)
-        return E.fail(SALTY_ERR_INVALID_ARG, "bad render size/spp/depth");
-    if ((int64_t)o->width * o->height > (1ll << 28)) return E.fail(SALTY_ERR_CAPACITY, "image too large");
+    SALTY_TRY(check_render_opts(ctx, sc, o));
     const bool cropped = o->crop_w > 0 || o->crop_h > 0 || o->crop_x != 0 || o->crop_y != 0;
-    if (cropped && (o->crop_w <= 0 || o->crop_h <= 0 || o->crop_x < 0 || o->crop_y < 0 ||
-                    (int64_t)o->crop_x + o->crop_w > o->width || (int64_t)o->crop_y + o->crop_h > o->height))
-        return E.fail(SALTY_ERR_INVALID_ARG, "crop window outside the frame");
-    if (o->profile != SALTY_PROFILE_COMPAT && o->profile != SALTY_PROFILE_PHYSICAL)
-        return E.fail(SALTY_ERR_INVALID_ARG, "bad profile");
-    if (!sc->bvh.built) return E.fail(SALTY_ERR_NOT_BUILT, "salty_bvh_build has not been called");
     cudaSetDevice(ctx->device);
     ctx->cancel = 0;
     salty_render_stats st{};
@@ -478,6 +494,132 @@ salty_status salty_render(salty_ctx* ctx, salty_scene* sc, const salty_render_op
 }
 
 salty_status salty_film_read(salty_ctx* ctx, salty_scene* sc, double* sum, double* sumsq, int64_t* samples);
+
+salty_status salty_render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salty_render_opts* opts,
+                                int32_t n, salty_render_stats* total) {
+    if (!ctx) return SALTY_ERR_INVALID_ARG;
+    auto& E = ctx->err;
+    if (!scenes || !opts || n < 1) return E.fail(SALTY_ERR_INVALID_ARG, "empty batch");
+    for (int i = 0; i < n; ++i) {
+        SALTY_TRY(check_render_opts(ctx, scenes[i], &opts[i]));
+        for (int j = 0; j < i; ++j)
+            if (scenes[j] == scenes[i]) return E.fail(SALTY_ERR_INVALID_ARG, "scene %d appears twice in the batch", i);
+    }
+    cudaSetDevice(ctx->device);
+    ctx->cancel = 0;
+    return render_batch(ctx, scenes, opts, n, total);
+}
+
+salty_status salty_get_tuning(salty_ctx* ctx, salty_tuning* out) {
+    if (!ctx || !out) return SALTY_ERR_INVALID_ARG;
+    out->trace_block = ctx->tune.trace.block;
+    out->trace_pool = ctx->tune.trace.pool;
+    out->trace_postpone = ctx->tune.trace.postpone;
+    out->shade_block = ctx->tune.shade_block;
+    out->wave_paths = ctx->tune.wave_paths;
+    return SALTY_OK;
+}
+
+salty_status salty_set_tuning(salty_ctx* ctx, const salty_tuning* t) {
+    if (!ctx) return SALTY_ERR_INVALID_ARG;
+    auto& E = ctx->err;
+    if (!t) return E.fail(SALTY_ERR_INVALID_ARG, "null tuning");
+    if (t->trace_block != 64 && t->trace_block != 128 && t->trace_block != 256)
+        return E.fail(SALTY_ERR_INVALID_ARG, "trace_block must be 64, 128 or 256");
+    if (t->trace_pool < 32 || t->trace_pool > 4096) return E.fail(SALTY_ERR_INVALID_ARG, "trace_pool must be 32..4096");
+    if (t->trace_postpone < 1 || t->trace_postpone > 32)
+        return E.fail(SALTY_ERR_INVALID_ARG, "trace_postpone must be 1..32");
+    if (t->shade_block < 64 || t->shade_block > 1024 || t->shade_block % 32)
+        return E.fail(SALTY_ERR_INVALID_ARG, "shade_block must be a multiple of 32 in 64..1024");
+    if (t->wave_paths < (1 << 16) || t->wave_paths > (1 << 26))
+        return E.fail(SALTY_ERR_INVALID_ARG, "wave_paths must be 2^16..2^26");
+    ctx->tune.trace.block = t->trace_block;
+    ctx->tune.trace.pool = t->trace_pool;
+    ctx->tune.trace.postpone = t->trace_postpone;
+    ctx->tune.shade_block = t->shade_block;
+    ctx->tune.wave_paths = t->wave_paths;
+    return SALTY_OK;
+}
+
+salty_status salty_autotune(salty_ctx* ctx, salty_scene* const* scenes, const salty_render_opts* opts, int32_t n,
+                            int32_t trial_spp, salty_tuning* out, float* best_ms) {
+    using namespace salty;
+    if (!ctx) return SALTY_ERR_INVALID_ARG;
+    auto& E = ctx->err;
+    if (!scenes || !opts || n < 1) return E.fail(SALTY_ERR_INVALID_ARG, "empty batch");
+    if (trial_spp < 1) return E.fail(SALTY_ERR_INVALID_ARG, "trial_spp must be >= 1");
+    std::vector<salty_render_opts> trial(opts, opts + n);
+    for (auto& o : trial) {
+        o.spp = std::min(o.spp, trial_spp);
+        o.accumulate = 0;
+    }
+    for (int i = 0; i < n; ++i) SALTY_TRY(check_render_opts(ctx, scenes[i], &trial[i]));
+    cudaSetDevice(ctx->device);
+    long long samples = 0;
+    for (int i = 0; i < n; ++i) {
+        const bool cr = trial[i].crop_w > 0 && trial[i].crop_h > 0;
+        samples += (long long)(cr ? trial[i].crop_w : trial[i].width) * (cr ? trial[i].crop_h : trial[i].height) *
+                   trial[i].spp;
+    }
+    // time of one trial render under a tuning: the better of two runs (device time)
+    auto time_of = [&](const Tuning& t, float* ms) -> salty_status {
+        ctx->tune = t;
+        float best = 1e30f;
+        for (int r = 0; r < 2; ++r) {
+            salty_render_stats st{};
+            SALTY_TRY(render_batch(ctx, scenes, trial.data(), n, &st));
+            best = std::min(best, (float)st.ms);
+        }
+        *ms = best;
+        return SALTY_OK;
+    };
+    const Tuning start = ctx->tune;
+    Tuning best = start;
+    float best_t = 0;
+    salty_status s = time_of(best, &best_t);
+    // coordinate descent, one pass over the knobs
+    const long long waves[] = {1ll << 20, 1ll << 21, 1ll << 22, 1ll << 23};
+    const int shade[] = {128, 256, 512};
+    const int tblock[] = {64, 128, 256};
+    const int pool[] = {64, 128, 256};
+    const int postpone[] = {1, 4, 7, 10};
+    auto try_knob = [&](auto set, const auto& values) -> salty_status {
+        for (auto v : values) {
+            Tuning t = best;
+            if (!set(t, v)) continue;
+            float ms = 0;
+            SALTY_TRY(time_of(t, &ms));
+            if (ms < best_t * 0.995f) { best_t = ms; best = t; }
+        }
+        return SALTY_OK;
+    };
+    if (s == SALTY_OK)
+        s = try_knob([&](Tuning& t, long long v) {
+                // capacities at or above the sample count all run one wave
+                if (std::min(v, samples) == std::min(best.wave_paths, samples)) return false;
+                t.wave_paths = v;
+                return true;
+            }, waves);
+    if (s == SALTY_OK)
+        s = try_knob([&](Tuning& t, int v) { if (v == best.shade_block) return false; t.shade_block = v; return true; },
+                     shade);
+    if (s == SALTY_OK)
+        s = try_knob([&](Tuning& t, int v) { if (v == best.trace.block) return false; t.trace.block = v; return true; },
+                     tblock);
+    if (s == SALTY_OK)
+        s = try_knob([&](Tuning& t, int v) { if (v == best.trace.pool) return false; t.trace.pool = v; return true; },
+                     pool);
+    if (s == SALTY_OK)
+        s = try_knob([&](Tuning& t, int v) {
+                if (v == best.trace.postpone) return false;
+                t.trace.postpone = v;
+                return true;
+            }, postpone);
+    ctx->tune = s == SALTY_OK ? best : start;
+    if (s != SALTY_OK) return s;
+    if (best_ms) *best_ms = best_t;
+    return out ? salty_get_tuning(ctx, out) : SALTY_OK;
+}
 
 salty_status salty_tonemap(salty_ctx* ctx, int32_t type, int32_t w, int32_t h, const float* rgb, float* out_rgb,
                            uint8_t* out_srgb8, int32_t ref_oetf, float* ave_lw, float* max_lw) {

@@ -108,7 +108,9 @@ struct GpuMaterial {
     float emission[3];
     float ior;
     float roughness;
-    float rr_threshold;  // compat Lambert dice threshold max(albedo, 0.01)
+    float rr_threshold;  // compat dice threshold max(colour, 0.01)
+    float specular[3];   // Plastic
+    float power;         // Phong, Plastic lobe exponent
 };
 
 struct SceneConsts {
@@ -144,9 +146,27 @@ struct Bvh {
     DevBuf<Bvh8Node> nodes;
     DevBuf<float4> tris;        // leaf order, kTriFloat4 per triangle
     int64_t n_nodes = 0;
+    int64_t n_tris = 0;         // leaf-order triangles
     int32_t depth = 0;
     bool built = false;
+    uint64_t generation = 0;    // bumped by every build (batch arenas key on it)
     salty_bvh_info info{};
+};
+
+// What one traversal launch walks: a BVH (or a batch arena of concatenated BVHs) and, per
+// ray, the node it starts at.
+struct TraceTarget {
+    const Bvh8Node* nodes = nullptr;
+    const float4* tris = nullptr;
+    int depth = 0;
+    const int* roots = nullptr;  // per-ray root node, or null (node 0)
+};
+
+// Launch shape of the traversal kernel, chosen by salty_autotune.
+struct TraceTuning {
+    int block = 128;     // threads per block: 64, 128 or 256
+    int pool = 128;      // rays a warp takes from the global cursor per refill
+    int postpone = 7;    // fewest lanes that test a triangle group together
 };
 
 }  // namespace salty
@@ -164,6 +184,38 @@ struct salty_scene {
     salty::Film film;
 };
 
+namespace salty {
+// Launch shapes of the renderer, chosen by salty_autotune (include/salty_gpu.h).
+struct Tuning {
+    TraceTuning trace;
+    long long wave_paths = 1ll << 22;  // paths in flight per wave (queue capacity)
+    int shade_block = 256;             // threads per block of the shading kernels
+};
+
+// Device queues of the wavefront renderer, kept by the context between renders.
+struct WaveStore {
+    DevBuf<float4> rays[2], W[2], L[2], hits, nee, srays, shits, lbuf, abuf;
+    DevBuf<uint4> meta[2];
+    DevBuf<int> roots[2], sroots;
+    DevBuf<int> counts;
+    DevBuf<long long> wave;
+    DevBuf<unsigned long long> stats, tc0, tc1;
+};
+
+// Scenes of a batch render concatenated: nodes and leaf triangles of every BVH back to
+// back (child, triangle and id fields rebased), triangle attributes and materials likewise.
+struct BatchArena {
+    std::vector<std::pair<const void*, uint64_t>> key;  // (scene, BVH generation) per slot
+    DevBuf<Bvh8Node> nodes;
+    DevBuf<float4> tris;
+    DevBuf<float> pos, nrm;
+    DevBuf<int> mat;
+    DevBuf<GpuMaterial> mats;
+    std::vector<long long> node_off, id_off;
+    int depth = 0;
+};
+}  // namespace salty
+
 struct salty_ctx {
     int device = 0;
     int num_sms = 0;
@@ -180,6 +232,10 @@ struct salty_ctx {
     salty::DevBuf<unsigned long long> counters;
     salty::DevBuf<int> status;   // device status word(s)
     void* pinned = nullptr;      // small pinned readback area
+    salty::Tuning tune;
+    salty::WaveStore waves;
+    salty::BatchArena arena;
+    salty::DevBuf<unsigned char> slots;  // SceneSlot table of the current render
 };
 
 namespace salty {
@@ -189,9 +245,15 @@ salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& 
 salty_status trace_launch(salty_ctx* ctx, salty_scene* sc, const float4* d_rays, long long n,
                           const int* n_dev, uint32_t flags, float4* d_hits,
                           unsigned long long* d_counters, cudaStream_t st, int* d_status);
+salty_status trace_launch(salty_ctx* ctx, const TraceTarget& tgt, const TraceTuning& tune, const float4* d_rays,
+                          long long n, const int* n_dev, uint32_t flags, float4* d_hits,
+                          unsigned long long* d_counters, cudaStream_t st, int* d_status);
 // render.cu
 salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
                     salty_render_stats* stats);
+salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salty_render_opts* opts, int n,
+                          salty_render_stats* total);
+salty_status check_render_opts(salty_ctx* ctx, const salty_scene* sc, const salty_render_opts* o);
 salty_status film_outputs(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
                           float* d_mean, float* d_var, uint8_t* d_srgb);
 salty_status film_features(salty_ctx* ctx, salty_scene* sc, float* d_mean, float* d_var, float* d_albedo,

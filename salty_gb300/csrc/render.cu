@@ -111,23 +111,48 @@ struct Camera {
     float pos[3], cx[3], cy[3], cz[3];
 };
 
+// One scene of a batch (one slot for a plain render).  Its samples are the global sample
+// indices [sample_off, sample_off + npx * spp), sample g -> (s, p) = divmod(g - sample_off,
+// npx); its film pixels are [pixel_off, pixel_off + npx) of the batch's pixel space.
+struct SceneSlot {
+    SceneConsts k;              // light_tri0 in the ids of the batch's triangle arrays
+    Camera cam;
+    int width, height;          // the frame
+    int crop_x, crop_y, film_w, film_h;
+    int spp, max_depth, rr_depth, profile;
+    int root;                   // BVH root node (batch arena index)
+    int pad;
+    long long npx;
+    unsigned long long seed;
+    float *sum, *comp, *sumsq, *aov;  // the scene's film (FP32 + Kahan, or FP64 below)
+    double *sum64, *sumsq64;
+};
+
 struct WaveParams {
     const float* pos;
     const float* nrm;
     const int* mat;
     const GpuMaterial* mats;
-    SceneConsts k;
-    Camera cam;
-    int width, height, spp, max_depth, rr_depth, profile;
-    int crop_x, crop_y, film_w, film_h;   // the film: a film_w x film_h window at (crop_x, crop_y)
-    unsigned long long seed;
-    long long total_samples;   // width*height*spp
+    const SceneSlot* slots;
+    const long long* sample_off;  // per slot, then the total (n_slots + 1 entries)
+    const long long* pixel_off;   // per slot, then the total
+    int n_slots;
     int capacity;
+    long long total_samples;
 };
+
+// Path state word meta.w: depth (bits 0..15), previous vertex delta (bit 16), slot (17..31).
+constexpr int kSlotShift = 17;
+constexpr int kMaxSlots = 1 << (32 - kSlotShift);
+__device__ __forceinline__ unsigned pack_w(int depth, bool delta, int slot) {
+    return (unsigned)depth | ((delta ? 1u : 0u) << 16) | ((unsigned)slot << kSlotShift);
+}
 
 struct WaveBuffers {
     float4* rays[2];
     PathSoA path[2];
+    int* roots[2];     // per queued ray: BVH root of its scene (null for one scene)
+    int* sroots;
     float4* hits;
     float4* nee;       // 2 per path: contribution xyz, w = shadow-queue index (int bits, -1 none)
     float4* srays;     // shadow queue rays (2 per path)
@@ -139,10 +164,20 @@ struct WaveBuffers {
     unsigned long long* stats;  // [0] rays traced, [1] paths
 };
 
+// the last slot whose offset is <= g (slots with no samples or pixels are skipped)
+__device__ __forceinline__ int find_slot(const long long* off, int lo, int hi, long long g) {
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // ---------------------------------------------------------------- kernels
-// Camera rays for samples [g0, g0 + n) of the frame; sample index g -> (sample s =
-// g / (W*H), pixel p = g % (W*H)).  PinholeCamera::GetRay (include/s3d_camera.h:95-100)
-// with separately rounded operations.
+// Camera rays for samples [g0, g0 + n) of the batch; sample g of slot S -> (sample s,
+// film pixel fp) = divmod(g - S.sample_off, S.npx).  PinholeCamera::GetRay
+// (include/s3d_camera.h:95-100) with separately rounded operations.
 __global__ void k_generate(WaveParams P, WaveBuffers B) {
     const long long g0 = B.wave[0];
     const long long remain = P.total_samples - g0;
@@ -154,35 +189,38 @@ __global__ void k_generate(WaveParams P, WaveBuffers B) {
         atomicAdd(&B.stats[1], (unsigned long long)n);
         atomicAdd(&B.stats[0], (unsigned long long)n);
     }
-    const long long npx = (long long)P.film_w * P.film_h;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const long long g = g0 + i;
-        const long long s = g / npx, fp = g % npx;
-        const int px = P.crop_x + (int)(fp % P.film_w), py = P.crop_y + (int)(fp / P.film_w);
-        const long long p = (long long)py * P.width + px;  // full-frame pixel: its random stream
-        Rng rng = rng_for(P.seed, (unsigned long long)p, (unsigned long long)s);
+        const int sid = P.n_slots == 1 ? 0 : find_slot(P.sample_off, 0, P.n_slots - 1, g);
+        const SceneSlot& S = P.slots[sid];
+        const long long gl = g - P.sample_off[sid];
+        const long long s = gl / S.npx, fp = gl % S.npx;
+        const int px = S.crop_x + (int)(fp % S.film_w), py = S.crop_y + (int)(fp / S.film_w);
+        const long long p = (long long)py * S.width + px;  // full-frame pixel: its random stream
+        Rng rng = rng_for(S.seed, (unsigned long long)p, (unsigned long long)s);
         float fx, fy;
-        if (P.profile == SALTY_PROFILE_COMPAT) {
-            fx = __fsub_rn(__fdiv_rn(__fadd_rn(0.5f, (float)px), (float)P.width), 0.5f);
-            fy = __fsub_rn(__fdiv_rn(__fadd_rn(0.5f, (float)py), (float)P.height), 0.5f);
+        if (S.profile == SALTY_PROFILE_COMPAT) {
+            fx = __fsub_rn(__fdiv_rn(__fadd_rn(0.5f, (float)px), (float)S.width), 0.5f);
+            fy = __fsub_rn(__fdiv_rn(__fadd_rn(0.5f, (float)py), (float)S.height), 0.5f);
         } else {
             float jx = rng.f32(), jy = rng.f32();
-            fx = __fsub_rn(__fdiv_rn(__fadd_rn(jx, (float)px), (float)P.width), 0.5f);
-            fy = __fsub_rn(__fdiv_rn(__fadd_rn(jy, (float)py), (float)P.height), 0.5f);
+            fx = __fsub_rn(__fdiv_rn(__fadd_rn(jx, (float)px), (float)S.width), 0.5f);
+            fy = __fsub_rn(__fdiv_rn(__fadd_rn(jy, (float)py), (float)S.height), 0.5f);
         }
         float q[3], d[3];
         for (int a = 0; a < 3; ++a) {
-            q[a] = __fadd_rn(__fadd_rn(__fmul_rn(P.cam.cx[a], fx), __fmul_rn(P.cam.cy[a], fy)), P.cam.cz[a]);
-            d[a] = __fsub_rn(q[a], P.cam.pos[a]);
+            q[a] = __fadd_rn(__fadd_rn(__fmul_rn(S.cam.cx[a], fx), __fmul_rn(S.cam.cy[a], fy)), S.cam.cz[a]);
+            d[a] = __fsub_rn(q[a], S.cam.pos[a]);
         }
         const float mag = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
-        const float tmin = P.profile == SALTY_PROFILE_COMPAT ? kFHitMin : kEps;
-        const float tmax = P.profile == SALTY_PROFILE_COMPAT ? kFHitMax : INFINITY;
-        B.rays[0][2 * i] = make_float4(P.cam.pos[0], P.cam.pos[1], P.cam.pos[2], tmin);
+        const float tmin = S.profile == SALTY_PROFILE_COMPAT ? kFHitMin : kEps;
+        const float tmax = S.profile == SALTY_PROFILE_COMPAT ? kFHitMax : INFINITY;
+        B.rays[0][2 * i] = make_float4(S.cam.pos[0], S.cam.pos[1], S.cam.pos[2], tmin);
         B.rays[0][2 * i + 1] = make_float4(__fdiv_rn(d[0], mag), __fdiv_rn(d[1], mag), __fdiv_rn(d[2], mag), tmax);
+        if (B.roots[0]) B.roots[0][i] = S.root;
         B.path[0].W[i] = make_float4(1.f, 1.f, 1.f, 0.f);
         B.path[0].L[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        B.path[0].meta[i] = make_uint4((unsigned)rng.s, (unsigned)(rng.s >> 32), (unsigned)i, 1u << 16);
+        B.path[0].meta[i] = make_uint4((unsigned)rng.s, (unsigned)(rng.s >> 32), (unsigned)i, pack_w(0, true, sid));
         B.lbuf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         B.abuf[2 * i] = make_float4(0.f, 0.f, 0.f, 0.f);
         B.abuf[2 * i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -211,8 +249,8 @@ __device__ __forceinline__ Surf surface(const WaveParams& P, int id, float t, fl
     return s;
 }
 
-__device__ __forceinline__ bool is_light(const WaveParams& P, int id) {
-    return P.k.light_tri0 >= 0 && id >= P.k.light_tri0 && id < P.k.light_tri0 + 2;
+__device__ __forceinline__ bool is_light(const SceneConsts& k, int id) {
+    return k.light_tri0 >= 0 && id >= k.light_tri0 && id < k.light_tri0 + 2;
 }
 
 __device__ __forceinline__ float ggx_d(float nh, float a2) {
@@ -224,10 +262,51 @@ __device__ __forceinline__ V schlick(V f0, float c) {
     float m = 1.0f - c, m2 = m * m, m5 = m2 * m2 * m;
     return mk(f0.x + (1.0f - f0.x) * m5, f0.y + (1.0f - f0.y) * m5, f0.z + (1.0f - f0.z) * m5);
 }
+// SamplePhong (include/s3d_math.h:2976-2982): cos(theta) = (1 - v)^(1 / (n + 1))
+__device__ __forceinline__ V sample_phong(float u, float v, float n) {
+    float p = k2Pi * u;
+    float ct = powf(1.0f - v, 1.0f / (n + 1.0f));
+    float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+    float sp, cp;
+    sincosf(p, &sp, &cp);
+    return mk(st * cp, st * sp, ct);
+}
+// Normalised Phong lobe around the mirror direction of wo (physical profile):
+// f = (n + 2) / (2 pi) cos^n, sampled with pdf (n + 1) / (2 pi) cos^n.
+__device__ __forceinline__ float phong_lobe(V n, V wo, V wi, float power, float& pdf) {
+    V r = reflect(-wo, n);
+    float c = dot(r, wi);
+    if (c <= 0.0f) { pdf = 0.0f; return 0.0f; }
+    float cn = powf(c, power);
+    pdf = (power + 1.0f) / k2Pi * cn;
+    return (power + 2.0f) / k2Pi * cn;
+}
+// Plastic (physical profile): Schlick F (R0 = 0.04) at the outgoing angle weighs a Phong
+// lobe (specular) against a Lambert base (1 - F); the lobe is sampled with probability
+// clamp(F, 0.1, 0.9) and the mixture pdf is used.
+__device__ __forceinline__ float plastic_fresnel(float cos_o) {
+    float m = 1.0f - fmaxf(cos_o, 0.0f), m2 = m * m;
+    return 0.04f + 0.96f * m2 * m2 * m;
+}
+__device__ __forceinline__ float plastic_ps(float F) { return fminf(0.9f, fmaxf(0.1f, F)); }
+
 // f(wo, wi) without the cosine, and the BSDF-sampling pdf (physical profile)
 __device__ __forceinline__ V phys_eval(const GpuMaterial& m, V n, V wo, V wi, float& pdf) {
     V col = ld3(m.color);
     float ni = dot(n, wi);
+    if (m.type == SALTY_PHONG) {
+        float lp;
+        float f = phong_lobe(n, wo, wi, m.power, lp);
+        pdf = lp;
+        return col * f;
+    }
+    if (m.type == SALTY_PLASTIC) {
+        float lp;
+        float fl = phong_lobe(n, wo, wi, m.power, lp);
+        float F = plastic_fresnel(dot(n, wo)), ps = plastic_ps(F);
+        pdf = ps * lp + (1.0f - ps) * fmaxf(ni, 0.0f) / kPi;
+        return ld3(m.specular) * (F * fl) + col * ((1.0f - F) / kPi);
+    }
     if (m.type == SALTY_GGX) {
         float a = m.roughness * m.roughness, a2 = a * a;
         float no = dot(n, wo);
@@ -265,16 +344,19 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
         bool want_l = false, want_s = false;
         float4 ray_l0, ray_l1, ray_s0, ray_s1;
         V cl = mk(0, 0, 0), cs = mk(0, 0, 0);
-        if (live && id >= 0 && !is_light(P, id)) {
+        const uint4 mt = live ? B.path[q].meta[i] : make_uint4(0, 0, 0, 0);
+        const int slot = (int)(mt.w >> kSlotShift);
+        const SceneSlot& S = P.slots[slot];
+        const SceneConsts& K = S.k;
+        if (live && id >= 0 && !is_light(K, id)) {
             const GpuMaterial m = P.mats[P.mat[id]];
             const bool delta = (m.type == SALTY_MIRROR || m.type == SALTY_GLASS);
-            uint4 mt = B.path[q].meta[i];
             Rng rng;
             rng.s = (unsigned long long)mt.x | ((unsigned long long)mt.y << 32);
             const float4 r0 = B.rays[q][2 * i], r1 = B.rays[q][2 * i + 1];
             V o = xyz(r0), d = xyz(r1);
-            if (P.profile == SALTY_PROFILE_COMPAT) {
-                if (!delta && P.k.has_light) {
+            if (S.profile == SALTY_PROFILE_COMPAT) {
+                if (!delta && K.has_light) {
                     Surf s;
                     s.p = mk(__fadd_rn(o.x, __fmul_rn(d.x, h.x)), __fadd_rn(o.y, __fmul_rn(d.y, h.x)),
                              __fadd_rn(o.z, __fmul_rn(d.z, h.x)));
@@ -284,18 +366,18 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
                                        np[2] * al + np[5] * h.z + np[8] * h.w));
                     (void)rng.u32();  // Scene::GetLight (include/s3d_scene.h:84-90), one light
                     float u = rng.f32(), w = rng.f32();
-                    V lp = ld3(P.k.lc) + ld3(P.k.la) * u + ld3(P.k.lb) * w;
-                    float pdf = 1.0f / P.k.larea;
+                    V lp = ld3(K.lc) + ld3(K.la) * u + ld3(K.lb) * w;
+                    float pdf = 1.0f / K.larea;
                     V ld = lp - s.p;
                     float dist2 = dot(ld, ld);
                     ld = safe_unit(ld);
                     float cos_s = fabsf(dot(n, ld));
-                    float cos_l = fabsf(dot(ld3(P.k.ln), -ld));
+                    float cos_l = fabsf(dot(ld3(K.ln), -ld));
                     V fs = ld3(m.color) * (1.0f / kPi);
                     float G = cos_s * cos_l / dist2;
                     float brdf_pdf = fabsf(ld.z / kPi) * cos_l / dist2;
                     float mis = pdf / (brdf_pdf + pdf);
-                    cl = ld3(P.k.le) * fs * mis * (G / pdf);
+                    cl = ld3(K.le) * fs * mis * (G / pdf);
                     want_l = true;
                     ray_l0 = make_float4(s.p.x, s.p.y, s.p.z, kFHitMin);
                     ray_l1 = make_float4(ld.x, ld.y, ld.z, kFHitMax);
@@ -304,45 +386,45 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
                 if (!delta) {
                     Surf s = surface(P, id, h.x, h.z, h.w, o, d);
                     V wo = -d;
-                    if (P.k.has_light) {
+                    if (K.has_light) {
                         float u1 = rng.f32(), u2 = rng.f32();
-                        V lp = ld3(P.k.lc) + ld3(P.k.la) * u1 + ld3(P.k.lb) * u2;
+                        V lp = ld3(K.lc) + ld3(K.la) * u1 + ld3(K.lb) * u2;
                         V wi = lp - s.p;
                         float dist2 = dot(wi, wi), dist = sqrtf(dist2);
                         wi = wi * (1.0f / dist);
-                        float cos_l = dot(ld3(P.k.ln), -wi);
+                        float cos_l = dot(ld3(K.ln), -wi);
                         float cos_s = dot(s.nsf, wi), cos_g = dot(s.ngf, wi);
                         if (cos_l > 0.0f && cos_s > 0.0f && cos_g > 0.0f) {
                             float pdf_b;
                             V f = phys_eval(m, s.nsf, wo, wi, pdf_b);
-                            float pdf_l = dist2 / (cos_l * P.k.larea);
+                            float pdf_l = dist2 / (cos_l * K.larea);
                             float mis = pdf_l / (pdf_l + pdf_b);
-                            cl = f * ld3(P.k.le) * (cos_s * mis / pdf_l);
+                            cl = f * ld3(K.le) * (cos_s * mis / pdf_l);
                             want_l = true;
                             ray_l0 = make_float4(s.p.x, s.p.y, s.p.z, kEps);
                             ray_l1 = make_float4(wi.x, wi.y, wi.z, dist * (1.0f - 1e-4f));
                         }
                     }
-                    if (P.k.has_sun) {
-                        V wi = ld3(P.k.sun_dir);
-                        if (P.k.sun_disk) {
+                    if (K.has_sun) {
+                        V wi = ld3(K.sun_dir);
+                        if (K.sun_disk) {
                             // uniform direction in the sun's cone
                             float u1 = rng.f32(), u2 = rng.f32();
-                            float ct = 1.0f - u1 * (1.0f - P.k.sun_cos_max);
+                            float ct = 1.0f - u1 * (1.0f - K.sun_cos_max);
                             float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
                             float sp, cp;
                             sincosf(k2Pi * u2, &sp, &cp);
-                            wi = safe_unit(ld3(P.k.sun_t) * (st * cp) + ld3(P.k.sun_b) * (st * sp) + wi * ct);
+                            wi = safe_unit(ld3(K.sun_t) * (st * cp) + ld3(K.sun_b) * (st * sp) + wi * ct);
                         }
                         float cos_s = dot(s.nsf, wi), cos_g = dot(s.ngf, wi);
                         if (cos_s > 0.0f && cos_g > 0.0f) {
                             float pdf_b;
                             V f = phys_eval(m, s.nsf, wo, wi, pdf_b);
-                            if (P.k.sun_disk) {
-                                float mis = P.k.sun_pdf / (P.k.sun_pdf + pdf_b);
-                                cs = f * ld3(P.k.sun_L) * (cos_s * mis / P.k.sun_pdf);
+                            if (K.sun_disk) {
+                                float mis = K.sun_pdf / (K.sun_pdf + pdf_b);
+                                cs = f * ld3(K.sun_L) * (cos_s * mis / K.sun_pdf);
                             } else {
-                                cs = f * ld3(P.k.sun_rad) * cos_s;
+                                cs = f * ld3(K.sun_rad) * cos_s;
                             }
                             want_s = true;
                             ray_s0 = make_float4(s.p.x, s.p.y, s.p.z, kEps);
@@ -358,10 +440,12 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
         if (want_l) {
             B.srays[2 * ql] = ray_l0;
             B.srays[2 * ql + 1] = ray_l1;
+            if (B.sroots) B.sroots[ql] = S.root;
         }
         if (want_s) {
             B.srays[2 * qs] = ray_s0;
             B.srays[2 * qs + 1] = ray_s1;
+            if (B.sroots) B.sroots[qs] = S.root;
         }
         if (live) {
             B.nee[2 * i] = make_float4(cl.x, cl.y, cl.z, __int_as_float(want_l ? ql : -1));
@@ -375,17 +459,22 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
     const int n = B.counts[q];
     const int stride = gridDim.x * blockDim.x;
     const int lim = (n + 31) & ~31;
-    const bool compat = P.profile == SALTY_PROFILE_COMPAT;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < lim; i += stride) {
         const bool live = i < n;
         bool cont = false;
         float4 nr0, nr1, nW, nL;
         uint4 nmeta;
+        int root = 0;
         if (live) {
             const float4 h = B.hits[i];
             const int id = __float_as_int(h.y);
             float4 W4 = B.path[q].W[i], L4 = B.path[q].L[i];
             uint4 mt = B.path[q].meta[i];
+            const int slot = (int)(mt.w >> kSlotShift);
+            const SceneSlot& S = P.slots[slot];
+            const SceneConsts& K = S.k;
+            const bool compat = S.profile == SALTY_PROFILE_COMPAT;
+            root = S.root;
             V W = xyz(W4), L = xyz(L4);
             float prev_pdf = W4.w;
             const bool prev_delta = (mt.w >> 16) & 1u;
@@ -398,7 +487,7 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
             const int q0 = __float_as_int(e0.w), q1 = __float_as_int(e1.w);
             if (q0 >= 0) {
                 const int sid = __float_as_int(B.shits[q0].y);
-                bool vis = compat ? (sid >= 0 && is_light(P, sid)) : (sid < 0);
+                bool vis = compat ? (sid >= 0 && is_light(K, sid)) : (sid < 0);
                 if (vis) L = L + W * xyz(e0);
             }
             if (q1 >= 0) {
@@ -414,17 +503,17 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                 V n = safe_unit(mk(np[0] * al + np[3] * h.z + np[6] * h.w, np[1] * al + np[4] * h.z + np[7] * h.w,
                                    np[2] * al + np[5] * h.z + np[8] * h.w));
                 if (dot(n, d) > 0.0f) n = -n;
-                const bool emitter = is_light(P, id);
+                const bool emitter = is_light(K, id);
                 B.abuf[2 * mt.z] = make_float4(emitter ? 1.0f : am.color[0], emitter ? 1.0f : am.color[1],
                                                emitter ? 1.0f : am.color[2], 1.0f / (1.0f + h.x));
                 B.abuf[2 * mt.z + 1] = make_float4(n.x, n.y, n.z, 0.0f);
             }
             if (id < 0) {
-                L = L + W * ld3(P.k.sky);
+                L = L + W * ld3(K.sky);
                 // an escaping ray inside the sun's disk (physical profile, finite sun)
-                if (!compat && P.k.has_sun && P.k.sun_disk && dot(d, ld3(P.k.sun_dir)) >= P.k.sun_cos_max) {
-                    const float w = prev_delta ? 1.0f : prev_pdf / (prev_pdf + P.k.sun_pdf);
-                    L = L + W * ld3(P.k.sun_L) * w;
+                if (!compat && K.has_sun && K.sun_disk && dot(d, ld3(K.sun_dir)) >= K.sun_cos_max) {
+                    const float w = prev_delta ? 1.0f : prev_pdf / (prev_pdf + K.sun_pdf);
+                    L = L + W * ld3(K.sun_L) * w;
                 }
             } else if (compat) {
                 const GpuMaterial m = P.mats[P.mat[id]];
@@ -461,6 +550,40 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                         if (rng.f32() < Pp) { out = refl; wgt = col * (Re / (Pp * 0.5f)); }
                         else { out = refr; wgt = col * (Tr / ((1.0f - Pp) * 0.5f)); }
                     }
+                } else if (m.type == SALTY_PHONG) {
+                    // Phong::Shade (src/s3d_phong.cpp:65-88)
+                    float uu = rng.f32(), vv = rng.f32();
+                    V sd = sample_phong(uu, vv, m.power);
+                    V w = safe_unit(reflect(d, nm)), t, b;
+                    tangent_space(w, t, b);
+                    out = safe_unit(t * sd.x + b * sd.y + w * sd.z);
+                    dice = rng.f32() >= m.rr_threshold;
+                    wgt = col * fabsf(dot(out, nm));
+                } else if (m.type == SALTY_PLASTIC) {
+                    // Plastic::Shade (src/s3d_plastic.cpp:71-142): R0 = 0.5, diffuse branch
+                    // with P = (R + 0.5) / 2 weighted R / P, Phong branch (1 - R) / (1 - P)
+                    float t1 = 1.0f - fabsf(dot(normal, d));
+                    float R = 0.5f + 0.5f * t1 * t1 * t1 * t1 * t1;
+                    float Pd = (R + 0.5f) * 0.5f;
+                    if (rng.f32() <= Pd) {
+                        V t, b;
+                        tangent_space(nm, t, b);
+                        float uu = rng.f32(), vv = rng.f32();
+                        float rr = sqrtf(1.0f - uu * uu), ph = k2Pi * vv;
+                        float sp, cp;
+                        sincosf(ph, &sp, &cp);
+                        out = safe_unit(t * (rr * cp) + b * (rr * sp) + nm * uu);
+                        dice = rng.f32() >= m.rr_threshold;
+                        wgt = col * (R / Pd);
+                    } else {
+                        float uu = rng.f32(), vv = rng.f32();
+                        V sd = sample_phong(uu, vv, m.power);
+                        V w = safe_unit(reflect(d, nm)), t, b;
+                        tangent_space(w, t, b);
+                        out = safe_unit(t * sd.x + b * sd.y + w * sd.z);
+                        dice = rng.f32() >= m.rr_threshold;  // derived from the diffuse threshold
+                        wgt = ld3(m.specular) * (dot(out, nm) * (1.0f - R) / (1.0f - Pd));
+                    }
                 } else {
                     V t, b;
                     tangent_space(nm, t, b);
@@ -474,21 +597,21 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                 }
                 W = W * wgt;
                 bool stop = dice || (W.x < FLT_EPSILON && W.y < FLT_EPSILON && W.z < FLT_EPSILON) ||
-                            depth + 1 >= P.max_depth;
+                            depth + 1 >= S.max_depth;
                 if (!stop) {
                     cont = true;
                     nr0 = make_float4(pos.x, pos.y, pos.z, kFHitMin);
                     nr1 = make_float4(out.x, out.y, out.z, kFHitMax);
                     nW = make_float4(W.x, W.y, W.z, 0.0f);
                 }
-            } else if (is_light(P, id)) {
-                float cos_l = dot(ld3(P.k.ln), -d);
+            } else if (is_light(K, id)) {
+                float cos_l = dot(ld3(K.ln), -d);
                 if (cos_l > 0.0f) {
-                    if (prev_delta) L = L + W * ld3(P.k.le);
+                    if (prev_delta) L = L + W * ld3(K.le);
                     else {
-                        float pdf_l = h.x * h.x / (cos_l * P.k.larea);
+                        float pdf_l = h.x * h.x / (cos_l * K.larea);
                         float mis = prev_pdf / (prev_pdf + pdf_l);
-                        L = L + W * ld3(P.k.le) * mis;
+                        L = L + W * ld3(K.le) * mis;
                     }
                 }
             } else {
@@ -539,6 +662,33 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                         wgt = schlick(col, oh) * (G * oh / (no * nh));
                         pdf = ggx_d(nh, a2) * nh / (4.0f * oh);
                     }
+                } else if (m.type == SALTY_PHONG || m.type == SALTY_PLASTIC) {
+                    bool lobe = true;
+                    V wo = -d;
+                    if (m.type == SALTY_PLASTIC) lobe = rng.f32() < plastic_ps(plastic_fresnel(dot(s.nsf, wo)));
+                    float r1 = rng.f32(), r2 = rng.f32();
+                    V t, b;
+                    if (lobe) {
+                        V sd = sample_phong(r1, r2, m.power);
+                        V rd = reflect(d, s.nsf);
+                        tangent_space(rd, t, b);
+                        wi = safe_unit(t * sd.x + b * sd.y + rd * sd.z);
+                    } else {
+                        float rr = sqrtf(r1), ph = k2Pi * r2;
+                        float z = sqrtf(fmaxf(0.0f, 1.0f - r1));
+                        tangent_space(s.nsf, t, b);
+                        float sp, cp;
+                        sincosf(ph, &sp, &cp);
+                        wi = safe_unit(t * (rr * cp) + b * (rr * sp) + s.nsf * z);
+                    }
+                    const float ni = dot(s.nsf, wi);
+                    if (ni <= 0.0f || dot(s.ngf, wi) <= 0.0f) {
+                        dead = true;
+                    } else {
+                        V f = phys_eval(m, s.nsf, wo, wi, pdf);
+                        if (!(pdf > 0.0f)) dead = true;
+                        else wgt = f * (ni / pdf);
+                    }
                 } else {
                     float r1 = rng.f32(), r2 = rng.f32();
                     float rr = sqrtf(r1), ph = k2Pi * r2;
@@ -555,32 +705,34 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                 if (!dead) {
                     W = W * wgt;
                     bool stop = (W.x <= 0.0f && W.y <= 0.0f && W.z <= 0.0f);
-                    if (!stop && depth >= P.rr_depth) {
+                    if (!stop && depth >= S.rr_depth) {
                         float qv = fminf(0.95f, maxc(W));
                         if (rng.f32() >= qv) stop = true;
                         else W = W * (1.0f / qv);
                     }
-                    if (depth + 1 >= P.max_depth) stop = true;
+                    if (depth + 1 >= S.max_depth) stop = true;
                     if (!stop) {
                         cont = true;
                         nr0 = make_float4(s.p.x, s.p.y, s.p.z, kEps);
                         nr1 = make_float4(wi.x, wi.y, wi.z, INFINITY);
                         nW = make_float4(W.x, W.y, W.z, pdf);
-                        mt.w = (unsigned)(depth + 1) | ((is_delta ? 1u : 0u) << 16);
+                        mt.w = pack_w(depth + 1, is_delta, slot);
                     }
                 }
             }
             nL = make_float4(L.x, L.y, L.z, 0.0f);
-            nmeta = make_uint4((unsigned)rng.s, (unsigned)(rng.s >> 32), mt.z, compat ? (unsigned)(depth + 1) : mt.w);
+            nmeta = make_uint4((unsigned)rng.s, (unsigned)(rng.s >> 32), mt.z,
+                               compat ? pack_w(depth + 1, false, slot) : mt.w);
             if (!cont) B.lbuf[mt.z] = nL;
         }
-        const int slot = warp_append(cont, &B.counts[q ^ 1]);
+        const int qi = warp_append(cont, &B.counts[q ^ 1]);
         if (cont) {
-            B.rays[q ^ 1][2 * slot] = nr0;
-            B.rays[q ^ 1][2 * slot + 1] = nr1;
-            B.path[q ^ 1].W[slot] = nW;
-            B.path[q ^ 1].L[slot] = nL;
-            B.path[q ^ 1].meta[slot] = nmeta;
+            B.rays[q ^ 1][2 * qi] = nr0;
+            B.rays[q ^ 1][2 * qi + 1] = nr1;
+            B.path[q ^ 1].W[qi] = nW;
+            B.path[q ^ 1].L[qi] = nL;
+            B.path[q ^ 1].meta[qi] = nmeta;
+            if (B.roots[q ^ 1]) B.roots[q ^ 1][qi] = root;
         }
     }
 }
@@ -594,57 +746,70 @@ __global__ void k_reset_queue(WaveBuffers B, int q) {
     B.counts[2] = 0;
 }
 
-// Adds the wave's samples to the film: one thread per pixel, samples in index order.
-__global__ void k_accumulate(WaveParams P, WaveBuffers B, float* __restrict__ sum, float* __restrict__ comp,
-                             float* __restrict__ sumsq, double* __restrict__ sum64, double* __restrict__ sumsq64,
-                             float* __restrict__ aov) {
+// Adds the wave's samples to the films: one thread per film pixel of the slots the wave
+// touches, that pixel's samples in index order.
+__global__ void k_accumulate(WaveParams P, WaveBuffers B) {
     const long long g0 = B.wave[0];
-    const long long npx = (long long)P.film_w * P.film_h;
     const long long remain = P.total_samples - g0;
     const long long n = remain < P.capacity ? remain : P.capacity;
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
-        // samples s with g0 <= s*npx + p < g0 + n
-        long long s_lo = (g0 - p + npx - 1) / npx;
-        if (g0 - p <= 0) s_lo = 0;
-        long long s_hi = (g0 + n - 1 - p) / npx;  // inclusive
-        if (g0 + n - 1 - p < 0) continue;
+    if (n <= 0) return;
+    const int s0 = P.n_slots == 1 ? 0 : find_slot(P.sample_off, 0, P.n_slots - 1, g0);
+    const int s1 = P.n_slots == 1 ? 0 : find_slot(P.sample_off, s0, P.n_slots - 1, g0 + n - 1);
+    const long long p_begin = P.pixel_off[s0], p_end = P.pixel_off[s1 + 1];
+    for (long long gp = p_begin + blockIdx.x * (long long)blockDim.x + threadIdx.x; gp < p_end;
+         gp += (long long)gridDim.x * blockDim.x) {
+        const int sid = s0 == s1 ? s0 : find_slot(P.pixel_off, s0, s1, gp);
+        const SceneSlot& S = P.slots[sid];
+        const long long npx = S.npx, p = gp - P.pixel_off[sid];
+        // the wave in slot-local sample indices [a, b), within the slot's npx * spp
+        const long long base = P.sample_off[sid];
+        const long long a = g0 - base;
+        long long b = g0 + n - base;
+        if (b > npx * S.spp) b = npx * S.spp;
+        // samples s of this pixel with a <= s * npx + p < b
+        const long long lo = a - p, hi = b - 1 - p;
+        if (hi < 0) continue;
+        const long long s_lo = lo <= 0 ? 0 : (lo + npx - 1) / npx;
+        const long long s_hi = hi / npx;
         if (s_lo > s_hi) continue;
-        if (sum64) {
-            double a0 = sum64[3 * p], a1 = sum64[3 * p + 1], a2 = sum64[3 * p + 2];
-            double b0 = sumsq64[3 * p], b1 = sumsq64[3 * p + 1], b2 = sumsq64[3 * p + 2];
-            for (long long s = s_lo; s <= s_hi; ++s) {
-                float4 l = B.lbuf[s * npx + p - g0];
+        const long long w0 = base - g0;  // wave index of slot-local sample 0
+        if (S.sum64) {
+            double a0 = S.sum64[3 * p], a1 = S.sum64[3 * p + 1], a2 = S.sum64[3 * p + 2];
+            double b0 = S.sumsq64[3 * p], b1 = S.sumsq64[3 * p + 1], b2 = S.sumsq64[3 * p + 2];
+            for (long long sm = s_lo; sm <= s_hi; ++sm) {
+                float4 l = B.lbuf[w0 + sm * npx + p];
                 a0 += l.x; a1 += l.y; a2 += l.z;
                 b0 += (double)l.x * l.x; b1 += (double)l.y * l.y; b2 += (double)l.z * l.z;
             }
-            sum64[3 * p] = a0; sum64[3 * p + 1] = a1; sum64[3 * p + 2] = a2;
-            sumsq64[3 * p] = b0; sumsq64[3 * p + 1] = b1; sumsq64[3 * p + 2] = b2;
+            S.sum64[3 * p] = a0; S.sum64[3 * p + 1] = a1; S.sum64[3 * p + 2] = a2;
+            S.sumsq64[3 * p] = b0; S.sumsq64[3 * p + 1] = b1; S.sumsq64[3 * p + 2] = b2;
         } else {
-            float a[3], c[3], q2[3];
-            for (int k = 0; k < 3; ++k) { a[k] = sum[3 * p + k]; c[k] = comp[3 * p + k]; q2[k] = sumsq[3 * p + k]; }
-            for (long long s = s_lo; s <= s_hi; ++s) {
-                float4 l = B.lbuf[s * npx + p - g0];
+            float sm3[3], c[3], q2[3];
+            for (int k = 0; k < 3; ++k) { sm3[k] = S.sum[3 * p + k]; c[k] = S.comp[3 * p + k]; q2[k] = S.sumsq[3 * p + k]; }
+            for (long long sm = s_lo; sm <= s_hi; ++sm) {
+                float4 l = B.lbuf[w0 + sm * npx + p];
                 float v[3] = {l.x, l.y, l.z};
                 for (int k = 0; k < 3; ++k) {
                     // Kahan-compensated sum
                     float y = __fsub_rn(v[k], c[k]);
-                    float t = __fadd_rn(a[k], y);
-                    c[k] = __fsub_rn(__fsub_rn(t, a[k]), y);
-                    a[k] = t;
+                    float t = __fadd_rn(sm3[k], y);
+                    c[k] = __fsub_rn(__fsub_rn(t, sm3[k]), y);
+                    sm3[k] = t;
                     q2[k] = __fadd_rn(q2[k], __fmul_rn(v[k], v[k]));
                 }
             }
-            for (int k = 0; k < 3; ++k) { sum[3 * p + k] = a[k]; comp[3 * p + k] = c[k]; sumsq[3 * p + k] = q2[k]; }
+            for (int k = 0; k < 3; ++k) { S.sum[3 * p + k] = sm3[k]; S.comp[3 * p + k] = c[k]; S.sumsq[3 * p + k] = q2[k]; }
         }
         // first-hit features: albedo (3), normal (3), 1/(1+t) (1)
         float f[7];
-        for (int k = 0; k < 7; ++k) f[k] = aov[7 * p + k];
-        for (long long s = s_lo; s <= s_hi; ++s) {
-            const float4 a0 = B.abuf[2 * (s * npx + p - g0)], a1 = B.abuf[2 * (s * npx + p - g0) + 1];
-            f[0] += a0.x; f[1] += a0.y; f[2] += a0.z; f[6] += a0.w;
-            f[3] += a1.x; f[4] += a1.y; f[5] += a1.z;
+        for (int k = 0; k < 7; ++k) f[k] = S.aov[7 * p + k];
+        for (long long sm = s_lo; sm <= s_hi; ++sm) {
+            const long long wi = w0 + sm * npx + p;
+            const float4 f0 = B.abuf[2 * wi], f1 = B.abuf[2 * wi + 1];
+            f[0] += f0.x; f[1] += f0.y; f[2] += f0.z; f[6] += f0.w;
+            f[3] += f1.x; f[4] += f1.y; f[5] += f1.z;
         }
-        for (int k = 0; k < 7; ++k) aov[7 * p + k] = f[k];
+        for (int k = 0; k < 7; ++k) S.aov[7 * p + k] = f[k];
     }
 }
 
@@ -677,17 +842,45 @@ __global__ void k_film_out(const float* sum, const float* sumsq, const double* s
     }
 }
 
-struct WaveStore {
-    DevBuf<float4> rays[2], W[2], L[2], hits, nee, srays, shits, lbuf, abuf;
-    DevBuf<uint4> meta[2];
-    DevBuf<int> counts;
-    DevBuf<long long> wave;
-    DevBuf<unsigned long long> stats, tc0, tc1;
-};
+// Batch arena: copies of a scene's BVH and triangles with their indices moved by the
+// scene's offsets in the arena.
+__global__ void k_arena_nodes(const Bvh8Node* __restrict__ src, long long n, unsigned node_off, unsigned leaf_off,
+                              Bvh8Node* __restrict__ dst) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        Bvh8Node v = src[i];
+        v.w[1].x += node_off;  // child_base
+        v.w[1].y += leaf_off;  // tri_base
+        dst[i] = v;
+    }
+}
+
+__global__ void k_arena_tris(const float4* __restrict__ src, long long n, int id_off, float4* __restrict__ dst) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float4 a = src[3 * i];
+        a.w = __int_as_float(__float_as_int(a.w) + id_off);  // input id
+        dst[3 * i] = a;
+        dst[3 * i + 1] = src[3 * i + 1];
+        dst[3 * i + 2] = src[3 * i + 2];
+    }
+}
+
+__global__ void k_arena_mat(const int* __restrict__ src, long long n, int mat_off, int* __restrict__ dst) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = src[i] + mat_off;
+}
+
+int grid_of(long long n, int per_sm_blocks, int num_sms, int block = 256) {
+    long long g = (n + block - 1) / block, cap = (long long)num_sms * per_sm_blocks;
+    return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+}
 
 }  // namespace
 
-salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o, salty_render_stats* stats) {
+namespace {
+
+// Resets the film when the call does not continue it (PathTracer::TracePath clears RT at
+// the start of a run, src/s3d_pt.cpp:297-353).
+salty_status prepare_film(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o) {
     auto& E = ctx->err;
     cudaStream_t st = ctx->stream;
     Film& F = sc->film;
@@ -697,44 +890,225 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
     const long long npx = (long long)fw * fh;
     const bool fresh = !o.accumulate || F.width != fw || F.height != fh || F.fp64 != o.fp64 || F.frame_w != o.width ||
                        F.frame_h != o.height || F.crop_x != cx || F.crop_y != cy;
-    if (fresh) {
-        F.width = fw;
-        F.height = fh;
-        F.frame_w = o.width;
-        F.frame_h = o.height;
-        F.crop_x = cx;
-        F.crop_y = cy;
-        F.fp64 = o.fp64;
-        F.samples = 0;
-        SALTY_TRY_CUDA(E, F.aov.ensure(npx * 7));
-        SALTY_TRY_CUDA(E, cudaMemsetAsync(F.aov.p, 0, npx * 7 * sizeof(float), st));
-        if (o.fp64) {
-            SALTY_TRY_CUDA(E, F.sum64.ensure(npx * 3));
-            SALTY_TRY_CUDA(E, F.sumsq64.ensure(npx * 3));
-            SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sum64.p, 0, npx * 3 * sizeof(double), st));
-            SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sumsq64.p, 0, npx * 3 * sizeof(double), st));
-        } else {
-            SALTY_TRY_CUDA(E, F.sum.ensure(npx * 3));
-            SALTY_TRY_CUDA(E, F.comp.ensure(npx * 3));
-            SALTY_TRY_CUDA(E, F.sumsq.ensure(npx * 3));
-            SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sum.p, 0, npx * 3 * sizeof(float), st));
-            SALTY_TRY_CUDA(E, cudaMemsetAsync(F.comp.p, 0, npx * 3 * sizeof(float), st));
-            SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sumsq.p, 0, npx * 3 * sizeof(float), st));
-        }
+    if (!fresh) return SALTY_OK;
+    F.width = fw;
+    F.height = fh;
+    F.frame_w = o.width;
+    F.frame_h = o.height;
+    F.crop_x = cx;
+    F.crop_y = cy;
+    F.fp64 = o.fp64;
+    F.samples = 0;
+    SALTY_TRY_CUDA(E, F.aov.ensure(npx * 7));
+    SALTY_TRY_CUDA(E, cudaMemsetAsync(F.aov.p, 0, npx * 7 * sizeof(float), st));
+    if (o.fp64) {
+        SALTY_TRY_CUDA(E, F.sum64.ensure(npx * 3));
+        SALTY_TRY_CUDA(E, F.sumsq64.ensure(npx * 3));
+        SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sum64.p, 0, npx * 3 * sizeof(double), st));
+        SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sumsq64.p, 0, npx * 3 * sizeof(double), st));
+    } else {
+        SALTY_TRY_CUDA(E, F.sum.ensure(npx * 3));
+        SALTY_TRY_CUDA(E, F.comp.ensure(npx * 3));
+        SALTY_TRY_CUDA(E, F.sumsq.ensure(npx * 3));
+        SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sum.p, 0, npx * 3 * sizeof(float), st));
+        SALTY_TRY_CUDA(E, cudaMemsetAsync(F.comp.p, 0, npx * 3 * sizeof(float), st));
+        SALTY_TRY_CUDA(E, cudaMemsetAsync(F.sumsq.p, 0, npx * 3 * sizeof(float), st));
     }
-    if (o.spp == 0) {
-        if (stats) { stats->samples = F.samples; }
+    return SALTY_OK;
+}
+
+// PinholeCamera::Update (include/s3d_camera.h:63-90), host floats, aspect of the frame
+Camera camera_of(const SceneConsts& k, int width, int height) {
+    Camera c;
+    float aspect = (float)width / (float)height;
+    float dir[3] = {k.cam_target[0] - k.cam_pos[0], k.cam_target[1] - k.cam_pos[1], k.cam_target[2] - k.cam_pos[2]};
+    auto unitv = [](float* v) {
+        float m = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        v[0] /= m; v[1] /= m; v[2] /= m;
+    };
+    auto crossv = [](const float* a, const float* b, float* r) {
+        r[0] = a[1] * b[2] - a[2] * b[1];
+        r[1] = a[2] * b[0] - a[0] * b[2];
+        r[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    unitv(dir);
+    float cx[3], cy[3];
+    crossv(dir, k.cam_up, cx);
+    unitv(cx);
+    for (int a = 0; a < 3; ++a) cx[a] = cx[a] * k.cam_fov * aspect;
+    crossv(dir, cx, cy);
+    unitv(cy);
+    for (int a = 0; a < 3; ++a) {
+        cy[a] = cy[a] * k.cam_fov;
+        c.pos[a] = k.cam_pos[a];
+        c.cx[a] = cx[a];
+        c.cy[a] = cy[a];
+        c.cz[a] = k.cam_pos[a] + dir[a] * k.cam_near;
+    }
+    return c;
+}
+
+// Builds (or reuses) the arena of a batch; offsets per slot in ctx->arena.
+salty_status ensure_arena(salty_ctx* ctx, salty_scene* const* scenes, int n) {
+    auto& E = ctx->err;
+    BatchArena& A = ctx->arena;
+    std::vector<std::pair<const void*, uint64_t>> key(n);
+    for (int i = 0; i < n; ++i) key[i] = {scenes[i], scenes[i]->bvh.generation};
+    if (key == A.key && A.nodes.p) return SALTY_OK;
+    A.key.clear();
+    long long nn = 0, nl = 0, nt = 0, nm = 0;
+    A.node_off.assign(n, 0);
+    A.id_off.assign(n, 0);
+    std::vector<long long> leaf_off(n), mat_off(n);
+    int depth = 0;
+    for (int i = 0; i < n; ++i) {
+        const salty_scene* sc = scenes[i];
+        A.node_off[i] = nn;
+        leaf_off[i] = nl;
+        A.id_off[i] = nt;
+        mat_off[i] = nm;
+        nn += sc->bvh.n_nodes;
+        nl += sc->bvh.n_tris;
+        nt += sc->n_tris;
+        nm += sc->n_mats;
+        depth = std::max(depth, (int)sc->bvh.depth);
+    }
+    if (nn >= (1ll << 31) || nl >= (1ll << 31) || nt >= (1ll << 31))
+        return E.fail(SALTY_ERR_CAPACITY, "a batch holds at most 2^31 - 1 nodes and triangles");
+    SALTY_TRY_CUDA(E, A.nodes.ensure(nn));
+    SALTY_TRY_CUDA(E, A.tris.ensure(nl * kTriFloat4));
+    SALTY_TRY_CUDA(E, A.pos.ensure(nt * 9));
+    SALTY_TRY_CUDA(E, A.nrm.ensure(nt * 9));
+    SALTY_TRY_CUDA(E, A.mat.ensure(nt));
+    SALTY_TRY_CUDA(E, A.mats.ensure(nm));
+    cudaStream_t st = ctx->stream;
+    for (int i = 0; i < n; ++i) {
+        const salty_scene* sc = scenes[i];
+        const int g = ctx->num_sms * 4;
+        k_arena_nodes<<<g, 256, 0, st>>>(sc->bvh.nodes.p, sc->bvh.n_nodes, (unsigned)A.node_off[i],
+                                         (unsigned)leaf_off[i], A.nodes.p + A.node_off[i]);
+        k_arena_tris<<<g, 256, 0, st>>>(sc->bvh.tris.p, sc->bvh.n_tris, (int)A.id_off[i],
+                                        A.tris.p + leaf_off[i] * kTriFloat4);
+        k_arena_mat<<<g, 256, 0, st>>>(sc->mat.p, sc->n_tris, (int)mat_off[i], A.mat.p + A.id_off[i]);
+        SALTY_TRY_CUDA(E, cudaMemcpyAsync(A.pos.p + A.id_off[i] * 9, sc->pos.p, sc->n_tris * 9 * sizeof(float),
+                                          cudaMemcpyDeviceToDevice, st));
+        SALTY_TRY_CUDA(E, cudaMemcpyAsync(A.nrm.p + A.id_off[i] * 9, sc->nrm.p, sc->n_tris * 9 * sizeof(float),
+                                          cudaMemcpyDeviceToDevice, st));
+        SALTY_TRY_CUDA(E, cudaMemcpyAsync(A.mats.p + mat_off[i], sc->mats.p, sc->n_mats * sizeof(GpuMaterial),
+                                          cudaMemcpyDeviceToDevice, st));
+    }
+    SALTY_TRY_CUDA(E, cudaGetLastError());
+    SALTY_TRY_CUDA(E, cudaStreamSynchronize(st));
+    A.depth = depth;
+    A.key = key;
+    return SALTY_OK;
+}
+
+}  // namespace
+
+salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salty_render_opts* opts, int n,
+                          salty_render_stats* total) {
+    auto& E = ctx->err;
+    cudaStream_t st = ctx->stream;
+    if (n < 1 || n > kMaxSlots) return E.fail(SALTY_ERR_INVALID_ARG, "a batch holds 1..%d scenes", kMaxSlots);
+    for (int i = 0; i < n; ++i) SALTY_TRY(prepare_film(ctx, scenes[i], opts[i]));
+    // what the traversal walks: the scene itself, or the batch arena
+    TraceTarget tgt;
+    const float *pos, *nrm;
+    const int* mat;
+    const GpuMaterial* mats;
+    if (n == 1) {
+        tgt.nodes = scenes[0]->bvh.nodes.p;
+        tgt.tris = scenes[0]->bvh.tris.p;
+        tgt.depth = scenes[0]->bvh.depth;
+        pos = scenes[0]->pos.p;
+        nrm = scenes[0]->nrm.p;
+        mat = scenes[0]->mat.p;
+        mats = scenes[0]->mats.p;
+    } else {
+        SALTY_TRY(ensure_arena(ctx, scenes, n));
+        const BatchArena& A = ctx->arena;
+        tgt.nodes = A.nodes.p;
+        tgt.tris = A.tris.p;
+        tgt.depth = A.depth;
+        pos = A.pos.p;
+        nrm = A.nrm.p;
+        mat = A.mat.p;
+        mats = A.mats.p;
+    }
+    // slot table
+    std::vector<SceneSlot> slots(n);
+    std::vector<long long> offs(2 * (n + 1));
+    long long* sample_off = offs.data();
+    long long* pixel_off = offs.data() + n + 1;
+    long long samples = 0, pixels = 0;
+    int max_depth = 0;
+    for (int i = 0; i < n; ++i) {
+        const salty_render_opts& o = opts[i];
+        salty_scene* sc = scenes[i];
+        Film& F = sc->film;
+        SceneSlot& S = slots[i];
+        std::memset(&S, 0, sizeof S);
+        S.k = sc->consts;
+        if (n > 1 && S.k.light_tri0 >= 0) S.k.light_tri0 += (int)ctx->arena.id_off[i];
+        S.cam = camera_of(sc->consts, o.width, o.height);
+        S.width = o.width;
+        S.height = o.height;
+        S.crop_x = F.crop_x;
+        S.crop_y = F.crop_y;
+        S.film_w = F.width;
+        S.film_h = F.height;
+        S.spp = o.spp;
+        S.max_depth = o.max_depth;
+        S.rr_depth = o.rr_depth;
+        S.profile = o.profile;
+        S.root = n > 1 ? (int)ctx->arena.node_off[i] : 0;
+        S.npx = (long long)F.width * F.height;
+        S.seed = o.seed + 0x9e3779b97f4a7c15ull * (unsigned long long)F.samples;  // new streams per progressive call
+        if (o.fp64) {
+            S.sum64 = F.sum64.p;
+            S.sumsq64 = F.sumsq64.p;
+        } else {
+            S.sum = F.sum.p;
+            S.comp = F.comp.p;
+            S.sumsq = F.sumsq.p;
+        }
+        S.aov = F.aov.p;
+        sample_off[i] = samples;
+        pixel_off[i] = pixels;
+        samples += S.npx * o.spp;
+        pixels += S.npx;
+        if (o.spp > 0) max_depth = std::max(max_depth, o.max_depth);
+        if (o.profile != opts[0].profile)
+            return E.fail(SALTY_ERR_INVALID_ARG, "the scenes of a batch share one profile");
+    }
+    sample_off[n] = samples;
+    pixel_off[n] = pixels;
+    if (samples == 0) {
+        if (total) *total = salty_render_stats{};
         return SALTY_OK;
     }
-    const long long total = npx * o.spp;
-    long long cap = std::min<long long>(total, 1ll << 22);
-    WaveStore S;
+    const size_t slot_bytes = (size_t)n * sizeof(SceneSlot), off_bytes = offs.size() * sizeof(long long);
+    const size_t slot_region = (slot_bytes + 255) / 256 * 256;
+    SALTY_TRY_CUDA(E, ctx->slots.ensure(slot_region + off_bytes));
+    unsigned char* dslots = ctx->slots.p;
+    long long* doffs = reinterpret_cast<long long*>(dslots + slot_region);
+    SALTY_TRY_CUDA(E, cudaMemcpyAsync(dslots, slots.data(), slot_bytes, cudaMemcpyHostToDevice, st));
+    SALTY_TRY_CUDA(E, cudaMemcpyAsync(doffs, offs.data(), off_bytes, cudaMemcpyHostToDevice, st));
+
+    // queues
+    const Tuning& T = ctx->tune;
+    const long long cap = std::min<long long>(samples, T.wave_paths);
+    WaveStore& S = ctx->waves;
+    const bool batch = n > 1;
     for (int i = 0; i < 2; ++i) {
         SALTY_TRY_CUDA(E, S.rays[i].ensure(cap * 2));
         SALTY_TRY_CUDA(E, S.W[i].ensure(cap));
         SALTY_TRY_CUDA(E, S.L[i].ensure(cap));
         SALTY_TRY_CUDA(E, S.meta[i].ensure(cap));
+        if (batch) SALTY_TRY_CUDA(E, S.roots[i].ensure(cap));
     }
+    if (batch) SALTY_TRY_CUDA(E, S.sroots.ensure(cap * 2));
     SALTY_TRY_CUDA(E, S.hits.ensure(cap));
     SALTY_TRY_CUDA(E, S.nee.ensure(cap * 2));
     SALTY_TRY_CUDA(E, S.srays.ensure(cap * 4));
@@ -749,61 +1123,27 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
     SALTY_TRY_CUDA(E, cudaMemsetAsync(S.counts.p, 0, 8 * sizeof(int), st));
     SALTY_TRY_CUDA(E, cudaMemsetAsync(S.wave.p, 0, sizeof(long long), st));
     SALTY_TRY_CUDA(E, cudaMemsetAsync(S.stats.p, 0, 4 * sizeof(unsigned long long), st));
+    SALTY_TRY_CUDA(E, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), st));
 
     WaveParams P;
-    P.pos = sc->pos.p;
-    P.nrm = sc->nrm.p;
-    P.mat = sc->mat.p;
-    P.mats = sc->mats.p;
-    P.k = sc->consts;
-    {
-        // PinholeCamera::Update (include/s3d_camera.h:63-90), host floats
-        const SceneConsts& k = sc->consts;
-        float aspect = (float)o.width / (float)o.height;
-        float dir[3] = {k.cam_target[0] - k.cam_pos[0], k.cam_target[1] - k.cam_pos[1], k.cam_target[2] - k.cam_pos[2]};
-        auto unitv = [](float* v) {
-            float m = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-            v[0] /= m; v[1] /= m; v[2] /= m;
-        };
-        auto crossv = [](const float* a, const float* b, float* r) {
-            r[0] = a[1] * b[2] - a[2] * b[1];
-            r[1] = a[2] * b[0] - a[0] * b[2];
-            r[2] = a[0] * b[1] - a[1] * b[0];
-        };
-        unitv(dir);
-        float cx[3], cy[3];
-        crossv(dir, k.cam_up, cx);
-        unitv(cx);
-        for (int a = 0; a < 3; ++a) cx[a] = cx[a] * k.cam_fov * aspect;
-        crossv(dir, cx, cy);
-        unitv(cy);
-        for (int a = 0; a < 3; ++a) {
-            cy[a] = cy[a] * k.cam_fov;
-            P.cam.pos[a] = k.cam_pos[a];
-            P.cam.cx[a] = cx[a];
-            P.cam.cy[a] = cy[a];
-            P.cam.cz[a] = k.cam_pos[a] + dir[a] * k.cam_near;
-        }
-    }
-    P.width = o.width;
-    P.height = o.height;
-    P.crop_x = cx;
-    P.crop_y = cy;
-    P.film_w = fw;
-    P.film_h = fh;
-    P.spp = o.spp;
-    P.max_depth = o.max_depth;
-    P.rr_depth = o.rr_depth;
-    P.profile = o.profile;
-    P.seed = o.seed + 0x9e3779b97f4a7c15ull * (unsigned long long)F.samples;  // new streams per progressive call
-    P.total_samples = total;
+    P.pos = pos;
+    P.nrm = nrm;
+    P.mat = mat;
+    P.mats = mats;
+    P.slots = reinterpret_cast<const SceneSlot*>(dslots);
+    P.sample_off = doffs;
+    P.pixel_off = doffs + n + 1;
+    P.n_slots = n;
     P.capacity = (int)cap;
+    P.total_samples = samples;
 
     WaveBuffers B;
     for (int i = 0; i < 2; ++i) {
         B.rays[i] = S.rays[i].p;
         B.path[i] = PathSoA{S.W[i].p, S.L[i].p, S.meta[i].p};
+        B.roots[i] = batch ? S.roots[i].p : nullptr;
     }
+    B.sroots = batch ? S.sroots.p : nullptr;
     B.hits = S.hits.p;
     B.nee = S.nee.p;
     B.srays = S.srays.p;
@@ -814,10 +1154,14 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
     B.wave = S.wave.p;
     B.stats = S.stats.p;
 
-    const bool compat = o.profile == SALTY_PROFILE_COMPAT;
+    const bool compat = opts[0].profile == SALTY_PROFILE_COMPAT;
     const uint32_t ext_flags = compat ? 0u : (uint32_t)SALTY_TRACE_WATERTIGHT;
     const uint32_t sh_flags = compat ? 0u : (uint32_t)(SALTY_TRACE_WATERTIGHT | SALTY_TRACE_ANY_HIT);
-    const int sgrid = ctx->num_sms * 8;
+    const int sb = T.shade_block;
+    const int sgrid = grid_of(cap, 2048 / sb, ctx->num_sms, sb);
+    TraceTarget ext = tgt, shd = tgt;
+    ext.roots = B.roots[0];
+    shd.roots = B.sroots;
 
     cudaEvent_t e0 = ctx->ev[0], e1 = ctx->ev[1];
     SALTY_TRY_CUDA(E, cudaEventRecord(e0, st));
@@ -827,25 +1171,24 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
     SALTY_TRY_CUDA(E, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     salty_status cap_status = SALTY_OK;
     do {
-        k_generate<<<sgrid, 256, 0, st>>>(P, B);
+        k_generate<<<sgrid, sb, 0, st>>>(P, B);
         int q = 0;
-        for (int depth = 0; depth < o.max_depth; ++depth) {
-            cap_status = trace_launch(ctx, sc, B.rays[q], cap, &B.counts[q], ext_flags, B.hits, S.tc0.p, st,
+        for (int depth = 0; depth < max_depth; ++depth) {
+            ext.roots = B.roots[q];
+            cap_status = trace_launch(ctx, ext, T.trace, B.rays[q], cap, &B.counts[q], ext_flags, B.hits, S.tc0.p, st,
                                       ctx->status.p);
             if (cap_status != SALTY_OK) break;
-            k_shade1<<<sgrid, 256, 0, st>>>(P, B, q);
-            cap_status = trace_launch(ctx, sc, B.srays, 2 * cap, &B.counts[2], sh_flags, B.shits, S.tc1.p, st,
-                                      ctx->status.p);
+            k_shade1<<<sgrid, sb, 0, st>>>(P, B, q);
+            cap_status = trace_launch(ctx, shd, T.trace, B.srays, 2 * cap, &B.counts[2], sh_flags, B.shits, S.tc1.p,
+                                      st, ctx->status.p);
             if (cap_status != SALTY_OK) break;
-            k_shade2<<<sgrid, 256, 0, st>>>(P, B, q, depth);
+            k_shade2<<<sgrid, sb, 0, st>>>(P, B, q, depth);
             k_count_rays<<<1, 1, 0, st>>>(B, q);
             k_reset_queue<<<1, 1, 0, st>>>(B, q);
             q ^= 1;
         }
         if (cap_status != SALTY_OK) break;
-        k_accumulate<<<sgrid, 256, 0, st>>>(P, B, o.fp64 ? nullptr : F.sum.p, o.fp64 ? nullptr : F.comp.p,
-                                            o.fp64 ? nullptr : F.sumsq.p, o.fp64 ? F.sum64.p : nullptr,
-                                            o.fp64 ? F.sumsq64.p : nullptr, F.aov.p);
+        k_accumulate<<<grid_of(std::min<long long>(pixels, cap), 2048 / 256, ctx->num_sms), 256, 0, st>>>(P, B);
         k_next_wave<<<1, 1, 0, st>>>(P, B);
     } while (0);
     cudaError_t ce = cudaStreamEndCapture(st, &graph);
@@ -855,7 +1198,7 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
     }
     SALTY_TRY_CUDA(E, ce);
     SALTY_TRY_CUDA(E, cudaGraphInstantiate(&exec, graph, 0));
-    const long long waves = (total + cap - 1) / cap;
+    const long long waves = (samples + cap - 1) / cap;
     salty_status rs = SALTY_OK;
     for (long long w = 0; w < waves; ++w) {
         if (ctx->cancel) { rs = E.fail(SALTY_ERR_CANCELLED, "render cancelled"); break; }
@@ -877,13 +1220,20 @@ salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o,
     SALTY_TRY_CUDA(E, cudaMemcpy(hs, S.stats.p, sizeof hs, cudaMemcpyDeviceToHost));
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
-    F.samples += o.spp;
-    if (stats) {
-        stats->ms = ms;
-        stats->samples = F.samples;
-        stats->rays = (int64_t)hs[0];
-        stats->paths = (int64_t)hs[1];
+    for (int i = 0; i < n; ++i) scenes[i]->film.samples += opts[i].spp;
+    if (total) {
+        total->ms = ms;
+        total->samples = n == 1 ? scenes[0]->film.samples : samples;
+        total->rays = (int64_t)hs[0];
+        total->paths = (int64_t)hs[1];
     }
+    return SALTY_OK;
+}
+
+salty_status render(salty_ctx* ctx, salty_scene* sc, const salty_render_opts& o, salty_render_stats* stats) {
+    salty_scene* one[1] = {sc};
+    SALTY_TRY(render_batch(ctx, one, &o, 1, stats));
+    if (stats) stats->samples = sc->film.samples;
     return SALTY_OK;
 }
 

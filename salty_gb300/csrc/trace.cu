@@ -1,35 +1,35 @@
 // trace.cu -- closest-hit / any-hit kernels over ray arrays in HBM.
 //
-// Persistent warps: each warp takes 32 consecutive rays from a global cursor, traces
-// them (one thread per ray, traverse.cuh) and takes the next 32 when all are done.  Rays
+// Persistent warps: each warp takes a pool of consecutive rays from a global cursor, traces
+// them (one thread per ray, traverse.cuh) and refills a lane as soon as its walk ends.  Rays
 // are two float4 (org, tmin | dir, tmax) and hits one float4 (t, id, u, v): both read and
 // written fully coalesced.  Replaces the per-pixel Scene::Intersect calls of the
 // reference's OpenMP row loop (src/s3d_pt.cpp:310-333, include/s3d_scene.h:63-75).
+//
+// A launch walks one BVH, or a batch arena holding several scenes' BVHs back to back; then
+// every ray names the root node of its scene.
 #include "internal.h"
 #include "traverse.cuh"
 
 namespace salty {
 namespace {
 
-constexpr int kTraceBlock = 128;
-constexpr int kPool = 128;          // rays taken from the global cursor per refill
-constexpr int kPostponeLanes = 7;   // test triangles only with at least this many lanes
-
 // counters: [0] ray cursor, [1] node fetches, [2] triangle fetches
-template <bool ANY, bool WT, bool COUNT, int DEPTH>
-__global__ void __launch_bounds__(kTraceBlock)
+template <bool ANY, bool WT, bool COUNT, int DEPTH, int TB>
+__global__ void __launch_bounds__(TB)
 k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, const float4* __restrict__ rays,
-        long long n_arg, const int* __restrict__ n_dev, float4* __restrict__ hits,
-        unsigned long long* __restrict__ counters, float cull_slack, int* __restrict__ status) {
-    __shared__ uint2 sstack[DEPTH * kTraceBlock];
-    TravStack<DEPTH> st{sstack + threadIdx.x, kTraceBlock};
+        const int* __restrict__ roots, long long n_arg, const int* __restrict__ n_dev, float4* __restrict__ hits,
+        unsigned long long* __restrict__ counters, float cull_slack, int pool, int postpone,
+        int* __restrict__ status) {
+    __shared__ uint2 sstack[DEPTH * TB];
+    TravStack<DEPTH> st{sstack + threadIdx.x, TB};
     const int lane = threadIdx.x & 31;
     // queue length from device memory when given (wavefront queues), else the argument
     const long long n = n_dev ? (long long)*n_dev : n_arg;
     const unsigned lt_mask = (1u << lane) - 1u;
     TravCount cnt{0, 0};
     int overflow = 0;
-    // Warp-uniform pool of ray indices [pool_next, pool_end), refilled kPool at a time
+    // Warp-uniform pool of ray indices [pool_next, pool_end), refilled `pool` at a time
     // from the global cursor; each lane holds one ray and takes a new one from the pool
     // as soon as its walk ends.
     long long pool_next = 0, pool_end = 0;
@@ -43,18 +43,18 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
         if (idle_mask) {
             if (pool_next >= pool_end && !drained) {
                 unsigned long long base = 0;
-                if (lane == 0) base = atomicAdd(&counters[0], (unsigned long long)kPool);
+                if (lane == 0) base = atomicAdd(&counters[0], (unsigned long long)pool);
                 base = __shfl_sync(0xffffffffu, base, 0);
                 pool_next = (long long)base;
-                pool_end = min((long long)base + kPool, n);
-                if ((long long)base + kPool >= n) drained = true;
+                pool_end = min((long long)base + pool, n);
+                if ((long long)base + pool >= n) drained = true;
             }
             const long long mine = pool_next + __popc(idle_mask & lt_mask);
             if (idle && mine < pool_end) {
                 rid = mine;
                 const float4 ra = __ldcs(rays + 2 * rid), rb = __ldcs(rays + 2 * rid + 1);
                 make_trav_ray(r, ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w);
-                trav_init(s, r);
+                trav_init(s, r, roots ? (unsigned)__ldcs(roots + rid) : 0u);
             }
             pool_next = min(pool_end, pool_next + __popc(idle_mask));
         }
@@ -66,7 +66,7 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
         const bool want = active && s.tg_hits != 0;
         const unsigned want_mask = __ballot_sync(0xffffffffu, want);
         bool run = want;
-        if (want && __popc(want_mask) < kPostponeLanes && s.ng_hits != 0 && s.sp < DEPTH) {
+        if (want && __popc(want_mask) < postpone && s.ng_hits != 0 && s.sp < DEPTH) {
             st.at(s.sp++) = make_uint2(s.tg_base, s.tg_hits | kTriGroupFlag);
             s.tg_hits = 0;
             run = false;
@@ -92,34 +92,52 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
     if (overflow) atomicOr(status, 1);
 }
 
-template <bool ANY, bool WT, bool COUNT, int DEPTH>
-salty_status launch(salty_ctx* ctx, salty_scene* sc, const float4* rays, long long n, const int* n_dev, float4* hits,
-                    unsigned long long* counters, cudaStream_t st, float cull_slack, int* status) {
-    auto kern = k_trace<ANY, WT, COUNT, DEPTH>;
+struct Launch {
+    const TraceTarget& tgt;
+    const float4* rays;
+    long long n;
+    const int* n_dev;
+    float4* hits;
+    unsigned long long* counters;
+    cudaStream_t st;
+    float slack;
+    int pool, postpone;
+    int* status;
+};
+
+template <bool ANY, bool WT, bool COUNT, int DEPTH, int TB>
+salty_status launch(salty_ctx* ctx, const Launch& L) {
+    auto kern = k_trace<ANY, WT, COUNT, DEPTH, TB>;
     int per_sm = 0;
-    SALTY_TRY_CUDA(ctx->err, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTraceBlock, 0));
+    SALTY_TRY_CUDA(ctx->err, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, 0));
     if (per_sm < 1) per_sm = 1;
-    long long want = (n + kTraceBlock - 1) / kTraceBlock;
+    long long want = (L.n + TB - 1) / TB;
     long long grid = (long long)ctx->num_sms * per_sm;
     if (grid > want) grid = want;
     if (grid < 1) grid = 1;
-    kern<<<(unsigned)grid, kTraceBlock, 0, st>>>(sc->bvh.nodes.p, sc->bvh.tris.p, rays, n, n_dev, hits, counters,
-                                                cull_slack, status);
+    kern<<<(unsigned)grid, TB, 0, L.st>>>(L.tgt.nodes, L.tgt.tris, L.rays, L.tgt.roots, L.n, L.n_dev, L.hits,
+                                          L.counters, L.slack, L.pool, L.postpone, L.status);
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;
 }
 
+template <int DEPTH, int TB>
+salty_status dispatch_flags(salty_ctx* ctx, const Launch& L, uint32_t flags) {
+    const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT;
+#define SALTY_L(A, W) \
+    if (any == A && wt == W) return launch<A, W, false, DEPTH, TB>(ctx, L)
+    SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
+#undef SALTY_L
+    return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad trace flags");
+}
+
+// Counting walks (node and triangle fetches) use the default launch shape.
 template <int DEPTH>
-salty_status dispatch_depth(salty_ctx* ctx, salty_scene* sc, const float4* rays, long long n, const int* n_dev,
-                            uint32_t flags, float4* hits, unsigned long long* counters, cudaStream_t st,
-                            int* status) {
-    const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT,
-               cnt = flags & SALTY_TRACE_COUNTERS;
-    const float slack = wt ? (1.0f / 65536.0f) : 1e-3f;
-#define SALTY_L(A, W, C) \
-    if (any == A && wt == W && cnt == C) return launch<A, W, C, DEPTH>(ctx, sc, rays, n, n_dev, hits, counters, st, slack, status)
-    SALTY_L(false, false, false); SALTY_L(false, false, true); SALTY_L(false, true, false); SALTY_L(false, true, true);
-    SALTY_L(true, false, false); SALTY_L(true, false, true); SALTY_L(true, true, false); SALTY_L(true, true, true);
+salty_status dispatch_count(salty_ctx* ctx, const Launch& L, uint32_t flags) {
+    const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT;
+#define SALTY_L(A, W) \
+    if (any == A && wt == W) return launch<A, W, true, DEPTH, 128>(ctx, L)
+    SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
 #undef SALTY_L
     return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad trace flags");
 }
@@ -128,16 +146,39 @@ salty_status dispatch_depth(salty_ctx* ctx, salty_scene* sc, const float4* rays,
 
 // Traces rays already resident on the device: n of them, or *n_dev when n_dev is given
 // (then n is the capacity used to size the grid).  counters (3 x u64) are zeroed here.
+salty_status trace_launch(salty_ctx* ctx, const TraceTarget& tgt, const TraceTuning& tune, const float4* d_rays,
+                          long long n, const int* n_dev, uint32_t flags, float4* d_hits,
+                          unsigned long long* d_counters, cudaStream_t st, int* d_status) {
+    SALTY_TRY_CUDA(ctx->err, cudaMemsetAsync(d_counters, 0, 3 * sizeof(unsigned long long), st));
+    const bool wt = flags & SALTY_TRACE_WATERTIGHT;
+    Launch L{tgt, d_rays, n, n_dev, d_hits, d_counters, st, wt ? (1.0f / 65536.0f) : 1e-3f,
+             tune.pool >= 32 ? tune.pool : 32, tune.postpone, d_status};
+    // Each BVH level can hold one pending node group and one postponed triangle group.
+    const int need = 2 * tgt.depth + 1;
+    if (need > 48) return ctx->err.fail(SALTY_ERR_CAPACITY, "BVH depth %d exceeds the traversal stack (23 levels)",
+                                        tgt.depth);
+    const bool shallow = need <= 24;
+    if (flags & SALTY_TRACE_COUNTERS)
+        return shallow ? dispatch_count<24>(ctx, L, flags) : dispatch_count<48>(ctx, L, flags);
+    // the 48-deep stack of a 256-thread block would not fit the 48 KB of static shared memory
+    const int tb = (!shallow && tune.block > 128) ? 128 : tune.block;
+    if (shallow) {
+        if (tb == 64) return dispatch_flags<24, 64>(ctx, L, flags);
+        if (tb == 256) return dispatch_flags<24, 256>(ctx, L, flags);
+        return dispatch_flags<24, 128>(ctx, L, flags);
+    }
+    if (tb == 64) return dispatch_flags<48, 64>(ctx, L, flags);
+    return dispatch_flags<48, 128>(ctx, L, flags);
+}
+
 salty_status trace_launch(salty_ctx* ctx, salty_scene* sc, const float4* d_rays, long long n, const int* n_dev,
                           uint32_t flags, float4* d_hits, unsigned long long* d_counters, cudaStream_t st,
                           int* d_status) {
-    SALTY_TRY_CUDA(ctx->err, cudaMemsetAsync(d_counters, 0, 3 * sizeof(unsigned long long), st));
-    // Each BVH level can hold one pending node group and one postponed triangle group.
-    if (2 * sc->bvh.depth + 1 <= 24)
-        return dispatch_depth<24>(ctx, sc, d_rays, n, n_dev, flags, d_hits, d_counters, st, d_status);
-    if (2 * sc->bvh.depth + 1 <= 48)
-        return dispatch_depth<48>(ctx, sc, d_rays, n, n_dev, flags, d_hits, d_counters, st, d_status);
-    return ctx->err.fail(SALTY_ERR_CAPACITY, "BVH depth %d exceeds the traversal stack (23 levels)", sc->bvh.depth);
+    TraceTarget t;
+    t.nodes = sc->bvh.nodes.p;
+    t.tris = sc->bvh.tris.p;
+    t.depth = sc->bvh.depth;
+    return trace_launch(ctx, t, ctx->tune.trace, d_rays, n, n_dev, flags, d_hits, d_counters, st, d_status);
 }
 
 }  // namespace salty

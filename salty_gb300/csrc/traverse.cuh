@@ -245,8 +245,9 @@ struct TravState {
 // Stack entries with this flag in .y are postponed triangle groups.
 constexpr unsigned kTriGroupFlag = 0x80000000u;
 
-__device__ __forceinline__ void trav_init(TravState& s, const TravRay& r) {
-    s.ng_base = 0;
+// root: index of the BVH's root node (0 for one scene; a scene's offset in a batch arena)
+__device__ __forceinline__ void trav_init(TravState& s, const TravRay& r, unsigned root = 0) {
+    s.ng_base = root;
     s.ng_hits = 1u << r.oct;  // a group holding only the root, in slot 0
     s.ng_imask = 1u;
     s.tg_base = 0;

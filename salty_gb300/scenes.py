@@ -10,7 +10,7 @@ import math
 
 import numpy as np
 
-from . import GGX, GLASS, LAMBERT, MIRROR, microbench_soup
+from . import GGX, GLASS, LAMBERT, MIRROR, PHONG, PLASTIC, microbench_soup
 
 
 def _quad(p0, p1, p2, p3):
@@ -51,7 +51,9 @@ def cornell(variant: str = "baseline") -> dict:
     red "left" wall is the x = 1 plane.
 
     variant "baseline": all Lambert.  "mixed": tall box mirror, short box glass (IOR 1.5),
-    back wall GGX (roughness 0.3) -- exercises every BSDF."""
+    back wall GGX (roughness 0.3) -- exercises every BSDF.  "glossy": tall box Phong
+    (specular 0.8, power 40), short box Plastic (diffuse (0.2, 0.4, 0.7), specular 0.6,
+    power 120), back wall Phong (power 8)."""
     W, R, G = (0.75, 0.75, 0.75), (0.75, 0.25, 0.25), (0.25, 0.75, 0.25)
     mats = [{"type": LAMBERT, "color": W}, {"type": LAMBERT, "color": R}, {"type": LAMBERT, "color": G}]
     tall_m = short_m = back_m = 0
@@ -59,6 +61,11 @@ def cornell(variant: str = "baseline") -> dict:
         mats += [{"type": MIRROR, "color": (0.9, 0.9, 0.9)},
                  {"type": GLASS, "color": (1.0, 1.0, 1.0), "ior": 1.5},
                  {"type": GGX, "color": (0.8, 0.6, 0.3), "roughness": 0.3}]
+        tall_m, short_m, back_m = 3, 4, 5
+    elif variant == "glossy":
+        mats += [{"type": PHONG, "color": (0.8, 0.8, 0.8), "power": 40.0},
+                 {"type": PLASTIC, "color": (0.2, 0.4, 0.7), "specular": (0.6, 0.6, 0.6), "power": 120.0},
+                 {"type": PHONG, "color": (0.7, 0.7, 0.6), "power": 8.0}]
         tall_m, short_m, back_m = 3, 4, 5
     tris, mid = [], []
 
@@ -218,3 +225,23 @@ def upload(ctx, scene: dict):
     """Context.upload_scene with a scene dict from this module."""
     kw = {k: v for k, v in scene.items() if k != "name"}
     return ctx.upload_scene(**kw)
+
+
+def batch_scene(seed: int) -> tuple[dict, dict]:
+    """One scene of the batched-render workload and its render options: a triangle soup or
+    a heightfield (even odds) with a triangle count log-uniform in [1e3, 1e6], a square
+    resolution from {64, 128, 256, 512} and 4, 16 or 64 samples per pixel, all drawn from
+    `seed`.  The heightfield keeps the 1080p scene's make-up at a smaller size: ~60% of the
+    triangles in the terrain, the rest in subdivision-2 icospheres (320 triangles each)."""
+    rng = np.random.default_rng(seed)
+    n = int(round(math.exp(rng.uniform(math.log(1e3), math.log(1e6)))))
+    res = int(rng.choice([64, 128, 256, 512]))
+    spp = int(rng.choice([4, 16, 64]))
+    if rng.random() < 0.5:
+        d = soup(n, seed=int(rng.integers(1 << 31)))
+    else:
+        grid = max(4, int(math.sqrt(0.6 * n / 2)))
+        n_sph = max(1, int((n - 2 * grid * grid) / 320))
+        d = heightfield(grid=grid, n_spheres=n_sph, seed=int(rng.integers(1 << 31)), subdiv=2)
+    opts = {"width": res, "height": res, "spp": spp, "max_depth": 8, "seed": int(rng.integers(1 << 31))}
+    return d, opts

@@ -78,9 +78,9 @@ def decode_png(path: str) -> np.ndarray:
     return out.reshape(h, w, 3)
 
 
-def cornell_scene() -> SceneData:
+def cornell_scene(variant: str = "baseline") -> SceneData:
     from salty_gb300 import scenes  # noqa: E402  (numpy-only module)
-    sc = scenes.cornell("baseline")
+    sc = scenes.cornell(variant)
     return SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], None,
                      sc["sky"], sc["camera"])
 
@@ -93,9 +93,25 @@ def hdr_image(seed: int, w: int, h: int) -> np.ndarray:
     return img
 
 
+def glossy_fixture(r) -> None:
+    """The Cornell box with Phong and Plastic surfaces through PathTracer::Radiance."""
+    sc = cornell_scene("glossy")
+    W = H = 48
+    spp, depth = 1024, 8
+    total, sq, secs = r.render(sc, W, H, spp, depth, seed=777)
+    mean = total / spp
+    var = (sq / spp - mean * mean) * spp / (spp - 1) / spp
+    np.savez_compressed(os.path.join(HERE, "cornell_glossy_ref_48.npz"), mean=mean.astype(np.float32),
+                        var=np.maximum(var, 0).astype(np.float32), spp=spp, max_bounce=depth, width=W, height=H)
+    print(f"glossy cornell reference render: {secs:.2f} s")
+
+
 def main() -> None:
     build(with_reference=True)
     o, r = Oracle(), Reference()
+    if sys.argv[1:] == ["glossy"]:
+        glossy_fixture(r)
+        return
 
     # 1. traversal: 1M-triangle soup, first 65536 rays of the microbenchmark stream
     tris = o.gen_soup(SOUP_SEED, 1_000_000)
@@ -127,6 +143,7 @@ def main() -> None:
     np.savez_compressed(os.path.join(HERE, "cornell_ref_64.npz"), mean=mean.astype(np.float32),
                         var=np.maximum(var, 0).astype(np.float32), spp=spp, max_bounce=depth, width=W, height=H)
     print(f"cornell reference render: {secs:.2f} s")
+    glossy_fixture(r)
 
     # 4. tonemapping and the sRGB8 capture
     img = hdr_image(99, 48, 32)

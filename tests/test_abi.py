@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol(salty_lib):
 
 
 def test_abi_version(salty_lib):
-    assert salty_lib.salty_abi_version() == 1
+    assert salty_lib.salty_abi_version() == 2
 
 
 def test_context_without_gpu_fails_cleanly(salty_lib):

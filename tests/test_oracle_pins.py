@@ -104,6 +104,44 @@ def test_oracle_compat_render_matches_reference_fixture(oracle):
     assert abs(m.mean() / g["mean"].mean() - 1) < 0.01
 
 
+def test_oracle_compat_glossy_matches_reference_fixture(oracle):
+    """Phong and Plastic (src/s3d_phong.cpp:65-88, src/s3d_plastic.cpp:71-142) through the
+    reference's PathTracer::Radiance."""
+    from oracle.oracle import PROFILE_COMPAT, SceneData
+    from salty_gb300 import scenes
+    g = np.load(os.path.join(GOLDEN, "cornell_glossy_ref_48.npz"))
+    sc = scenes.cornell("glossy")
+    sd = SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], None, sc["sky"],
+                   sc["camera"])
+    spp = int(g["spp"])
+    tot, sq = oracle.render(sd, int(g["width"]), int(g["height"]), spp, int(g["max_bounce"]),
+                            profile=PROFILE_COMPAT, seed=31)
+    m = tot / spp
+    v = np.maximum((sq / spp - m * m) * spp / (spp - 1) / spp, 0)
+    z = zscores(m, v, g["mean"], g["var"])
+    assert np.mean(np.abs(z) > 3) < 0.01
+    assert np.max(np.abs(z)) < 6
+    assert abs(m.mean() / g["mean"].mean() - 1) < 0.01
+
+
+def test_oracle_physical_glossy_is_consistent(oracle):
+    """Physical Phong / Plastic: two independent seeds agree within 3 sigma, and the one-sample
+    mixture of the plastic converges (no NaN, finite variance)."""
+    from oracle.oracle import PROFILE_PHYSICAL, SceneData
+    from salty_gb300 import scenes
+    sc = scenes.cornell("glossy")
+    sd = SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], None, sc["sky"],
+                   sc["camera"])
+    res = []
+    for seed in (1, 2):
+        tot, sq = oracle.render(sd, 32, 32, 256, 8, rr_depth=3, profile=PROFILE_PHYSICAL, seed=seed)
+        m = tot / 256
+        res.append((m, np.maximum((sq / 256 - m * m) * 256 / 255 / 256, 0)))
+    assert all(np.all(np.isfinite(m)) for m, _ in res)
+    z = zscores(res[0][0], res[0][1], res[1][0], res[1][1])
+    assert np.mean(np.abs(z) > 3) < 0.015 and np.max(np.abs(z)) < 6
+
+
 def test_oracle_tonemap_matches_reference_fixture(oracle):
     g = np.load(os.path.join(GOLDEN, "tonemap_ref.npz"))
     img = g["img"]

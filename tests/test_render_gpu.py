@@ -46,7 +46,20 @@ def test_compat_cornell_matches_reference_fixture(ctx):
     assert abs(r["mean"].mean() / g["mean"].mean() - 1) < 0.01
 
 
-@pytest.mark.parametrize("variant", ["baseline", "mixed"])
+def test_compat_glossy_cornell_matches_reference_fixture(ctx):
+    """Phong and Plastic in the reference's estimator vs the GPU compat profile."""
+    import salty_gb300
+    from salty_gb300 import scenes
+    g = np.load(os.path.join(GOLDEN, "cornell_glossy_ref_48.npz"))
+    s = _gpu_scene(ctx, scenes.cornell("glossy"))
+    r = s.render(int(g["width"]), int(g["height"]), int(g["spp"]), int(g["max_bounce"]),
+                 profile=salty_gb300.PROFILE_COMPAT, seed=4343)
+    frac, zmax = zstats(r["mean"], r["var"], g["mean"], g["var"])
+    assert frac < 0.01 and zmax < 6, (frac, zmax)
+    assert abs(r["mean"].mean() / g["mean"].mean() - 1) < 0.01
+
+
+@pytest.mark.parametrize("variant", ["baseline", "mixed", "glossy"])
 def test_physical_cornell_matches_oracle(ctx, oracle, variant):
     import salty_gb300
     from oracle.oracle import PROFILE_PHYSICAL
