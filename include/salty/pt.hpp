@@ -106,9 +106,22 @@ struct PinholeCamera {
     Vector3 Position, Target, Upward{0, 1, 0};
     float Fov = 1.0f;        // the reference's linear screen extent (2 tan(half angle))
     float NearClip = 1.0f;
+    float LensRadius = 0.0f;     // > 0: a thin lens (ThinLensCamera)
+    float FocalDistance = 0.0f;  // 0: |Target - Position|
     void Update(Vector3 position, Vector3 target, Vector3 upward, float fov, float /*aspect: from Config*/,
                 float nearClip) {
         Position = position; Target = target; Upward = upward; Fov = fov; NearClip = nearClip;
+    }
+};
+
+// ThinLensCamera::Update (include/s3d_camera.h:167-196): a pinhole plus a lens radius,
+// focused at the target distance.
+struct ThinLensCamera : PinholeCamera {
+    void Update(Vector3 position, Vector3 target, Vector3 upward, float fov, float aspect, float nearClip,
+                float lensRadius) {
+        PinholeCamera::Update(position, target, upward, fov, aspect, nearClip);
+        LensRadius = lensRadius;
+        FocalDistance = 0.0f;
     }
 };
 
@@ -153,6 +166,8 @@ public:
         put(d.camera.pos, camera_.Position); put(d.camera.target, camera_.Target); put(d.camera.up, camera_.Upward);
         d.camera.fov = camera_.Fov;
         d.camera.near_clip = camera_.NearClip;
+        d.camera.lens_radius = camera_.LensRadius;
+        d.camera.focal_distance = camera_.FocalDistance;
         return d;
     }
 

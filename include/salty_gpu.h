@@ -83,12 +83,19 @@ typedef struct salty_material {
     float power;        /* Phong, Plastic: lobe exponent (> 0) */
 } salty_material;
 
-/* PinholeCamera (include/s3d_camera.h:63-100).  fov is the reference's linear screen
- * half-extent factor (a 40 degree field of view is fov = 2 tan 20 deg). */
+/* PinholeCamera (include/s3d_camera.h:63-100) and ThinLensCamera (:150-267).  fov is the
+ * reference's linear screen half-extent factor (a 40 degree field of view is
+ * fov = 2 tan 20 deg).  lens_radius > 0 makes a thin lens focused at focal_distance
+ * (0: |target - pos|, as ThinLensCamera::Update).  The compat profile reproduces the
+ * reference's lens (offset in the world xy plane, focal plane z = const, a z-aligned
+ * view); the physical profile puts the lens in the camera's screen axes and the focal
+ * plane perpendicular to the view direction. */
 typedef struct salty_camera {
     float pos[3], target[3], up[3];
     float fov;
     float near_clip;
+    float lens_radius;
+    float focal_distance;
 } salty_camera;
 
 typedef struct salty_scene_desc {
@@ -119,6 +126,36 @@ void salty_scene_destroy(salty_ctx* ctx, salty_scene* scene);
  * include/s3d_camera.h:63-90) without touching geometry or BVH.  Render the next frame
  * with accumulate = 0: the film's samples belong to the old view. */
 salty_status salty_scene_set_camera(salty_ctx* ctx, salty_scene* scene, const salty_camera* camera);
+
+/* ---------------------------------------------------------------- meshes */
+/* A mesh in host memory, owned by the library (salty_mesh_free). */
+typedef struct salty_mesh {
+    int64_t n_tris;
+    float* tri_pos;             /* n_tris * 9 */
+    float* tri_nrm;             /* n_tris * 9 vertex normals */
+    float* tri_uv;              /* n_tris * 6 texture coordinates */
+    int32_t* tri_mat;           /* n_tris material indices */
+    int32_t n_mats;
+    salty_material* mats;
+    int32_t* mat_texture;       /* per material: its colour map's texture index, or -1 */
+    int32_t n_textures;
+    const char* texture_names;  /* n_textures x 256 bytes, names relative to the file */
+} salty_mesh;
+
+/* Reads an SMD file (Mesh::LoadFromFile, src/s3d_mesh.cpp:250-465; version 2): matte ->
+ * Lambert, mirror, dielectric -> Glass, glossy -> Phong, plastic.  Texture maps are listed
+ * but not applied.  Triangles with a negative material index take material 0.  ctx may
+ * be NULL (no GPU is needed; errors then come without a message). */
+salty_status salty_mesh_load_smd(salty_ctx* ctx, const char* path, salty_mesh** out);
+void salty_mesh_free(salty_mesh* mesh);
+
+/* Places n_tris triangles by a row-major 3x4 affine matrix (x' = M[0..2].x + M[3], ...):
+ * positions by the matrix, normals by the inverse transpose of its linear part,
+ * renormalised.  Instance (src/s3d_instance.cpp:22-101) keeps one copy of a mesh under
+ * several transforms in a two-level BVH; here each placement is a transformed copy in the
+ * scene's single BVH (same images, memory per copy).  nrm_in/nrm_out may be NULL. */
+salty_status salty_mesh_transform(const float* matrix, int64_t n_tris, const float* pos_in, const float* nrm_in,
+                                  float* pos_out, float* nrm_out);
 
 /* ---------------------------------------------------------------- BVH */
 typedef struct salty_build_opts {

@@ -31,6 +31,13 @@ PROFILE_COMPAT, PROFILE_PHYSICAL = 0, 1
 TM_REINHARD, TM_UNCHARTED2, TM_ACES = 0, 1, 2
 
 
+def reference_dir() -> str | None:
+    """The reference project's source root as oracle/Makefile knows it, if present here."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "ref-dir"], capture_output=True, text=True)
+    d = r.stdout.strip()
+    return d if r.returncode == 0 and d and os.path.isdir(d) else None
+
+
 def build(with_reference: bool | None = None) -> None:
     """Runs oracle/Makefile (the restatement always; the reference when its sources exist)."""
     target = ["all"] if with_reference is None else (["oracle", "ref"] if with_reference else ["oracle"])
@@ -51,7 +58,7 @@ class _Scene(C.Structure):
                 ("sun_dir", C.c_float * 3), ("sun_radiance", C.c_float * 3), ("sun_half_angle", C.c_float),
                 ("sky", C.c_float * 3),
                 ("cam_pos", C.c_float * 3), ("cam_target", C.c_float * 3), ("cam_up", C.c_float * 3),
-                ("cam_fov", C.c_float), ("cam_near", C.c_float)]
+                ("cam_fov", C.c_float), ("cam_near", C.c_float), ("cam_lens", C.c_float), ("cam_focal", C.c_float)]
 
 
 class _Opts(C.Structure):
@@ -73,7 +80,7 @@ class _RefScene(C.Structure):
                 ("light_emission", C.c_float * 3), ("cam_pos", C.c_float * 3),
                 ("cam_target", C.c_float * 3), ("cam_up", C.c_float * 3),
                 ("cam_fov", C.c_float), ("cam_near", C.c_float), ("sky_over_10", C.c_float),
-                ("tmp_dir", C.c_char_p)]
+                ("tmp_dir", C.c_char_p), ("cam_lens", C.c_float)]
 
 
 def _f3(v):
@@ -186,6 +193,8 @@ class Oracle:
         s.cam_up = _f3(cam["up"])
         s.cam_fov = cam["fov"]
         s.cam_near = cam.get("near", 1.0)
+        s.cam_lens = cam.get("lens_radius", 0.0)
+        s.cam_focal = cam.get("focal_distance", 0.0)
         o = _Opts(width, height, spp, max_depth, rr_depth, profile, seed, nthreads,
                   rows[0] if rows else 0, rows[1] if rows else 0)
         total = np.zeros((height, width, 3), np.float64)
@@ -307,6 +316,7 @@ class Reference:
         cam = sc.camera
         s.cam_pos, s.cam_target, s.cam_up = _f3(cam["pos"]), _f3(cam["target"]), _f3(cam["up"])
         s.cam_fov, s.cam_near = cam["fov"], cam.get("near", 1.0)
+        s.cam_lens = cam.get("lens_radius", 0.0)
         s.sky_over_10 = float(sc.sky[0]) / 10.0
         s.tmp_dir = tmp_dir.encode()
         h = self.L.sref_scene_create(C.byref(s), width, height)

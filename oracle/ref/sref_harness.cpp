@@ -44,12 +44,12 @@
 #include <s3d_plastic.h>
 #include <s3d_mirror.h>
 #include <s3d_glass.h>
-#include <s3d_camera.h>
 #include <s3d_texture.h>
 #include <s3d_tonemapper.h>
 #include <s3d_denoiser.h>
 #define private public
 #define protected public
+#include <s3d_camera.h>
 #include <s3d_scene.h>
 #include <s3d_pt.h>
 #undef private
@@ -171,6 +171,7 @@ struct sref_scene_desc {
     float cam_fov, cam_near;
     float sky_over_10;       // constant sky radiance / 10 (Scene::SampleIBL scales by 10)
     const char* tmp_dir;     // where the 2x2 sky .hdr file is written
+    float cam_lens;          // > 0: ThinLensCamera with this lens radius
 };
 
 // ---------------------------------------------------------------- traversal
@@ -240,6 +241,8 @@ namespace {
 class HarnessScene : public Scene {
 public:
     PinholeCamera camera;
+    ThinLensCamera lens;
+    float lens_radius = 0.0f;
     std::vector<IMaterial*> mats;
 };
 }  // namespace
@@ -294,6 +297,10 @@ void* sref_scene_create(const sref_scene_desc* d, int width, int height) {
     sc.camera.Update(v3(d->cam_pos), v3(d->cam_target), v3(d->cam_up), d->cam_fov,
                      float(width) / float(height), d->cam_near);
     sc.m_pCamera = &sc.camera;
+    sc.lens_radius = d->cam_lens;
+    if (d->cam_lens > 0.0f)
+        sc.lens.Update(v3(d->cam_pos), v3(d->cam_target), v3(d->cam_up), d->cam_fov, float(width) / float(height),
+                       d->cam_near, d->cam_lens);
 
     // Constant sky through the reference's own HDR loader: a 2x2 flat RGBE file.
     std::string path = std::string(d->tmp_dir ? d->tmp_dir : "/tmp") + "/sref_sky_" +
@@ -347,10 +354,16 @@ double sref_render(void* p, int width, int height, int spp, int max_bounce, uint
         pt.m_Config.CpuCoreCount = 1;
         pt.m_Updatable = true;
         pt.m_Random.SetSeed(seed * 1000003ull + (uint64_t)y);
+        // a thin lens samples its aperture with its own generator on every GetRay
+        // (include/s3d_camera.h:206-222): one camera copy per row, seeded per row
+        ThinLensCamera lens = h->scene.lens;
+        lens.m_Random.SetSeed((unsigned)(seed * 7919ull + (uint64_t)y + 1));
         for (int x = 0; x < width; ++x) {
-            Ray ray = h->scene.GetRay((0.5f + x) / width - 0.5f, (0.5f + y) / height - 0.5f);
+            const float fx = (0.5f + x) / width - 0.5f, fy = (0.5f + y) / height - 0.5f;
+            Ray ray = h->scene.GetRay(fx, fy);
             double s[3] = {0, 0, 0}, q[3] = {0, 0, 0};
             for (int k = 0; k < spp; ++k) {
+                if (h->scene.lens_radius > 0.0f) ray = lens.GetRay(fx, fy);
                 Color3 L = pt.Radiance(ray);
                 s[0] += L.x; s[1] += L.y; s[2] += L.z;
                 q[0] += (double)L.x * L.x; q[1] += (double)L.y * L.y; q[2] += (double)L.z * L.z;

@@ -102,6 +102,7 @@ static inline v3 cross(v3 a, v3 b) {
     return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 static inline float maxc(v3 a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
+static inline float length(v3 a) { return sqrtf(dot(a, a)); }
 /* Vector3::SafeUnitVector (include/s3d_math.h:847-859) */
 static inline v3 safe_unit(v3 v) {
     float mag = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
@@ -385,6 +386,8 @@ typedef struct {
     v3 lc, la, lb, ln, le;   /* light corner, edges, unit normal, emission */
     float larea;
     v3 cam_pos, cam_cx, cam_cy, cam_cz;
+    v3 cam_dir, cam_u, cam_v;  /* unit view direction and screen axes (thin lens) */
+    float cam_lens, cam_focal;
     /* sun disk: direction, frame, cos of the angular radius, radiance, 1/solid angle */
     v3 sun_dir, sun_t, sun_b, sun_L;
     int sun_disk;
@@ -399,6 +402,30 @@ static void camera_update(rscene* r, const oracle_scene* sc, float aspect) {
     r->cam_cy = scl(unit(cross(dir, r->cam_cx)), sc->cam_fov);
     r->cam_cz = add(pos, scl(dir, sc->cam_near));
     r->cam_pos = pos;
+    r->cam_dir = dir;
+    r->cam_u = unit(r->cam_cx);
+    r->cam_v = unit(r->cam_cy);
+    r->cam_lens = sc->cam_lens;
+    r->cam_focal = sc->cam_focal > 0.0f ? sc->cam_focal : length(sub(tgt, pos));
+}
+
+/* ThinLensCamera::GetRay (include/s3d_camera.h:206-222) for the compat profile: the lens
+ * offset lies in the world xy plane and the focal plane is z = const (the reference's
+ * z-aligned view).  Physical profile: offset in the camera's screen axes, focal plane
+ * perpendicular to the view direction.  Two random numbers (angle, radius). */
+static void thin_lens(const rscene* r, int compat, opcg* rnd, v3* o, v3* d) {
+    float th = 6.283185307179586476925286766559f * opcg_f32(rnd);
+    float rad = r->cam_lens * sqrtf(fmaxf(opcg_f32(rnd), 0.0f));
+    float cx = rad * cosf(th), cy = rad * sinf(th);
+    v3 focus;
+    if (compat) {
+        focus = add(r->cam_pos, scl(*d, r->cam_focal / fabsf(d->z)));
+        *o = add(r->cam_pos, mk(cx, cy, 0.0f));
+    } else {
+        focus = add(r->cam_pos, scl(*d, r->cam_focal / dot(*d, r->cam_dir)));
+        *o = add(add(r->cam_pos, scl(r->cam_u, cx)), scl(r->cam_v, cy));
+    }
+    *d = unit(sub(focus, *o));
 }
 
 /* PinholeCamera::GetRay (include/s3d_camera.h:95-100) */
@@ -906,11 +933,15 @@ static void* render_worker(void* arg) {
                 v3 L;
                 if (o->profile == ORACLE_PROFILE_COMPAT) {
                     v3 d = camera_dir(j->r, (0.5f + x) / o->width - 0.5f, (0.5f + y) / o->height - 0.5f);
-                    L = compat_radiance(j->r, j->r->cam_pos, d, o->max_depth, &rnd);
+                    v3 org = j->r->cam_pos;
+                    if (j->r->cam_lens > 0.0f) thin_lens(j->r, 1, &rnd, &org, &d);
+                    L = compat_radiance(j->r, org, d, o->max_depth, &rnd);
                 } else {
                     float jx = opcg_f32(&rnd), jy = opcg_f32(&rnd);
                     v3 d = camera_dir(j->r, (jx + x) / o->width - 0.5f, (jy + y) / o->height - 0.5f);
-                    L = phys_radiance(j->r, j->r->cam_pos, d, o, &rnd);
+                    v3 org = j->r->cam_pos;
+                    if (j->r->cam_lens > 0.0f) thin_lens(j->r, 0, &rnd, &org, &d);
+                    L = phys_radiance(j->r, org, d, o, &rnd);
                 }
                 s[0] += L.x; s[1] += L.y; s[2] += L.z;
                 q[0] += (double)L.x * L.x; q[1] += (double)L.y * L.y; q[2] += (double)L.z * L.z;

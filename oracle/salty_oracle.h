@@ -77,6 +77,8 @@ typedef struct {
     float        sky[3];            /* constant sky radiance */
     float        cam_pos[3], cam_target[3], cam_up[3];
     float        cam_fov, cam_near; /* fov used linearly as in include/s3d_camera.h:85-86 */
+    float        cam_lens;          /* thin-lens radius (0: pinhole) */
+    float        cam_focal;         /* focal distance (0: |target - pos|, as ThinLensCamera) */
 } oracle_scene;
 
 typedef struct {

@@ -46,7 +46,8 @@ class Material(C.Structure):
 
 class Camera(C.Structure):
     _fields_ = [("pos", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3),
-                ("fov", C.c_float), ("near_clip", C.c_float)]
+                ("fov", C.c_float), ("near_clip", C.c_float), ("lens_radius", C.c_float),
+                ("focal_distance", C.c_float)]
 
 
 class SceneDesc(C.Structure):
@@ -84,6 +85,13 @@ class RenderStats(C.Structure):
     _fields_ = [("ms", C.c_double), ("samples", C.c_int64), ("rays", C.c_int64), ("paths", C.c_int64)]
 
 
+class Mesh(C.Structure):
+    _fields_ = [("n_tris", C.c_int64), ("tri_pos", C.POINTER(C.c_float)), ("tri_nrm", C.POINTER(C.c_float)),
+                ("tri_uv", C.POINTER(C.c_float)), ("tri_mat", C.POINTER(C.c_int32)), ("n_mats", C.c_int32),
+                ("mats", C.POINTER(Material)), ("mat_texture", C.POINTER(C.c_int32)), ("n_textures", C.c_int32),
+                ("texture_names", C.c_void_p)]
+
+
 class Tuning(C.Structure):
     _fields_ = [("trace_block", C.c_int32), ("trace_pool", C.c_int32), ("trace_postpone", C.c_int32),
                 ("shade_block", C.c_int32), ("wave_paths", C.c_int64)]
@@ -100,7 +108,8 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_tonemap_noalloc", "salty_film_aov", "salty_unet_create", "salty_unet_destroy",
            "salty_unet_param_count", "salty_unet_get_params", "salty_unet_set_params", "salty_unet_forward",
            "salty_unet_train_step", "salty_scene_set_camera", "salty_denoise_unet", "salty_render_batch",
-           "salty_get_tuning", "salty_set_tuning", "salty_autotune"]
+           "salty_get_tuning", "salty_set_tuning", "salty_autotune", "salty_mesh_load_smd", "salty_mesh_free",
+           "salty_mesh_transform"]
 
 _lib = None
 
@@ -146,6 +155,9 @@ def lib() -> C.CDLL:
         "salty_unet_train_step": (i32, [vp, vp, vp, vp, i32, i32, i32, f32, C.POINTER(f32)]),
         "salty_denoise_unet": (i32, [vp, vp, vp, vp]),
         "salty_render_batch": (i32, [vp, vp, vp, i32, C.POINTER(RenderStats)]),
+        "salty_mesh_load_smd": (i32, [vp, C.c_char_p, C.POINTER(C.POINTER(Mesh))]),
+        "salty_mesh_free": (None, [C.POINTER(Mesh)]),
+        "salty_mesh_transform": (i32, [vp, i64, vp, vp, vp, vp]),
         "salty_get_tuning": (i32, [vp, C.POINTER(Tuning)]),
         "salty_set_tuning": (i32, [vp, C.POINTER(Tuning)]),
         "salty_autotune": (i32, [vp, vp, vp, i32, i32, C.POINTER(Tuning), C.POINTER(f32)]),
@@ -200,6 +212,50 @@ def render_opts(width: int, height: int, spp: int, max_depth: int, rr_depth: int
     cx, cy, cw, ch = crop if crop else (0, 0, 0, 0)
     return RenderOpts(width, height, spp, max_depth, rr_depth, profile, seed, int(accumulate), int(fp64), tonemap,
                       int(ref_oetf), cx, cy, cw, ch)
+
+
+def load_smd(path: str, ctx: "Context | None" = None) -> dict:
+    """salty_mesh_load_smd: an SMD mesh as a scene dict piece (tri_pos, tri_nrm, tri_uv,
+    tri_mat, materials as dicts, textures, mat_texture).  Needs no GPU."""
+    m = C.POINTER(Mesh)()
+    st = lib().salty_mesh_load_smd(ctx.h if ctx else None, os.fsencode(path), C.byref(m))
+    if st:
+        msg = lib().salty_last_error(ctx.h).decode() if ctx else f"cannot load {path}"
+        raise SaltyError(st, msg)
+    try:
+        M = m.contents
+        n = M.n_tris
+        arr = lambda p, k, dt: np.ctypeslib.as_array(p, shape=(n * k,)).astype(dt).reshape(n, k) if k > 1 else \
+            np.ctypeslib.as_array(p, shape=(n,)).astype(dt)
+        mats = []
+        for i in range(M.n_mats):
+            x = M.mats[i]
+            mats.append({"type": x.type, "color": tuple(x.color), "emission": tuple(x.emission), "ior": x.ior,
+                         "roughness": x.roughness, "specular": tuple(x.specular), "power": x.power})
+        names = C.string_at(M.texture_names, 256 * M.n_textures) if M.n_textures else b""
+        return {"tri_pos": arr(M.tri_pos, 9, np.float32), "tri_nrm": arr(M.tri_nrm, 9, np.float32),
+                "tri_uv": arr(M.tri_uv, 6, np.float32), "tri_mat": arr(M.tri_mat, 1, np.int32),
+                "materials": mats,
+                "textures": [names[256 * t:256 * (t + 1)].split(b"\0", 1)[0].decode("utf-8", "replace")
+                             for t in range(M.n_textures)],
+                "mat_texture": [M.mat_texture[i] for i in range(M.n_mats)]}
+    finally:
+        lib().salty_mesh_free(m)
+
+
+def transform_mesh(matrix, tri_pos, tri_nrm=None):
+    """salty_mesh_transform: positions by a 3x4 affine matrix, normals by the inverse
+    transpose of its linear part (an instance of the mesh, flattened into the scene)."""
+    M = np.ascontiguousarray(np.asarray(matrix, np.float32).reshape(3, 4))
+    pos = np.ascontiguousarray(tri_pos, np.float32)
+    n = pos.shape[0]
+    out_p = np.empty_like(pos)
+    nrm = None if tri_nrm is None else np.ascontiguousarray(tri_nrm, np.float32)
+    out_n = None if nrm is None else np.empty_like(nrm)
+    st = lib().salty_mesh_transform(_ptr(M), n, _ptr(pos), _ptr(nrm), _ptr(out_p), _ptr(out_n))
+    if st:
+        raise SaltyError(st, "mesh_transform: singular matrix or bad arguments")
+    return out_p, out_n
 
 
 class Context:
@@ -281,6 +337,8 @@ class Context:
         d.camera.pos, d.camera.target, d.camera.up = _f3(cam["pos"]), _f3(cam["target"]), _f3(cam["up"])
         d.camera.fov = float(cam["fov"])
         d.camera.near_clip = float(cam.get("near", 1.0))
+        d.camera.lens_radius = float(cam.get("lens_radius", 0.0))
+        d.camera.focal_distance = float(cam.get("focal_distance", 0.0))
         h = C.c_void_p()
         self.check(lib().salty_scene_upload(self.h, C.byref(d), C.byref(h)), "scene_upload")
         return Scene(self, h, n)
@@ -442,10 +500,12 @@ class Scene:
         return self.render(width, height, 0, kw.pop("max_depth", 1), accumulate=True, fp64=fp64, crop=crop,
                            want=want, out=out, **kw)
 
-    def set_camera(self, pos, target, up=(0.0, 1.0, 0.0), fov: float = 1.0, near: float = 1.0) -> None:
+    def set_camera(self, pos, target, up=(0.0, 1.0, 0.0), fov: float = 1.0, near: float = 1.0,
+                   lens_radius: float = 0.0, focal_distance: float = 0.0) -> None:
         c = Camera()
         c.pos, c.target, c.up = _f3(pos), _f3(target), _f3(up)
         c.fov, c.near_clip = float(fov), float(near)
+        c.lens_radius, c.focal_distance = float(lens_radius), float(focal_distance)
         self.ctx.check(lib().salty_scene_set_camera(self.ctx.h, self.h, C.byref(c)), "scene_set_camera")
 
     def aov(self, width: int, height: int) -> dict:

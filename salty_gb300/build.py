@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "lib", "obj")
 LIB = os.path.join(HERE, "lib", "libsalty_gpu.so")
 
-SOURCES = ["capi.cu", "bvh_build.cu", "trace.cu", "render.cu", "post.cu", "unet.cu"]
+SOURCES = ["capi.cu", "bvh_build.cu", "trace.cu", "render.cu", "post.cu", "unet.cu", "smd.cpp"]
 HEADERS = ["internal.h", "traverse.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -50,7 +50,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     objs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OBJ, src.replace(".cu", ".o"))
+        o = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s, *hdrs, __file__]):
             jobs.append([cc, *_flags(), "-c", s, "-o", o])

@@ -304,6 +304,10 @@ salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* d, salty
     }
     k.cam_fov = cam.fov;
     k.cam_near = cam.near_clip > 0 ? cam.near_clip : 1.0f;
+    if (!(cam.lens_radius >= 0.0f) || !(cam.focal_distance >= 0.0f))
+        return fail(E.fail(SALTY_ERR_INVALID_ARG, "camera lens radius and focal distance must be >= 0"));
+    k.cam_lens = cam.lens_radius;
+    k.cam_focal = cam.focal_distance;
     UP_CUDA(cudaStreamSynchronize(ctx->stream));
     UP_CUDA(cudaGetLastError());
 #undef UP_TRY
@@ -328,6 +332,10 @@ salty_status salty_scene_set_camera(salty_ctx* ctx, salty_scene* scene, const sa
     }
     k.cam_fov = cam->fov;
     k.cam_near = cam->near_clip > 0 ? cam->near_clip : 1.0f;
+    if (!(cam->lens_radius >= 0.0f) || !(cam->focal_distance >= 0.0f))
+        return ctx->err.fail(SALTY_ERR_INVALID_ARG, "camera lens radius and focal distance must be >= 0");
+    k.cam_lens = cam->lens_radius;
+    k.cam_focal = cam->focal_distance;
     return SALTY_OK;
 }
 

@@ -129,6 +129,7 @@ struct SceneConsts {
     float cam_pos[3], cam_cx[3], cam_cy[3], cam_cz[3];
     float cam_fov, cam_near;
     float cam_target[3], cam_up[3];
+    float cam_lens, cam_focal;  // thin lens radius (0: pinhole), focal distance
 };
 
 struct Film {

@@ -109,6 +109,8 @@ struct PathSoA {
 
 struct Camera {
     float pos[3], cx[3], cy[3], cz[3];
+    float dir[3], u[3], v[3];  // unit view direction and screen axes
+    float lens, focal;         // thin lens radius (0: pinhole) and focal distance
 };
 
 // One scene of a batch (one slot for a plain render).  Its samples are the global sample
@@ -215,8 +217,29 @@ __global__ void k_generate(WaveParams P, WaveBuffers B) {
         const float mag = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
         const float tmin = S.profile == SALTY_PROFILE_COMPAT ? kFHitMin : kEps;
         const float tmax = S.profile == SALTY_PROFILE_COMPAT ? kFHitMax : INFINITY;
-        B.rays[0][2 * i] = make_float4(S.cam.pos[0], S.cam.pos[1], S.cam.pos[2], tmin);
-        B.rays[0][2 * i + 1] = make_float4(__fdiv_rn(d[0], mag), __fdiv_rn(d[1], mag), __fdiv_rn(d[2], mag), tmax);
+        V org = mk(S.cam.pos[0], S.cam.pos[1], S.cam.pos[2]);
+        V dir = mk(__fdiv_rn(d[0], mag), __fdiv_rn(d[1], mag), __fdiv_rn(d[2], mag));
+        if (S.cam.lens > 0.0f) {
+            // ThinLensCamera::GetRay (include/s3d_camera.h:206-222): compat keeps the
+            // reference's world-xy lens and z = const focal plane, physical uses the
+            // screen axes and a focal plane perpendicular to the view
+            const float th = k2Pi * rng.f32();
+            const float rad = S.cam.lens * sqrtf(fmaxf(rng.f32(), 0.0f));
+            float sn, cs;
+            sincosf(th, &sn, &cs);
+            const float lx = rad * cs, ly = rad * sn;
+            V focus;
+            if (S.profile == SALTY_PROFILE_COMPAT) {
+                focus = org + dir * (S.cam.focal / fabsf(dir.z));
+                org = org + mk(lx, ly, 0.0f);
+            } else {
+                focus = org + dir * (S.cam.focal / dot(dir, ld3(S.cam.dir)));
+                org = org + ld3(S.cam.u) * lx + ld3(S.cam.v) * ly;
+            }
+            dir = safe_unit(focus - org);
+        }
+        B.rays[0][2 * i] = make_float4(org.x, org.y, org.z, tmin);
+        B.rays[0][2 * i + 1] = make_float4(dir.x, dir.y, dir.z, tmax);
         if (B.roots[0]) B.roots[0][i] = S.root;
         B.path[0].W[i] = make_float4(1.f, 1.f, 1.f, 0.f);
         B.path[0].L[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -944,7 +967,15 @@ Camera camera_of(const SceneConsts& k, int width, int height) {
         c.cx[a] = cx[a];
         c.cy[a] = cy[a];
         c.cz[a] = k.cam_pos[a] + dir[a] * k.cam_near;
+        c.dir[a] = dir[a];
     }
+    float u[3] = {cx[0], cx[1], cx[2]}, v[3] = {cy[0], cy[1], cy[2]};
+    unitv(u);
+    unitv(v);
+    float foc[3] = {k.cam_target[0] - k.cam_pos[0], k.cam_target[1] - k.cam_pos[1], k.cam_target[2] - k.cam_pos[2]};
+    for (int a = 0; a < 3; ++a) { c.u[a] = u[a]; c.v[a] = v[a]; }
+    c.lens = k.cam_lens;
+    c.focal = k.cam_focal > 0.0f ? k.cam_focal : std::sqrt(foc[0] * foc[0] + foc[1] * foc[1] + foc[2] * foc[2]);
     return c;
 }
 

@@ -80,6 +80,8 @@ class Denoiser:
             if hq_weights and os.path.exists(hq_weights):
                 self.hq = Unet(ctx)
                 self.hq_meta = load_weights(self.hq, hq_weights)
+                # from the lowest sample count it was trained on
+                self.hq_from_spp = int(min(self.hq_meta.get("levels", [hq_from_spp])))
         elif method == "unet":
             raise FileNotFoundError(f"no U-Net weights at {weights}")
         self.method = "unet" if self.net is not None else "nlm"

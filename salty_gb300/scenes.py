@@ -53,7 +53,8 @@ def cornell(variant: str = "baseline") -> dict:
     variant "baseline": all Lambert.  "mixed": tall box mirror, short box glass (IOR 1.5),
     back wall GGX (roughness 0.3) -- exercises every BSDF.  "glossy": tall box Phong
     (specular 0.8, power 40), short box Plastic (diffuse (0.2, 0.4, 0.7), specular 0.6,
-    power 120), back wall Phong (power 8)."""
+    power 120), back wall Phong (power 8).  "thinlens": the baseline box seen through a thin
+    lens of radius 0.06 focused on the tall box (target z = 0.6, focal distance 2.0)."""
     W, R, G = (0.75, 0.75, 0.75), (0.75, 0.25, 0.25), (0.25, 0.75, 0.25)
     mats = [{"type": LAMBERT, "color": W}, {"type": LAMBERT, "color": R}, {"type": LAMBERT, "color": G}]
     tall_m = short_m = back_m = 0
@@ -90,8 +91,9 @@ def cornell(variant: str = "baseline") -> dict:
         "light": {"corner": (0.375, 0.999, 0.375), "edge_a": (0.25, 0.0, 0.0), "edge_b": (0.0, 0.0, 0.25),
                   "emission": (17.0, 12.0, 4.0)},
         "sun": None, "sky": (0.0, 0.0, 0.0),
-        "camera": {"pos": (0.5, 0.5, -1.4), "target": (0.5, 0.5, 0.0), "up": (0.0, 1.0, 0.0),
-                   "fov": 2.0 * math.tan(math.radians(20.0)), "near": 1.0},
+        "camera": {"pos": (0.5, 0.5, -1.4), "target": (0.5, 0.5, 0.6 if variant == "thinlens" else 0.0),
+                   "up": (0.0, 1.0, 0.0), "fov": 2.0 * math.tan(math.radians(20.0)), "near": 1.0,
+                   "lens_radius": 0.06 if variant == "thinlens" else 0.0},
     }
 
 

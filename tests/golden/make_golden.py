@@ -106,11 +106,26 @@ def glossy_fixture(r) -> None:
     print(f"glossy cornell reference render: {secs:.2f} s")
 
 
+def thinlens_fixture(r) -> None:
+    """The Cornell box through ThinLensCamera (include/s3d_camera.h:150-267)."""
+    sc = cornell_scene("thinlens")
+    W = H = 48
+    spp, depth = 1024, 8
+    total, sq, secs = r.render(sc, W, H, spp, depth, seed=4242)
+    mean = total / spp
+    var = (sq / spp - mean * mean) * spp / (spp - 1) / spp
+    np.savez_compressed(os.path.join(HERE, "cornell_thinlens_ref_48.npz"), mean=mean.astype(np.float32),
+                        var=np.maximum(var, 0).astype(np.float32), spp=spp, max_bounce=depth, width=W, height=H)
+    print(f"thin-lens cornell reference render: {secs:.2f} s")
+
+
 def main() -> None:
     build(with_reference=True)
     o, r = Oracle(), Reference()
-    if sys.argv[1:] == ["glossy"]:
-        glossy_fixture(r)
+    only = {"glossy": glossy_fixture, "thinlens": thinlens_fixture}
+    if sys.argv[1:] and all(a in only for a in sys.argv[1:]):
+        for a in sys.argv[1:]:
+            only[a](r)
         return
 
     # 1. traversal: 1M-triangle soup, first 65536 rays of the microbenchmark stream
@@ -144,6 +159,7 @@ def main() -> None:
                         var=np.maximum(var, 0).astype(np.float32), spp=spp, max_bounce=depth, width=W, height=H)
     print(f"cornell reference render: {secs:.2f} s")
     glossy_fixture(r)
+    thinlens_fixture(r)
 
     # 4. tonemapping and the sRGB8 capture
     img = hdr_image(99, 48, 32)

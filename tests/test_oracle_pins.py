@@ -104,18 +104,21 @@ def test_oracle_compat_render_matches_reference_fixture(oracle):
     assert abs(m.mean() / g["mean"].mean() - 1) < 0.01
 
 
-def test_oracle_compat_glossy_matches_reference_fixture(oracle):
-    """Phong and Plastic (src/s3d_phong.cpp:65-88, src/s3d_plastic.cpp:71-142) through the
-    reference's PathTracer::Radiance."""
+@pytest.mark.parametrize("variant,fixture,seed", [("glossy", "cornell_glossy_ref_48.npz", 31),
+                                                  ("thinlens", "cornell_thinlens_ref_48.npz", 32)])
+def test_oracle_compat_variants_match_reference_fixtures(oracle, variant, fixture, seed):
+    """Phong and Plastic (src/s3d_phong.cpp:65-88, src/s3d_plastic.cpp:71-142), and the
+    ThinLensCamera (include/s3d_camera.h:150-267), through the reference's
+    PathTracer::Radiance."""
     from oracle.oracle import PROFILE_COMPAT, SceneData
     from salty_gb300 import scenes
-    g = np.load(os.path.join(GOLDEN, "cornell_glossy_ref_48.npz"))
-    sc = scenes.cornell("glossy")
+    g = np.load(os.path.join(GOLDEN, fixture))
+    sc = scenes.cornell(variant)
     sd = SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], None, sc["sky"],
                    sc["camera"])
     spp = int(g["spp"])
     tot, sq = oracle.render(sd, int(g["width"]), int(g["height"]), spp, int(g["max_bounce"]),
-                            profile=PROFILE_COMPAT, seed=31)
+                            profile=PROFILE_COMPAT, seed=seed)
     m = tot / spp
     v = np.maximum((sq / spp - m * m) * spp / (spp - 1) / spp, 0)
     z = zscores(m, v, g["mean"], g["var"])

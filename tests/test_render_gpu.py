@@ -46,12 +46,15 @@ def test_compat_cornell_matches_reference_fixture(ctx):
     assert abs(r["mean"].mean() / g["mean"].mean() - 1) < 0.01
 
 
-def test_compat_glossy_cornell_matches_reference_fixture(ctx):
-    """Phong and Plastic in the reference's estimator vs the GPU compat profile."""
+@pytest.mark.parametrize("variant,fixture", [("glossy", "cornell_glossy_ref_48.npz"),
+                                             ("thinlens", "cornell_thinlens_ref_48.npz")])
+def test_compat_variants_match_reference_fixtures(ctx, variant, fixture):
+    """Phong and Plastic, and the thin-lens camera, in the reference's estimator vs the GPU
+    compat profile."""
     import salty_gb300
     from salty_gb300 import scenes
-    g = np.load(os.path.join(GOLDEN, "cornell_glossy_ref_48.npz"))
-    s = _gpu_scene(ctx, scenes.cornell("glossy"))
+    g = np.load(os.path.join(GOLDEN, fixture))
+    s = _gpu_scene(ctx, scenes.cornell(variant))
     r = s.render(int(g["width"]), int(g["height"]), int(g["spp"]), int(g["max_bounce"]),
                  profile=salty_gb300.PROFILE_COMPAT, seed=4343)
     frac, zmax = zstats(r["mean"], r["var"], g["mean"], g["var"])
@@ -59,7 +62,7 @@ def test_compat_glossy_cornell_matches_reference_fixture(ctx):
     assert abs(r["mean"].mean() / g["mean"].mean() - 1) < 0.01
 
 
-@pytest.mark.parametrize("variant", ["baseline", "mixed", "glossy"])
+@pytest.mark.parametrize("variant", ["baseline", "mixed", "glossy", "thinlens"])
 def test_physical_cornell_matches_oracle(ctx, oracle, variant):
     import salty_gb300
     from oracle.oracle import PROFILE_PHYSICAL
@@ -174,3 +177,38 @@ def test_render_rejects_bad_options(ctx):
         s.render(10, 10, 1, 0)
     with pytest.raises(salty_gb300.SaltyError):
         s.render(10, 10, 1, 8, profile=7)
+
+
+def test_smd_mesh_instances_match_oracle(ctx, oracle, tmp_path):
+    """An SMD mesh (an icosphere with a Plastic material) placed twice by affine transforms
+    inside the Cornell box: GPU physical profile vs the oracle."""
+    import salty_gb300
+    from oracle.oracle import PROFILE_PHYSICAL
+    from salty_gb300 import scenes
+    from test_smd import write_smd
+    unit = scenes._icosphere(2).astype(np.float32).reshape(-1, 9)
+    n = unit.shape[0]
+    p = str(tmp_path / "ball.smd")
+    write_smd(p, unit, unit, np.zeros((n, 6), np.float32), np.zeros(n, np.int32),
+              [(4, {"diffuse": (0.7, 0.3, 0.2), "specular": (0.6, 0.6, 0.6), "power": 60.0, "emission": (0, 0, 0)})])
+    mesh = salty_gb300.load_smd(p)
+    sc = scenes.cornell("baseline")
+    pos, nrm, mat = [sc["tri_pos"]], [sc["tri_nrm"]], [sc["tri_mat"]]
+    base = len(sc["materials"])
+    for M in ([[0.12, 0, 0, 0.3], [0, 0.12, 0, 0.12], [0, 0, 0.12, 0.25]],
+              [[0.1, 0.02, 0, 0.72], [0, 0.09, 0, 0.7], [0, 0, 0.11, 0.4]]):
+        p2, n2 = salty_gb300.transform_mesh(M, mesh["tri_pos"], mesh["tri_nrm"])
+        pos.append(p2)
+        nrm.append(n2)
+        mat.append(mesh["tri_mat"] + base)
+    sc = dict(sc, tri_pos=np.concatenate(pos), tri_nrm=np.concatenate(nrm), tri_mat=np.concatenate(mat),
+              materials=sc["materials"] + mesh["materials"])
+    W = H = 40
+    spp = 256
+    s = _gpu_scene(ctx, sc)
+    r = s.render(W, H, spp, 8, rr_depth=3, profile=salty_gb300.PROFILE_PHYSICAL, seed=8)
+    tot, sq = oracle.render(_oracle_scene(sc), W, H, spp, 8, rr_depth=3, profile=PROFILE_PHYSICAL, seed=9)
+    m = tot / spp
+    v = np.maximum((sq / spp - m * m) * spp / (spp - 1) / spp, 0)
+    frac, zmax = zstats(r["mean"], r["var"], m, v)
+    assert frac < 0.015 and zmax < 6, (frac, zmax)
