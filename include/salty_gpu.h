@@ -81,6 +81,8 @@ typedef struct salty_material {
     float roughness;    /* GGX: alpha = roughness^2 */
     float specular[3];  /* Plastic: specular colour (color is its diffuse colour) */
     float power;        /* Phong, Plastic: lobe exponent (> 0) */
+    int32_t color_map;  /* 1 + index of a texture that multiplies the base colour, 0 = none
+                         * (TexturedMaterial, src/s3d_texturedmaterial.cpp:63-87) */
 } salty_material;
 
 /* PinholeCamera (include/s3d_camera.h:63-100) and ThinLensCamera (:150-267).  fov is the
@@ -97,6 +99,13 @@ typedef struct salty_camera {
     float lens_radius;
     float focal_distance;
 } salty_camera;
+
+/* An RGB float image; texel (x, y) is rgb[3 * (y * width + x)].  Sampled bilinearly with
+ * the reference's wrap (Texture::SampleColor, src/s3d_texture.cpp:925-952). */
+typedef struct salty_texture {
+    int32_t width, height;
+    const float* rgb;          /* host or device */
+} salty_texture;
 
 typedef struct salty_scene_desc {
     const float* tri_pos;      /* n_tris * 9: v0, v1, v2 (host or device) */
@@ -118,6 +127,13 @@ typedef struct salty_scene_desc {
     float sun_half_angle;
     float sky[3];              /* constant sky radiance (Scene::SampleIBL) */
     salty_camera camera;
+    /* Textures (Texture, src/s3d_texture.cpp): colour maps and an environment map. */
+    const float* tri_uv;       /* n_tris * 6 texture coordinates (host or device), or NULL */
+    const struct salty_texture* textures;  /* host table */
+    int32_t n_textures;
+    int32_t ibl_map;           /* 1 + index of a sphere-mapped environment texture that replaces
+                                * the constant sky (Texture::SampleColor(dir)), 0 = none */
+    float ibl_scale;           /* environment radiance = texel * ibl_scale (Scene::SampleIBL: 10) */
 } salty_scene_desc;
 
 salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* desc, salty_scene** out);
@@ -260,13 +276,14 @@ typedef struct salty_tuning {
     int32_t trace_pool;      /* rays a warp takes from the queue per refill, 32..4096 */
     int32_t trace_postpone;  /* fewest lanes that test a triangle group together, 1..32 */
     int32_t shade_block;     /* shading threads per block, a multiple of 32 in 64..1024 */
+    int32_t trace_regs;      /* traversal registers per thread: 64, or 48 (more resident warps) */
     int64_t wave_paths;      /* paths in flight per wave (queue capacity), 2^16..2^26 */
 } salty_tuning;
 salty_status salty_get_tuning(salty_ctx* ctx, salty_tuning* out);
 salty_status salty_set_tuning(salty_ctx* ctx, const salty_tuning* t);
 /* Picks the tuning for a render: trial renders of the batch with at most trial_spp samples
  * per pixel, timed with CUDA events, one pass of coordinate descent over wave_paths,
- * shade_block, trace_block, trace_pool and trace_postpone.  Leaves the best tuning set on
+ * shade_block, trace_block, trace_regs, trace_pool and trace_postpone.  Leaves the best tuning set on
  * the context (also copied to out and its trial time to best_ms; either may be NULL) and
  * each film holding its last trial render: render with accumulate = 0 afterwards.  BVH node
  * width (8) and traversal stack depth (from the BVH depth) are fixed by the build. */

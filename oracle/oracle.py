@@ -46,7 +46,23 @@ def build(with_reference: bool | None = None) -> None:
 
 class _Mat(C.Structure):
     _fields_ = [("type", C.c_int), ("color", C.c_float * 3), ("emission", C.c_float * 3),
-                ("ior", C.c_float), ("roughness", C.c_float), ("specular", C.c_float * 3), ("power", C.c_float)]
+                ("ior", C.c_float), ("roughness", C.c_float), ("specular", C.c_float * 3), ("power", C.c_float),
+                ("color_map", C.c_int)]
+
+
+class _Tex(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("rgb", C.c_void_p)]
+
+
+def _textures(textures, keep):
+    """(table, count) of (H, W, 3) float32 images for the C structs."""
+    tt = (_Tex * max(1, len(textures)))()
+    for i, t in enumerate(textures):
+        a = np.ascontiguousarray(t, np.float32)
+        keep.append(a)
+        tt[i].height, tt[i].width, tt[i].rgb = a.shape[0], a.shape[1], a.ctypes.data
+    keep.append(tt)
+    return tt, len(textures)
 
 
 class _Scene(C.Structure):
@@ -58,7 +74,9 @@ class _Scene(C.Structure):
                 ("sun_dir", C.c_float * 3), ("sun_radiance", C.c_float * 3), ("sun_half_angle", C.c_float),
                 ("sky", C.c_float * 3),
                 ("cam_pos", C.c_float * 3), ("cam_target", C.c_float * 3), ("cam_up", C.c_float * 3),
-                ("cam_fov", C.c_float), ("cam_near", C.c_float), ("cam_lens", C.c_float), ("cam_focal", C.c_float)]
+                ("cam_fov", C.c_float), ("cam_near", C.c_float), ("cam_lens", C.c_float), ("cam_focal", C.c_float),
+                ("tri_uv", C.c_void_p), ("textures", C.c_void_p), ("n_textures", C.c_int), ("ibl_map", C.c_int),
+                ("ibl_scale", C.c_float)]
 
 
 class _Opts(C.Structure):
@@ -69,7 +87,7 @@ class _Opts(C.Structure):
 
 class _RefMat(C.Structure):
     _fields_ = [("type", C.c_int), ("color", C.c_float * 3), ("emission", C.c_float * 3), ("ior", C.c_float),
-                ("specular", C.c_float * 3), ("power", C.c_float)]
+                ("specular", C.c_float * 3), ("power", C.c_float), ("color_map", C.c_int)]
 
 
 class _RefScene(C.Structure):
@@ -80,7 +98,8 @@ class _RefScene(C.Structure):
                 ("light_emission", C.c_float * 3), ("cam_pos", C.c_float * 3),
                 ("cam_target", C.c_float * 3), ("cam_up", C.c_float * 3),
                 ("cam_fov", C.c_float), ("cam_near", C.c_float), ("sky_over_10", C.c_float),
-                ("tmp_dir", C.c_char_p), ("cam_lens", C.c_float)]
+                ("tmp_dir", C.c_char_p), ("cam_lens", C.c_float), ("tri_uv", C.c_void_p), ("textures", C.c_void_p),
+                ("n_textures", C.c_int), ("ibl_map", C.c_int)]
 
 
 def _f3(v):
@@ -98,6 +117,10 @@ class SceneData:
     sun: dict | None = None             # dir, radiance
     sky: tuple = (0.0, 0.0, 0.0)
     camera: dict = field(default_factory=dict)  # pos, target, up, fov, near
+    tri_uv: np.ndarray | None = None    # (n, 6) float32 texture coordinates
+    textures: list = field(default_factory=list)  # (H, W, 3) float32 images
+    ibl: int | None = None              # texture index of the environment map
+    ibl_scale: float = 10.0
 
 
 class Oracle:
@@ -168,7 +191,16 @@ class Oracle:
             mats[i].roughness = m.get("roughness", 0.3)
             mats[i].specular = _f3(m.get("specular", (0.0, 0.0, 0.0)))
             mats[i].power = m.get("power", 32.0)
+            mats[i].color_map = 0 if m.get("texture") is None else int(m["texture"]) + 1
         s = _Scene()
+        tt, nt = _textures(sc.textures, keep)
+        s.textures, s.n_textures = C.addressof(tt), nt
+        s.ibl_map = 0 if sc.ibl is None else int(sc.ibl) + 1
+        s.ibl_scale = sc.ibl_scale
+        if sc.tri_uv is not None:
+            uv = np.ascontiguousarray(sc.tri_uv, np.float32)
+            keep.append(uv)
+            s.tri_uv = uv.ctypes.data
         s.tri_pos = pos.ctypes.data
         s.tri_nrm = nrm.ctypes.data if nrm is not None else None
         s.tri_mat = mat.ctypes.data
@@ -302,6 +334,7 @@ class Reference:
             mats[i].ior = m.get("ior", 1.5)
             mats[i].specular = _f3(m.get("specular", (0.0, 0.0, 0.0)))
             mats[i].power = m.get("power", 32.0)
+            mats[i].color_map = 0 if m.get("texture") is None else int(m["texture"]) + 1
         s = _RefScene()
         s.tri_pos, s.tri_nrm, s.tri_mat = pos.ctypes.data, nrm.ctypes.data, mat.ctypes.data
         s.n_tris = pos.shape[0]
@@ -319,6 +352,14 @@ class Reference:
         s.cam_lens = cam.get("lens_radius", 0.0)
         s.sky_over_10 = float(sc.sky[0]) / 10.0
         s.tmp_dir = tmp_dir.encode()
+        keep = []
+        tt, nt = _textures(sc.textures, keep)
+        s.textures, s.n_textures = C.addressof(tt), nt
+        s.ibl_map = 0 if sc.ibl is None else int(sc.ibl) + 1
+        if sc.tri_uv is not None:
+            uv = np.ascontiguousarray(sc.tri_uv, np.float32)
+            keep.append(uv)
+            s.tri_uv = uv.ctypes.data
         h = self.L.sref_scene_create(C.byref(s), width, height)
         try:
             total = np.zeros((height, width, 3), np.float64)

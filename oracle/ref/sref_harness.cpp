@@ -33,6 +33,10 @@
 #include <unordered_map>
 #include <vector>
 
+// private members of the reference's classes (Texture texels, PathTracer state, camera
+// generator) are set directly by this harness
+#define private public
+#define protected public
 #include <s3d_math.h>
 #include <s3d_shape.h>
 #include <s3d_material.h>
@@ -47,8 +51,7 @@
 #include <s3d_texture.h>
 #include <s3d_tonemapper.h>
 #include <s3d_denoiser.h>
-#define private public
-#define protected public
+#include <s3d_texturedmaterial.h>
 #include <s3d_camera.h>
 #include <s3d_scene.h>
 #include <s3d_pt.h>
@@ -156,6 +159,12 @@ struct sref_material {
     float ior;
     float specular[3];   // Plastic
     float power;         // Phong, Plastic
+    int color_map;       // 1 + texture index (TexturedMaterial), 0 = none
+};
+
+struct sref_texture {
+    int width, height;
+    const float* rgb;    // texel (x, y) at rgb[3 * (y * width + x)]
 };
 
 struct sref_scene_desc {
@@ -172,6 +181,10 @@ struct sref_scene_desc {
     float sky_over_10;       // constant sky radiance / 10 (Scene::SampleIBL scales by 10)
     const char* tmp_dir;     // where the 2x2 sky .hdr file is written
     float cam_lens;          // > 0: ThinLensCamera with this lens radius
+    const float* tri_uv;     // n_tris * 6, or NULL
+    const sref_texture* textures;
+    int n_textures;
+    int ibl_map;             // 1 + texture index of the environment (replaces the constant sky), 0 = none
 };
 
 // ---------------------------------------------------------------- traversal
@@ -240,6 +253,7 @@ struct SrefScene;
 namespace {
 class HarnessScene : public Scene {
 public:
+    std::vector<Texture> textures;
     PinholeCamera camera;
     ThinLensCamera lens;
     float lens_radius = 0.0f;
@@ -253,9 +267,21 @@ struct SrefScene {
 
 extern "C" {
 
+// A Texture (src/s3d_texture.cpp) holding the given float texels, as its loaders leave it.
+static void fill_texture(Texture& t, const sref_texture& x) {
+    t.Term();
+    t.m_Width = x.width;
+    t.m_Height = x.height;
+    t.m_Size = (u32)(x.width * x.height);
+    t.m_pColors = new Color3[t.m_Size];
+    for (u32 i = 0; i < t.m_Size; ++i) t.m_pColors[i] = Color3(x.rgb[3 * i], x.rgb[3 * i + 1], x.rgb[3 * i + 2]);
+}
+
 void* sref_scene_create(const sref_scene_desc* d, int width, int height) {
     auto* h = new SrefScene();
     HarnessScene& sc = h->scene;
+    sc.textures.resize(d->n_textures > 0 ? d->n_textures : 0);
+    for (int t = 0; t < d->n_textures; ++t) fill_texture(sc.textures[t], d->textures[t]);
     for (int m = 0; m < d->n_mats; ++m) {
         const sref_material& sm = d->mats[m];
         Color3 c(sm.color[0], sm.color[1], sm.color[2]);
@@ -267,6 +293,11 @@ void* sref_scene_create(const sref_scene_desc* d, int width, int height) {
         else if (sm.type == 5)
             mat = Plastic::Create(c, Color3(sm.specular[0], sm.specular[1], sm.specular[2]), sm.power, e);
         else mat = Lambert::Create(c, e);
+        if (sm.color_map > 0 && sm.color_map <= (int)sc.textures.size()) {
+            IMaterial* tm = TexturedMaterial::Create(&sc.textures[sm.color_map - 1], mat);
+            SafeRelease(mat);
+            mat = tm;
+        }
         sc.mats.push_back(mat);
     }
     // one Mesh per material, vertices in input order
@@ -278,7 +309,7 @@ void* sref_scene_create(const sref_scene_desc* d, int width, int height) {
                 Vertex v;
                 v.Position = v3(d->tri_pos + i * 9 + k * 3);
                 v.Normal = v3(d->tri_nrm + i * 9 + k * 3);
-                v.TexCoord = Vector2(0, 0);
+                v.TexCoord = d->tri_uv ? Vector2(d->tri_uv[i * 6 + 2 * k], d->tri_uv[i * 6 + 2 * k + 1]) : Vector2(0, 0);
                 verts.push_back(v);
             }
         }
@@ -302,6 +333,11 @@ void* sref_scene_create(const sref_scene_desc* d, int width, int height) {
         sc.lens.Update(v3(d->cam_pos), v3(d->cam_target), v3(d->cam_up), d->cam_fov, float(width) / float(height),
                        d->cam_near, d->cam_lens);
 
+    if (d->ibl_map > 0 && d->ibl_map <= d->n_textures) {
+        // an environment texture as the IBL (Scene::SampleIBL scales it by 10)
+        fill_texture(sc.m_IBL, d->textures[d->ibl_map - 1]);
+        return h;
+    }
     // Constant sky through the reference's own HDR loader: a 2x2 flat RGBE file.
     std::string path = std::string(d->tmp_dir ? d->tmp_dir : "/tmp") + "/sref_sky_" +
                        std::to_string((long)(uintptr_t)h) + ".hdr";

@@ -504,6 +504,50 @@ static int is_light_tri(const rscene* r, int id) {
 }
 
 /* Triangle::CalcParam (src/s3d_triangle.cpp:107-121): interpolated, SafeNormalize'd. */
+/* Texture::SampleColor (src/s3d_texture.cpp:925-952): bilinear with the weights taken
+ * before the wrap, indices wrapped as |i % size| */
+static v3 tex_sample(const oracle_texture* t, float u, float v) {
+    float fx = u * (float)(t->width - 1), fy = v * (float)(t->height - 1);
+    if (!(fabsf(fx) < 1e9f)) fx = 0.0f;
+    if (!(fabsf(fy) < 1e9f)) fy = 0.0f;
+    int x0 = (int)floorf(fx), y0 = (int)floorf(fy);
+    int x1 = x0 + 1, y1 = y0 + 1;
+    float xw0 = (float)x1 - fx, xw1 = fx - (float)x0, yw0 = (float)y1 - fy, yw1 = fy - (float)y0;
+    x0 = abs(x0 % t->width); x1 = abs(x1 % t->width);
+    y0 = abs(y0 % t->height); y1 = abs(y1 % t->height);
+    v3 c00 = ld3(t->rgb + 3 * ((long)y0 * t->width + x0)), c01 = ld3(t->rgb + 3 * ((long)y1 * t->width + x0));
+    v3 c10 = ld3(t->rgb + 3 * ((long)y0 * t->width + x1)), c11 = ld3(t->rgb + 3 * ((long)y1 * t->width + x1));
+    return add(scl(add(scl(c00, yw0), scl(c01, yw1)), xw0), scl(add(scl(c10, yw0), scl(c11, yw1)), xw1));
+}
+
+/* Texture::SampleColor(dir) (src/s3d_texture.cpp:957-972) */
+static v3 tex_sphere(const oracle_texture* t, v3 d) {
+    const float pi = 3.1415926535897932384626433832795f, two_pi = 6.283185307179586476925286766559f;
+    float theta = acosf(fminf(1.0f, fmaxf(-1.0f, d.y)));
+    float u = 0.0f, v = theta * (1.0f / pi);
+    if (!(fabsf(d.x) <= FLT_EPSILON) && !(fabsf(d.z) <= FLT_EPSILON)) {
+        float phi = atan2f(d.z, d.x);
+        u = (d.z < 0.0f ? phi + two_pi : phi) * (1.0f / two_pi);
+    }
+    return tex_sample(t, u, v);
+}
+
+/* Scene::SampleIBL (include/s3d_scene.h:81-82): environment map or constant sky */
+static v3 environment(const rscene* r, v3 d) {
+    const oracle_scene* sc = r->sc;
+    if (sc->ibl_map > 0) return scl(tex_sphere(&sc->textures[sc->ibl_map - 1], d), sc->ibl_scale);
+    return ld3(sc->sky);
+}
+
+/* the material's colour map at the hit (Triangle::CalcParam's texture coordinate), or 1 */
+static v3 color_map(const rscene* r, const oracle_material* m, int id, float b1, float b2) {
+    if (m->color_map <= 0 || !r->sc->tri_uv || id >= r->sc->n_tris) return mk(1.0f, 1.0f, 1.0f);
+    const float* t = r->sc->tri_uv + (long)id * 6;
+    float a = 1.0f - b1 - b2;
+    return tex_sample(&r->sc->textures[m->color_map - 1], t[0] * a + t[2] * b1 + t[4] * b2,
+                      t[1] * a + t[3] * b1 + t[5] * b2);
+}
+
 static v3 shading_normal(const rscene* r, int id, float beta, float gamma) {
     const float* n = r->nrm + (long)id * 9;
     float alpha = 1.0f - beta - gamma;
@@ -660,17 +704,22 @@ static v3 compat_radiance(const rscene* r, v3 o, v3 d, int max_bounce, opcg* rnd
     for (int depth = 0; depth < max_bounce; ++depth) {
         ohit h;
         if (!closest(r, o, d, kFHitMin, kFHitMax, 0, &h)) {
-            L = add(L, mul(W, ld3(r->sc->sky)));
+            L = add(L, mul(W, environment(r, d)));
             break;
         }
         v3 pos = add(o, scl(d, h.t));
         const oracle_material* m = &r->mats[r->mat[h.id]];
         L = add(L, mul(W, ld3(m->emission)));
         v3 n = shading_normal(r, h.id, h.u, h.v);
+        /* TexturedMaterial (src/s3d_texturedmaterial.cpp:63-87): the map scales the NEE base
+         * colour and the Shade weight */
+        v3 tx = color_map(r, m, h.id, h.u, h.v);
+        oracle_material mt = *m;
+        for (int c = 0; c < 3; ++c) mt.color[c] *= (c == 0 ? tx.x : c == 1 ? tx.y : tx.z);
         int delta = (m->type == ORACLE_MIRROR || m->type == ORACLE_GLASS);
-        if (!delta && r->sc->has_light) L = add(L, mul(W, compat_nee(r, pos, n, m, rnd)));
+        if (!delta && r->sc->has_light) L = add(L, mul(W, compat_nee(r, pos, n, &mt, rnd)));
         v3 out; int dice = 0;
-        W = mul(W, compat_shade(m, d, n, rnd, &out, &dice));
+        W = mul(W, mul(compat_shade(m, d, n, rnd, &out, &dice), tx));
         if (dice) break;
         if (W.x < FLT_EPSILON && W.y < FLT_EPSILON && W.z < FLT_EPSILON) break;
         o = pos; d = out;
@@ -760,7 +809,7 @@ static v3 phys_radiance(const rscene* r, v3 o, v3 d, const oracle_render_opts* o
     for (int depth = 0; depth < opt->max_depth; ++depth) {
         ohit h;
         if (!closest(r, o, d, kEps, INFINITY, 1, &h)) {
-            L = add(L, mul(W, ld3(sc->sky)));
+            L = add(L, mul(W, environment(r, d)));
             if (sc->has_sun && r->sun_disk && dot(d, r->sun_dir) >= r->sun_cos_max) {
                 float w = prev_delta ? 1.0f : prev_pdf / (prev_pdf + r->sun_pdf);
                 L = add(L, scl(mul(W, r->sun_L), w));
@@ -780,7 +829,12 @@ static v3 phys_radiance(const rscene* r, v3 o, v3 d, const oracle_render_opts* o
             }
             break;
         }
-        const oracle_material* m = &r->mats[r->mat[h.id]];
+        oracle_material mtex = r->mats[r->mat[h.id]];
+        {   /* the colour map scales the base colour */
+            v3 tx = color_map(r, &mtex, h.id, h.u, h.v);
+            mtex.color[0] *= tx.x; mtex.color[1] *= tx.y; mtex.color[2] *= tx.z;
+        }
+        const oracle_material* m = &mtex;
         L = add(L, mul(W, ld3(m->emission)));
         v3 ng = geometric_normal(r, h.id);
         int into = dot(ng, d) < 0.0f;

@@ -59,7 +59,13 @@ typedef struct {
     float roughness;
     float specular[3];  /* Plastic: specular colour (color is the diffuse one) */
     float power;        /* Phong / Plastic: lobe exponent */
+    int   color_map;    /* 1 + texture index multiplying the base colour, 0 = none */
 } oracle_material;
+
+typedef struct {
+    int          width, height;
+    const float* rgb;   /* texel (x, y) at rgb[3 * (y * width + x)] */
+} oracle_texture;
 
 typedef struct {
     const float* tri_pos;   /* n*9 */
@@ -79,6 +85,11 @@ typedef struct {
     float        cam_fov, cam_near; /* fov used linearly as in include/s3d_camera.h:85-86 */
     float        cam_lens;          /* thin-lens radius (0: pinhole) */
     float        cam_focal;         /* focal distance (0: |target - pos|, as ThinLensCamera) */
+    const float* tri_uv;            /* n*6 texture coordinates, or NULL */
+    const oracle_texture* textures;
+    int          n_textures;
+    int          ibl_map;           /* 1 + texture index of the environment, 0 = constant sky */
+    float        ibl_scale;
 } oracle_scene;
 
 typedef struct {

@@ -41,7 +41,8 @@ class SaltyError(RuntimeError):
 
 class Material(C.Structure):
     _fields_ = [("type", C.c_int32), ("color", C.c_float * 3), ("emission", C.c_float * 3),
-                ("ior", C.c_float), ("roughness", C.c_float), ("specular", C.c_float * 3), ("power", C.c_float)]
+                ("ior", C.c_float), ("roughness", C.c_float), ("specular", C.c_float * 3), ("power", C.c_float),
+                ("color_map", C.c_int32)]
 
 
 class Camera(C.Structure):
@@ -56,7 +57,13 @@ class SceneDesc(C.Structure):
                 ("has_light", C.c_int32), ("light_corner", C.c_float * 3), ("light_edge_a", C.c_float * 3),
                 ("light_edge_b", C.c_float * 3), ("light_emission", C.c_float * 3),
                 ("has_sun", C.c_int32), ("sun_dir", C.c_float * 3), ("sun_radiance", C.c_float * 3),
-                ("sun_half_angle", C.c_float), ("sky", C.c_float * 3), ("camera", Camera)]
+                ("sun_half_angle", C.c_float), ("sky", C.c_float * 3), ("camera", Camera),
+                ("tri_uv", C.c_void_p), ("textures", C.c_void_p), ("n_textures", C.c_int32), ("ibl_map", C.c_int32),
+                ("ibl_scale", C.c_float)]
+
+
+class Texture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgb", C.c_void_p)]
 
 
 class BuildOpts(C.Structure):
@@ -94,7 +101,7 @@ class Mesh(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("trace_block", C.c_int32), ("trace_pool", C.c_int32), ("trace_postpone", C.c_int32),
-                ("shade_block", C.c_int32), ("wave_paths", C.c_int64)]
+                ("shade_block", C.c_int32), ("trace_regs", C.c_int32), ("wave_paths", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -303,7 +310,10 @@ class Context:
         return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
 
     def upload_scene(self, tri_pos, tri_nrm=None, tri_mat=None, materials=(), light=None, sun=None,
-                     sky=(0.0, 0.0, 0.0), camera=None) -> "Scene":
+                     sky=(0.0, 0.0, 0.0), camera=None, tri_uv=None, textures=(), ibl=None,
+                     ibl_scale: float = 10.0) -> "Scene":
+        """textures: (H, W, 3) float arrays; a material's "texture" key names its colour map
+        and `ibl` the environment map (indices into textures)."""
         tri_pos = tri_pos if hasattr(tri_pos, "data_ptr") else np.ascontiguousarray(tri_pos, np.float32)
         n = tri_pos.shape[0] if tri_pos.ndim == 2 else tri_pos.size // 9
         if tri_nrm is not None and not hasattr(tri_nrm, "data_ptr"):
@@ -319,7 +329,20 @@ class Context:
             mats[i].roughness = float(m.get("roughness", 0.3))
             mats[i].specular = _f3(m.get("specular", (0.0, 0.0, 0.0)))
             mats[i].power = float(m.get("power", 32.0))
+            mats[i].color_map = 0 if m.get("texture") is None else int(m["texture"]) + 1
+        texs = [np.ascontiguousarray(t, np.float32) for t in textures]
+        ttab = (Texture * max(1, len(texs)))()
+        for i, t in enumerate(texs):
+            ttab[i].height, ttab[i].width = t.shape[0], t.shape[1]
+            ttab[i].rgb = t.ctypes.data
+        if tri_uv is not None and not hasattr(tri_uv, "data_ptr"):
+            tri_uv = np.ascontiguousarray(tri_uv, np.float32)
         d = SceneDesc()
+        d.tri_uv = _ptr(tri_uv)
+        d.textures = C.addressof(ttab) if texs else None
+        d.n_textures = len(texs)
+        d.ibl_map = 0 if ibl is None else int(ibl) + 1
+        d.ibl_scale = float(ibl_scale)
         d.tri_pos, d.tri_nrm, d.tri_mat = _ptr(tri_pos), _ptr(tri_nrm), _ptr(tri_mat)
         d.n_tris = n
         d.mats = C.addressof(mats) if materials else None

@@ -53,6 +53,11 @@ __global__ void k_validate(const float* __restrict__ pos, const int* __restrict_
     if (mat[i] < 0 || mat[i] >= n_mats) atomicAdd(&bad[1], 1);
 }
 
+__global__ void k_rgb_to_texels(const float* __restrict__ rgb, long long n, float4* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = make_float4(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], 0.0f);
+}
+
 __global__ void k_fill_int(int* p, long long n, int v) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) p[i] = v;
@@ -215,6 +220,9 @@ salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* d, salty
         g.roughness = m.roughness;
         for (int c = 0; c < 3; ++c) g.specular[c] = m.specular[c];
         g.power = m.power;
+        g.color_map = m.color_map - 1;
+        if (g.color_map < -1 || g.color_map >= d->n_textures)
+            return fail(E.fail(SALTY_ERR_INVALID_ARG, "material %d: color_map outside the texture table", i));
         // Lambert::Lambert (src/s3d_lambert.cpp:22-31), Phong::Phong (src/s3d_phong.cpp:22-31),
         // Plastic::Plastic (src/s3d_plastic.cpp:22-37): max(colour, 0.01)
         g.rr_threshold = std::max(std::max(std::max(m.color[0], m.color[1]), m.color[2]), 0.01f);
@@ -227,6 +235,7 @@ salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* d, salty
         // the light: a black Lambert emitter (two-sided in the compat profile)
         GpuMaterial lm{};
         lm.type = SALTY_LAMBERT;
+        lm.color_map = -1;
         for (int c = 0; c < 3; ++c) lm.emission[c] = d->light_emission[c];
         lm.rr_threshold = 0.01f;
         mats[d->n_mats] = lm;
@@ -253,6 +262,7 @@ salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* d, salty
     if (sc->n_mats == 0) {  // no table: one grey Lambert
         GpuMaterial g{};
         g.type = SALTY_LAMBERT;
+        g.color_map = -1;
         g.color[0] = g.color[1] = g.color[2] = 0.75f;
         g.rr_threshold = 0.75f;
         mats[0] = g;
@@ -269,6 +279,44 @@ salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* d, salty
         if (hb[0]) return fail(E.fail(SALTY_ERR_INVALID_ARG, "%d triangles have non-finite vertices", hb[0]));
         if (hb[1]) return fail(E.fail(SALTY_ERR_INVALID_ARG, "%d triangles reference a material outside 0..%d", hb[1], n_user_mats - 1));
     }
+    // texture coordinates and textures
+    UP_CUDA(sc->uv.ensure((size_t)n * 6));
+    UP_CUDA(cudaMemsetAsync(sc->uv.p, 0, (size_t)n * 6 * sizeof(float), ctx->stream));
+    if (d->tri_uv && n_in > 0) UP_TRY(copy_in(ctx, sc->uv.p, d->tri_uv, (size_t)n_in * 6 * sizeof(float)));
+    if (d->n_textures < 0 || (d->n_textures > 0 && !d->textures))
+        return fail(E.fail(SALTY_ERR_INVALID_ARG, "bad texture table"));
+    {
+        std::vector<GpuTexture> tt(std::max(d->n_textures, 1));
+        long long texels = 0;
+        for (int t = 0; t < d->n_textures; ++t) {
+            const salty_texture& x = d->textures[t];
+            if (x.width <= 0 || x.height <= 0 || !x.rgb || (long long)x.width * x.height > (1ll << 28))
+                return fail(E.fail(SALTY_ERR_INVALID_ARG, "texture %d: bad size or data", t));
+            tt[t] = GpuTexture{texels, x.width, x.height};
+            texels += (long long)x.width * x.height;
+        }
+        UP_CUDA(sc->textures.ensure(tt.size()));
+        UP_CUDA(sc->texels.ensure((size_t)std::max(texels, 1ll)));
+        DevBuf<float> stage;
+        for (int t = 0; t < d->n_textures; ++t) {
+            const salty_texture& x = d->textures[t];
+            const long long np = (long long)x.width * x.height;
+            UP_CUDA(stage.ensure((size_t)np * 3));
+            UP_TRY(copy_in(ctx, stage.p, x.rgb, (size_t)np * 3 * sizeof(float)));
+            k_rgb_to_texels<<<(unsigned)((np + 255) / 256), 256, 0, ctx->stream>>>(stage.p, np,
+                                                                                    sc->texels.p + tt[t].offset);
+            UP_CUDA(cudaStreamSynchronize(ctx->stream));
+        }
+        UP_CUDA(cudaMemcpyAsync(sc->textures.p, tt.data(), sizeof(GpuTexture) * tt.size(), cudaMemcpyHostToDevice,
+                                ctx->stream));
+        UP_CUDA(cudaStreamSynchronize(ctx->stream));
+        sc->n_textures = d->n_textures;
+        sc->n_texels = texels;
+    }
+    if (d->ibl_map < 0 || d->ibl_map > d->n_textures)
+        return fail(E.fail(SALTY_ERR_INVALID_ARG, "ibl_map outside the texture table"));
+    k.ibl_map = d->ibl_map - 1;
+    k.ibl_scale = d->ibl_scale > 0.0f ? d->ibl_scale : 10.0f;
     UP_CUDA(sc->mats.ensure(sc->n_mats));
     UP_CUDA(cudaMemcpyAsync(sc->mats.p, mats.data(), sizeof(GpuMaterial) * sc->n_mats, cudaMemcpyHostToDevice,
                             ctx->stream));
@@ -524,6 +572,7 @@ salty_status salty_get_tuning(salty_ctx* ctx, salty_tuning* out) {
     out->trace_pool = ctx->tune.trace.pool;
     out->trace_postpone = ctx->tune.trace.postpone;
     out->shade_block = ctx->tune.shade_block;
+    out->trace_regs = ctx->tune.trace.regs;
     out->wave_paths = ctx->tune.wave_paths;
     return SALTY_OK;
 }
@@ -539,12 +588,14 @@ salty_status salty_set_tuning(salty_ctx* ctx, const salty_tuning* t) {
         return E.fail(SALTY_ERR_INVALID_ARG, "trace_postpone must be 1..32");
     if (t->shade_block < 64 || t->shade_block > 1024 || t->shade_block % 32)
         return E.fail(SALTY_ERR_INVALID_ARG, "shade_block must be a multiple of 32 in 64..1024");
+    if (t->trace_regs != 64 && t->trace_regs != 48) return E.fail(SALTY_ERR_INVALID_ARG, "trace_regs must be 64 or 48");
     if (t->wave_paths < (1 << 16) || t->wave_paths > (1 << 26))
         return E.fail(SALTY_ERR_INVALID_ARG, "wave_paths must be 2^16..2^26");
     ctx->tune.trace.block = t->trace_block;
     ctx->tune.trace.pool = t->trace_pool;
     ctx->tune.trace.postpone = t->trace_postpone;
     ctx->tune.shade_block = t->shade_block;
+    ctx->tune.trace.regs = t->trace_regs;
     ctx->tune.wave_paths = t->wave_paths;
     return SALTY_OK;
 }
@@ -590,6 +641,7 @@ salty_status salty_autotune(salty_ctx* ctx, salty_scene* const* scenes, const sa
     const int shade[] = {128, 256, 512};
     const int tblock[] = {64, 128, 256};
     const int pool[] = {64, 128, 256};
+    const int regs[] = {64, 48};
     const int postpone[] = {1, 4, 7, 10};
     auto try_knob = [&](auto set, const auto& values) -> salty_status {
         for (auto v : values) {
@@ -614,6 +666,9 @@ salty_status salty_autotune(salty_ctx* ctx, salty_scene* const* scenes, const sa
     if (s == SALTY_OK)
         s = try_knob([&](Tuning& t, int v) { if (v == best.trace.block) return false; t.trace.block = v; return true; },
                      tblock);
+    if (s == SALTY_OK)
+        s = try_knob([&](Tuning& t, int v) { if (v == best.trace.regs) return false; t.trace.regs = v; return true; },
+                     regs);
     if (s == SALTY_OK)
         s = try_knob([&](Tuning& t, int v) { if (v == best.trace.pool) return false; t.trace.pool = v; return true; },
                      pool);

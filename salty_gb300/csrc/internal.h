@@ -111,6 +111,13 @@ struct GpuMaterial {
     float rr_threshold;  // compat dice threshold max(colour, 0.01)
     float specular[3];   // Plastic
     float power;         // Phong, Plastic lobe exponent
+    int color_map;       // texture multiplying the base colour, -1 none
+};
+
+// A texture in the scene's texel array: float4 texels (rgb, unused) from `offset`.
+struct GpuTexture {
+    long long offset;
+    int width, height;
 };
 
 struct SceneConsts {
@@ -130,6 +137,8 @@ struct SceneConsts {
     float cam_fov, cam_near;
     float cam_target[3], cam_up[3];
     float cam_lens, cam_focal;  // thin lens radius (0: pinhole), focal distance
+    int ibl_map;                // environment texture, -1: constant sky
+    float ibl_scale;
 };
 
 struct Film {
@@ -168,6 +177,7 @@ struct TraceTuning {
     int block = 128;     // threads per block: 64, 128 or 256
     int pool = 128;      // rays a warp takes from the global cursor per refill
     int postpone = 7;    // fewest lanes that test a triangle group together
+    int regs = 64;       // register budget per thread: 64 (as compiled) or 48 (more resident warps)
 };
 
 }  // namespace salty
@@ -180,6 +190,11 @@ struct salty_scene {
     salty::DevBuf<int> mat;      // n_tris
     salty::DevBuf<salty::GpuMaterial> mats;
     int n_mats = 0;
+    salty::DevBuf<float> uv;     // n_tris * 6 (zeros when none were given)
+    salty::DevBuf<salty::GpuTexture> textures;
+    salty::DevBuf<float4> texels;
+    int n_textures = 0;
+    int64_t n_texels = 0;
     salty::SceneConsts consts{};
     salty::Bvh bvh;
     salty::Film film;
@@ -209,10 +224,12 @@ struct BatchArena {
     std::vector<std::pair<const void*, uint64_t>> key;  // (scene, BVH generation) per slot
     DevBuf<Bvh8Node> nodes;
     DevBuf<float4> tris;
-    DevBuf<float> pos, nrm;
+    DevBuf<float> pos, nrm, uv;
     DevBuf<int> mat;
     DevBuf<GpuMaterial> mats;
-    std::vector<long long> node_off, id_off;
+    DevBuf<GpuTexture> textures;
+    DevBuf<float4> texels;
+    std::vector<long long> node_off, id_off, tex_off;
     int depth = 0;
 };
 }  // namespace salty

@@ -133,8 +133,11 @@ struct SceneSlot {
 struct WaveParams {
     const float* pos;
     const float* nrm;
+    const float* uv;
     const int* mat;
     const GpuMaterial* mats;
+    const GpuTexture* textures;
+    const float4* texels;
     const SceneSlot* slots;
     const long long* sample_off;  // per slot, then the total (n_slots + 1 entries)
     const long long* pixel_off;   // per slot, then the total
@@ -272,6 +275,51 @@ __device__ __forceinline__ Surf surface(const WaveParams& P, int id, float t, fl
     return s;
 }
 
+// Texture::SampleColor (src/s3d_texture.cpp:925-952): bilinear, weights taken before the
+// wrap, indices wrapped as |i % size| (which mirrors negative ones, as the reference does).
+__device__ V tex_sample(const WaveParams& P, int map, float u, float v) {
+    const GpuTexture t = P.textures[map];
+    float fx = u * (float)(t.width - 1), fy = v * (float)(t.height - 1);
+    if (!(fabsf(fx) < 1e9f)) fx = 0.0f;  // NaN / huge coordinates: keep the index arithmetic defined
+    if (!(fabsf(fy) < 1e9f)) fy = 0.0f;
+    int x0 = (int)floorf(fx), y0 = (int)floorf(fy);
+    int x1 = x0 + 1, y1 = y0 + 1;
+    const float xw0 = (float)x1 - fx, xw1 = fx - (float)x0, yw0 = (float)y1 - fy, yw1 = fy - (float)y0;
+    x0 = abs(x0 % t.width);
+    x1 = abs(x1 % t.width);
+    y0 = abs(y0 % t.height);
+    y1 = abs(y1 % t.height);
+    const float4* T = P.texels + t.offset;
+    const float4 c00 = T[(long long)y0 * t.width + x0], c01 = T[(long long)y1 * t.width + x0];
+    const float4 c10 = T[(long long)y0 * t.width + x1], c11 = T[(long long)y1 * t.width + x1];
+    return (xyz(c00) * yw0 + xyz(c01) * yw1) * xw0 + (xyz(c10) * yw0 + xyz(c11) * yw1) * xw1;
+}
+
+// Texture::SampleColor(dir) (src/s3d_texture.cpp:957-972): latitude-longitude lookup
+__device__ V tex_sphere(const WaveParams& P, int map, V d) {
+    const float theta = acosf(fminf(1.0f, fmaxf(-1.0f, d.y)));
+    float u = 0.0f;
+    const float v = theta * (1.0f / kPi);
+    if (!(fabsf(d.x) <= FLT_EPSILON) && !(fabsf(d.z) <= FLT_EPSILON)) {
+        const float phi = atan2f(d.z, d.x);
+        u = (d.z < 0.0f ? phi + k2Pi : phi) * (1.0f / k2Pi);
+    }
+    return tex_sample(P, map, u, v);
+}
+
+// radiance arriving from the environment along d (Scene::SampleIBL, include/s3d_scene.h:81-82)
+__device__ __forceinline__ V environment(const WaveParams& P, const SceneConsts& k, V d) {
+    return k.ibl_map >= 0 ? tex_sphere(P, k.ibl_map, d) * k.ibl_scale : ld3(k.sky);
+}
+
+// the material's colour map at the hit (Triangle::CalcParam's texture coordinate), or 1
+__device__ __forceinline__ V color_map(const WaveParams& P, const GpuMaterial& m, int id, float b1, float b2) {
+    if (m.color_map < 0) return mk(1.0f, 1.0f, 1.0f);
+    const float* t = P.uv + (size_t)id * 6;
+    const float a = 1.0f - b1 - b2;
+    return tex_sample(P, m.color_map, t[0] * a + t[2] * b1 + t[4] * b2, t[1] * a + t[3] * b1 + t[5] * b2);
+}
+
 __device__ __forceinline__ bool is_light(const SceneConsts& k, int id) {
     return k.light_tri0 >= 0 && id >= k.light_tri0 && id < k.light_tri0 + 2;
 }
@@ -372,7 +420,10 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
         const SceneSlot& S = P.slots[slot];
         const SceneConsts& K = S.k;
         if (live && id >= 0 && !is_light(K, id)) {
-            const GpuMaterial m = P.mats[P.mat[id]];
+            GpuMaterial m = P.mats[P.mat[id]];
+            // TexturedMaterial::GetBaseColor: the colour map multiplies the base colour
+            const V tx = color_map(P, m, id, h.z, h.w);
+            m.color[0] *= tx.x; m.color[1] *= tx.y; m.color[2] *= tx.z;
             const bool delta = (m.type == SALTY_MIRROR || m.type == SALTY_GLASS);
             Rng rng;
             rng.s = (unsigned long long)mt.x | ((unsigned long long)mt.y << 32);
@@ -527,12 +578,13 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                                    np[2] * al + np[5] * h.z + np[8] * h.w));
                 if (dot(n, d) > 0.0f) n = -n;
                 const bool emitter = is_light(K, id);
-                B.abuf[2 * mt.z] = make_float4(emitter ? 1.0f : am.color[0], emitter ? 1.0f : am.color[1],
-                                               emitter ? 1.0f : am.color[2], 1.0f / (1.0f + h.x));
+                const V atx = color_map(P, am, id, h.z, h.w);
+                B.abuf[2 * mt.z] = make_float4(emitter ? 1.0f : am.color[0] * atx.x, emitter ? 1.0f : am.color[1] * atx.y,
+                                               emitter ? 1.0f : am.color[2] * atx.z, 1.0f / (1.0f + h.x));
                 B.abuf[2 * mt.z + 1] = make_float4(n.x, n.y, n.z, 0.0f);
             }
             if (id < 0) {
-                L = L + W * ld3(K.sky);
+                L = L + W * environment(P, K, d);
                 // an escaping ray inside the sun's disk (physical profile, finite sun)
                 if (!compat && K.has_sun && K.sun_disk && dot(d, ld3(K.sun_dir)) >= K.sun_cos_max) {
                     const float w = prev_delta ? 1.0f : prev_pdf / (prev_pdf + K.sun_pdf);
@@ -540,6 +592,7 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                 }
             } else if (compat) {
                 const GpuMaterial m = P.mats[P.mat[id]];
+                const V tx = color_map(P, m, id, h.z, h.w);  // TexturedMaterial::Shade scales the weight
                 V pos = mk(__fadd_rn(o.x, __fmul_rn(d.x, h.x)), __fadd_rn(o.y, __fmul_rn(d.y, h.x)),
                            __fadd_rn(o.z, __fmul_rn(d.z, h.x)));
                 L = L + W * ld3(m.emission);
@@ -618,7 +671,7 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                     dice = rng.f32() >= m.rr_threshold;
                     wgt = col;
                 }
-                W = W * wgt;
+                W = W * (wgt * tx);
                 bool stop = dice || (W.x < FLT_EPSILON && W.y < FLT_EPSILON && W.z < FLT_EPSILON) ||
                             depth + 1 >= S.max_depth;
                 if (!stop) {
@@ -638,7 +691,9 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                     }
                 }
             } else {
-                const GpuMaterial m = P.mats[P.mat[id]];
+                GpuMaterial m = P.mats[P.mat[id]];
+                const V tx = color_map(P, m, id, h.z, h.w);
+                m.color[0] *= tx.x; m.color[1] *= tx.y; m.color[2] *= tx.z;
                 Surf s = surface(P, id, h.x, h.z, h.w, o, d);
                 L = L + W * ld3(m.emission);
                 V col = ld3(m.color), wi, wgt;
@@ -887,6 +942,23 @@ __global__ void k_arena_tris(const float4* __restrict__ src, long long n, int id
     }
 }
 
+__global__ void k_arena_mats(const GpuMaterial* __restrict__ src, int n, int tex_off, GpuMaterial* __restrict__ dst) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        GpuMaterial m = src[i];
+        if (m.color_map >= 0) m.color_map += tex_off;
+        dst[i] = m;
+    }
+}
+
+__global__ void k_arena_textures(const GpuTexture* __restrict__ src, int n, long long texel_off,
+                                 GpuTexture* __restrict__ dst) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        GpuTexture t = src[i];
+        t.offset += texel_off;
+        dst[i] = t;
+    }
+}
+
 __global__ void k_arena_mat(const int* __restrict__ src, long long n, int mat_off, int* __restrict__ dst) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         dst[i] = src[i] + mat_off;
@@ -987,10 +1059,11 @@ salty_status ensure_arena(salty_ctx* ctx, salty_scene* const* scenes, int n) {
     for (int i = 0; i < n; ++i) key[i] = {scenes[i], scenes[i]->bvh.generation};
     if (key == A.key && A.nodes.p) return SALTY_OK;
     A.key.clear();
-    long long nn = 0, nl = 0, nt = 0, nm = 0;
+    long long nn = 0, nl = 0, nt = 0, nm = 0, ntex = 0, ntx = 0;
     A.node_off.assign(n, 0);
     A.id_off.assign(n, 0);
-    std::vector<long long> leaf_off(n), mat_off(n);
+    A.tex_off.assign(n, 0);
+    std::vector<long long> leaf_off(n), mat_off(n), texel_off(n);
     int depth = 0;
     for (int i = 0; i < n; ++i) {
         const salty_scene* sc = scenes[i];
@@ -998,10 +1071,14 @@ salty_status ensure_arena(salty_ctx* ctx, salty_scene* const* scenes, int n) {
         leaf_off[i] = nl;
         A.id_off[i] = nt;
         mat_off[i] = nm;
+        A.tex_off[i] = ntex;
+        texel_off[i] = ntx;
         nn += sc->bvh.n_nodes;
         nl += sc->bvh.n_tris;
         nt += sc->n_tris;
         nm += sc->n_mats;
+        ntex += sc->n_textures;
+        ntx += sc->n_texels;
         depth = std::max(depth, (int)sc->bvh.depth);
     }
     if (nn >= (1ll << 31) || nl >= (1ll << 31) || nt >= (1ll << 31))
@@ -1010,6 +1087,9 @@ salty_status ensure_arena(salty_ctx* ctx, salty_scene* const* scenes, int n) {
     SALTY_TRY_CUDA(E, A.tris.ensure(nl * kTriFloat4));
     SALTY_TRY_CUDA(E, A.pos.ensure(nt * 9));
     SALTY_TRY_CUDA(E, A.nrm.ensure(nt * 9));
+    SALTY_TRY_CUDA(E, A.uv.ensure(nt * 6));
+    SALTY_TRY_CUDA(E, A.textures.ensure(std::max(ntex, 1ll)));
+    SALTY_TRY_CUDA(E, A.texels.ensure(std::max(ntx, 1ll)));
     SALTY_TRY_CUDA(E, A.mat.ensure(nt));
     SALTY_TRY_CUDA(E, A.mats.ensure(nm));
     cudaStream_t st = ctx->stream;
@@ -1025,8 +1105,15 @@ salty_status ensure_arena(salty_ctx* ctx, salty_scene* const* scenes, int n) {
                                           cudaMemcpyDeviceToDevice, st));
         SALTY_TRY_CUDA(E, cudaMemcpyAsync(A.nrm.p + A.id_off[i] * 9, sc->nrm.p, sc->n_tris * 9 * sizeof(float),
                                           cudaMemcpyDeviceToDevice, st));
-        SALTY_TRY_CUDA(E, cudaMemcpyAsync(A.mats.p + mat_off[i], sc->mats.p, sc->n_mats * sizeof(GpuMaterial),
+        SALTY_TRY_CUDA(E, cudaMemcpyAsync(A.uv.p + A.id_off[i] * 6, sc->uv.p, sc->n_tris * 6 * sizeof(float),
                                           cudaMemcpyDeviceToDevice, st));
+        k_arena_mats<<<1, 256, 0, st>>>(sc->mats.p, sc->n_mats, (int)A.tex_off[i], A.mats.p + mat_off[i]);
+        if (sc->n_textures > 0) {
+            k_arena_textures<<<1, 256, 0, st>>>(sc->textures.p, sc->n_textures, texel_off[i],
+                                                A.textures.p + A.tex_off[i]);
+            SALTY_TRY_CUDA(E, cudaMemcpyAsync(A.texels.p + texel_off[i], sc->texels.p, sc->n_texels * sizeof(float4),
+                                              cudaMemcpyDeviceToDevice, st));
+        }
     }
     SALTY_TRY_CUDA(E, cudaGetLastError());
     SALTY_TRY_CUDA(E, cudaStreamSynchronize(st));
@@ -1045,17 +1132,22 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     for (int i = 0; i < n; ++i) SALTY_TRY(prepare_film(ctx, scenes[i], opts[i]));
     // what the traversal walks: the scene itself, or the batch arena
     TraceTarget tgt;
-    const float *pos, *nrm;
+    const float *pos, *nrm, *uv;
     const int* mat;
     const GpuMaterial* mats;
+    const GpuTexture* textures;
+    const float4* texels;
     if (n == 1) {
         tgt.nodes = scenes[0]->bvh.nodes.p;
         tgt.tris = scenes[0]->bvh.tris.p;
         tgt.depth = scenes[0]->bvh.depth;
         pos = scenes[0]->pos.p;
         nrm = scenes[0]->nrm.p;
+        uv = scenes[0]->uv.p;
         mat = scenes[0]->mat.p;
         mats = scenes[0]->mats.p;
+        textures = scenes[0]->textures.p;
+        texels = scenes[0]->texels.p;
     } else {
         SALTY_TRY(ensure_arena(ctx, scenes, n));
         const BatchArena& A = ctx->arena;
@@ -1064,8 +1156,11 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
         tgt.depth = A.depth;
         pos = A.pos.p;
         nrm = A.nrm.p;
+        uv = A.uv.p;
         mat = A.mat.p;
         mats = A.mats.p;
+        textures = A.textures.p;
+        texels = A.texels.p;
     }
     // slot table
     std::vector<SceneSlot> slots(n);
@@ -1082,6 +1177,7 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
         std::memset(&S, 0, sizeof S);
         S.k = sc->consts;
         if (n > 1 && S.k.light_tri0 >= 0) S.k.light_tri0 += (int)ctx->arena.id_off[i];
+        if (n > 1 && S.k.ibl_map >= 0) S.k.ibl_map += (int)ctx->arena.tex_off[i];
         S.cam = camera_of(sc->consts, o.width, o.height);
         S.width = o.width;
         S.height = o.height;
@@ -1159,8 +1255,11 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     WaveParams P;
     P.pos = pos;
     P.nrm = nrm;
+    P.uv = uv;
     P.mat = mat;
     P.mats = mats;
+    P.textures = textures;
+    P.texels = texels;
     P.slots = reinterpret_cast<const SceneSlot*>(dslots);
     P.sample_off = doffs;
     P.pixel_off = doffs + n + 1;

@@ -14,9 +14,11 @@
 namespace salty {
 namespace {
 
-// counters: [0] ray cursor, [1] node fetches, [2] triangle fetches
-template <bool ANY, bool WT, bool COUNT, int DEPTH, int TB>
-__global__ void __launch_bounds__(TB)
+// counters: [0] ray cursor, [1] node fetches, [2] triangle fetches.  CAP: ask for
+// 1280 / TB resident blocks, which caps registers at 48 per thread (more warps per SM to
+// hide fetch latency, at the price of a few spilled values).
+template <bool ANY, bool WT, bool COUNT, int DEPTH, int TB, bool CAP>
+__global__ void __launch_bounds__(TB, CAP ? 1280 / TB : 1)
 k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, const float4* __restrict__ rays,
         const int* __restrict__ roots, long long n_arg, const int* __restrict__ n_dev, float4* __restrict__ hits,
         unsigned long long* __restrict__ counters, float cull_slack, int pool, int postpone,
@@ -105,9 +107,9 @@ struct Launch {
     int* status;
 };
 
-template <bool ANY, bool WT, bool COUNT, int DEPTH, int TB>
+template <bool ANY, bool WT, bool COUNT, int DEPTH, int TB, bool CAP>
 salty_status launch(salty_ctx* ctx, const Launch& L) {
-    auto kern = k_trace<ANY, WT, COUNT, DEPTH, TB>;
+    auto kern = k_trace<ANY, WT, COUNT, DEPTH, TB, CAP>;
     int per_sm = 0;
     SALTY_TRY_CUDA(ctx->err, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, 0));
     if (per_sm < 1) per_sm = 1;
@@ -121,11 +123,11 @@ salty_status launch(salty_ctx* ctx, const Launch& L) {
     return SALTY_OK;
 }
 
-template <int DEPTH, int TB>
+template <int DEPTH, int TB, bool CAP>
 salty_status dispatch_flags(salty_ctx* ctx, const Launch& L, uint32_t flags) {
     const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT;
 #define SALTY_L(A, W) \
-    if (any == A && wt == W) return launch<A, W, false, DEPTH, TB>(ctx, L)
+    if (any == A && wt == W) return launch<A, W, false, DEPTH, TB, CAP>(ctx, L)
     SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
 #undef SALTY_L
     return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad trace flags");
@@ -136,7 +138,7 @@ template <int DEPTH>
 salty_status dispatch_count(salty_ctx* ctx, const Launch& L, uint32_t flags) {
     const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT;
 #define SALTY_L(A, W) \
-    if (any == A && wt == W) return launch<A, W, true, DEPTH, 128>(ctx, L)
+    if (any == A && wt == W) return launch<A, W, true, DEPTH, 128, false>(ctx, L)
     SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
 #undef SALTY_L
     return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad trace flags");
@@ -162,13 +164,17 @@ salty_status trace_launch(salty_ctx* ctx, const TraceTarget& tgt, const TraceTun
         return shallow ? dispatch_count<24>(ctx, L, flags) : dispatch_count<48>(ctx, L, flags);
     // the 48-deep stack of a 256-thread block would not fit the 48 KB of static shared memory
     const int tb = (!shallow && tune.block > 128) ? 128 : tune.block;
+    const bool cap = tune.regs == 48;
+#define SALTY_D(D, B)                                                                                \
+    return cap ? dispatch_flags<D, B, true>(ctx, L, flags) : dispatch_flags<D, B, false>(ctx, L, flags)
     if (shallow) {
-        if (tb == 64) return dispatch_flags<24, 64>(ctx, L, flags);
-        if (tb == 256) return dispatch_flags<24, 256>(ctx, L, flags);
-        return dispatch_flags<24, 128>(ctx, L, flags);
+        if (tb == 64) SALTY_D(24, 64);
+        if (tb == 256) SALTY_D(24, 256);
+        SALTY_D(24, 128);
     }
-    if (tb == 64) return dispatch_flags<48, 64>(ctx, L, flags);
-    return dispatch_flags<48, 128>(ctx, L, flags);
+    if (tb == 64) SALTY_D(48, 64);
+    SALTY_D(48, 128);
+#undef SALTY_D
 }
 
 salty_status trace_launch(salty_ctx* ctx, salty_scene* sc, const float4* d_rays, long long n, const int* n_dev,

@@ -54,7 +54,9 @@ def cornell(variant: str = "baseline") -> dict:
     back wall GGX (roughness 0.3) -- exercises every BSDF.  "glossy": tall box Phong
     (specular 0.8, power 40), short box Plastic (diffuse (0.2, 0.4, 0.7), specular 0.6,
     power 120), back wall Phong (power 8).  "thinlens": the baseline box seen through a thin
-    lens of radius 0.06 focused on the tall box (target z = 0.6, focal distance 2.0)."""
+    lens of radius 0.06 focused on the tall box (target z = 0.6, focal distance 2.0).
+    "textured": a checkerboard colour map on the floor and back wall (TexturedMaterial) and
+    an environment map in place of the black sky, seen through the open front."""
     W, R, G = (0.75, 0.75, 0.75), (0.75, 0.25, 0.25), (0.25, 0.75, 0.25)
     mats = [{"type": LAMBERT, "color": W}, {"type": LAMBERT, "color": R}, {"type": LAMBERT, "color": G}]
     tall_m = short_m = back_m = 0
@@ -63,6 +65,9 @@ def cornell(variant: str = "baseline") -> dict:
                  {"type": GLASS, "color": (1.0, 1.0, 1.0), "ior": 1.5},
                  {"type": GGX, "color": (0.8, 0.6, 0.3), "roughness": 0.3}]
         tall_m, short_m, back_m = 3, 4, 5
+    elif variant == "textured":
+        mats += [{"type": LAMBERT, "color": (0.9, 0.9, 0.9), "texture": 0}]
+        back_m = 3
     elif variant == "glossy":
         mats += [{"type": PHONG, "color": (0.8, 0.8, 0.8), "power": 40.0},
                  {"type": PLASTIC, "color": (0.2, 0.4, 0.7), "specular": (0.6, 0.6, 0.6), "power": 120.0},
@@ -74,7 +79,7 @@ def cornell(variant: str = "baseline") -> dict:
         tris.extend(ts)
         mid.extend([m] * len(ts))
 
-    add(_quad((0, 0, 0), (0, 0, 1), (1, 0, 1), (1, 0, 0)), 0)      # floor, normal +y
+    add(_quad((0, 0, 0), (0, 0, 1), (1, 0, 1), (1, 0, 0)), 3 if variant == "textured" else 0)  # floor, +y
     add(_quad((0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1)), 0)      # ceiling, normal -y
     add(_quad((0, 0, 1), (0, 1, 1), (1, 1, 1), (1, 0, 1)), back_m)  # back wall, normal -z
     add(_quad((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0)), 1)      # x = 1 (image left), red
@@ -85,6 +90,21 @@ def cornell(variant: str = "baseline") -> dict:
     g = np.cross(pos[:, 3:6] - pos[:, 0:3], pos[:, 6:9] - pos[:, 0:3])
     g /= np.linalg.norm(g, axis=1, keepdims=True)
     nrm = np.tile(g, (1, 3)).astype(np.float32)
+    extra = {}
+    if variant == "textured":
+        # texture coordinates from the floor's (x, z) and the back wall's (x, y); a 64 x 64
+        # checkerboard of 8 x 8 blocks, and a 32 x 16 latitude-longitude environment
+        uv = np.zeros((pos.shape[0], 6), np.float32)
+        for k in range(3):
+            p = pos[:, 3 * k:3 * k + 3]
+            uv[0:2, 2 * k], uv[0:2, 2 * k + 1] = p[0:2, 0], p[0:2, 2]
+            uv[4:6, 2 * k], uv[4:6, 2 * k + 1] = p[4:6, 0], p[4:6, 1]
+        yy, xx = np.mgrid[0:64, 0:64]
+        chk = ((xx // 8 + yy // 8) % 2).astype(np.float32)
+        tex = np.stack([0.2 + 0.7 * chk, 0.25 + 0.5 * chk, 0.9 - 0.6 * chk], -1).astype(np.float32)
+        ev, eu = np.mgrid[0:16, 0:32]
+        env = np.stack([0.02 + 0.03 * eu / 31, 0.04 * (1 - ev / 15), 0.05 + 0.0 * eu], -1).astype(np.float32)
+        extra = {"tri_uv": uv, "textures": [tex, env], "ibl": 1}
     return {
         "name": f"cornell-{variant}",
         "tri_pos": pos, "tri_nrm": nrm, "tri_mat": np.array(mid, np.int32), "materials": mats,
@@ -94,6 +114,7 @@ def cornell(variant: str = "baseline") -> dict:
         "camera": {"pos": (0.5, 0.5, -1.4), "target": (0.5, 0.5, 0.6 if variant == "thinlens" else 0.0),
                    "up": (0.0, 1.0, 0.0), "fov": 2.0 * math.tan(math.radians(20.0)), "near": 1.0,
                    "lens_radius": 0.06 if variant == "thinlens" else 0.0},
+        **extra,
     }
 
 

@@ -82,7 +82,8 @@ def cornell_scene(variant: str = "baseline") -> SceneData:
     from salty_gb300 import scenes  # noqa: E402  (numpy-only module)
     sc = scenes.cornell(variant)
     return SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], None,
-                     sc["sky"], sc["camera"])
+                     sc["sky"], sc["camera"], tri_uv=sc.get("tri_uv"), textures=sc.get("textures", []),
+                     ibl=sc.get("ibl"))
 
 
 def hdr_image(seed: int, w: int, h: int) -> np.ndarray:
@@ -119,10 +120,23 @@ def thinlens_fixture(r) -> None:
     print(f"thin-lens cornell reference render: {secs:.2f} s")
 
 
+def textured_fixture(r) -> None:
+    """The Cornell box with colour maps and an environment map (TexturedMaterial, the IBL)."""
+    sc = cornell_scene("textured")
+    W = H = 48
+    spp, depth = 1024, 8
+    total, sq, secs = r.render(sc, W, H, spp, depth, seed=5151)
+    mean = total / spp
+    var = (sq / spp - mean * mean) * spp / (spp - 1) / spp
+    np.savez_compressed(os.path.join(HERE, "cornell_textured_ref_48.npz"), mean=mean.astype(np.float32),
+                        var=np.maximum(var, 0).astype(np.float32), spp=spp, max_bounce=depth, width=W, height=H)
+    print(f"textured cornell reference render: {secs:.2f} s")
+
+
 def main() -> None:
     build(with_reference=True)
     o, r = Oracle(), Reference()
-    only = {"glossy": glossy_fixture, "thinlens": thinlens_fixture}
+    only = {"glossy": glossy_fixture, "thinlens": thinlens_fixture, "textured": textured_fixture}
     if sys.argv[1:] and all(a in only for a in sys.argv[1:]):
         for a in sys.argv[1:]:
             only[a](r)
@@ -160,6 +174,7 @@ def main() -> None:
     print(f"cornell reference render: {secs:.2f} s")
     glossy_fixture(r)
     thinlens_fixture(r)
+    textured_fixture(r)
 
     # 4. tonemapping and the sRGB8 capture
     img = hdr_image(99, 48, 32)

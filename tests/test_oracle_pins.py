@@ -105,17 +105,19 @@ def test_oracle_compat_render_matches_reference_fixture(oracle):
 
 
 @pytest.mark.parametrize("variant,fixture,seed", [("glossy", "cornell_glossy_ref_48.npz", 31),
-                                                  ("thinlens", "cornell_thinlens_ref_48.npz", 32)])
+                                                  ("thinlens", "cornell_thinlens_ref_48.npz", 32),
+                                                  ("textured", "cornell_textured_ref_48.npz", 33)])
 def test_oracle_compat_variants_match_reference_fixtures(oracle, variant, fixture, seed):
-    """Phong and Plastic (src/s3d_phong.cpp:65-88, src/s3d_plastic.cpp:71-142), and the
-    ThinLensCamera (include/s3d_camera.h:150-267), through the reference's
-    PathTracer::Radiance."""
+    """Phong and Plastic (src/s3d_phong.cpp:65-88, src/s3d_plastic.cpp:71-142), the
+    ThinLensCamera (include/s3d_camera.h:150-267), and colour maps with an environment map
+    (src/s3d_texturedmaterial.cpp:63-87, src/s3d_texture.cpp:925-972), through the
+    reference's PathTracer::Radiance."""
     from oracle.oracle import PROFILE_COMPAT, SceneData
     from salty_gb300 import scenes
     g = np.load(os.path.join(GOLDEN, fixture))
     sc = scenes.cornell(variant)
     sd = SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], None, sc["sky"],
-                   sc["camera"])
+                   sc["camera"], tri_uv=sc.get("tri_uv"), textures=sc.get("textures", []), ibl=sc.get("ibl"))
     spp = int(g["spp"])
     tot, sq = oracle.render(sd, int(g["width"]), int(g["height"]), spp, int(g["max_bounce"]),
                             profile=PROFILE_COMPAT, seed=seed)

@@ -30,7 +30,8 @@ def _gpu_scene(ctx, sc):
 def _oracle_scene(sc):
     from oracle.oracle import SceneData
     return SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], sc["sun"],
-                     sc["sky"], sc["camera"])
+                     sc["sky"], sc["camera"], tri_uv=sc.get("tri_uv"), textures=sc.get("textures", []),
+                     ibl=sc.get("ibl"))
 
 
 def test_compat_cornell_matches_reference_fixture(ctx):
@@ -47,7 +48,8 @@ def test_compat_cornell_matches_reference_fixture(ctx):
 
 
 @pytest.mark.parametrize("variant,fixture", [("glossy", "cornell_glossy_ref_48.npz"),
-                                             ("thinlens", "cornell_thinlens_ref_48.npz")])
+                                             ("thinlens", "cornell_thinlens_ref_48.npz"),
+                                             ("textured", "cornell_textured_ref_48.npz")])
 def test_compat_variants_match_reference_fixtures(ctx, variant, fixture):
     """Phong and Plastic, and the thin-lens camera, in the reference's estimator vs the GPU
     compat profile."""
@@ -62,7 +64,7 @@ def test_compat_variants_match_reference_fixtures(ctx, variant, fixture):
     assert abs(r["mean"].mean() / g["mean"].mean() - 1) < 0.01
 
 
-@pytest.mark.parametrize("variant", ["baseline", "mixed", "glossy", "thinlens"])
+@pytest.mark.parametrize("variant", ["baseline", "mixed", "glossy", "thinlens", "textured"])
 def test_physical_cornell_matches_oracle(ctx, oracle, variant):
     import salty_gb300
     from oracle.oracle import PROFILE_PHYSICAL
