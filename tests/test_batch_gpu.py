@@ -16,7 +16,8 @@ def batch(ctx):
     from salty_gb300 import scenes
     descs = [scenes.cornell("baseline"), scenes.cornell("mixed"),
              scenes.heightfield(grid=64, n_spheres=40, seed=3, subdiv=2),
-             dict(scenes.soup(20000, seed=5), sky=(1.0, 1.0, 1.0))]
+             dict(scenes.soup(20000, seed=5), sky=(1.0, 1.0, 1.0)),
+             scenes.cornell("textured"), scenes.cornell("thinlens")]
     ss = []
     for d in descs:
         s = scenes.upload(ctx, d)
@@ -26,7 +27,9 @@ def batch(ctx):
     opts = [dict(width=48, height=40, spp=8, max_depth=8, seed=1, profile=P),
             dict(width=64, height=64, spp=4, max_depth=6, seed=2, profile=P, crop=(8, 16, 40, 24)),
             dict(width=96, height=54, spp=5, max_depth=12, seed=3, profile=P),
-            dict(width=32, height=32, spp=16, max_depth=4, seed=4, profile=P)]
+            dict(width=32, height=32, spp=16, max_depth=4, seed=4, profile=P),
+            dict(width=40, height=40, spp=6, max_depth=8, seed=5, profile=P),
+            dict(width=36, height=28, spp=7, max_depth=8, seed=6, profile=P)]
     yield ss, opts
     for s in ss:
         s.close()
