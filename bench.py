@@ -37,7 +37,7 @@ N_RAYS = 16_777_216
 SOUP_SEED, RAY_SEED = 20260001, 20260002
 TMIN = 1e-4
 METRIC = "Mrays/s"
-CPU_SAMPLE = 131_072        # rays of the same stream timed on the host cores
+CPU_SAMPLE = 4_194_304      # rays of the same stream timed on the host cores (~10 s of CPU work)
 # DRAM bytes (read + write) per ray of the closest-hit k_trace launch, from the ncu capture
 # of the same kernel on the same soup at 4,194,304 rays (profiles/trace_closest_soup1m_4Mrays.md);
 # rays in and hits out dominate and scale with the ray count, so traffic per launch is this
@@ -224,11 +224,20 @@ def run_time_to_rmse(args):
     r = s.render(W, H, 64, D, seed=5, want=())
     render = {"spp": 64, "ms": r["ms"], "Mrays_s": r["rays"] / r["ms"] / 1e3, "Mpaths_s": r["paths"] / r["ms"] / 1e3,
               "rays_per_path": r["rays"] / max(r["paths"], 1)}
+    # the plain path renders with the default launch shapes; the denoised paths with the
+    # shapes salty_autotune picks for this frame (trial renders at 1 spp, untimed)
+    default = ctx.tuning
+    t0 = time.perf_counter()
+    tuned, trial_ms = ctx.autotune([s], [{"width": W, "height": H, "spp": 1, "max_depth": D,
+                                          "profile": salty_gb300.PROFILE_PHYSICAL}], trial_spp=1)
+    tune_s = time.perf_counter() - t0
     res = {}
     with ClockSampler(0) as clk:
         for m in args.methods.split(","):
+            ctx.tuning = default if m == "plain" else tuned
             res[m] = cv.converge(s, W, H, crop, ref, D, args.target, method=m, ctx=ctx, denoiser=den,
                                  max_spp=args.max_spp)
+    ctx.tuning = default
     clocks = clk.summary()
     plain = res.get("plain", {}).get("seconds_to_target")
     best = res.get("unet", {}).get("seconds_to_target")
@@ -242,7 +251,10 @@ def run_time_to_rmse(args):
                    "window": crop, "ref_spp": args.ref_spp, "ref_noise_rel_mse": ref["noise"],
                    "ref_seconds": ref["seconds"], "setup_seconds": setup_s,
                    "denoiser": {"method": den.method, "hq_from_spp": den.hq_from_spp,
-                                "weights": {k: v for k, v in den.meta.items() if k != "scenes"}}},
+                                "weights": {k: v for k, v in den.meta.items() if k != "scenes"},
+                                "hq_weights": {k: v for k, v in den.hq_meta.items() if k != "scenes"}},
+                   "tuning_plain": default, "tuning_denoised": tuned, "autotune_seconds": tune_s,
+                   "autotune_trial_ms": trial_ms},
         "plain_seconds": plain, "speedup_vs_plain": (plain / best) if plain and best else None,
         "methods": {m: {"seconds_to_target": v["seconds_to_target"], "curve": v["curve"]} for m, v in res.items()},
         "render_c3": render, "clocks": clocks,
@@ -379,6 +391,10 @@ def main():
     torch.cuda.synchronize()  # the library runs on its own stream
     any_hit = args.any_hit
 
+    # launch shape for this workload (salty_autotune_trace, untimed)
+    default_tuning = ctx.tuning
+    tuning, tune_ms = scene.autotune_trace(d_rays, any_hit=any_hit)
+
     # fetch counts (untimed): algorithmic bytes per ray
     st = scene.trace_raw(d_rays, d_hits, any_hit=any_hit, counters=True)
     n_node = st["node_fetches"] / n_rays
@@ -443,6 +459,7 @@ def main():
                    "bvh_nodes": info["n_nodes"], "bvh_depth": info["depth"], "bvh_build_ms": info["build_ms"],
                    "sah_cost": info["sah_cost"], "triangle_test": "reference-compatible (bit-exact ids)",
                    "l2": "inputs larger than L2 (rays 512 MiB, hits 256 MiB); BVH resident",
+                   "tuning": tuning, "default_tuning": default_tuning,
                    "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": args.steps + e2e_kernels,

@@ -83,6 +83,12 @@ struct Material {
         r.m.power = power;
         return r;
     }
+    // TexturedMaterial (src/s3d_texturedmaterial.cpp): a texture of Scene::AddTexture scales
+    // the base colour
+    Material& SetColorMap(int texture) {
+        m.color_map = texture + 1;
+        return *this;
+    }
     static Material Plastic(Color3 diffuse, Color3 specular, float power, Color3 emissive = {}) {
         Material r = make(SALTY_PLASTIC, diffuse, emissive, 1.5f, 0.f);
         r.m.specular[0] = specular.x; r.m.specular[1] = specular.y; r.m.specular[2] = specular.z;
@@ -135,9 +141,43 @@ public:
         for (const Vertex& v : vertices) {
             pos_.insert(pos_.end(), {v.Position.x, v.Position.y, v.Position.z});
             nrm_.insert(nrm_.end(), {v.Normal.x, v.Normal.y, v.Normal.z});
+            uv_.insert(uv_.end(), {v.TexCoord.x, v.TexCoord.y});
         }
         for (size_t i = 0; i < vertices.size() / 3; ++i) mat_.push_back(id);
     }
+    // Mesh::Create(filename) (src/s3d_mesh.cpp:250-465), optionally placed as an Instance by
+    // a row-major 3x4 matrix (normals by its inverse transpose); returns the triangle count.
+    int64_t AddSmd(const char* path, const float* matrix3x4 = nullptr) {
+        salty_mesh* m = nullptr;
+        const salty_status st = salty_mesh_load_smd(nullptr, path, &m);
+        if (st != SALTY_OK) throw Error(st, std::string("cannot load ") + path);
+        const size_t n = (size_t)m->n_tris, p0 = pos_.size();
+        pos_.resize(p0 + n * 9);
+        nrm_.resize(p0 + n * 9);
+        if (matrix3x4) {
+            salty_mesh_transform(matrix3x4, m->n_tris, m->tri_pos, m->tri_nrm, pos_.data() + p0, nrm_.data() + p0);
+        } else {
+            std::copy(m->tri_pos, m->tri_pos + n * 9, pos_.begin() + p0);
+            std::copy(m->tri_nrm, m->tri_nrm + n * 9, nrm_.begin() + p0);
+        }
+        uv_.insert(uv_.end(), m->tri_uv, m->tri_uv + n * 6);
+        const int base = (int)mats_.size();
+        mats_.insert(mats_.end(), m->mats, m->mats + m->n_mats);
+        for (size_t t = 0; t < n; ++t) mat_.push_back(base + m->tri_mat[t]);
+        salty_mesh_free(m);
+        return (int64_t)n;
+    }
+    // Texture (src/s3d_texture.cpp): float RGB, texel (x, y) at rgb[3 * (y * width + x)];
+    // returns its index for Material::SetColorMap and SetEnvironment.
+    int AddTexture(int width, int height, std::vector<float> rgb) {
+        if (width <= 0 || height <= 0 || rgb.size() != (size_t)width * height * 3)
+            throw Error(SALTY_ERR_INVALID_ARG, "AddTexture: size does not match the texels");
+        tex_data_.push_back(std::move(rgb));
+        tex_.push_back(salty_texture{width, height, nullptr});
+        return (int)tex_.size() - 1;
+    }
+    // Scene::SampleIBL with a latitude-longitude texture (radiance = texel * scale)
+    void SetEnvironment(int texture, float scale = 10.0f) { ibl_ = texture + 1; ibl_scale_ = scale; }
     void SetQuadLight(Vector3 corner, Vector3 edgeA, Vector3 edgeB, Color3 emission) {
         has_light_ = true;
         light_ = {corner, edgeA, edgeB, emission};
@@ -168,6 +208,12 @@ public:
         d.camera.near_clip = camera_.NearClip;
         d.camera.lens_radius = camera_.LensRadius;
         d.camera.focal_distance = camera_.FocalDistance;
+        d.tri_uv = uv_.data();
+        for (size_t t = 0; t < tex_.size(); ++t) tex_[t].rgb = tex_data_[t].data();
+        d.textures = tex_.data();
+        d.n_textures = (int32_t)tex_.size();
+        d.ibl_map = ibl_;
+        d.ibl_scale = ibl_scale_;
         return d;
     }
 
@@ -175,9 +221,13 @@ private:
     static void put(float* d, Vector3 v) { d[0] = v.x; d[1] = v.y; d[2] = v.z; }
     struct Light { Vector3 corner, a, b; Color3 e; } light_{};
     struct Sun { Vector3 dir; Color3 e; } sun_{};
-    std::vector<float> pos_, nrm_;
+    std::vector<float> pos_, nrm_, uv_;
     std::vector<int32_t> mat_;
     std::vector<salty_material> mats_;
+    std::vector<std::vector<float>> tex_data_;
+    mutable std::vector<salty_texture> tex_;
+    int32_t ibl_ = 0;
+    float ibl_scale_ = 10.0f;
     bool has_light_ = false, has_sun_ = false;
     Color3 sky_{};
     PinholeCamera camera_{};

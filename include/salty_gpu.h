@@ -289,6 +289,11 @@ salty_status salty_set_tuning(salty_ctx* ctx, const salty_tuning* t);
  * width (8) and traversal stack depth (from the BVH depth) are fixed by the build. */
 salty_status salty_autotune(salty_ctx* ctx, salty_scene* const* scenes, const salty_render_opts* opts, int32_t n,
                             int32_t trial_spp, salty_tuning* out, float* best_ms);
+/* Picks the traversal launch shape (trace_block with trace_regs as pairs, then trace_pool,
+ * then trace_postpone) for salty_trace of these rays on this scene, timing launches with
+ * CUDA events; sets it on the context.  rays host or device; hits are discarded. */
+salty_status salty_autotune_trace(salty_ctx* ctx, salty_scene* scene, const salty_ray* rays, int64_t n,
+                                  uint32_t flags, salty_tuning* out, float* best_ms);
 
 /* Film sums as stored (W*H*3 each): FP32 sum + Kahan compensation, or FP64 sums when the
  * film was rendered with fp64.  Arrays host or device; NULL skips. */

@@ -116,7 +116,7 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_unet_param_count", "salty_unet_get_params", "salty_unet_set_params", "salty_unet_forward",
            "salty_unet_train_step", "salty_scene_set_camera", "salty_denoise_unet", "salty_render_batch",
            "salty_get_tuning", "salty_set_tuning", "salty_autotune", "salty_mesh_load_smd", "salty_mesh_free",
-           "salty_mesh_transform"]
+           "salty_mesh_transform", "salty_autotune_trace"]
 
 _lib = None
 
@@ -168,6 +168,7 @@ def lib() -> C.CDLL:
         "salty_get_tuning": (i32, [vp, C.POINTER(Tuning)]),
         "salty_set_tuning": (i32, [vp, C.POINTER(Tuning)]),
         "salty_autotune": (i32, [vp, vp, vp, i32, i32, C.POINTER(Tuning), C.POINTER(f32)]),
+        "salty_autotune_trace": (i32, [vp, vp, vp, i64, u32, C.POINTER(Tuning), C.POINTER(f32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -486,6 +487,16 @@ class Scene:
         s = TraceStats()
         lib().salty_last_trace_stats(self.ctx.h, C.byref(s))
         return {k: getattr(s, k) for k, _ in TraceStats._fields_}
+
+    def autotune_trace(self, rays, any_hit=False, watertight=False) -> tuple[dict, float]:
+        """salty_autotune_trace: the fastest traversal launch shape for these rays (set on the
+        context); returns it and its launch time in ms."""
+        n = rays.shape[0]
+        flags = (TRACE_ANY_HIT if any_hit else 0) | (TRACE_WATERTIGHT if watertight else 0)
+        t, ms = Tuning(), C.c_float()
+        self.ctx.check(lib().salty_autotune_trace(self.ctx.h, self.h, _ptr(rays), n, flags, C.byref(t), C.byref(ms)),
+                       "autotune_trace")
+        return t.as_dict(), ms.value
 
     def trace(self, rays: np.ndarray, any_hit=False, watertight=False, counters=False) -> TraceResult:
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)

@@ -600,6 +600,83 @@ salty_status salty_set_tuning(salty_ctx* ctx, const salty_tuning* t) {
     return SALTY_OK;
 }
 
+salty_status salty_autotune_trace(salty_ctx* ctx, salty_scene* sc, const salty_ray* rays, int64_t n, uint32_t flags,
+                                  salty_tuning* out, float* best_ms) {
+    using namespace salty;
+    if (!ctx) return SALTY_ERR_INVALID_ARG;
+    auto& E = ctx->err;
+    if (!sc || !rays || n <= 0) return E.fail(SALTY_ERR_INVALID_ARG, "null scene or no rays");
+    if (flags & ~(uint32_t)(SALTY_TRACE_ANY_HIT | SALTY_TRACE_WATERTIGHT))
+        return E.fail(SALTY_ERR_INVALID_ARG, "unknown trace flags 0x%x", flags);
+    if (!sc->bvh.built) return E.fail(SALTY_ERR_NOT_BUILT, "salty_bvh_build has not been called");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    const float4* d_rays = reinterpret_cast<const float4*>(rays);
+    DevBuf<float4> copy;
+    if (!is_device_ptr(rays) || (uintptr_t)rays % 16) {
+        SALTY_TRY_CUDA(E, copy.ensure((size_t)n * 2));
+        SALTY_TRY_CUDA(E, cudaMemcpyAsync(copy.p, rays, (size_t)n * sizeof(salty_ray), cudaMemcpyDefault, st));
+        d_rays = copy.p;
+    }
+    DevBuf<float4> hits;
+    SALTY_TRY_CUDA(E, hits.ensure((size_t)n));
+    // time of one launch under a tuning: the better of two, after one untimed
+    auto time_of = [&](const TraceTuning& t, float* ms) -> salty_status {
+        float best = 1e30f;
+        for (int r = 0; r < 3; ++r) {
+            SALTY_TRY_CUDA(E, cudaEventRecord(ctx->ev[3], st));
+            SALTY_TRY(trace_launch(ctx, sc, d_rays, n, nullptr, flags, hits.p, ctx->counters.p, st, ctx->status.p));
+            SALTY_TRY_CUDA(E, cudaEventRecord(ctx->ev[4], st));
+            SALTY_TRY_CUDA(E, cudaEventSynchronize(ctx->ev[4]));
+            float m = 0;
+            cudaEventElapsedTime(&m, ctx->ev[3], ctx->ev[4]);
+            if (r > 0) best = std::min(best, m);
+        }
+        (void)t;
+        *ms = best;
+        return SALTY_OK;
+    };
+    const TraceTuning start = ctx->tune.trace;
+    TraceTuning best = start;
+    float best_t = 0;
+    salty_status s = time_of(best, &best_t);
+    const int block_regs[][2] = {{64, 64}, {128, 64}, {256, 64}, {64, 48}, {128, 48}, {256, 48}};
+    const int pool[] = {64, 128, 256};
+    const int postpone[] = {1, 4, 7, 10};
+    auto consider = [&](TraceTuning t) -> salty_status {
+        ctx->tune.trace = t;
+        float ms = 0;
+        SALTY_TRY(time_of(t, &ms));
+        if (ms < best_t * 0.995f) { best_t = ms; best = t; }
+        return SALTY_OK;
+    };
+    for (auto& br : block_regs) {
+        if (s != SALTY_OK) break;
+        TraceTuning t = best;
+        t.block = br[0];
+        t.regs = br[1];
+        if (t.block != best.block || t.regs != best.regs) s = consider(t);
+    }
+    for (int v : pool) {
+        if (s != SALTY_OK) break;
+        TraceTuning t = best;
+        t.pool = v;
+        if (v != best.pool) s = consider(t);
+    }
+    for (int v : postpone) {
+        if (s != SALTY_OK) break;
+        TraceTuning t = best;
+        t.postpone = v;
+        if (v != best.postpone) s = consider(t);
+    }
+    ctx->tune.trace = s == SALTY_OK ? best : start;
+    if (s != SALTY_OK) return s;
+    int status = 0;
+    SALTY_TRY_CUDA(E, cudaMemcpy(&status, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (best_ms) *best_ms = best_t;
+    return out ? salty_get_tuning(ctx, out) : SALTY_OK;
+}
+
 salty_status salty_autotune(salty_ctx* ctx, salty_scene* const* scenes, const salty_render_opts* opts, int32_t n,
                             int32_t trial_spp, salty_tuning* out, float* best_ms) {
     using namespace salty;
@@ -639,9 +716,10 @@ salty_status salty_autotune(salty_ctx* ctx, salty_scene* const* scenes, const sa
     // coordinate descent, one pass over the knobs
     const long long waves[] = {1ll << 20, 1ll << 21, 1ll << 22, 1ll << 23};
     const int shade[] = {128, 256, 512};
-    const int tblock[] = {64, 128, 256};
+    // traversal block size and register budget interact (registers x threads x blocks per
+    // SM against the shared stack), so they are searched as pairs
+    const int block_regs[][2] = {{64, 64}, {128, 64}, {256, 64}, {64, 48}, {128, 48}, {256, 48}};
     const int pool[] = {64, 128, 256};
-    const int regs[] = {64, 48};
     const int postpone[] = {1, 4, 7, 10};
     auto try_knob = [&](auto set, const auto& values) -> salty_status {
         for (auto v : values) {
@@ -664,11 +742,12 @@ salty_status salty_autotune(salty_ctx* ctx, salty_scene* const* scenes, const sa
         s = try_knob([&](Tuning& t, int v) { if (v == best.shade_block) return false; t.shade_block = v; return true; },
                      shade);
     if (s == SALTY_OK)
-        s = try_knob([&](Tuning& t, int v) { if (v == best.trace.block) return false; t.trace.block = v; return true; },
-                     tblock);
-    if (s == SALTY_OK)
-        s = try_knob([&](Tuning& t, int v) { if (v == best.trace.regs) return false; t.trace.regs = v; return true; },
-                     regs);
+        s = try_knob([&](Tuning& t, const int* v) {
+                if (v[0] == best.trace.block && v[1] == best.trace.regs) return false;
+                t.trace.block = v[0];
+                t.trace.regs = v[1];
+                return true;
+            }, block_regs);
     if (s == SALTY_OK)
         s = try_knob([&](Tuning& t, int v) { if (v == best.trace.pool) return false; t.trace.pool = v; return true; },
                      pool);

@@ -60,6 +60,19 @@ __device__ __forceinline__ void ldmatrix_x4_trans(unsigned (&r)[4], const void* 
 // wt:  [9][wrows][Cin] BF16 (tap-major, input channel contiguous); output channel co reads row co
 // out: [N][H][W][out_cs] BF16 at channel offset out_co (channels co < Cout written)
 // NT n8-tiles per CTA; blockIdx.y selects output channels [blockIdx.y*NT*8, +NT*8).
+// Shared memory: the 18x10-pixel halo tile, then one tap's weight slice [NT*8][Cin], both
+// with rows padded by 8 halves so the 8 row addresses of an ldmatrix fall in distinct banks.
+// Per 16-channel k-step a warp issues 2 ldmatrix.x4 for A (its two 16-pixel rows), NT/2
+// ldmatrix.x4 for B and 2*NT mma.
+__device__ __forceinline__ void ldmatrix_x4(unsigned (&r)[4], const void* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void ldmatrix_x2(unsigned& r0, unsigned& r1, const void* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(smem_addr(p)));
+}
+
 template <int NT>
 __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const bf16* __restrict__ in, int in_cs, int Cin,
                                                           const bf16* __restrict__ wt, const float* __restrict__ bias,
@@ -67,7 +80,8 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const bf16* __restrict
                                                           int N, int H, int W, int relu) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     bf16* tile = reinterpret_cast<bf16*>(smem_raw);
-    const int stride = Cin + 8;  // halves per halo pixel (conflict-free fragment loads)
+    const int stride = Cin + 8;  // halves per halo pixel and per weight row
+    bf16* wsm = tile + kHaloX * kHaloY * stride;
     const int tiles_x = (W + kTileX - 1) / kTileX, tiles_y = (H + kTileY - 1) / kTileY;
     int t = blockIdx.x;
     const int tx = t % tiles_x;
@@ -85,10 +99,11 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const bf16* __restrict
             v = *reinterpret_cast<const uint4*>(in + (((size_t)n * H + gy) * W + gx) * in_cs + c * 8);
         *reinterpret_cast<uint4*>(tile + pix * stride + c * 8) = v;
     }
-    __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, tq = lane & 3;
     const int co_base = blockIdx.y * NT * 8;
+    // ldmatrix lane roles: matrix lane >> 3, row lane & 7
+    const int lm = lane >> 3, lr = lane & 7;
     float acc[2][NT][4];
 #pragma unroll
     for (int m = 0; m < 2; ++m)
@@ -96,28 +111,37 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const bf16* __restrict
         for (int j = 0; j < NT; ++j)
 #pragma unroll
             for (int k = 0; k < 4; ++k) acc[m][j][k] = 0.0f;
-    const int wrows_stride = Cin;  // halves per weight row
     for (int tap = 0; tap < 9; ++tap) {
         const int ky = tap / 3, kx = tap % 3;
-        const bf16* wtap = wt + (size_t)tap * gridDim.y * NT * 8 * wrows_stride;
+        // this tap's weight rows [co_base, co_base + NT*8)
+        __syncthreads();  // the previous tap's reads of wsm are done (and, for tap 0, the halo is in)
+        const bf16* wtap = wt + ((size_t)tap * gridDim.y * NT * 8 + co_base) * Cin;
+        for (int i = threadIdx.x; i < NT * 8 * chunks; i += kConvThreads) {
+            const int r = i / chunks, c = i % chunks;
+            *reinterpret_cast<uint4*>(wsm + r * stride + c * 8) =
+                __ldg(reinterpret_cast<const uint4*>(wtap + (size_t)r * Cin + c * 8));
+        }
+        __syncthreads();
         for (int cb = 0; cb < Cin; cb += 16) {
+            // B: n-tiles j, j+1 from one x4 (matrices: rows n, k 0-7 | n, k 8-15 | n+8, k 0-7 | n+8, k 8-15)
             unsigned b[NT][2];
 #pragma unroll
-            for (int j = 0; j < NT; ++j) {
-                const bf16* wr = wtap + (size_t)(co_base + j * 8 + g) * wrows_stride + cb + 2 * tq;
-                b[j][0] = __ldg(reinterpret_cast<const unsigned*>(wr));
-                b[j][1] = __ldg(reinterpret_cast<const unsigned*>(wr + 8));
+            for (int j = 0; j + 1 < NT; j += 2) {
+                unsigned r4[4];
+                ldmatrix_x4(r4, wsm + ((j + (lm >> 1)) * 8 + lr) * stride + cb + (lm & 1) * 8);
+                b[j][0] = r4[0];
+                b[j][1] = r4[1];
+                b[j + 1][0] = r4[2];
+                b[j + 1][1] = r4[3];
             }
+            if (NT & 1) ldmatrix_x2(b[NT - 1][0], b[NT - 1][1], wsm + ((NT - 1) * 8 + lr) * stride + cb + (lm & 1) * 8);
 #pragma unroll
             for (int m = 0; m < 2; ++m) {
-                const int row = 2 * warp + m;  // tile row handled by this m16 tile
-                const bf16* p0 = tile + ((row + ky) * kHaloX + (g + kx)) * stride + cb + 2 * tq;
-                const bf16* p1 = p0 + 8 * stride;  // pixel g + 8
+                // A: the 16 pixels of tile row 2*warp + m (matrices: px 0-7, k 0-7 | px 8-15, k 0-7 |
+                // px 0-7, k 8-15 | px 8-15, k 8-15)
+                const int row = 2 * warp + m;
                 unsigned a[4];
-                a[0] = *reinterpret_cast<const unsigned*>(p0);
-                a[1] = *reinterpret_cast<const unsigned*>(p1);
-                a[2] = *reinterpret_cast<const unsigned*>(p0 + 8);
-                a[3] = *reinterpret_cast<const unsigned*>(p1 + 8);
+                ldmatrix_x4(a, tile + ((row + ky) * kHaloX + lr + (lm & 1) * 8 + kx) * stride + cb + (lm >> 1) * 8);
 #pragma unroll
                 for (int j = 0; j < NT; ++j) mma_bf16(acc[m][j], a, b[j][0], b[j][1]);
             }
@@ -572,7 +596,7 @@ salty_status launch_conv(salty_ctx* ctx, const bf16* in, int in_cs, int cin, con
                          const float* bias, bf16* out, int out_cs, int cout, int N, int H, int W, int relu) {
     const int tiles = N * ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
     dim3 grid(tiles, rows / (nt * 8));
-    const size_t smem = (size_t)kHaloX * kHaloY * (cin + 8) * sizeof(bf16);
+    const size_t smem = ((size_t)kHaloX * kHaloY + (size_t)nt * 8) * (cin + 8) * sizeof(bf16);
 #define SALTY_CONV_CASE(NTV)                                                                                         \
     case NTV: {                                                                                                     \
         SALTY_TRY_CUDA(ctx->err,                                                                                    \

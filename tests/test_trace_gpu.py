@@ -210,3 +210,19 @@ def test_errors_are_reported_not_crashing(ctx):
     assert e.value.status == salty_gb300.ERR_INVALID_ARG
     with pytest.raises(salty_gb300.SaltyError):
         ctx.upload_scene(np.zeros((0, 9), np.float32))
+
+
+def test_autotune_trace_keeps_results(ctx, gpu_soup_1m):
+    """Every traversal launch shape gives the same hits; the autotuner picks one of them."""
+    import torch
+    import salty_gb300
+    rays = torch.from_numpy(salty_gb300.microbench_rays(20260002, 1 << 20, 1e-4)).cuda()
+    hits = torch.empty((1 << 20, 4), device="cuda")
+    default = ctx.tuning
+    gpu_soup_1m.trace_raw(rays, hits)
+    ref = hits.cpu().numpy().view(np.int32).copy()
+    t, ms = gpu_soup_1m.autotune_trace(rays)
+    assert ms > 0 and t == ctx.tuning and t["trace_block"] in (64, 128, 256) and t["trace_regs"] in (48, 64)
+    gpu_soup_1m.trace_raw(rays, hits)
+    np.testing.assert_array_equal(hits.cpu().numpy().view(np.int32), ref)
+    ctx.tuning = default
