@@ -38,11 +38,12 @@ SOUP_SEED, RAY_SEED = 20260001, 20260002
 TMIN = 1e-4
 METRIC = "Mrays/s"
 CPU_SAMPLE = 4_194_304      # rays of the same stream timed on the host cores (~10 s of CPU work)
-# DRAM bytes (read + write) per ray of the closest-hit k_trace launch, from the ncu capture
-# of the same kernel on the same soup at 4,194,304 rays (profiles/trace_closest_soup1m_4Mrays.md);
-# rays in and hits out dominate and scale with the ray count, so traffic per launch is this
-# figure times the rays of the launch.
-NCU_DRAM_BYTES_PER_RAY = (485.8e6 + 69.9e6) / 4_194_304
+# DRAM bytes (read + write) per ray of the closest-hit k_trace launch in the shape the
+# traversal autotuner picks (256 threads, 48 registers), from the ncu capture of that
+# kernel on the same soup at 4,194,304 rays (profiles/trace_closest_soup1m_4Mrays.md); the
+# traffic (rays in, hits out, L2 misses) scales with the ray count, so traffic per launch is
+# this figure times the rays of the launch.
+NCU_DRAM_BYTES_PER_RAY = (723.864064e6 + 80.84608e6) / 4_194_304
 
 
 def measured_peaks() -> dict:
@@ -162,7 +163,7 @@ def run_reference(args, ws, rank, local, pg):
         return
     import salty_gb300
     tris = salty_gb300.microbench_soup(SOUP_SEED, N_TRIS)
-    sample = 16384
+    sample = 524_288  # ~1 s per step on 16 host threads: the default run stays within a minute
     rays = salty_gb300.microbench_rays(RAY_SEED, sample, TMIN)
     from oracle.oracle import Oracle, build
     build(with_reference=False)
@@ -353,6 +354,7 @@ def main():
     ap.add_argument("--any-hit", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (smaller cases for profiling)")
+    ap.add_argument("--trace-shape", default="", help="block,regs,pool,postpone instead of salty_autotune_trace")
     ap.add_argument("--workload", default="traversal", choices=["traversal", "time-to-rmse", "batch"])
     ap.add_argument("--scenes", type=int, default=256, help="batch: number of scenes")
     ap.add_argument("--target", type=float, default=0.01, help="time-to-rmse: relRMSE target")
@@ -391,9 +393,14 @@ def main():
     torch.cuda.synchronize()  # the library runs on its own stream
     any_hit = args.any_hit
 
-    # launch shape for this workload (salty_autotune_trace, untimed)
+    # launch shape for this workload: salty_autotune_trace (untimed), or given
     default_tuning = ctx.tuning
-    tuning, tune_ms = scene.autotune_trace(d_rays, any_hit=any_hit)
+    if args.trace_shape:
+        b_, r_, p_, q_ = (int(x) for x in args.trace_shape.split(","))
+        ctx.tuning = {"trace_block": b_, "trace_regs": r_, "trace_pool": p_, "trace_postpone": q_}
+        tuning = ctx.tuning
+    else:
+        tuning, tune_ms = scene.autotune_trace(d_rays, any_hit=any_hit)
 
     # fetch counts (untimed): algorithmic bytes per ray
     st = scene.trace_raw(d_rays, d_hits, any_hit=any_hit, counters=True)

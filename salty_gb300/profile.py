@@ -1,0 +1,92 @@
+"""Small fixed workloads for profiling the kernels (run them under ncu or alone).
+
+    python -m salty_gb300.profile render [--spp 1] [--frames 2]   1080p heightfield frames
+    python -m salty_gb300.profile unet [--n 1 --h 1088 --w 1920]     one denoiser forward pass
+    python -m salty_gb300.profile trace-sweep                        traversal launch shapes
+
+`render` and `unet` print one line of timings; `trace-sweep` times every traversal launch
+shape (block size x register budget x pool x postpone) on the 1M-triangle microbenchmark
+soup with 16,777,216 rays and checks that all give the same hits.
+"""
+from __future__ import annotations
+
+import argparse
+import itertools
+import json
+import time
+
+import numpy as np
+
+from . import Context, Unet, UNET_FEATURES, microbench_rays, microbench_soup
+from . import scenes
+
+
+def render(spp: int, frames: int) -> dict:
+    ctx = Context(0)
+    s = scenes.upload(ctx, scenes.heightfield())
+    info = s.build()
+    out = []
+    for i in range(frames):
+        r = s.render(1920, 1080, spp, 12, seed=3 + i, want=())
+        out.append({"ms": r["ms"], "rays": r["rays"], "paths": r["paths"]})
+    return {"workload": f"1080p heightfield, {spp} spp x {frames} frames", "bvh_build_ms": info["build_ms"],
+            "frames": out}
+
+
+def unet(n: int, h: int, w: int) -> dict:
+    import torch
+    ctx = Context(0)
+    net = Unet(ctx, seed=1)
+    f = torch.rand((n, h, w, UNET_FEATURES), device="cuda")
+    o = torch.empty((n, h, w, 3), device="cuda")
+    net.forward(f, out=o)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net.forward(f, out=o)
+    torch.cuda.synchronize()
+    return {"workload": f"U-Net forward {n}x{h}x{w}", "ms": (time.perf_counter() - t0) * 1e3}
+
+
+def trace_sweep() -> dict:
+    import torch
+    ctx = Context(0)
+    sc = ctx.upload_scene(microbench_soup(20260001, 1_000_000))
+    sc.build()
+    n = 16_777_216
+    rays = torch.from_numpy(microbench_rays(20260002, n, 1e-4)).cuda()
+    hits = torch.empty((n, 4), device="cuda")
+    ref, res = None, []
+    for blk, regs, pool, post in itertools.product((64, 128, 256), (64, 48), (64, 128, 256), (1, 4, 7, 10)):
+        ctx.tuning = {"trace_block": blk, "trace_regs": regs, "trace_pool": pool, "trace_postpone": post}
+        for _ in range(2):
+            sc.trace_raw(rays, hits)
+        ms = min(sc.trace_raw(rays, hits)["kernel_ms"] for _ in range(4))
+        ids = hits.cpu().numpy().view(np.int32)[:, 1]
+        if ref is None:
+            ref = ids.copy()
+        res.append({"ms": ms, "Mrays_s": n / ms / 1e3, "trace_block": blk, "trace_regs": regs, "trace_pool": pool,
+                    "trace_postpone": post, "same_hits": bool(np.array_equal(ids, ref))})
+    res.sort(key=lambda r: r["ms"])
+    return {"workload": "traversal microbenchmark, 1M triangles, 16,777,216 rays, closest hit", "shapes": res}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("what", choices=["render", "unet", "trace-sweep"])
+    ap.add_argument("--spp", type=int, default=1)
+    ap.add_argument("--frames", type=int, default=2)
+    ap.add_argument("--n", type=int, default=1)
+    ap.add_argument("--h", type=int, default=1088)
+    ap.add_argument("--w", type=int, default=1920)
+    a = ap.parse_args(argv)
+    if a.what == "render":
+        r = render(a.spp, a.frames)
+    elif a.what == "unet":
+        r = unet(a.n, a.h, a.w)
+    else:
+        r = trace_sweep()
+    print(json.dumps(r))
+
+
+if __name__ == "__main__":
+    main()
