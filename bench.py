@@ -251,7 +251,7 @@ def run_time_to_rmse(args):
                    "n_tris": int(sc["tri_pos"].shape[0]), "bvh_nodes": info["n_nodes"], "bvh_build_ms": info["build_ms"],
                    "window": crop, "ref_spp": args.ref_spp, "ref_noise_rel_mse": ref["noise"],
                    "ref_seconds": ref["seconds"], "setup_seconds": setup_s,
-                   "denoiser": {"method": den.method, "hq_from_spp": den.hq_from_spp,
+                   "denoiser": {"method": den.method, "hq_from_spp": den.hq_from_spp, "mirrors": den.mirrors,
                                 "weights": {k: v for k, v in den.meta.items() if k != "scenes"},
                                 "hq_weights": {k: v for k, v in den.hq_meta.items() if k != "scenes"}},
                    "tuning_plain": default, "tuning_denoised": tuned, "autotune_seconds": tune_s,

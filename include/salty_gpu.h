@@ -380,6 +380,11 @@ salty_status salty_unet_train_step(salty_ctx* ctx, salty_unet* net, const float*
  * multiples of 16) -> network.  out_rgb: film width * height * 3 floats, host or device.
  * NLM (salty_denoise_nlm) is the fallback where no trained weights exist. */
 salty_status salty_denoise_unet(salty_ctx* ctx, salty_unet* net, salty_scene* scene, float* out_rgb);
+/* The same, averaged over `mirrors` mirror images of the frame (1: as salty_denoise_unet;
+ * 2: also left-right; 4: also top-bottom and both) -- a self-ensemble that lowers the
+ * network's own error at the cost of `mirrors` forward passes. */
+salty_status salty_denoise_unet_ensemble(salty_ctx* ctx, salty_unet* net, salty_scene* scene, int32_t mirrors,
+                                        float* out_rgb);
 
 /* ---------------------------------------------------------------- inputs */
 /* The traversal microbenchmark's seeded inputs (host arrays): a triangle soup with

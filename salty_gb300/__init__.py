@@ -116,7 +116,7 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_unet_param_count", "salty_unet_get_params", "salty_unet_set_params", "salty_unet_forward",
            "salty_unet_train_step", "salty_scene_set_camera", "salty_denoise_unet", "salty_render_batch",
            "salty_get_tuning", "salty_set_tuning", "salty_autotune", "salty_mesh_load_smd", "salty_mesh_free",
-           "salty_mesh_transform", "salty_autotune_trace"]
+           "salty_mesh_transform", "salty_autotune_trace", "salty_denoise_unet_ensemble"]
 
 _lib = None
 
@@ -161,6 +161,7 @@ def lib() -> C.CDLL:
         "salty_unet_forward": (i32, [vp, vp, vp, i32, i32, i32, vp]),
         "salty_unet_train_step": (i32, [vp, vp, vp, vp, i32, i32, i32, f32, C.POINTER(f32)]),
         "salty_denoise_unet": (i32, [vp, vp, vp, vp]),
+        "salty_denoise_unet_ensemble": (i32, [vp, vp, vp, i32, vp]),
         "salty_render_batch": (i32, [vp, vp, vp, i32, C.POINTER(RenderStats)]),
         "salty_mesh_load_smd": (i32, [vp, C.c_char_p, C.POINTER(C.POINTER(Mesh))]),
         "salty_mesh_free": (None, [C.POINTER(Mesh)]),
@@ -631,12 +632,14 @@ class Unet:
         self.ctx.check(lib().salty_unet_forward(self.ctx.h, self.h, _ptr(f), n, h, w, _ptr(out)), "unet_forward")
         return out[0] if features.ndim == 3 and isinstance(out, np.ndarray) else out
 
-    def denoise_film(self, scene: "Scene", out=None):
-        """Denoised image of the scene's film (H, W, 3), computed on the device."""
+    def denoise_film(self, scene: "Scene", out=None, mirrors: int = 1):
+        """Denoised image of the scene's film (H, W, 3), computed on the device; mirrors > 1
+        averages the network over mirror images of the frame (salty_denoise_unet_ensemble)."""
         h, w = scene.film_shape
         if out is None:
             out = np.empty((h, w, 3), np.float32)
-        self.ctx.check(lib().salty_denoise_unet(self.ctx.h, self.h, scene.h, _ptr(out)), "denoise_unet")
+        self.ctx.check(lib().salty_denoise_unet_ensemble(self.ctx.h, self.h, scene.h, mirrors, _ptr(out)),
+                       "denoise_unet")
         return out
 
     def train_step(self, features, target, lr: float) -> float:

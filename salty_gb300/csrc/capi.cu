@@ -611,6 +611,7 @@ salty_status salty_autotune_trace(salty_ctx* ctx, salty_scene* sc, const salty_r
     if (!sc->bvh.built) return E.fail(SALTY_ERR_NOT_BUILT, "salty_bvh_build has not been called");
     cudaSetDevice(ctx->device);
     cudaStream_t st = ctx->stream;
+    SALTY_TRY_CUDA(E, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), st));
     const float4* d_rays = reinterpret_cast<const float4*>(rays);
     DevBuf<float4> copy;
     if (!is_device_ptr(rays) || (uintptr_t)rays % 16) {
@@ -620,8 +621,8 @@ salty_status salty_autotune_trace(salty_ctx* ctx, salty_scene* sc, const salty_r
     }
     DevBuf<float4> hits;
     SALTY_TRY_CUDA(E, hits.ensure((size_t)n));
-    // time of one launch under a tuning: the better of two, after one untimed
-    auto time_of = [&](const TraceTuning& t, float* ms) -> salty_status {
+    // time of one launch under the context's current tuning: the better of two, after one untimed
+    auto time_of = [&](float* ms) -> salty_status {
         float best = 1e30f;
         for (int r = 0; r < 3; ++r) {
             SALTY_TRY_CUDA(E, cudaEventRecord(ctx->ev[3], st));
@@ -632,21 +633,20 @@ salty_status salty_autotune_trace(salty_ctx* ctx, salty_scene* sc, const salty_r
             cudaEventElapsedTime(&m, ctx->ev[3], ctx->ev[4]);
             if (r > 0) best = std::min(best, m);
         }
-        (void)t;
         *ms = best;
         return SALTY_OK;
     };
     const TraceTuning start = ctx->tune.trace;
     TraceTuning best = start;
     float best_t = 0;
-    salty_status s = time_of(best, &best_t);
+    salty_status s = time_of(&best_t);
     const int block_regs[][2] = {{64, 64}, {128, 64}, {256, 64}, {64, 48}, {128, 48}, {256, 48}};
     const int pool[] = {64, 128, 256};
     const int postpone[] = {1, 4, 7, 10};
     auto consider = [&](TraceTuning t) -> salty_status {
         ctx->tune.trace = t;
         float ms = 0;
-        SALTY_TRY(time_of(t, &ms));
+        SALTY_TRY(time_of(&ms));
         if (ms < best_t * 0.995f) { best_t = ms; best = t; }
         return SALTY_OK;
     };
@@ -673,6 +673,7 @@ salty_status salty_autotune_trace(salty_ctx* ctx, salty_scene* sc, const salty_r
     if (s != SALTY_OK) return s;
     int status = 0;
     SALTY_TRY_CUDA(E, cudaMemcpy(&status, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (status) return E.fail(SALTY_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
     if (best_ms) *best_ms = best_t;
     return out ? salty_get_tuning(ctx, out) : SALTY_OK;
 }

@@ -14,17 +14,22 @@
 namespace salty {
 namespace {
 
-// counters: [0] ray cursor, [1] node fetches, [2] triangle fetches.  CAP: ask for
-// 1280 / TB resident blocks, which caps registers at 48 per thread (more warps per SM to
-// hide fetch latency, at the price of a few spilled values).
-template <bool ANY, bool WT, bool COUNT, int DEPTH, int TB, bool CAP>
-__global__ void __launch_bounds__(TB, CAP ? 1280 / TB : 1)
+constexpr int kMaxStack = 63;  // stack entries per thread: BVHs up to 31 levels
+
+// counters: [0] ray cursor, [1] node fetches, [2] triangle fetches.  The register budget
+// is set through the resident blocks asked for: 1024 / TB caps registers at 64 per thread,
+// CAP's 1280 / TB at 48 (more warps per SM to hide fetch latency, at the price of a few
+// spilled values).
+// The short stack lives in dynamic shared memory, `depth` entries per thread (two per BVH
+// level plus one), so shallow trees leave room for more resident blocks.
+template <bool ANY, bool WT, bool COUNT, int TB, bool CAP>
+__global__ void __launch_bounds__(TB, CAP ? 1280 / TB : 1024 / TB)
 k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, const float4* __restrict__ rays,
         const int* __restrict__ roots, long long n_arg, const int* __restrict__ n_dev, float4* __restrict__ hits,
-        unsigned long long* __restrict__ counters, float cull_slack, int pool, int postpone,
+        unsigned long long* __restrict__ counters, float cull_slack, int pool, int postpone, int depth,
         int* __restrict__ status) {
-    __shared__ uint2 sstack[DEPTH * TB];
-    TravStack<DEPTH> st{sstack + threadIdx.x, TB};
+    extern __shared__ uint2 sstack[];
+    TravStack st{sstack + threadIdx.x, TB, depth};
     const int lane = threadIdx.x & 31;
     // queue length from device memory when given (wavefront queues), else the argument
     const long long n = n_dev ? (long long)*n_dev : n_arg;
@@ -62,13 +67,13 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
         }
         const bool active = rid >= 0;
         if (__ballot_sync(0xffffffffu, active) == 0) break;
-        if (active && s.ng_hits) trav_node_step<DEPTH, COUNT>(s, nodes, r, st, cnt, overflow);
+        if (active && s.ng_hits) trav_node_step<COUNT>(s, nodes, r, st, cnt, overflow);
         // Triangle postponing: with too few lanes holding triangles, set the group aside
         // and keep walking nodes with the rest of the warp.
         const bool want = active && s.tg_hits != 0;
         const unsigned want_mask = __ballot_sync(0xffffffffu, want);
         bool run = want;
-        if (want && __popc(want_mask) < postpone && s.ng_hits != 0 && s.sp < DEPTH) {
+        if (want && __popc(want_mask) < postpone && s.ng_hits != 0 && s.sp < depth) {
             st.at(s.sp++) = make_uint2(s.tg_base, s.tg_hits | kTriGroupFlag);
             s.tg_hits = 0;
             run = false;
@@ -103,42 +108,44 @@ struct Launch {
     unsigned long long* counters;
     cudaStream_t st;
     float slack;
-    int pool, postpone;
+    int pool, postpone, depth;
     int* status;
 };
 
-template <bool ANY, bool WT, bool COUNT, int DEPTH, int TB, bool CAP>
+template <bool ANY, bool WT, bool COUNT, int TB, bool CAP>
 salty_status launch(salty_ctx* ctx, const Launch& L) {
-    auto kern = k_trace<ANY, WT, COUNT, DEPTH, TB, CAP>;
+    auto kern = k_trace<ANY, WT, COUNT, TB, CAP>;
+    const size_t smem = (size_t)L.depth * TB * sizeof(uint2);
+    if (smem > 48 * 1024)
+        SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    SALTY_TRY_CUDA(ctx->err, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, 0));
+    SALTY_TRY_CUDA(ctx->err, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, smem));
     if (per_sm < 1) per_sm = 1;
     long long want = (L.n + TB - 1) / TB;
     long long grid = (long long)ctx->num_sms * per_sm;
     if (grid > want) grid = want;
     if (grid < 1) grid = 1;
-    kern<<<(unsigned)grid, TB, 0, L.st>>>(L.tgt.nodes, L.tgt.tris, L.rays, L.tgt.roots, L.n, L.n_dev, L.hits,
-                                          L.counters, L.slack, L.pool, L.postpone, L.status);
+    kern<<<(unsigned)grid, TB, smem, L.st>>>(L.tgt.nodes, L.tgt.tris, L.rays, L.tgt.roots, L.n, L.n_dev, L.hits,
+                                             L.counters, L.slack, L.pool, L.postpone, L.depth, L.status);
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;
 }
 
-template <int DEPTH, int TB, bool CAP>
+template <int TB, bool CAP>
 salty_status dispatch_flags(salty_ctx* ctx, const Launch& L, uint32_t flags) {
     const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT;
 #define SALTY_L(A, W) \
-    if (any == A && wt == W) return launch<A, W, false, DEPTH, TB, CAP>(ctx, L)
+    if (any == A && wt == W) return launch<A, W, false, TB, CAP>(ctx, L)
     SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
 #undef SALTY_L
     return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad trace flags");
 }
 
 // Counting walks (node and triangle fetches) use the default launch shape.
-template <int DEPTH>
 salty_status dispatch_count(salty_ctx* ctx, const Launch& L, uint32_t flags) {
     const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT;
 #define SALTY_L(A, W) \
-    if (any == A && wt == W) return launch<A, W, true, DEPTH, 128, false>(ctx, L)
+    if (any == A && wt == W) return launch<A, W, true, 128, false>(ctx, L)
     SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
 #undef SALTY_L
     return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad trace flags");
@@ -153,27 +160,19 @@ salty_status trace_launch(salty_ctx* ctx, const TraceTarget& tgt, const TraceTun
                           unsigned long long* d_counters, cudaStream_t st, int* d_status) {
     SALTY_TRY_CUDA(ctx->err, cudaMemsetAsync(d_counters, 0, 3 * sizeof(unsigned long long), st));
     const bool wt = flags & SALTY_TRACE_WATERTIGHT;
-    Launch L{tgt, d_rays, n, n_dev, d_hits, d_counters, st, wt ? (1.0f / 65536.0f) : 1e-3f,
-             tune.pool >= 32 ? tune.pool : 32, tune.postpone, d_status};
     // Each BVH level can hold one pending node group and one postponed triangle group.
     const int need = 2 * tgt.depth + 1;
-    if (need > 48) return ctx->err.fail(SALTY_ERR_CAPACITY, "BVH depth %d exceeds the traversal stack (23 levels)",
-                                        tgt.depth);
-    const bool shallow = need <= 24;
-    if (flags & SALTY_TRACE_COUNTERS)
-        return shallow ? dispatch_count<24>(ctx, L, flags) : dispatch_count<48>(ctx, L, flags);
-    // the 48-deep stack of a 256-thread block would not fit the 48 KB of static shared memory
-    const int tb = (!shallow && tune.block > 128) ? 128 : tune.block;
+    if (need > kMaxStack)
+        return ctx->err.fail(SALTY_ERR_CAPACITY, "BVH depth %d exceeds the traversal stack (%d levels)", tgt.depth,
+                             (kMaxStack - 1) / 2);
+    Launch L{tgt, d_rays, n, n_dev, d_hits, d_counters, st, wt ? (1.0f / 65536.0f) : 1e-3f,
+             tune.pool >= 32 ? tune.pool : 32, tune.postpone, need, d_status};
+    if (flags & SALTY_TRACE_COUNTERS) return dispatch_count(ctx, L, flags);
     const bool cap = tune.regs == 48;
-#define SALTY_D(D, B)                                                                                \
-    return cap ? dispatch_flags<D, B, true>(ctx, L, flags) : dispatch_flags<D, B, false>(ctx, L, flags)
-    if (shallow) {
-        if (tb == 64) SALTY_D(24, 64);
-        if (tb == 256) SALTY_D(24, 256);
-        SALTY_D(24, 128);
-    }
-    if (tb == 64) SALTY_D(48, 64);
-    SALTY_D(48, 128);
+#define SALTY_D(B) return cap ? dispatch_flags<B, true>(ctx, L, flags) : dispatch_flags<B, false>(ctx, L, flags)
+    if (tune.block == 64) SALTY_D(64);
+    if (tune.block == 256) SALTY_D(256);
+    SALTY_D(128);
 #undef SALTY_D
 }
 

@@ -17,10 +17,10 @@
 namespace salty {
 
 // Group stack entry: x = child base index, y = (hit bits in key order << 8) | imask.
-template <int DEPTH>
 struct TravStack {
-    uint2* base;    // shared memory, [DEPTH][blockDim]
+    uint2* base;    // shared memory, [depth][blockDim]
     int stride;     // blockDim.x
+    int depth;      // entries per thread
     __device__ __forceinline__ uint2& at(int i) const { return base[i * stride]; }
 };
 
@@ -261,15 +261,15 @@ __device__ __forceinline__ void trav_init(TravState& s, const TravRay& r, unsign
 
 // Visits the nearest pending child of the current node group.  A full stack drops the
 // remaining group and raises `overflow` (reported to the caller as an error).
-template <int DEPTH, bool COUNT>
+template <bool COUNT>
 __device__ __forceinline__ void trav_node_step(TravState& s, const Bvh8Node* __restrict__ nodes, const TravRay& r,
-                                               TravStack<DEPTH> st, TravCount& cnt, int& overflow) {
+                                               TravStack st, TravCount& cnt, int& overflow) {
     const unsigned key = __ffs(s.ng_hits) - 1;
     s.ng_hits &= s.ng_hits - 1;
     const unsigned slot = key ^ r.oct;
     const unsigned idx = s.ng_base + __popc(s.ng_imask & ((1u << slot) - 1u));
     if (s.ng_hits) {
-        if (s.sp < DEPTH) st.at(s.sp++) = make_uint2(s.ng_base, (s.ng_hits << 8) | s.ng_imask);
+        if (s.sp < st.depth) st.at(s.sp++) = make_uint2(s.ng_base, (s.ng_hits << 8) | s.ng_imask);
         else overflow = 1;
     }
     unsigned cb, im, ih, tb, th;
@@ -315,8 +315,7 @@ __device__ __forceinline__ bool trav_tri_step(TravState& s, const float4* __rest
 }
 
 // Makes a group current when both are exhausted.  Returns false when the walk is over.
-template <int DEPTH>
-__device__ __forceinline__ bool trav_pop(TravState& s, TravStack<DEPTH> st) {
+__device__ __forceinline__ bool trav_pop(TravState& s, TravStack st) {
     if (s.ng_hits || s.tg_hits) return true;
     if (s.sp == 0) return false;
     const uint2 e = st.at(--s.sp);

@@ -375,6 +375,23 @@ __global__ void k_loss(const bf16* __restrict__ out, const bf16* __restrict__ x,
     if ((threadIdx.x & 31) == 0) atomicAdd(loss_sum, s);
 }
 
+// One mirrored pass of the self-ensemble: adds weight * (the prediction of pixel (px, py),
+// found at its mirrored place in the Wp-wide padded output) to rgb [H][W][3].
+__global__ void k_output_flipped(const bf16* __restrict__ out, const bf16* __restrict__ x, int W, int H, int Wp,
+                                 int flip, float weight, int first, float* __restrict__ rgb) {
+    const long long total = (long long)W * H;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total; p += (long long)gridDim.x * blockDim.x) {
+        const int px = (int)(p % W), py = (int)(p / W);
+        const int qx = (flip & 1) ? W - 1 - px : px, qy = (flip & 2) ? H - 1 - py : py;
+        const long long q = (long long)qy * Wp + qx;
+        for (int c = 0; c < 3; ++c) {
+            const float v =
+                weight * fmaxf(expm1f(__bfloat162float(out[q * 8 + c]) + __bfloat162float(x[q * 16 + c])), 0.0f);
+            rgb[p * 3 + c] = first ? v : rgb[p * 3 + c] + v;
+        }
+    }
+}
+
 // prediction (input log colour + network correction) -> linear colour
 __global__ void k_output(const bf16* __restrict__ out, const bf16* __restrict__ x, long long npx,
                          float* __restrict__ rgb) {
@@ -474,14 +491,18 @@ __global__ void k_weights_to_bf16(const float* __restrict__ w, int Cout, int Cin
 }
 
 // Film planes (W x H) -> network input (Wp x Hp, multiples of 16) with reflected borders:
-// colour, albedo, normal, 1/(1+t), noise level mean_c sqrt(var_c) / (1 + colour_c).
+// colour, albedo, normal, 1/(1+t), noise level mean_c sqrt(var_c) / (1 + colour_c).  With
+// flip bit 0 (1) the frame is mirrored left-right (top-bottom) first.
 __global__ void k_pack_features(const float* __restrict__ mean, const float* __restrict__ var,
                                 const float* __restrict__ albedo, const float* __restrict__ normal,
-                                const float* __restrict__ depth, int W, int H, int Wp, int Hp, float* __restrict__ f) {
+                                const float* __restrict__ depth, int W, int H, int Wp, int Hp, int flip,
+                                float* __restrict__ f) {
     const long long total = (long long)Wp * Hp;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
         const int x = (int)(i % Wp), y = (int)(i / Wp);
-        const int sx = x < W ? x : max(2 * W - 2 - x, 0), sy = y < H ? y : max(2 * H - 2 - y, 0);
+        int sx = x < W ? x : max(2 * W - 2 - x, 0), sy = y < H ? y : max(2 * H - 2 - y, 0);
+        if (flip & 1) sx = W - 1 - sx;
+        if (flip & 2) sy = H - 1 - sy;
         const long long p = (long long)sy * W + sx;
         float* d = f + i * kFeatures;
         float noise = 0.0f;
@@ -954,9 +975,12 @@ salty_status salty_unet_train_step(salty_ctx* ctx, salty_unet* net, const float*
     return SALTY_OK;
 }
 
-salty_status salty_denoise_unet(salty_ctx* ctx, salty_unet* net, salty_scene* scene, float* out_rgb) {
+salty_status salty_denoise_unet_ensemble(salty_ctx* ctx, salty_unet* net, salty_scene* scene, int32_t mirrors,
+                                        float* out_rgb) {
     using namespace salty;
     if (!ctx || !net || !scene || !out_rgb) return SALTY_ERR_INVALID_ARG;
+    if (mirrors != 1 && mirrors != 2 && mirrors != 4)
+        return ctx->err.fail(SALTY_ERR_INVALID_ARG, "mirrors must be 1, 2 or 4");
     cudaSetDevice(ctx->device);
     Unet& u = net->net;
     const Film& Fm = scene->film;
@@ -965,26 +989,32 @@ salty_status salty_denoise_unet(salty_ctx* ctx, salty_unet* net, salty_scene* sc
     const int Wp = (W + 15) / 16 * 16, Hp = (H + 15) / 16 * 16;
     SALTY_TRY(check_shape(ctx, 1, Hp, Wp));
     const long long npx = (long long)W * H, npp = (long long)Wp * Hp;
-    // [mean 3 | var 3 | albedo 3 | normal 3 | depth 1] per film pixel, then features, then output
-    SALTY_TRY_CUDA(ctx->err, u.film_ws.ensure((size_t)(npx * 13 + npp * (kFeatures + 3))));
+    // [mean 3 | var 3 | albedo 3 | normal 3 | depth 1] per film pixel, then features, then the image
+    SALTY_TRY_CUDA(ctx->err, u.film_ws.ensure((size_t)(npx * 16 + npp * kFeatures)));
     float* mean = u.film_ws.p;
     float* var = mean + npx * 3;
     float* alb = var + npx * 3;
     float* nrm = alb + npx * 3;
     float* dep = nrm + npx * 3;
     float* feat = dep + npx;
-    float* outp = feat + npp * kFeatures;
+    float* img = feat + npp * kFeatures;
     SALTY_TRY(film_features(ctx, scene, mean, var, alb, nrm, dep));
-    k_pack_features<<<gsz(npp), 256, 0, ctx->stream>>>(mean, var, alb, nrm, dep, W, H, Wp, Hp, feat);
-    Fwd F;
-    SALTY_TRY(forward(ctx, u, feat, 1, Hp, Wp, F));
-    k_output<<<gsz(npp), 256, 0, ctx->stream>>>(F.t[T_OUT], F.t[T_X], npp, outp);
+    for (int k = 0; k < mirrors; ++k) {
+        k_pack_features<<<gsz(npp), 256, 0, ctx->stream>>>(mean, var, alb, nrm, dep, W, H, Wp, Hp, k, feat);
+        Fwd F;
+        SALTY_TRY(forward(ctx, u, feat, 1, Hp, Wp, F));
+        k_output_flipped<<<gsz(npx), 256, 0, ctx->stream>>>(F.t[T_OUT], F.t[T_X], W, H, Wp, k, 1.0f / (float)mirrors,
+                                                           k == 0, img);
+    }
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
-    SALTY_TRY_CUDA(ctx->err, cudaMemcpy2DAsync(out_rgb, (size_t)W * 3 * sizeof(float), outp,
-                                               (size_t)Wp * 3 * sizeof(float), (size_t)W * 3 * sizeof(float), H,
-                                               cudaMemcpyDefault, ctx->stream));
+    SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(out_rgb, img, (size_t)npx * 3 * sizeof(float), cudaMemcpyDefault,
+                                             ctx->stream));
     SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(ctx->stream));
     return SALTY_OK;
+}
+
+salty_status salty_denoise_unet(salty_ctx* ctx, salty_unet* net, salty_scene* scene, float* out_rgb) {
+    return salty_denoise_unet_ensemble(ctx, net, scene, 1, out_rgb);
 }
 
 }  // extern "C"

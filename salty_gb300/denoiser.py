@@ -66,8 +66,10 @@ class Denoiser:
     high-spp weights too, films of at least hq_from_spp samples per pixel use those."""
 
     def __init__(self, ctx: Context, weights: str | None = DEFAULT_WEIGHTS, method: str = "auto",
-                 nlm_k: float = 0.45, hq_weights: str | None = DEFAULT_HQ_WEIGHTS, hq_from_spp: int = 1024):
+                 nlm_k: float = 0.45, hq_weights: str | None = DEFAULT_HQ_WEIGHTS, hq_from_spp: int = 1024,
+                 mirrors: int = 4):
         self.ctx = ctx
+        self.mirrors = mirrors  # film denoising averages the network over this many mirror images
         self.nlm_k = nlm_k
         self.net = self.hq = None
         self.meta = self.hq_meta = {}
@@ -105,7 +107,7 @@ class Denoiser:
         when `out` is a device tensor."""
         if self.method == "nlm":
             raise RuntimeError("film denoising needs U-Net weights; use __call__ for NLM")
-        return self.pick(scene.film_samples).denoise_film(scene, out=out)
+        return self.pick(scene.film_samples).denoise_film(scene, out=out, mirrors=self.mirrors)
 
     def close(self):
         for n in (self.net, self.hq):
