@@ -300,6 +300,20 @@ salty_status salty_autotune_trace(salty_ctx* ctx, salty_scene* scene, const salt
 salty_status salty_film_read(salty_ctx* ctx, salty_scene* scene, double* sum, double* sumsq,
                              int64_t* samples);
 
+/* Checkpoint / resume of a progressive render (the reference's dead app saved a BMP every
+ * 29.9 s, src/s3d_app.cpp:491-501; this keeps the estimator's state instead).  Checkpoint:
+ * per-pixel sums and sums of squares (W*H*3 doubles each), the FP32 film's Kahan
+ * compensation (W*H*3 floats; pass NULL for an FP64 film), the first-hit feature sums (W*H*7
+ * floats) and the sample count; any output may be NULL.  Restore: the film takes that state
+ * for the frame/window/precision `opts` describe, and a salty_render with accumulate = 1 and
+ * the same options then continues it exactly as if it had never stopped (comp and aov may be
+ * NULL: zeros). */
+salty_status salty_film_checkpoint(salty_ctx* ctx, salty_scene* scene, double* sum, double* sumsq, float* comp,
+                                   float* aov, int64_t* samples);
+salty_status salty_film_restore(salty_ctx* ctx, salty_scene* scene, const salty_render_opts* opts,
+                                const double* sum, const double* sumsq, const float* comp, const float* aov,
+                                int64_t samples);
+
 /* Mean first-hit features of the film (the learned denoiser's auxiliary inputs): albedo
  * (W*H*3), shading normal facing the camera (W*H*3) and 1/(1 + hit distance) (W*H; 0 where
  * the camera ray escapes).  Arrays host or device; NULL skips. */

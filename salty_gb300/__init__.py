@@ -116,7 +116,8 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_unet_param_count", "salty_unet_get_params", "salty_unet_set_params", "salty_unet_forward",
            "salty_unet_train_step", "salty_scene_set_camera", "salty_denoise_unet", "salty_render_batch",
            "salty_get_tuning", "salty_set_tuning", "salty_autotune", "salty_mesh_load_smd", "salty_mesh_free",
-           "salty_mesh_transform", "salty_autotune_trace", "salty_denoise_unet_ensemble"]
+           "salty_mesh_transform", "salty_autotune_trace", "salty_denoise_unet_ensemble", "salty_film_checkpoint",
+           "salty_film_restore"]
 
 _lib = None
 
@@ -162,6 +163,8 @@ def lib() -> C.CDLL:
         "salty_unet_train_step": (i32, [vp, vp, vp, vp, i32, i32, i32, f32, C.POINTER(f32)]),
         "salty_denoise_unet": (i32, [vp, vp, vp, vp]),
         "salty_denoise_unet_ensemble": (i32, [vp, vp, vp, i32, vp]),
+        "salty_film_checkpoint": (i32, [vp, vp, vp, vp, vp, vp, C.POINTER(i64)]),
+        "salty_film_restore": (i32, [vp, vp, C.POINTER(RenderOpts), vp, vp, vp, vp, i64]),
         "salty_render_batch": (i32, [vp, vp, vp, i32, C.POINTER(RenderStats)]),
         "salty_mesh_load_smd": (i32, [vp, C.c_char_p, C.POINTER(C.POINTER(Mesh))]),
         "salty_mesh_free": (None, [C.POINTER(Mesh)]),
@@ -391,6 +394,11 @@ class Context:
             sc.film_shape = (crop[3], crop[2]) if crop else (o["height"], o["width"])
         return {"ms": st.ms, "samples": st.samples, "rays": st.rays, "paths": st.paths}
 
+    def cancel(self) -> None:
+        """salty_ctx_cancel: a render running on this context (in another thread) stops at its
+        next wave and returns ERR_CANCELLED; the context stays usable."""
+        lib().salty_ctx_cancel(self.h)
+
     @property
     def tuning(self) -> dict:
         t = Tuning()
@@ -550,6 +558,33 @@ class Scene:
         dp = np.empty((height, width), np.float32)
         self.ctx.check(lib().salty_film_aov(self.ctx.h, self.h, _ptr(al), _ptr(nr), _ptr(dp)), "film_aov")
         return {"albedo": al, "normal": nr, "depth": dp}
+
+    def checkpoint(self) -> dict:
+        """salty_film_checkpoint: the film's raw state (numpy arrays) and sample count."""
+        h, w = self.film_shape
+        sum_ = np.empty((h, w, 3), np.float64)
+        sq = np.empty((h, w, 3), np.float64)
+        aov = np.empty((h, w, 7), np.float32)
+        n = C.c_int64()
+        self.ctx.check(lib().salty_film_read(self.ctx.h, self.h, None, None, C.byref(n)), "film_read")
+        # FP32 films also keep their Kahan terms; try with them first
+        comp = np.empty((h, w, 3), np.float32)
+        st = lib().salty_film_checkpoint(self.ctx.h, self.h, _ptr(sum_), _ptr(sq), _ptr(comp), _ptr(aov), C.byref(n))
+        if st:
+            comp = None
+            self.ctx.check(lib().salty_film_checkpoint(self.ctx.h, self.h, _ptr(sum_), _ptr(sq), None, _ptr(aov),
+                                                       C.byref(n)), "film_checkpoint")
+        return {"sum": sum_, "sumsq": sq, "comp": comp, "aov": aov, "samples": n.value, "shape": (h, w)}
+
+    def restore(self, state: dict, width: int, height: int, crop: tuple | None = None, fp64: bool = False,
+                **kw) -> None:
+        """salty_film_restore: the film takes a checkpoint's state for this frame / window."""
+        o = render_opts(width, height, 0, kw.pop("max_depth", 1), fp64=fp64, crop=crop, **kw)
+        self.ctx.check(lib().salty_film_restore(self.ctx.h, self.h, C.byref(o), _ptr(state["sum"]),
+                                                _ptr(state["sumsq"]), _ptr(state.get("comp")), _ptr(state.get("aov")),
+                                                int(state["samples"])), "film_restore")
+        self.film_shape = (crop[3], crop[2]) if crop else (height, width)
+        self.film_samples = int(state["samples"])
 
     def film(self, width: int, height: int):
         s = np.empty((height, width, 3), np.float64)

@@ -1409,6 +1409,59 @@ salty_status film_features(salty_ctx* ctx, salty_scene* sc, float* d_mean, float
 
 }  // namespace salty
 
+// Checkpoint and resume of a progressive film: its raw state out and back in.
+extern "C" salty_status salty_film_checkpoint(salty_ctx* ctx, salty_scene* sc, double* sum, double* sumsq, float* comp,
+                                              float* aov, int64_t* samples) {
+    using namespace salty;
+    if (!ctx) return SALTY_ERR_INVALID_ARG;
+    if (!sc) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "null scene");
+    SALTY_TRY(salty_film_read(ctx, sc, sum, sumsq, samples));
+    const Film& F = sc->film;
+    const long long npx = (long long)F.width * F.height;
+    if (npx == 0) return SALTY_OK;
+    cudaSetDevice(ctx->device);
+    if (comp) {
+        if (F.fp64) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "an FP64 film has no compensation terms");
+        SALTY_TRY_CUDA(ctx->err, cudaMemcpy(comp, F.comp.p, npx * 3 * sizeof(float), cudaMemcpyDefault));
+    }
+    if (aov) SALTY_TRY_CUDA(ctx->err, cudaMemcpy(aov, F.aov.p, npx * 7 * sizeof(float), cudaMemcpyDefault));
+    return SALTY_OK;
+}
+
+extern "C" salty_status salty_film_restore(salty_ctx* ctx, salty_scene* sc, const salty_render_opts* o,
+                                           const double* sum, const double* sumsq, const float* comp, const float* aov,
+                                           int64_t samples) {
+    using namespace salty;
+    if (!ctx) return SALTY_ERR_INVALID_ARG;
+    SALTY_TRY(check_render_opts(ctx, sc, o));
+    if (!sum || !sumsq || samples < 0) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad film state");
+    if (comp && o->fp64) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "an FP64 film has no compensation terms");
+    cudaSetDevice(ctx->device);
+    salty_render_opts fresh = *o;
+    fresh.accumulate = 0;
+    SALTY_TRY(prepare_film(ctx, sc, fresh));  // sizes and zeroes the film as the options say
+    Film& F = sc->film;
+    const long long n = (long long)F.width * F.height * 3;
+    auto put = [&](float* dst32, double* dst64, const double* src) -> salty_status {
+        if (dst64) {
+            SALTY_TRY_CUDA(ctx->err, cudaMemcpy(dst64, src, n * sizeof(double), cudaMemcpyDefault));
+            return SALTY_OK;
+        }
+        std::vector<double> h(n);
+        SALTY_TRY_CUDA(ctx->err, cudaMemcpy(h.data(), src, n * sizeof(double), cudaMemcpyDefault));
+        std::vector<float> hf(h.begin(), h.end());
+        SALTY_TRY_CUDA(ctx->err, cudaMemcpy(dst32, hf.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        return SALTY_OK;
+    };
+    SALTY_TRY(put(F.fp64 ? nullptr : F.sum.p, F.fp64 ? F.sum64.p : nullptr, sum));
+    SALTY_TRY(put(F.fp64 ? nullptr : F.sumsq.p, F.fp64 ? F.sumsq64.p : nullptr, sumsq));
+    if (comp) SALTY_TRY_CUDA(ctx->err, cudaMemcpy(F.comp.p, comp, n * sizeof(float), cudaMemcpyDefault));
+    if (aov) SALTY_TRY_CUDA(ctx->err, cudaMemcpy(F.aov.p, aov, n / 3 * 7 * sizeof(float), cudaMemcpyDefault));
+    SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(ctx->stream));
+    F.samples = samples;
+    return SALTY_OK;
+}
+
 extern "C" salty_status salty_film_read(salty_ctx* ctx, salty_scene* sc, double* sum, double* sumsq,
                                         int64_t* samples) {
     using namespace salty;

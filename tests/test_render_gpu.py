@@ -218,3 +218,54 @@ def test_smd_mesh_instances_match_oracle(ctx, oracle, tmp_path):
     v = np.maximum((sq / spp - m * m) * spp / (spp - 1) / spp, 0)
     frac, zmax = zstats(r["mean"], r["var"], m, v)
     assert frac < 0.015 and zmax < 6, (frac, zmax)
+
+
+@pytest.mark.parametrize("fp64", [False, True])
+def test_checkpoint_resume_continues_exactly(ctx, fp64):
+    """A film checkpointed after one pass and restored into a fresh scene continues with the
+    same random streams and the same sums: identical to never stopping."""
+    from salty_gb300 import scenes
+    desc = scenes.cornell("mixed")
+    a = _gpu_scene(ctx, desc)
+    a.render(40, 30, 8, 8, seed=5, fp64=fp64, want=())
+    state = a.checkpoint()
+    assert state["samples"] == 8 and (state["comp"] is None) == fp64
+    a.render(40, 30, 8, 8, seed=5, fp64=fp64, accumulate=True, want=())
+    want = a.read(40, 30, fp64=fp64)
+    b = _gpu_scene(ctx, desc)
+    b.restore(state, 40, 30, fp64=fp64)
+    b.render(40, 30, 8, 8, seed=5, fp64=fp64, accumulate=True, want=())
+    got = b.read(40, 30, fp64=fp64)
+    np.testing.assert_array_equal(got["mean"], want["mean"])
+    np.testing.assert_array_equal(got["var"], want["var"])
+    np.testing.assert_array_equal(b.aov(40, 30)["albedo"], a.aov(40, 30)["albedo"])
+
+
+def test_cancel_stops_a_render_and_the_context_recovers(ctx):
+    """salty_ctx_cancel from another thread: the render stops between waves with
+    ERR_CANCELLED (a host-side stop, nothing waits on the device), and the next render works."""
+    import threading
+    import time
+    import salty_gb300
+    from salty_gb300 import scenes
+    s = _gpu_scene(ctx, scenes.cornell("baseline"))
+    default = ctx.tuning
+    ctx.tuning = {"wave_paths": 1 << 16}  # many waves: ~4,000 for this render
+    err = {}
+
+    def run():
+        try:
+            s.render(512, 512, 1024, 8, seed=1, want=())
+        except salty_gb300.SaltyError as e:
+            err["status"] = e.status
+
+    th = threading.Thread(target=run)
+    th.start()
+    time.sleep(0.2)
+    ctx.cancel()
+    th.join(timeout=120)
+    ctx.tuning = default
+    assert not th.is_alive()
+    assert err.get("status") == salty_gb300.ERR_CANCELLED, err
+    r = s.render(32, 32, 4, 8, seed=2, want=("mean",))
+    assert np.all(np.isfinite(r["mean"])) and r["samples"] == 4
