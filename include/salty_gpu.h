@@ -380,6 +380,10 @@ int64_t salty_unet_param_count(const salty_unet* net);
 /* Copies the FP32 parameters and/or the gradients of the last train step (either may be NULL). */
 salty_status salty_unet_get_params(salty_ctx* ctx, salty_unet* net, float* params, float* grads);
 salty_status salty_unet_set_params(salty_ctx* ctx, salty_unet* net, const float* params);
+/* The optimiser's state (Adam first and second moments, one float per parameter each, and
+ * the step count), for checkpointing a training run; any output of get may be NULL. */
+salty_status salty_unet_get_adam(salty_ctx* ctx, salty_unet* net, float* m, float* v, int64_t* step);
+salty_status salty_unet_set_adam(salty_ctx* ctx, salty_unet* net, const float* m, const float* v, int64_t step);
 /* Denoised linear RGB, n*h*w*3 floats. */
 salty_status salty_unet_forward(salty_ctx* ctx, salty_unet* net, const float* features, int32_t n, int32_t h,
                                 int32_t w, float* out_rgb);

@@ -117,7 +117,7 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_unet_train_step", "salty_scene_set_camera", "salty_denoise_unet", "salty_render_batch",
            "salty_get_tuning", "salty_set_tuning", "salty_autotune", "salty_mesh_load_smd", "salty_mesh_free",
            "salty_mesh_transform", "salty_autotune_trace", "salty_denoise_unet_ensemble", "salty_film_checkpoint",
-           "salty_film_restore"]
+           "salty_film_restore", "salty_unet_get_adam", "salty_unet_set_adam"]
 
 _lib = None
 
@@ -165,6 +165,8 @@ def lib() -> C.CDLL:
         "salty_denoise_unet_ensemble": (i32, [vp, vp, vp, i32, vp]),
         "salty_film_checkpoint": (i32, [vp, vp, vp, vp, vp, vp, C.POINTER(i64)]),
         "salty_film_restore": (i32, [vp, vp, C.POINTER(RenderOpts), vp, vp, vp, vp, i64]),
+        "salty_unet_get_adam": (i32, [vp, vp, vp, vp, C.POINTER(i64)]),
+        "salty_unet_set_adam": (i32, [vp, vp, vp, vp, i64]),
         "salty_render_batch": (i32, [vp, vp, vp, i32, C.POINTER(RenderStats)]),
         "salty_mesh_load_smd": (i32, [vp, C.c_char_p, C.POINTER(C.POINTER(Mesh))]),
         "salty_mesh_free": (None, [C.POINTER(Mesh)]),
@@ -642,6 +644,19 @@ class Unet:
         g = np.empty(self.n_params, np.float32)
         self.ctx.check(lib().salty_unet_get_params(self.ctx.h, self.h, None, _ptr(g)), "unet_get_params")
         return g
+
+    def adam_state(self) -> dict:
+        m = np.empty(self.n_params, np.float32)
+        v = np.empty(self.n_params, np.float32)
+        step = C.c_int64()
+        self.ctx.check(lib().salty_unet_get_adam(self.ctx.h, self.h, _ptr(m), _ptr(v), C.byref(step)), "unet_get_adam")
+        return {"m": m, "v": v, "step": step.value}
+
+    def set_adam_state(self, st: dict) -> None:
+        m = np.ascontiguousarray(st["m"], np.float32)
+        v = np.ascontiguousarray(st["v"], np.float32)
+        self.ctx.check(lib().salty_unet_set_adam(self.ctx.h, self.h, _ptr(m), _ptr(v), int(st["step"])),
+                       "unet_set_adam")
 
     def set_params(self, p) -> None:
         p = np.ascontiguousarray(p, np.float32)

@@ -907,6 +907,28 @@ salty_status salty_unet_get_params(salty_ctx* ctx, salty_unet* net, float* param
     return SALTY_OK;
 }
 
+salty_status salty_unet_get_adam(salty_ctx* ctx, salty_unet* net, float* m, float* v, int64_t* step) {
+    using namespace salty;
+    if (!ctx || !net) return SALTY_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Unet& u = net->net;
+    if (m) SALTY_TRY_CUDA(ctx->err, cudaMemcpy(m, u.adam_m.p, u.n_params * sizeof(float), cudaMemcpyDefault));
+    if (v) SALTY_TRY_CUDA(ctx->err, cudaMemcpy(v, u.adam_v.p, u.n_params * sizeof(float), cudaMemcpyDefault));
+    if (step) *step = u.step;
+    return SALTY_OK;
+}
+
+salty_status salty_unet_set_adam(salty_ctx* ctx, salty_unet* net, const float* m, const float* v, int64_t step) {
+    using namespace salty;
+    if (!ctx || !net || !m || !v || step < 0) return SALTY_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    Unet& u = net->net;
+    SALTY_TRY_CUDA(ctx->err, cudaMemcpy(u.adam_m.p, m, u.n_params * sizeof(float), cudaMemcpyDefault));
+    SALTY_TRY_CUDA(ctx->err, cudaMemcpy(u.adam_v.p, v, u.n_params * sizeof(float), cudaMemcpyDefault));
+    u.step = step;
+    return SALTY_OK;
+}
+
 salty_status salty_unet_set_params(salty_ctx* ctx, salty_unet* net, const float* params) {
     using namespace salty;
     if (!ctx || !net || !params) return SALTY_ERR_INVALID_ARG;

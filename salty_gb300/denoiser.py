@@ -35,19 +35,27 @@ MAX_DEPTH = 12
 
 
 # ---------------------------------------------------------------- weights
-def save_weights(net: Unet, path: str, meta: dict | None = None) -> None:
+def save_weights(net: Unet, path: str, meta: dict | None = None, optimizer: bool = False) -> None:
+    """Parameters (and, with optimizer=True, the Adam state: a training checkpoint)."""
     from . import UNET_LAYERS
     os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    extra = {}
+    if optimizer:
+        st = net.adam_state()
+        extra = {"adam_m": st["m"], "adam_v": st["v"], "adam_step": np.array(st["step"])}
     np.savez_compressed(path, params=net.params(), layers=np.array(UNET_LAYERS, np.int32),
-                        meta=np.array(json.dumps(meta or {})))
+                        meta=np.array(json.dumps(meta or {})), **extra)
 
 
 def load_weights(net: Unet, path: str) -> dict:
+    """Parameters, and the Adam state when the file is a training checkpoint."""
     from . import UNET_LAYERS
     z = np.load(path)
     if not np.array_equal(z["layers"], np.array(UNET_LAYERS, np.int32)):
         raise ValueError(f"{path} holds weights of another architecture")
     net.set_params(z["params"])
+    if "adam_m" in z:
+        net.set_adam_state({"m": z["adam_m"], "v": z["adam_v"], "step": int(z["adam_step"])})
     return json.loads(str(z["meta"]))
 
 

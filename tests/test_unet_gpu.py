@@ -114,3 +114,34 @@ def test_rejects_bad_shapes(net):
         net.forward(np.zeros((1, 20, 16, 11), np.float32))
     with pytest.raises(ValueError):
         net.train_step(f, t[:, :8], lr=0.0)
+
+
+def test_training_checkpoint_resumes_exactly(ctx, tmp_path):
+    """Parameters + Adam state saved mid-training and loaded into a new network: the next
+    steps give the parameters of an uninterrupted run."""
+    import salty_gb300
+    from salty_gb300 import denoiser as dn
+    f, t = _batch(7, n=2, h=32, w=32)
+    a = salty_gb300.Unet(ctx, seed=8)
+    for _ in range(3):
+        a.train_step(f, t, lr=1e-3)
+    p = str(tmp_path / "ckpt.npz")
+    dn.save_weights(a, p, optimizer=True)
+    for _ in range(2):
+        a.train_step(f, t, lr=1e-3)
+    b = salty_gb300.Unet(ctx, seed=99)
+    dn.load_weights(b, p)
+    assert b.adam_state()["step"] == 3
+    for _ in range(2):
+        b.train_step(f, t, lr=1e-3)
+    # weight gradients are summed with FP32 atomics, so runs agree to rounding, not bits;
+    # a resume without the optimiser state lands far further away
+    c = salty_gb300.Unet(ctx, seed=99)
+    c.set_params(np.load(p)["params"])
+    for _ in range(2):
+        c.train_step(f, t, lr=1e-3)
+    d_state = np.abs(b.params() - a.params()).max()
+    d_fresh = np.abs(c.params() - a.params()).max()
+    assert d_state < 2e-5 and d_fresh > 10 * d_state, (d_state, d_fresh)
+    for n in (a, b, c):
+        n.close()
