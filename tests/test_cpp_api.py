@@ -12,21 +12,22 @@ import pytest
 from conftest import ROOT
 
 
-def _compile(salty_lib, tmp_path):
+def _compile(salty_lib, tmp_path, name="cornell_pt"):
     import salty_gb300
     if not shutil.which("g++"):
         pytest.skip("no C++ compiler")
-    exe = str(tmp_path / "cornell_pt")
+    exe = str(tmp_path / name)
     libdir = os.path.dirname(salty_gb300.LIB_PATH)
     r = subprocess.run(["g++", "-std=c++17", "-O2", f"-I{os.path.join(ROOT, 'include')}",
-                        os.path.join(ROOT, "tests", "cpp", "cornell_pt.cpp"), f"-L{libdir}", "-lsalty_gpu",
+                        os.path.join(ROOT, "tests", "cpp", f"{name}.cpp"), f"-L{libdir}", "-lsalty_gpu",
                         f"-Wl,-rpath,{libdir}", "-o", exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     return exe
 
 
-def test_cpp_api_compiles_and_links(salty_lib, tmp_path):
-    _compile(salty_lib, tmp_path)
+@pytest.mark.parametrize("name", ["cornell_pt", "textured_pt"])
+def test_cpp_api_compiles_and_links(salty_lib, tmp_path, name):
+    _compile(salty_lib, tmp_path, name)
 
 
 def _read_png(path):
@@ -69,3 +70,27 @@ def test_cpp_pathtracer_run_renders_the_cornell_box(salty_lib, tmp_path, oracle)
     tot, _ = oracle.render(sd, 64, 64, 64, 8, profile=PROFILE_PHYSICAL, seed=2)
     om = (tot / 64).reshape(-1, 3).mean(axis=0)
     np.testing.assert_allclose(mean, om, rtol=0.05)
+
+
+@pytest.mark.gpu
+def test_cpp_textures_environment_and_smd_instances(salty_lib, tmp_path):
+    """AddTexture / SetColorMap / SetEnvironment / AddSmd (with and without a transform)
+    from C++: the program renders and writes its PNG."""
+    from salty_gb300 import scenes
+    from test_smd import write_smd
+    unit = scenes._icosphere(2).astype(np.float32).reshape(-1, 9)
+    n = unit.shape[0]
+    mesh = str(tmp_path / "ball.smd")
+    write_smd(mesh, unit * 0.4 + np.tile([0, 0.4, 0], 3).astype(np.float32), unit, np.zeros((n, 6), np.float32),
+              np.zeros(n, np.int32),
+              [(4, {"diffuse": (0.7, 0.3, 0.2), "specular": (0.5, 0.5, 0.5), "power": 50.0, "emission": (0, 0, 0)})])
+    exe = _compile(salty_lib, tmp_path, "textured_pt")
+    png = str(tmp_path / "t.png")
+    r = subprocess.run([exe, mesh, png, "4"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    words = r.stdout.split()
+    assert words[0] == "passes" and int(words[1]) == 4
+    mean = np.array([float(x) for x in words[3:6]])
+    assert np.all(np.isfinite(mean)) and mean.min() > 0
+    img = _read_png(png)
+    assert img.shape == (64, 96, 3) and img.std() > 5  # textured floor, spheres, sky: not flat
