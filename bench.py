@@ -344,6 +344,74 @@ def run_batch(args):
     ctx.close()
 
 
+def run_cornell(args):
+    """The small Cornell box (36 triangles, area light) at 256 x 256, 16 spp, depth 8, Russian
+    roulette from depth 3, the reference-compatible estimator, Reinhard to sRGB8 -- the
+    configuration the reference renders on its CPU.  value: device time of the render calls
+    (film already resident); e2e: the same call writing the sRGB8 image and the linear mean
+    to host memory every step.  cpu_baseline: the oracle's compat renderer on the host cores,
+    same scene, size and samples."""
+    import torch
+    import salty_gb300
+    from salty_gb300 import build as b
+    from salty_gb300 import scenes
+    b.build()
+    W, H, SPP, D = 256, 256, 16, 8
+    ctx = salty_gb300.Context(0)
+    c = scenes.cornell("baseline")
+    s = scenes.upload(ctx, c)
+    s.build()
+    kw = dict(profile=salty_gb300.PROFILE_COMPAT, tonemap=salty_gb300.TM_REINHARD)
+    for i in range(args.warmup):
+        s.render(W, H, SPP, D, seed=1 + i, want=(), **kw)
+    torch.cuda.synchronize()
+    dev_ms, rays, paths = 0.0, 0, 0
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            r = s.render(W, H, SPP, D, seed=100 + i, want=(), **kw)
+            dev_ms += r["ms"]
+            rays += r["rays"]
+            paths += r["paths"]
+        wall = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        e2e_rays = 0
+        for i in range(args.steps):
+            r = s.render(W, H, SPP, D, seed=200 + i, want=("mean", "srgb"), **kw)
+            e2e_rays += r["rays"]
+        e2e_wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": rays / dev_ms / 1e3, "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (the Cornell box scene generated on the host)",
+        "config": {"workload": "Cornell box (36 triangles), 256x256, 16 spp, depth 8, RR from 3, compat profile, "
+                               "Reinhard sRGB8", "rays_per_step": rays // args.steps,
+                   "paths_per_step": paths // args.steps, "wall_ms_per_step": wall * 1e3 / args.steps,
+                   "l2": "scene and film fit in L2 (the workload is this small)"},
+        "e2e": {"value": e2e_rays / e2e_wall / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": W * H * (3 + 12)},
+        "clocks": clocks,
+    }
+    if not args.no_cpu:
+        from oracle.oracle import PROFILE_COMPAT, Oracle, SceneData, build
+        build(with_reference=False)
+        o = Oracle()
+        sd = SceneData(c["tri_pos"], c["tri_nrm"], c["tri_mat"], c["materials"], c["light"], None, c["sky"],
+                       c["camera"])
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        o.render(sd, W, H, SPP, D, profile=PROFILE_COMPAT, seed=1, nthreads=cores)
+        secs = time.perf_counter() - t0
+        # the port traces the same number of rays per path on average as the device renderer
+        line["cpu_baseline"] = {"value": rays / args.steps / secs / 1e6, "unit": "Mrays/s", "cores": cores,
+                                "kind": "port", "sample": f"the whole workload, one frame ({secs:.2f} s); rays "
+                                                          "counted as the device renderer's per frame"}
+    print(json.dumps(line), flush=True)
+    s.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -354,7 +422,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (smaller cases for profiling)")
     ap.add_argument("--trace-shape", default="", help="block,regs,pool,postpone instead of salty_autotune_trace")
-    ap.add_argument("--workload", default="traversal", choices=["traversal", "time-to-rmse", "batch"])
+    ap.add_argument("--workload", default="traversal", choices=["traversal", "time-to-rmse", "batch", "cornell"])
     ap.add_argument("--scenes", type=int, default=256, help="batch: number of scenes")
     ap.add_argument("--target", type=float, default=0.01, help="time-to-rmse: relRMSE target")
     ap.add_argument("--ref-spp", type=int, default=65536, help="time-to-rmse: samples of the FP64 reference")
@@ -366,6 +434,9 @@ def main():
         return
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "cornell":
+        run_cornell(args)
         return
     n_rays = args.rays
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup

@@ -3,6 +3,7 @@
     python -m salty_gb300.profile render [--spp 1] [--frames 2]   1080p heightfield frames
     python -m salty_gb300.profile unet [--n 1 --h 1088 --w 1920]     one denoiser forward pass
     python -m salty_gb300.profile trace-sweep                        traversal launch shapes
+    python -m salty_gb300.profile cornell                            the 256^2 Cornell box, 16 spp
 
 `render` and `unet` print one line of timings; `trace-sweep` times every traversal launch
 shape (block size x register budget x pool x postpone) on the 1M-triangle microbenchmark
@@ -31,6 +32,21 @@ def render(spp: int, frames: int) -> dict:
         out.append({"ms": r["ms"], "rays": r["rays"], "paths": r["paths"]})
     return {"workload": f"1080p heightfield, {spp} spp x {frames} frames", "bvh_build_ms": info["build_ms"],
             "frames": out}
+
+
+def cornell() -> dict:
+    """The small Cornell box at 256 x 256, 16 spp, depth 8, Russian roulette from depth 3, in
+    the reference-compatible estimator: device time per frame (best of 5 after a warm-up)."""
+    from . import PROFILE_COMPAT, TM_REINHARD
+    ctx = Context(0)
+    s = scenes.upload(ctx, scenes.cornell("baseline"))
+    s.build()
+    s.render(256, 256, 16, 8, profile=PROFILE_COMPAT, seed=1, want=())
+    runs = [s.render(256, 256, 16, 8, profile=PROFILE_COMPAT, seed=2 + i, tonemap=TM_REINHARD, want=())
+            for i in range(5)]
+    best = min(runs, key=lambda r: r["ms"])
+    return {"workload": "Cornell box 256x256, 16 spp, depth 8, compat profile", "ms": best["ms"],
+            "Mrays_s": best["rays"] / best["ms"] / 1e3, "Mpaths_s": best["paths"] / best["ms"] / 1e3}
 
 
 def unet(n: int, h: int, w: int) -> dict:
@@ -72,7 +88,7 @@ def trace_sweep() -> dict:
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("what", choices=["render", "unet", "trace-sweep"])
+    ap.add_argument("what", choices=["render", "unet", "trace-sweep", "cornell"])
     ap.add_argument("--spp", type=int, default=1)
     ap.add_argument("--frames", type=int, default=2)
     ap.add_argument("--n", type=int, default=1)
@@ -83,6 +99,8 @@ def main(argv=None):
         r = render(a.spp, a.frames)
     elif a.what == "unet":
         r = unet(a.n, a.h, a.w)
+    elif a.what == "cornell":
+        r = cornell()
     else:
         r = trace_sweep()
     print(json.dumps(r))
