@@ -31,6 +31,7 @@ LAMBERT, MIRROR, GLASS, GGX, PHONG, PLASTIC = 0, 1, 2, 3, 4, 5
 TRACE_ANY_HIT, TRACE_WATERTIGHT, TRACE_COUNTERS = 1, 2, 4
 PROFILE_COMPAT, PROFILE_PHYSICAL = 0, 1
 TM_NONE, TM_REINHARD, TM_UNCHARTED2, TM_ACES = -1, 0, 1, 2
+CONV_TCGEN05, CONV_MMA_SYNC = 0, 1
 
 
 class SaltyError(RuntimeError):
@@ -117,7 +118,7 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_unet_train_step", "salty_scene_set_camera", "salty_denoise_unet", "salty_render_batch",
            "salty_get_tuning", "salty_set_tuning", "salty_autotune", "salty_mesh_load_smd", "salty_mesh_free",
            "salty_mesh_transform", "salty_autotune_trace", "salty_denoise_unet_ensemble", "salty_film_checkpoint",
-           "salty_film_restore", "salty_unet_get_adam", "salty_unet_set_adam"]
+           "salty_film_restore", "salty_unet_get_adam", "salty_unet_set_adam", "salty_unet_set_conv_kernel"]
 
 _lib = None
 
@@ -167,6 +168,7 @@ def lib() -> C.CDLL:
         "salty_film_restore": (i32, [vp, vp, C.POINTER(RenderOpts), vp, vp, vp, vp, i64]),
         "salty_unet_get_adam": (i32, [vp, vp, vp, vp, C.POINTER(i64)]),
         "salty_unet_set_adam": (i32, [vp, vp, vp, vp, i64]),
+        "salty_unet_set_conv_kernel": (i32, [vp, vp, i32]),
         "salty_render_batch": (i32, [vp, vp, vp, i32, C.POINTER(RenderStats)]),
         "salty_mesh_load_smd": (i32, [vp, C.c_char_p, C.POINTER(C.POINTER(Mesh))]),
         "salty_mesh_free": (None, [C.POINTER(Mesh)]),
@@ -634,6 +636,10 @@ class Unet:
             self.close()
         except Exception:
             pass
+
+    def set_conv_kernel(self, kind: int) -> None:
+        """CONV_TCGEN05 (default) or CONV_MMA_SYNC for the forward / backward-data convolutions."""
+        self.ctx.check(lib().salty_unet_set_conv_kernel(self.ctx.h, self.h, int(kind)), "unet_set_conv_kernel")
 
     def params(self) -> np.ndarray:
         p = np.empty(self.n_params, np.float32)

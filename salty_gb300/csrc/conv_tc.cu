@@ -1,0 +1,284 @@
+// conv_tc.cu -- the denoiser's 3x3 convolutions on the fifth-generation tensor cores.
+//
+// Implicit GEMM with the accumulators in tensor memory (TMEM).  One CTA computes a strip of
+// R image rows x 128 pixels and all output channels:
+//   M = 128 pixels of one image row (TMEM lane i holds pixel x0 + i),
+//   N = output channels, padded to a multiple of 16 (16..256),
+//   K = 9 taps x Cin, walked 16 input channels (one MMA's K) at a time.
+// Operands sit in shared memory in the tensor core's K-major layout without swizzle: "core
+// matrices" of 8 rows x 16 bytes (8 BF16 channels), 128 contiguous bytes each.  The
+// descriptors' leading byte offset is the distance between the two 8-channel halves of K,
+// the stride byte offset the distance between consecutive 8-row groups (128 B here).
+//   halo  [2 channel octets][R + 2 rows][130 pixels][8 channels] -- output row r, tap
+//         (ky, kx) reads the 128-pixel window starting at halo pixel (r + ky, kx), so the A
+//         descriptor of every tap is the same tile with its start moved 16 B per pixel
+//   wts   [9 taps][2 channel octets][Npad rows][8 channels]
+// Both are staged per 16-channel chunk into one of two buffers with cp.async (zero fill
+// outside the image and beyond the real output channels).  Thread 0 issues the chunk's
+// 9 x R MMAs (tcgen05.mma kind::f16, BF16 x BF16 -> FP32) and commits them to that
+// buffer's mbarrier; the loaders wait on it before refilling the buffer.  R x Npad <= 256
+// FP32 accumulator columns are allocated per CTA.  Epilogue: tcgen05.ld of each row's
+// columns, bias, ReLU, BF16, 16-byte stores.
+//
+// Every wait is bounded (2 s of the global timer); a wait that gives up sets
+// status[0] |= 1, skips the rest of the strip, frees the CTA's TMEM and returns.
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "internal.h"
+
+namespace salty {
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int kTcThreads = 128;
+constexpr int kStrip = 128;              // pixels per image row of a strip (the MMA's M)
+constexpr int kHaloW = kStrip + 2;       // staged pixels per halo row
+constexpr int kTmemCols = 256;           // accumulator columns per CTA
+constexpr int kBarBytes = 128;           // mbarriers + TMEM address at the start of shared memory
+constexpr unsigned long long kWaitNs = 2000000000ull;
+
+__host__ __device__ constexpr int halo_bytes(int R) { return 2 * (R + 2) * kHaloW * 16; }
+__host__ __device__ constexpr int wts_bytes(int npad) { return 9 * 2 * npad * 16; }
+__host__ __device__ constexpr int stage_bytes(int R, int npad) { return (halo_bytes(R) + wts_bytes(npad) + 127) / 128 * 128; }
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: start, leading and stride byte offsets (all >> 4), the
+// descriptor version bit of this architecture (bit 46), no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator (bits 4-5 = 1), A and B BF16
+// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__device__ __forceinline__ uint32_t idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        :: "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase with the given parity to complete; false after kWaitNs.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    if (mbar_try(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_try(bar, parity))
+        if (global_ns() - t0 > kWaitNs) return false;
+    return true;
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" :: "r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" :: "n"(N) : "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+struct TcConvArgs {
+    const bf16* in;
+    int in_cs, cin;        // channel stride and used channels of the input (cin % 16 == 0)
+    const bf16* wt;        // [9][wrows][cin]
+    int wrows;
+    const float* bias;     // [cout] or null
+    bf16* out;
+    int out_cs, out_co, cout;
+    int npad, R;           // MMA N (cout rounded up to 16) and image rows per strip
+    int N, H, W, relu;
+    int* status;
+};
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const TcConvArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem);           // [2] chunk buffers consumed
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 16);
+    unsigned char* stage0 = smem + kBarBytes;
+    const int R = a.R, npad = a.npad;
+    const int sbytes = stage_bytes(R, npad), hbytes = halo_bytes(R);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    const int strips_x = (a.W + kStrip - 1) / kStrip, strips_y = (a.H + R - 1) / R;
+    int t = blockIdx.x;
+    const int sx = t % strips_x;
+    t /= strips_x;
+    const int sy = t % strips_y;
+    const int n = t / strips_y;
+    const int x0 = sx * kStrip, y0 = sy * R;
+
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(bars + 0)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(saddr(bars + 1)) : "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(saddr(tmem_slot)), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+
+    // stages chunk c (input channels 16c .. 16c + 15) into buffer b
+    const int hrow = (R + 2) * kHaloW;
+    auto load = [&](int c, int b) {
+        unsigned char* hs = stage0 + b * sbytes;
+        unsigned char* ws = hs + hbytes;
+        const int c0 = c * 16;
+        for (int i = tid; i < 2 * hrow; i += kTcThreads) {
+            const int k8 = i & 1, p = i >> 1;             // neighbouring threads: the two octets of a pixel
+            const int hy = p / kHaloW, hx = p - hy * kHaloW;
+            const int gy = y0 - 1 + hy, gx = x0 - 1 + hx;
+            const bool ok = gy >= 0 && gy < a.H && gx >= 0 && gx < a.W;
+            const bf16* src = ok ? a.in + (((size_t)n * a.H + gy) * a.W + gx) * a.in_cs + c0 + k8 * 8 : a.in;
+            cp_async16(saddr(hs + (k8 * hrow + p) * 16), src, ok ? 16u : 0u);
+        }
+        const int live = a.cout < a.wrows ? a.cout : a.wrows;
+        for (int i = tid; i < 9 * 2 * npad; i += kTcThreads) {
+            const int k8 = i & 1, q = i >> 1;
+            const int tap = q / npad, row = q - tap * npad;
+            const bool ok = row < live;
+            const bf16* src = ok ? a.wt + ((size_t)tap * a.wrows + row) * a.cin + c0 + k8 * 8 : a.wt;
+            cp_async16(saddr(ws + ((tap * 2 + k8) * npad + row) * 16), src, ok ? 16u : 0u);
+        }
+    };
+
+    const int nchunks = a.cin / 16;
+    load(0, 0);
+    cp_async_commit();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();  // barriers initialised, TMEM address written
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t idesc = idesc_bf16(kStrip, npad);
+    bool failed = false;
+    for (int c = 0; c < nchunks; ++c) {
+        const int b = c & 1;
+        if (c + 1 < nchunks) {
+            bool ok = true;
+            if (c >= 1) ok = mbar_wait(saddr(bars + (b ^ 1)), ((c - 1) >> 1) & 1);  // chunk c-1's MMAs are done
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            load(c + 1, b ^ 1);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // cp.async data -> tensor core reads
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t hs = saddr(stage0 + b * sbytes), ws = hs + hbytes;
+            const uint32_t lbo_a = (uint32_t)hrow * 16, lbo_b = (uint32_t)npad * 16;
+            for (int tap = 0; tap < 9; ++tap) {
+                const int ky = tap / 3, kx = tap - ky * 3;
+                const uint64_t bd = sdesc(ws + tap * 2 * npad * 16, lbo_b, 128);
+                for (int r = 0; r < R; ++r) {
+                    const uint64_t ad = sdesc(hs + ((r + ky) * kHaloW + kx) * 16, lbo_a, 128);
+                    umma_bf16(tmem + r * npad, ad, bd, idesc, (c > 0 || tap > 0) ? 1u : 0u);
+                }
+            }
+            umma_commit(saddr(bars + b));
+        }
+    }
+    cp_async_wait<0>();
+    // the last commit completes when every MMA issued before it has
+    bool ok = !failed && mbar_wait(saddr(bars + ((nchunks - 1) & 1)), ((nchunks - 1) >> 1) & 1);
+    if (__syncthreads_or(!ok)) failed = true;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!failed) {
+        const int x = x0 + warp * 32 + lane;
+        for (int r = 0; r < R; ++r) {
+            const int y = y0 + r;
+            for (int j = 0; j < npad / 16; ++j) {
+                uint32_t v[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + r * npad + j * 16, v);
+                if (y >= a.H || x >= a.W) continue;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int co = j * 16 + h * 8;
+                    if (co >= a.cout) continue;
+                    uint32_t pk[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        float v0 = __uint_as_float(v[h * 8 + 2 * e]), v1 = __uint_as_float(v[h * 8 + 2 * e + 1]);
+                        if (a.bias) { v0 += a.bias[co + 2 * e]; v1 += a.bias[co + 2 * e + 1]; }
+                        if (a.relu) { v0 = fmaxf(v0, 0.0f); v1 = fmaxf(v1, 0.0f); }
+                        const __nv_bfloat162 p2 = __floats2bfloat162_rn(v0, v1);
+                        pk[e] = *reinterpret_cast<const uint32_t*>(&p2);
+                    }
+                    *reinterpret_cast<uint4*>(a.out + (((size_t)n * a.H + y) * a.W + x) * a.out_cs + a.out_co + co) =
+                        make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicOr(a.status, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+}  // namespace
+
+// Image rows per strip for an output width of npad channels: R x npad accumulator columns
+// fit in the CTA's 256.
+int conv_tc_rows(int cout) {
+    const int npad = (cout + 15) / 16 * 16;
+    int R = kTmemCols / npad;
+    return R > 8 ? 8 : R;
+}
+
+salty_status conv3x3_tc(salty_ctx* ctx, const void* in, int in_cs, int cin, const void* wt, int wrows,
+                        const float* bias, void* out, int out_cs, int out_co, int cout, int N, int H, int W, int relu,
+                        int* d_status) {
+    const int npad = (cout + 15) / 16 * 16;
+    if (cin % 16 || cin <= 0 || npad > 256 || npad < 16 || cout % 8 || in_cs % 8 || out_cs % 8 || out_co % 8 ||
+        wrows < 1)
+        return ctx->err.fail(SALTY_ERR_INVALID_ARG, "conv3x3_tc: unsupported shape (cin %d, cout %d)", cin, cout);
+    const int R = conv_tc_rows(cout);
+    const size_t smem = (size_t)kBarBytes + 2 * (size_t)stage_bytes(R, npad);
+    SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long tiles = (long long)N * ((H + R - 1) / R) * ((W + kStrip - 1) / kStrip);
+    TcConvArgs a{static_cast<const bf16*>(in), in_cs, cin, static_cast<const bf16*>(wt), wrows, bias,
+                 static_cast<bf16*>(out), out_cs, out_co, cout, npad, R, N, H, W, relu, d_status};
+    k_conv3x3_tc<<<(unsigned)tiles, kTcThreads, smem, ctx->stream>>>(a);
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+}  // namespace salty

@@ -19,6 +19,9 @@
 //   backward wts  M = Cout, N = Cin, K = pixels: ldmatrix.trans turns the NHWC tiles of dY and
 //                 of the shifted input into fragments with pixels along K; each CTA sums its
 //                 pixel tiles in registers and adds the partial into FP32 gradients.
+// The forward and backward-data convolutions run by default on tcgen05 (conv_tc.cu: TMEM
+// accumulators, 128-pixel strips); the mma.sync kernel below stays selectable
+// (salty_unet_set_conv_kernel) and is the reference the tcgen05 kernel is tested against.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -583,6 +586,7 @@ struct Unet {
     DevBuf<float> io;       // device copies of host features / targets / outputs
     DevBuf<float> film_ws;  // film planes, packed features and padded output of salty_denoise_unet
     DevBuf<double> loss;
+    int conv_kind = SALTY_CONV_TCGEN05;  // forward / backward-data convolution kernel
 };
 
 namespace {
@@ -613,8 +617,10 @@ void init_layers(Unet& u) {
     u.n_params = off;
 }
 
-salty_status launch_conv(salty_ctx* ctx, const bf16* in, int in_cs, int cin, const bf16* w, int rows, int nt,
-                         const float* bias, bf16* out, int out_cs, int cout, int N, int H, int W, int relu) {
+salty_status launch_conv(salty_ctx* ctx, int kind, const bf16* in, int in_cs, int cin, const bf16* w, int rows,
+                         int nt, const float* bias, bf16* out, int out_cs, int cout, int N, int H, int W, int relu) {
+    if (kind == SALTY_CONV_TCGEN05)
+        return conv3x3_tc(ctx, in, in_cs, cin, w, rows, bias, out, out_cs, 0, cout, N, H, W, relu, ctx->status.p + 8);
     const int tiles = N * ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
     dim3 grid(tiles, rows / (nt * 8));
     const size_t smem = ((size_t)kHaloX * kHaloY + (size_t)nt * 8) * (cin + 8) * sizeof(bf16);
@@ -691,8 +697,8 @@ salty_status forward(salty_ctx* ctx, Unet& u, const float* d_feat, int N, int H,
     k_prep_input<<<gsz(P0), 256, 0, st>>>(d_feat, P0, F.t[T_X]);
     auto conv = [&](int li, int in, int in_cs, int out, int h, int w) {
         const UnetLayer& L = u.layers[li];
-        return launch_conv(ctx, F.t[in], in_cs, L.cin, u.wf.p + L.wf_off, L.rows_fwd, L.nt, u.params.p + L.b_off,
-                           F.t[out], L.cout, L.cout, N, h, w, L.relu);
+        return launch_conv(ctx, u.conv_kind, F.t[in], in_cs, L.cin, u.wf.p + L.wf_off, L.rows_fwd, L.nt,
+                           u.params.p + L.b_off, F.t[out], L.cout, L.cout, N, h, w, L.relu);
     };
     auto pool = [&](int in, int out, int h, int w, int c) {
         k_pool<<<gsz((long long)N * (h / 2) * (w / 2) * c), 256, 0, st>>>(F.t[in], F.t[out], N, h, w, c);
@@ -743,8 +749,8 @@ salty_status conv_backward(salty_ctx* ctx, Unet& u, Fwd& F, int li, int x, int y
                                                                        u.grads.p + L.b_off);
     SALTY_TRY(launch_wgrad(ctx, g, L.cout_pad, L.cout, F.t[x], L.cin, L.cin, u.grads.p + L.w_off, N, h, w));
     if (want_dx)
-        SALTY_TRY(launch_conv(ctx, g, L.cout_pad, L.cout_pad, u.wb.p + L.wb_off, L.rows_bwd, L.nt_b, nullptr,
-                              F.t[T_G2], L.cin, L.cin, N, h, w, 0));
+        SALTY_TRY(launch_conv(ctx, u.conv_kind, g, L.cout_pad, L.cout_pad, u.wb.p + L.wb_off, L.rows_bwd, L.nt_b,
+                              nullptr, F.t[T_G2], L.cin, L.cin, N, h, w, 0));
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;
 }
@@ -818,6 +824,19 @@ salty_status stage(salty_ctx* ctx, Unet& u, const float* src, long long n, long 
     }
     SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(u.io.p + off, src, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     *out = u.io.p + off;
+    return SALTY_OK;
+}
+
+// The tensor-core convolutions' status word: zeroed before a call's first launch, read
+// after its last synchronisation.
+salty_status conv_status_reset(salty_ctx* ctx) {
+    SALTY_TRY_CUDA(ctx->err, cudaMemsetAsync(ctx->status.p + 8, 0, sizeof(int), ctx->stream));
+    return SALTY_OK;
+}
+salty_status conv_status_check(salty_ctx* ctx) {
+    int s = 0;
+    SALTY_TRY_CUDA(ctx->err, cudaMemcpy(&s, ctx->status.p + 8, sizeof(int), cudaMemcpyDeviceToHost));
+    if (s) return ctx->err.fail(SALTY_ERR_TIMEOUT, "unet: a tensor-core convolution gave up waiting for its MMAs");
     return SALTY_OK;
 }
 
@@ -951,6 +970,7 @@ salty_status salty_unet_forward(salty_ctx* ctx, salty_unet* net, const float* fe
     SALTY_TRY_CUDA(ctx->err, u.io.ensure((size_t)P0 * 16));
     const float* df;
     SALTY_TRY(stage(ctx, u, features, P0 * kFeatures, 0, &df));
+    SALTY_TRY(conv_status_reset(ctx));
     Fwd F;
     SALTY_TRY(forward(ctx, u, df, n, h, w, F));
     const bool dev_out = is_device_ptr(out_rgb);
@@ -960,7 +980,7 @@ salty_status salty_unet_forward(salty_ctx* ctx, salty_unet* net, const float* fe
         SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(out_rgb, dout, P0 * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(ctx->stream));
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
-    return SALTY_OK;
+    return conv_status_check(ctx);
 }
 
 salty_status salty_unet_train_step(salty_ctx* ctx, salty_unet* net, const float* features, const float* target_rgb,
@@ -975,6 +995,7 @@ salty_status salty_unet_train_step(salty_ctx* ctx, salty_unet* net, const float*
     const float *df, *dt;
     SALTY_TRY(stage(ctx, u, features, P0 * kFeatures, 0, &df));
     SALTY_TRY(stage(ctx, u, target_rgb, P0 * 3, P0 * kFeatures, &dt));
+    SALTY_TRY(conv_status_reset(ctx));
     Fwd F;
     SALTY_TRY(forward(ctx, u, df, n, h, w, F));
     double l = 0.0;
@@ -994,7 +1015,7 @@ salty_status salty_unet_train_step(salty_ctx* ctx, salty_unet* net, const float*
     }
     SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(ctx->stream));
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
-    return SALTY_OK;
+    return conv_status_check(ctx);
 }
 
 salty_status salty_denoise_unet_ensemble(salty_ctx* ctx, salty_unet* net, salty_scene* scene, int32_t mirrors,
@@ -1021,6 +1042,7 @@ salty_status salty_denoise_unet_ensemble(salty_ctx* ctx, salty_unet* net, salty_
     float* feat = dep + npx;
     float* img = feat + npp * kFeatures;
     SALTY_TRY(film_features(ctx, scene, mean, var, alb, nrm, dep));
+    SALTY_TRY(conv_status_reset(ctx));
     for (int k = 0; k < mirrors; ++k) {
         k_pack_features<<<gsz(npp), 256, 0, ctx->stream>>>(mean, var, alb, nrm, dep, W, H, Wp, Hp, k, feat);
         Fwd F;
@@ -1032,6 +1054,14 @@ salty_status salty_denoise_unet_ensemble(salty_ctx* ctx, salty_unet* net, salty_
     SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(out_rgb, img, (size_t)npx * 3 * sizeof(float), cudaMemcpyDefault,
                                              ctx->stream));
     SALTY_TRY_CUDA(ctx->err, cudaStreamSynchronize(ctx->stream));
+    return conv_status_check(ctx);
+}
+
+salty_status salty_unet_set_conv_kernel(salty_ctx* ctx, salty_unet* net, int32_t kind) {
+    if (!ctx || !net) return SALTY_ERR_INVALID_ARG;
+    if (kind != SALTY_CONV_TCGEN05 && kind != SALTY_CONV_MMA_SYNC)
+        return ctx->err.fail(SALTY_ERR_INVALID_ARG, "unknown convolution kernel %d", (int)kind);
+    net->net.conv_kind = kind;
     return SALTY_OK;
 }
 

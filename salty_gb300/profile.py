@@ -1,7 +1,8 @@
 """Small fixed workloads for profiling the kernels (run them under ncu or alone).
 
     python -m salty_gb300.profile render [--spp 1] [--frames 2]   1080p heightfield frames
-    python -m salty_gb300.profile unet [--n 1 --h 1088 --w 1920]     one denoiser forward pass
+    python -m salty_gb300.profile unet [--n 1 --h 1088 --w 1920] [--conv tcgen05|mma_sync|both]
+                                                                     denoiser forward passes
     python -m salty_gb300.profile trace-sweep                        traversal launch shapes
     python -m salty_gb300.profile cornell                            the 256^2 Cornell box, 16 spp
 
@@ -49,18 +50,36 @@ def cornell() -> dict:
             "Mrays_s": best["rays"] / best["ms"] / 1e3, "Mpaths_s": best["paths"] / best["ms"] / 1e3}
 
 
-def unet(n: int, h: int, w: int) -> dict:
+def unet(n: int, h: int, w: int, conv: str = "tcgen05", train: bool = False) -> dict:
+    """Forward passes (and, with train, training steps at lr 0) on random features: the
+    best of 5 wall-clock times after a warm-up, per convolution kernel."""
     import torch
+    from . import CONV_MMA_SYNC, CONV_TCGEN05
     ctx = Context(0)
     net = Unet(ctx, seed=1)
     f = torch.rand((n, h, w, UNET_FEATURES), device="cuda")
     o = torch.empty((n, h, w, 3), device="cuda")
-    net.forward(f, out=o)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    net.forward(f, out=o)
-    torch.cuda.synchronize()
-    return {"workload": f"U-Net forward {n}x{h}x{w}", "ms": (time.perf_counter() - t0) * 1e3}
+    tgt = torch.rand((n, h, w, 3), device="cuda")
+    kinds = {"tcgen05": [CONV_TCGEN05], "mma_sync": [CONV_MMA_SYNC], "both": [CONV_TCGEN05, CONV_MMA_SYNC]}[conv]
+    res = {"workload": f"U-Net {n}x{h}x{w}"}
+    for k in kinds:
+        net.set_conv_kernel(k)
+        name = "tcgen05" if k == CONV_TCGEN05 else "mma_sync"
+        steps = [("forward_ms", lambda: net.forward(f, out=o))]
+        if train:
+            steps.append(("train_step_ms", lambda: net.train_step(f, tgt, lr=0.0)))
+        for key, fn in steps:
+            fn()
+            torch.cuda.synchronize()
+            best = float("inf")
+            for _ in range(5):
+                t0 = time.perf_counter()
+                fn()
+                torch.cuda.synchronize()
+                best = min(best, (time.perf_counter() - t0) * 1e3)
+            res[f"{name}_{key}"] = best
+    net.close()
+    return res
 
 
 def trace_sweep() -> dict:
@@ -94,11 +113,13 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=1)
     ap.add_argument("--h", type=int, default=1088)
     ap.add_argument("--w", type=int, default=1920)
+    ap.add_argument("--conv", default="tcgen05", choices=["tcgen05", "mma_sync", "both"])
+    ap.add_argument("--train", action="store_true", help="unet: also time training steps")
     a = ap.parse_args(argv)
     if a.what == "render":
         r = render(a.spp, a.frames)
     elif a.what == "unet":
-        r = unet(a.n, a.h, a.w)
+        r = unet(a.n, a.h, a.w, a.conv, a.train)
     elif a.what == "cornell":
         r = cornell()
     else:

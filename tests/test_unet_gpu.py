@@ -145,3 +145,55 @@ def test_training_checkpoint_resumes_exactly(ctx, tmp_path):
     assert d_state < 2e-5 and d_fresh > 10 * d_state, (d_state, d_fresh)
     for n in (a, b, c):
         n.close()
+
+
+@pytest.mark.parametrize("kind", ["tcgen05", "mma_sync"])
+def test_both_conv_kernels_match_oracle_on_ragged_strips(ctx, kind):
+    """1 x 48 x 272 pixels: the tensor-core kernel's 128-pixel strips end ragged (272 =
+    2 x 128 + 16) and its row groups (8, 5, 4, 3 or 2 rows by channel count) do not divide
+    the level heights 48, 24, 12, 6, 3; forward output and every layer's gradients against
+    the oracle, for both convolution kernels."""
+    import salty_gb300
+    from oracle.unet_oracle import LAYERS, UnetOracle
+    net = salty_gb300.Unet(ctx, seed=12)
+    net.set_conv_kernel(salty_gb300.CONV_TCGEN05 if kind == "tcgen05" else salty_gb300.CONV_MMA_SYNC)
+    f, t = _batch(8, n=1, h=48, w=272)
+    p0 = net.params()
+    orc = UnetOracle(p0)
+    out = net.forward(f)
+    want, _ = orc.forward(f)
+    assert _rel(out, want) < 0.02, _rel(out, want)
+    loss = net.train_step(f, t, lr=0.0)
+    lo, go = orc.loss_and_grads(f, t)
+    assert abs(loss / lo - 1) < 1e-2, (loss, lo)
+    g = net.grads()
+    o = 0
+    for i, (ci, co, _) in enumerate(LAYERS):
+        n = 9 * ci * co + co
+        a, b = g[o:o + n], go[o:o + n]
+        cos = a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
+        assert _rel(a, b) < 0.05 and cos > 0.998, (i, _rel(a, b), cos)
+        o += n
+    net.close()
+
+
+def test_tcgen05_and_mma_sync_agree(ctx):
+    """The two convolution kernels on a 2 x 144 x 400 batch: same outputs and gradients up to
+    the order of the FP32 sums (a BF16 rounding step now and then)."""
+    import salty_gb300
+    net = salty_gb300.Unet(ctx, seed=13)
+    f, t = _batch(9, n=2, h=144, w=400)
+    res = {}
+    for kind in (salty_gb300.CONV_MMA_SYNC, salty_gb300.CONV_TCGEN05):
+        net.set_conv_kernel(kind)
+        out = net.forward(f)
+        loss = net.train_step(f, t, lr=0.0)
+        res[kind] = (out, loss, net.grads())
+    (o1, l1, g1), (o2, l2, g2) = res[salty_gb300.CONV_MMA_SYNC], res[salty_gb300.CONV_TCGEN05]
+    assert _rel(o2, o1) < 0.01, _rel(o2, o1)
+    assert abs(l2 / l1 - 1) < 1e-3, (l1, l2)
+    cos = g1 @ g2 / (np.linalg.norm(g1) * np.linalg.norm(g2))
+    assert _rel(g2, g1) < 0.02 and cos > 0.9995, (_rel(g2, g1), cos)
+    with pytest.raises(salty_gb300.SaltyError):
+        net.set_conv_kernel(7)
+    net.close()
