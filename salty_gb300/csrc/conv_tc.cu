@@ -27,6 +27,7 @@
 #include <cstdint>
 
 #include "internal.h"
+#include "unet_src.cuh"
 
 namespace salty {
 namespace {
@@ -110,8 +111,8 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 }
 
 struct TcConvArgs {
-    const bf16* in;
-    int in_cs, cin;        // channel stride and used channels of the input (cin % 16 == 0)
+    ConvSrc src;           // the input's channels (one tensor, or [up2(coarse) | skip])
+    int cin;               // cin % 16 == 0
     const bf16* wt;        // [9][wrows][cin]
     int wrows;
     const float* bias;     // [cout] or null
@@ -160,7 +161,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const TcConvArgs a
             const int hy = p / kHaloW, hx = p - hy * kHaloW;
             const int gy = y0 - 1 + hy, gx = x0 - 1 + hx;
             const bool ok = gy >= 0 && gy < a.H && gx >= 0 && gx < a.W;
-            const bf16* src = ok ? a.in + (((size_t)n * a.H + gy) * a.W + gx) * a.in_cs + c0 + k8 * 8 : a.in;
+            const bf16* src = ok ? src_at(a.src, n, gy, gx, a.H, a.W, c0 + k8 * 8) : a.src.a;
             cp_async16(saddr(hs + (k8 * hrow + p) * 16), src, ok ? 16u : 0u);
         }
         const int live = a.cout < a.wrows ? a.cout : a.wrows;
@@ -263,19 +264,17 @@ int conv_tc_rows(int cout) {
     return R > 8 ? 8 : R;
 }
 
-salty_status conv3x3_tc(salty_ctx* ctx, const void* in, int in_cs, int cin, const void* wt, int wrows,
-                        const float* bias, void* out, int out_cs, int out_co, int cout, int N, int H, int W, int relu,
-                        int* d_status) {
+salty_status conv3x3_tc(salty_ctx* ctx, const ConvSrc& in, int cin, const bf16* wt, int wrows, const float* bias,
+                        bf16* out, int out_cs, int out_co, int cout, int N, int H, int W, int relu, int* d_status) {
     const int npad = (cout + 15) / 16 * 16;
-    if (cin % 16 || cin <= 0 || npad > 256 || npad < 16 || cout % 8 || in_cs % 8 || out_cs % 8 || out_co % 8 ||
-        wrows < 1)
+    if (cin % 16 || cin <= 0 || npad > 256 || npad < 16 || cout % 8 || in.a_cs % 8 || in.a_ch % 16 ||
+        (in.a_ch < cin && (!in.b || in.b_cs % 8)) || out_cs % 8 || out_co % 8 || wrows < 1)
         return ctx->err.fail(SALTY_ERR_INVALID_ARG, "conv3x3_tc: unsupported shape (cin %d, cout %d)", cin, cout);
     const int R = conv_tc_rows(cout);
     const size_t smem = (size_t)kBarBytes + 2 * (size_t)stage_bytes(R, npad);
     SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long tiles = (long long)N * ((H + R - 1) / R) * ((W + kStrip - 1) / kStrip);
-    TcConvArgs a{static_cast<const bf16*>(in), in_cs, cin, static_cast<const bf16*>(wt), wrows, bias,
-                 static_cast<bf16*>(out), out_cs, out_co, cout, npad, R, N, H, W, relu, d_status};
+    TcConvArgs a{in, cin, wt, wrows, bias, out, out_cs, out_co, cout, npad, R, N, H, W, relu, d_status};
     k_conv3x3_tc<<<(unsigned)tiles, kTcThreads, smem, ctx->stream>>>(a);
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;

@@ -276,11 +276,6 @@ salty_status film_outputs(salty_ctx* ctx, salty_scene* sc, const salty_render_op
                           float* d_mean, float* d_var, uint8_t* d_srgb);
 salty_status film_features(salty_ctx* ctx, salty_scene* sc, float* d_mean, float* d_var, float* d_albedo,
                            float* d_normal, float* d_depth);
-// conv_tc.cu: 3x3 convolution, BF16 NHWC, on tcgen05 (cin % 16 == 0, cout % 8 == 0, cout <= 256)
-int conv_tc_rows(int cout);
-salty_status conv3x3_tc(salty_ctx* ctx, const void* in, int in_cs, int cin, const void* wt, int wrows,
-                        const float* bias, void* out, int out_cs, int out_co, int cout, int N, int H, int W, int relu,
-                        int* d_status);
 // post.cu
 salty_status tonemap_device(salty_ctx* ctx, int type, int w, int h, const float* d_rgb,
                             float* d_out, uint8_t* d_srgb, int ref_oetf, float* ave, float* mx);

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "unet_src.cuh"
 
 namespace salty {
 namespace {
@@ -59,7 +60,7 @@ __device__ __forceinline__ void ldmatrix_x4_trans(unsigned (&r)[4], const void* 
 }
 
 // ---------------------------------------------------------------- conv3x3 (forward, backward data)
-// in:  [N][H][W][in_cs] BF16 (channels 0..Cin-1 used, Cin % 16 == 0)
+// in:  BF16 NHWC input channels 0..Cin-1 (Cin % 16 == 0) from one or two sources (ConvSrc)
 // wt:  [9][wrows][Cin] BF16 (tap-major, input channel contiguous); output channel co reads row co
 // out: [N][H][W][out_cs] BF16 at channel offset out_co (channels co < Cout written)
 // NT n8-tiles per CTA; blockIdx.y selects output channels [blockIdx.y*NT*8, +NT*8).
@@ -77,8 +78,7 @@ __device__ __forceinline__ void ldmatrix_x2(unsigned& r0, unsigned& r1, const vo
 }
 
 template <int NT>
-__global__ void __launch_bounds__(kConvThreads) k_conv3x3(const bf16* __restrict__ in, int in_cs, int Cin,
-                                                          const bf16* __restrict__ wt, const float* __restrict__ bias,
+__global__ void __launch_bounds__(kConvThreads) k_conv3x3(const ConvSrc in, int Cin, const bf16* __restrict__ wt, const float* __restrict__ bias,
                                                           bf16* __restrict__ out, int out_cs, int out_co, int Cout,
                                                           int N, int H, int W, int relu) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -98,8 +98,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const bf16* __restrict
         const int pix = i / chunks, c = i % chunks;
         const int gy = y0 - 1 + pix / kHaloX, gx = x0 - 1 + pix % kHaloX;
         uint4 v = make_uint4(0, 0, 0, 0);
-        if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-            v = *reinterpret_cast<const uint4*>(in + (((size_t)n * H + gy) * W + gx) * in_cs + c * 8);
+        if (gy >= 0 && gy < H && gx >= 0 && gx < W) v = __ldg(reinterpret_cast<const uint4*>(src_at(in, n, gy, gx, H, W, c * 8)));
         *reinterpret_cast<uint4*>(tile + pix * stride + c * 8) = v;
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -177,10 +176,11 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const bf16* __restrict
 // dW[tap][co][ci] += sum_p dY[p][co] * X[p + (ky-1, kx-1)][ci] for one tap (blockIdx.y) and a
 // 16-wide input-channel slice (blockIdx.z); CTAs stride over 8x16 pixel tiles (blockIdx.x).
 // dY: [N][H][W][dy_cs] with Cpad = dy_cs channels (multiple of 16, zero beyond the layer's
-// real outputs); rows co >= cout_real are not written.  X: [N][H][W][x_cs], Cin % 16 == 0.
+// real outputs); rows co >= cout_real are not written.  X: the layer's input (ConvSrc),
+// Cin % 16 == 0.
 __global__ void __launch_bounds__(kConvThreads) k_conv3x3_wgrad(const bf16* __restrict__ dy, int Cpad, int cout_real,
-                                                                const bf16* __restrict__ x, int x_cs, int Cin,
-                                                                float* __restrict__ dw, int N, int H, int W) {
+                                                                const ConvSrc x, int Cin, float* __restrict__ dw,
+                                                                int N, int H, int W) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int dstride = Cpad + 8;
     constexpr int xstride = 16 + 8;
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_wgrad(const bf16* __re
             const int gy = y0 - 1 + pix / kHaloX, gx = x0 - 1 + pix % kHaloX;
             uint4 v = make_uint4(0, 0, 0, 0);
             if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-                v = *reinterpret_cast<const uint4*>(x + (((size_t)n * H + gy) * W + gx) * x_cs + ci0 + c * 8);
+                v = __ldg(reinterpret_cast<const uint4*>(src_at(x, n, gy, gx, H, W, ci0 + c * 8)));
             *reinterpret_cast<uint4*>(xs + pix * xstride + c * 8) = v;
         }
         __syncthreads();
@@ -279,28 +279,49 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_wgrad(const bf16* __re
 __global__ void k_prep_input(const float* __restrict__ f, long long npx, bf16* __restrict__ x) {
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
         const float* s = f + p * kFeatures;
-        bf16* d = x + p * 16;
-        for (int c = 0; c < 3; ++c) d[c] = __float2bfloat16(log1pf(fmaxf(s[c], 0.0f)));
-        for (int c = 3; c < kFeatures; ++c) d[c] = __float2bfloat16(s[c]);
-        for (int c = kFeatures; c < 16; ++c) d[c] = __float2bfloat16(0.0f);
+        float v[16];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[c] = log1pf(fmaxf(__ldg(s + c), 0.0f));
+#pragma unroll
+        for (int c = 3; c < kFeatures; ++c) v[c] = __ldg(s + c);
+#pragma unroll
+        for (int c = kFeatures; c < 16; ++c) v[c] = 0.0f;
+        uint32_t w[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+            w[k] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+        uint4* d = reinterpret_cast<uint4*>(x + p * 16);
+        d[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        d[1] = make_uint4(w[4], w[5], w[6], w[7]);
     }
 }
 
-// 2x2 max-pool: in [N][H][W][C] -> out [N][H/2][W/2][C]
+// 2x2 max-pool: in [N][H][W][C] -> out [N][H/2][W/2][C], C % 8 == 0; one thread per output
+// pixel and 8 channels (16-byte loads and store; max of BF16 values is exact)
 __global__ void k_pool(const bf16* __restrict__ in, bf16* __restrict__ out, int N, int H, int W, int C) {
-    const int Ho = H / 2, Wo = W / 2;
-    const long long total = (long long)N * Ho * Wo * C;
+    const int Ho = H / 2, Wo = W / 2, G = C / 8;
+    const long long total = (long long)N * Ho * Wo * G;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        long long p = i / C;
+        const int g = (int)(i % G);
+        long long p = i / G;
         const int xo = (int)(p % Wo);
         p /= Wo;
         const int yo = (int)(p % Ho);
         const int n = (int)(p / Ho);
-        const bf16* s = in + (((size_t)n * H + 2 * yo) * W + 2 * xo) * C + c;
-        float m = fmaxf(fmaxf(__bfloat162float(s[0]), __bfloat162float(s[C])),
-                        fmaxf(__bfloat162float(s[(size_t)W * C]), __bfloat162float(s[(size_t)W * C + C])));
-        out[i] = __float2bfloat16(m);
+        const bf16* s = in + (((size_t)n * H + 2 * yo) * W + 2 * xo) * C + g * 8;
+        uint4 q[4] = {__ldg(reinterpret_cast<const uint4*>(s)), __ldg(reinterpret_cast<const uint4*>(s + C)),
+                      __ldg(reinterpret_cast<const uint4*>(s + (size_t)W * C)),
+                      __ldg(reinterpret_cast<const uint4*>(s + (size_t)W * C + C))};
+        __nv_bfloat162* m = reinterpret_cast<__nv_bfloat162*>(&q[0]);
+#pragma unroll
+        for (int k = 1; k < 4; ++k) {
+            const __nv_bfloat162* o = reinterpret_cast<const __nv_bfloat162*>(&q[k]);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) m[e] = __hmax2(m[e], o[e]);
+        }
+        *reinterpret_cast<uint4*>(out + i * 8) = q[0];
     }
 }
 
@@ -325,32 +346,6 @@ __global__ void k_pool_bwd(const bf16* __restrict__ in, const float* __restrict_
             if (v > m) { m = v; arg = k; }
         }
         din[base + off[arg]] += dout[i];
-    }
-}
-
-// nearest 2x up-sampling of coarse [N][H/2][W/2][Cc] into channels [0, Cc) of cat [N][H][W][Ccat]
-__global__ void k_upsample(const bf16* __restrict__ coarse, int Cc, bf16* __restrict__ cat, int Ccat, int N, int H,
-                           int W) {
-    const long long total = (long long)N * H * W * Cc;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % Cc);
-        long long p = i / Cc;
-        const int x = (int)(p % W);
-        p /= W;
-        const int y = (int)(p % H);
-        const int n = (int)(p / H);
-        cat[(((size_t)n * H + y) * W + x) * Ccat + c] = coarse[(((size_t)n * (H / 2) + y / 2) * (W / 2) + x / 2) * Cc + c];
-    }
-}
-
-// copy skip [N][H][W][Cs] into channels [off, off + Cs) of cat
-__global__ void k_copy_channels(const bf16* __restrict__ src, int Cs, bf16* __restrict__ dst, int Cd, int off,
-                                long long npx) {
-    const long long total = npx * Cs;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const long long p = i / Cs;
-        const int c = (int)(i % Cs);
-        dst[p * Cd + off + c] = src[i];
     }
 }
 
@@ -563,7 +558,7 @@ inline int round_up(int a, int b) { return (a + b - 1) / b * b; }
 // Activation workspace (BF16), by name; sizes in elements for N x H x W inputs.
 enum {
     T_X, T_A0, T_E0, T_P0, T_A1, T_E1, T_P1, T_A2, T_E2, T_P2, T_A3, T_E3, T_P3, T_B,
-    T_C3, T_D3, T_C2, T_D2, T_C1, T_D1, T_C0, T_D0, T_OUT, T_G, T_G2, T_COUNT
+    T_D3, T_D2, T_D1, T_D0, T_OUT, T_G, T_G2, T_COUNT
 };
 // FP32 gradients, by name.
 enum {
@@ -617,10 +612,10 @@ void init_layers(Unet& u) {
     u.n_params = off;
 }
 
-salty_status launch_conv(salty_ctx* ctx, int kind, const bf16* in, int in_cs, int cin, const bf16* w, int rows,
-                         int nt, const float* bias, bf16* out, int out_cs, int cout, int N, int H, int W, int relu) {
+salty_status launch_conv(salty_ctx* ctx, int kind, const ConvSrc& in, int cin, const bf16* w, int rows, int nt,
+                         const float* bias, bf16* out, int out_cs, int cout, int N, int H, int W, int relu) {
     if (kind == SALTY_CONV_TCGEN05)
-        return conv3x3_tc(ctx, in, in_cs, cin, w, rows, bias, out, out_cs, 0, cout, N, H, W, relu, ctx->status.p + 8);
+        return conv3x3_tc(ctx, in, cin, w, rows, bias, out, out_cs, 0, cout, N, H, W, relu, ctx->status.p + 8);
     const int tiles = N * ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
     dim3 grid(tiles, rows / (nt * 8));
     const size_t smem = ((size_t)kHaloX * kHaloY + (size_t)nt * 8) * (cin + 8) * sizeof(bf16);
@@ -628,8 +623,8 @@ salty_status launch_conv(salty_ctx* ctx, int kind, const bf16* in, int in_cs, in
     case NTV: {                                                                                                     \
         SALTY_TRY_CUDA(ctx->err,                                                                                    \
                        cudaFuncSetAttribute(k_conv3x3<NTV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
-        k_conv3x3<NTV><<<grid, kConvThreads, smem, ctx->stream>>>(in, in_cs, cin, w, bias, out, out_cs, 0, cout, N, H, \
-                                                                  W, relu);                                         \
+        k_conv3x3<NTV><<<grid, kConvThreads, smem, ctx->stream>>>(in, cin, w, bias, out, out_cs, 0, cout, N, H, W,   \
+                                                                  relu);                                            \
         break;                                                                                                      \
     }
     switch (nt) {
@@ -643,8 +638,8 @@ salty_status launch_conv(salty_ctx* ctx, int kind, const bf16* in, int in_cs, in
     return SALTY_OK;
 }
 
-salty_status launch_wgrad(salty_ctx* ctx, const bf16* dy, int cpad, int cout, const bf16* x, int x_cs, int cin,
-                          float* dw, int N, int H, int W) {
+salty_status launch_wgrad(salty_ctx* ctx, const bf16* dy, int cpad, int cout, const ConvSrc& x, int cin, float* dw,
+                          int N, int H, int W) {
     const size_t smem = ((size_t)kTileX * kTileY * (cpad + 8) + (size_t)kHaloX * kHaloY * 24) * sizeof(bf16);
     SALTY_TRY_CUDA(ctx->err,
                    cudaFuncSetAttribute(k_conv3x3_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -653,7 +648,7 @@ salty_status launch_wgrad(salty_ctx* ctx, const bf16* dy, int cpad, int cout, co
     if (gx < 1) gx = 1;
     if (gx > tiles) gx = tiles;
     dim3 grid(gx, 9, cin / 16);
-    k_conv3x3_wgrad<<<grid, kConvThreads, smem, ctx->stream>>>(dy, cpad, cout, x, x_cs, cin, dw, N, H, W);
+    k_conv3x3_wgrad<<<grid, kConvThreads, smem, ctx->stream>>>(dy, cpad, cout, x, cin, dw, N, H, W);
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;
 }
@@ -662,8 +657,8 @@ salty_status ensure_workspace(salty_ctx* ctx, Unet& u, int N, int H, int W) {
     if (u.N == N && u.H == H && u.W == W && u.act.p) return SALTY_OK;
     const long long P0 = (long long)N * H * W, P1 = P0 / 4, P2 = P0 / 16, P3 = P0 / 64, P4 = P0 / 256;
     const long long asz[T_COUNT] = {P0 * 16, P0 * 32, P0 * 32, P1 * 32, P1 * 48, P1 * 48, P2 * 48, P2 * 64, P2 * 64,
-                                    P3 * 64, P3 * 80, P3 * 80, P4 * 80, P4 * 96, P3 * 176, P3 * 80, P2 * 144, P2 * 64,
-                                    P1 * 112, P1 * 48, P0 * 80, P0 * 32, P0 * 8, P0 * 176, P0 * 176};
+                                    P3 * 64, P3 * 80, P3 * 80, P4 * 80, P4 * 96, P3 * 80, P2 * 64, P1 * 48, P0 * 32,
+                                    P0 * 8, P0 * 176, P0 * 176};
     const long long gsz_[G_COUNT] = {P0 * 8, P0 * 32, P0 * 32, P1 * 48, P2 * 64, P3 * 80, P4 * 96, P0 * 32, P1 * 48,
                                      P2 * 64, P3 * 80, P4 * 80, P3 * 80, P3 * 64, P2 * 64, P2 * 48, P1 * 48, P1 * 32,
                                      P0 * 32};
@@ -695,42 +690,37 @@ salty_status forward(salty_ctx* ctx, Unet& u, const float* d_feat, int N, int H,
     cudaStream_t st = ctx->stream;
     const long long P0 = (long long)N * H * W;
     k_prep_input<<<gsz(P0), 256, 0, st>>>(d_feat, P0, F.t[T_X]);
-    auto conv = [&](int li, int in, int in_cs, int out, int h, int w) {
+    auto conv = [&](int li, const ConvSrc& in, int out, int h, int w) {
         const UnetLayer& L = u.layers[li];
-        return launch_conv(ctx, u.conv_kind, F.t[in], in_cs, L.cin, u.wf.p + L.wf_off, L.rows_fwd, L.nt,
-                           u.params.p + L.b_off, F.t[out], L.cout, L.cout, N, h, w, L.relu);
+        return launch_conv(ctx, u.conv_kind, in, L.cin, u.wf.p + L.wf_off, L.rows_fwd, L.nt, u.params.p + L.b_off,
+                           F.t[out], L.cout, L.cout, N, h, w, L.relu);
     };
     auto pool = [&](int in, int out, int h, int w, int c) {
-        k_pool<<<gsz((long long)N * (h / 2) * (w / 2) * c), 256, 0, st>>>(F.t[in], F.t[out], N, h, w, c);
+        const long long groups = (long long)N * (h / 2) * (w / 2) * (c / 8);
+        k_pool<<<gsz(groups), 256, 0, st>>>(F.t[in], F.t[out], N, h, w, c);
     };
-    auto upcat = [&](int coarse, int cc, int skip, int cs, int cat, int h, int w) {
-        const long long np = (long long)N * h * w;
-        k_upsample<<<gsz(np * cc), 256, 0, st>>>(F.t[coarse], cc, F.t[cat], cc + cs, N, h, w);
-        k_copy_channels<<<gsz(np * cs), 256, 0, st>>>(F.t[skip], cs, F.t[cat], cc + cs, cc, np);
-    };
+    auto x = [&](int t, int c) { return conv_src(F.t[t], c, c); };
+    // decoder inputs: [up2(coarse) | skip], read by the convolutions from both tensors
+    auto cat = [&](int coarse, int cc, int skip, int cs) { return conv_src_cat(F.t[coarse], cc, F.t[skip], cs); };
     const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8, H4 = H / 16, W4 = W / 16;
-    SALTY_TRY(conv(0, T_X, 16, T_A0, H, W));
-    SALTY_TRY(conv(1, T_A0, 32, T_E0, H, W));
+    SALTY_TRY(conv(0, x(T_X, 16), T_A0, H, W));
+    SALTY_TRY(conv(1, x(T_A0, 32), T_E0, H, W));
     pool(T_E0, T_P0, H, W, 32);
-    SALTY_TRY(conv(2, T_P0, 32, T_A1, H1, W1));
-    SALTY_TRY(conv(3, T_A1, 48, T_E1, H1, W1));
+    SALTY_TRY(conv(2, x(T_P0, 32), T_A1, H1, W1));
+    SALTY_TRY(conv(3, x(T_A1, 48), T_E1, H1, W1));
     pool(T_E1, T_P1, H1, W1, 48);
-    SALTY_TRY(conv(4, T_P1, 48, T_A2, H2, W2));
-    SALTY_TRY(conv(5, T_A2, 64, T_E2, H2, W2));
+    SALTY_TRY(conv(4, x(T_P1, 48), T_A2, H2, W2));
+    SALTY_TRY(conv(5, x(T_A2, 64), T_E2, H2, W2));
     pool(T_E2, T_P2, H2, W2, 64);
-    SALTY_TRY(conv(6, T_P2, 64, T_A3, H3, W3));
-    SALTY_TRY(conv(7, T_A3, 80, T_E3, H3, W3));
+    SALTY_TRY(conv(6, x(T_P2, 64), T_A3, H3, W3));
+    SALTY_TRY(conv(7, x(T_A3, 80), T_E3, H3, W3));
     pool(T_E3, T_P3, H3, W3, 80);
-    SALTY_TRY(conv(8, T_P3, 80, T_B, H4, W4));
-    upcat(T_B, 96, T_E3, 80, T_C3, H3, W3);
-    SALTY_TRY(conv(9, T_C3, 176, T_D3, H3, W3));
-    upcat(T_D3, 80, T_E2, 64, T_C2, H2, W2);
-    SALTY_TRY(conv(10, T_C2, 144, T_D2, H2, W2));
-    upcat(T_D2, 64, T_E1, 48, T_C1, H1, W1);
-    SALTY_TRY(conv(11, T_C1, 112, T_D1, H1, W1));
-    upcat(T_D1, 48, T_E0, 32, T_C0, H, W);
-    SALTY_TRY(conv(12, T_C0, 80, T_D0, H, W));
-    SALTY_TRY(conv(13, T_D0, 32, T_OUT, H, W));
+    SALTY_TRY(conv(8, x(T_P3, 80), T_B, H4, W4));
+    SALTY_TRY(conv(9, cat(T_B, 96, T_E3, 80), T_D3, H3, W3));
+    SALTY_TRY(conv(10, cat(T_D3, 80, T_E2, 64), T_D2, H2, W2));
+    SALTY_TRY(conv(11, cat(T_D2, 64, T_E1, 48), T_D1, H1, W1));
+    SALTY_TRY(conv(12, cat(T_D1, 48, T_E0, 32), T_D0, H, W));
+    SALTY_TRY(conv(13, x(T_D0, 32), T_OUT, H, W));
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;
 }
@@ -738,8 +728,8 @@ salty_status forward(salty_ctx* ctx, Unet& u, const float* d_feat, int N, int H,
 // One conv layer backward.  dy: FP32 [npx][cout] gradient of the layer output y.  Adds the
 // weight and bias gradients; leaves dL/d(input) in BF16 in F.t[T_G2] ([npx][cin]) when
 // want_dx.
-salty_status conv_backward(salty_ctx* ctx, Unet& u, Fwd& F, int li, int x, int y, const float* dy, int N, int h,
-                           int w, bool want_dx) {
+salty_status conv_backward(salty_ctx* ctx, Unet& u, Fwd& F, int li, const ConvSrc& x, int y, const float* dy, int N,
+                           int h, int w, bool want_dx) {
     const UnetLayer& L = u.layers[li];
     const long long npx = (long long)N * h * w;
     cudaStream_t st = ctx->stream;
@@ -747,10 +737,10 @@ salty_status conv_backward(salty_ctx* ctx, Unet& u, Fwd& F, int li, int x, int y
     k_relu_bwd<<<gsz(npx * L.cout_pad), 256, 0, st>>>(F.t[y], L.cout, dy, L.cout, L.relu, npx, g, L.cout_pad);
     k_bias_grad<<<gsz(npx * L.cout), 256, L.cout * sizeof(float), st>>>(g, L.cout_pad, L.cout, npx,
                                                                        u.grads.p + L.b_off);
-    SALTY_TRY(launch_wgrad(ctx, g, L.cout_pad, L.cout, F.t[x], L.cin, L.cin, u.grads.p + L.w_off, N, h, w));
+    SALTY_TRY(launch_wgrad(ctx, g, L.cout_pad, L.cout, x, L.cin, u.grads.p + L.w_off, N, h, w));
     if (want_dx)
-        SALTY_TRY(launch_conv(ctx, u.conv_kind, g, L.cout_pad, L.cout_pad, u.wb.p + L.wb_off, L.rows_bwd, L.nt_b,
-                              nullptr, F.t[T_G2], L.cin, L.cin, N, h, w, 0));
+        SALTY_TRY(launch_conv(ctx, u.conv_kind, conv_src(g, L.cout_pad, L.cout_pad), L.cout_pad, u.wb.p + L.wb_off,
+                              L.rows_bwd, L.nt_b, nullptr, F.t[T_G2], L.cin, L.cin, N, h, w, 0));
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;
 }
@@ -767,6 +757,8 @@ salty_status backward(salty_ctx* ctx, Unet& u, Fwd& F, const float* d_target, in
     k_loss<<<gsz(P0), 256, 0, st>>>(F.t[T_OUT], F.t[T_X], d_target, P0, G[G_OUT], u.loss.p);
     const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8, H4 = H / 16, W4 = W / 16;
     const long long P1 = P0 / 4, P2 = P0 / 16, P3 = P0 / 64, P4 = P0 / 256;
+    auto x = [&](int t, int c) { return conv_src(F.t[t], c, c); };
+    auto cat = [&](int coarse, int cc, int skip, int cs) { return conv_src_cat(F.t[coarse], cc, F.t[skip], cs); };
     auto to_f32 = [&](int cs, int off, int c, long long np, float* dst, int acc) {
         k_grad_to_f32<<<gsz(np * c), 256, 0, st>>>(F.t[T_G2], cs, off, c, np, dst, acc);
     };
@@ -776,37 +768,37 @@ salty_status backward(salty_ctx* ctx, Unet& u, Fwd& F, const float* d_target, in
         k_upsample_bwd<<<gsz(np / 4 * cc), 256, 0, st>>>(F.t[T_G2], cc + cs, g_coarse, cc, N, h, w);
         to_f32(cc + cs, cc, cs, np, g_skip, 0);
     };
-    SALTY_TRY(conv_backward(ctx, u, F, 13, T_D0, T_OUT, G[G_OUT], N, H, W, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 13, x(T_D0, 32), T_OUT, G[G_OUT], N, H, W, true));
     to_f32(32, 0, 32, P0, G[G_D0], 0);
-    SALTY_TRY(conv_backward(ctx, u, F, 12, T_C0, T_D0, G[G_D0], N, H, W, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 12, cat(T_D1, 48, T_E0, 32), T_D0, G[G_D0], N, H, W, true));
     split(48, 32, H, W, G[G_D1], G[G_E0]);
-    SALTY_TRY(conv_backward(ctx, u, F, 11, T_C1, T_D1, G[G_D1], N, H1, W1, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 11, cat(T_D2, 64, T_E1, 48), T_D1, G[G_D1], N, H1, W1, true));
     split(64, 48, H1, W1, G[G_D2], G[G_E1]);
-    SALTY_TRY(conv_backward(ctx, u, F, 10, T_C2, T_D2, G[G_D2], N, H2, W2, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 10, cat(T_D3, 80, T_E2, 64), T_D2, G[G_D2], N, H2, W2, true));
     split(80, 64, H2, W2, G[G_D3], G[G_E2]);
-    SALTY_TRY(conv_backward(ctx, u, F, 9, T_C3, T_D3, G[G_D3], N, H3, W3, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 9, cat(T_B, 96, T_E3, 80), T_D3, G[G_D3], N, H3, W3, true));
     split(96, 80, H3, W3, G[G_B], G[G_E3]);
-    SALTY_TRY(conv_backward(ctx, u, F, 8, T_P3, T_B, G[G_B], N, H4, W4, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 8, x(T_P3, 80), T_B, G[G_B], N, H4, W4, true));
     to_f32(80, 0, 80, P4, G[G_P3], 0);
     k_pool_bwd<<<gsz(P4 * 80), 256, 0, st>>>(F.t[T_E3], G[G_P3], G[G_E3], N, H3, W3, 80);
-    SALTY_TRY(conv_backward(ctx, u, F, 7, T_A3, T_E3, G[G_E3], N, H3, W3, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 7, x(T_A3, 80), T_E3, G[G_E3], N, H3, W3, true));
     to_f32(80, 0, 80, P3, G[G_A3], 0);
-    SALTY_TRY(conv_backward(ctx, u, F, 6, T_P2, T_A3, G[G_A3], N, H3, W3, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 6, x(T_P2, 64), T_A3, G[G_A3], N, H3, W3, true));
     to_f32(64, 0, 64, P3, G[G_P2], 0);
     k_pool_bwd<<<gsz(P3 * 64), 256, 0, st>>>(F.t[T_E2], G[G_P2], G[G_E2], N, H2, W2, 64);
-    SALTY_TRY(conv_backward(ctx, u, F, 5, T_A2, T_E2, G[G_E2], N, H2, W2, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 5, x(T_A2, 64), T_E2, G[G_E2], N, H2, W2, true));
     to_f32(64, 0, 64, P2, G[G_A2], 0);
-    SALTY_TRY(conv_backward(ctx, u, F, 4, T_P1, T_A2, G[G_A2], N, H2, W2, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 4, x(T_P1, 48), T_A2, G[G_A2], N, H2, W2, true));
     to_f32(48, 0, 48, P2, G[G_P1], 0);
     k_pool_bwd<<<gsz(P2 * 48), 256, 0, st>>>(F.t[T_E1], G[G_P1], G[G_E1], N, H1, W1, 48);
-    SALTY_TRY(conv_backward(ctx, u, F, 3, T_A1, T_E1, G[G_E1], N, H1, W1, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 3, x(T_A1, 48), T_E1, G[G_E1], N, H1, W1, true));
     to_f32(48, 0, 48, P1, G[G_A1], 0);
-    SALTY_TRY(conv_backward(ctx, u, F, 2, T_P0, T_A1, G[G_A1], N, H1, W1, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 2, x(T_P0, 32), T_A1, G[G_A1], N, H1, W1, true));
     to_f32(32, 0, 32, P1, G[G_P0], 0);
     k_pool_bwd<<<gsz(P1 * 32), 256, 0, st>>>(F.t[T_E0], G[G_P0], G[G_E0], N, H, W, 32);
-    SALTY_TRY(conv_backward(ctx, u, F, 1, T_A0, T_E0, G[G_E0], N, H, W, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 1, x(T_A0, 32), T_E0, G[G_E0], N, H, W, true));
     to_f32(32, 0, 32, P0, G[G_A0], 0);
-    SALTY_TRY(conv_backward(ctx, u, F, 0, T_X, T_A0, G[G_A0], N, H, W, false));
+    SALTY_TRY(conv_backward(ctx, u, F, 0, x(T_X, 16), T_A0, G[G_A0], N, H, W, false));
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     double l = 0.0;
     SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(&l, u.loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
