@@ -31,7 +31,7 @@ LAMBERT, MIRROR, GLASS, GGX, PHONG, PLASTIC = 0, 1, 2, 3, 4, 5
 TRACE_ANY_HIT, TRACE_WATERTIGHT, TRACE_COUNTERS = 1, 2, 4
 PROFILE_COMPAT, PROFILE_PHYSICAL = 0, 1
 TM_NONE, TM_REINHARD, TM_UNCHARTED2, TM_ACES = -1, 0, 1, 2
-CONV_TCGEN05, CONV_MMA_SYNC = 0, 1
+CONV_TCGEN05, CONV_MMA_SYNC, CONV_TCGEN05_CP_ASYNC = 0, 1, 2
 
 
 class SaltyError(RuntimeError):
@@ -638,7 +638,8 @@ class Unet:
             pass
 
     def set_conv_kernel(self, kind: int) -> None:
-        """CONV_TCGEN05 (default) or CONV_MMA_SYNC for the forward / backward-data convolutions."""
+        """CONV_TCGEN05 (default), CONV_TCGEN05_CP_ASYNC or CONV_MMA_SYNC for the forward /
+        backward-data convolutions."""
         self.ctx.check(lib().salty_unet_set_conv_kernel(self.ctx.h, self.h, int(kind)), "unet_set_conv_kernel")
 
     def params(self) -> np.ndarray:

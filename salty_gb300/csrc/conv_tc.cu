@@ -22,6 +22,22 @@
 //
 // Every wait is bounded (2 s of the global timer); a wait that gives up sets
 // status[0] |= 1, skips the rest of the strip, frees the CTA's TMEM and returns.
+//
+// k_conv3x3_tma is the same convolution for inputs held in one tensor, as a persistent,
+// warp-specialised kernel (one CTA per SM looping over strips):
+//   warp 0    one lane issues TMA tensor copies (cp.async.bulk.tensor): per 16-channel
+//             chunk the two halo planes (boxes of 8 channels x 130 pixels x R+2 rows, the
+//             image border zero-filled by the copy engine) and the two weight planes
+//             (8 channels x Npad rows x 9 taps) into a ring of up to 4 stages, each
+//             guarded by a "full" (transaction bytes) and an "empty" (MMAs done) mbarrier
+//   warp 1    one lane issues the MMAs of each chunk and commits them to the stage's
+//             "empty" barrier, and after a strip's last chunk to its accumulator's barrier
+//   warps 2-5 the epilogue: TMEM -> bias, ReLU, BF16 -> global, one warp per TMEM lane
+//             quarter, then release the accumulator
+// Two accumulators of R x Npad columns (512 TMEM columns) let the epilogue of one strip
+// overlap the MMAs of the next.  Waits are bounded as above; a wait that gives up raises
+// a shared abort flag that ends every role's loop.
+#include <cuda.h>  // CUtensorMap and its enums (the encoder is fetched from the driver at run time)
 #include <cuda_bf16.h>
 
 #include <cstdint>
@@ -124,7 +140,7 @@ struct TcConvArgs {
 };
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const TcConvArgs a) {
-    extern __shared__ __align__(128) unsigned char smem[];
+    extern __shared__ __align__(1024) unsigned char smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem);           // [2] chunk buffers consumed
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 16);
     unsigned char* stage0 = smem + kBarBytes;
@@ -254,6 +270,226 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const TcConvArgs a
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTmemCols) : "memory");
 }
 
+// ---------------------------------------------------------------- persistent TMA kernel
+constexpr int kTmaThreads = 192;   // warp 0: TMA, warp 1: MMA, warps 2-5: epilogue
+constexpr int kMaxStages = 4;
+constexpr int kTmaHeader = 2048;   // barriers, TMEM address, abort flag, bias
+constexpr int kTmaMinSmem = 120 * 1024;  // above half an SM's shared memory: one CTA per SM owns all 512 TMEM columns
+
+__host__ __device__ constexpr int tma_plane(int R) { return ((R + 2) * kHaloW * 16 + 127) / 128 * 128; }
+__host__ __device__ constexpr int tma_wplane(int npad) { return 9 * npad * 16; }
+__host__ __device__ constexpr int tma_stage(int R, int npad) { return 2 * tma_plane(R) + 2 * tma_wplane(npad); }
+
+struct TmaConvArgs {
+    int cin, npad, R, cout, relu, out_cs, out_co;
+    int N, H, W, tiles, stages;
+    const float* bias;
+    bf16* out;
+    int* status;
+};
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+        :: "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar) : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        :: "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar) : "memory");
+}
+
+// Bounded wait that also gives up when another role has raised the abort flag.
+__device__ __forceinline__ bool wait_or_abort(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* status) {
+    if (mbar_try(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        if (mbar_try(bar, parity)) return true;
+        if (*abort_flag) return false;
+        if (global_ns() - t0 > kWaitNs) {
+            *abort_flag = 1;
+            atomicOr(status, 1);
+            return false;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTmaThreads, 1)
+k_conv3x3_tma(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_w, const TmaConvArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kMaxStages]
+    uint64_t* empty = full + kMaxStages;                 // [kMaxStages]
+    uint64_t* acc_full = empty + kMaxStages;             // [2]
+    uint64_t* acc_empty = acc_full + 2;                  // [2]
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 128);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 132);
+    float* sbias = reinterpret_cast<float*>(smem + 256);  // [npad]
+    unsigned char* ring = smem + kTmaHeader;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // TMA destinations and the descriptors below assume a 1024-byte aligned base
+    if (saddr(smem) & 1023u) {
+        if (tid == 0) atomicOr(a.status, 2);
+        return;
+    }
+    const int R = a.R, npad = a.npad, S = a.stages;
+    const int plane = tma_plane(R), wplane = tma_wplane(npad), sbytes = tma_stage(R, npad);
+    const uint32_t tx_bytes = 2u * (R + 2) * kHaloW * 16 + 2u * wplane;
+    const int nchunks = a.cin / 16;
+    const int strips_x = (a.W + kStrip - 1) / kStrip, strips_y = (a.H + R - 1) / R;
+    if (tid == 0) {
+        for (int s = 0; s < kMaxStages; ++s) {
+            mbar_init(saddr(full + s), 1);
+            mbar_init(saddr(empty + s), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(saddr(acc_full + b), 1);
+            mbar_init(saddr(acc_empty + b), 4);  // one arrival per epilogue warp
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int i = tid; i < npad; i += kTmaThreads) sbias[i] = (a.bias && i < a.cout) ? a.bias[i] : 0.0f;
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" :: "r"(saddr(tmem_slot)) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            asm volatile("prefetch.tensormap [%0];" :: "l"(reinterpret_cast<uint64_t>(&tm_in)) : "memory");
+            asm volatile("prefetch.tensormap [%0];" :: "l"(reinterpret_cast<uint64_t>(&tm_w)) : "memory");
+            int k = 0;
+            for (int t = blockIdx.x; t < a.tiles; t += gridDim.x) {
+                int tt = t;
+                const int sx = tt % strips_x;
+                tt /= strips_x;
+                const int sy = tt % strips_y;
+                const int n = tt / strips_y;
+                const int x0 = sx * kStrip, y0 = sy * R;
+                bool ok = true;
+                for (int c = 0; c < nchunks; ++c, ++k) {
+                    const int s = k % S;
+                    const uint32_t ph = (uint32_t)(k / S) & 1u;
+                    if (!wait_or_abort(saddr(empty + s), ph ^ 1u, abort_flag, a.status)) { ok = false; break; }
+                    const uint32_t bar = saddr(full + s);
+                    mbar_expect_tx(bar, tx_bytes);
+                    const uint32_t dst = saddr(ring + s * sbytes);
+                    tma_load_4d(dst, &tm_in, c * 16, x0 - 1, y0 - 1, n, bar);
+                    tma_load_4d(dst + plane, &tm_in, c * 16 + 8, x0 - 1, y0 - 1, n, bar);
+                    tma_load_3d(dst + 2 * plane, &tm_w, c * 16, 0, 0, bar);
+                    tma_load_3d(dst + 2 * plane + wplane, &tm_w, c * 16 + 8, 0, 0, bar);
+                }
+                if (!ok) break;
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(kStrip, npad);
+            int k = 0, i = 0;
+            for (int t = blockIdx.x; t < a.tiles; t += gridDim.x, ++i) {
+                const int ab = i & 1;
+                if (!wait_or_abort(saddr(acc_empty + ab), ((uint32_t)(i >> 1) & 1u) ^ 1u, abort_flag, a.status)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t d0 = tmem + (uint32_t)ab * 256u;
+                bool ok = true;
+                for (int c = 0; c < nchunks; ++c, ++k) {
+                    const int s = k % S;
+                    if (!wait_or_abort(saddr(full + s), (uint32_t)(k / S) & 1u, abort_flag, a.status)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t hs = saddr(ring + s * sbytes), ws = hs + 2 * plane;
+                    for (int tap = 0; tap < 9; ++tap) {
+                        const int ky = tap / 3, kx = tap - ky * 3;
+                        const uint64_t bd = sdesc(ws + tap * npad * 16, (uint32_t)wplane, 128);
+                        for (int r = 0; r < R; ++r) {
+                            const uint64_t ad = sdesc(hs + ((r + ky) * kHaloW + kx) * 16, (uint32_t)plane, 128);
+                            umma_bf16(d0 + r * npad, ad, bd, idesc, (c > 0 || tap > 0) ? 1u : 0u);
+                        }
+                    }
+                    umma_commit(saddr(empty + s));
+                }
+                if (!ok) break;
+                umma_commit(saddr(acc_full + ab));
+            }
+        }
+    } else {
+        const int q = warp & 3;  // this warp's TMEM lane quarter
+        int i = 0;
+        for (int t = blockIdx.x; t < a.tiles; t += gridDim.x, ++i) {
+            const int ab = i & 1;
+            const bool got = wait_or_abort(saddr(acc_full + ab), (uint32_t)(i >> 1) & 1u, abort_flag, a.status);
+            if (!__all_sync(0xffffffffu, got)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            int tt = t;
+            const int sx = tt % strips_x;
+            tt /= strips_x;
+            const int sy = tt % strips_y;
+            const int n = tt / strips_y;
+            const int x = sx * kStrip + q * 32 + lane;
+            for (int r = 0; r < R; ++r) {
+                const int y = sy * R + r;
+                for (int j = 0; j < npad / 16; ++j) {
+                    uint32_t v[16];
+                    tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)ab * 256u + r * npad + j * 16, v);
+                    if (y >= a.H || x >= a.W) continue;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int co = j * 16 + h * 8;
+                        if (co >= a.cout) continue;
+                        uint32_t pk[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            float v0 = __uint_as_float(v[h * 8 + 2 * e]) + sbias[co + 2 * e];
+                            float v1 = __uint_as_float(v[h * 8 + 2 * e + 1]) + sbias[co + 2 * e + 1];
+                            if (a.relu) { v0 = fmaxf(v0, 0.0f); v1 = fmaxf(v1, 0.0f); }
+                            const __nv_bfloat162 p2 = __floats2bfloat162_rn(v0, v1);
+                            pk[e] = *reinterpret_cast<const uint32_t*>(&p2);
+                        }
+                        *reinterpret_cast<uint4*>(a.out + (((size_t)n * a.H + y) * a.W + x) * a.out_cs + a.out_co + co) =
+                            make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(saddr(acc_empty + ab));
+        }
+    }
+    __syncthreads();
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" :: "r"(tmem) : "memory");
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn tensor_map_encoder() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
 }  // namespace
 
 // Image rows per strip for an output width of npad channels: R x npad accumulator columns
@@ -276,6 +512,50 @@ salty_status conv3x3_tc(salty_ctx* ctx, const ConvSrc& in, int cin, const bf16* 
     const long long tiles = (long long)N * ((H + R - 1) / R) * ((W + kStrip - 1) / kStrip);
     TcConvArgs a{in, cin, wt, wrows, bias, out, out_cs, out_co, cout, npad, R, N, H, W, relu, d_status};
     k_conv3x3_tc<<<(unsigned)tiles, kTcThreads, smem, ctx->stream>>>(a);
+    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    return SALTY_OK;
+}
+
+salty_status conv3x3_tma(salty_ctx* ctx, const bf16* in, int in_cs, int cin, const bf16* wt, int wrows,
+                         const float* bias, bf16* out, int out_cs, int out_co, int cout, int N, int H, int W, int relu,
+                         int* d_status) {
+    const int npad = (cout + 15) / 16 * 16;
+    if (cin % 16 || cin <= 0 || cin > in_cs || in_cs % 8 || npad > 256 || npad < 16 || cout % 8 || out_cs % 8 ||
+        out_co % 8 || wrows < 1 || wrows > 256 || reinterpret_cast<uintptr_t>(in) % 16 ||
+        reinterpret_cast<uintptr_t>(wt) % 16)
+        return ctx->err.fail(SALTY_ERR_INVALID_ARG, "conv3x3_tma: unsupported shape (cin %d, cout %d)", cin, cout);
+    EncodeTiledFn enc = tensor_map_encoder();
+    if (!enc) return ctx->err.fail(SALTY_ERR_CUDA, "conv3x3_tma: cuTensorMapEncodeTiled is not available");
+    const int R = conv_tc_rows(cout);
+    const int sbytes = tma_stage(R, npad);
+    int S = (int)((227 * 1024 - kTmaHeader) / sbytes);
+    if (S > kMaxStages) S = kMaxStages;
+    if (S < 2) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "conv3x3_tma: stage too large");
+    size_t smem = (size_t)kTmaHeader + (size_t)S * sbytes;
+    if (smem < (size_t)kTmaMinSmem) smem = kTmaMinSmem;
+    // input: 4-D (channels, x, y, image), boxes of 8 channels x 130 pixels x R + 2 rows
+    CUtensorMap tm_in, tm_w;
+    const cuuint64_t gdim[4] = {(cuuint64_t)in_cs, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+    const cuuint64_t gstride[3] = {(cuuint64_t)in_cs * 2, (cuuint64_t)W * in_cs * 2, (cuuint64_t)H * W * in_cs * 2};
+    const cuuint32_t box[4] = {8, (cuuint32_t)kHaloW, (cuuint32_t)(R + 2), 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    if (enc(&tm_in, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(in), gdim, gstride, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return ctx->err.fail(SALTY_ERR_CUDA, "conv3x3_tma: input tensor map");
+    // weights: 3-D (input channel, row, tap), boxes of 8 channels x npad rows x 9 taps
+    const cuuint64_t wdim[3] = {(cuuint64_t)cin, (cuuint64_t)wrows, 9};
+    const cuuint64_t wstride[2] = {(cuuint64_t)cin * 2, (cuuint64_t)wrows * cin * 2};
+    const cuuint32_t wbox[3] = {8, (cuuint32_t)npad, 9};
+    if (enc(&tm_w, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16*>(wt), wdim, wstride, wbox, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return ctx->err.fail(SALTY_ERR_CUDA, "conv3x3_tma: weight tensor map");
+    SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(k_conv3x3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long tiles = (long long)N * ((H + R - 1) / R) * ((W + kStrip - 1) / kStrip);
+    const int grid = (int)(tiles < ctx->num_sms ? tiles : ctx->num_sms);
+    TmaConvArgs a{cin, npad, R, cout, relu, out_cs, out_co, N, H, W, (int)tiles, S, bias, out, d_status};
+    k_conv3x3_tma<<<grid, kTmaThreads, smem, ctx->stream>>>(tm_in, tm_w, a);
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;
 }

@@ -20,8 +20,10 @@
 //                 of the shifted input into fragments with pixels along K; each CTA sums its
 //                 pixel tiles in registers and adds the partial into FP32 gradients.
 // The forward and backward-data convolutions run by default on tcgen05 (conv_tc.cu: TMEM
-// accumulators, 128-pixel strips); the mma.sync kernel below stays selectable
-// (salty_unet_set_conv_kernel) and is the reference the tcgen05 kernel is tested against.
+// accumulators, 128-pixel strips; inputs in one tensor staged by TMA in a persistent
+// warp-specialised kernel, the decoder's two-source inputs by cp.async); the mma.sync kernel
+// below stays selectable (salty_unet_set_conv_kernel) and is the reference the tcgen05
+// kernels are tested against.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -614,7 +616,10 @@ void init_layers(Unet& u) {
 
 salty_status launch_conv(salty_ctx* ctx, int kind, const ConvSrc& in, int cin, const bf16* w, int rows, int nt,
                          const float* bias, bf16* out, int out_cs, int cout, int N, int H, int W, int relu) {
-    if (kind == SALTY_CONV_TCGEN05)
+    if (kind == SALTY_CONV_TCGEN05 && in.a_shift == 0 && in.a_ch >= cin && rows <= 256)
+        return conv3x3_tma(ctx, in.a, in.a_cs, cin, w, rows, bias, out, out_cs, 0, cout, N, H, W, relu,
+                           ctx->status.p + 8);
+    if (kind == SALTY_CONV_TCGEN05 || kind == SALTY_CONV_TCGEN05_CP_ASYNC)
         return conv3x3_tc(ctx, in, cin, w, rows, bias, out, out_cs, 0, cout, N, H, W, relu, ctx->status.p + 8);
     const int tiles = N * ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
     dim3 grid(tiles, rows / (nt * 8));
@@ -828,7 +833,8 @@ salty_status conv_status_reset(salty_ctx* ctx) {
 salty_status conv_status_check(salty_ctx* ctx) {
     int s = 0;
     SALTY_TRY_CUDA(ctx->err, cudaMemcpy(&s, ctx->status.p + 8, sizeof(int), cudaMemcpyDeviceToHost));
-    if (s) return ctx->err.fail(SALTY_ERR_TIMEOUT, "unet: a tensor-core convolution gave up waiting for its MMAs");
+    if (s & 1) return ctx->err.fail(SALTY_ERR_TIMEOUT, "unet: a tensor-core convolution gave up waiting");
+    if (s) return ctx->err.fail(SALTY_ERR_CUDA, "unet: a tensor-core convolution found its shared memory misaligned");
     return SALTY_OK;
 }
 
@@ -1051,7 +1057,7 @@ salty_status salty_denoise_unet_ensemble(salty_ctx* ctx, salty_unet* net, salty_
 
 salty_status salty_unet_set_conv_kernel(salty_ctx* ctx, salty_unet* net, int32_t kind) {
     if (!ctx || !net) return SALTY_ERR_INVALID_ARG;
-    if (kind != SALTY_CONV_TCGEN05 && kind != SALTY_CONV_MMA_SYNC)
+    if (kind != SALTY_CONV_TCGEN05 && kind != SALTY_CONV_MMA_SYNC && kind != SALTY_CONV_TCGEN05_CP_ASYNC)
         return ctx->err.fail(SALTY_ERR_INVALID_ARG, "unknown convolution kernel %d", (int)kind);
     net->net.conv_kind = kind;
     return SALTY_OK;

@@ -43,5 +43,10 @@ int conv_tc_rows(int cout);
 salty_status conv3x3_tc(salty_ctx* ctx, const ConvSrc& in, int cin, const __nv_bfloat16* wt, int wrows,
                         const float* bias, __nv_bfloat16* out, int out_cs, int out_co, int cout, int N, int H, int W,
                         int relu, int* d_status);
+// The same for an input held in one tensor [N][H][W][in_cs] (16-byte aligned), by TMA in a
+// persistent warp-specialised kernel; wrows <= 256.
+salty_status conv3x3_tma(salty_ctx* ctx, const __nv_bfloat16* in, int in_cs, int cin, const __nv_bfloat16* wt,
+                         int wrows, const float* bias, __nv_bfloat16* out, int out_cs, int out_co, int cout, int N,
+                         int H, int W, int relu, int* d_status);
 
 }  // namespace salty

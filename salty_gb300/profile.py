@@ -1,7 +1,7 @@
 """Small fixed workloads for profiling the kernels (run them under ncu or alone).
 
     python -m salty_gb300.profile render [--spp 1] [--frames 2]   1080p heightfield frames
-    python -m salty_gb300.profile unet [--n 1 --h 1088 --w 1920] [--conv tcgen05|mma_sync|both]
+    python -m salty_gb300.profile unet [--n 1 --h 1088 --w 1920] [--conv tcgen05|tcgen05_cp_async|mma_sync|all]
                                                                      denoiser forward passes
     python -m salty_gb300.profile trace-sweep                        traversal launch shapes
     python -m salty_gb300.profile cornell                            the 256^2 Cornell box, 16 spp
@@ -54,17 +54,19 @@ def unet(n: int, h: int, w: int, conv: str = "tcgen05", train: bool = False) -> 
     """Forward passes (and, with train, training steps at lr 0) on random features: the
     best of 5 wall-clock times after a warm-up, per convolution kernel."""
     import torch
-    from . import CONV_MMA_SYNC, CONV_TCGEN05
+    from . import CONV_MMA_SYNC, CONV_TCGEN05, CONV_TCGEN05_CP_ASYNC
     ctx = Context(0)
     net = Unet(ctx, seed=1)
     f = torch.rand((n, h, w, UNET_FEATURES), device="cuda")
     o = torch.empty((n, h, w, 3), device="cuda")
     tgt = torch.rand((n, h, w, 3), device="cuda")
-    kinds = {"tcgen05": [CONV_TCGEN05], "mma_sync": [CONV_MMA_SYNC], "both": [CONV_TCGEN05, CONV_MMA_SYNC]}[conv]
+    names = {CONV_TCGEN05: "tcgen05", CONV_TCGEN05_CP_ASYNC: "tcgen05_cp_async", CONV_MMA_SYNC: "mma_sync"}
+    kinds = {"tcgen05": [CONV_TCGEN05], "tcgen05_cp_async": [CONV_TCGEN05_CP_ASYNC], "mma_sync": [CONV_MMA_SYNC],
+             "all": [CONV_TCGEN05, CONV_TCGEN05_CP_ASYNC, CONV_MMA_SYNC]}[conv]
     res = {"workload": f"U-Net {n}x{h}x{w}"}
     for k in kinds:
         net.set_conv_kernel(k)
-        name = "tcgen05" if k == CONV_TCGEN05 else "mma_sync"
+        name = names[k]
         steps = [("forward_ms", lambda: net.forward(f, out=o))]
         if train:
             steps.append(("train_step_ms", lambda: net.train_step(f, tgt, lr=0.0)))
@@ -113,7 +115,7 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=1)
     ap.add_argument("--h", type=int, default=1088)
     ap.add_argument("--w", type=int, default=1920)
-    ap.add_argument("--conv", default="tcgen05", choices=["tcgen05", "mma_sync", "both"])
+    ap.add_argument("--conv", default="tcgen05", choices=["tcgen05", "tcgen05_cp_async", "mma_sync", "all"])
     ap.add_argument("--train", action="store_true", help="unet: also time training steps")
     a = ap.parse_args(argv)
     if a.what == "render":

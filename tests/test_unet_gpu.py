@@ -147,16 +147,17 @@ def test_training_checkpoint_resumes_exactly(ctx, tmp_path):
         n.close()
 
 
-@pytest.mark.parametrize("kind", ["tcgen05", "mma_sync"])
-def test_both_conv_kernels_match_oracle_on_ragged_strips(ctx, kind):
+@pytest.mark.parametrize("kind", ["tcgen05", "tcgen05_cp_async", "mma_sync"])
+def test_conv_kernels_match_oracle_on_ragged_strips(ctx, kind):
     """1 x 48 x 272 pixels: the tensor-core kernel's 128-pixel strips end ragged (272 =
     2 x 128 + 16) and its row groups (8, 5, 4, 3 or 2 rows by channel count) do not divide
     the level heights 48, 24, 12, 6, 3; forward output and every layer's gradients against
-    the oracle, for both convolution kernels."""
+    the oracle, for every convolution kernel."""
     import salty_gb300
     from oracle.unet_oracle import LAYERS, UnetOracle
     net = salty_gb300.Unet(ctx, seed=12)
-    net.set_conv_kernel(salty_gb300.CONV_TCGEN05 if kind == "tcgen05" else salty_gb300.CONV_MMA_SYNC)
+    net.set_conv_kernel({"tcgen05": salty_gb300.CONV_TCGEN05, "tcgen05_cp_async": salty_gb300.CONV_TCGEN05_CP_ASYNC,
+                         "mma_sync": salty_gb300.CONV_MMA_SYNC}[kind])
     f, t = _batch(8, n=1, h=48, w=272)
     p0 = net.params()
     orc = UnetOracle(p0)
@@ -178,13 +179,14 @@ def test_both_conv_kernels_match_oracle_on_ragged_strips(ctx, kind):
 
 
 def test_tcgen05_and_mma_sync_agree(ctx):
-    """The two convolution kernels on a 2 x 144 x 400 batch: same outputs and gradients up to
-    the order of the FP32 sums (a BF16 rounding step now and then)."""
+    """The convolution kernels on a 2 x 144 x 400 batch: same outputs and gradients up to the
+    order of the FP32 sums (a BF16 rounding step now and then); the two tcgen05 variants run
+    the same MMAs in the same order, so they agree bit for bit."""
     import salty_gb300
     net = salty_gb300.Unet(ctx, seed=13)
     f, t = _batch(9, n=2, h=144, w=400)
     res = {}
-    for kind in (salty_gb300.CONV_MMA_SYNC, salty_gb300.CONV_TCGEN05):
+    for kind in (salty_gb300.CONV_MMA_SYNC, salty_gb300.CONV_TCGEN05, salty_gb300.CONV_TCGEN05_CP_ASYNC):
         net.set_conv_kernel(kind)
         out = net.forward(f)
         loss = net.train_step(f, t, lr=0.0)
@@ -194,6 +196,7 @@ def test_tcgen05_and_mma_sync_agree(ctx):
     assert abs(l2 / l1 - 1) < 1e-3, (l1, l2)
     cos = g1 @ g2 / (np.linalg.norm(g1) * np.linalg.norm(g2))
     assert _rel(g2, g1) < 0.02 and cos > 0.9995, (_rel(g2, g1), cos)
+    np.testing.assert_array_equal(res[salty_gb300.CONV_TCGEN05_CP_ASYNC][0], o2)
     with pytest.raises(salty_gb300.SaltyError):
         net.set_conv_kernel(7)
     net.close()
