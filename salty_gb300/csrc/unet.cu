@@ -17,8 +17,9 @@
 //                 in shared memory; A fragments come from it, B fragments from the weights.
 //   backward data the same kernel on dY with the weights flipped and transposed.
 //   backward wts  M = Cout, N = Cin, K = pixels: ldmatrix.trans turns the NHWC tiles of dY and
-//                 of the shifted input into fragments with pixels along K; each CTA sums its
-//                 pixel tiles in registers and adds the partial into FP32 gradients.
+//                 of the shifted input into fragments with pixels along K; a CTA covers all
+//                 nine taps of a 16-channel input slice (one dY fragment serves nine taps),
+//                 sums its pixel tiles in registers and adds the partial into FP32 gradients.
 // The forward and backward-data convolutions run by default on tcgen05 (conv_tc.cu: TMEM
 // accumulators, 128-pixel strips; inputs in one tensor staged by TMA in a persistent
 // warp-specialised kernel, the decoder's two-source inputs by cp.async); the mma.sync kernel
@@ -26,6 +27,7 @@
 // kernels are tested against.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -175,32 +177,38 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const ConvSrc in, int 
 }
 
 // ---------------------------------------------------------------- conv3x3 backward weights
-// dW[tap][co][ci] += sum_p dY[p][co] * X[p + (ky-1, kx-1)][ci] for one tap (blockIdx.y) and a
-// 16-wide input-channel slice (blockIdx.z); CTAs stride over 8x16 pixel tiles (blockIdx.x).
-// dY: [N][H][W][dy_cs] with Cpad = dy_cs channels (multiple of 16, zero beyond the layer's
-// real outputs); rows co >= cout_real are not written.  X: the layer's input (ConvSrc),
+// dW[tap][co][ci] += sum_p dY[p][co] * X[p + (ky-1, kx-1)][ci] for all nine taps, a group of
+// up to four 16-row output-channel tiles (blockIdx.y; warp w takes tile 4 * blockIdx.y + w)
+// and a 16-wide input-channel slice (blockIdx.z); CTAs stride over 8x16 pixel tiles
+// (blockIdx.x).  Per tile the CTA stages its dY columns and the X halo once; per 16-pixel
+// k-step a warp loads its dY^T fragment once and reuses it for the nine taps' X fragments,
+// keeping 9 x 2 accumulator tiles in registers until the end, then adds them into the FP32
+// gradients.  dY: [N][H][W][Cpad] (Cpad multiple of 16, zero beyond the layer's real
+// outputs); rows co >= cout_real are not written.  X: the layer's input (ConvSrc),
 // Cin % 16 == 0.
+constexpr int kWgradCo = 64;  // output channels per CTA (4 warps x 16)
 __global__ void __launch_bounds__(kConvThreads) k_conv3x3_wgrad(const bf16* __restrict__ dy, int Cpad, int cout_real,
                                                                 const ConvSrc x, int Cin, float* __restrict__ dw,
                                                                 int N, int H, int W) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int dstride = Cpad + 8;
+    constexpr int dstride = kWgradCo + 8;
     constexpr int xstride = 16 + 8;
     bf16* dys = reinterpret_cast<bf16*>(smem_raw);         // [128][dstride]
     bf16* xs = dys + kTileX * kTileY * dstride;            // [10*18][xstride]
-    const int tap = blockIdx.y, ky = tap / 3, kx = tap % 3;
+    const int co0 = blockIdx.y * kWgradCo;
     const int ci0 = blockIdx.z * 16;
+    const int cw = min(kWgradCo, Cpad - co0);             // this CTA's output channels (multiple of 16)
     const int tiles_x = (W + kTileX - 1) / kTileX, tiles_y = (H + kTileY - 1) / kTileY;
     const int ntiles = N * tiles_x * tiles_y;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int mtiles = Cpad / 16;
-    float acc[2][2][4];
+    const bool active = warp * 16 < cw;
+    float acc[9][2][4];
 #pragma unroll
-    for (int a = 0; a < 2; ++a)
+    for (int t = 0; t < 9; ++t)
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int k = 0; k < 4; ++k) acc[a][j][k] = 0.0f;
+            for (int k = 0; k < 4; ++k) acc[t][j][k] = 0.0f;
     const int kk = lane & 7, which = lane >> 3;  // ldmatrix: row within matrix, matrix index
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         int tt = t;
@@ -210,12 +218,13 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_wgrad(const bf16* __re
         const int n = tt / tiles_y;
         const int x0 = tx * kTileX, y0 = ty * kTileY;
         __syncthreads();
-        const int dchunks = Cpad / 8;
+        const int dchunks = cw / 8;
         for (int i = threadIdx.x; i < kTileX * kTileY * dchunks; i += kConvThreads) {
             const int pix = i / dchunks, c = i % dchunks;
             const int gy = y0 + pix / kTileX, gx = x0 + pix % kTileX;
             uint4 v = make_uint4(0, 0, 0, 0);
-            if (gy < H && gx < W) v = *reinterpret_cast<const uint4*>(dy + (((size_t)n * H + gy) * W + gx) * Cpad + c * 8);
+            if (gy < H && gx < W)
+                v = __ldg(reinterpret_cast<const uint4*>(dy + (((size_t)n * H + gy) * W + gx) * Cpad + co0 + c * 8));
             *reinterpret_cast<uint4*>(dys + pix * dstride + c * 8) = v;
         }
         for (int i = threadIdx.x; i < kHaloX * kHaloY * 2; i += kConvThreads) {
@@ -227,55 +236,74 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_wgrad(const bf16* __re
             *reinterpret_cast<uint4*>(xs + pix * xstride + c * 8) = v;
         }
         __syncthreads();
+        if (!active) continue;
         // K = the tile's 128 pixels in 8 steps of 16 (one tile row each)
+#pragma unroll 1
         for (int s = 0; s < kTileY; ++s) {
-            // B: pixels (row s, cols 0..15) shifted by the tap x 16 input channels.  Matrices:
-            // 0 = (px 0-7, ci 0-7), 1 = (px 8-15, ci 0-7), 2 = (px 0-7, ci 8-15), 3 = (px 8-15, ci 8-15)
-            unsigned bq[4];
+            // A: output channels (rows) x pixels (k).  Matrices: 0 = (co 0-7, px 0-7),
+            // 1 = (co 8-15, px 0-7), 2 = (co 0-7, px 8-15), 3 = (co 8-15, px 8-15)
+            unsigned a[4];
             {
+                const int px = kk + ((which & 2) ? 8 : 0);
+                const int co = warp * 16 + ((which & 1) ? 8 : 0);
+                ldmatrix_x4_trans(a, dys + (s * kTileX + px) * dstride + co);
+            }
+#pragma unroll
+            for (int tap = 0; tap < 9; ++tap) {
+                const int ky = tap / 3, kx = tap % 3;
+                // B: pixels (row s, cols 0..15) shifted by the tap x 16 input channels.  Matrices:
+                // 0 = (px 0-7, ci 0-7), 1 = (px 8-15, ci 0-7), 2 = (px 0-7, ci 8-15), 3 = (px 8-15, ci 8-15)
+                unsigned bq[4];
                 const int px = kk + ((which & 1) ? 8 : 0);
                 const int cc = (which & 2) ? 8 : 0;
                 ldmatrix_x4_trans(bq, xs + ((s + ky) * kHaloX + px + kx) * xstride + cc);
-            }
-            for (int mi = 0; mi < 2; ++mi) {
-                const int mt = warp + 4 * mi;
-                if (mt >= mtiles) break;
-                // A: output channels (rows) x pixels (k).  Matrices: 0 = (co 0-7, px 0-7),
-                // 1 = (co 8-15, px 0-7), 2 = (co 0-7, px 8-15), 3 = (co 8-15, px 8-15)
-                unsigned a[4];
-                {
-                    const int px = kk + ((which & 2) ? 8 : 0);
-                    const int co = mt * 16 + ((which & 1) ? 8 : 0);
-                    ldmatrix_x4_trans(a, dys + (s * kTileX + px) * dstride + co);
-                }
-                mma_bf16(acc[mi][0], a, bq[0], bq[1]);
-                mma_bf16(acc[mi][1], a, bq[2], bq[3]);
+                mma_bf16(acc[tap][0], a, bq[0], bq[1]);
+                mma_bf16(acc[tap][1], a, bq[2], bq[3]);
             }
         }
     }
+    if (!active) return;
     const int g = lane >> 2, tq = lane & 3;
-    for (int mi = 0; mi < 2; ++mi) {
-        const int mt = warp + 4 * mi;
-        if (mt >= mtiles) break;
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap)
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
             const int ci = ci0 + j * 8 + 2 * tq;
-            const int co0 = mt * 16 + g, co1 = co0 + 8;
-            if (co0 < cout_real) {
-                float* r0 = dw + ((size_t)tap * cout_real + co0) * Cin + ci;
-                atomicAdd(r0, acc[mi][j][0]);
-                atomicAdd(r0 + 1, acc[mi][j][1]);
+            const int c0 = co0 + warp * 16 + g, c1 = c0 + 8;
+            if (c0 < cout_real) {
+                float* r0 = dw + ((size_t)tap * cout_real + c0) * Cin + ci;
+                atomicAdd(r0, acc[tap][j][0]);
+                atomicAdd(r0 + 1, acc[tap][j][1]);
             }
-            if (co1 < cout_real) {
-                float* r1 = dw + ((size_t)tap * cout_real + co1) * Cin + ci;
-                atomicAdd(r1, acc[mi][j][2]);
-                atomicAdd(r1 + 1, acc[mi][j][3]);
+            if (c1 < cout_real) {
+                float* r1 = dw + ((size_t)tap * cout_real + c1) * Cin + ci;
+                atomicAdd(r1, acc[tap][j][2]);
+                atomicAdd(r1 + 1, acc[tap][j][3]);
             }
         }
-    }
 }
 
 // ---------------------------------------------------------------- elementwise / layout
+// Packs 8 floats into 8 BF16 (round to nearest) in one 16-byte word.
+__device__ __forceinline__ uint4 pack_bf16x8(const float (&v)[8]) {
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+        w[k] = *reinterpret_cast<const uint32_t*>(&h);
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+__device__ __forceinline__ void unpack_bf16x8(uint4 q, float (&v)[8]) {
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float2 f = __bfloat1622float2(h[k]);
+        v[2 * k] = f.x;
+        v[2 * k + 1] = f.y;
+    }
+}
+
 // features (kFeatures floats per pixel: colour, albedo, normal, 1/(1+t), noise level)
 // -> 16-channel BF16 input, colour as log(1 + colour)
 __global__ void k_prep_input(const float* __restrict__ f, long long npx, bf16* __restrict__ x) {
@@ -327,27 +355,48 @@ __global__ void k_pool(const bf16* __restrict__ in, bf16* __restrict__ out, int 
     }
 }
 
-// max-pool backward: the gradient goes to the first input equal to the max (ties: first)
+// max-pool backward: the gradient goes to the first input equal to the max (ties: first).
+// One thread per output pixel and 8 channels (C % 8 == 0); din += at the chosen inputs.
 __global__ void k_pool_bwd(const bf16* __restrict__ in, const float* __restrict__ dout, float* __restrict__ din, int N,
                            int H, int W, int C) {
-    const int Ho = H / 2, Wo = W / 2;
-    const long long total = (long long)N * Ho * Wo * C;
+    const int Ho = H / 2, Wo = W / 2, G = C / 8;
+    const long long total = (long long)N * Ho * Wo * G;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        long long p = i / C;
+        const int c = (int)(i % G) * 8;
+        long long p = i / G;
+        const long long po = p;
         const int xo = (int)(p % Wo);
         p /= Wo;
         const int yo = (int)(p % Ho);
         const int n = (int)(p / Ho);
         const size_t base = (((size_t)n * H + 2 * yo) * W + 2 * xo) * C + c;
         const size_t off[4] = {0, (size_t)C, (size_t)W * C, (size_t)W * C + C};
-        float m = -INFINITY;
-        int arg = 0;
-        for (int k = 0; k < 4; ++k) {
-            float v = __bfloat162float(in[base + off[k]]);
-            if (v > m) { m = v; arg = k; }
+        float m[8], v[4][8];
+        int arg[8];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) unpack_bf16x8(__ldg(reinterpret_cast<const uint4*>(in + base + off[k])), v[k]);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            m[e] = -INFINITY;
+            arg[e] = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (v[k][e] > m[e]) { m[e] = v[k][e]; arg[e] = k; }
         }
-        din[base + off[arg]] += dout[i];
+        const float4* dp = reinterpret_cast<const float4*>(dout + po * C + c);
+        const float4 d0 = __ldg(dp), d1 = __ldg(dp + 1);
+        const float d[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            float4* q = reinterpret_cast<float4*>(din + base + off[k]);
+            float4 a = q[0], b = q[1];
+            a.x += arg[0] == k ? d[0] : 0.0f; a.y += arg[1] == k ? d[1] : 0.0f;
+            a.z += arg[2] == k ? d[2] : 0.0f; a.w += arg[3] == k ? d[3] : 0.0f;
+            b.x += arg[4] == k ? d[4] : 0.0f; b.y += arg[5] == k ? d[5] : 0.0f;
+            b.z += arg[6] == k ? d[6] : 0.0f; b.w += arg[7] == k ? d[7] : 0.0f;
+            q[0] = a;
+            q[1] = b;
+        }
     }
 }
 
@@ -402,63 +451,108 @@ __global__ void k_output(const bf16* __restrict__ out, const bf16* __restrict__ 
 }
 
 // ReLU backward on a layer's output y: g = dy * (y > 0) in BF16 (the next GEMMs' operand),
-// with g_cs >= C channels per pixel, the extra ones zero.
+// with g_cs >= C channels per pixel, the extra ones zero.  One thread per pixel and 8
+// channels (C, y_cs, g_cs multiples of 8).
 __global__ void k_relu_bwd(const bf16* __restrict__ y, int y_cs, const float* __restrict__ dy, int C, int relu,
                            long long npx, bf16* __restrict__ g, int g_cs) {
-    const long long total = npx * g_cs;
+    const int G = g_cs / 8;
+    const long long total = npx * G;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const long long p = i / g_cs;
-        const int c = (int)(i % g_cs);
-        float v = 0.0f;
+        const long long p = i / G;
+        const int c = (int)(i % G) * 8;
+        float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         if (c < C) {
-            v = dy[p * C + c];
-            if (relu && !(__bfloat162float(y[p * y_cs + c]) > 0.0f)) v = 0.0f;
+            const float4* d = reinterpret_cast<const float4*>(dy + p * C + c);
+            const float4 a = __ldg(d), b = __ldg(d + 1);
+            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+            if (relu) {
+                float yv[8];
+                unpack_bf16x8(__ldg(reinterpret_cast<const uint4*>(y + p * y_cs + c)), yv);
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (!(yv[k] > 0.0f)) v[k] = 0.0f;
+            }
         }
-        g[i] = __float2bfloat16(v);
+        *reinterpret_cast<uint4*>(g + p * g_cs + c) = pack_bf16x8(v);
     }
 }
 
-// bias gradient: db[c] += sum_p g[p][c] for c < C (g has g_cs channels per pixel)
+// bias gradient: db[c] += sum_p g[p][c] for c < C (g has g_cs channels per pixel).  A
+// block of 256 threads takes 8-channel groups j = threadIdx.x % G of the pixels
+// threadIdx.x / G, (threadIdx.x / G) + 256 / G, ... of its pixel range (threads beyond a
+// multiple of G idle), sums in registers, then once into shared and global memory.
 __global__ void k_bias_grad(const bf16* __restrict__ g, int g_cs, int C, long long npx, float* __restrict__ db) {
     extern __shared__ float sb[];
+    const int G = C / 8, lanes = (blockDim.x / G) * G, per = blockDim.x / G;
     for (int c = threadIdx.x; c < C; c += blockDim.x) sb[c] = 0.0f;
     __syncthreads();
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx * C; i += (long long)gridDim.x * blockDim.x)
-        atomicAdd(&sb[i % C], __bfloat162float(g[(i / C) * g_cs + i % C]));
+    if ((int)threadIdx.x < lanes) {
+        const int j = threadIdx.x % G;
+        float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (long long p = (long long)blockIdx.x * per + threadIdx.x / G; p < npx; p += (long long)gridDim.x * per) {
+            float v[8];
+            unpack_bf16x8(__ldg(reinterpret_cast<const uint4*>(g + p * g_cs + j * 8)), v);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) s[k] += v[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) atomicAdd(&sb[j * 8 + k], s[k]);
+    }
     __syncthreads();
     for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&db[c], sb[c]);
 }
 
 // BF16 activation gradient (from a backward-data GEMM) -> FP32, optionally accumulated;
 // channels [off, off + C) of src [npx][Cs]
+// (one thread per pixel and 8 channels; Cs, off, C multiples of 8)
 __global__ void k_grad_to_f32(const bf16* __restrict__ src, int Cs, int off, int C, long long npx, float* __restrict__ dst,
                               int accumulate) {
-    const long long total = npx * C;
+    const int G = C / 8;
+    const long long total = npx * G;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const long long p = i / C;
-        const int c = (int)(i % C);
-        const float v = __bfloat162float(src[p * Cs + off + c]);
-        dst[i] = accumulate ? dst[i] + v : v;
+        const long long p = i / G;
+        const int c = (int)(i % G) * 8;
+        float v[8];
+        unpack_bf16x8(__ldg(reinterpret_cast<const uint4*>(src + p * Cs + off + c)), v);
+        float4* d = reinterpret_cast<float4*>(dst + p * C + c);
+        float4 a = make_float4(v[0], v[1], v[2], v[3]), b = make_float4(v[4], v[5], v[6], v[7]);
+        if (accumulate) {
+            const float4 a0 = d[0], b0 = d[1];
+            a.x += a0.x; a.y += a0.y; a.z += a0.z; a.w += a0.w;
+            b.x += b0.x; b.y += b0.y; b.z += b0.z; b.w += b0.w;
+        }
+        d[0] = a;
+        d[1] = b;
     }
 }
 
 // up-sampling backward: coarse grad = sum of its 2x2 children's grads (channels [0, Cc) of dcat)
+// (one thread per coarse pixel and 8 channels; Ccat, Cc multiples of 8)
 __global__ void k_upsample_bwd(const bf16* __restrict__ dcat, int Ccat, float* __restrict__ dcoarse, int Cc, int N,
                                int H, int W) {
-    const int Hc = H / 2, Wc = W / 2;
-    const long long total = (long long)N * Hc * Wc * Cc;
+    const int Hc = H / 2, Wc = W / 2, G = Cc / 8;
+    const long long total = (long long)N * Hc * Wc * G;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % Cc);
-        long long p = i / Cc;
+        const int c = (int)(i % G) * 8;
+        long long p = i / G;
+        const long long pc = p;
         const int x = (int)(p % Wc);
         p /= Wc;
         const int y = (int)(p % Hc);
         const int n = (int)(p / Hc);
-        float s = 0.0f;
+        float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int dy = 0; dy < 2; ++dy)
-            for (int dx = 0; dx < 2; ++dx)
-                s += __bfloat162float(dcat[(((size_t)n * H + 2 * y + dy) * W + 2 * x + dx) * Ccat + c]);
-        dcoarse[i] = s;
+            for (int dx = 0; dx < 2; ++dx) {
+                float v[8];
+                unpack_bf16x8(__ldg(reinterpret_cast<const uint4*>(
+                                  dcat + (((size_t)n * H + 2 * y + dy) * W + 2 * x + dx) * Ccat + c)),
+                              v);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) s[k] += v[k];
+            }
+        float4* d = reinterpret_cast<float4*>(dcoarse + pc * Cc + c);
+        d[0] = make_float4(s[0], s[1], s[2], s[3]);
+        d[1] = make_float4(s[4], s[5], s[6], s[7]);
     }
 }
 
@@ -645,14 +739,14 @@ salty_status launch_conv(salty_ctx* ctx, int kind, const ConvSrc& in, int cin, c
 
 salty_status launch_wgrad(salty_ctx* ctx, const bf16* dy, int cpad, int cout, const ConvSrc& x, int cin, float* dw,
                           int N, int H, int W) {
-    const size_t smem = ((size_t)kTileX * kTileY * (cpad + 8) + (size_t)kHaloX * kHaloY * 24) * sizeof(bf16);
-    SALTY_TRY_CUDA(ctx->err,
-                   cudaFuncSetAttribute(k_conv3x3_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = ((size_t)kTileX * kTileY * (kWgradCo + 8) + (size_t)kHaloX * kHaloY * 24) * sizeof(bf16);
     const int tiles = N * ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
-    int gx = ctx->num_sms * 8 / (9 * (cin / 16));
+    const int mg = (cpad + kWgradCo - 1) / kWgradCo;
+    // about four resident CTAs per SM over all (output-channel group, input slice) pairs
+    int gx = ctx->num_sms * 4 / (mg * (cin / 16));
     if (gx < 1) gx = 1;
     if (gx > tiles) gx = tiles;
-    dim3 grid(gx, 9, cin / 16);
+    dim3 grid(gx, mg, cin / 16);
     k_conv3x3_wgrad<<<grid, kConvThreads, smem, ctx->stream>>>(dy, cpad, cout, x, cin, dw, N, H, W);
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;
@@ -739,9 +833,10 @@ salty_status conv_backward(salty_ctx* ctx, Unet& u, Fwd& F, int li, const ConvSr
     const long long npx = (long long)N * h * w;
     cudaStream_t st = ctx->stream;
     bf16* g = F.t[T_G];
-    k_relu_bwd<<<gsz(npx * L.cout_pad), 256, 0, st>>>(F.t[y], L.cout, dy, L.cout, L.relu, npx, g, L.cout_pad);
-    k_bias_grad<<<gsz(npx * L.cout), 256, L.cout * sizeof(float), st>>>(g, L.cout_pad, L.cout, npx,
-                                                                       u.grads.p + L.b_off);
+    k_relu_bwd<<<gsz(npx * L.cout_pad / 8), 256, 0, st>>>(F.t[y], L.cout, dy, L.cout, L.relu, npx, g, L.cout_pad);
+    // few blocks: each adds its partial sums into the C gradient words once
+    const int bias_blocks = (int)std::min<long long>((long long)ctx->num_sms * 2, (npx + 255) / 256);
+    k_bias_grad<<<bias_blocks, 256, L.cout * sizeof(float), st>>>(g, L.cout_pad, L.cout, npx, u.grads.p + L.b_off);
     SALTY_TRY(launch_wgrad(ctx, g, L.cout_pad, L.cout, x, L.cin, u.grads.p + L.w_off, N, h, w));
     if (want_dx)
         SALTY_TRY(launch_conv(ctx, u.conv_kind, conv_src(g, L.cout_pad, L.cout_pad), L.cout_pad, u.wb.p + L.wb_off,
@@ -765,12 +860,12 @@ salty_status backward(salty_ctx* ctx, Unet& u, Fwd& F, const float* d_target, in
     auto x = [&](int t, int c) { return conv_src(F.t[t], c, c); };
     auto cat = [&](int coarse, int cc, int skip, int cs) { return conv_src_cat(F.t[coarse], cc, F.t[skip], cs); };
     auto to_f32 = [&](int cs, int off, int c, long long np, float* dst, int acc) {
-        k_grad_to_f32<<<gsz(np * c), 256, 0, st>>>(F.t[T_G2], cs, off, c, np, dst, acc);
+        k_grad_to_f32<<<gsz(np * c / 8), 256, 0, st>>>(F.t[T_G2], cs, off, c, np, dst, acc);
     };
     // decoder: a conv's input gradient splits into the up-sampled part and the skip part
     auto split = [&](int cc, int cs, int h, int w, float* g_coarse, float* g_skip) {
         const long long np = (long long)N * h * w;
-        k_upsample_bwd<<<gsz(np / 4 * cc), 256, 0, st>>>(F.t[T_G2], cc + cs, g_coarse, cc, N, h, w);
+        k_upsample_bwd<<<gsz(np / 4 * cc / 8), 256, 0, st>>>(F.t[T_G2], cc + cs, g_coarse, cc, N, h, w);
         to_f32(cc + cs, cc, cs, np, g_skip, 0);
     };
     SALTY_TRY(conv_backward(ctx, u, F, 13, x(T_D0, 32), T_OUT, G[G_OUT], N, H, W, true));
@@ -785,22 +880,22 @@ salty_status backward(salty_ctx* ctx, Unet& u, Fwd& F, const float* d_target, in
     split(96, 80, H3, W3, G[G_B], G[G_E3]);
     SALTY_TRY(conv_backward(ctx, u, F, 8, x(T_P3, 80), T_B, G[G_B], N, H4, W4, true));
     to_f32(80, 0, 80, P4, G[G_P3], 0);
-    k_pool_bwd<<<gsz(P4 * 80), 256, 0, st>>>(F.t[T_E3], G[G_P3], G[G_E3], N, H3, W3, 80);
+    k_pool_bwd<<<gsz(P4 * 80 / 8), 256, 0, st>>>(F.t[T_E3], G[G_P3], G[G_E3], N, H3, W3, 80);
     SALTY_TRY(conv_backward(ctx, u, F, 7, x(T_A3, 80), T_E3, G[G_E3], N, H3, W3, true));
     to_f32(80, 0, 80, P3, G[G_A3], 0);
     SALTY_TRY(conv_backward(ctx, u, F, 6, x(T_P2, 64), T_A3, G[G_A3], N, H3, W3, true));
     to_f32(64, 0, 64, P3, G[G_P2], 0);
-    k_pool_bwd<<<gsz(P3 * 64), 256, 0, st>>>(F.t[T_E2], G[G_P2], G[G_E2], N, H2, W2, 64);
+    k_pool_bwd<<<gsz(P3 * 64 / 8), 256, 0, st>>>(F.t[T_E2], G[G_P2], G[G_E2], N, H2, W2, 64);
     SALTY_TRY(conv_backward(ctx, u, F, 5, x(T_A2, 64), T_E2, G[G_E2], N, H2, W2, true));
     to_f32(64, 0, 64, P2, G[G_A2], 0);
     SALTY_TRY(conv_backward(ctx, u, F, 4, x(T_P1, 48), T_A2, G[G_A2], N, H2, W2, true));
     to_f32(48, 0, 48, P2, G[G_P1], 0);
-    k_pool_bwd<<<gsz(P2 * 48), 256, 0, st>>>(F.t[T_E1], G[G_P1], G[G_E1], N, H1, W1, 48);
+    k_pool_bwd<<<gsz(P2 * 48 / 8), 256, 0, st>>>(F.t[T_E1], G[G_P1], G[G_E1], N, H1, W1, 48);
     SALTY_TRY(conv_backward(ctx, u, F, 3, x(T_A1, 48), T_E1, G[G_E1], N, H1, W1, true));
     to_f32(48, 0, 48, P1, G[G_A1], 0);
     SALTY_TRY(conv_backward(ctx, u, F, 2, x(T_P0, 32), T_A1, G[G_A1], N, H1, W1, true));
     to_f32(32, 0, 32, P1, G[G_P0], 0);
-    k_pool_bwd<<<gsz(P1 * 32), 256, 0, st>>>(F.t[T_E0], G[G_P0], G[G_E0], N, H, W, 32);
+    k_pool_bwd<<<gsz(P1 * 32 / 8), 256, 0, st>>>(F.t[T_E0], G[G_P0], G[G_E0], N, H, W, 32);
     SALTY_TRY(conv_backward(ctx, u, F, 1, x(T_A0, 32), T_E0, G[G_E0], N, H, W, true));
     to_f32(32, 0, 32, P0, G[G_A0], 0);
     SALTY_TRY(conv_backward(ctx, u, F, 0, x(T_X, 16), T_A0, G[G_A0], N, H, W, false));

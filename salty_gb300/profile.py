@@ -1,6 +1,7 @@
 """Small fixed workloads for profiling the kernels (run them under ncu or alone).
 
-    python -m salty_gb300.profile render [--spp 1] [--frames 2]   1080p heightfield frames
+    python -m salty_gb300.profile render [--spp 1] [--frames 2] [--width 1920 --height 1080]
+                                                                     heightfield frames
     python -m salty_gb300.profile unet [--n 1 --h 1088 --w 1920] [--conv tcgen05|tcgen05_cp_async|mma_sync|all]
                                                                      denoiser forward passes
     python -m salty_gb300.profile trace-sweep                        traversal launch shapes
@@ -23,15 +24,15 @@ from . import Context, Unet, UNET_FEATURES, microbench_rays, microbench_soup
 from . import scenes
 
 
-def render(spp: int, frames: int) -> dict:
+def render(spp: int, frames: int, width: int = 1920, height: int = 1080) -> dict:
     ctx = Context(0)
     s = scenes.upload(ctx, scenes.heightfield())
     info = s.build()
     out = []
     for i in range(frames):
-        r = s.render(1920, 1080, spp, 12, seed=3 + i, want=())
-        out.append({"ms": r["ms"], "rays": r["rays"], "paths": r["paths"]})
-    return {"workload": f"1080p heightfield, {spp} spp x {frames} frames", "bvh_build_ms": info["build_ms"],
+        r = s.render(width, height, spp, 12, seed=3 + i, want=())
+        out.append({"ms": r["ms"], "rays": r["rays"], "paths": r["paths"], "Mrays_s": r["rays"] / r["ms"] / 1e3})
+    return {"workload": f"{width}x{height} heightfield, {spp} spp x {frames} frames", "bvh_build_ms": info["build_ms"],
             "frames": out}
 
 
@@ -112,6 +113,8 @@ def main(argv=None):
     ap.add_argument("what", choices=["render", "unet", "trace-sweep", "cornell"])
     ap.add_argument("--spp", type=int, default=1)
     ap.add_argument("--frames", type=int, default=2)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--n", type=int, default=1)
     ap.add_argument("--h", type=int, default=1088)
     ap.add_argument("--w", type=int, default=1920)
@@ -119,7 +122,7 @@ def main(argv=None):
     ap.add_argument("--train", action="store_true", help="unet: also time training steps")
     a = ap.parse_args(argv)
     if a.what == "render":
-        r = render(a.spp, a.frames)
+        r = render(a.spp, a.frames, a.width, a.height)
     elif a.what == "unet":
         r = unet(a.n, a.h, a.w, a.conv, a.train)
     elif a.what == "cornell":
