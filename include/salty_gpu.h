@@ -277,7 +277,9 @@ typedef struct salty_tuning {
     int32_t trace_postpone;  /* fewest lanes that test a triangle group together, 1..32 */
     int32_t shade_block;     /* shading threads per block, a multiple of 32 in 64..1024 */
     int32_t trace_regs;      /* traversal registers per thread: 64, or 48 (more resident warps) */
-    int64_t wave_paths;      /* paths in flight per wave (queue capacity), 2^16..2^26 */
+    int64_t wave_paths;      /* paths in flight per wave (queue capacity), 2^16..2^27; default
+                              * 2^26 (about 23 GB of path state for a render of that many
+                              * samples or more; smaller renders allocate what they use) */
 } salty_tuning;
 salty_status salty_get_tuning(salty_ctx* ctx, salty_tuning* out);
 salty_status salty_set_tuning(salty_ctx* ctx, const salty_tuning* t);

@@ -589,8 +589,8 @@ salty_status salty_set_tuning(salty_ctx* ctx, const salty_tuning* t) {
     if (t->shade_block < 64 || t->shade_block > 1024 || t->shade_block % 32)
         return E.fail(SALTY_ERR_INVALID_ARG, "shade_block must be a multiple of 32 in 64..1024");
     if (t->trace_regs != 64 && t->trace_regs != 48) return E.fail(SALTY_ERR_INVALID_ARG, "trace_regs must be 64 or 48");
-    if (t->wave_paths < (1 << 16) || t->wave_paths > (1 << 26))
-        return E.fail(SALTY_ERR_INVALID_ARG, "wave_paths must be 2^16..2^26");
+    if (t->wave_paths < (1 << 16) || t->wave_paths > (1 << 27))
+        return E.fail(SALTY_ERR_INVALID_ARG, "wave_paths must be 2^16..2^27");
     ctx->tune.trace.block = t->trace_block;
     ctx->tune.trace.pool = t->trace_pool;
     ctx->tune.trace.postpone = t->trace_postpone;
@@ -715,7 +715,7 @@ salty_status salty_autotune(salty_ctx* ctx, salty_scene* const* scenes, const sa
     float best_t = 0;
     salty_status s = time_of(best, &best_t);
     // coordinate descent, one pass over the knobs
-    const long long waves[] = {1ll << 20, 1ll << 21, 1ll << 22, 1ll << 23};
+    const long long waves[] = {1ll << 22, 1ll << 24, 1ll << 26};
     const int shade[] = {128, 256, 512};
     // traversal block size and register budget interact (registers x threads x blocks per
     // SM against the shared stack), so they are searched as pairs

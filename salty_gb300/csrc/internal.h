@@ -204,7 +204,11 @@ namespace salty {
 // Launch shapes of the renderer, chosen by salty_autotune (include/salty_gpu.h).
 struct Tuning {
     TraceTuning trace;
-    long long wave_paths = 1ll << 22;  // paths in flight per wave (queue capacity)
+    // Paths in flight per wave (queue capacity).  Each depth level of a wave ends with a
+    // tail of a few long walks; a large wave spreads that tail over more samples (1080p
+    // heightfield, 64 spp: 717 Mrays/s at 2^22, 1,274 at 2^24, 1,573 at 2^26).  352 bytes of
+    // path state per path: 23.6 GB at 2^26.
+    long long wave_paths = 1ll << 26;
     int shade_block = 256;             // threads per block of the shading kernels
 };
 

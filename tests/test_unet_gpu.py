@@ -200,3 +200,33 @@ def test_tcgen05_and_mma_sync_agree(ctx):
     with pytest.raises(salty_gb300.SaltyError):
         net.set_conv_kernel(7)
     net.close()
+
+
+@pytest.mark.parametrize("shape", [(1, 1088, 1920), (3, 16, 16)])
+def test_tcgen05_full_frame_and_tiny_batch(ctx, shape):
+    """The tensor-core kernels at the denoiser's working size (a 1080p frame padded to 1088
+    rows: 15 strips of 128 pixels, 136 row groups, the persistent TMA kernel looping over
+    many strips per CTA) and at the smallest legal size (16 x 16, one ragged strip at every
+    level, 1 x 1 at the bottleneck): outputs equal the mma.sync kernel's up to FP32
+    summation order, and the input gradients of a training step as well."""
+    import torch
+    import salty_gb300
+    n, h, w = shape
+    net = salty_gb300.Unet(ctx, seed=14)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    f = torch.rand((n, h, w, salty_gb300.UNET_FEATURES), device="cuda", generator=g)
+    t = f[..., :3] * (0.6 + 0.8 * torch.rand((n, h, w, 3), device="cuda", generator=g))
+    res = {}
+    for kind in (salty_gb300.CONV_MMA_SYNC, salty_gb300.CONV_TCGEN05):
+        net.set_conv_kernel(kind)
+        o = torch.empty((n, h, w, 3), device="cuda")
+        net.forward(f, out=o)
+        loss = net.train_step(f, t.contiguous(), lr=0.0)
+        res[kind] = (o.cpu().numpy(), loss, net.grads())
+    (o1, l1, g1), (o2, l2, g2) = res[salty_gb300.CONV_MMA_SYNC], res[salty_gb300.CONV_TCGEN05]
+    assert np.all(np.isfinite(o2))
+    assert _rel(o2, o1) < 0.01, _rel(o2, o1)
+    assert abs(l2 / l1 - 1) < 1e-3, (l1, l2)
+    cos = g1 @ g2 / (np.linalg.norm(g1) * np.linalg.norm(g2))
+    assert cos > 0.999, cos
+    net.close()
