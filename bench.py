@@ -225,11 +225,12 @@ def run_time_to_rmse(args):
     render = {"spp": 64, "ms": r["ms"], "Mrays_s": r["rays"] / r["ms"] / 1e3, "Mpaths_s": r["paths"] / r["ms"] / 1e3,
               "rays_per_path": r["rays"] / max(r["paths"], 1)}
     # the plain path renders with the default launch shapes; the denoised paths with the
-    # shapes salty_autotune picks for this frame (trial renders at 1 spp, untimed)
+    # shapes salty_autotune picks for this frame (trial renders at 64 spp -- 132.7M samples,
+    # enough to tell wave sizes up to 2^27 apart -- untimed, reported as autotune_seconds)
     default = ctx.tuning
     t0 = time.perf_counter()
-    tuned, trial_ms = ctx.autotune([s], [{"width": W, "height": H, "spp": 1, "max_depth": D,
-                                          "profile": salty_gb300.PROFILE_PHYSICAL}], trial_spp=1)
+    tuned, trial_ms = ctx.autotune([s], [{"width": W, "height": H, "spp": 64, "max_depth": D,
+                                          "profile": salty_gb300.PROFILE_PHYSICAL}], trial_spp=64)
     tune_s = time.perf_counter() - t0
     res = {}
     with ClockSampler(0) as clk:

@@ -401,8 +401,9 @@ salty_status salty_unet_train_step(salty_ctx* ctx, salty_unet* net, const float*
  * NLM (salty_denoise_nlm) is the fallback where no trained weights exist. */
 salty_status salty_denoise_unet(salty_ctx* ctx, salty_unet* net, salty_scene* scene, float* out_rgb);
 /* The same, averaged over `mirrors` mirror images of the frame (1: as salty_denoise_unet;
- * 2: also left-right; 4: also top-bottom and both) -- a self-ensemble that lowers the
- * network's own error at the cost of `mirrors` forward passes. */
+ * 2: also left-right; 4: also top-bottom and both; 8: also the transposes of those four,
+ * i.e. every symmetry of the pixel grid) -- a self-ensemble that lowers the network's own
+ * error at the cost of `mirrors` forward passes. */
 salty_status salty_denoise_unet_ensemble(salty_ctx* ctx, salty_unet* net, salty_scene* scene, int32_t mirrors,
                                         float* out_rgb);
 /* The kernel of the network's forward and backward-data convolutions: SALTY_CONV_TCGEN05

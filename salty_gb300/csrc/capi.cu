@@ -715,7 +715,7 @@ salty_status salty_autotune(salty_ctx* ctx, salty_scene* const* scenes, const sa
     float best_t = 0;
     salty_status s = time_of(best, &best_t);
     // coordinate descent, one pass over the knobs
-    const long long waves[] = {1ll << 22, 1ll << 24, 1ll << 26};
+    const long long waves[] = {1ll << 22, 1ll << 24, 1ll << 26, 1ll << 27};
     const int shade[] = {128, 256, 512};
     // traversal block size and register budget interact (registers x threads x blocks per
     // SM against the shared stack), so they are searched as pairs

@@ -424,15 +424,16 @@ __global__ void k_loss(const bf16* __restrict__ out, const bf16* __restrict__ x,
     if ((threadIdx.x & 31) == 0) atomicAdd(loss_sum, s);
 }
 
-// One mirrored pass of the self-ensemble: adds weight * (the prediction of pixel (px, py),
-// found at its mirrored place in the Wp-wide padded output) to rgb [H][W][3].
+// One pass of the self-ensemble: adds weight * (the prediction of pixel (px, py), found at
+// its mirrored place in the padded Wp x Hp output, or, with flip bit 2, at the transposed
+// place of the Hp-wide transposed output) to rgb [H][W][3].
 __global__ void k_output_flipped(const bf16* __restrict__ out, const bf16* __restrict__ x, int W, int H, int Wp,
-                                 int flip, float weight, int first, float* __restrict__ rgb) {
+                                 int Hp, int flip, float weight, int first, float* __restrict__ rgb) {
     const long long total = (long long)W * H;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total; p += (long long)gridDim.x * blockDim.x) {
         const int px = (int)(p % W), py = (int)(p / W);
         const int qx = (flip & 1) ? W - 1 - px : px, qy = (flip & 2) ? H - 1 - py : py;
-        const long long q = (long long)qy * Wp + qx;
+        const long long q = (flip & 4) ? (long long)qx * Hp + qy : (long long)qy * Wp + qx;
         for (int c = 0; c < 3; ++c) {
             const float v =
                 weight * fmaxf(expm1f(__bfloat162float(out[q * 8 + c]) + __bfloat162float(x[q * 16 + c])), 0.0f);
@@ -586,14 +587,15 @@ __global__ void k_weights_to_bf16(const float* __restrict__ w, int Cout, int Cin
 
 // Film planes (W x H) -> network input (Wp x Hp, multiples of 16) with reflected borders:
 // colour, albedo, normal, 1/(1+t), noise level mean_c sqrt(var_c) / (1 + colour_c).  With
-// flip bit 0 (1) the frame is mirrored left-right (top-bottom) first.
+// flip bit 0 (1) the frame is mirrored left-right (top-bottom) first; with bit 2 the input
+// is the transposed frame, Hp wide and Wp tall.
 __global__ void k_pack_features(const float* __restrict__ mean, const float* __restrict__ var,
                                 const float* __restrict__ albedo, const float* __restrict__ normal,
                                 const float* __restrict__ depth, int W, int H, int Wp, int Hp, int flip,
                                 float* __restrict__ f) {
     const long long total = (long long)Wp * Hp;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(i % Wp), y = (int)(i / Wp);
+        const int x = (flip & 4) ? (int)(i / Hp) : (int)(i % Wp), y = (flip & 4) ? (int)(i % Hp) : (int)(i / Wp);
         int sx = x < W ? x : max(2 * W - 2 - x, 0), sy = y < H ? y : max(2 * H - 2 - y, 0);
         if (flip & 1) sx = W - 1 - sx;
         if (flip & 2) sy = H - 1 - sy;
@@ -1115,8 +1117,8 @@ salty_status salty_denoise_unet_ensemble(salty_ctx* ctx, salty_unet* net, salty_
                                         float* out_rgb) {
     using namespace salty;
     if (!ctx || !net || !scene || !out_rgb) return SALTY_ERR_INVALID_ARG;
-    if (mirrors != 1 && mirrors != 2 && mirrors != 4)
-        return ctx->err.fail(SALTY_ERR_INVALID_ARG, "mirrors must be 1, 2 or 4");
+    if (mirrors != 1 && mirrors != 2 && mirrors != 4 && mirrors != 8)
+        return ctx->err.fail(SALTY_ERR_INVALID_ARG, "mirrors must be 1, 2, 4 or 8");
     cudaSetDevice(ctx->device);
     Unet& u = net->net;
     const Film& Fm = scene->film;
@@ -1139,9 +1141,12 @@ salty_status salty_denoise_unet_ensemble(salty_ctx* ctx, salty_unet* net, salty_
     for (int k = 0; k < mirrors; ++k) {
         k_pack_features<<<gsz(npp), 256, 0, ctx->stream>>>(mean, var, alb, nrm, dep, W, H, Wp, Hp, k, feat);
         Fwd F;
-        SALTY_TRY(forward(ctx, u, feat, 1, Hp, Wp, F));
-        k_output_flipped<<<gsz(npx), 256, 0, ctx->stream>>>(F.t[T_OUT], F.t[T_X], W, H, Wp, k, 1.0f / (float)mirrors,
-                                                           k == 0, img);
+        if (k & 4)
+            SALTY_TRY(forward(ctx, u, feat, 1, Wp, Hp, F));  // the transposed frame: Hp wide, Wp tall
+        else
+            SALTY_TRY(forward(ctx, u, feat, 1, Hp, Wp, F));
+        k_output_flipped<<<gsz(npx), 256, 0, ctx->stream>>>(F.t[T_OUT], F.t[T_X], W, H, Wp, Hp, k,
+                                                           1.0f / (float)mirrors, k == 0, img);
     }
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(out_rgb, img, (size_t)npx * 3 * sizeof(float), cudaMemcpyDefault,

