@@ -6,6 +6,7 @@
                                                                      denoiser forward passes
     python -m salty_gb300.profile trace-sweep                        traversal launch shapes
     python -m salty_gb300.profile cornell                            the 256^2 Cornell box, 16 spp
+    python -m salty_gb300.profile wave-sweep [--spp 64]              1080p heightfield per wave size
 
 `render` and `unet` print one line of timings; `trace-sweep` times every traversal launch
 shape (block size x register budget x pool x postpone) on the 1M-triangle microbenchmark
@@ -49,6 +50,25 @@ def cornell() -> dict:
     best = min(runs, key=lambda r: r["ms"])
     return {"workload": "Cornell box 256x256, 16 spp, depth 8, compat profile", "ms": best["ms"],
             "Mrays_s": best["rays"] / best["ms"] / 1e3, "Mpaths_s": best["paths"] / best["ms"] / 1e3}
+
+
+def wave_sweep(spp: int) -> dict:
+    """The 1080p heightfield at `spp` samples, depth 12, default launch shapes, for waves of
+    2^22 .. 2^27 paths: best of two renders each after an 8-spp warm-up."""
+    ctx = Context(0)
+    s = scenes.upload(ctx, scenes.heightfield())
+    s.build()
+    base = ctx.tuning
+    res = []
+    for e in range(22, 28):
+        t = dict(base)
+        t["wave_paths"] = 1 << e
+        ctx.tuning = t
+        s.render(1920, 1080, 8, 12, seed=1, want=())
+        best = min((s.render(1920, 1080, spp, 12, seed=2 + i, want=()) for i in range(2)), key=lambda r: r["ms"])
+        res.append({"wave_paths": 1 << e, "ms": best["ms"], "Mrays_s": best["rays"] / best["ms"] / 1e3,
+                    "Mpaths_s": best["paths"] / best["ms"] / 1e3})
+    return {"workload": f"1920x1080 heightfield, {spp} spp, depth 12, default launch shapes", "waves": res}
 
 
 def unet(n: int, h: int, w: int, conv: str = "tcgen05", train: bool = False) -> dict:
@@ -110,8 +130,8 @@ def trace_sweep() -> dict:
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("what", choices=["render", "unet", "trace-sweep", "cornell"])
-    ap.add_argument("--spp", type=int, default=1)
+    ap.add_argument("what", choices=["render", "unet", "trace-sweep", "cornell", "wave-sweep"])
+    ap.add_argument("--spp", type=int, default=None, help="render: 1, wave-sweep: 64")
     ap.add_argument("--frames", type=int, default=2)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
@@ -122,11 +142,13 @@ def main(argv=None):
     ap.add_argument("--train", action="store_true", help="unet: also time training steps")
     a = ap.parse_args(argv)
     if a.what == "render":
-        r = render(a.spp, a.frames, a.width, a.height)
+        r = render(a.spp or 1, a.frames, a.width, a.height)
     elif a.what == "unet":
         r = unet(a.n, a.h, a.w, a.conv, a.train)
     elif a.what == "cornell":
         r = cornell()
+    elif a.what == "wave-sweep":
+        r = wave_sweep(a.spp or 64)
     else:
         r = trace_sweep()
     print(json.dumps(r))
