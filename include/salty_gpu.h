@@ -355,6 +355,10 @@ salty_status salty_denoise_nlm_ref(salty_ctx* ctx, int32_t width, int32_t height
 
 /* Variance-scaled NLM on RGB with per-pixel variance of the mean (W*H*3 each):
  * search window (2 search_r + 1)^2, patch (2 patch_r + 1)^2, strength k. */
+/* Diagnostics: this GPU's FP32 CUDA-core throughput (fused multiply-adds, 2 flops each), in
+ * TFLOP/s, measured by a microkernel with CUDA events -- the peak the NLM kernels' roofline
+ * is quoted against.  No counterpart in the reference. */
+salty_status salty_fp32_peak(salty_ctx* ctx, double* tflops);
 salty_status salty_denoise_nlm(salty_ctx* ctx, int32_t width, int32_t height, int32_t search_r,
                                int32_t patch_r, float k, const float* rgb, const float* var,
                                float* out);

@@ -815,6 +815,12 @@ salty_status salty_denoise_nlm_ref(salty_ctx* ctx, int32_t w, int32_t h, float c
     return SALTY_OK;
 }
 
+salty_status salty_fp32_peak(salty_ctx* ctx, double* tflops) {
+    if (!ctx || !tflops) return SALTY_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    return fp32_peak(ctx, tflops);
+}
+
 salty_status salty_denoise_nlm(salty_ctx* ctx, int32_t w, int32_t h, int32_t search_r, int32_t patch_r, float k,
                                const float* rgb, const float* var, float* out) {
     if (!ctx) return SALTY_ERR_INVALID_ARG;

@@ -185,6 +185,14 @@ __global__ void __launch_bounds__(kNlmTile* kNlmTile) k_nlm_ref(const float4* __
 // ---------------------------------------------------------------- NLM (variance scaled)
 // Rousselle, Knaus, Zwicker, "Adaptive rendering with non-local means filtering"
 // (SIGGRAPH Asia 2012): patch distance normalised by the pixels' variances.
+//
+// Separable form: for one search offset (dx, dy) the patch distance of every pixel is a
+// (2P+1)^2 box sum of the per-pixel term
+//   D(x) = sum_c [(I_c(x) - I_c(x+d))^2 - (V_c(x) + min(V_c(x), V_c(x+d)))] / (eps + k^2 (V_c(x) + V_c(x+d)))
+// (each coordinate clamped to the image), so a CTA computes D once over its tile plus the
+// patch border, sums it along rows and then columns in shared memory, and every pixel reads
+// its distance: O(1) work per pixel and offset instead of O(patch).  The same sums as the
+// direct double loop in a different order.
 constexpr int kVTile = 16;
 
 __global__ void __launch_bounds__(kVTile* kVTile) k_nlm_var(const float* __restrict__ rgb, const float* __restrict__ var,
@@ -192,11 +200,16 @@ __global__ void __launch_bounds__(kVTile* kVTile) k_nlm_var(const float* __restr
                                                             float* __restrict__ out) {
     extern __shared__ float sm[];
     const int H = R + P;
-    const int S = kVTile + 2 * H;
+    const int S = kVTile + 2 * H;   // staged halo side
+    const int E = kVTile + 2 * P;   // tile plus patch border
     float* tc = sm;                 // S*S*3 colours
-    float* tv = sm + S * S * 3;     // S*S*3 variances
-    const int x0 = blockIdx.x * kVTile - H, y0 = blockIdx.y * kVTile - H;
-    for (int i = threadIdx.y * kVTile + threadIdx.x; i < S * S; i += kVTile * kVTile) {
+    float* tv = tc + S * S * 3;     // S*S*3 variances
+    float* dd = tv + S * S * 3;     // E*E per-pixel terms D
+    float* hs = dd + E * E;         // E rows x kVTile columns of row sums
+    const int tid = threadIdx.y * kVTile + threadIdx.x, nt = kVTile * kVTile;
+    const int bx = blockIdx.x * kVTile, by = blockIdx.y * kVTile;
+    const int x0 = bx - H, y0 = by - H;
+    for (int i = tid; i < S * S; i += nt) {
         const int ty = i / S, tx = i % S;
         const size_t g = ((size_t)clampi(y0 + ty, 0, h - 1) * w + clampi(x0 + tx, 0, w - 1)) * 3;
         for (int c = 0; c < 3; ++c) {
@@ -205,25 +218,39 @@ __global__ void __launch_bounds__(kVTile* kVTile) k_nlm_var(const float* __restr
         }
     }
     __syncthreads();
-    const int x = blockIdx.x * kVTile + threadIdx.x, y = blockIdx.y * kVTile + threadIdx.y;
-    if (x >= w || y >= h) return;
+    const int x = bx + threadIdx.x, y = by + threadIdx.y;
     const float eps = 1e-10f;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, sw = 0.f;
     for (int dy = -R; dy <= R; ++dy) {
         for (int dx = -R; dx <= R; ++dx) {
-            float d2 = 0.0f;
-            for (int py = -P; py <= P; ++py) {
-                for (int px = -P; px <= P; ++px) {
-                    const int ia = ((clampi(y + py, 0, h - 1) - y0) * S + (clampi(x + px, 0, w - 1) - x0)) * 3;
-                    const int ib = ((clampi(y + dy + py, 0, h - 1) - y0) * S + (clampi(x + dx + px, 0, w - 1) - x0)) * 3;
+            // D over the tile plus its patch border (image coordinates bx - P .. bx + kVTile + P)
+            for (int i = tid; i < E * E; i += nt) {
+                const int u = i % E, v = i / E;
+                const int ax = clampi(bx - P + u, 0, w - 1), ay = clampi(by - P + v, 0, h - 1);
+                const int qx = clampi(bx - P + u + dx, 0, w - 1), qy = clampi(by - P + v + dy, 0, h - 1);
+                const int ia = ((ay - y0) * S + (ax - x0)) * 3, ib = ((qy - y0) * S + (qx - x0)) * 3;
+                float d = 0.0f;
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const float a = tc[ia + c], b = tc[ib + c], va = tv[ia + c], vb = tv[ib + c];
-                        const float num = (a - b) * (a - b) - (va + fminf(va, vb));
-                        d2 += num / (eps + k2 * (va + vb));
-                    }
+                for (int c = 0; c < 3; ++c) {
+                    const float a = tc[ia + c], b = tc[ib + c], va = tv[ia + c], vb = tv[ib + c];
+                    const float num = (a - b) * (a - b) - (va + fminf(va, vb));
+                    d += num / (eps + k2 * (va + vb));
                 }
+                dd[i] = d;
             }
+            __syncthreads();
+            // row sums over the patch width
+            for (int i = tid; i < E * kVTile; i += nt) {
+                const int u = i % kVTile, v = i / kVTile;
+                const float* r = dd + v * E + u;
+                float t = 0.0f;
+                for (int k = 0; k <= 2 * P; ++k) t += r[k];
+                hs[i] = t;
+            }
+            __syncthreads();
+            // column sum over the patch height: this pixel's patch distance
+            float d2 = 0.0f;
+            for (int k = 0; k <= 2 * P; ++k) d2 += hs[(threadIdx.y + k) * kVTile + threadIdx.x];
             const float wt = expf(-fmaxf(0.0f, d2 * norm));
             const int iq = ((clampi(y + dy, 0, h - 1) - y0) * S + (clampi(x + dx, 0, w - 1) - x0)) * 3;
             sw += wt;
@@ -232,6 +259,7 @@ __global__ void __launch_bounds__(kVTile* kVTile) k_nlm_var(const float* __restr
             s2 += wt * tc[iq + 2];
         }
     }
+    if (x >= w || y >= h) return;
     const size_t o = ((size_t)y * w + x) * 3;
     out[o] = s0 / sw;
     out[o + 1] = s1 / sw;
@@ -301,10 +329,47 @@ salty_status nlm_ref_device(salty_ctx* ctx, int w, int h, float coeff, const flo
     return SALTY_OK;
 }
 
+// FP32 throughput probe: kFmaChains independent fused multiply-add chains per thread, so
+// every scheduler always has a ready FMA; nothing but the final sum leaves the registers.
+constexpr int kFmaChains = 8;
+__global__ void __launch_bounds__(256) k_fp32_peak(float* __restrict__ sink, int iters, float b, float c) {
+    float a[kFmaChains];
+#pragma unroll
+    for (int k = 0; k < kFmaChains; ++k) a[k] = (float)(threadIdx.x + k);
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int k = 0; k < kFmaChains; ++k) a[k] = fmaf(a[k], b, c);
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kFmaChains; ++k) s += a[k];
+    if (s == 1234.5f) sink[0] = s;  // keeps the chains live; never true for these inputs
+}
+
+salty_status fp32_peak(salty_ctx* ctx, double* tflops) {
+    auto& E = ctx->err;
+    const int blocks = ctx->num_sms * 8, threads = 256, iters = 1 << 14;
+    float* sink = reinterpret_cast<float*>(ctx->counters.p + 48);
+    cudaEvent_t e0 = ctx->ev[0], e1 = ctx->ev[1];
+    float best = 1e30f;
+    for (int r = 0; r < 4; ++r) {  // the first launch warms up
+        SALTY_TRY_CUDA(E, cudaEventRecord(e0, ctx->stream));
+        k_fp32_peak<<<blocks, threads, 0, ctx->stream>>>(sink, iters, 0.999999f, 1e-7f);
+        SALTY_TRY_CUDA(E, cudaEventRecord(e1, ctx->stream));
+        SALTY_TRY_CUDA(E, cudaEventSynchronize(e1));
+        float ms = 0;
+        SALTY_TRY_CUDA(E, cudaEventElapsedTime(&ms, e0, e1));
+        if (r > 0 && ms < best) best = ms;
+    }
+    SALTY_TRY_CUDA(E, cudaGetLastError());
+    const double flops = 2.0 * kFmaChains * (double)iters * blocks * threads;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return SALTY_OK;
+}
+
 salty_status nlm_var_device(salty_ctx* ctx, int w, int h, int search_r, int patch_r, float k, const float* d_rgb,
                             const float* d_var, float* d_out) {
-    const int H = search_r + patch_r, S = kVTile + 2 * H;
-    size_t smem = (size_t)S * S * 6 * sizeof(float);
+    const int H = search_r + patch_r, S = kVTile + 2 * H, Eb = kVTile + 2 * patch_r;
+    size_t smem = ((size_t)S * S * 6 + (size_t)Eb * Eb + (size_t)Eb * kVTile) * sizeof(float);
     if (smem > 200 * 1024) return ctx->err.fail(SALTY_ERR_CAPACITY, "NLM window too large");
     SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(k_nlm_var, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     float norm = 1.0f / (3.0f * (float)((2 * patch_r + 1) * (2 * patch_r + 1)));

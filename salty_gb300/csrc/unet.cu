@@ -178,9 +178,10 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const ConvSrc in, int 
 
 // ---------------------------------------------------------------- conv3x3 backward weights
 // dW[tap][co][ci] += sum_p dY[p][co] * X[p + (ky-1, kx-1)][ci] for all nine taps, a group of
-// up to four 16-row output-channel tiles (blockIdx.y; warp w takes tile 4 * blockIdx.y + w)
-// and a 16-wide input-channel slice (blockIdx.z); CTAs stride over 8x16 pixel tiles
-// (blockIdx.x).  Per tile the CTA stages its dY columns and the X halo once; per 16-pixel
+// up to four 16-row output-channel tiles (blockIdx.y) and a 16-wide input-channel slice
+// (blockIdx.z); CTAs stride over 8x16 pixel tiles (blockIdx.x).  With nm output tiles in the
+// group, warp w takes tile w % nm and the tile rows s = w / nm, w / nm + 4 / nm, ... (all
+// four warps busy for 1, 2 or 4 tiles).  Per tile the CTA stages its dY columns and the X halo once; per 16-pixel
 // k-step a warp loads its dY^T fragment once and reuses it for the nine taps' X fragments,
 // keeping 9 x 2 accumulator tiles in registers until the end, then adds them into the FP32
 // gradients.  dY: [N][H][W][Cpad] (Cpad multiple of 16, zero beyond the layer's real
@@ -201,7 +202,9 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_wgrad(const bf16* __re
     const int tiles_x = (W + kTileX - 1) / kTileX, tiles_y = (H + kTileY - 1) / kTileY;
     const int ntiles = N * tiles_x * tiles_y;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const bool active = warp * 16 < cw;
+    const int nm = cw / 16, ngrp = 4 / nm;                 // output tiles, row groups
+    const int mt = warp % nm, kgrp = warp / nm;
+    const bool active = kgrp < ngrp;
     float acc[9][2][4];
 #pragma unroll
     for (int t = 0; t < 9; ++t)
@@ -239,13 +242,13 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_wgrad(const bf16* __re
         if (!active) continue;
         // K = the tile's 128 pixels in 8 steps of 16 (one tile row each)
 #pragma unroll 1
-        for (int s = 0; s < kTileY; ++s) {
+        for (int s = kgrp; s < kTileY; s += ngrp) {
             // A: output channels (rows) x pixels (k).  Matrices: 0 = (co 0-7, px 0-7),
             // 1 = (co 8-15, px 0-7), 2 = (co 0-7, px 8-15), 3 = (co 8-15, px 8-15)
             unsigned a[4];
             {
                 const int px = kk + ((which & 2) ? 8 : 0);
-                const int co = warp * 16 + ((which & 1) ? 8 : 0);
+                const int co = mt * 16 + ((which & 1) ? 8 : 0);
                 ldmatrix_x4_trans(a, dys + (s * kTileX + px) * dstride + co);
             }
 #pragma unroll
@@ -269,7 +272,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_wgrad(const bf16* __re
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
             const int ci = ci0 + j * 8 + 2 * tq;
-            const int c0 = co0 + warp * 16 + g, c1 = c0 + 8;
+            const int c0 = co0 + mt * 16 + g, c1 = c0 + 8;
             if (c0 < cout_real) {
                 float* r0 = dw + ((size_t)tap * cout_real + c0) * Cin + ci;
                 atomicAdd(r0, acc[tap][j][0]);

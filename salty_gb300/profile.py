@@ -7,6 +7,7 @@
     python -m salty_gb300.profile trace-sweep                        traversal launch shapes
     python -m salty_gb300.profile cornell                            the 256^2 Cornell box, 16 spp
     python -m salty_gb300.profile wave-sweep [--spp 64]              1080p heightfield per wave size
+    python -m salty_gb300.profile nlm --h 1080                       1080p NLM vs the FP32 peak
 
 `render` and `unet` print one line of timings; `trace-sweep` times every traversal launch
 shape (block size x register budget x pool x postpone) on the 1M-triangle microbenchmark
@@ -71,6 +72,32 @@ def wave_sweep(spp: int) -> dict:
     return {"workload": f"1920x1080 heightfield, {spp} spp, depth 12, default launch shapes", "waves": res}
 
 
+def nlm(h: int, w: int) -> dict:
+    """salty_denoise_nlm (21x21 search, 7x7 patch) on a w x h device-resident image: the
+    best of 5 host-timed synchronous calls, against the measured FP32 peak.  Algorithmic
+    work of the filter: 441 offsets x 49 taps x 3 channels x 3 flops (difference, square,
+    sum) = 194,481 FP32 flops per pixel."""
+    import torch
+    ctx = Context(0)
+    peak = ctx.fp32_peak()
+    g = torch.Generator(device="cuda").manual_seed(1)
+    rgb = torch.rand((h, w, 3), device="cuda", generator=g)
+    var = torch.rand((h, w, 3), device="cuda", generator=g) * 0.01
+    out = torch.empty_like(rgb)
+    ctx.nlm(rgb, var, 10, 3, 0.45, out=out)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        t0 = time.perf_counter()
+        ctx.nlm(rgb, var, 10, 3, 0.45, out=out)
+        torch.cuda.synchronize()
+        best = min(best, (time.perf_counter() - t0) * 1e3)
+    flops = 194481.0 * w * h
+    ach = flops / (best * 1e-3) / 1e12
+    return {"workload": f"NLM 21x21 search, 7x7 patch, {w}x{h}", "ms": best, "algorithmic_tflops": ach,
+            "fp32_peak_tflops": peak, "frac": ach / peak}
+
+
 def unet(n: int, h: int, w: int, conv: str = "tcgen05", train: bool = False) -> dict:
     """Forward passes (and, with train, training steps at lr 0) on random features: the
     best of 5 wall-clock times after a warm-up, per convolution kernel."""
@@ -130,7 +157,7 @@ def trace_sweep() -> dict:
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("what", choices=["render", "unet", "trace-sweep", "cornell", "wave-sweep"])
+    ap.add_argument("what", choices=["render", "unet", "trace-sweep", "cornell", "wave-sweep", "nlm"])
     ap.add_argument("--spp", type=int, default=None, help="render: 1, wave-sweep: 64")
     ap.add_argument("--frames", type=int, default=2)
     ap.add_argument("--width", type=int, default=1920)
@@ -147,6 +174,8 @@ def main(argv=None):
         r = unet(a.n, a.h, a.w, a.conv, a.train)
     elif a.what == "cornell":
         r = cornell()
+    elif a.what == "nlm":
+        r = nlm(a.h, a.w)
     elif a.what == "wave-sweep":
         r = wave_sweep(a.spp or 64)
     else:
