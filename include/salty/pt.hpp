@@ -67,6 +67,11 @@ struct Config {
     int ToneMapping = SALTY_TM_ACES; // the reference captures with ACES (src/s3d_pt.cpp:43)
     uint64_t Seed = 3141592;         // the reference seeds its PCG with 3141592 (src/s3d_pt.cpp:304)
     int MaxPasses = 0;               // > 0: stop after this many passes even before the time budget
+    // Time-budgeted runs (MaxPasses == 0): each pass doubles the samples of the last while two
+    // such passes still fit the remaining budget.  Large passes fill the wavefront's queues,
+    // so more samples fit the budget; the image is the same as with fixed passes of the same
+    // total (sample k of a pixel is the same in any pass split).
+    bool GrowPasses = true;
 };
 
 struct Material {
@@ -254,19 +259,29 @@ public:
         check(salty_bvh_build(ctx_, scene_, nullptr, nullptr), ctx_, "salty_bvh_build");
         const auto t0 = std::chrono::steady_clock::now();
         passes_ = 0;
+        samples_ = 0;
+        int spp = config_.SamplesPerPass;
         for (;;) {
             salty_render_opts o = opts(passes_ > 0);
+            o.spp = spp;
             salty_render_stats st{};
             check(salty_render(ctx_, scene_, &o, nullptr, nullptr, nullptr, &st), ctx_, "salty_render");
             ++passes_;
+            samples_ += spp;
             const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             if (secs >= config_.MaxRenderingSec || (config_.MaxPasses > 0 && passes_ >= config_.MaxPasses)) break;
+            if (config_.GrowPasses && config_.MaxPasses <= 0) {
+                const double per_spp = secs / samples_, left = config_.MaxRenderingSec - secs;
+                if (2.0 * spp * per_spp * 2.0 <= left && spp < (1 << 20)) spp *= 2;
+            }
         }
         if (capturePath && *capturePath) Capture(capturePath);
         return true;
     }
 
     int Passes() const { return passes_; }
+    // Samples per pixel rendered by the last Run.
+    long long SamplesPerPixel() const { return samples_; }
 
     // Per-pixel mean radiance of the film (W*H*3).
     std::vector<float> Image() {
@@ -364,6 +379,7 @@ private:
     salty_scene* scene_ = nullptr;
     Config config_{};
     int passes_ = 0;
+    long long samples_ = 0;
 };
 
 }  // namespace salty

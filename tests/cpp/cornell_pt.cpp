@@ -1,6 +1,7 @@
 // Renders the Cornell box through the C++ host API (include/salty/pt.hpp) the way a
 // Salty host drives PathTracer::Run, and prints the pass count and image mean.
-// Usage: cornell_pt <out.png> [passes]
+// Usage: cornell_pt <out.png> [passes] [budget seconds]
+// passes 0: a time-budgeted run (MaxRenderingSec = budget, passes growing).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -21,6 +22,7 @@ static void quad(std::vector<Vertex>& v, Vector3 p0, Vector3 p1, Vector3 p2, Vec
 int main(int argc, char** argv) {
     const char* out = argc > 1 ? argv[1] : "final.png";
     int passes = argc > 2 ? std::atoi(argv[2]) : 8;
+    const float budget = argc > 3 ? (float)std::atof(argv[3]) : 1.0f;
     salty::Scene scene;
     std::vector<Vertex> white, red, green;
     quad(white, {0, 0, 0}, {0, 0, 1}, {1, 0, 1}, {1, 0, 0});
@@ -40,7 +42,7 @@ int main(int argc, char** argv) {
     cfg.Width = 128;
     cfg.Height = 128;
     cfg.MaxBounceCount = 8;
-    cfg.MaxRenderingSec = 1e9f;
+    cfg.MaxRenderingSec = passes > 0 ? 1e9f : budget;
     cfg.MaxPasses = passes;
     cfg.SamplesPerPass = 4;
     try {
@@ -50,7 +52,8 @@ int main(int argc, char** argv) {
         double s[3] = {0, 0, 0};
         for (size_t i = 0; i < img.size(); ++i) s[i % 3] += img[i];
         const double n = (double)cfg.Width * cfg.Height;
-        std::printf("passes %d mean %.6f %.6f %.6f\n", pt.Passes(), s[0] / n, s[1] / n, s[2] / n);
+        std::printf("passes %d spp %lld mean %.6f %.6f %.6f\n", pt.Passes(), pt.SamplesPerPixel(), s[0] / n, s[1] / n,
+                    s[2] / n);
     } catch (const salty::Error& e) {
         std::fprintf(stderr, "error %d: %s\n", (int)e.status, e.what());
         return 2;

@@ -58,8 +58,8 @@ def test_cpp_pathtracer_run_renders_the_cornell_box(salty_lib, tmp_path, oracle)
     r = subprocess.run([exe, png, "16"], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     words = r.stdout.split()
-    assert words[0] == "passes" and int(words[1]) == 16
-    mean = np.array([float(x) for x in words[3:6]])
+    assert words[0] == "passes" and int(words[1]) == 16 and words[2] == "spp" and int(words[3]) == 64
+    mean = np.array([float(x) for x in words[5:8]])
     img = _read_png(png)
     assert img.shape == (128, 128, 3) and img.max() <= 247 and img.mean() > 20
     # same scene, oracle estimator: image means agree to a few percent (64 spp each)
@@ -70,6 +70,24 @@ def test_cpp_pathtracer_run_renders_the_cornell_box(salty_lib, tmp_path, oracle)
     tot, _ = oracle.render(sd, 64, 64, 64, 8, profile=PROFILE_PHYSICAL, seed=2)
     om = (tot / 64).reshape(-1, 3).mean(axis=0)
     np.testing.assert_allclose(mean, om, rtol=0.05)
+
+
+@pytest.mark.gpu
+def test_cpp_pathtracer_time_budget_grows_passes(salty_lib, tmp_path):
+    """PathTracer::Run with a time budget and no pass limit (Salty's MaxRenderingSec loop):
+    passes double while they fit, so the 0.5 s budget holds many more samples than passes
+    of the first size would, and the image is a converged Cornell box."""
+    exe = _compile(salty_lib, tmp_path)
+    png = str(tmp_path / "budget.png")
+    r = subprocess.run([exe, png, "0", "0.5"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    words = r.stdout.split()
+    passes, spp = int(words[1]), int(words[3])
+    # spp = 4 * (2^k - 1) + the repeats of the last size: far more than 4 per pass
+    assert spp >= 16 * passes and spp % 4 == 0, (passes, spp)
+    mean = np.array([float(x) for x in words[5:8]])
+    assert np.all(np.isfinite(mean)) and mean.min() > 0
+    assert _read_png(png).mean() > 20
 
 
 @pytest.mark.gpu
