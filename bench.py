@@ -45,6 +45,15 @@ CPU_SAMPLE = 4_194_304      # rays of the same stream timed on the host cores (~
 NCU_DRAM_BYTES_PER_RAY = (527.964672e6 + 70.359808e6) / 4_194_304
 
 
+def measured_peaks_tensor() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"bf16_tflops": d.get("bf16_tflops", 1900.0), "source": "measured (burst)"}
+    return {"bf16_tflops": 1900.0, "source": "fallback"}
+
+
 def measured_peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -345,6 +354,82 @@ def run_batch(args):
     ctx.close()
 
 
+UNET_FWD_GFLOP_1080P = 305.0  # sum over the 14 convolutions of 2*9*cin*cout*pixels, 1 x 1088 x 1920
+
+
+def run_denoise(args):
+    """The learned denoiser against NLM (the C5 comparison): the held-out 1080p heightfield
+    rendered at 4 spp; the film denoised whole by the U-Net (averaged over the 8 grid
+    symmetries) and by NLM (21x21 search, 7x7 patch, variance-scaled); relMSE on the
+    256x256 window at (832, 412) against an FP64 65,536-spp render of it, the reference's
+    own noise subtracted.  value: the U-Net's relMSE (lower is better); timings are the
+    synchronous calls on device-resident films (best of 3)."""
+    import torch
+    import salty_gb300
+    from salty_gb300 import build as b
+    from salty_gb300 import convergence as cv
+    from salty_gb300 import denoiser as dn
+    from salty_gb300 import scenes
+    b.build()
+    W, H, D, SPP = 1920, 1080, 12, 4
+    crop = (832, 412, 256, 256)
+    ctx = salty_gb300.Context(0)
+    s = scenes.upload(ctx, scenes.heightfield())
+    s.build()
+    ref = cv.reference_image(s, W, H, crop, D, spp=65536)
+    s.render(W, H, SPP, D, seed=4242, want=())
+    film = s.read(W, H)
+    den = dn.Denoiser(ctx)
+
+    def best_of(fn, k=3):
+        fn()
+        torch.cuda.synchronize()
+        t = float("inf")
+        for _ in range(k):
+            t0 = time.perf_counter()
+            out = fn()
+            torch.cuda.synchronize()
+            t = min(t, time.perf_counter() - t0)
+        return out, t * 1e3
+
+    dev = torch.empty((H, W, 3), device="cuda")
+    with ClockSampler(0) as clk:
+        _, unet_ms = best_of(lambda: den.film(s, out=dev))
+        unet = dev.cpu().numpy()
+        mean_d = torch.from_numpy(film["mean"]).cuda()
+        var_d = torch.from_numpy(film["var"]).cuda()
+        nlm_d = torch.empty_like(mean_d)
+        _, nlm_ms = best_of(lambda: ctx.nlm(mean_d, var_d, 10, 3, 0.45, out=nlm_d))
+        nlm = nlm_d.cpu().numpy()
+    clocks = clk.summary()
+    e = {"noisy": cv.corrected_rel_mse(cv.crop_of(film["mean"], crop), ref),
+         "nlm": cv.corrected_rel_mse(cv.crop_of(nlm, crop), ref),
+         "unet": cv.corrected_rel_mse(cv.crop_of(unet, crop), ref)}
+    peaks = measured_peaks_tensor()
+    mirrors = den.mirrors
+    achieved = mirrors * UNET_FWD_GFLOP_1080P / unet_ms  # GFLOP/ms = TFLOP/s
+    line = {
+        "metric": "relMSE of the denoised 4-spp film (256x256 window vs FP64 65,536 spp, reference noise subtracted)",
+        "value": e["unet"], "unit": "relMSE", "n_gpus": 1, "higher_is_better": False, "dtype": "bf16",
+        "data": "synthetic (the held-out heightfield scene generated on the host; weights trained on seeds 1-16)",
+        "config": {"workload": "1920x1080 heightfield (seed 2026, held out), 4 spp, depth 12; U-Net over "
+                               f"{mirrors} grid symmetries vs NLM 21x21/7x7", "window": crop,
+                   "ref_spp": 65536, "ref_noise_rel_mse": ref["noise"]},
+        "rel_mse": e, "unet_vs_nlm": e["nlm"] / e["unet"],
+        "unet_ms_per_frame": unet_ms, "nlm_ms_per_frame": nlm_ms,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                     "frac": achieved / peaks["bf16_tflops"], "traffic": None,
+                     "note": f"{mirrors} forward passes of {UNET_FWD_GFLOP_1080P} GFLOP each, over the whole "
+                             "film denoise call (feature packing and output included)",
+                     "peak_source": peaks["source"]},
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    den.close()
+    s.close()
+    ctx.close()
+
+
 def run_cornell(args):
     """The small Cornell box (36 triangles, area light) at 256 x 256, 16 spp, depth 8, Russian
     roulette from depth 3, the reference-compatible estimator, Reinhard to sRGB8 -- the
@@ -423,7 +508,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (smaller cases for profiling)")
     ap.add_argument("--trace-shape", default="", help="block,regs,pool,postpone instead of salty_autotune_trace")
-    ap.add_argument("--workload", default="traversal", choices=["traversal", "time-to-rmse", "batch", "cornell"])
+    ap.add_argument("--workload", default="traversal",
+                    choices=["traversal", "time-to-rmse", "batch", "cornell", "denoise"])
     ap.add_argument("--scenes", type=int, default=256, help="batch: number of scenes")
     ap.add_argument("--target", type=float, default=0.01, help="time-to-rmse: relRMSE target")
     ap.add_argument("--ref-spp", type=int, default=65536, help="time-to-rmse: samples of the FP64 reference")
@@ -438,6 +524,9 @@ def main():
         return
     if args.workload == "cornell":
         run_cornell(args)
+        return
+    if args.workload == "denoise":
+        run_denoise(args)
         return
     n_rays = args.rays
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
