@@ -13,6 +13,12 @@ Rays (512 MiB) and hits (256 MiB) are larger than L2, so no flush is needed betw
 the BVH (nodes + leaf triangles) stays resident, as in any traversal.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Other workloads (--workload), one JSON line each:
+  time-to-rmse  1080p heightfield: seconds to relRMSE 0.01, plain vs autotuned + U-Net
+  batch         256 uneven scenes in one salty_render_batch vs one call per scene
+  cornell       the 256x256 Cornell box at 16 spp, with the CPU port beside it
+  denoise       U-Net vs NLM on the held-out 4-spp 1080p film (relMSE, time, tensor roofline)
 """
 from __future__ import annotations
 
