@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(kVTile* kVTile) k_nlm_var(const float* __restr
                 for (int c = 0; c < 3; ++c) {
                     const float a = tc[ia + c], b = tc[ib + c], va = tv[ia + c], vb = tv[ib + c];
                     const float num = (a - b) * (a - b) - (va + fminf(va, vb));
-                    d += num / (eps + k2 * (va + vb));
+                    d += __fdividef(num, eps + k2 * (va + vb));  // 2-ulp division: the weights need no IEEE quotient
                 }
                 dd[i] = d;
             }
