@@ -8,6 +8,7 @@
     python -m salty_gb300.profile cornell                            the 256^2 Cornell box, 16 spp
     python -m salty_gb300.profile wave-sweep [--spp 64]              1080p heightfield per wave size
     python -m salty_gb300.profile nlm --h 1080                       1080p NLM vs the FP32 peak
+    python -m salty_gb300.profile tonemap                            tonemap + sRGB8 vs the copy peak
 
 `render` and `unet` print one line of timings; `trace-sweep` times every traversal launch
 shape (block size x register budget x pool x postpone) on the 1M-triangle microbenchmark
@@ -70,6 +71,40 @@ def wave_sweep(spp: int) -> dict:
         res.append({"wave_paths": 1 << e, "ms": best["ms"], "Mrays_s": best["rays"] / best["ms"] / 1e3,
                     "Mpaths_s": best["paths"] / best["ms"] / 1e3})
     return {"workload": f"1920x1080 heightfield, {spp} spp, depth 12, default launch shapes", "waves": res}
+
+
+def tonemap() -> dict:
+    """salty_tonemap_noalloc (Reinhard, linear + sRGB8 outputs) on device-resident images,
+    timed with CUDA events on the caller's stream (mean of 20 calls after 3 warm-ups).
+    Algorithmic bytes per pixel: 12 read for the log-average, 12 read + 12 written + 3
+    written for the map = 39."""
+    import ctypes as C
+    import torch
+    from . import lib, TM_REINHARD
+    ctx = Context(0)
+    st = torch.cuda.current_stream()
+    res = []
+    for w, h in ((1920, 1080), (4096, 4096)):
+        rgb = torch.rand((h, w, 3), device="cuda") * 4.0
+        out = torch.empty_like(rgb)
+        s8 = torch.empty((h, w, 3), dtype=torch.uint8, device="cuda")
+
+        def call():
+            ctx.check(lib().salty_tonemap_noalloc(ctx.h, C.c_void_p(st.cuda_stream), TM_REINHARD, w, h,
+                                                  C.c_void_p(rgb.data_ptr()), C.c_void_p(out.data_ptr()),
+                                                  C.c_void_p(s8.data_ptr()), 1), "tonemap_noalloc")
+        for _ in range(3):
+            call()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(20):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 20
+        gbs = 39.0 * w * h / (ms * 1e-3) / 1e9
+        res.append({"width": w, "height": h, "ms": ms, "GB_s": gbs})
+    return {"workload": "tonemap (Reinhard) + sRGB8, device arrays", "sizes": res}
 
 
 def nlm(h: int, w: int) -> dict:
@@ -157,7 +192,7 @@ def trace_sweep() -> dict:
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("what", choices=["render", "unet", "trace-sweep", "cornell", "wave-sweep", "nlm"])
+    ap.add_argument("what", choices=["render", "unet", "trace-sweep", "cornell", "wave-sweep", "nlm", "tonemap"])
     ap.add_argument("--spp", type=int, default=None, help="render: 1, wave-sweep: 64")
     ap.add_argument("--frames", type=int, default=2)
     ap.add_argument("--width", type=int, default=1920)
@@ -174,6 +209,8 @@ def main(argv=None):
         r = unet(a.n, a.h, a.w, a.conv, a.train)
     elif a.what == "cornell":
         r = cornell()
+    elif a.what == "tonemap":
+        r = tonemap()
     elif a.what == "nlm":
         r = nlm(a.h, a.w)
     elif a.what == "wave-sweep":
