@@ -345,7 +345,8 @@ salty_status salty_tonemap(salty_ctx* ctx, int32_t type, int32_t width, int32_t 
  *   - Every call reuses the same array and overwrites all of it that it reads, so nothing
  *     carries over between calls -- but calls that overlap on the GPU (other streams,
  *     other host threads) race on it: serialise them.
- * Results equal salty_tonemap's up to the order of the log-luminance sum. */
+ * Results equal salty_tonemap's up to the order of the log-luminance sum (16-byte aligned
+ * inputs add four pixels' logarithms in FP32 before the FP64 sum). */
 salty_status salty_tonemap_noalloc(salty_ctx* ctx, void* stream, int32_t type, int32_t width, int32_t height,
                                    const float* d_rgb, float* d_out_rgb, uint8_t* d_out_srgb8, int32_t ref_oetf);
 

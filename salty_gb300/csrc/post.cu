@@ -8,6 +8,7 @@
 //   double, where the reference adds them one by one in single precision.
 //   FilterNLM (src/s3d_denoiser.cpp:19-95): each block stages its tile plus halo in
 //   shared memory and evaluates the reference's weights in the reference's order.
+#include <algorithm>
 #include <cfloat>
 #include <cstring>
 
@@ -405,20 +406,38 @@ struct NoAllocScratch {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
 // Per-block luminance partials in a fixed pixel-to-block mapping (deterministic).
-__global__ void __launch_bounds__(kRedBlock) k_lum_partials(const float* __restrict__ rgb, long long npx,
-                                                            NoAllocScratch* sc) {
+// log(eps + Lw) of one pixel, with the reference's guards, and the running maximum of Lw.
+__device__ __forceinline__ float lum_log(float r, float g, float b, float& mx) {
     const float eps = 0.00001f;
+    float lw = rgb_to_y(r, g, b);
+    if (lw != lw) lw = eps;
+    if (lw < FLT_EPSILON) lw = eps;
+    mx = fmaxf(mx, lw);
+    return logf(__fadd_rn(eps, lw));
+}
+
+// vec: rgb is 16-byte aligned -- four pixels (three float4) per load step, their four logs
+// summed in FP32 before the FP64 running sum (a quarter of the FP64 additions).
+__global__ void __launch_bounds__(kRedBlock) k_lum_partials(const float* __restrict__ rgb, long long npx,
+                                                            NoAllocScratch* sc, int vec) {
     const long long b0 = (long long)blockIdx.x * kNoAllocPixelsPerBlock;
     const long long b1 = min(npx, b0 + kNoAllocPixelsPerBlock);
     double s = 0.0;
     float mx = -FLT_MAX;
-    for (long long i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-        float lw = rgb_to_y(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
-        if (lw != lw) lw = eps;
-        if (lw < FLT_EPSILON) lw = eps;
-        mx = fmaxf(mx, lw);
-        s += (double)logf(__fadd_rn(eps, lw));
+    long long i0 = b0;
+    if (vec) {
+        const float4* q = reinterpret_cast<const float4*>(rgb);
+        const long long ge = b1 / 4;  // b0 is a multiple of 4
+        for (long long gi = b0 / 4 + threadIdx.x; gi < ge; gi += blockDim.x) {
+            const float4 a = __ldg(q + 3 * gi), b = __ldg(q + 3 * gi + 1), c = __ldg(q + 3 * gi + 2);
+            const float l4 = lum_log(a.x, a.y, a.z, mx) + lum_log(a.w, b.x, b.y, mx) + lum_log(b.z, b.w, c.x, mx) +
+                             lum_log(c.y, c.z, c.w, mx);
+            s += (double)l4;
+        }
+        i0 = ge * 4;
     }
+    for (long long i = i0 + threadIdx.x; i < b1; i += blockDim.x)
+        s += (double)lum_log(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], mx);
     for (int off = 16; off > 0; off >>= 1) {
         s += __shfl_xor_sync(0xffffffffu, s, off);
         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
@@ -476,18 +495,48 @@ __global__ void __launch_bounds__(kRedBlock) k_lum_finalize(NoAllocScratch* sc, 
     sc->ave_max[1] = max_lw;
 }
 
+__device__ __forceinline__ float tm_curve(float v, const TmParams& p) {
+    const float x = __fmul_rn(v, p.coeff);
+    if (p.type == SALTY_TM_ACES) return aces_curve(x);
+    if (p.type == SALTY_TM_UNCHARTED2) return __fdiv_rn(u2_curve(__fmul_rn(2.0f, x)), p.white);
+    return __fdiv_rn(__fmul_rn(x, __fadd_rn(1.0f, __fdiv_rn(x, p.m2))), __fadd_rn(1.0f, x));
+}
+
 __global__ void k_tonemap_params(const float* __restrict__ in, long long n, const NoAllocScratch* __restrict__ sc,
                                  float* __restrict__ out, unsigned char* __restrict__ srgb) {
     const TmParams p = sc->params;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        const float x = __fmul_rn(in[i], p.coeff);
-        float y;
-        if (p.type == SALTY_TM_ACES) y = aces_curve(x);
-        else if (p.type == SALTY_TM_UNCHARTED2) y = __fdiv_rn(u2_curve(__fmul_rn(2.0f, x)), p.white);
-        else y = __fdiv_rn(__fmul_rn(x, __fadd_rn(1.0f, __fdiv_rn(x, p.m2))), __fadd_rn(1.0f, x));
+        const float y = tm_curve(in[i], p);
         if (out) out[i] = y;
         if (srgb) srgb[i] = to_srgb8(y, p.ref_oetf);
+    }
+}
+
+// The same map, four pixels (twelve values) per step: three 16-byte loads and stores and
+// three 4-byte sRGB8 words.  in/out 16-byte aligned, srgb 4-byte aligned.
+__global__ void k_tonemap_params4(const float4* __restrict__ in, long long groups, const NoAllocScratch* __restrict__ sc,
+                                  float4* __restrict__ out, uint32_t* __restrict__ srgb) {
+    const TmParams p = sc->params;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < groups;
+         g += (long long)gridDim.x * blockDim.x) {
+        float4 q[3] = {__ldg(in + 3 * g), __ldg(in + 3 * g + 1), __ldg(in + 3 * g + 2)};
+        float* v = reinterpret_cast<float*>(q);
+#pragma unroll
+        for (int k = 0; k < 12; ++k) v[k] = tm_curve(v[k], p);
+        if (out) {
+            out[3 * g] = q[0];
+            out[3 * g + 1] = q[1];
+            out[3 * g + 2] = q[2];
+        }
+        if (srgb) {
+#pragma unroll
+            for (int w = 0; w < 3; ++w)
+                srgb[3 * g + w] = (uint32_t)to_srgb8(v[4 * w], p.ref_oetf) |
+                                  ((uint32_t)to_srgb8(v[4 * w + 1], p.ref_oetf) << 8) |
+                                  ((uint32_t)to_srgb8(v[4 * w + 2], p.ref_oetf) << 16) |
+                                  ((uint32_t)to_srgb8(v[4 * w + 3], p.ref_oetf) << 24);
+        }
     }
 }
 
@@ -540,12 +589,25 @@ extern "C" salty_status salty_tonemap_noalloc(salty_ctx* ctx, void* stream, int3
     SALTY_TRY_CUDA(E, noalloc_scratch(ctx->device, &sc));
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     const int nparts = (int)((npx + kNoAllocPixelsPerBlock - 1) / kNoAllocPixelsPerBlock);
-    k_lum_partials<<<nparts, kRedBlock, 0, st>>>(d_rgb, npx, sc);
+    auto aligned = [](const void* p, uintptr_t a) { return p == nullptr || reinterpret_cast<uintptr_t>(p) % a == 0; };
+    const bool vec = aligned(d_rgb, 16) && aligned(d_out_rgb, 16) && aligned(d_out_srgb8, 4);
+    k_lum_partials<<<nparts, kRedBlock, 0, st>>>(d_rgb, npx, sc, aligned(d_rgb, 16) ? 1 : 0);
     k_lum_finalize<<<1, kRedBlock, 0, st>>>(sc, nparts, npx, type, ref_oetf);
     const long long n = npx * 3;
-    long long g = (n + 255) / 256;
-    if (g > (long long)ctx->num_sms * 8) g = (long long)ctx->num_sms * 8;
-    k_tonemap_params<<<(unsigned)g, 256, 0, st>>>(d_rgb, n, sc, d_out_rgb, d_out_srgb8);
+    const long long groups = vec ? npx / 4 : 0;  // whole groups of four pixels
+    const long long done = groups * 12;          // channel values the vector kernel maps
+    const long long cap = (long long)ctx->num_sms * 8;
+    if (groups > 0) {
+        const long long g4 = std::min((groups + 255) / 256, cap);
+        k_tonemap_params4<<<(unsigned)g4, 256, 0, st>>>(reinterpret_cast<const float4*>(d_rgb), groups, sc,
+                                                         reinterpret_cast<float4*>(d_out_rgb),
+                                                         reinterpret_cast<uint32_t*>(d_out_srgb8));
+    }
+    if (n > done) {
+        const long long g = std::min((n - done + 255) / 256, cap);
+        k_tonemap_params<<<(unsigned)g, 256, 0, st>>>(d_rgb + done, n - done, sc, d_out_rgb ? d_out_rgb + done : nullptr,
+                                                      d_out_srgb8 ? d_out_srgb8 + done : nullptr);
+    }
     SALTY_TRY_CUDA(E, cudaGetLastError());
     return SALTY_OK;
 }

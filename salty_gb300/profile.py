@@ -75,14 +75,16 @@ def wave_sweep(spp: int) -> dict:
 
 def tonemap() -> dict:
     """salty_tonemap_noalloc (Reinhard, linear + sRGB8 outputs) on device-resident images,
-    timed with CUDA events on the caller's stream (mean of 20 calls after 3 warm-ups).
+    timed with CUDA events on the caller's stream, a torch stream of its own (a NULL stream
+    would mean the library's stream, which torch's events do not see); mean of 20 calls after
+    3 warm-ups.
     Algorithmic bytes per pixel: 12 read for the log-average, 12 read + 12 written + 3
     written for the map = 39."""
     import ctypes as C
     import torch
     from . import lib, TM_REINHARD
     ctx = Context(0)
-    st = torch.cuda.current_stream()
+    st = torch.cuda.Stream()
     res = []
     for w, h in ((1920, 1080), (4096, 4096)):
         rgb = torch.rand((h, w, 3), device="cuda") * 4.0
@@ -93,13 +95,15 @@ def tonemap() -> dict:
             ctx.check(lib().salty_tonemap_noalloc(ctx.h, C.c_void_p(st.cuda_stream), TM_REINHARD, w, h,
                                                   C.c_void_p(rgb.data_ptr()), C.c_void_p(out.data_ptr()),
                                                   C.c_void_p(s8.data_ptr()), 1), "tonemap_noalloc")
-        for _ in range(3):
-            call()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(20):
-            call()
-        e1.record()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(st):
+            for _ in range(3):
+                call()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(20):
+                call()
+            e1.record(st)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / 20
         gbs = 39.0 * w * h / (ms * 1e-3) / 1e9
