@@ -45,10 +45,12 @@ TMIN = 1e-4
 METRIC = "Mrays/s"
 CPU_SAMPLE = 4_194_304      # rays of the same stream timed on the host cores (~10 s of CPU work)
 # DRAM bytes (read + write) per ray of the closest-hit k_trace launch, from the ncu capture
-# of that kernel (128 threads, 64 registers) on the same soup at 4,194,304 rays
-# (profiles/trace_closest_soup1m_4Mrays.md); the traffic (rays in, hits out, L2 misses)
-# scales with the ray count, so traffic per launch is this figure times the rays of the launch.
-NCU_DRAM_BYTES_PER_RAY = (527.964672e6 + 70.359808e6) / 4_194_304
+# of that kernel at the launch shape salty_autotune_trace picks here (256 threads, 64
+# registers, pool 64, postpone 7) on the same soup at 4,194,304 rays
+# (profiles/trace_closest_soup1m_4Mrays.md; 142.6 B/ray at 128 threads); the traffic (rays
+# in, hits out, L2 misses) scales with the ray count, so traffic per launch is this figure
+# times the rays of the launch.
+NCU_DRAM_BYTES_PER_RAY = (530.681856e6 + 69.582848e6) / 4_194_304
 
 
 def measured_peaks_tensor() -> dict:
