@@ -119,3 +119,25 @@ def test_bench_reads_the_measured_peaks():
         assert t["bf16_tflops"] == d["bf16_tflops"]
     else:
         assert p["source"] == "fallback" and t["source"] == "fallback"
+
+
+def test_clock_sampler_summary_reports_median_max_and_throttle_reasons(tmp_path):
+    """The bench's nvidia-smi sampling: median SM clock under the timed region, the maximum
+    clock, and every throttle reason seen Active (a run showing hw_slowdown or a thermal
+    slowdown is to be taken again; sw_power_cap is kept and noted)."""
+    import bench
+    rows = [
+        "0, 2070, 2070, 900.5, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 2055, 2070, 1390.1, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "0, 1980, 2070, 1395.0, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "garbage line",
+    ]
+    p = tmp_path / "clocks.csv"
+    p.write_text("\n".join(rows) + "\n")
+    s = bench.ClockSampler(0)
+    s.path = str(p)
+    out = s.summary()
+    assert out == {"sm_mhz": 2055.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    assert not os.path.exists(p)  # the sample file is removed once read
+    s2 = bench.ClockSampler(0)
+    assert s2.summary() is None  # no nvidia-smi, no samples
