@@ -67,3 +67,22 @@ def test_microbench_rays_are_unit_and_aimed_at_the_cube(salty_lib):
     assert np.all(r[:, 3] == np.float32(1e-4)) and np.all(np.isinf(r[:, 7]))
     # origin on the sphere is uniform: mean near the centre
     assert np.all(np.abs(o.mean(axis=0) - 0.5) < 0.05)
+
+
+def test_header_is_plain_c99_and_links(salty_lib, tmp_path):
+    """A C host (an FFI binding, a C caller) includes salty_gpu.h as strict C99 and links the
+    library; the version query needs no GPU."""
+    import shutil
+    import salty_gb300
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    src = tmp_path / "abi.c"
+    src.write_text('#include "salty_gpu.h"\n'
+                   "int main(void) { salty_ctx* c = 0; (void)c; return salty_abi_version() > 0 ? 0 : 1; }\n")
+    exe = str(tmp_path / "abi")
+    libdir = os.path.dirname(salty_gb300.LIB_PATH)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Wpedantic", "-Werror",
+                        f"-I{os.path.join(ROOT, 'include')}", str(src), f"-L{libdir}", "-lsalty_gpu",
+                        f"-Wl,-rpath,{libdir}", "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([exe]).returncode == 0
