@@ -19,10 +19,18 @@ Other workloads (--workload), one JSON line each:
   batch         256 uneven scenes in one salty_render_batch vs one call per scene
   cornell       the 256x256 Cornell box at 16 spp, with the CPU port beside it
   denoise       U-Net vs NLM on the held-out 4-spp 1080p film (relMSE, time, tensor roofline)
+Profiling workloads (fixed small cases to time alone or under ncu):
+  render        1080p heightfield frames (--spp, --frames, --width, --height)
+  wave-sweep    1080p heightfield at --spp for waves of 2^22..2^27 paths
+  trace-sweep   every traversal launch shape on the microbenchmark
+  unet          U-Net forward passes / training steps (--unet-n/-h/-w, --conv, --train)
+  nlm           variance-scaled NLM on a --width x --height image vs the nominal FP32 peak
+  tonemap       salty_tonemap_noalloc at 1080p and 4096^2 vs the copy peak
 """
 from __future__ import annotations
 
 import argparse
+import itertools
 import json
 import math
 import os
@@ -44,12 +52,11 @@ SOUP_SEED, RAY_SEED = 20260001, 20260002
 TMIN = 1e-4
 METRIC = "Mrays/s"
 CPU_SAMPLE = 4_194_304      # rays of the same stream timed on the host cores (~10 s of CPU work)
-# DRAM bytes (read + write) per ray of the closest-hit k_trace launch, from the ncu capture
+# DRAM bytes (read + write) per ray of the closest-hit k_trace launch, from one ncu capture
 # of that kernel at the launch shape salty_autotune_trace picks here (256 threads, 64
-# registers, pool 64, postpone 7) on the same soup at 4,194,304 rays
-# (profiles/trace_closest_soup1m_4Mrays.md; 142.6 B/ray at 128 threads); the traffic (rays
-# in, hits out, L2 misses) scales with the ray count, so traffic per launch is this figure
-# times the rays of the launch.
+# registers, pool 64, postpone 7) on the same soup at 4,194,304 rays; the traffic (rays in,
+# hits out, L2 misses) scales with the ray count, so traffic per launch is this figure times
+# the rays of the launch.
 NCU_DRAM_BYTES_PER_RAY = (530.681856e6 + 69.582848e6) / 4_194_304
 
 
@@ -506,6 +513,210 @@ def run_cornell(args):
     ctx.close()
 
 
+# ---------------------------------------------------------------- profiling workloads
+# Small fixed workloads to time alone or to run under ncu: `bench.py --workload NAME`
+# prints one JSON line of timings (render, unet, trace-sweep, wave-sweep, nlm, tonemap,
+# prof-cornell).
+
+
+def fp32_nominal_tflops() -> float:
+    """SMs x 128 FP32 lanes x 2 flops (a fused multiply-add) x the maximum SM clock."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = 2070.0
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            mhz = float(json.load(f).get("sm_max_mhz", mhz))
+    return sms * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def prof_render(spp: int, frames: int, width: int = 1920, height: int = 1080) -> dict:
+    """The 1080p heightfield: `frames` renders of `spp` samples, depth 12, default launch
+    shapes; device time and rays per frame."""
+    from salty_gb300 import Context, scenes
+    ctx = Context(0)
+    s = scenes.upload(ctx, scenes.heightfield())
+    info = s.build()
+    out = []
+    for i in range(frames):
+        r = s.render(width, height, spp, 12, seed=3 + i, want=())
+        out.append({"ms": r["ms"], "rays": r["rays"], "paths": r["paths"], "Mrays_s": r["rays"] / r["ms"] / 1e3})
+    return {"workload": f"{width}x{height} heightfield, {spp} spp x {frames} frames", "bvh_build_ms": info["build_ms"],
+            "frames": out}
+
+
+def prof_wave_sweep(spp: int) -> dict:
+    """The 1080p heightfield at `spp` samples, depth 12, default launch shapes, for waves of
+    2^22 .. 2^27 paths: best of two renders each after an 8-spp warm-up."""
+    from salty_gb300 import Context, scenes
+    ctx = Context(0)
+    s = scenes.upload(ctx, scenes.heightfield())
+    s.build()
+    base = ctx.tuning
+    res = []
+    for e in range(22, 28):
+        t = dict(base)
+        t["wave_paths"] = 1 << e
+        ctx.tuning = t
+        s.render(1920, 1080, 8, 12, seed=1, want=())
+        best = min((s.render(1920, 1080, spp, 12, seed=2 + i, want=()) for i in range(2)), key=lambda r: r["ms"])
+        res.append({"wave_paths": 1 << e, "ms": best["ms"], "Mrays_s": best["rays"] / best["ms"] / 1e3,
+                    "Mpaths_s": best["paths"] / best["ms"] / 1e3})
+    return {"workload": f"1920x1080 heightfield, {spp} spp, depth 12, default launch shapes", "waves": res}
+
+
+def prof_tonemap() -> dict:
+    """salty_tonemap_noalloc (Reinhard, linear + sRGB8 outputs) on device-resident images,
+    timed with CUDA events on the caller's stream, a torch stream of its own (a NULL stream
+    would mean the library's stream, which torch's events do not see); mean of 20 calls after
+    3 warm-ups.
+    Algorithmic bytes per pixel: 12 read for the log-average, 12 read + 12 written + 3
+    written for the map = 39."""
+    import ctypes as C
+    import torch
+    from salty_gb300 import lib, TM_REINHARD
+    from salty_gb300 import Context
+    ctx = Context(0)
+    st = torch.cuda.Stream()
+    res = []
+    for w, h in ((1920, 1080), (4096, 4096)):
+        rgb = torch.rand((h, w, 3), device="cuda") * 4.0
+        out = torch.empty_like(rgb)
+        s8 = torch.empty((h, w, 3), dtype=torch.uint8, device="cuda")
+
+        def call():
+            ctx.check(lib().salty_tonemap_noalloc(ctx.h, C.c_void_p(st.cuda_stream), TM_REINHARD, w, h,
+                                                  C.c_void_p(rgb.data_ptr()), C.c_void_p(out.data_ptr()),
+                                                  C.c_void_p(s8.data_ptr()), 1), "tonemap_noalloc")
+        torch.cuda.synchronize()
+        with torch.cuda.stream(st):
+            for _ in range(3):
+                call()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(20):
+                call()
+            e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 20
+        gbs = 39.0 * w * h / (ms * 1e-3) / 1e9
+        res.append({"width": w, "height": h, "ms": ms, "GB_s": gbs})
+    return {"workload": "tonemap (Reinhard) + sRGB8, device arrays", "sizes": res}
+
+
+def prof_nlm(h: int, w: int) -> dict:
+    """salty_denoise_nlm (21x21 search, 7x7 patch) on a w x h device-resident image: the
+    best of 5 host-timed synchronous calls, against the nominal FP32 peak (SMs x 128 lanes x
+    2 flops x the maximum SM clock).  Algorithmic work of the filter: 441 offsets x 49 taps
+    x 3 channels x 3 flops (difference, square, sum) = 194,481 FP32 flops per pixel."""
+    import torch
+    from salty_gb300 import Context
+    ctx = Context(0)
+    peak = fp32_nominal_tflops()
+    g = torch.Generator(device="cuda").manual_seed(1)
+    rgb = torch.rand((h, w, 3), device="cuda", generator=g)
+    var = torch.rand((h, w, 3), device="cuda", generator=g) * 0.01
+    out = torch.empty_like(rgb)
+    ctx.nlm(rgb, var, 10, 3, 0.45, out=out)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        t0 = time.perf_counter()
+        ctx.nlm(rgb, var, 10, 3, 0.45, out=out)
+        torch.cuda.synchronize()
+        best = min(best, (time.perf_counter() - t0) * 1e3)
+    flops = 194481.0 * w * h
+    ach = flops / (best * 1e-3) / 1e12
+    return {"workload": f"NLM 21x21 search, 7x7 patch, {w}x{h}", "ms": best, "algorithmic_tflops": ach,
+            "fp32_peak_tflops": peak, "peak_source": "nominal", "frac": ach / peak}
+
+
+def prof_unet(n: int, h: int, w: int, conv: str = "tcgen05", train: bool = False) -> dict:
+    """Forward passes (and, with train, training steps at lr 0) on random features: the
+    best of 5 wall-clock times after a warm-up, per convolution kernel."""
+    import torch
+    from salty_gb300 import CONV_MMA_SYNC, CONV_TCGEN05, CONV_TCGEN05_CP_ASYNC, UNET_FEATURES, Unet
+    from salty_gb300 import Context
+    ctx = Context(0)
+    net = Unet(ctx, seed=1)
+    f = torch.rand((n, h, w, UNET_FEATURES), device="cuda")
+    o = torch.empty((n, h, w, 3), device="cuda")
+    tgt = torch.rand((n, h, w, 3), device="cuda")
+    names = {CONV_TCGEN05: "tcgen05", CONV_TCGEN05_CP_ASYNC: "tcgen05_cp_async", CONV_MMA_SYNC: "mma_sync"}
+    kinds = {"tcgen05": [CONV_TCGEN05], "tcgen05_cp_async": [CONV_TCGEN05_CP_ASYNC], "mma_sync": [CONV_MMA_SYNC],
+             "all": [CONV_TCGEN05, CONV_TCGEN05_CP_ASYNC, CONV_MMA_SYNC]}[conv]
+    res = {"workload": f"U-Net {n}x{h}x{w}"}
+    for k in kinds:
+        net.set_conv_kernel(k)
+        name = names[k]
+        steps = [("forward_ms", lambda: net.forward(f, out=o))]
+        if train:
+            steps.append(("train_step_ms", lambda: net.train_step(f, tgt, lr=0.0)))
+        for key, fn in steps:
+            fn()
+            torch.cuda.synchronize()
+            best = float("inf")
+            for _ in range(5):
+                t0 = time.perf_counter()
+                fn()
+                torch.cuda.synchronize()
+                best = min(best, (time.perf_counter() - t0) * 1e3)
+            res[f"{name}_{key}"] = best
+    net.close()
+    return res
+
+
+def prof_trace_sweep() -> dict:
+    """Every traversal launch shape (block x registers x pool x postpone) on the microbenchmark
+    (1M triangles, 16,777,216 rays, closest hit): kernel time, and whether the hits are the
+    same as the first shape's."""
+    import torch
+    from salty_gb300 import Context
+    ctx = Context(0)
+    from salty_gb300 import microbench_rays, microbench_soup
+    sc = ctx.upload_scene(microbench_soup(20260001, 1_000_000))
+    sc.build()
+    n = 16_777_216
+    rays = torch.from_numpy(microbench_rays(20260002, n, 1e-4)).cuda()
+    hits = torch.empty((n, 4), device="cuda")
+    ref, res = None, []
+    for blk, regs, pool, post in itertools.product((64, 128, 256), (64, 48), (64, 128, 256), (1, 4, 7, 10)):
+        ctx.tuning = {"trace_block": blk, "trace_regs": regs, "trace_pool": pool, "trace_postpone": post}
+        for _ in range(2):
+            sc.trace_raw(rays, hits)
+        ms = min(sc.trace_raw(rays, hits)["kernel_ms"] for _ in range(4))
+        ids = hits.cpu().numpy().view(np.int32)[:, 1]
+        if ref is None:
+            ref = ids.copy()
+        res.append({"ms": ms, "Mrays_s": n / ms / 1e3, "trace_block": blk, "trace_regs": regs, "trace_pool": pool,
+                    "trace_postpone": post, "same_hits": bool(np.array_equal(ids, ref))})
+    res.sort(key=lambda r: r["ms"])
+    return {"workload": "traversal microbenchmark, 1M triangles, 16,777,216 rays, closest hit", "shapes": res}
+
+
+PROFILING = ("render", "unet", "trace-sweep", "wave-sweep", "nlm", "tonemap")
+
+
+def run_profiling(args) -> None:
+    from salty_gb300 import build as b
+    b.build()
+    w = args.workload
+    if w == "render":
+        r = prof_render(args.spp or 1, args.frames, args.width, args.height)
+    elif w == "unet":
+        r = prof_unet(args.unet_n, args.unet_h, args.unet_w, args.conv, args.train)
+    elif w == "trace-sweep":
+        r = prof_trace_sweep()
+    elif w == "wave-sweep":
+        r = prof_wave_sweep(args.spp or 64)
+    elif w == "nlm":
+        r = prof_nlm(args.height, args.width)
+    else:
+        r = prof_tonemap()
+    print(json.dumps(r), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -517,13 +728,25 @@ def main():
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (smaller cases for profiling)")
     ap.add_argument("--trace-shape", default="", help="block,regs,pool,postpone instead of salty_autotune_trace")
     ap.add_argument("--workload", default="traversal",
-                    choices=["traversal", "time-to-rmse", "batch", "cornell", "denoise"])
+                    choices=["traversal", "time-to-rmse", "batch", "cornell", "denoise", *PROFILING])
     ap.add_argument("--scenes", type=int, default=256, help="batch: number of scenes")
     ap.add_argument("--target", type=float, default=0.01, help="time-to-rmse: relRMSE target")
     ap.add_argument("--ref-spp", type=int, default=65536, help="time-to-rmse: samples of the FP64 reference")
     ap.add_argument("--max-spp", type=int, default=1 << 17, help="time-to-rmse: give up beyond this")
     ap.add_argument("--methods", default="plain,unet", help="time-to-rmse: plain,unet,nlm")
+    ap.add_argument("--spp", type=int, default=None, help="render: 1, wave-sweep: 64")
+    ap.add_argument("--frames", type=int, default=2, help="render: frames")
+    ap.add_argument("--width", type=int, default=1920, help="render, nlm: image width")
+    ap.add_argument("--height", type=int, default=1080, help="render, nlm: image height")
+    ap.add_argument("--unet-n", type=int, default=1, help="unet: images per batch")
+    ap.add_argument("--unet-h", type=int, default=1088, help="unet: image height (multiple of 16)")
+    ap.add_argument("--unet-w", type=int, default=1920, help="unet: image width (multiple of 16)")
+    ap.add_argument("--conv", default="tcgen05", choices=["tcgen05", "tcgen05_cp_async", "mma_sync", "all"])
+    ap.add_argument("--train", action="store_true", help="unet: also time training steps")
     args = ap.parse_args()
+    if args.workload in PROFILING:
+        run_profiling(args)
+        return
     if args.workload == "time-to-rmse":
         run_time_to_rmse(args)
         return

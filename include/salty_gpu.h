@@ -329,24 +329,29 @@ salty_status salty_tonemap(salty_ctx* ctx, int32_t type, int32_t width, int32_t 
                            float* ave_lw, float* max_lw);
 
 /* salty_tonemap, for callers that must not allocate device memory when they tonemap.
- * No counterpart in the reference: it exists for hosts such as a real-time viewer that
- * tonemaps every frame inside its render loop, a CUDA-graph capture (where cudaMalloc is
- * not allowed), or an engine that owns all GPU memory and forbids allocation after start-up
- * -- cudaMalloc also synchronises the device, which such loops cannot afford.
- *   - Arrays are device memory only: d_rgb (W*H*3 float), d_out_rgb and/or d_out_srgb8
- *     (either may be NULL, not both).  The call allocates nothing and does not wait: it
- *     enqueues three kernels on `stream` (a cudaStream_t; NULL = the context's stream) and
- *     returns; synchronise the stream before reading the outputs.
+ * No counterpart in the reference: it exists for hosts that cannot call cudaMalloc at the
+ * point where they tonemap -- a real-time viewer that tonemaps every frame inside its
+ * render loop (cudaMalloc synchronises the whole device, which such a loop cannot afford),
+ * or an engine that owns all GPU memory and forbids allocation after start-up.
+ *   - Arrays are device memory of the context's GPU only: d_rgb (W*H*3 float), d_out_rgb
+ *     and/or d_out_srgb8 (either may be NULL, not both).  The call allocates nothing and
+ *     does not wait: it enqueues three kernels on `stream` (a cudaStream_t; NULL = the
+ *     context's own stream) and returns; synchronise that stream before reading the outputs.
+ *   - The context's own stream does not wait for work on other streams (the legacy default
+ *     stream included, where most callers produce d_rgb): order the work that writes d_rgb
+ *     before the call (an event or a synchronisation), or pass the producer's own stream.
  *   - Its scratch is a fixed 64 KiB device array inside the library, present on every GPU
  *     that loads the library until the process exits; images are limited to 16,777,216
  *     pixels (4096 x 4096).  Larger images return SALTY_ERR_CAPACITY before any launch.
  *   - The first call on each device looks up that array's device address once (with the
- *     device current); make that first call before capturing the stream into a graph.
+ *     device current); make that first call before any stream capture.
  *   - Every call reuses the same array and overwrites all of it that it reads, so nothing
  *     carries over between calls -- but calls that overlap on the GPU (other streams,
  *     other host threads) race on it: serialise them.
- * Results equal salty_tonemap's up to the order of the log-luminance sum (16-byte aligned
- * inputs add four pixels' logarithms in FP32 before the FP64 sum). */
+ * Results equal salty_tonemap's to within rounding: the log-luminance sum is added in a
+ * different order (16-byte aligned inputs add four pixels' logarithms in FP32 before the
+ * FP64 sum), and the log-average's exponential and the curve parameters are evaluated on
+ * the GPU rather than on the host, so the scale factor can differ in the last bits. */
 salty_status salty_tonemap_noalloc(salty_ctx* ctx, void* stream, int32_t type, int32_t width, int32_t height,
                                    const float* d_rgb, float* d_out_rgb, uint8_t* d_out_srgb8, int32_t ref_oetf);
 
@@ -356,10 +361,6 @@ salty_status salty_denoise_nlm_ref(salty_ctx* ctx, int32_t width, int32_t height
 
 /* Variance-scaled NLM on RGB with per-pixel variance of the mean (W*H*3 each):
  * search window (2 search_r + 1)^2, patch (2 patch_r + 1)^2, strength k. */
-/* Diagnostics: this GPU's FP32 CUDA-core throughput (fused multiply-adds, 2 flops each), in
- * TFLOP/s, measured by a microkernel with CUDA events -- the peak the NLM kernels' roofline
- * is quoted against.  No counterpart in the reference. */
-salty_status salty_fp32_peak(salty_ctx* ctx, double* tflops);
 salty_status salty_denoise_nlm(salty_ctx* ctx, int32_t width, int32_t height, int32_t search_r,
                                int32_t patch_r, float k, const float* rgb, const float* var,
                                float* out);

@@ -485,10 +485,14 @@ static void rscene_init(rscene* r, const oracle_scene* sc) {
         r->sun_dir = unit(ld3(sc->sun_dir));
         r->sun_disk = sc->sun_half_angle > 0.0f;
         r->sun_cos_max = (float)cos((double)sc->sun_half_angle);
-        double omega = 2.0 * 3.14159265358979323846 * (1.0 - cos((double)sc->sun_half_angle));
+        /* uniform cone sampling pdf 1/omega; radiance L with L pi sin^2 = sun_radiance, the
+           irradiance on a surface facing the sun */
+        double ca = cos((double)sc->sun_half_angle);
+        double omega = 2.0 * 3.14159265358979323846 * (1.0 - ca);
+        double facing = 3.14159265358979323846 * (1.0 - ca) * (1.0 + ca);
         r->sun_pdf = r->sun_disk ? (float)(1.0 / omega) : 0.0f;
-        r->sun_L = r->sun_disk ? mk((float)(sc->sun_radiance[0] / omega), (float)(sc->sun_radiance[1] / omega),
-                                    (float)(sc->sun_radiance[2] / omega))
+        r->sun_L = r->sun_disk ? mk((float)(sc->sun_radiance[0] / facing), (float)(sc->sun_radiance[1] / facing),
+                                    (float)(sc->sun_radiance[2] / facing))
                                : mk(0, 0, 0);
         tangent_space(r->sun_dir, &r->sun_t, &r->sun_b);
     }
@@ -732,11 +736,30 @@ static v3 compat_radiance(const rscene* r, v3 o, v3 d, int max_bounce, opcg* rnd
  * Schlick Fresnel and separable Smith G (NDF sampling as SampleGGX, include/s3d_math.h:
  * 2985-2993, alpha = roughness^2).  NEE to the one-sided quad light with balance-heuristic
  * MIS, NEE to a delta sun, constant sky on escape, Russian roulette from rr_depth with
- * survival min(0.95, max W).  Ray epsilon 1e-4.  Random numbers per (pixel, sample) stream,
+ * survival min(1, max W), rolled only while it is below 1.  Camera rays start at t = 1e-4, rays leaving a surface at t = 0
+ * from an origin pushed off it (spawn).  Random numbers per (pixel, sample) stream,
  * consumed in this order: jitter x, y; per vertex: light point u, v (non-delta, light
  * present); BSDF (Lambert 2, glass 1, GGX 2, mirror 0, Phong 2, plastic 3); RR 1
- * (depth >= rr_depth). */
+ * (depth >= rr_depth and survival below 1). */
 static const float kEps = 1e-4f;
+
+/* Origin of a ray leaving the surface point p in direction w: p pushed off the surface along
+ * the geometric normal ng (either orientation) to the side w points to, by 256 units in the
+ * last place of each coordinate, or by 2^-16 near the world origin where ulps are tiny
+ * (Waechter and Binder, "A Fast and Robust Method for Avoiding Self-Intersection", Ray
+ * Tracing Gems, 2019).  Rays spawned this way start at t = 0. */
+static float nudge(float p, float n) {
+    int32_t o = (int32_t)(256.0f * n), b;
+    float q;
+    memcpy(&b, &p, 4);
+    b += p < 0.0f ? -o : o;
+    memcpy(&q, &b, 4);
+    return fabsf(p) < 1.0f / 32.0f ? p + n * (1.0f / 65536.0f) : q;
+}
+static v3 spawn(v3 p, v3 ng, v3 w) {
+    v3 n = dot(ng, w) >= 0.0f ? ng : neg(ng);
+    return mk(nudge(p.x, n.x), nudge(p.y, n.y), nudge(p.z, n.z));
+}
 
 static float ggx_d(float nh, float a2) {
     float k = nh * nh * (a2 - 1.0f) + 1.0f;
@@ -805,10 +828,10 @@ static v3 phys_eval(const oracle_material* m, v3 n, v3 wo, v3 wi, float* pdf) {
 static v3 phys_radiance(const rscene* r, v3 o, v3 d, const oracle_render_opts* opt, opcg* rnd) {
     const oracle_scene* sc = r->sc;
     v3 W = mk(1, 1, 1), L = mk(0, 0, 0);
-    int prev_delta = 1; float prev_pdf = 0.0f;
+    int prev_delta = 1; float prev_pdf = 0.0f, tmin = kEps;
     for (int depth = 0; depth < opt->max_depth; ++depth) {
         ohit h;
-        if (!closest(r, o, d, kEps, INFINITY, 1, &h)) {
+        if (!closest(r, o, d, tmin, INFINITY, 1, &h)) {
             L = add(L, mul(W, environment(r, d)));
             if (sc->has_sun && r->sun_disk && dot(d, r->sun_dir) >= r->sun_cos_max) {
                 float w = prev_delta ? 1.0f : prev_pdf / (prev_pdf + r->sun_pdf);
@@ -853,7 +876,7 @@ static v3 phys_radiance(const rscene* r, v3 o, v3 d, const oracle_render_opts* o
                 float cos_l = dot(r->ln, neg(wi));
                 float cos_s = dot(nsf, wi), cos_g = dot(ngf, wi);
                 if (cos_l > 0.0f && cos_s > 0.0f && cos_g > 0.0f &&
-                    !occluded(r, p, wi, kEps, dist * (1.0f - 1e-4f))) {
+                    !occluded(r, spawn(p, ng, wi), wi, 0.0f, dist * (1.0f - 1e-4f))) {
                     float pdf_b;
                     v3 f = phys_eval(m, nsf, wo, wi, &pdf_b);
                     float pdf_l = dist2 / (cos_l * r->larea);
@@ -871,7 +894,7 @@ static v3 phys_radiance(const rscene* r, v3 o, v3 d, const oracle_render_opts* o
                     wi = safe_unit(add(add(scl(r->sun_t, st * cosf(ph)), scl(r->sun_b, st * sinf(ph))), scl(wi, ct)));
                 }
                 float cos_s = dot(nsf, wi), cos_g = dot(ngf, wi);
-                if (cos_s > 0.0f && cos_g > 0.0f && !occluded(r, p, wi, kEps, INFINITY)) {
+                if (cos_s > 0.0f && cos_g > 0.0f && !occluded(r, spawn(p, ng, wi), wi, 0.0f, INFINITY)) {
                     float pdf_b;
                     v3 f = phys_eval(m, nsf, wo, wi, &pdf_b);
                     if (r->sun_disk) {
@@ -957,11 +980,16 @@ static v3 phys_radiance(const rscene* r, v3 o, v3 d, const oracle_render_opts* o
         prev_delta = is_delta; prev_pdf = pdf;
         if (W.x <= 0.0f && W.y <= 0.0f && W.z <= 0.0f) break;
         if (depth >= opt->rr_depth) {
-            float q = fminf(0.95f, maxc(W));
-            if (opcg_f32(rnd) >= q) break;
-            W = scl(W, 1.0f / q);
+            /* survival min(1, max W): a path whose throughput has not dropped below 1 (a
+               chain of lossless mirror or glass bounces) is never cut, so its weight never
+               grows beyond what the BSDFs gave it */
+            float q = fminf(1.0f, maxc(W));
+            if (q < 1.0f) {
+                if (opcg_f32(rnd) >= q) break;
+                W = scl(W, 1.0f / q);
+            }
         }
-        o = p; d = wi;
+        o = spawn(p, ng, wi); d = wi; tmin = 0.0f;
     }
     return L;
 }

@@ -118,8 +118,7 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_unet_train_step", "salty_scene_set_camera", "salty_denoise_unet", "salty_render_batch",
            "salty_get_tuning", "salty_set_tuning", "salty_autotune", "salty_mesh_load_smd", "salty_mesh_free",
            "salty_mesh_transform", "salty_autotune_trace", "salty_denoise_unet_ensemble", "salty_film_checkpoint",
-           "salty_film_restore", "salty_unet_get_adam", "salty_unet_set_adam", "salty_unet_set_conv_kernel",
-           "salty_fp32_peak"]
+           "salty_film_restore", "salty_unet_get_adam", "salty_unet_set_adam", "salty_unet_set_conv_kernel"]
 
 _lib = None
 
@@ -170,7 +169,6 @@ def lib() -> C.CDLL:
         "salty_unet_get_adam": (i32, [vp, vp, vp, vp, C.POINTER(i64)]),
         "salty_unet_set_adam": (i32, [vp, vp, vp, vp, i64]),
         "salty_unet_set_conv_kernel": (i32, [vp, vp, i32]),
-        "salty_fp32_peak": (i32, [vp, C.POINTER(C.c_double)]),
         "salty_render_batch": (i32, [vp, vp, vp, i32, C.POINTER(RenderStats)]),
         "salty_mesh_load_smd": (i32, [vp, C.c_char_p, C.POINTER(C.POINTER(Mesh))]),
         "salty_mesh_free": (None, [C.POINTER(Mesh)]),
@@ -442,12 +440,6 @@ class Context:
         out = np.empty_like(rgba)
         self.check(lib().salty_denoise_nlm_ref(self.h, w, h, coeff, _ptr(rgba), _ptr(out)), "nlm_ref")
         return out
-
-    def fp32_peak(self) -> float:
-        """salty_fp32_peak: measured FP32 FMA throughput of this GPU, TFLOP/s."""
-        t = C.c_double()
-        self.check(lib().salty_fp32_peak(self.h, C.byref(t)), "fp32_peak")
-        return t.value
 
     def nlm(self, rgb, var, search_r: int = 10, patch_r: int = 3, k: float = 0.45, out=None):
         """Variance-scaled NLM of an (H, W, 3) image; numpy arrays or device tensors."""

@@ -333,10 +333,14 @@ salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* d, salty
         put(k.sun_dir, sd);
         k.sun_disk = d->sun_half_angle > 0.0f;
         k.sun_cos_max = std::cos((double)d->sun_half_angle);
-        // solid angle of the cone, in double (1 - cos is tiny for small disks)
-        const double omega = 2.0 * 3.14159265358979323846 * (1.0 - std::cos((double)d->sun_half_angle));
+        // solid angle of the cone (the pdf of a uniform direction in it), in double since
+        // 1 - cos is tiny for small disks; the disk's radiance L makes the irradiance on a
+        // surface facing the sun, L pi sin^2(half angle), equal to sun_radiance
+        const double ca = std::cos((double)d->sun_half_angle);
+        const double omega = 2.0 * 3.14159265358979323846 * (1.0 - ca);
+        const double facing = 3.14159265358979323846 * (1.0 - ca) * (1.0 + ca);
         k.sun_pdf = k.sun_disk ? (float)(1.0 / omega) : 0.0f;
-        for (int i = 0; i < 3; ++i) k.sun_L[i] = k.sun_disk ? (float)(d->sun_radiance[i] / omega) : 0.0f;
+        for (int i = 0; i < 3; ++i) k.sun_L[i] = k.sun_disk ? (float)(d->sun_radiance[i] / facing) : 0.0f;
         // Duff et al. 2017 frame around the sun direction
         float s = sd.z >= 0.0f ? 1.0f : -1.0f, a = -1.0f / (s + sd.z), b = sd.x * sd.y * a;
         V3 t{1.0f + s * sd.x * sd.x * a, s * b, -s * sd.x}, bb{b, s + sd.y * sd.y * a, -sd.y};
@@ -813,12 +817,6 @@ salty_status salty_denoise_nlm_ref(salty_ctx* ctx, int32_t w, int32_t h, float c
     if (hout) SALTY_TRY_CUDA(E, cudaMemcpyAsync(out, dout, npx * 16, cudaMemcpyDeviceToHost, ctx->stream));
     SALTY_TRY_CUDA(E, cudaStreamSynchronize(ctx->stream));
     return SALTY_OK;
-}
-
-salty_status salty_fp32_peak(salty_ctx* ctx, double* tflops) {
-    if (!ctx || !tflops) return SALTY_ERR_INVALID_ARG;
-    cudaSetDevice(ctx->device);
-    return fp32_peak(ctx, tflops);
 }
 
 salty_status salty_denoise_nlm(salty_ctx* ctx, int32_t w, int32_t h, int32_t search_r, int32_t patch_r, float k,

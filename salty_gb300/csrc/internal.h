@@ -285,7 +285,6 @@ salty_status tonemap_device(salty_ctx* ctx, int type, int w, int h, const float*
                             float* d_out, uint8_t* d_srgb, int ref_oetf, float* ave, float* mx);
 salty_status nlm_ref_device(salty_ctx* ctx, int w, int h, float coeff, const float* d_in,
                             float* d_out);
-salty_status fp32_peak(salty_ctx* ctx, double* tflops);
 salty_status nlm_var_device(salty_ctx* ctx, int w, int h, int search_r, int patch_r, float k,
                             const float* d_rgb, const float* d_var, float* d_out);
 

@@ -330,43 +330,6 @@ salty_status nlm_ref_device(salty_ctx* ctx, int w, int h, float coeff, const flo
     return SALTY_OK;
 }
 
-// FP32 throughput probe: kFmaChains independent fused multiply-add chains per thread, so
-// every scheduler always has a ready FMA; nothing but the final sum leaves the registers.
-constexpr int kFmaChains = 8;
-__global__ void __launch_bounds__(256) k_fp32_peak(float* __restrict__ sink, int iters, float b, float c) {
-    float a[kFmaChains];
-#pragma unroll
-    for (int k = 0; k < kFmaChains; ++k) a[k] = (float)(threadIdx.x + k);
-    for (int i = 0; i < iters; ++i)
-#pragma unroll
-        for (int k = 0; k < kFmaChains; ++k) a[k] = fmaf(a[k], b, c);
-    float s = 0.0f;
-#pragma unroll
-    for (int k = 0; k < kFmaChains; ++k) s += a[k];
-    if (s == 1234.5f) sink[0] = s;  // keeps the chains live; never true for these inputs
-}
-
-salty_status fp32_peak(salty_ctx* ctx, double* tflops) {
-    auto& E = ctx->err;
-    const int blocks = ctx->num_sms * 8, threads = 256, iters = 1 << 14;
-    float* sink = reinterpret_cast<float*>(ctx->counters.p + 48);
-    cudaEvent_t e0 = ctx->ev[0], e1 = ctx->ev[1];
-    float best = 1e30f;
-    for (int r = 0; r < 4; ++r) {  // the first launch warms up
-        SALTY_TRY_CUDA(E, cudaEventRecord(e0, ctx->stream));
-        k_fp32_peak<<<blocks, threads, 0, ctx->stream>>>(sink, iters, 0.999999f, 1e-7f);
-        SALTY_TRY_CUDA(E, cudaEventRecord(e1, ctx->stream));
-        SALTY_TRY_CUDA(E, cudaEventSynchronize(e1));
-        float ms = 0;
-        SALTY_TRY_CUDA(E, cudaEventElapsedTime(&ms, e0, e1));
-        if (r > 0 && ms < best) best = ms;
-    }
-    SALTY_TRY_CUDA(E, cudaGetLastError());
-    const double flops = 2.0 * kFmaChains * (double)iters * blocks * threads;
-    *tflops = flops / (best * 1e-3) / 1e12;
-    return SALTY_OK;
-}
-
 salty_status nlm_var_device(salty_ctx* ctx, int w, int h, int search_r, int patch_r, float k, const float* d_rgb,
                             const float* d_var, float* d_out) {
     const int H = search_r + patch_r, S = kVTile + 2 * H, Eb = kVTile + 2 * patch_r;
@@ -557,13 +520,16 @@ cudaError_t noalloc_scratch(int device, NoAllocScratch** out) {
     return cudaSuccess;
 }
 
-bool on_device(const void* p) {
+// true for device memory of `device` itself, or managed memory; an array on another GPU
+// would be read as peer memory (a fault without peer access), so it is refused
+bool on_device(const void* p, int device) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == device;
 }
 
 }  // namespace
@@ -583,8 +549,10 @@ extern "C" salty_status salty_tonemap_noalloc(salty_ctx* ctx, void* stream, int3
     if (type < SALTY_TM_REINHARD || type > SALTY_TM_ACES) return E.fail(SALTY_ERR_INVALID_ARG, "bad tonemap type");
     if (!d_out_rgb && !d_out_srgb8) return E.fail(SALTY_ERR_INVALID_ARG, "tonemap_noalloc: no output");
     SALTY_TRY_CUDA(E, cudaSetDevice(ctx->device));
-    if (!on_device(d_rgb) || (d_out_rgb && !on_device(d_out_rgb)) || (d_out_srgb8 && !on_device(d_out_srgb8)))
-        return E.fail(SALTY_ERR_INVALID_ARG, "tonemap_noalloc: arrays must be device memory");
+    const int dv = ctx->device;
+    if (!on_device(d_rgb, dv) || (d_out_rgb && !on_device(d_out_rgb, dv)) ||
+        (d_out_srgb8 && !on_device(d_out_srgb8, dv)))
+        return E.fail(SALTY_ERR_INVALID_ARG, "tonemap_noalloc: arrays must be device memory of the context's GPU");
     NoAllocScratch* sc = nullptr;
     SALTY_TRY_CUDA(E, noalloc_scratch(ctx->device, &sc));
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;

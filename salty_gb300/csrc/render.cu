@@ -23,7 +23,9 @@
 //     cosine-weighted Lambert, exact-Fresnel dielectric, GGX, balance-heuristic MIS
 //     between BSDF sampling and the one-sided area light, a directional sun (delta, or a
 //     disk sampled by NEE and hit by BSDF rays, combined by MIS), constant sky, Russian
-//     roulette from rr_depth, watertight triangle test, ray epsilon 1e-4.
+//     roulette from rr_depth (survival min(1, max W), rolled only below 1), watertight
+//     triangle test; camera rays start at t = 1e-4, rays leaving a surface at t = 0 from an
+//     origin pushed off it (spawn).
 // The first bounce of every sample also records the denoiser's features (albedo, shading
 // normal, 1/(1 + distance)), averaged in the film next to the radiance.
 // Random numbers: one PCG stream (include/s3d_math.h:2769-2817 step) per (pixel, sample).
@@ -98,6 +100,21 @@ __device__ __forceinline__ void tangent_space(V n, V& t, V& b) {
     b = mk(bb, s + n.y * n.y * a, -n.y);
 }
 __device__ __forceinline__ V ld3(const float* p) { return mk(p[0], p[1], p[2]); }
+
+// Origin of a ray leaving the surface point p in direction w: p pushed off the surface along
+// the geometric normal ng (either orientation) to the side w points to, by 256 units in the
+// last place of each coordinate, or by 2^-16 near the world origin where ulps are tiny
+// (Waechter and Binder, "A Fast and Robust Method for Avoiding Self-Intersection", Ray
+// Tracing Gems, 2019).  Rays spawned this way start at t = 0.
+__device__ __forceinline__ float nudge(float p, float n) {
+    const int o = (int)(256.0f * n);
+    const float q = __int_as_float(__float_as_int(p) + (p < 0.0f ? -o : o));
+    return fabsf(p) < 1.0f / 32.0f ? p + n * (1.0f / 65536.0f) : q;
+}
+__device__ __forceinline__ V spawn(V p, V ng, V w) {
+    const V n = (ng.x * w.x + ng.y * w.y + ng.z * w.z) >= 0.0f ? ng : mk(-ng.x, -ng.y, -ng.z);
+    return mk(nudge(p.x, n.x), nudge(p.y, n.y), nudge(p.z, n.z));
+}
 __device__ __forceinline__ V xyz(float4 v) { return mk(v.x, v.y, v.z); }
 
 // ---------------------------------------------------------------- state
@@ -475,7 +492,8 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
                             float mis = pdf_l / (pdf_l + pdf_b);
                             cl = f * ld3(K.le) * (cos_s * mis / pdf_l);
                             want_l = true;
-                            ray_l0 = make_float4(s.p.x, s.p.y, s.p.z, kEps);
+                            const V so = spawn(s.p, s.ng, wi);
+                            ray_l0 = make_float4(so.x, so.y, so.z, 0.0f);
                             ray_l1 = make_float4(wi.x, wi.y, wi.z, dist * (1.0f - 1e-4f));
                         }
                     }
@@ -501,7 +519,8 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
                                 cs = f * ld3(K.sun_rad) * cos_s;
                             }
                             want_s = true;
-                            ray_s0 = make_float4(s.p.x, s.p.y, s.p.z, kEps);
+                            const V so = spawn(s.p, s.ng, wi);
+                            ray_s0 = make_float4(so.x, so.y, so.z, 0.0f);
                             ray_s1 = make_float4(wi.x, wi.y, wi.z, INFINITY);
                         }
                     }
@@ -784,14 +803,19 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                     W = W * wgt;
                     bool stop = (W.x <= 0.0f && W.y <= 0.0f && W.z <= 0.0f);
                     if (!stop && depth >= S.rr_depth) {
-                        float qv = fminf(0.95f, maxc(W));
-                        if (rng.f32() >= qv) stop = true;
-                        else W = W * (1.0f / qv);
+                        // survival min(1, max W): lossless chains of mirror or glass bounces
+                        // (W still 1) are never cut, so their weights never grow
+                        const float qv = fminf(1.0f, maxc(W));
+                        if (qv < 1.0f) {
+                            if (rng.f32() >= qv) stop = true;
+                            else W = W * (1.0f / qv);
+                        }
                     }
                     if (depth + 1 >= S.max_depth) stop = true;
                     if (!stop) {
                         cont = true;
-                        nr0 = make_float4(s.p.x, s.p.y, s.p.z, kEps);
+                        const V so = spawn(s.p, s.ng, wi);
+                        nr0 = make_float4(so.x, so.y, so.z, 0.0f);
                         nr1 = make_float4(wi.x, wi.y, wi.z, INFINITY);
                         nW = make_float4(W.x, W.y, W.z, pdf);
                         mt.w = pack_w(depth + 1, is_delta, slot);

@@ -51,7 +51,9 @@ def cornell(variant: str = "baseline") -> dict:
     red "left" wall is the x = 1 plane.
 
     variant "baseline": all Lambert.  "mixed": tall box mirror, short box glass (IOR 1.5),
-    back wall GGX (roughness 0.3) -- exercises every BSDF.  "glossy": tall box Phong
+    back wall GGX (roughness 0.3) -- exercises every BSDF.  "specular": the same mirror and
+    glass boxes with Lambert walls (the materials the reference itself has), the glass box
+    2 mm above the floor.  "glossy": tall box Phong
     (specular 0.8, power 40), short box Plastic (diffuse (0.2, 0.4, 0.7), specular 0.6,
     power 120), back wall Phong (power 8).  "thinlens": the baseline box seen through a thin
     lens of radius 0.06 focused on the tall box (target z = 0.6, focal distance 2.0).
@@ -65,6 +67,10 @@ def cornell(variant: str = "baseline") -> dict:
                  {"type": GLASS, "color": (1.0, 1.0, 1.0), "ior": 1.5},
                  {"type": GGX, "color": (0.8, 0.6, 0.3), "roughness": 0.3}]
         tall_m, short_m, back_m = 3, 4, 5
+    elif variant == "specular":
+        mats += [{"type": MIRROR, "color": (0.9, 0.9, 0.9)},
+                 {"type": GLASS, "color": (1.0, 1.0, 1.0), "ior": 1.5}]
+        tall_m, short_m = 3, 4
     elif variant == "textured":
         mats += [{"type": LAMBERT, "color": (0.9, 0.9, 0.9), "texture": 0}]
         back_m = 3
@@ -85,7 +91,10 @@ def cornell(variant: str = "baseline") -> dict:
     add(_quad((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0)), 1)      # x = 1 (image left), red
     add(_quad((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1)), 2)      # x = 0 (image right), green
     add(_box((0.3, 0.6, 0.3), 15.0, (0.33, 0.0, 0.6)), tall_m)
-    add(_box((0.3, 0.3, 0.3), -18.0, (0.66, 0.0, 0.35)), short_m)
+    # the specular variant lifts the glass box 2 mm off the floor: rays inside it would
+    # otherwise meet its bottom face and the floor at the same distance, a tie that floating
+    # point rounding decides differently on every machine
+    add(_box((0.3, 0.3, 0.3), -18.0, (0.66, 0.002 if variant == "specular" else 0.0, 0.35)), short_m)
     pos = np.stack(tris).reshape(-1, 9).astype(np.float32)
     g = np.cross(pos[:, 3:6] - pos[:, 0:3], pos[:, 6:9] - pos[:, 0:3])
     g /= np.linalg.norm(g, axis=1, keepdims=True)

@@ -133,10 +133,26 @@ def textured_fixture(r) -> None:
     print(f"textured cornell reference render: {secs:.2f} s")
 
 
+def specular_fixture(r) -> None:
+    """The Cornell box with a mirror tall box and a glass short box through
+    PathTracer::Radiance: Mirror::Shade (src/s3d_mirror.cpp:59-71) and Glass::Shade with its
+    1/0.5 branch weights (src/s3d_glass.cpp:60-128)."""
+    sc = cornell_scene("specular")
+    W = H = 48
+    spp, depth = 16384, 8
+    total, sq, secs = r.render(sc, W, H, spp, depth, seed=6161)
+    mean = total / spp
+    var = (sq / spp - mean * mean) * spp / (spp - 1) / spp
+    np.savez_compressed(os.path.join(HERE, "cornell_specular_ref_48.npz"), mean=mean.astype(np.float32),
+                        var=np.maximum(var, 0).astype(np.float32), spp=spp, max_bounce=depth, width=W, height=H)
+    print(f"specular cornell reference render: {secs:.2f} s")
+
+
 def main() -> None:
     build(with_reference=True)
     o, r = Oracle(), Reference()
-    only = {"glossy": glossy_fixture, "thinlens": thinlens_fixture, "textured": textured_fixture}
+    only = {"glossy": glossy_fixture, "thinlens": thinlens_fixture, "textured": textured_fixture,
+            "specular": specular_fixture}
     if sys.argv[1:] and all(a in only for a in sys.argv[1:]):
         for a in sys.argv[1:]:
             only[a](r)
@@ -175,6 +191,7 @@ def main() -> None:
     glossy_fixture(r)
     thinlens_fixture(r)
     textured_fixture(r)
+    specular_fixture(r)
 
     # 4. tonemapping and the sRGB8 capture
     img = hdr_image(99, 48, 32)

@@ -106,12 +106,15 @@ def test_oracle_compat_render_matches_reference_fixture(oracle):
 
 @pytest.mark.parametrize("variant,fixture,seed", [("glossy", "cornell_glossy_ref_48.npz", 31),
                                                   ("thinlens", "cornell_thinlens_ref_48.npz", 32),
-                                                  ("textured", "cornell_textured_ref_48.npz", 33)])
+                                                  ("textured", "cornell_textured_ref_48.npz", 33),
+                                                  ("specular", "cornell_specular_ref_48.npz", 34)])
 def test_oracle_compat_variants_match_reference_fixtures(oracle, variant, fixture, seed):
     """Phong and Plastic (src/s3d_phong.cpp:65-88, src/s3d_plastic.cpp:71-142), the
-    ThinLensCamera (include/s3d_camera.h:150-267), and colour maps with an environment map
-    (src/s3d_texturedmaterial.cpp:63-87, src/s3d_texture.cpp:925-972), through the
-    reference's PathTracer::Radiance."""
+    ThinLensCamera (include/s3d_camera.h:150-267), colour maps with an environment map
+    (src/s3d_texturedmaterial.cpp:63-87, src/s3d_texture.cpp:925-972), and Mirror and Glass
+    (src/s3d_mirror.cpp:59-71, src/s3d_glass.cpp:60-128), through the reference's
+    PathTracer::Radiance, at the fixture's sample count (the caustics of the glass box are
+    heavy-tailed: at equal counts both sides miss their rare paths alike)."""
     from oracle.oracle import PROFILE_COMPAT, SceneData
     from salty_gb300 import scenes
     g = np.load(os.path.join(GOLDEN, fixture))

@@ -59,12 +59,3 @@ def test_variance_nlm_matches_oracle(ctx, oracle):
     ref = oracle.nlm_var(noisy, var, 10, 3, 0.45)
     np.testing.assert_allclose(out, ref, rtol=1e-4, atol=1e-5)
     assert np.mean((out - clean) ** 2) < 0.5 * np.mean((noisy - clean) ** 2)
-
-
-def test_fp32_peak_probe(ctx):
-    """salty_fp32_peak: the FMA microkernel's throughput lies between half and 1.2x the
-    nominal FP32 rate of this part (152 SMs x 128 lanes x 2 flops x 2.07 GHz = 80.5 TFLOP/s)
-    and repeats within 10 %."""
-    a, b = ctx.fp32_peak(), ctx.fp32_peak()
-    assert 40.0 < a < 97.0, a
-    assert abs(a / b - 1.0) < 0.1, (a, b)

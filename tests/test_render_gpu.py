@@ -53,10 +53,12 @@ def test_compat_cornell_matches_reference_fixture(ctx):
 
 @pytest.mark.parametrize("variant,fixture", [("glossy", "cornell_glossy_ref_48.npz"),
                                              ("thinlens", "cornell_thinlens_ref_48.npz"),
-                                             ("textured", "cornell_textured_ref_48.npz")])
+                                             ("textured", "cornell_textured_ref_48.npz"),
+                                             ("specular", "cornell_specular_ref_48.npz")])
 def test_compat_variants_match_reference_fixtures(ctx, variant, fixture):
-    """Phong and Plastic, and the thin-lens camera, in the reference's estimator vs the GPU
-    compat profile."""
+    """Phong and Plastic, the thin-lens camera, textures, and Mirror and Glass (the latter
+    with the reference's 1/0.5 branch weights, src/s3d_glass.cpp:112-126) in the
+    reference's estimator vs the GPU compat profile."""
     import salty_gb300
     from salty_gb300 import scenes
     g = np.load(os.path.join(GOLDEN, fixture))

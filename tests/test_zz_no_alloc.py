@@ -1,9 +1,9 @@
 """salty_tonemap_noalloc: the tonemap entry point for callers that cannot allocate.
 
-A render loop that tonemaps every frame for display, a CUDA-graph capture or an engine
-that owns all GPU memory cannot call cudaMalloc at that point; this entry point works
-only on device arrays the caller already owns and on a fixed scratch array inside the
-library.  Its output must match salty_tonemap's (same tolerance as the tonemap tests),
+A render loop that tonemaps every frame for display (where cudaMalloc would synchronise
+the device) or an engine that owns all GPU memory cannot call cudaMalloc at that point;
+this entry point works only on device arrays the caller already owns and on a fixed
+scratch array inside the library.  Its output must match salty_tonemap's (same tolerance as the tonemap tests),
 call after call.  This file is collected last, so a run that stops at the first failure
 has already run every other test; it also passes alone in a fresh process.
 """
