@@ -9,8 +9,14 @@ on a radius-2 sphere about (0.5,0.5,0.5) and aim at uniform points of the cube; 
   value  device-resident rays and hits (torch CUDA tensors), one salty_trace per step
   e2e    the same call with rays in pinned host memory and hits written back to it:
          host->device and device->host copies inside every step
+  any_hit  the same rays as occlusion queries (first hit ends the walk)
 Rays (512 MiB) and hits (256 MiB) are larger than L2, so no flush is needed between steps;
 the BVH (nodes + leaf triangles) stays resident, as in any traversal.
+
+The default run then measures the 1080p heightfield scene as configured (measure_c3:
+directional sun, depth 12): one 64-spp frame (render_c3) and the time to relRMSE 0.01 of
+plain rendering and of the chosen path (autotuned launch shapes + U-Net), against FP64
+references of four windows at 2^20 spp (time_to_rmse); --no-c3 skips it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -51,7 +57,7 @@ N_RAYS = 16_777_216
 SOUP_SEED, RAY_SEED = 20260001, 20260002
 TMIN = 1e-4
 METRIC = "Mrays/s"
-CPU_SAMPLE = 4_194_304      # rays of the same stream timed on the host cores (~10 s of CPU work)
+CPU_SAMPLE = 2_097_152      # rays of the same stream timed on the host cores (~10 s of CPU work)
 # DRAM bytes (read + write) per ray of the closest-hit k_trace launch, from one ncu capture
 # of that kernel at the launch shape salty_autotune_trace picks here (256 threads, 64
 # registers, pool 64, postpone 7) on the same soup at 4,194,304 rays; the traffic (rays in,
@@ -157,27 +163,27 @@ def max_over_ranks(pg, x: float, device) -> float:
     return float(t.item())
 
 
-def cpu_port_rays_per_s(tris: np.ndarray, rays: np.ndarray) -> tuple[float, int, float]:
-    """The oracle restatement of the reference traversal (the reference's triangle test,
-    no t-culling) on all host cores.  Returns (rays/s, threads, seconds)."""
+def cpu_reference_rays_per_s(tris: np.ndarray, rays: np.ndarray) -> tuple[float, int, float, float]:
+    """The reference's own traversal on all host cores: BVH8::Create and BVH8::IsHit
+    (src/s3d_bvh8.cpp:191-206,401-479) with Triangle::IsHit, as restated in the oracle (same
+    tree, walk order and answers as the compiled reference; it cannot travel, being built
+    from the reference's sources).  Returns (rays/s, threads, trace seconds, build seconds)."""
     from oracle.oracle import Oracle, build
     build(with_reference=False)
     o = Oracle()
     threads = os.cpu_count() or 1
-    import ctypes as C
-    h = o.L.oracle_bvh_create(np.ascontiguousarray(tris), tris.shape[0])
+    b = o.ref_bvh(tris)
     try:
-        n = rays.shape[0]
-        ids = np.empty(n, np.int32)
-        t = np.empty(n, np.float32)
-        u = np.empty(n, np.float32)
-        v = np.empty(n, np.float32)
-        t0 = time.perf_counter()
-        o.L.oracle_trace(h, np.ascontiguousarray(rays), n, 0, 0, threads, ids, t, u, v)
-        dt = time.perf_counter() - t0
+        _, _, _, _, secs = b.trace(rays, nthreads=threads)
     finally:
-        o.L.oracle_bvh_destroy(h)
-    return n / dt, threads, dt
+        b.close()
+    return rays.shape[0] / secs, threads, secs, b.build_seconds
+
+
+REFERENCE_NOTE = ("the reference's BVH8::Create + BVH8::IsHit + Triangle::IsHit (16-bucket SAH, 8-wide "
+                  "boxes without clipping to the best hit, child order 0..7), restated in C (oracle/) "
+                  "with the compiled reference's tree, walk order and hit ids; its speed equals the "
+                  "compiled reference's within 10 % on an x86 host (0.0137 vs 0.0128 Mrays/s per thread)")
 
 
 def run_reference(args, ws, rank, local, pg):
@@ -186,24 +192,21 @@ def run_reference(args, ws, rank, local, pg):
         return
     import salty_gb300
     tris = salty_gb300.microbench_soup(SOUP_SEED, N_TRIS)
-    sample = 524_288  # ~1 s per step on 16 host threads: the default run stays within a minute
+    sample = 262_144  # ~1.3 s per step on 16 host threads: the default run stays within a minute
     rays = salty_gb300.microbench_rays(RAY_SEED, sample, TMIN)
     from oracle.oracle import Oracle, build
     build(with_reference=False)
     o = Oracle()
     threads = os.cpu_count() or 1
-    h = o.L.oracle_bvh_create(tris, N_TRIS)
-    ids = np.empty(sample, np.int32)
-    t = np.empty(sample, np.float32)
-    u = np.empty(sample, np.float32)
-    v = np.empty(sample, np.float32)
+    b = o.ref_bvh(tris)
     for _ in range(args.warmup):
-        o.L.oracle_trace(h, rays, sample, 0, 0, threads, ids, t, u, v)
+        b.trace(rays, nthreads=threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        o.L.oracle_trace(h, rays, sample, 0, 0, threads, ids, t, u, v)
+        b.trace(rays, nthreads=threads)
     dt = time.perf_counter() - t0
-    o.L.oracle_bvh_destroy(h)
+    build_s = b.build_seconds
+    b.close()
     value = sample * args.steps / dt / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
@@ -211,19 +214,27 @@ def run_reference(args, ws, rank, local, pg):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded PCG soup and rays)",
         "config": {"workload": "traversal microbenchmark: 1M-triangle soup, closest hit", "n_tris": N_TRIS,
-                   "rays_per_step": sample, "full_rays": N_RAYS},
+                   "rays_per_step": sample, "full_rays": N_RAYS, "bvh_build_seconds": build_s},
         "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
-                         "sample": f"first {sample} rays of the 16,777,216-ray stream per step, 1M triangles"},
+                         "sample": f"first {sample} rays of the 16,777,216-ray stream per step, 1M triangles",
+                         "implementation": REFERENCE_NOTE},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def run_time_to_rmse(args):
-    """The 1080p heightfield scene (13.6M triangles, sky + sun disk, depth 12): seconds until
-    the image of each method reaches relRMSE <= target on a 256x256 window against an FP64
-    render of that window at --ref-spp samples (its own noise subtracted).  Methods: plain
-    progressive rendering, the U-Net on the film (salty_denoise_unet), NLM."""
+C3_WINDOWS = ((448, 560, 128, 128), (1344, 560, 128, 128), (704, 860, 128, 128), (1088, 860, 128, 128))
+
+
+def measure_c3(args) -> dict:
+    """The 1080p heightfield scene as configured (2048^2 terrain + 4096 icospheres, 13.6M
+    triangles, sky 1.0 + a directional sun, max depth 12, physical profile):
+      render_c3     one 64-spp frame with the default launch shapes (Mrays/s, Mpaths/s)
+      time_to_rmse  seconds until each method's image reaches relRMSE <= target on four
+                    128x128 windows of the frame against FP64 renders of them at
+                    --ref-spp samples (their own noise subtracted): plain progressive
+                    rendering with the default launch shapes, and the chosen path (launch
+                    shapes from salty_autotune, untimed; the film denoised by the U-Net)."""
     import torch
     import salty_gb300
     from salty_gb300 import build as b
@@ -232,23 +243,21 @@ def run_time_to_rmse(args):
     from salty_gb300 import scenes
     b.build()
     W, H, D = 1920, 1080, 12
-    crop = (832, 412, 256, 256)
     ctx = salty_gb300.Context(0)
     t0 = time.perf_counter()
-    sc = scenes.heightfield()
+    sc = scenes.heightfield(sun_half_angle=args.sun_half_angle)
     s = scenes.upload(ctx, sc)
     info = s.build()
     setup_s = time.perf_counter() - t0
-    ref = cv.reference_image(s, W, H, crop, D, spp=args.ref_spp)
+    ref = cv.reference_image(s, W, H, list(C3_WINDOWS), D, spp=args.ref_spp)
     den = dn.Denoiser(ctx)
-    for _ in range(args.warmup):
+    for _ in range(3):
         s.render(W, H, 4, D, seed=3, want=())
-    # the C3 render configuration on its own: 1080p, 64 spp, depth 12
     torch.cuda.synchronize()
     r = s.render(W, H, 64, D, seed=5, want=())
     render = {"spp": 64, "ms": r["ms"], "Mrays_s": r["rays"] / r["ms"] / 1e3, "Mpaths_s": r["paths"] / r["ms"] / 1e3,
               "rays_per_path": r["rays"] / max(r["paths"], 1)}
-    # the plain path renders with the default launch shapes; the denoised paths with the
+    # the plain path renders with the default launch shapes; the denoised path with the
     # shapes salty_autotune picks for this frame (trial renders at 64 spp -- 132.7M samples,
     # enough to tell wave sizes up to 2^27 apart -- untimed, reported as autotune_seconds)
     default = ctx.tuning
@@ -260,34 +269,45 @@ def run_time_to_rmse(args):
     with ClockSampler(0) as clk:
         for m in args.methods.split(","):
             ctx.tuning = default if m == "plain" else tuned
-            res[m] = cv.converge(s, W, H, crop, ref, D, args.target, method=m, ctx=ctx, denoiser=den,
+            res[m] = cv.converge(s, W, H, ref, D, args.target, method=m, ctx=ctx, denoiser=den,
                                  max_spp=args.max_spp)
     ctx.tuning = default
-    clocks = clk.summary()
     plain = res.get("plain", {}).get("seconds_to_target")
     best = res.get("unet", {}).get("seconds_to_target")
-    line = {
-        "metric": f"seconds to relRMSE <= {args.target} (1080p heightfield, 256x256 window vs FP64 {args.ref_spp}-spp)",
-        "value": best, "unit": "s", "n_gpus": 1, "higher_is_better": False, "dtype": "f32",
-        "data": "synthetic (seeded heightfield scene generated on the host)",
-        "config": {"workload": "1920x1080 heightfield: 2048^2 terrain + 4096 icospheres (13.6M triangles), sky 1.0 + "
-                               "sun disk, max depth 12, physical profile",
-                   "n_tris": int(sc["tri_pos"].shape[0]), "bvh_nodes": info["n_nodes"], "bvh_build_ms": info["build_ms"],
-                   "window": crop, "ref_spp": args.ref_spp, "ref_noise_rel_mse": ref["noise"],
-                   "ref_seconds": ref["seconds"], "setup_seconds": setup_s,
-                   "denoiser": {"method": den.method, "hq_from_spp": den.hq_from_spp, "mirrors": den.mirrors,
-                                "weights": {k: v for k, v in den.meta.items() if k != "scenes"},
-                                "hq_weights": {k: v for k, v in den.hq_meta.items() if k != "scenes"}},
-                   "tuning_plain": default, "tuning_denoised": tuned, "autotune_seconds": tune_s,
-                   "autotune_trial_ms": trial_ms},
-        "plain_seconds": plain, "speedup_vs_plain": (plain / best) if plain and best else None,
+    out = {
+        "workload": "1920x1080 heightfield: 2048^2 terrain + 4096 icospheres (13.6M triangles), sky 1.0 + "
+                    + ("a directional sun" if args.sun_half_angle == 0 else
+                       f"a sun disk of {math.degrees(args.sun_half_angle):.1f} deg") + ", max depth 12, physical profile",
+        "n_tris": int(sc["tri_pos"].shape[0]), "bvh_nodes": info["n_nodes"], "bvh_build_ms": info["build_ms"],
+        "target_rel_rmse": args.target, "windows": [list(c) for c in C3_WINDOWS], "ref_spp": args.ref_spp,
+        "ref_noise_rel_mse": ref["noise"], "ref_noise_of_target": ref["noise"] / args.target ** 2,
+        "ref_seconds": ref["seconds"], "setup_seconds": setup_s,
+        "plain_seconds": plain, "chosen_seconds": best,
+        "speedup_vs_plain": (plain / best) if plain and best else None,
+        "denoiser": {"method": den.method, "hq_from_spp": den.hq_from_spp, "mirrors": den.mirrors,
+                     "weights": {k: v for k, v in den.meta.items() if k != "scenes"},
+                     "hq_weights": {k: v for k, v in den.hq_meta.items() if k != "scenes"}},
+        "tuning_plain": default, "tuning_chosen": tuned, "autotune_seconds": tune_s, "autotune_trial_ms": trial_ms,
         "methods": {m: {"seconds_to_target": v["seconds_to_target"], "curve": v["curve"]} for m, v in res.items()},
-        "render_c3": render, "clocks": clocks,
+        "render_c3": render, "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
     den.close()
     s.close()
     ctx.close()
+    return out
+
+
+def run_time_to_rmse(args):
+    """measure_c3 as its own JSON line (value: the chosen path's seconds to the target)."""
+    r = measure_c3(args)
+    line = {
+        "metric": f"seconds to relRMSE <= {args.target} (1080p heightfield, four 128x128 windows vs FP64 "
+                  f"{args.ref_spp}-spp)",
+        "value": r["chosen_seconds"], "unit": "s", "n_gpus": 1, "higher_is_better": False, "dtype": "f32",
+        "data": "synthetic (seeded heightfield scene generated on the host)",
+        "config": {"workload": r["workload"]}, "time_to_rmse": r, "clocks": r["clocks"],
+    }
+    print(json.dumps(line), flush=True)
 
 
 def run_batch(args):
@@ -375,9 +395,9 @@ UNET_FWD_GFLOP_1080P = 305.0  # sum over the 14 convolutions of 2*9*cin*cout*pix
 def run_denoise(args):
     """The learned denoiser against NLM (the C5 comparison): the held-out 1080p heightfield
     rendered at 4 spp; the film denoised whole by the U-Net (averaged over the 8 grid
-    symmetries) and by NLM (21x21 search, 7x7 patch, variance-scaled); relMSE on the
-    256x256 window at (832, 412) against an FP64 65,536-spp render of it, the reference's
-    own noise subtracted.  value: the U-Net's relMSE (lower is better); timings are the
+    symmetries) and by NLM (21x21 search, 7x7 patch, variance-scaled); relMSE on the four
+    128x128 windows of the time-to-RMSE measurement against FP64 65,536-spp renders of them,
+    the reference's own noise subtracted.  value: the U-Net's relMSE (lower is better); timings are the
     synchronous calls on device-resident films (best of 3)."""
     import torch
     import salty_gb300
@@ -387,11 +407,10 @@ def run_denoise(args):
     from salty_gb300 import scenes
     b.build()
     W, H, D, SPP = 1920, 1080, 12, 4
-    crop = (832, 412, 256, 256)
     ctx = salty_gb300.Context(0)
     s = scenes.upload(ctx, scenes.heightfield())
     s.build()
-    ref = cv.reference_image(s, W, H, crop, D, spp=65536)
+    ref = cv.reference_image(s, W, H, list(C3_WINDOWS), D, spp=65536)
     s.render(W, H, SPP, D, seed=4242, want=())
     film = s.read(W, H)
     den = dn.Denoiser(ctx)
@@ -417,18 +436,19 @@ def run_denoise(args):
         _, nlm_ms = best_of(lambda: ctx.nlm(mean_d, var_d, 10, 3, 0.45, out=nlm_d))
         nlm = nlm_d.cpu().numpy()
     clocks = clk.summary()
-    e = {"noisy": cv.corrected_rel_mse(cv.crop_of(film["mean"], crop), ref),
-         "nlm": cv.corrected_rel_mse(cv.crop_of(nlm, crop), ref),
-         "unet": cv.corrected_rel_mse(cv.crop_of(unet, crop), ref)}
+    e = {"noisy": cv.corrected_rel_mse(film["mean"], ref),
+         "nlm": cv.corrected_rel_mse(nlm, ref),
+         "unet": cv.corrected_rel_mse(unet, ref)}
     peaks = measured_peaks_tensor()
     mirrors = den.mirrors
     achieved = mirrors * UNET_FWD_GFLOP_1080P / unet_ms  # GFLOP/ms = TFLOP/s
     line = {
-        "metric": "relMSE of the denoised 4-spp film (256x256 window vs FP64 65,536 spp, reference noise subtracted)",
+        "metric": "relMSE of the denoised 4-spp film (four 128x128 windows vs FP64 65,536 spp, reference noise "
+                  "subtracted)",
         "value": e["unet"], "unit": "relMSE", "n_gpus": 1, "higher_is_better": False, "dtype": "bf16",
         "data": "synthetic (the held-out heightfield scene generated on the host; weights trained on seeds 1-16)",
         "config": {"workload": "1920x1080 heightfield (seed 2026, held out), 4 spp, depth 12; U-Net over "
-                               f"{mirrors} grid symmetries vs NLM 21x21/7x7", "window": crop,
+                               f"{mirrors} grid symmetries vs NLM 21x21/7x7", "windows": [list(c) for c in C3_WINDOWS],
                    "ref_spp": 65536, "ref_noise_rel_mse": ref["noise"]},
         "rel_mse": e, "unet_vs_nlm": e["nlm"] / e["unet"],
         "unet_ms_per_frame": unet_ms, "nlm_ms_per_frame": nlm_ms,
@@ -731,9 +751,13 @@ def main():
                     choices=["traversal", "time-to-rmse", "batch", "cornell", "denoise", *PROFILING])
     ap.add_argument("--scenes", type=int, default=256, help="batch: number of scenes")
     ap.add_argument("--target", type=float, default=0.01, help="time-to-rmse: relRMSE target")
-    ap.add_argument("--ref-spp", type=int, default=65536, help="time-to-rmse: samples of the FP64 reference")
+    ap.add_argument("--ref-spp", type=int, default=1 << 20, help="time-to-rmse: samples of the FP64 reference")
+    ap.add_argument("--sun-half-angle", type=float, default=0.0,
+                    help="time-to-rmse: the sun's angular radius in radians (0: directional, as configured)")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 1080p heightfield measurement of the "
+                                                        "default run")
     ap.add_argument("--max-spp", type=int, default=1 << 17, help="time-to-rmse: give up beyond this")
-    ap.add_argument("--methods", default="plain,unet", help="time-to-rmse: plain,unet,nlm")
+    ap.add_argument("--methods", default="plain,unet", help="time-to-rmse: plain,unet (U-Net: the chosen path),nlm")
     ap.add_argument("--spp", type=int, default=None, help="render: 1, wave-sweep: 64")
     ap.add_argument("--frames", type=int, default=2, help="render: frames")
     ap.add_argument("--width", type=int, default=1920, help="render, nlm: image width")
@@ -844,6 +868,27 @@ def main():
     # id -1, whose float bit pattern is a NaN, so compare the raw words)
     same = bool(np.array_equal(d_hits.cpu().numpy().view(np.int32), hits_h.view(np.int32)))
 
+    # ---- any-hit (occlusion) queries of the same rays, device-resident, same launch shape
+    anyhit = None
+    if not any_hit:
+        for _ in range(args.warmup):
+            scene.trace_raw(d_rays, d_hits, any_hit=True)
+        barrier(pg)
+        torch.cuda.synchronize()
+        a_kernel = 0.0
+        e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e4.record()
+        for _ in range(args.steps):
+            a_kernel += scene.trace_raw(d_rays, d_hits, any_hit=True)["kernel_ms"]
+        e5.record()
+        torch.cuda.synchronize()
+        barrier(pg)
+        a_ms = max_over_ranks(pg, e4.elapsed_time(e5), dev)
+        occluded = int((d_hits[:, 1].view(torch.int32) >= 0).sum().item())
+        anyhit = {"value": ws * n_rays * args.steps / (a_ms / 1e3) / 1e6, "unit": "Mrays/s",
+                  "ms_per_step": a_ms / args.steps, "kernel_ms": a_kernel / args.steps,
+                  "occluded_fraction": occluded / n_rays}
+
     peaks = measured_peaks()
     achieved = bytes_per_ray * n_rays / (launch_ms / 1e3) / 1e9
     line = {
@@ -869,17 +914,25 @@ def main():
                      "bytes_per_ray": bytes_per_ray, "node_fetches_per_ray": n_node, "tri_fetches_per_ray": n_tri},
         "clocks": clocks,
         "host_device_hits_equal": same,
+        "any_hit": anyhit,
     }
     if rank == 0 and ws == 1 and not args.no_cpu:
         sample = CPU_SAMPLE
-        cps, cores, secs = cpu_port_rays_per_s(tris, rays_h[:sample].copy())
+        cps, cores, secs, build_s = cpu_reference_rays_per_s(tris, rays_h[:sample].copy())
         line["cpu_baseline"] = {"value": cps / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
                                 "sample": f"first {sample} rays of the same stream, same 1M triangles "
-                                          f"({secs:.1f} s on {cores} threads)"}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+                                          f"({secs:.1f} s on {cores} threads; BVH build {build_s:.1f} s)",
+                                "implementation": REFERENCE_NOTE}
     scene.close()
     ctx.close()
+    del d_rays, d_hits
+    if rank == 0 and ws == 1 and not args.no_c3 and not any_hit:
+        c3 = measure_c3(args)
+        line["render_c3"] = c3["render_c3"]
+        line["time_to_rmse"] = {k: v for k, v in c3.items() if k != "render_c3"}
+        line["gpu_launches_note"] = "gpu_launches counts the traversal steps only (the C3 keys run after them)"
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
 

@@ -123,6 +123,38 @@ class SceneData:
     ibl_scale: float = 10.0
 
 
+class RefBVH:
+    """The reference's BVH8 over a triangle soup and its closest-hit walk (BVH8::IsHit,
+    src/s3d_bvh8.cpp:191-206), restated in C: trace(rays) -> ids, t, u, v, seconds."""
+
+    def __init__(self, o: "Oracle", tri_pos: np.ndarray):
+        self.o = o
+        self.pos = np.ascontiguousarray(tri_pos, np.float32).reshape(-1, 9)
+        secs = C.c_double()
+        self.h = o.L.oracle_refbvh_create(self.pos, self.pos.shape[0], C.byref(secs))
+        self.build_seconds = secs.value
+
+    def stats(self) -> dict:
+        n8, n4, nl, d = C.c_long(), C.c_long(), C.c_long(), C.c_int()
+        self.o.L.oracle_refbvh_stats(self.h, C.byref(n8), C.byref(n4), C.byref(nl), C.byref(d))
+        return {"bvh8": n8.value, "bvh4": n4.value, "leaves": nl.value, "depth": d.value}
+
+    def trace(self, rays: np.ndarray, nthreads: int = 0):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        ids = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        u = np.empty(n, np.float32)
+        v = np.empty(n, np.float32)
+        secs = self.o.L.oracle_refbvh_trace(self.h, rays, n, nthreads, ids, t, u, v)
+        return ids, t, u, v, secs
+
+    def close(self):
+        if self.h:
+            self.o.L.oracle_refbvh_destroy(self.h)
+            self.h = None
+
+
 class Oracle:
     """The C restatement."""
 
@@ -139,6 +171,13 @@ class Oracle:
         L.oracle_trace.argtypes = [C.c_void_p, _f32p, C.c_long, C.c_int, C.c_int, C.c_int,
                                    _i32p, _f32p, _f32p, _f32p]
         L.oracle_render.argtypes = [C.POINTER(_Scene), C.POINTER(_Opts), _f64p, _f64p]
+        L.oracle_refbvh_create.argtypes = [_f32p, C.c_long, C.POINTER(C.c_double)]
+        L.oracle_refbvh_create.restype = C.c_void_p
+        L.oracle_refbvh_destroy.argtypes = [C.c_void_p]
+        L.oracle_refbvh_stats.argtypes = [C.c_void_p, C.POINTER(C.c_long), C.POINTER(C.c_long),
+                                          C.POINTER(C.c_long), C.POINTER(C.c_int)]
+        L.oracle_refbvh_trace.argtypes = [C.c_void_p, _f32p, C.c_long, C.c_int, _i32p, _f32p, _f32p, _f32p]
+        L.oracle_refbvh_trace.restype = C.c_double
         L.oracle_tonemap.argtypes = [C.c_int, C.c_int, C.c_int, _f32p, _f32p,
                                      C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.oracle_srgb8.argtypes = [_f32p, C.c_long, C.c_int, _u8p]
@@ -170,6 +209,10 @@ class Oracle:
         finally:
             self.L.oracle_bvh_destroy(h)
         return ids, t, u, v
+
+    def ref_bvh(self, tri_pos: np.ndarray) -> "RefBVH":
+        """The reference's own BVH8 (BVH8::Create, src/s3d_bvh8.cpp:401-479), restated."""
+        return RefBVH(self, tri_pos)
 
     def render(self, sc: SceneData, width: int, height: int, spp: int, max_depth: int,
                rr_depth: int = 3, profile: int = PROFILE_PHYSICAL, seed: int = 1,

@@ -13,6 +13,7 @@
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #include <unistd.h>
 
 /* ------------------------------------------------------------------ PCG */
@@ -370,6 +371,366 @@ void oracle_trace(void* bvh, const float* rays8, long n, int mode, int any_hit, 
     for (int i = 1; i < nthreads; ++i) pthread_create(&th[i], NULL, trace_worker, &j);
     trace_worker(&j);
     for (int i = 1; i < nthreads; ++i) pthread_join(th[i], NULL);
+}
+
+/* ------------------------------------------------------- the reference's BVH8 */
+/* A restatement of the reference's own acceleration structure and walk, for the CPU
+ * baseline: the same tree as BVH8::Create builds (src/s3d_bvh8.cpp:254-342,401-479, with
+ * BVH4::Create src/s3d_bvh4.cpp:237-325,384-423 and Leaf src/s3d_leaf.cpp:22-35 where a
+ * split is refused), walked as BVH8::IsHit / BVH4::IsHit / Leaf::IsHit do
+ * (src/s3d_bvh8.cpp:191-206, src/s3d_bvh4.cpp:174-189, src/s3d_leaf.cpp:74-87): a
+ * depth-first walk in child order 0..7, every child whose box the line of the ray pierces
+ * (BoundingBox8::IsHit, include/s3d_math.h:2549-2586: slabs from -1e12 to 1e12, no clip to
+ * the best hit), and Triangle::IsHit (src/s3d_triangle.cpp:73-105) with its shared record
+ * (a later triangle must be strictly closer).  Floating-point operations follow the
+ * reference's order; min/max follow the SSE/AVX semantics (a < b ? a : b, a > b ? a : b). */
+#define RB_BUCKETS 16
+#define RB_FMAX FLT_MAX
+#define RB_HITMAX 1e12f
+#define RB_HITMIN 1e-3f
+
+typedef struct { float mn[3], mx[3], c[3]; int empty; } rbox;
+
+static rbox rbox_empty(void) {
+    rbox b;
+    for (int a = 0; a < 3; ++a) { b.mn[a] = RB_FMAX; b.mx[a] = -RB_FMAX; b.c[a] = 0.0f; }
+    b.empty = 1;
+    return b;
+}
+static rbox rbox_of(const float mn[3], const float mx[3]) {   /* BoundingBox(mini, maxi) */
+    rbox b;
+    for (int a = 0; a < 3; ++a) { b.mn[a] = mn[a]; b.mx[a] = mx[a]; b.c[a] = (mn[a] + mx[a]) * 0.5f; }
+    b.empty = 0;
+    return b;
+}
+static float rmin(float a, float b) { return a < b ? a : b; }
+static float rmax(float a, float b) { return a > b ? a : b; }
+static rbox rbox_merge(const rbox* a, const rbox* b) {       /* BoundingBox::Merge(box, box) */
+    if (!a->empty && !b->empty) {
+        float mn[3], mx[3];
+        for (int k = 0; k < 3; ++k) { mn[k] = rmin(a->mn[k], b->mn[k]); mx[k] = rmax(a->mx[k], b->mx[k]); }
+        return rbox_of(mn, mx);
+    }
+    if (a->empty && !b->empty) return *b;
+    return *a;
+}
+static rbox rbox_merge_pt(const rbox* a, const float p[3]) { /* BoundingBox::Merge(box, point) */
+    if (!a->empty) {
+        float mn[3], mx[3];
+        for (int k = 0; k < 3; ++k) { mn[k] = rmin(a->mn[k], p[k]); mx[k] = rmax(a->mx[k], p[k]); }
+        return rbox_of(mn, mx);
+    }
+    rbox b;
+    for (int k = 0; k < 3; ++k) b.mn[k] = b.mx[k] = b.c[k] = p[k];
+    b.empty = 0;
+    return b;
+}
+static float rbox_area(const rbox* b) {                      /* SurfaceArea, include/s3d_math.h:2904-2910 */
+    float X = fabsf(b->mx[0] - b->mn[0]), Y = fabsf(b->mx[1] - b->mn[1]), Z = fabsf(b->mx[2] - b->mn[2]);
+    return 2.0f * ((X * Y) + (X * Z) + (Y * Z));
+}
+
+typedef struct { float v0[3], e1[3], e2[3]; rbox box; } rtri;
+/* kind 8 / 4: inner node with that many children and their boxes (SoA); kind 0: a leaf
+ * of `count` triangles at tri_index[first ..] */
+typedef struct { int kind, first, count; int child[8]; float lo[3][8], hi[3][8]; } rnode;
+typedef struct {
+    rtri* tris; long n;
+    int* idx;                 /* the work array BVH8::Create partitions */
+    rnode* nodes; long n_nodes, cap;
+    rbox* node_box;           /* GetBox() of every node */
+    long n8, n4, n_leaf; int depth;
+} rbvh;
+
+static long rb_new_node(rbvh* b) {
+    if (b->n_nodes == b->cap) {
+        b->cap = b->cap ? b->cap * 2 : 1024;
+        b->nodes = (rnode*)realloc(b->nodes, sizeof(rnode) * (size_t)b->cap);
+        b->node_box = (rbox*)realloc(b->node_box, sizeof(rbox) * (size_t)b->cap);
+    }
+    return b->n_nodes++;
+}
+
+/* CalcOffset(box, p).a[axis] (src/s3d_bvh8.cpp:75-89) */
+static float rb_offset(const rbox* cb, const float p[3], int axis) {
+    float o = p[axis] - cb->mn[axis];
+    if (cb->mx[axis] > cb->mn[axis]) o /= cb->mx[axis] - cb->mn[axis];
+    return o;
+}
+
+/* SplitSAH (src/s3d_bvh8.cpp:254-342; BVH4's differs only in its leaf threshold) */
+static int rb_split(rbvh* b, int* sh, long count, int min_leaf, long* mid) {
+    if (count <= min_leaf) return 0;
+    rbox bound = b->tris[sh[0]].box, cen = rbox_empty();
+    for (long i = 1; i < count; ++i) bound = rbox_merge(&bound, &b->tris[sh[i]].box);
+    cen = rbox_merge_pt(&cen, b->tris[sh[0]].box.c);
+    for (long i = 1; i < count; ++i) cen = rbox_merge_pt(&cen, b->tris[sh[i]].box.c);
+    float ext[3] = {cen.mx[0] - cen.mn[0], cen.mx[1] - cen.mn[1], cen.mx[2] - cen.mn[2]};
+    int axis = (ext[0] > ext[1] && ext[0] > ext[2]) ? 0 : (ext[1] > ext[2] ? 1 : 2);
+    if (cen.mx[axis] == cen.mn[axis]) return 0;
+    unsigned cnt[RB_BUCKETS];
+    rbox bb[RB_BUCKETS];
+    for (int k = 0; k < RB_BUCKETS; ++k) { cnt[k] = 0; bb[k] = rbox_empty(); }
+    for (long i = 0; i < count; ++i) {
+        int k = (int)((float)RB_BUCKETS * rb_offset(&cen, b->tris[sh[i]].box.c, axis));
+        if (k == RB_BUCKETS) k = RB_BUCKETS - 1;
+        cnt[k]++;
+        bb[k] = rbox_merge(&bb[k], &b->tris[sh[i]].box);
+    }
+    float cost[RB_BUCKETS - 1];
+    const float area = rbox_area(&bound);
+    for (int i = 0; i < RB_BUCKETS - 1; ++i) {
+        rbox b0 = rbox_empty(), b1 = rbox_empty();
+        int c0 = 0, c1 = 0;
+        for (int j = 0; j <= i; ++j) { b0 = rbox_merge(&b0, &bb[j]); c0 += (int)cnt[j]; }
+        for (int j = i + 1; j < RB_BUCKETS; ++j) { b1 = rbox_merge(&b1, &bb[j]); c1 += (int)cnt[j]; }
+        cost[i] = 1.0f + ((float)c0 * rbox_area(&b0) + (float)c1 * rbox_area(&b1)) / area;
+    }
+    float best = cost[0];
+    int split = 0;
+    for (int i = 1; i < RB_BUCKETS - 1; ++i)
+        if (cost[i] < best) { best = cost[i]; split = i; }
+    if (!(best < (float)count)) return 0;
+    /* std::partition (bidirectional form) with the reference's predicate: the bucket
+     * position is compared as a float, `16 * offset <= split` */
+    int* first = sh;
+    int* last = sh + count;
+    for (;;) {
+        for (;;) {
+            if (first == last) goto done;
+            float k = (float)RB_BUCKETS * rb_offset(&cen, b->tris[*first].box.c, axis);
+            if (k == (float)RB_BUCKETS) k = (float)(RB_BUCKETS - 1);
+            if (k <= (float)split) ++first; else break;
+        }
+        --last;
+        for (;;) {
+            if (first == last) goto done;
+            float k = (float)RB_BUCKETS * rb_offset(&cen, b->tris[*last].box.c, axis);
+            if (k == (float)RB_BUCKETS) k = (float)(RB_BUCKETS - 1);
+            if (!(k <= (float)split)) --last; else break;
+        }
+        int tmp = *first; *first = *last; *last = tmp;
+        ++first;
+    }
+done:
+    *mid = first - sh;
+    return 1;
+}
+
+/* Leaf::Create (src/s3d_leaf.cpp:22-35): its box merges the triangles' boxes */
+static long rb_leaf(rbvh* b, int* sh, long count, int depth) {
+    long id = rb_new_node(b);
+    rnode* nd = &b->nodes[id];
+    nd->kind = 0;
+    nd->first = (int)(sh - b->idx);
+    nd->count = (int)count;
+    rbox bx = b->tris[sh[0]].box;
+    for (long i = 1; i < count; ++i) bx = rbox_merge(&bx, &b->tris[sh[i]].box);
+    b->node_box[id] = bx;
+    b->n_leaf++;
+    if (depth > b->depth) b->depth = depth;
+    return id;
+}
+
+/* BVH8 / BVH4 node from its children: BoundingBox8/4 of their GetBox(), and its own
+ * GetBox() (the lanes merged) */
+static long rb_inner(rbvh* b, int kind, const long* ch) {
+    long id = rb_new_node(b);
+    rnode* nd = &b->nodes[id];
+    nd->kind = kind;
+    float mn[3] = {RB_FMAX, RB_FMAX, RB_FMAX}, mx[3] = {-RB_FMAX, -RB_FMAX, -RB_FMAX};
+    for (int i = 0; i < kind; ++i) {
+        const rbox* cb = &b->node_box[ch[i]];
+        nd->child[i] = (int)ch[i];
+        for (int a = 0; a < 3; ++a) {
+            nd->lo[a][i] = cb->mn[a];
+            nd->hi[a][i] = cb->mx[a];
+            mn[a] = rmin(mn[a], cb->mn[a]);
+            mx[a] = rmax(mx[a], cb->mx[a]);
+        }
+    }
+    b->node_box[id] = rbox_of(mn, mx);
+    if (kind == 8) b->n8++; else b->n4++;
+    return id;
+}
+
+/* BVH4::Create (src/s3d_bvh4.cpp:384-423); its CreateNode is always a Leaf (:94-104) */
+static long rb_create4(rbvh* b, int* sh, long count, int depth) {
+    if (count <= 4) return rb_leaf(b, sh, count, depth);
+    long mid = 0, midL = 0, midR = 0;
+    if (!rb_split(b, sh, count, 4, &mid)) return rb_leaf(b, sh, count, depth);
+    if (!rb_split(b, sh, mid, 4, &midL)) return rb_leaf(b, sh, count, depth);
+    if (!rb_split(b, sh + mid, count - mid, 4, &midR)) return rb_leaf(b, sh, count, depth);
+    long i1 = midL, i2 = mid, i3 = mid + midR;
+    long ch[4];
+    ch[0] = rb_create4(b, sh, i1, depth + 1);
+    ch[1] = rb_create4(b, sh + i1, i2 - i1, depth + 1);
+    ch[2] = rb_create4(b, sh + i2, i3 - i2, depth + 1);
+    ch[3] = rb_create4(b, sh + i3, count - i3, depth + 1);
+    return rb_inner(b, 4, ch);
+}
+
+/* CreateNode of the BVH8 file (src/s3d_bvh8.cpp:94-110): a Leaf up to 8, else BVH4 */
+static long rb_node8(rbvh* b, int* sh, long count, int depth) {
+    return count <= 8 ? rb_leaf(b, sh, count, depth) : rb_create4(b, sh, count, depth);
+}
+
+/* BVH8::Create (src/s3d_bvh8.cpp:401-479): three levels of binary splits, 8 children */
+static long rb_create8(rbvh* b, int* sh, long count, int depth) {
+    if (count <= 8) return rb_node8(b, sh, count, depth);
+    long mid = 0, midL = 0, midR = 0, m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+    if (!rb_split(b, sh, count, 8, &mid)) return rb_node8(b, sh, count, depth);
+    if (!rb_split(b, sh, mid, 8, &midL)) return rb_node8(b, sh, count, depth);
+    if (!rb_split(b, sh + mid, count - mid, 8, &midR)) return rb_node8(b, sh, count, depth);
+    long iB = midL, iC = mid, iD = mid + midR;
+    if (!rb_split(b, sh, iB, 8, &m0)) return rb_node8(b, sh, count, depth);
+    if (!rb_split(b, sh + iB, iC - iB, 8, &m1)) return rb_node8(b, sh, count, depth);
+    if (!rb_split(b, sh + iC, iD - iC, 8, &m2)) return rb_node8(b, sh, count, depth);
+    if (!rb_split(b, sh + iD, count - iD, 8, &m3)) return rb_node8(b, sh, count, depth);
+    long idx[9] = {0, m0, midL, midL + m1, mid, mid + m2, mid + midR, mid + midR + m3, count};
+    long ch[8];
+    for (int i = 0; i < 8; ++i) ch[i] = rb_create8(b, sh + idx[i], idx[i + 1] - idx[i], depth + 1);
+    return rb_inner(b, 8, ch);
+}
+
+void* oracle_refbvh_create(const float* pos9, long n, double* build_seconds) {
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    rbvh* b = (rbvh*)calloc(1, sizeof(rbvh));
+    b->n = n;
+    b->tris = (rtri*)malloc(sizeof(rtri) * (size_t)(n ? n : 1));
+    b->idx = (int*)malloc(sizeof(int) * (size_t)(n ? n : 1));
+    for (long i = 0; i < n; ++i) {   /* Triangle::Triangle (src/s3d_triangle.cpp:22-40) */
+        const float* p = pos9 + i * 9;
+        rtri* t = &b->tris[i];
+        float mn[3], mx[3];
+        for (int a = 0; a < 3; ++a) {
+            t->v0[a] = p[a];
+            mn[a] = rmin(rmin(p[a], p[3 + a]), p[6 + a]);
+            mx[a] = rmax(rmax(p[a], p[3 + a]), p[6 + a]);
+            t->e1[a] = p[3 + a] - p[a];
+            t->e2[a] = p[6 + a] - p[a];
+        }
+        t->box = rbox_of(mn, mx);
+        b->idx[i] = (int)i;
+    }
+    if (n > 0) rb_create8(b, b->idx, n, 1);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    if (build_seconds) *build_seconds = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+    return b;
+}
+
+void oracle_refbvh_destroy(void* h) {
+    rbvh* b = (rbvh*)h;
+    if (!b) return;
+    free(b->tris); free(b->idx); free(b->nodes); free(b->node_box); free(b);
+}
+
+void oracle_refbvh_stats(void* h, long* n8, long* n4, long* n_leaf, int* depth) {
+    const rbvh* b = (const rbvh*)h;
+    *n8 = b->n8; *n4 = b->n4; *n_leaf = b->n_leaf; *depth = b->depth;
+}
+
+typedef struct { float t, u, v; int id; } rrec;
+
+/* Triangle::IsHit against the shared record (src/s3d_triangle.cpp:73-105) */
+static void rb_tri(const rtri* T, int id, const float o[3], const float d[3], rrec* rec) {
+    v3 D = ld3(d), e1 = ld3(T->e1), e2 = ld3(T->e2);
+    v3 s1 = cross(D, e2);
+    float div = dot(s1, e1);
+    if (fabsf(div) <= FLT_EPSILON) return;
+    v3 dv = sub(ld3(o), ld3(T->v0));
+    float beta = dot(dv, s1) / div;
+    if (beta <= 0.0f || beta >= 1.0f) return;
+    v3 s2 = cross(dv, e1);
+    float gamma = dot(D, s2) / div;
+    if (gamma <= 0.0f || (beta + gamma) >= 1.0f) return;
+    float dist = dot(e2, s2) / div;
+    if (dist < RB_HITMIN || dist > RB_HITMAX) return;
+    if (dist >= rec->t) return;
+    rec->t = dist; rec->u = beta; rec->v = gamma; rec->id = id;
+}
+
+/* BoundingBox8/4::IsHit (include/s3d_math.h:2549-2586, 2364-2401): one bit per child */
+static unsigned rb_box_mask(const rnode* nd, const float o[3], const float d[3]) {
+    unsigned m = 0;
+    for (int i = 0; i < nd->kind; ++i) {
+        float tmin = -RB_HITMAX, tmax = RB_HITMAX;
+        for (int a = 0; a < 3; ++a) {
+            float t0 = (nd->lo[a][i] - o[a]) / d[a];
+            float t1 = (nd->hi[a][i] - o[a]) / d[a];
+            float n = t0 < t1 ? t0 : t1, f = t0 > t1 ? t0 : t1;
+            tmin = tmin > n ? tmin : n;
+            tmax = tmax < f ? tmax : f;
+        }
+        if (tmax >= tmin) m |= 1u << i;
+    }
+    return m;
+}
+
+static void rb_trace_one(const rbvh* b, const float o[3], const float d[3], rrec* rec) {
+    rec->t = RB_FMAX; rec->u = rec->v = 0.0f; rec->id = -1;
+    if (b->n_nodes == 0) return;
+    int stack[1024];
+    int sp = 0;
+    stack[sp++] = (int)(b->n_nodes - 1);   /* the root is built last */
+    while (sp) {
+        const rnode* nd = &b->nodes[stack[--sp]];
+        if (nd->kind == 0) {
+            for (int i = 0; i < nd->count; ++i) {
+                int id = b->idx[nd->first + i];
+                rb_tri(&b->tris[id], id, o, d, rec);
+            }
+            continue;
+        }
+        unsigned m = rb_box_mask(nd, o, d);
+        for (int i = nd->kind - 1; i >= 0; --i)   /* child 0 is walked first */
+            if (m & (1u << i)) stack[sp++] = nd->child[i];
+    }
+}
+
+typedef struct {
+    const rbvh* b; const float* rays; long n; int32_t* ids; float *t, *u, *v;
+    long next; pthread_mutex_t mu;
+} rtrace_job;
+
+static void* rtrace_worker(void* arg) {
+    rtrace_job* j = (rtrace_job*)arg;
+    for (;;) {
+        pthread_mutex_lock(&j->mu);
+        long s = j->next; j->next += 256;
+        pthread_mutex_unlock(&j->mu);
+        if (s >= j->n) break;
+        long e = s + 256 < j->n ? s + 256 : j->n;
+        for (long i = s; i < e; ++i) {
+            const float* r = j->rays + i * 8;
+            rrec rec;
+            rb_trace_one(j->b, r, r + 4, &rec);
+            j->ids[i] = rec.id;
+            if (j->t) j->t[i] = rec.t;
+            if (j->u) j->u[i] = rec.u;
+            if (j->v) j->v[i] = rec.v;
+        }
+    }
+    return NULL;
+}
+
+/* Closest hits of n rays (n x 8: o, tmin, d, tmax; tmin/tmax ignored: the reference's
+ * limits F_HIT_MIN = 1e-3 and F_HIT_MAX = 1e12 apply) on `nthreads` host threads (0: all);
+ * misses: id -1, t = FLT_MAX (the record's initial distance).  Returns the seconds taken. */
+double oracle_refbvh_trace(void* h, const float* rays8, long n, int nthreads, int32_t* ids, float* t, float* u,
+                           float* v) {
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    rtrace_job j = {(const rbvh*)h, rays8, n, ids, t, u, v, 0, PTHREAD_MUTEX_INITIALIZER};
+    nthreads = resolve_threads(nthreads);
+    pthread_t th[256];
+    if (nthreads > 256) nthreads = 256;
+    for (int i = 1; i < nthreads; ++i) pthread_create(&th[i], NULL, rtrace_worker, &j);
+    rtrace_worker(&j);
+    for (int i = 1; i < nthreads; ++i) pthread_join(th[i], NULL);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
 }
 
 /* ------------------------------------------------------- rendering */

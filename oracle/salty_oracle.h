@@ -46,6 +46,15 @@ void  oracle_bvh_destroy(void* bvh);
 void  oracle_trace(void* bvh, const float* rays8, long n, int mode, int any_hit, int nthreads,
                    int32_t* ids, float* t, float* u, float* v);
 
+/* ---- the reference's own BVH8 (BVH8::Create / BVH8::IsHit, src/s3d_bvh8.cpp), restated
+ * for the CPU baseline: same tree, same walk order, same triangle test and ties (the
+ * first triangle walked keeps an equal t). ---- */
+void*  oracle_refbvh_create(const float* pos9, long n, double* build_seconds);
+void   oracle_refbvh_destroy(void* bvh);
+void   oracle_refbvh_stats(void* bvh, long* n8, long* n4, long* n_leaf, int* depth);
+double oracle_refbvh_trace(void* bvh, const float* rays8, long n, int nthreads, int32_t* ids, float* t, float* u,
+                           float* v);
+
 /* ---- rendering ---- */
 enum { ORACLE_LAMBERT = 0, ORACLE_MIRROR = 1, ORACLE_GLASS = 2, ORACLE_GGX = 3, ORACLE_PHONG = 4,
        ORACLE_PLASTIC = 5 };

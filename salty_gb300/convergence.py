@@ -2,16 +2,16 @@
 
 Error metric (relative MSE, used throughout the denoising literature):
     relMSE = mean over pixels and channels of (x - r)^2 / (r^2 + 0.01),  relRMSE = sqrt(relMSE)
-where r is the converged image: an FP64-accumulated render at 65,536 samples per pixel.
-At 1080p that reference would cost ~1.4e11 camera paths, so it is rendered for a window
-(crop) of the frame; the window's pixels keep their full-frame rays, so the methods render
-the whole frame and are scored on the window.
+where r is the converged image: an FP64-accumulated render at many samples per pixel
+(65,536 or more).  At 1080p that reference would cost ~1.4e11 camera paths or more, so it
+is rendered for a few windows (crops) of the frame; the windows' pixels keep their
+full-frame rays, so the methods render the whole frame and are scored on the windows.
 
 The reference is itself a Monte Carlo estimate: against it, an image's measured relMSE is
 its true relMSE plus the reference's own, E = mean(var_r / (r^2 + 0.01)) with var_r the
-variance of the reference's mean (independent samples).  At relRMSE 0.01 the two are of
-the same size, so every error reported here is the measured relMSE minus E (an unbiased
-estimate of the error against the exact image), and E is reported beside it.
+variance of the reference's mean (independent samples).  Every error reported here is the
+measured relMSE minus E (an unbiased estimate of the error against the exact image), and E
+is reported beside it; with 2^20 reference samples E is a few percent of the 1e-4 target.
 
 A method's time to reach a target relRMSE is measured with a doubling sample schedule:
 the frame is rendered progressively (each pass doubles the samples), after each pass the
@@ -40,26 +40,43 @@ def rel_rmse(x: np.ndarray, ref: np.ndarray) -> float:
     return math.sqrt(rel_mse(x, ref))
 
 
-def reference_image(scene, width: int, height: int, crop: tuple, max_depth: int, spp: int = 65536,
+def reference_image(scene, width: int, height: int, crops, max_depth: int, spp: int = 65536,
                     chunk: int = 4096, seed: int = 987654321, rr_depth: int = 3) -> dict:
-    """FP64-accumulated crop window at `spp` samples: {"mean", "var" (of the mean), "noise"
-    (the relMSE its own noise adds, E above), "spp", "seconds"}."""
+    """FP64-accumulated windows of the frame at `spp` samples each: {"mean", "var" (of the
+    mean), lists with one array per window, "noise" (the relMSE its own noise adds, E above,
+    over all windows' pixels), "spp", "seconds", "crops"}.  `crops` is one (x, y, w, h)
+    window or a list of them."""
+    crops = [tuple(crops)] if isinstance(crops[0], int) else [tuple(c) for c in crops]
     t0 = time.perf_counter()
-    done = 0
-    out = None
-    while done < spp:
-        k = min(chunk, spp - done)
-        out = scene.render(width, height, k, max_depth, rr_depth=rr_depth, profile=PROFILE_PHYSICAL, seed=seed,
-                           accumulate=done > 0, fp64=True, want=("mean", "var"), crop=crop)
-        done += k
-    m, v = out["mean"].astype(np.float64), out["var"].astype(np.float64)
-    return {"mean": out["mean"], "var": out["var"], "noise": float(np.mean(v / (m * m + 1e-2))), "spp": spp,
-            "seconds": time.perf_counter() - t0}
+    means, vars_ = [], []
+    for crop in crops:
+        done = 0
+        out = None
+        while done < spp:
+            k = min(chunk, spp - done)
+            out = scene.render(width, height, k, max_depth, rr_depth=rr_depth, profile=PROFILE_PHYSICAL, seed=seed,
+                               accumulate=done > 0, fp64=True, want=("mean", "var"), crop=crop)
+            done += k
+        means.append(out["mean"])
+        vars_.append(out["var"])
+    m = np.concatenate([a.reshape(-1, 3) for a in means]).astype(np.float64)
+    v = np.concatenate([a.reshape(-1, 3) for a in vars_]).astype(np.float64)
+    return {"mean": means, "var": vars_, "noise": float(np.mean(v / (m * m + 1e-2))), "spp": spp,
+            "seconds": time.perf_counter() - t0, "crops": crops}
 
 
-def corrected_rel_mse(x: np.ndarray, ref: dict) -> float:
-    """relMSE against the exact image, estimated as measured minus the reference's noise."""
-    return rel_mse(x, ref["mean"]) - ref["noise"]
+def corrected_rel_mse(x, ref: dict) -> float:
+    """relMSE against the exact image, estimated as measured minus the reference's noise.
+    x: a list of window images, one window image, or the full frame (its windows are then
+    cut out here)."""
+    means = ref["mean"] if isinstance(ref["mean"], (list, tuple)) else [ref["mean"]]
+    crops = ref.get("crops")
+    if not isinstance(x, (list, tuple)):
+        whole_window = len(means) == 1 and np.shape(x)[:2] == np.shape(means[0])[:2]
+        x = [crop_of(x, c) for c in crops] if crops and not whole_window else [x]
+    xs = np.concatenate([np.asarray(a, np.float64).reshape(-1, 3) for a in x])
+    rs = np.concatenate([np.asarray(a, np.float64).reshape(-1, 3) for a in means])
+    return rel_mse(xs, rs) - ref["noise"]
 
 
 def crop_of(img, crop: tuple):
@@ -67,11 +84,11 @@ def crop_of(img, crop: tuple):
     return img[y:y + h, x:x + w]
 
 
-def converge(scene, width: int, height: int, crop: tuple, ref: dict, max_depth: int, target: float,
+def converge(scene, width: int, height: int, ref: dict, max_depth: int, target: float,
              method: str = "plain", ctx=None, denoiser=None, spp0: int = 4, max_spp: int = 1 << 16, seed: int = 1,
              rr_depth: int = 3, nlm_k: float = 0.45) -> dict:
     """Progressive full-frame rendering with doubling spp until the method's image reaches
-    relRMSE <= target on the crop.  method: "plain" (the film mean), "nlm" (salty_denoise_nlm
+    relRMSE <= target on the reference's windows.  method: "plain" (the film mean), "nlm" (salty_denoise_nlm
     of mean and variance) or "unet" (salty_denoise_unet of the film through `denoiser`, a
     salty_gb300.denoiser.Denoiser, which picks its network by the film's samples)."""
     import torch
@@ -106,7 +123,7 @@ def converge(scene, width: int, height: int, crop: tuple, ref: dict, max_depth: 
         torch.cuda.synchronize()
         spent += time.perf_counter() - t0
         total += step
-        err = corrected_rel_mse(crop_of(out, crop).cpu().numpy(), ref)
+        err = corrected_rel_mse([crop_of(out, c).cpu().numpy() for c in ref["crops"]], ref)
         curve.append({"spp": total, "seconds": spent, "rel_mse": err})
         if err <= target_mse:
             break

@@ -185,14 +185,14 @@ def _icosphere(subdiv: int) -> np.ndarray:
 
 
 def heightfield(grid: int = 2048, n_spheres: int = 4096, seed: int = 2026, height: float = 0.15,
-                subdiv: int = 3, sun_half_angle: float = math.radians(4.0)) -> dict:
+                subdiv: int = 3, sun_half_angle: float = 0.0) -> dict:
     """The 1080p heightfield scene: a grid x grid terrain (2 grid^2 triangles) over [0,1]^2
     with 6-octave value-noise heights (amplitude 0.5^k), n_spheres icospheres (20 * 4^subdiv
     triangles each) with radii log-uniform in [0.005, 0.05] above it; sphere materials 60%
     Lambert (albedo U[0.1,0.9]), 20% mirror, 10% dielectric (IOR 1.5), 10% GGX (roughness
-    U[0.05,0.5]); constant sky 1.0 and a directional sun whose disk has a 4 degree angular
-    radius (sampled together with the BSDF by MIS; a delta sun makes the glints of the
-    low-roughness GGX spheres unbounded fireflies)."""
+    U[0.05,0.5]); constant sky 1.0 and a directional sun (a delta light, reached by
+    next-event estimation only), or, with sun_half_angle > 0, a sun disk of that angular
+    radius (sampled together with the BSDF by multiple importance sampling)."""
     rng = np.random.default_rng(seed)
     n = grid + 1
     h = value_noise(n, 6, seed) * height

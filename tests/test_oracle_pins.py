@@ -75,6 +75,39 @@ def test_oracle_trace_matches_live_reference(oracle, reference):
     assert np.array_equal(t[hit], rt[hit]) and np.array_equal(u[hit], ru[hit]) and np.array_equal(v[hit], rv[hit])
 
 
+def test_restated_reference_bvh_matches_reference_fixture_1m(oracle):
+    """The restatement of the reference's own BVH8 and walk (the CPU baseline) gives the
+    compiled reference's answers on its 1M-triangle fixture, bit for bit."""
+    g = np.load(os.path.join(GOLDEN, "trace_soup_1m.npz"))
+    tris = oracle.gen_soup(SOUP_SEED, 1_000_000)
+    rays = oracle.gen_rays(RAY_SEED, 65536)
+    b = oracle.ref_bvh(tris)
+    ids, t, _, _, _ = b.trace(rays)
+    st = b.stats()
+    b.close()
+    assert np.array_equal(ids, g["ids"]), f"{(ids != g['ids']).sum()} id mismatches"
+    hit = ids >= 0
+    assert np.array_equal(t[hit], g["t"][hit])
+    assert st["bvh8"] > 0 and st["leaves"] > 0
+
+
+def test_restated_reference_bvh_matches_live_reference(oracle, reference):
+    """Same tree, same walk: equal ids, t and barycentrics with the compiled reference on a
+    soup with duplicated triangles, where the first triangle walked keeps a tie."""
+    tris = oracle.gen_soup(51, 20000)
+    tris[5000:5100] = tris[100:200]          # exact duplicates: ties decided by walk order
+    rays = oracle.gen_rays(52, 8192)
+    s = reference.soup(tris)
+    rid, rt, ru, rv, _ = s.trace(rays)
+    s.close()
+    b = oracle.ref_bvh(tris)
+    ids, t, u, v, _ = b.trace(rays)
+    b.close()
+    assert np.array_equal(ids, rid)
+    hit = ids >= 0
+    assert np.array_equal(t[hit], rt[hit]) and np.array_equal(u[hit], ru[hit]) and np.array_equal(v[hit], rv[hit])
+
+
 def test_watertight_differs_only_at_edges(oracle):
     tris = oracle.gen_soup(41, 200000)
     rays = oracle.gen_rays(42, 20000)
