@@ -483,7 +483,8 @@ class Scene:
         except Exception:
             pass
 
-    def build(self, bins: int = 32, max_leaf: int = 3, trav_cost: float = 1.0) -> dict:
+    def build(self, bins: int = 32, max_leaf: int = 3, trav_cost: float = 0.0) -> dict:
+        """salty_bvh_build; trav_cost 0 = the library's default (0.3)."""
         o = BuildOpts(bins, max_leaf, trav_cost)
         info = BvhInfo()
         self.ctx.check(lib().salty_bvh_build(self.ctx.h, self.h, C.byref(o), C.byref(info)), "bvh_build")

@@ -5,18 +5,21 @@
 // recurses on the CPU.  Here:
 //   1. a binary tree is built breadth first, one level per pass over all primitives:
 //      32 bins on each of the three centroid axes, cost = ntrav*SA(node) +
-//      nL*SA(L) + nR*SA(R) against count*SA(node) for a leaf (the reference's cost with
-//      the same unit weights, src/s3d_bvh8.cpp:300-317), leaves of at most 3 triangles;
+//      nL*SA(L) + nR*SA(R) against count*SA(node) for a leaf (the reference's cost form,
+//      src/s3d_bvh8.cpp:300-317; ntrav is 0.3 by default instead of its 1, since small
+//      leaves trace fastest here), leaves of at most 3 triangles;
 //      ranges larger than kSmall are binned by all threads with block-aggregated atomics,
 //      smaller ones by one warp in shared memory;
-//   2. the binary tree is collapsed top-down: each 8-wide node repeatedly opens its
-//      largest-area inner child until it has 8 children;
+//   2. the binary tree is collapsed into 8-wide nodes: dynamic programming over the binary
+//      tree picks the SAH-cheapest choice of wide nodes, leaves (subtrees of up to three
+//      triangles) and opened nodes; the wide nodes are then written top down;
 //   3. child boxes are quantised to 8 bits per plane against a per-node power-of-two
 //      grid, rounding outward, so every quantised box contains the exact one.
 #include <cfloat>
 #include <cmath>
 
 #include <atomic>
+#include <vector>
 
 #include "internal.h"
 
@@ -24,6 +27,12 @@ namespace salty {
 namespace {
 
 constexpr int kBins = 32;
+// SAH weights of the collapse: one 8-wide node visit against one triangle test.  Measured
+// on the traversal microbenchmark and the 1080p heightfield (GB300): any triangle weight
+// from 1 to 2.6 node visits gives the same speed within noise, lighter ones put more
+// triangles in each leaf and lose 3-10 %.
+constexpr float kCollapseNodeCost = 1.0f;
+constexpr float kCollapseTriCost = 2.0f;
 constexpr int kSmall = 256;
 constexpr int kBinWords = 3 * kBins * 7;  // count + lo[3] + hi[3] per bin per axis
 
@@ -449,33 +458,116 @@ __device__ int quant_exponent(float lo, float hi) {
     return e;
 }
 
+// ---------------------------------------------------------------- SAH-optimal collapse
+// Which binary nodes become 8-wide nodes, which become leaves of the wide tree, and which
+// are opened into their parent's child slots is decided by dynamic programming over the
+// binary tree (Ylitie, Karras, Laine, "Efficient Incoherent Ray Traversal on GPUs Through
+// Compressed Wide BVHs", HPG 2017, section 3.1): for every binary node n and every
+// i = 1..7, C(n, i) is the least SAH cost of covering n's subtree with at most i roots, each
+// an 8-wide node or a leaf of at most kMaxLeafTris triangles:
+//   C(n, 1)  = min(leaf: A(n) p(n) c_tri  if p(n) <= kMaxLeafTris,
+//                  node: A(n) c_node + D(n, 8))
+//   C(n, i)  = min(C(n, i - 1), D(n, i))                           i = 2..7
+//   D(n, j)  = min over k = 1..j-1 of C(left, k) + C(right, j - k)
+// with A the surface area and p the triangle count.  Binary leaves can only be leaves.
+// The nodes of one binary level are solved together, deepest level first.
+struct CollapseDP {
+    float c[7];          // C(n, 1..7)
+    int first, count;    // the subtree's triangles: prim positions [first, first + count)
+    unsigned dec;        // bit 0: C(n, 1) is a leaf; bits 1..6: C(n, i) takes D(n, i), i = 2..7;
+                         // bits 8 + 3 (j - 2): the k of D(n, j), j = 2..8
+};
+
+__global__ void k_collapse_dp(const BNode* __restrict__ bn, CollapseDP* __restrict__ dp, int begin, int end,
+                              float c_node, float c_tri) {
+    const int i = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= end) return;
+    const BNode b = bn[i];
+    const float A = bnode_area(b);
+    CollapseDP r;
+    if (b.count > 0) {
+        r.first = b.a;
+        r.count = b.count;
+        const float leaf = A * (float)b.count * c_tri;
+        for (int k = 0; k < 7; ++k) r.c[k] = leaf;
+        r.dec = 1u;
+        dp[i] = r;
+        return;
+    }
+    const CollapseDP L = dp[b.a], R = dp[b.a + 1];
+    r.first = min(L.first, R.first);
+    r.count = L.count + R.count;
+    float D[9];
+    unsigned dec = 0;
+    for (int j = 2; j <= 8; ++j) {
+        float best = INFINITY;
+        int bk = 1;
+        for (int k = 1; k < j; ++k) {
+            const int kr = j - k;
+            if (k > 7 || kr > 7) continue;
+            const float v = L.c[k - 1] + R.c[kr - 1];
+            if (v < best) { best = v; bk = k; }
+        }
+        D[j] = best;
+        dec |= (unsigned)bk << (8 + 3 * (j - 2));
+    }
+    const float node = A * c_node + D[8];
+    const float leaf = r.count <= kMaxLeafTris ? A * (float)r.count * c_tri : INFINITY;
+    if (leaf <= node) { r.c[0] = leaf; dec |= 1u; }
+    else r.c[0] = node;
+    for (int k = 2; k <= 7; ++k) {
+        if (D[k] < r.c[k - 2]) { r.c[k - 1] = D[k]; dec |= 1u << (k - 1); }
+        else r.c[k - 1] = r.c[k - 2];
+    }
+    r.dec = dec;
+    dp[i] = r;
+}
+
+// The children of the 8-wide node made from binary node `bid`: D(bid, 8) unfolded.  Each
+// child is a binary node standing for itself (leaf[] tells whether as a leaf of the wide
+// tree or as an 8-wide node).  Returns the number of children (1..8).
+__device__ int collapse_children(const BNode* __restrict__ bn, const CollapseDP* __restrict__ dp, int bid,
+                                 int* set, bool* leaf) {
+    int k = 0;
+    if (bn[bid].count > 0) {  // a binary leaf at the root: one leaf child
+        set[0] = bid;
+        leaf[0] = true;
+        return 1;
+    }
+    int sn[16], sj[16], sp = 0;
+    sn[sp] = bid; sj[sp] = 8; ++sp;
+    bool top = true;
+    while (sp > 0) {
+        --sp;
+        const int m = sn[sp];
+        int j = sj[sp];
+        const BNode b = bn[m];
+        const unsigned dec = dp[m].dec;
+        if (!top) {
+            if (b.count > 0) { set[k] = m; leaf[k] = true; ++k; continue; }
+            while (j > 1 && j <= 7 && !((dec >> (j - 1)) & 1u)) --j;  // C(m, j) = C(m, j - 1)
+            if (j == 1) { set[k] = m; leaf[k] = (dec & 1u) != 0; ++k; continue; }
+        }
+        top = false;
+        const int kl = (dec >> (8 + 3 * (j - 2))) & 7u;
+        sn[sp] = b.a + 1; sj[sp] = j - kl; ++sp;  // right, visited after left
+        sn[sp] = b.a; sj[sp] = kl; ++sp;
+    }
+    return k;
+}
+
 __global__ void k_collapse(const BNode* __restrict__ bn, int nwork, const int2* __restrict__ work,
                            Bvh8Node* __restrict__ out, float4* __restrict__ tris,
                            const int* __restrict__ prim, const float* __restrict__ pos,
-                           int2* __restrict__ work_next, Counters* ctr, float root_sa) {
+                           int2* __restrict__ work_next, Counters* ctr, float root_sa,
+                           const CollapseDP* __restrict__ dp) {
     int wi = blockIdx.x * blockDim.x + threadIdx.x;
     if (wi >= nwork) return;
     int bid = work[wi].x, oid = work[wi].y;
     BNode b = bn[bid];
     int set[8];
-    int k = 0;
-    if (b.count > 0) set[k++] = bid;
-    else { set[0] = b.a; set[1] = b.a + 1; k = 2; }
-    while (k < 8) {
-        int best = -1;
-        float bsa = -1.0f;
-        for (int i = 0; i < k; ++i) {
-            BNode c = bn[set[i]];
-            if (c.count == 0) {
-                float sa = bnode_area(c);
-                if (sa > bsa) { bsa = sa; best = i; }
-            }
-        }
-        if (best < 0) break;
-        int ca = bn[set[best]].a;
-        set[best] = ca;
-        set[k++] = ca + 1;
-    }
+    bool as_leaf[8];
+    const int k = collapse_children(bn, dp, bid, set, as_leaf);
     // slot assignment by octant of the child centre around the node centre
     float cx = (b.lo[0] + b.hi[0]) * 0.5f, cy = (b.lo[1] + b.hi[1]) * 0.5f, cz = (b.lo[2] + b.hi[2]) * 0.5f;
     int slot_child[8];
@@ -504,8 +596,7 @@ __global__ void k_collapse(const BNode* __restrict__ bn, int nwork, const int2* 
     }
     int n_int = 0, n_tri = 0;
     for (int i = 0; i < k; ++i) {
-        BNode c = bn[set[i]];
-        if (c.count == 0) ++n_int; else n_tri += c.count;
+        if (!as_leaf[i]) ++n_int; else n_tri += dp[set[i]].count;
     }
     int child_base = n_int ? atomicAdd(&ctr->n8, n_int) : 0;
     int tri_base = n_tri ? atomicAdd(&ctr->ntris, n_tri) : 0;
@@ -531,6 +622,9 @@ __global__ void k_collapse(const BNode* __restrict__ bn, int nwork, const int2* 
             qlo[a][s] = (unsigned char)fmin(fmax(lo, 0.0), 255.0);
             qhi[a][s] = (unsigned char)fmin(fmax(hi, 0.0), 255.0);
         }
+        // a leaf child holds the triangles of its whole binary subtree
+        c.a = dp[set[i]].first;
+        c.count = as_leaf[i] ? dp[set[i]].count : 0;
         if (c.count == 0) {
             imask |= 1u << s;
             meta[s] = (unsigned char)((1u << 5) | (24u + s));  // one hit bit at 24 + slot
@@ -622,6 +716,8 @@ salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& 
     k_root_init<<<1, 1, 0, st>>>(ctr.p, tasks[0].p, bnodes.p, n, 0);
     int cur = 0;
     int ntasks = 1, nlarge = (n > kSmall) ? 1 : 0;
+    // binary node index ranges per level: level l holds nodes [lvl[l], lvl[l + 1])
+    std::vector<int> lvl{0, 1};
     for (int level = 0; ntasks > 0; ++level) {
         if (level > 4096) return E.fail(SALTY_ERR_CAPACITY, "binary build did not terminate");
         if (nlarge > 0) {
@@ -642,13 +738,22 @@ salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& 
         if (hc->error) return E.fail(SALTY_ERR_CUDA, "BVH partition disagreed with its bins at level %d", level);
         ntasks = hc->next_tasks;
         nlarge = hc->next_large;
+        if (hc->nodes > lvl.back()) lvl.push_back(hc->nodes);
         cur ^= 1;
     }
     SALTY_TRY_CUDA(E, cudaGetLastError());
     const int n_binary = hc->nodes;
     const int bdepth = hc->depth;
 
-    // collapse
+    // collapse: costs of every binary subtree, deepest level first, then the 8-wide nodes
+    // top down
+    DevBuf<CollapseDP> dp;
+    SALTY_TRY_CUDA(E, dp.ensure((size_t)n_binary));
+    for (int l = (int)lvl.size() - 2; l >= 0; --l) {
+        const int b0 = lvl[l], b1 = lvl[l + 1];
+        k_collapse_dp<<<grid_for(b1 - b0, 128), 128, 0, st>>>(bnodes.p, dp.p, b0, b1, kCollapseNodeCost,
+                                                               kCollapseTriCost);
+    }
     SALTY_TRY_CUDA(E, sc->bvh.nodes.ensure((size_t)n + 1));
     SALTY_TRY_CUDA(E, sc->bvh.tris.ensure((size_t)n * kTriFloat4));
     BNode root;
@@ -668,7 +773,7 @@ salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& 
         cudaMemsetAsync(&ctr.p->next_work, 0, sizeof(int), st);
         k_collapse<<<grid_for(nwork, 128), 128, 0, st>>>(bnodes.p, nwork, work[wcur].p, sc->bvh.nodes.p,
                                                          sc->bvh.tris.p, prim[cur].p, sc->pos.p,
-                                                         work[wcur ^ 1].p, ctr.p, root_sa);
+                                                         work[wcur ^ 1].p, ctr.p, root_sa, dp.p);
         SALTY_TRY_CUDA(E, cudaMemcpyAsync(hc, ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, st));
         SALTY_TRY_CUDA(E, cudaStreamSynchronize(st));
         nwork = hc->next_work;

@@ -403,7 +403,7 @@ salty_status salty_bvh_build(salty_ctx* ctx, salty_scene* scene, const salty_bui
                              salty_bvh_info* info) {
     if (!ctx) return SALTY_ERR_INVALID_ARG;
     if (!scene) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "null scene");
-    salty_build_opts o{32, 3, 1.0f};
+    salty_build_opts o{32, 3, 0.3f};
     if (opts) {
         if (opts->bins) o.bins = opts->bins;
         if (opts->max_leaf) o.max_leaf = opts->max_leaf;
