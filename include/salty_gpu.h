@@ -413,12 +413,13 @@ salty_status salty_denoise_unet(salty_ctx* ctx, salty_unet* net, salty_scene* sc
  * error at the cost of `mirrors` forward passes. */
 salty_status salty_denoise_unet_ensemble(salty_ctx* ctx, salty_unet* net, salty_scene* scene, int32_t mirrors,
                                         float* out_rgb);
-/* The kernel of the network's forward and backward-data convolutions: SALTY_CONV_TCGEN05
- * (default; fifth-generation tensor cores, accumulators in tensor memory, inputs staged by
- * the TMA copy engine where they sit in one tensor), SALTY_CONV_TCGEN05_CP_ASYNC (the same
- * MMAs with every input staged by cp.async) or SALTY_CONV_MMA_SYNC (warp-level mma.sync).
- * All give the same result up to the order of the FP32 sums.  The weight-gradient
- * convolution is mma.sync in all. */
+/* The kernel of the network's convolutions: SALTY_CONV_TCGEN05 (default; fifth-generation
+ * tensor cores, accumulators in tensor memory, inputs staged by the TMA copy engine where
+ * they sit in one tensor), SALTY_CONV_TCGEN05_CP_ASYNC (the same MMAs with every input
+ * staged by cp.async) or SALTY_CONV_MMA_SYNC (warp-level mma.sync).  All give the same
+ * result up to the order of the FP32 sums.  The weight gradients follow: with the tcgen05
+ * kinds they are tensor-core GEMMs summed in a fixed order (a training step is
+ * deterministic); with SALTY_CONV_MMA_SYNC, mma.sync tiles added by FP32 atomics. */
 enum { SALTY_CONV_TCGEN05 = 0, SALTY_CONV_MMA_SYNC = 1, SALTY_CONV_TCGEN05_CP_ASYNC = 2 };
 salty_status salty_unet_set_conv_kernel(salty_ctx* ctx, salty_unet* net, int32_t kind);
 

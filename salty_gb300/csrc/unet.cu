@@ -481,29 +481,40 @@ __global__ void k_relu_bwd(const bf16* __restrict__ y, int y_cs, const float* __
     }
 }
 
-// bias gradient: db[c] += sum_p g[p][c] for c < C (g has g_cs channels per pixel).  A
-// block of 256 threads takes 8-channel groups j = threadIdx.x % G of the pixels
-// threadIdx.x / G, (threadIdx.x / G) + 256 / G, ... of its pixel range (threads beyond a
-// multiple of G idle), sums in registers, then once into shared and global memory.
-__global__ void k_bias_grad(const bf16* __restrict__ g, int g_cs, int C, long long npx, float* __restrict__ db) {
-    extern __shared__ float sb[];
+// bias gradient, in a fixed summation order (no atomics): a block of 256 threads takes
+// 8-channel groups j = threadIdx.x % G of the pixels r = threadIdx.x / G, r + 256 / G, ...
+// of its pixel range (threads beyond a multiple of G idle) and sums them in registers; the
+// per-thread sums are added in shared memory in thread order into the block's partial
+// part[blockIdx.x][c], and k_bias_reduce adds the blocks' partials in block order.
+__global__ void k_bias_grad(const bf16* __restrict__ g, int g_cs, int C, long long npx, float* __restrict__ part) {
+    extern __shared__ float sb[];  // [256 / G][C]
     const int G = C / 8, lanes = (blockDim.x / G) * G, per = blockDim.x / G;
-    for (int c = threadIdx.x; c < C; c += blockDim.x) sb[c] = 0.0f;
-    __syncthreads();
     if ((int)threadIdx.x < lanes) {
-        const int j = threadIdx.x % G;
+        const int j = threadIdx.x % G, r = threadIdx.x / G;
         float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (long long p = (long long)blockIdx.x * per + threadIdx.x / G; p < npx; p += (long long)gridDim.x * per) {
+        for (long long p = (long long)blockIdx.x * per + r; p < npx; p += (long long)gridDim.x * per) {
             float v[8];
             unpack_bf16x8(__ldg(reinterpret_cast<const uint4*>(g + p * g_cs + j * 8)), v);
 #pragma unroll
             for (int k = 0; k < 8; ++k) s[k] += v[k];
         }
 #pragma unroll
-        for (int k = 0; k < 8; ++k) atomicAdd(&sb[j * 8 + k], s[k]);
+        for (int k = 0; k < 8; ++k) sb[r * C + j * 8 + k] = s[k];
     }
     __syncthreads();
-    for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&db[c], sb[c]);
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        float t = 0.0f;
+        for (int r = 0; r < per; ++r) t += sb[r * C + c];
+        part[(size_t)blockIdx.x * C + c] = t;
+    }
+}
+
+__global__ void k_bias_reduce(const float* __restrict__ part, int blocks, int C, float* __restrict__ db) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    float t = 0.0f;
+    for (int b = 0; b < blocks; ++b) t += part[(size_t)b * C + c];
+    db[c] += t;
 }
 
 // BF16 activation gradient (from a backward-data GEMM) -> FP32, optionally accumulated;
@@ -645,6 +656,8 @@ const int kLayers[][3] = {
     {80, 32, 1},                // dec0: up(d1) + e0 -> d0
     {32, 8, 0},                 // output
 };
+// pyramid level (resolution H >> level) each layer runs at
+const int kLayerLevel[] = {0, 0, 1, 1, 2, 2, 3, 3, 4, 3, 2, 1, 0, 0};
 constexpr int kNumLayers = 14;
 
 int pick_nt(int c) {
@@ -682,7 +695,9 @@ struct Unet {
     DevBuf<float> io;       // device copies of host features / targets / outputs
     DevBuf<float> film_ws;  // film planes, packed features and padded output of salty_denoise_unet
     DevBuf<double> loss;
-    int conv_kind = SALTY_CONV_TCGEN05;  // forward / backward-data convolution kernel
+    DevBuf<float> wg_ws;    // per-CTA partial weight and bias gradients (fixed-order sums)
+    DevBuf<bf16> cat_ws;    // a decoder convolution's concatenated input, for its weight gradient
+    int conv_kind = SALTY_CONV_TCGEN05;  // convolution kernels (forward, backward-data, weights)
 };
 
 namespace {
@@ -742,8 +757,11 @@ salty_status launch_conv(salty_ctx* ctx, int kind, const ConvSrc& in, int cin, c
     return SALTY_OK;
 }
 
-salty_status launch_wgrad(salty_ctx* ctx, const bf16* dy, int cpad, int cout, const ConvSrc& x, int cin, float* dw,
-                          int N, int H, int W) {
+salty_status launch_wgrad(salty_ctx* ctx, Unet& u, const bf16* dy, int cpad, int cout, const ConvSrc& x, int cin,
+                          float* dw, int N, int H, int W) {
+    if (u.conv_kind != SALTY_CONV_MMA_SYNC)
+        return conv_wgrad_tc(ctx, dy, cpad, cout, x, cin, dw, N, H, W, u.wg_ws.p, u.wg_ws.cap, u.cat_ws.p,
+                             u.cat_ws.cap, ctx->status.p + 8);
     const size_t smem = ((size_t)kTileX * kTileY * (kWgradCo + 8) + (size_t)kHaloX * kHaloY * 24) * sizeof(bf16);
     const int tiles = N * ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
     const int mg = (cpad + kWgradCo - 1) / kWgradCo;
@@ -772,6 +790,20 @@ salty_status ensure_workspace(salty_ctx* ctx, Unet& u, int N, int H, int W) {
     o = 0;
     for (int i = 0; i < G_COUNT; ++i) { u.g_off[i] = o; o += (gsz_[i] + 63) / 64 * 64; }
     SALTY_TRY_CUDA(ctx->err, u.gbuf.ensure((size_t)o));
+    size_t ws = 0;
+    for (int i = 0; i < kNumLayers; ++i) {
+        const UnetLayer& L = u.layers[i];
+        const int lv = kLayerLevel[i];
+        ws = std::max(ws, conv_wgrad_tc_workspace(ctx->num_sms, L.cin, L.cout_pad, N, H >> lv, W >> lv));
+    }
+    // the bias gradients' per-block partials use the same workspace: up to 2 blocks per SM
+    // x 128 channels
+    ws = std::max(ws, (size_t)ctx->num_sms * 2 * 128);
+    SALTY_TRY_CUDA(ctx->err, u.wg_ws.ensure(ws));
+    size_t cat = 0;
+    for (int i = 0; i < kNumLayers; ++i)
+        cat = std::max(cat, (size_t)N * (H >> kLayerLevel[i]) * (W >> kLayerLevel[i]) * u.layers[i].cin);
+    SALTY_TRY_CUDA(ctx->err, u.cat_ws.ensure(cat));
     u.N = N; u.H = H; u.W = W;
     return SALTY_OK;
 }
@@ -841,8 +873,10 @@ salty_status conv_backward(salty_ctx* ctx, Unet& u, Fwd& F, int li, const ConvSr
     k_relu_bwd<<<gsz(npx * L.cout_pad / 8), 256, 0, st>>>(F.t[y], L.cout, dy, L.cout, L.relu, npx, g, L.cout_pad);
     // few blocks: each adds its partial sums into the C gradient words once
     const int bias_blocks = (int)std::min<long long>((long long)ctx->num_sms * 2, (npx + 255) / 256);
-    k_bias_grad<<<bias_blocks, 256, L.cout * sizeof(float), st>>>(g, L.cout_pad, L.cout, npx, u.grads.p + L.b_off);
-    SALTY_TRY(launch_wgrad(ctx, g, L.cout_pad, L.cout, x, L.cin, u.grads.p + L.w_off, N, h, w));
+    k_bias_grad<<<bias_blocks, 256, 256 / (L.cout / 8) * L.cout * sizeof(float), st>>>(g, L.cout_pad, L.cout, npx,
+                                                                                       u.wg_ws.p);
+    k_bias_reduce<<<(L.cout + 127) / 128, 128, 0, st>>>(u.wg_ws.p, bias_blocks, L.cout, u.grads.p + L.b_off);
+    SALTY_TRY(launch_wgrad(ctx, u, g, L.cout_pad, L.cout, x, L.cin, u.grads.p + L.w_off, N, h, w));
     if (want_dx)
         SALTY_TRY(launch_conv(ctx, u.conv_kind, conv_src(g, L.cout_pad, L.cout_pad), L.cout_pad, u.wb.p + L.wb_off,
                               L.rows_bwd, L.nt_b, nullptr, F.t[T_G2], L.cin, L.cin, N, h, w, 0));

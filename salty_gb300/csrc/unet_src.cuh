@@ -49,4 +49,15 @@ salty_status conv3x3_tma(salty_ctx* ctx, const __nv_bfloat16* in, int in_cs, int
                          int wrows, const float* bias, __nv_bfloat16* out, int out_cs, int out_co, int cout, int N,
                          int H, int W, int relu, int* d_status);
 
+// Weight gradient of a 3x3 convolution on tcgen05, deterministic (partial sums per CTA,
+// added in a fixed order): dw[9][cout][cin] += sum over pixels of dY x X(tap).  dy
+// [N][H][W][cpad] (cpad = cout rounded up to 16, <= 128, zero beyond cout, 16-byte
+// aligned); x the layer's input (cin % 16 == 0; a decoder's concatenation is first written
+// out into cat_ws, N*H*W*cin elements); ws a workspace of at least
+// conv_wgrad_tc_workspace(...) floats.
+size_t conv_wgrad_tc_workspace(int num_sms, int cin, int cpad, int N, int H, int W);
+salty_status conv_wgrad_tc(salty_ctx* ctx, const __nv_bfloat16* dy, int cpad, int cout, const ConvSrc& x, int cin,
+                           float* dw, int N, int H, int W, float* ws, size_t ws_floats, __nv_bfloat16* cat_ws,
+                           size_t cat_elems, int* d_status);
+
 }  // namespace salty

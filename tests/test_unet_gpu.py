@@ -69,6 +69,45 @@ def test_gradients_match_oracle(net):
         o += n
 
 
+def test_weight_gradient_kernels_agree(ctx):
+    """The tensor-core weight gradient (tcgen05, partial sums per CTA added in a fixed
+    order) against the mma.sync one, layer by layer: the two differ only by FP32 summation
+    order, in the weight gradients and in the BF16 roundings of the backward pass."""
+    import salty_gb300
+    from oracle.unet_oracle import LAYERS
+    f, t = _batch(21, n=2, h=64, w=96)
+    grads = {}
+    for kind in (salty_gb300.CONV_MMA_SYNC, salty_gb300.CONV_TCGEN05):
+        net = salty_gb300.Unet(ctx, seed=13)
+        net.set_conv_kernel(kind)
+        net.train_step(f, t, lr=0.0)
+        grads[kind] = net.grads()
+        net.close()
+    a, b = grads[salty_gb300.CONV_TCGEN05], grads[salty_gb300.CONV_MMA_SYNC]
+    o = 0
+    for i, (ci, co, _) in enumerate(LAYERS):
+        n = 9 * ci * co
+        wa, wb = a[o:o + n], b[o:o + n]
+        cos = wa @ wb / max(np.linalg.norm(wa) * np.linalg.norm(wb), 1e-30)
+        assert _rel(wa, wb) < 0.02 and cos > 0.9998, (i, _rel(wa, wb), cos)
+        o += n + co
+
+
+def test_tensor_core_training_is_deterministic(ctx):
+    """Two identical training steps give bit-identical gradients: no atomics in the
+    tensor-core backward pass."""
+    import salty_gb300
+    f, t = _batch(22, n=2, h=48, w=64)
+    g = []
+    for _ in range(2):
+        net = salty_gb300.Unet(ctx, seed=14)
+        net.set_conv_kernel(salty_gb300.CONV_TCGEN05)
+        net.train_step(f, t, lr=0.0)
+        g.append(net.grads())
+        net.close()
+    np.testing.assert_array_equal(g[0], g[1])
+
+
 def test_adam_first_step(ctx):
     """First Adam step moves every parameter with a clear gradient by lr against its sign."""
     import salty_gb300
