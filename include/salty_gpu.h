@@ -173,6 +173,28 @@ void salty_mesh_free(salty_mesh* mesh);
 salty_status salty_mesh_transform(const float* matrix, int64_t n_tris, const float* pos_in, const float* nrm_in,
                                   float* pos_out, float* nrm_out);
 
+/* ---------------------------------------------------------------- instances */
+/* One placed copy of a mesh: the scene's triangles [first_tri, first_tri + n_tris) under a
+ * row-major 3x4 object-to-world matrix (x' = M[0..2].x + M[3], ...; invertible). */
+typedef struct salty_instance {
+    int64_t first_tri;
+    int64_t n_tris;
+    float object_to_world[12];
+} salty_instance;
+
+/* Instance (src/s3d_instance.cpp:22-101): makes the scene's world n placed copies of its
+ * meshes, each stored once, in a two-level BVH -- a top-level BVH over the instances' world
+ * boxes whose leaves lead into one BVH per distinct mesh, which rays enter transformed to
+ * object space (directions not renormalised, so hit distances stay world distances; the
+ * reference renormalises, which makes distances of scaled instances incomparable).  Call
+ * after salty_scene_upload and before salty_bvh_build; n = 0 returns to the flat scene.
+ * The area light stays in world space.  Triangle ids (salty_trace, hit records) are then
+ * virtual: instance i's triangle j is id base_i + j, base_i the triangle count of the
+ * instances before it, the light's two triangles last.  Instanced scenes render through
+ * salty_render (not salty_render_batch).  instances: host array. */
+salty_status salty_scene_set_instances(salty_ctx* ctx, salty_scene* scene, const salty_instance* instances,
+                                       int32_t n);
+
 /* ---------------------------------------------------------------- BVH */
 typedef struct salty_build_opts {
     int32_t bins;          /* SAH bins per axis, 8..32 (default 32) */

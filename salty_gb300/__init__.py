@@ -67,6 +67,10 @@ class Texture(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgb", C.c_void_p)]
 
 
+class Instance(C.Structure):
+    _fields_ = [("first_tri", C.c_int64), ("n_tris", C.c_int64), ("object_to_world", C.c_float * 12)]
+
+
 class BuildOpts(C.Structure):
     _fields_ = [("bins", C.c_int32), ("max_leaf", C.c_int32), ("trav_cost", C.c_float)]
 
@@ -118,7 +122,8 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_unet_train_step", "salty_scene_set_camera", "salty_denoise_unet", "salty_render_batch",
            "salty_get_tuning", "salty_set_tuning", "salty_autotune", "salty_mesh_load_smd", "salty_mesh_free",
            "salty_mesh_transform", "salty_autotune_trace", "salty_denoise_unet_ensemble", "salty_film_checkpoint",
-           "salty_film_restore", "salty_unet_get_adam", "salty_unet_set_adam", "salty_unet_set_conv_kernel"]
+           "salty_film_restore", "salty_unet_get_adam", "salty_unet_set_adam", "salty_unet_set_conv_kernel",
+           "salty_scene_set_instances"]
 
 _lib = None
 
@@ -143,6 +148,7 @@ def lib() -> C.CDLL:
         "salty_scene_upload": (i32, [vp, C.POINTER(SceneDesc), C.POINTER(vp)]),
         "salty_scene_destroy": (None, [vp, vp]),
         "salty_scene_set_camera": (i32, [vp, vp, C.POINTER(Camera)]),
+        "salty_scene_set_instances": (i32, [vp, vp, vp, C.c_int32]),
         "salty_bvh_build": (i32, [vp, vp, C.POINTER(BuildOpts), C.POINTER(BvhInfo)]),
         "salty_trace": (i32, [vp, vp, vp, i64, u32, vp]),
         "salty_last_trace_stats": (i32, [vp, C.POINTER(TraceStats)]),
@@ -555,6 +561,16 @@ class Scene:
         c.fov, c.near_clip = float(fov), float(near)
         c.lens_radius, c.focal_distance = float(lens_radius), float(focal_distance)
         self.ctx.check(lib().salty_scene_set_camera(self.ctx.h, self.h, C.byref(c)), "scene_set_camera")
+
+    def set_instances(self, instances) -> None:
+        """salty_scene_set_instances: the world becomes placed copies of the scene's meshes,
+        each an (first_tri, n_tris, 3x4 object-to-world matrix) triple; build afterwards."""
+        arr = (Instance * max(1, len(instances)))()
+        for i, (first, n, m) in enumerate(instances):
+            arr[i].first_tri, arr[i].n_tris = int(first), int(n)
+            arr[i].object_to_world = (C.c_float * 12)(*np.asarray(m, np.float32).reshape(12).tolist())
+        self.ctx.check(lib().salty_scene_set_instances(self.ctx.h, self.h, C.byref(arr), len(instances)),
+                       "scene_set_instances")
 
     def aov(self, width: int, height: int) -> dict:
         """Mean first-hit features of the film: albedo, normal (H, W, 3), depth = 1/(1+t) (H, W)."""

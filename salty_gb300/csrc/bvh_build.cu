@@ -676,10 +676,18 @@ inline unsigned grid_for(long long n, int block) { return (unsigned)((n + block 
 }  // namespace
 
 salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& opts) {
+    if (sc->n_inst > 0) return build_instanced(ctx, sc, opts);
+    if (sc->n_tris <= 0) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "scene has no triangles");
+    if (sc->n_tris > (int64_t)0x3fffffff)
+        return ctx->err.fail(SALTY_ERR_CAPACITY, "too many triangles (%lld)", (long long)sc->n_tris);
+    float box[6];
+    return build_bvh_tris(ctx, sc->pos.p, (int)sc->n_tris, opts, sc->bvh, box);
+}
+
+salty_status build_bvh_tris(salty_ctx* ctx, const float* d_pos, int n, const salty_build_opts& opts, Bvh& out,
+                            float root_box[6]) {
     auto& E = ctx->err;
-    const int n = (int)sc->n_tris;
-    if (sc->n_tris <= 0) return E.fail(SALTY_ERR_INVALID_ARG, "scene has no triangles");
-    if (sc->n_tris > (int64_t)0x3fffffff) return E.fail(SALTY_ERR_CAPACITY, "too many triangles (%lld)", (long long)sc->n_tris);
+    if (n <= 0) return E.fail(SALTY_ERR_INVALID_ARG, "no triangles to build a BVH over");
     BuildParams prm;
     prm.B = opts.bins;
     prm.max_leaf = opts.max_leaf;
@@ -711,7 +719,7 @@ salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& 
     cudaEvent_t e0 = ctx->ev[0], e1 = ctx->ev[1];
     cudaEventRecord(e0, st);
     k_init_counters<<<1, 1, 0, st>>>(ctr.p);
-    k_prim_setup<<<grid_for(n, 256), 256, 0, st>>>(sc->pos.p, n, lo4.p, hi4.p, cen4.p, prim[0].p,
+    k_prim_setup<<<grid_for(n, 256), 256, 0, st>>>(d_pos, n, lo4.p, hi4.p, cen4.p, prim[0].p,
                                                    pos_task[0].p, ctr.p);
     k_root_init<<<1, 1, 0, st>>>(ctr.p, tasks[0].p, bnodes.p, n, 0);
     int cur = 0;
@@ -754,11 +762,12 @@ salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& 
         k_collapse_dp<<<grid_for(b1 - b0, 128), 128, 0, st>>>(bnodes.p, dp.p, b0, b1, kCollapseNodeCost,
                                                                kCollapseTriCost);
     }
-    SALTY_TRY_CUDA(E, sc->bvh.nodes.ensure((size_t)n + 1));
-    SALTY_TRY_CUDA(E, sc->bvh.tris.ensure((size_t)n * kTriFloat4));
+    SALTY_TRY_CUDA(E, out.nodes.ensure((size_t)n + 1));
+    SALTY_TRY_CUDA(E, out.tris.ensure((size_t)n * kTriFloat4));
     BNode root;
     SALTY_TRY_CUDA(E, cudaMemcpyAsync(&root, bnodes.p, sizeof(BNode), cudaMemcpyDeviceToHost, st));
     SALTY_TRY_CUDA(E, cudaStreamSynchronize(st));
+    for (int a = 0; a < 3; ++a) { root_box[a] = root.lo[a]; root_box[3 + a] = root.hi[a]; }
     float rdx = root.hi[0] - root.lo[0], rdy = root.hi[1] - root.lo[1], rdz = root.hi[2] - root.lo[2];
     float root_sa = 2.0f * (rdx * rdy + rdx * rdz + rdy * rdz);
     if (!(root_sa > 0.0f)) root_sa = 1.0f;
@@ -771,8 +780,8 @@ salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& 
     int nwork = 1, wcur = 0, depth8 = 0;
     while (nwork > 0) {
         cudaMemsetAsync(&ctr.p->next_work, 0, sizeof(int), st);
-        k_collapse<<<grid_for(nwork, 128), 128, 0, st>>>(bnodes.p, nwork, work[wcur].p, sc->bvh.nodes.p,
-                                                         sc->bvh.tris.p, prim[cur].p, sc->pos.p,
+        k_collapse<<<grid_for(nwork, 128), 128, 0, st>>>(bnodes.p, nwork, work[wcur].p, out.nodes.p,
+                                                         out.tris.p, prim[cur].p, d_pos,
                                                          work[wcur ^ 1].p, ctr.p, root_sa, dp.p);
         SALTY_TRY_CUDA(E, cudaMemcpyAsync(hc, ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, st));
         SALTY_TRY_CUDA(E, cudaStreamSynchronize(st));
@@ -787,18 +796,18 @@ salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& 
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     if (hc->ntris != n) return E.fail(SALTY_ERR_CUDA, "collapse wrote %d of %d triangles", hc->ntris, n);
-    sc->bvh.n_nodes = hc->n8;
-    sc->bvh.n_tris = n;
-    sc->bvh.depth = depth8;
-    sc->bvh.built = true;
+    out.n_nodes = hc->n8;
+    out.n_tris = n;
+    out.depth = depth8;
+    out.built = true;
     static std::atomic<uint64_t> builds{0};
-    sc->bvh.generation = ++builds;  // unique in the process
-    sc->bvh.info.n_nodes = hc->n8;
-    sc->bvh.info.n_binary = n_binary;
-    sc->bvh.info.depth = depth8;
-    sc->bvh.info.binary_depth = bdepth;
-    sc->bvh.info.sah_cost = hc->sah;
-    sc->bvh.info.build_ms = ms;
+    out.generation = ++builds;  // unique in the process
+    out.info.n_nodes = hc->n8;
+    out.info.n_binary = n_binary;
+    out.info.depth = depth8;
+    out.info.binary_depth = bdepth;
+    out.info.sah_cost = hc->sah;
+    out.info.build_ms = ms;
     return SALTY_OK;
 }
 

@@ -163,13 +163,33 @@ struct Bvh {
     salty_bvh_info info{};
 };
 
+// One placed copy of a mesh in a two-level BVH, as the traversal reads it: the world-to-
+// object transform for rays, the mesh's BVH root in the scene's node arena and the virtual
+// triangle id of the instance's first triangle.
+struct alignas(16) InstRec {
+    float w2o[12];      // row-major 3x4
+    unsigned root;      // the mesh's BVH8 root node
+    int vbase;          // instance triangle j has id vbase + j
+    int first;          // scene index of the mesh's first triangle
+    int pad;
+};
+// The same instance as shading reads it: object-to-world transform of positions and the
+// normal matrix (inverse transpose of its linear part).
+struct alignas(16) InstShade {
+    float o2w[12];
+    float nrm[9];
+    float pad[3];
+};
+
 // What one traversal launch walks: a BVH (or a batch arena of concatenated BVHs) and, per
-// ray, the node it starts at.
+// ray, the node it starts at.  With `inst`, node 0 starts a top-level BVH whose leaf
+// entries are instances (two levels).
 struct TraceTarget {
     const Bvh8Node* nodes = nullptr;
     const float4* tris = nullptr;
     int depth = 0;
     const int* roots = nullptr;  // per-ray root node, or null (node 0)
+    const InstRec* inst = nullptr;
 };
 
 // Launch shape of the traversal kernel, chosen by salty_autotune.
@@ -198,6 +218,14 @@ struct salty_scene {
     salty::SceneConsts consts{};
     salty::Bvh bvh;
     salty::Film film;
+    // Instance (src/s3d_instance.cpp:22-101): when n_inst > 0 the world is these placed
+    // copies of the scene's meshes (the light's triangles are one more, untransformed)
+    std::vector<salty_instance> inst_host;
+    salty::DevBuf<salty::InstRec> inst_rec;
+    salty::DevBuf<salty::InstShade> inst_shade;
+    salty::DevBuf<int> inst_vbase;  // n_inst + 1 prefix sums of triangle counts
+    int n_inst = 0;
+    int64_t n_virtual = 0;          // triangles of all instances
 };
 
 namespace salty {
@@ -263,6 +291,11 @@ struct salty_ctx {
 namespace salty {
 // bvh_build.cu
 salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& opts);
+// a BVH over n triangles (9 floats each, device) into `out`; root box lo, hi (host)
+salty_status build_bvh_tris(salty_ctx* ctx, const float* d_pos, int n, const salty_build_opts& opts, Bvh& out,
+                            float root_box[6]);
+// instance.cu
+salty_status build_instanced(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& opts);
 // trace.cu
 salty_status trace_launch(salty_ctx* ctx, salty_scene* sc, const float4* d_rays, long long n,
                           const int* n_dev, uint32_t flags, float4* d_hits,

@@ -158,6 +158,10 @@ struct WaveParams {
     const SceneSlot* slots;
     const long long* sample_off;  // per slot, then the total (n_slots + 1 entries)
     const long long* pixel_off;   // per slot, then the total
+    const InstRec* irec;          // instances (two-level scenes, one slot), or null
+    const InstShade* ishade;
+    const int* ivbase;            // n_inst + 1 first virtual ids
+    int n_inst;
     int n_slots;
     int capacity;
     long long total_samples;
@@ -275,19 +279,53 @@ struct Surf {
     bool into;
 };
 
-__device__ __forceinline__ Surf surface(const WaveParams& P, int id, float t, float u, float v, V o, V d) {
+// The scene triangle behind a hit id: the id itself, or, in a scene of instances, the mesh
+// triangle of the (virtual) id and its instance (inst = -1 when there are none).
+__device__ __forceinline__ int mesh_tri(const WaveParams& P, int id, int& inst) {
+    inst = -1;
+    if (P.n_inst == 0) return id;
+    int lo = 0, hi = P.n_inst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.ivbase[mid] <= id) lo = mid;
+        else hi = mid - 1;
+    }
+    inst = lo;
+    return P.irec[lo].first + (id - P.ivbase[lo]);
+}
+__device__ __forceinline__ V inst_point(const InstShade& S, V p) {
+    return mk(S.o2w[0] * p.x + S.o2w[1] * p.y + S.o2w[2] * p.z + S.o2w[3],
+              S.o2w[4] * p.x + S.o2w[5] * p.y + S.o2w[6] * p.z + S.o2w[7],
+              S.o2w[8] * p.x + S.o2w[9] * p.y + S.o2w[10] * p.z + S.o2w[11]);
+}
+// Triangle::CalcParam's normal (src/s3d_triangle.cpp:107-121), not normalised, in world
+// space: Instance::CalcParam (src/s3d_instance.cpp:80-84) applies the inverse transpose
+__device__ __forceinline__ V interp_normal(const WaveParams& P, int mt, int inst, float u, float v) {
+    const float* np = P.nrm + (size_t)mt * 9;
+    const float al = 1.0f - u - v;
+    const V n = mk(np[0] * al + np[3] * u + np[6] * v, np[1] * al + np[4] * u + np[7] * v,
+                   np[2] * al + np[5] * u + np[8] * v);
+    if (inst < 0) return n;
+    const float* m = P.ishade[inst].nrm;
+    return mk(m[0] * n.x + m[1] * n.y + m[2] * n.z, m[3] * n.x + m[4] * n.y + m[5] * n.z,
+              m[6] * n.x + m[7] * n.y + m[8] * n.z);
+}
+
+__device__ __forceinline__ Surf surface(const WaveParams& P, int mt, int inst, float t, float u, float v, V o, V d) {
     Surf s;
     s.p = o + d * t;
-    const float* tp = P.pos + (size_t)id * 9;
+    const float* tp = P.pos + (size_t)mt * 9;
     V v0 = ld3(tp), v1 = ld3(tp + 3), v2 = ld3(tp + 6);
+    if (inst >= 0) {
+        const InstShade& S = P.ishade[inst];
+        v0 = inst_point(S, v0);
+        v1 = inst_point(S, v1);
+        v2 = inst_point(S, v2);
+    }
     s.ng = safe_unit(cross(v1 - v0, v2 - v0));
     s.into = dot(s.ng, d) < 0.0f;
     s.ngf = s.into ? s.ng : -s.ng;
-    // Triangle::CalcParam (src/s3d_triangle.cpp:107-121)
-    const float* np = P.nrm + (size_t)id * 9;
-    float al = 1.0f - u - v;
-    V n = mk(np[0] * al + np[3] * u + np[6] * v, np[1] * al + np[4] * u + np[7] * v, np[2] * al + np[5] * u + np[8] * v);
-    s.ns = safe_unit(n);
+    s.ns = safe_unit(interp_normal(P, mt, inst, u, v));
     s.nsf = dot(s.ns, d) < 0.0f ? s.ns : -s.ns;
     return s;
 }
@@ -437,9 +475,11 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
         const SceneSlot& S = P.slots[slot];
         const SceneConsts& K = S.k;
         if (live && id >= 0 && !is_light(K, id)) {
-            GpuMaterial m = P.mats[P.mat[id]];
+            int inst;
+            const int mtri = mesh_tri(P, id, inst);
+            GpuMaterial m = P.mats[P.mat[mtri]];
             // TexturedMaterial::GetBaseColor: the colour map multiplies the base colour
-            const V tx = color_map(P, m, id, h.z, h.w);
+            const V tx = color_map(P, m, mtri, h.z, h.w);
             m.color[0] *= tx.x; m.color[1] *= tx.y; m.color[2] *= tx.z;
             const bool delta = (m.type == SALTY_MIRROR || m.type == SALTY_GLASS);
             Rng rng;
@@ -451,10 +491,7 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
                     Surf s;
                     s.p = mk(__fadd_rn(o.x, __fmul_rn(d.x, h.x)), __fadd_rn(o.y, __fmul_rn(d.y, h.x)),
                              __fadd_rn(o.z, __fmul_rn(d.z, h.x)));
-                    const float* np = P.nrm + (size_t)id * 9;
-                    float al = 1.0f - h.z - h.w;
-                    V n = safe_unit(mk(np[0] * al + np[3] * h.z + np[6] * h.w, np[1] * al + np[4] * h.z + np[7] * h.w,
-                                       np[2] * al + np[5] * h.z + np[8] * h.w));
+                    V n = safe_unit(interp_normal(P, mtri, inst, h.z, h.w));
                     (void)rng.u32();  // Scene::GetLight (include/s3d_scene.h:84-90), one light
                     float u = rng.f32(), w = rng.f32();
                     V lp = ld3(K.lc) + ld3(K.la) * u + ld3(K.lb) * w;
@@ -475,7 +512,7 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
                 }
             } else {
                 if (!delta) {
-                    Surf s = surface(P, id, h.x, h.z, h.w, o, d);
+                    Surf s = surface(P, mtri, inst, h.x, h.z, h.w, o, d);
                     V wo = -d;
                     if (K.has_light) {
                         float u1 = rng.f32(), u2 = rng.f32();
@@ -590,14 +627,13 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
             if (depth == 0 && id >= 0) {
                 // first-hit features of the sample (denoiser inputs): albedo, 1/(1+t),
                 // shading normal facing the camera
-                const GpuMaterial am = P.mats[P.mat[id]];
-                const float* np = P.nrm + (size_t)id * 9;
-                const float al = 1.0f - h.z - h.w;
-                V n = safe_unit(mk(np[0] * al + np[3] * h.z + np[6] * h.w, np[1] * al + np[4] * h.z + np[7] * h.w,
-                                   np[2] * al + np[5] * h.z + np[8] * h.w));
+                int inst;
+                const int mtri = mesh_tri(P, id, inst);
+                const GpuMaterial am = P.mats[P.mat[mtri]];
+                V n = safe_unit(interp_normal(P, mtri, inst, h.z, h.w));
                 if (dot(n, d) > 0.0f) n = -n;
                 const bool emitter = is_light(K, id);
-                const V atx = color_map(P, am, id, h.z, h.w);
+                const V atx = color_map(P, am, mtri, h.z, h.w);
                 B.abuf[2 * mt.z] = make_float4(emitter ? 1.0f : am.color[0] * atx.x, emitter ? 1.0f : am.color[1] * atx.y,
                                                emitter ? 1.0f : am.color[2] * atx.z, 1.0f / (1.0f + h.x));
                 B.abuf[2 * mt.z + 1] = make_float4(n.x, n.y, n.z, 0.0f);
@@ -610,15 +646,14 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                     L = L + W * ld3(K.sun_L) * w;
                 }
             } else if (compat) {
-                const GpuMaterial m = P.mats[P.mat[id]];
-                const V tx = color_map(P, m, id, h.z, h.w);  // TexturedMaterial::Shade scales the weight
+                int inst;
+                const int mtri = mesh_tri(P, id, inst);
+                const GpuMaterial m = P.mats[P.mat[mtri]];
+                const V tx = color_map(P, m, mtri, h.z, h.w);  // TexturedMaterial::Shade scales the weight
                 V pos = mk(__fadd_rn(o.x, __fmul_rn(d.x, h.x)), __fadd_rn(o.y, __fmul_rn(d.y, h.x)),
                            __fadd_rn(o.z, __fmul_rn(d.z, h.x)));
                 L = L + W * ld3(m.emission);
-                const float* np = P.nrm + (size_t)id * 9;
-                float al = 1.0f - h.z - h.w;
-                V normal = safe_unit(mk(np[0] * al + np[3] * h.z + np[6] * h.w, np[1] * al + np[4] * h.z + np[7] * h.w,
-                                        np[2] * al + np[5] * h.z + np[8] * h.w));
+                V normal = safe_unit(interp_normal(P, mtri, inst, h.z, h.w));
                 V nm = dot(normal, d) < 0.0f ? normal : -normal;
                 V col = ld3(m.color), out, wgt;
                 bool dice = false;
@@ -710,10 +745,12 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                     }
                 }
             } else {
-                GpuMaterial m = P.mats[P.mat[id]];
-                const V tx = color_map(P, m, id, h.z, h.w);
+                int inst;
+                const int mtri = mesh_tri(P, id, inst);
+                GpuMaterial m = P.mats[P.mat[mtri]];
+                const V tx = color_map(P, m, mtri, h.z, h.w);
                 m.color[0] *= tx.x; m.color[1] *= tx.y; m.color[2] *= tx.z;
-                Surf s = surface(P, id, h.x, h.z, h.w, o, d);
+                Surf s = surface(P, mtri, inst, h.x, h.z, h.w, o, d);
                 L = L + W * ld3(m.emission);
                 V col = ld3(m.color), wi, wgt;
                 float pdf = 0.0f;
@@ -1161,10 +1198,16 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     const GpuMaterial* mats;
     const GpuTexture* textures;
     const float4* texels;
+    if (n > 1)
+        for (int i = 0; i < n; ++i)
+            if (scenes[i]->n_inst > 0)
+                return E.fail(SALTY_ERR_INVALID_ARG, "scene %d of the batch holds instances: render it with salty_render",
+                              i);
     if (n == 1) {
         tgt.nodes = scenes[0]->bvh.nodes.p;
         tgt.tris = scenes[0]->bvh.tris.p;
         tgt.depth = scenes[0]->bvh.depth;
+        tgt.inst = scenes[0]->n_inst > 0 ? scenes[0]->inst_rec.p : nullptr;
         pos = scenes[0]->pos.p;
         nrm = scenes[0]->nrm.p;
         uv = scenes[0]->uv.p;
@@ -1287,6 +1330,10 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     P.slots = reinterpret_cast<const SceneSlot*>(dslots);
     P.sample_off = doffs;
     P.pixel_off = doffs + n + 1;
+    P.n_inst = (n == 1) ? scenes[0]->n_inst : 0;
+    P.irec = P.n_inst ? scenes[0]->inst_rec.p : nullptr;
+    P.ishade = P.n_inst ? scenes[0]->inst_shade.p : nullptr;
+    P.ivbase = P.n_inst ? scenes[0]->inst_vbase.p : nullptr;
     P.n_slots = n;
     P.capacity = (int)cap;
     P.total_samples = samples;

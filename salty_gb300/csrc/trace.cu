@@ -6,8 +6,11 @@
 // written fully coalesced.  Replaces the per-pixel Scene::Intersect calls of the
 // reference's OpenMP row loop (src/s3d_pt.cpp:310-333, include/s3d_scene.h:63-75).
 //
-// A launch walks one BVH, or a batch arena holding several scenes' BVHs back to back; then
-// every ray names the root node of its scene.
+// A launch walks one BVH, or a batch arena holding several scenes' BVHs back to back (then
+// every ray names the root node of its scene), or a two-level BVH of instances: its top
+// level's leaf entries are instances, and a ray reaching one is transformed into the
+// instance's object space and walks the instance's mesh BVH, above a marker on its stack;
+// popping the marker brings back the world ray and the top-level walk (instance.cu).
 #include "internal.h"
 #include "traverse.cuh"
 
@@ -22,12 +25,15 @@ constexpr int kMaxStack = 63;  // stack entries per thread: BVHs up to 31 levels
 // spilled values).
 // The short stack lives in dynamic shared memory, `depth` entries per thread (two per BVH
 // level plus one), so shallow trees leave room for more resident blocks.
-template <bool ANY, bool WT, bool COUNT, int TB, bool CAP>
+// Stack entry (.y) that marks where a ray entered an instance.
+constexpr unsigned kInstMarker = 0x40000000u;
+
+template <bool ANY, bool WT, bool COUNT, int TB, bool CAP, bool INST>
 __global__ void __launch_bounds__(TB, CAP ? 1280 / TB : 1024 / TB)
 k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, const float4* __restrict__ rays,
         const int* __restrict__ roots, long long n_arg, const int* __restrict__ n_dev, float4* __restrict__ hits,
         unsigned long long* __restrict__ counters, float cull_slack, int pool, int postpone, int depth,
-        int* __restrict__ status) {
+        int* __restrict__ status, const InstRec* __restrict__ inst) {
     extern __shared__ uint2 sstack[];
     TravStack st{sstack + threadIdx.x, TB, depth};
     const int lane = threadIdx.x & 31;
@@ -44,6 +50,8 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
     long long rid = -1;
     TravRay r;
     TravState s;
+    bool in_mesh = false;  // INST: walking an instance's mesh (else the top level)
+    int vbase = 0;         // INST: virtual id of the current instance's first triangle
     for (;;) {
         const bool idle = rid < 0;
         const unsigned idle_mask = __ballot_sync(0xffffffffu, idle);
@@ -62,15 +70,48 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
                 const float4 ra = __ldcs(rays + 2 * rid), rb = __ldcs(rays + 2 * rid + 1);
                 make_trav_ray(r, ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w);
                 trav_init(s, r, roots ? (unsigned)__ldcs(roots + rid) : 0u);
+                in_mesh = false;
+                vbase = 0;
             }
             pool_next = min(pool_end, pool_next + __popc(idle_mask));
         }
         const bool active = rid >= 0;
         if (__ballot_sync(0xffffffffu, active) == 0) break;
         if (active && s.ng_hits) trav_node_step<COUNT>(s, nodes, r, st, cnt, overflow);
+        // INST: a top-level leaf group holds instances; enter the first one, leaving the rest
+        // of the group, the pending node group and a return marker on the stack
+        if (INST && active && !in_mesh && s.tg_hits) {
+            const unsigned k = __ffs(s.tg_hits) - 1;
+            s.tg_hits &= s.tg_hits - 1;
+            const int iid = __float_as_int(__ldg(tris + (size_t)(s.tg_base + k) * kTriFloat4).w);
+            if (s.sp + 3 <= depth) {
+                if (s.ng_hits) st.at(s.sp++) = make_uint2(s.ng_base, (s.ng_hits << 8) | s.ng_imask);
+                if (s.tg_hits) st.at(s.sp++) = make_uint2(s.tg_base, s.tg_hits | kTriGroupFlag);
+                st.at(s.sp++) = make_uint2(0u, kInstMarker);
+                s.tg_hits = 0;
+                const InstRec& R = inst[iid];
+                const float* m = R.w2o;
+                const float ox = fmaf(m[0], r.ox, fmaf(m[1], r.oy, fmaf(m[2], r.oz, m[3])));
+                const float oy = fmaf(m[4], r.ox, fmaf(m[5], r.oy, fmaf(m[6], r.oz, m[7])));
+                const float oz = fmaf(m[8], r.ox, fmaf(m[9], r.oy, fmaf(m[10], r.oz, m[11])));
+                const float dx = fmaf(m[0], r.dx, fmaf(m[1], r.dy, m[2] * r.dz));
+                const float dy = fmaf(m[4], r.dx, fmaf(m[5], r.dy, m[6] * r.dz));
+                const float dz = fmaf(m[8], r.dx, fmaf(m[9], r.dy, m[10] * r.dz));
+                make_trav_ray(r, ox, oy, oz, r.tmin, dx, dy, dz, r.tmax);
+                s.ng_base = R.root;
+                s.ng_hits = 1u << r.oct;
+                s.ng_imask = 1u;
+                in_mesh = true;
+                vbase = R.vbase;
+            } else {
+                overflow = 1;
+                s.ng_hits = 0;
+                s.tg_hits = 0;
+            }
+        }
         // Triangle postponing: with too few lanes holding triangles, set the group aside
         // and keep walking nodes with the rest of the warp.
-        const bool want = active && s.tg_hits != 0;
+        const bool want = active && s.tg_hits != 0 && (!INST || in_mesh);
         const unsigned want_mask = __ballot_sync(0xffffffffu, want);
         bool run = want;
         if (want && __popc(want_mask) < postpone && s.ng_hits != 0 && s.sp < depth) {
@@ -79,8 +120,20 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
             run = false;
         }
         bool done = false;
-        if (run) done = trav_tri_step<ANY, WT, COUNT>(s, tris, r, cull_slack, cnt);
-        if (active && (done || !trav_pop(s, st))) {
+        if (run) done = trav_tri_step<ANY, WT, COUNT>(s, tris, r, cull_slack, cnt, vbase);
+        bool more = true;
+        if (INST && active && !done && !s.ng_hits && !s.tg_hits && s.sp > 0 &&
+            st.at(s.sp - 1).y == kInstMarker) {
+            // the instance's walk is over: back to the world ray and the top level
+            --s.sp;
+            const float4 ra = __ldcs(rays + 2 * rid), rb = __ldcs(rays + 2 * rid + 1);
+            make_trav_ray(r, ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w);
+            in_mesh = false;
+            vbase = 0;
+        } else if (active && !done) {
+            more = trav_pop(s, st);
+        }
+        if (active && (done || !more)) {
             __stcs(hits + rid, make_float4(s.hit.t, __int_as_float(s.hit.id), s.hit.u, s.hit.v));
             rid = -1;
         }
@@ -112,9 +165,9 @@ struct Launch {
     int* status;
 };
 
-template <bool ANY, bool WT, bool COUNT, int TB, bool CAP>
+template <bool ANY, bool WT, bool COUNT, int TB, bool CAP, bool INST>
 salty_status launch(salty_ctx* ctx, const Launch& L) {
-    auto kern = k_trace<ANY, WT, COUNT, TB, CAP>;
+    auto kern = k_trace<ANY, WT, COUNT, TB, CAP, INST>;
     const size_t smem = (size_t)L.depth * TB * sizeof(uint2);
     if (smem > 48 * 1024)
         SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -126,7 +179,8 @@ salty_status launch(salty_ctx* ctx, const Launch& L) {
     if (grid > want) grid = want;
     if (grid < 1) grid = 1;
     kern<<<(unsigned)grid, TB, smem, L.st>>>(L.tgt.nodes, L.tgt.tris, L.rays, L.tgt.roots, L.n, L.n_dev, L.hits,
-                                             L.counters, L.slack, L.pool, L.postpone, L.depth, L.status);
+                                             L.counters, L.slack, L.pool, L.postpone, L.depth, L.status,
+                                             L.tgt.inst);
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;
 }
@@ -135,7 +189,18 @@ template <int TB, bool CAP>
 salty_status dispatch_flags(salty_ctx* ctx, const Launch& L, uint32_t flags) {
     const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT;
 #define SALTY_L(A, W) \
-    if (any == A && wt == W) return launch<A, W, false, TB, CAP>(ctx, L)
+    if (any == A && wt == W) return launch<A, W, false, TB, CAP, false>(ctx, L)
+    SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
+#undef SALTY_L
+    return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad trace flags");
+}
+
+// Two-level walks (instances), at the register budget of 64.
+template <int TB>
+salty_status dispatch_inst(salty_ctx* ctx, const Launch& L, uint32_t flags) {
+    const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT;
+#define SALTY_L(A, W) \
+    if (any == A && wt == W) return launch<A, W, false, TB, false, true>(ctx, L)
     SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
 #undef SALTY_L
     return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad trace flags");
@@ -144,8 +209,14 @@ salty_status dispatch_flags(salty_ctx* ctx, const Launch& L, uint32_t flags) {
 // Counting walks (node and triangle fetches) use the default launch shape.
 salty_status dispatch_count(salty_ctx* ctx, const Launch& L, uint32_t flags) {
     const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT;
+    if (L.tgt.inst) {
 #define SALTY_L(A, W) \
-    if (any == A && wt == W) return launch<A, W, true, 128, false>(ctx, L)
+    if (any == A && wt == W) return launch<A, W, true, 128, false, true>(ctx, L)
+        SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
+#undef SALTY_L
+    }
+#define SALTY_L(A, W) \
+    if (any == A && wt == W) return launch<A, W, true, 128, false, false>(ctx, L)
     SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
 #undef SALTY_L
     return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad trace flags");
@@ -168,6 +239,11 @@ salty_status trace_launch(salty_ctx* ctx, const TraceTarget& tgt, const TraceTun
     Launch L{tgt, d_rays, n, n_dev, d_hits, d_counters, st, wt ? (1.0f / 65536.0f) : 1e-3f,
              tune.pool >= 32 ? tune.pool : 32, tune.postpone, need, d_status};
     if (flags & SALTY_TRACE_COUNTERS) return dispatch_count(ctx, L, flags);
+    if (tgt.inst) {
+        if (tune.block == 64) return dispatch_inst<64>(ctx, L, flags);
+        if (tune.block == 256) return dispatch_inst<256>(ctx, L, flags);
+        return dispatch_inst<128>(ctx, L, flags);
+    }
     const bool cap = tune.regs == 48;
 #define SALTY_D(B) return cap ? dispatch_flags<B, true>(ctx, L, flags) : dispatch_flags<B, false>(ctx, L, flags)
     if (tune.block == 64) SALTY_D(64);
@@ -183,6 +259,7 @@ salty_status trace_launch(salty_ctx* ctx, salty_scene* sc, const float4* d_rays,
     t.nodes = sc->bvh.nodes.p;
     t.tris = sc->bvh.tris.p;
     t.depth = sc->bvh.depth;
+    t.inst = sc->n_inst > 0 ? sc->inst_rec.p : nullptr;
     return trace_launch(ctx, t, ctx->tune.trace, d_rays, n, n_dev, flags, d_hits, d_counters, st, d_status);
 }
 

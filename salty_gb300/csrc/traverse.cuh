@@ -288,7 +288,7 @@ __device__ __forceinline__ void trav_node_step(TravState& s, const Bvh8Node* __r
 // Returns true when an any-hit query has its answer.
 template <bool ANY, bool WATERTIGHT, bool COUNT>
 __device__ __forceinline__ bool trav_tri_step(TravState& s, const float4* __restrict__ tris, const TravRay& r,
-                                              float cull_slack, TravCount& cnt) {
+                                              float cull_slack, TravCount& cnt, int id_off = 0) {
     while (s.tg_hits) {
         const unsigned k = __ffs(s.tg_hits) - 1;
         s.tg_hits &= s.tg_hits - 1;
@@ -300,7 +300,7 @@ __device__ __forceinline__ bool trav_tri_step(TravState& s, const float4* __rest
         const bool h = WATERTIGHT ? tri_watertight(r, a, b, c, r.tmin, tlim, t, u, v)
                                   : tri_ref(r, a, b, c, r.tmin, r.tmax, tlim, t, u, v);
         if (h) {
-            const int id = __float_as_int(a.w);
+            const int id = __float_as_int(a.w) + id_off;  // an instance's first virtual id
             if (t < s.hit.t || (t == s.hit.t && id < s.hit.id)) {
                 s.hit.t = t;
                 s.hit.u = u;
