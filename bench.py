@@ -413,7 +413,10 @@ def run_denoise(args):
     ref = cv.reference_image(s, W, H, list(C3_WINDOWS), D, spp=65536)
     s.render(W, H, SPP, D, seed=4242, want=())
     film = s.read(W, H)
-    den = dn.Denoiser(ctx)
+    # the network trained as configured (512 crops of 512^2 at 4 vs 4096 spp), and the
+    # multi-level one the time-to-RMSE path uses below 1024 spp
+    den = dn.Denoiser(ctx, weights=dn.C5_WEIGHTS, hq_weights=None)
+    den_multi = dn.Denoiser(ctx, hq_weights=None)
 
     def best_of(fn, k=3):
         fn()
@@ -430,6 +433,9 @@ def run_denoise(args):
     with ClockSampler(0) as clk:
         _, unet_ms = best_of(lambda: den.film(s, out=dev))
         unet = dev.cpu().numpy()
+        den_multi.film(s, out=dev)
+        torch.cuda.synchronize()
+        unet_multi = dev.cpu().numpy()
         mean_d = torch.from_numpy(film["mean"]).cuda()
         var_d = torch.from_numpy(film["var"]).cuda()
         nlm_d = torch.empty_like(mean_d)
@@ -438,7 +444,8 @@ def run_denoise(args):
     clocks = clk.summary()
     e = {"noisy": cv.corrected_rel_mse(film["mean"], ref),
          "nlm": cv.corrected_rel_mse(nlm, ref),
-         "unet": cv.corrected_rel_mse(unet, ref)}
+         "unet": cv.corrected_rel_mse(unet, ref),
+         "unet_multilevel": cv.corrected_rel_mse(unet_multi, ref)}
     peaks = measured_peaks_tensor()
     mirrors = den.mirrors
     achieved = mirrors * UNET_FWD_GFLOP_1080P / unet_ms  # GFLOP/ms = TFLOP/s
@@ -446,11 +453,13 @@ def run_denoise(args):
         "metric": "relMSE of the denoised 4-spp film (four 128x128 windows vs FP64 65,536 spp, reference noise "
                   "subtracted)",
         "value": e["unet"], "unit": "relMSE", "n_gpus": 1, "higher_is_better": False, "dtype": "bf16",
-        "data": "synthetic (the held-out heightfield scene generated on the host; weights trained on seeds 1-16)",
+        "data": "synthetic (the held-out heightfield scene generated on the host; weights trained on "
+                "renderer-generated pairs of other seeds)",
         "config": {"workload": "1920x1080 heightfield (seed 2026, held out), 4 spp, depth 12; U-Net over "
                                f"{mirrors} grid symmetries vs NLM 21x21/7x7", "windows": [list(c) for c in C3_WINDOWS],
                    "ref_spp": 65536, "ref_noise_rel_mse": ref["noise"]},
         "rel_mse": e, "unet_vs_nlm": e["nlm"] / e["unet"],
+        "training": {k: v for k, v in den.meta.items() if k != "scenes"},
         "unet_ms_per_frame": unet_ms, "nlm_ms_per_frame": nlm_ms,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": achieved / peaks["bf16_tflops"], "traffic": None,
@@ -461,6 +470,7 @@ def run_denoise(args):
     }
     print(json.dumps(line), flush=True)
     den.close()
+    den_multi.close()
     s.close()
     ctx.close()
 
@@ -567,15 +577,15 @@ def prof_render(spp: int, frames: int, width: int = 1920, height: int = 1080) ->
 
 
 def prof_wave_sweep(spp: int) -> dict:
-    """The 1080p heightfield at `spp` samples, depth 12, default launch shapes, for waves of
-    2^22 .. 2^27 paths: best of two renders each after an 8-spp warm-up."""
+    """The 1080p heightfield at `spp` samples, depth 12, default launch shapes, for queues of
+    2^20 .. 2^27 paths in flight: best of two renders each after an 8-spp warm-up."""
     from salty_gb300 import Context, scenes
     ctx = Context(0)
     s = scenes.upload(ctx, scenes.heightfield())
     s.build()
     base = ctx.tuning
     res = []
-    for e in range(22, 28):
+    for e in range(20, 28):
         t = dict(base)
         t["wave_paths"] = 1 << e
         ctx.tuning = t

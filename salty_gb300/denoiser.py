@@ -29,6 +29,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_WEIGHTS = os.path.join(HERE, "weights", "unet_heightfield.npz")
 # the same network trained only on inputs of >= 1024 samples per pixel
 DEFAULT_HQ_WEIGHTS = os.path.join(HERE, "weights", "unet_heightfield_hq.npz")
+# trained as the learned-denoiser configuration asks: 512 crops of 512 x 512 pixels (32
+# seeded heightfield scenes x 16 views, directional sun) at 4 vs 4096 samples per pixel
+C5_WEIGHTS = os.path.join(HERE, "weights", "unet_c5.npz")
 
 FRAME = (1920, 1080)
 MAX_DEPTH = 12
