@@ -9,6 +9,9 @@
  *                        (src/s3d_materialfactory.cpp:28-132), PinholeCamera::Update
  *                        (include/s3d_camera.h:63-90), Scene members
  *                        (include/s3d_scene.h:98-103)
+ *   salty_scene_set_instances  Instance (src/s3d_instance.cpp:22-101)
+ *   salty_scene_set_spheres    Sphere (src/s3d_sphere.cpp:22-115), Scene::GetLight
+ *                        (include/s3d_scene.h:84-90)
  *   salty_bvh_build      BVH8::Create / SplitSAH (src/s3d_bvh8.cpp:254-342,401-479)
  *   salty_trace          Scene::Intersect -> BVH8::IsHit -> Triangle::IsHit
  *                        (include/s3d_scene.h:63-75, src/s3d_bvh8.cpp:191-206,
@@ -59,7 +62,9 @@ void salty_ctx_destroy(salty_ctx* ctx);
 /* Last error text of this context ("" if none).  Valid until the next call. */
 const char* salty_last_error(const salty_ctx* ctx);
 int salty_abi_version(void);
-/* Requests that a running salty_render stop at the next sample boundary (any thread). */
+/* Requests that a running salty_render stop (any thread): the render returns
+ * SALTY_ERR_CANCELLED after its current graph launch, at most 256 iterations of the path
+ * loop. */
 void salty_ctx_cancel(salty_ctx* ctx);
 
 /* Page-locked host memory for fast copies (cudaHostAlloc). */
@@ -195,6 +200,27 @@ typedef struct salty_instance {
 salty_status salty_scene_set_instances(salty_ctx* ctx, salty_scene* scene, const salty_instance* instances,
                                        int32_t n);
 
+/* An analytic sphere (Sphere, src/s3d_sphere.cpp:22-115). */
+typedef struct salty_sphere {
+    float center[3];
+    float radius;       /* > 0 */
+    int32_t material;   /* index into the scene's material table */
+    int32_t light;      /* nonzero: also a light of the scene, sampled by next-event estimation
+                         * with its material's emission */
+} salty_sphere;
+
+/* Sphere shapes of the scene, in the same BVH as its triangles: hits report id n_tris + k
+ * for sphere k (n_tris counting the area light's two triangles), t as for triangles and
+ * u = v = 0.  Spheres marked as lights join the light list after the area light, in input
+ * order; next-event estimation picks one light uniformly (Scene::GetLight,
+ * include/s3d_scene.h:84-90), in the compat profile with Sphere::Sample's point on the
+ * radius + 0.1 sphere and pdf 1/(4 pi r^2) (src/s3d_sphere.cpp:106-115), in the physical
+ * profile with a direction uniform in the cone the sphere subtends, combined with BSDF
+ * sampling by MIS.  Call after salty_scene_upload and before salty_bvh_build; n = 0 removes
+ * them.  Not combined with instances; sphere scenes render through salty_render (not
+ * salty_render_batch).  spheres: host array. */
+salty_status salty_scene_set_spheres(salty_ctx* ctx, salty_scene* scene, const salty_sphere* spheres, int32_t n);
+
 /* ---------------------------------------------------------------- BVH */
 typedef struct salty_build_opts {
     int32_t bins;          /* SAH bins per axis, 8..32 (default 32) */
@@ -300,9 +326,11 @@ typedef struct salty_tuning {
     int32_t trace_postpone;  /* fewest lanes that test a triangle group together, 1..32 */
     int32_t shade_block;     /* shading threads per block, a multiple of 32 in 64..1024 */
     int32_t trace_regs;      /* traversal registers per thread: 64, or 48 (more resident warps) */
-    int64_t wave_paths;      /* paths in flight per wave (queue capacity), 2^16..2^27; default
-                              * 2^26 (about 23 GB of path state for a render of that many
-                              * samples or more; smaller renders allocate what they use) */
+    int64_t wave_paths;      /* paths in flight (queue capacity), 2^16..2^27; default 2^24
+                              * (352 bytes of path state per path plus per-sample buffers of
+                              * up to 7x as many samples at 48 bytes: about 11 GB for a
+                              * depth-12 render of that many samples or more; smaller renders
+                              * allocate what they use) */
 } salty_tuning;
 salty_status salty_get_tuning(salty_ctx* ctx, salty_tuning* out);
 salty_status salty_set_tuning(salty_ctx* ctx, const salty_tuning* t);

@@ -76,7 +76,7 @@ class _Scene(C.Structure):
                 ("cam_pos", C.c_float * 3), ("cam_target", C.c_float * 3), ("cam_up", C.c_float * 3),
                 ("cam_fov", C.c_float), ("cam_near", C.c_float), ("cam_lens", C.c_float), ("cam_focal", C.c_float),
                 ("tri_uv", C.c_void_p), ("textures", C.c_void_p), ("n_textures", C.c_int), ("ibl_map", C.c_int),
-                ("ibl_scale", C.c_float)]
+                ("ibl_scale", C.c_float), ("spheres", C.c_void_p), ("n_spheres", C.c_long)]
 
 
 class _Opts(C.Structure):
@@ -99,7 +99,7 @@ class _RefScene(C.Structure):
                 ("cam_target", C.c_float * 3), ("cam_up", C.c_float * 3),
                 ("cam_fov", C.c_float), ("cam_near", C.c_float), ("sky_over_10", C.c_float),
                 ("tmp_dir", C.c_char_p), ("cam_lens", C.c_float), ("tri_uv", C.c_void_p), ("textures", C.c_void_p),
-                ("n_textures", C.c_int), ("ibl_map", C.c_int)]
+                ("n_textures", C.c_int), ("ibl_map", C.c_int), ("spheres", C.c_void_p), ("n_spheres", C.c_int)]
 
 
 def _f3(v):
@@ -121,6 +121,18 @@ class SceneData:
     textures: list = field(default_factory=list)  # (H, W, 3) float32 images
     ibl: int | None = None              # texture index of the environment map
     ibl_scale: float = 10.0
+    spheres: list = field(default_factory=list)  # dicts: center, radius, material, light
+
+
+def _sphere_array(spheres) -> np.ndarray:
+    """(n, 6) float32: centre xyz, radius, material, light (0/1)."""
+    a = np.zeros((max(1, len(spheres)), 6), np.float32)
+    for i, sp in enumerate(spheres):
+        a[i, 0:3] = sp["center"]
+        a[i, 3] = sp["radius"]
+        a[i, 4] = sp.get("material", 0)
+        a[i, 5] = 1.0 if sp.get("light") else 0.0
+    return a
 
 
 class RefBVH:
@@ -250,6 +262,10 @@ class Oracle:
         s.n_tris = pos.shape[0]
         s.mats = C.addressof(mats)
         s.n_mats = len(sc.materials)
+        if sc.spheres:
+            sph = _sphere_array(sc.spheres)
+            keep.append(sph)
+            s.spheres, s.n_spheres = sph.ctypes.data, len(sc.spheres)
         if sc.light:
             s.has_light = 1
             s.light_corner = _f3(sc.light["corner"])
@@ -403,6 +419,10 @@ class Reference:
             uv = np.ascontiguousarray(sc.tri_uv, np.float32)
             keep.append(uv)
             s.tri_uv = uv.ctypes.data
+        if sc.spheres:
+            sph = _sphere_array(sc.spheres)
+            keep.append(sph)
+            s.spheres, s.n_spheres = sph.ctypes.data, len(sc.spheres)
         h = self.L.sref_scene_create(C.byref(s), width, height)
         try:
             total = np.zeros((height, width, 3), np.float64)

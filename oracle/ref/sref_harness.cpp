@@ -41,6 +41,7 @@
 #include <s3d_shape.h>
 #include <s3d_material.h>
 #include <s3d_triangle.h>
+#include <s3d_sphere.h>
 #include <s3d_bvh8.h>
 #include <s3d_mesh.h>
 #include <s3d_lambert.h>
@@ -185,6 +186,8 @@ struct sref_scene_desc {
     const sref_texture* textures;
     int n_textures;
     int ibl_map;             // 1 + texture index of the environment (replaces the constant sky), 0 = none
+    const float* spheres;    // n_spheres * 6: centre xyz, radius, material, light (0/1)
+    int n_spheres;
 };
 
 // ---------------------------------------------------------------- traversal
@@ -324,6 +327,14 @@ void* sref_scene_create(const sref_scene_desc* d, int width, int height) {
         auto* q = new QuadLight(v3(d->light_corner), v3(d->light_edge_a), v3(d->light_edge_b), lm);
         sc.m_Shapes.push_back(q);
         sc.m_pLightList.push_back(q);
+    }
+    // the reference's own Sphere shape (src/s3d_sphere.cpp); light spheres join the light
+    // list after the quad light, in input order
+    for (int k = 0; k < d->n_spheres; ++k) {
+        const float* p = d->spheres + 6 * k;
+        IShape* sp = Sphere::Create(p[3], Vector3(p[0], p[1], p[2]), sc.mats[(int)p[4]]);
+        sc.m_Shapes.push_back(sp);
+        if (p[5] != 0.0f) sc.m_pLightList.push_back(sp);
     }
     sc.camera.Update(v3(d->cam_pos), v3(d->cam_target), v3(d->cam_up), d->cam_fov,
                      float(width) / float(height), d->cam_near);

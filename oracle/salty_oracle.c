@@ -753,6 +753,12 @@ typedef struct {
     v3 sun_dir, sun_t, sun_b, sun_L;
     int sun_disk;
     float sun_cos_max, sun_pdf;
+    /* spheres (Sphere, src/s3d_sphere.cpp): ids sph_base + k; the light list is the quad
+       light (if any) and then the light spheres in input order */
+    const float* sph;
+    long n_sph, sph_base;
+    int* light_sph;
+    int n_light_sph, n_lights;
 } rscene;
 
 /* PinholeCamera::Update (include/s3d_camera.h:63-90) */
@@ -842,6 +848,13 @@ static void rscene_init(rscene* r, const oracle_scene* sc) {
         }
     }
     r->bvh = (obvh*)oracle_bvh_create(r->pos, n);
+    r->sph = sc->spheres;
+    r->n_sph = sc->spheres ? sc->n_spheres : 0;
+    r->sph_base = n;
+    r->light_sph = (int*)malloc(sizeof(int) * (r->n_sph ? r->n_sph : 1));
+    for (long k = 0; k < r->n_sph; ++k)
+        if (r->sph[k * 6 + 5] != 0.0f) r->light_sph[r->n_light_sph++] = (int)k;
+    r->n_lights = (sc->has_light ? 1 : 0) + r->n_light_sph;
     if (sc->has_sun) {
         r->sun_dir = unit(ld3(sc->sun_dir));
         r->sun_disk = sc->sun_half_angle > 0.0f;
@@ -861,7 +874,7 @@ static void rscene_init(rscene* r, const oracle_scene* sc) {
 
 static void rscene_free(rscene* r) {
     oracle_bvh_destroy(r->bvh);
-    free(r->pos); free(r->nrm); free(r->mat); free(r->mats);
+    free(r->pos); free(r->nrm); free(r->mat); free(r->mats); free(r->light_sph);
 }
 
 static int is_light_tri(const rscene* r, int id) {
@@ -927,14 +940,90 @@ static v3 geometric_normal(const rscene* r, int id) {
     return safe_unit(cross(sub(ld3(p + 3), ld3(p)), sub(ld3(p + 6), ld3(p))));
 }
 
+/* Sphere::IsHit (src/s3d_sphere.cpp:66-92) with the reference's operation order: the
+ * nearer root above tmin, else the farther. */
+static int sph_ref(const float* c, v3 o, v3 d, float tmin, float tmax, float* t) {
+    v3 po = sub(ld3(c), o);
+    float b = dot(po, d);
+    float D4 = b * b - dot(po, po) + c[3] * c[3];
+    if (D4 < 0.0f) return 0;
+    float sq = sqrtf(D4), t1 = b - sq, t2 = b + sq;
+    if (t1 < tmin && t2 < tmin) return 0;
+    *t = t1 > tmin ? t1 : t2;
+    return *t <= tmax;
+}
+/* the same in double precision (physical profile): smallest root in [tmin, tmax] */
+static int sph_exact(const float* c, v3 o, v3 d, float tmin, float tmax, float* t) {
+    double f[3] = {(double)o.x - c[0], (double)o.y - c[1], (double)o.z - c[2]};
+    double dd[3] = {d.x, d.y, d.z};
+    double a = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
+    double b = -(f[0] * dd[0] + f[1] * dd[1] + f[2] * dd[2]);
+    double cc = f[0] * f[0] + f[1] * f[1] + f[2] * f[2] - (double)c[3] * c[3];
+    double disc = b * b - a * cc;
+    if (disc < 0.0) return 0;
+    double sq = sqrt(disc), t0 = (b - sq) / a, t1 = (b + sq) / a;
+    double tt = t0 >= tmin ? t0 : t1;
+    if (!(tt >= tmin) || tt > tmax) return 0;
+    *t = (float)tt;
+    return 1;
+}
+
+/* closest hit over the triangles' BVH and then every sphere (equal t: the lower id) */
 static int closest(const rscene* r, v3 o, v3 d, float tmin, float tmax, int mode, ohit* h) {
     float of[3] = {o.x, o.y, o.z}, df[3] = {d.x, d.y, d.z};
-    return obvh_trace_one(r->bvh, of, df, tmin, tmax, mode, 0, 1e-3, h);
+    int hit = obvh_trace_one(r->bvh, of, df, tmin, tmax, mode, 0, 1e-3, h);
+    for (long k = 0; k < r->n_sph; ++k) {
+        float t;
+        const float* c = r->sph + k * 6;
+        int ok = mode == 0 ? sph_ref(c, o, d, tmin, tmax, &t) : sph_exact(c, o, d, tmin, tmax, &t);
+        if (ok && (!hit || t < h->t)) {
+            hit = 1;
+            h->t = t; h->u = 0.0f; h->v = 0.0f; h->id = (int)(r->sph_base + k);
+        }
+    }
+    return hit;
 }
 static int occluded(const rscene* r, v3 o, v3 d, float tmin, float tmax) {
     float of[3] = {o.x, o.y, o.z}, df[3] = {d.x, d.y, d.z};
     ohit h;
-    return obvh_trace_one(r->bvh, of, df, tmin, tmax, 1, 1, 1e-3, &h);
+    if (obvh_trace_one(r->bvh, of, df, tmin, tmax, 1, 1, 1e-3, &h)) return 1;
+    for (long k = 0; k < r->n_sph; ++k) {
+        float t;
+        if (sph_exact(r->sph + k * 6, o, d, tmin, tmax, &t)) return 1;
+    }
+    return 0;
+}
+
+/* solid-angle pdf of a direction uniform in the cone sphere c subtends from x: 1 / (2 pi
+ * (1 - cos theta_max)), 0 from inside */
+static float sph_cone_pdf(const float* c, v3 x) {
+    v3 w = sub(ld3(c), x);
+    float d2 = dot(w, w), r2 = c[3] * c[3];
+    if (!(d2 > r2)) return 0.0f;
+    float s2 = r2 / d2, cm = sqrtf(fmaxf(0.0f, 1.0f - s2));
+    return 1.0f / (6.283185307179586476925286766559f * (s2 / (1.0f + cm)));
+}
+
+/* ---- what shading needs of a hit: material, normal, texture coordinate ---- */
+static int is_sph(const rscene* r, int id) { return r->n_sph > 0 && id >= r->sph_base; }
+static const oracle_material* hit_mat(const rscene* r, int id) {
+    if (is_sph(r, id)) return &r->mats[(int)r->sph[(id - r->sph_base) * 6 + 4]];
+    return &r->mats[r->mat[id]];
+}
+/* Sphere::CalcParam (src/s3d_sphere.cpp:94-104): outward normal, (phi/2pi, (pi-theta)/pi) */
+static v3 sph_normal(const rscene* r, int id, v3 p) {
+    return safe_unit(sub(p, ld3(r->sph + (id - r->sph_base) * 6)));
+}
+
+static v3 hit_color_map(const rscene* r, const oracle_material* m, int id, float b1, float b2, v3 p) {
+    if (!is_sph(r, id)) return color_map(r, m, id, b1, b2);
+    if (m->color_map <= 0) return mk(1.0f, 1.0f, 1.0f);
+    v3 n = sph_normal(r, id, p);
+    float theta = acosf(fminf(1.0f, fmaxf(-1.0f, n.y)));
+    float phi = atan2f(n.x, n.z);
+    if (phi < 0.0f) phi += 6.283185307179586476925286766559f;
+    return tex_sample(&r->sc->textures[m->color_map - 1], phi * (1.0f / 6.283185307179586476925286766559f),
+                      (3.1415926535897932384626433832795f - theta) * (1.0f / 3.1415926535897932384626433832795f));
 }
 
 /* ---- compat profile: PathTracer::Radiance / NextEventEstimation (src/s3d_pt.cpp:182-292) */
@@ -943,22 +1032,41 @@ static const float k2Pi = 6.283185307179586476925286766559f;
 static const float kFHitMin = 1e-3f, kFHitMax = 1e12f;
 
 static v3 compat_nee(const rscene* r, v3 pos, v3 n, const oracle_material* m, opcg* rnd) {
-    (void)opcg_u32(rnd) ;                   /* Scene::GetLight: u32 % 1 light (include/s3d_scene.h:84-90) */
-    float u = opcg_f32(rnd), w = opcg_f32(rnd);
-    v3 lp = add(add(r->lc, scl(r->la, u)), scl(r->lb, w));
-    float pdf = 1.0f / r->larea;
+    /* Scene::GetLight (include/s3d_scene.h:84-90): u32 % (number of lights) */
+    int li = (int)(opcg_u32(rnd) % (uint32_t)r->n_lights);
+    v3 lp; float pdf; long want;  /* the light's point and pdf, and the id range it covers */
+    const float* sp = NULL;
+    if (li < r->sc->has_light) {
+        float u = opcg_f32(rnd), w = opcg_f32(rnd);
+        lp = add(add(r->lc, scl(r->la, u)), scl(r->lb, w));
+        pdf = 1.0f / r->larea;
+        want = -1;
+    } else {
+        /* Sphere::Sample (src/s3d_sphere.cpp:106-115): a point on the radius + 0.1 sphere */
+        int k = r->light_sph[li - r->sc->has_light];
+        sp = r->sph + k * 6;
+        float r1 = k2Pi * opcg_f32(rnd);
+        float r2 = 1.0f - 2.0f * opcg_f32(rnd);
+        float r3 = sqrtf(1.0f - r2 * r2);
+        lp = add(ld3(sp), scl(safe_unit(mk(r3 * cosf(r1), r3 * sinf(r1), r2)), sp[3] + 1e-1f));
+        pdf = 1.0f / (4.0f * kPi * sp[3] * sp[3]);
+        want = r->sph_base + k;
+    }
     v3 ld = sub(lp, pos);
     float dist2 = dot(ld, ld);
     ld = safe_unit(ld);
     ohit h;
-    if (closest(r, pos, ld, kFHitMin, kFHitMax, 0, &h) && is_light_tri(r, h.id)) {
+    /* accepted when the first hit is the sampled light (src/s3d_pt.cpp:274) */
+    if (closest(r, pos, ld, kFHitMin, kFHitMax, 0, &h) && (want < 0 ? is_light_tri(r, h.id) : h.id == want)) {
+        v3 hp = add(pos, scl(ld, h.t));
+        v3 ln = want < 0 ? r->ln : sph_normal(r, h.id, hp);
         float cos_s = fabsf(dot(n, ld));
-        float cos_l = fabsf(dot(r->ln, neg(ld)));
+        float cos_l = fabsf(dot(ln, neg(ld)));
         v3 fs = mk(m->color[0] / kPi, m->color[1] / kPi, m->color[2] / kPi);
         float G = (cos_s * cos_l) / dist2;
         float brdf_pdf = fabsf(ld.z / kPi) * cos_l / dist2;
         float mis = pdf / (brdf_pdf + pdf);
-        v3 le = ld3(r->mats[r->mat[h.id]].emission);
+        v3 le = ld3(hit_mat(r, h.id)->emission);
         return scl(scl(mul(le, fs), mis), G / pdf);
     }
     return mk(0, 0, 0);
@@ -1073,16 +1181,16 @@ static v3 compat_radiance(const rscene* r, v3 o, v3 d, int max_bounce, opcg* rnd
             break;
         }
         v3 pos = add(o, scl(d, h.t));
-        const oracle_material* m = &r->mats[r->mat[h.id]];
+        const oracle_material* m = hit_mat(r, h.id);
         L = add(L, mul(W, ld3(m->emission)));
-        v3 n = shading_normal(r, h.id, h.u, h.v);
+        v3 n = is_sph(r, h.id) ? sph_normal(r, h.id, pos) : shading_normal(r, h.id, h.u, h.v);
         /* TexturedMaterial (src/s3d_texturedmaterial.cpp:63-87): the map scales the NEE base
          * colour and the Shade weight */
-        v3 tx = color_map(r, m, h.id, h.u, h.v);
+        v3 tx = hit_color_map(r, m, h.id, h.u, h.v, pos);
         oracle_material mt = *m;
         for (int c = 0; c < 3; ++c) mt.color[c] *= (c == 0 ? tx.x : c == 1 ? tx.y : tx.z);
         int delta = (m->type == ORACLE_MIRROR || m->type == ORACLE_GLASS);
-        if (!delta && r->sc->has_light) L = add(L, mul(W, compat_nee(r, pos, n, &mt, rnd)));
+        if (!delta && r->n_lights > 0 && !is_light_tri(r, h.id)) L = add(L, mul(W, compat_nee(r, pos, n, &mt, rnd)));
         v3 out; int dice = 0;
         W = mul(W, mul(compat_shade(m, d, n, rnd, &out, &dice), tx));
         if (dice) break;
@@ -1206,29 +1314,42 @@ static v3 phys_radiance(const rscene* r, v3 o, v3 d, const oracle_render_opts* o
             if (cos_l > 0.0f) {
                 if (prev_delta) L = add(L, mul(W, r->le));
                 else {
-                    float pdf_l = (h.t * h.t) / (cos_l * r->larea);
+                    float pdf_l = (h.t * h.t) / (cos_l * r->larea * (float)r->n_lights);
                     float mis = prev_pdf / (prev_pdf + pdf_l);
                     L = add(L, scl(mul(W, r->le), mis));
                 }
             }
             break;
         }
-        oracle_material mtex = r->mats[r->mat[h.id]];
+        oracle_material mtex = *hit_mat(r, h.id);
         {   /* the colour map scales the base colour */
-            v3 tx = color_map(r, &mtex, h.id, h.u, h.v);
+            v3 tx = hit_color_map(r, &mtex, h.id, h.u, h.v, p);
             mtex.color[0] *= tx.x; mtex.color[1] *= tx.y; mtex.color[2] *= tx.z;
         }
         const oracle_material* m = &mtex;
-        L = add(L, mul(W, ld3(m->emission)));
-        v3 ng = geometric_normal(r, h.id);
+        const int hs = is_sph(r, h.id) ? (int)(h.id - r->sph_base) : -1;
+        if (hs >= 0 && r->sph[hs * 6 + 5] != 0.0f && !prev_delta) {
+            /* a light sphere reached by BSDF sampling: MIS against its cone sampling */
+            float pdf_l = sph_cone_pdf(r->sph + hs * 6, o) / (float)r->n_lights;
+            L = add(L, scl(mul(W, ld3(m->emission)), prev_pdf / (prev_pdf + pdf_l)));
+        } else {
+            L = add(L, mul(W, ld3(m->emission)));
+        }
+        v3 ng = hs >= 0 ? sph_normal(r, h.id, p) : geometric_normal(r, h.id);
         int into = dot(ng, d) < 0.0f;
         v3 ngf = into ? ng : neg(ng);
-        v3 ns = shading_normal(r, h.id, h.u, h.v);
+        v3 ns = hs >= 0 ? ng : shading_normal(r, h.id, h.u, h.v);
         v3 nsf = (dot(ns, d) < 0.0f) ? ns : neg(ns);
         v3 wo = neg(d);
         int delta = (m->type == ORACLE_MIRROR || m->type == ORACLE_GLASS);
         if (!delta) {
-            if (sc->has_light) {
+            int li = 0;
+            if (r->n_lights > 1) {  /* one light of the list, uniformly */
+                li = (int)(opcg_f32(rnd) * (float)r->n_lights);
+                if (li > r->n_lights - 1) li = r->n_lights - 1;
+            }
+            float psel = r->n_lights > 0 ? 1.0f / (float)r->n_lights : 0.0f;
+            if (r->n_lights > 0 && li < sc->has_light) {
                 float u1 = opcg_f32(rnd), u2 = opcg_f32(rnd);
                 v3 lp = add(add(r->lc, scl(r->la, u1)), scl(r->lb, u2));
                 v3 wi = sub(lp, p);
@@ -1240,9 +1361,47 @@ static v3 phys_radiance(const rscene* r, v3 o, v3 d, const oracle_render_opts* o
                     !occluded(r, spawn(p, ng, wi), wi, 0.0f, dist * (1.0f - 1e-4f))) {
                     float pdf_b;
                     v3 f = phys_eval(m, nsf, wo, wi, &pdf_b);
-                    float pdf_l = dist2 / (cos_l * r->larea);
+                    float pdf_l = psel * dist2 / (cos_l * r->larea);
                     float mis = pdf_l / (pdf_l + pdf_b);
                     L = add(L, scl(mul(mul(W, f), r->le), cos_s * mis / pdf_l));
+                }
+            } else if (r->n_lights > 0) {
+                /* a direction uniform in the cone the light sphere subtends from p */
+                const float* sp = r->sph + r->light_sph[li - sc->has_light] * 6;
+                float u1 = opcg_f32(rnd), u2 = opcg_f32(rnd);
+                float pdf_c = sph_cone_pdf(sp, p);
+                if (pdf_c > 0.0f) {
+                    v3 w = sub(ld3(sp), p);
+                    float dc = sqrtf(dot(w, w));
+                    v3 wz = scl(w, 1.0f / dc);
+                    float cos_max = sqrtf(fmaxf(0.0f, 1.0f - sp[3] * sp[3] / (dc * dc)));
+                    float one_m = (1.0f - cos_max) * u1, ct = 1.0f - one_m;
+                    float st = sqrtf(fmaxf(0.0f, one_m * (2.0f - one_m)));
+                    v3 tx_, ty_;
+                    tangent_space(wz, &tx_, &ty_);
+                    v3 wi = safe_unit(add(add(scl(tx_, st * cosf(k2Pi * u2)), scl(ty_, st * sinf(k2Pi * u2))),
+                                          scl(wz, ct)));
+                    /* near intersection (dc^2 - r^2) / (dc cos + sqrt(r^2 - dc^2 sin^2)):
+                       no cancellation at the cone's edge */
+                    float dist = (dc * dc - sp[3] * sp[3]) /
+                                 (dc * ct + sqrtf(fmaxf(0.0f, sp[3] * sp[3] - dc * dc * st * st)));
+                    float cos_s = dot(nsf, wi), cos_g = dot(ngf, wi);
+                    /* the shadow ray runs from the light point back to the surface: from
+                       just outside the sphere it cannot meet the sphere itself, which a ray
+                       towards a grazing point on its silhouette could, by rounding */
+                    v3 q = add(p, scl(wi, dist));
+                    v3 qs = spawn(q, safe_unit(sub(q, ld3(sp))), neg(wi)), ps = spawn(p, ng, wi);
+                    v3 back = sub(ps, qs);
+                    float blen = sqrtf(dot(back, back));
+                    if (cos_s > 0.0f && cos_g > 0.0f && dist > 0.0f &&
+                        !occluded(r, qs, scl(back, 1.0f / blen), 0.0f, blen * (1.0f - 1e-4f))) {
+                        float pdf_b;
+                        v3 f = phys_eval(m, nsf, wo, wi, &pdf_b);
+                        float pdf_l = psel * pdf_c;
+                        float mis = pdf_l / (pdf_l + pdf_b);
+                        v3 le = ld3(r->mats[(int)sp[4]].emission);
+                        L = add(L, scl(mul(mul(W, f), le), cos_s * mis / pdf_l));
+                    }
                 }
             }
             if (sc->has_sun) {

@@ -99,6 +99,8 @@ typedef struct {
     int          n_textures;
     int          ibl_map;           /* 1 + texture index of the environment, 0 = constant sky */
     float        ibl_scale;
+    const float* spheres;           /* n_spheres * 6: centre xyz, radius, material, light (0/1) */
+    long         n_spheres;
 } oracle_scene;
 
 typedef struct {

@@ -71,6 +71,10 @@ class Instance(C.Structure):
     _fields_ = [("first_tri", C.c_int64), ("n_tris", C.c_int64), ("object_to_world", C.c_float * 12)]
 
 
+class Sphere(C.Structure):
+    _fields_ = [("center", C.c_float * 3), ("radius", C.c_float), ("material", C.c_int32), ("light", C.c_int32)]
+
+
 class BuildOpts(C.Structure):
     _fields_ = [("bins", C.c_int32), ("max_leaf", C.c_int32), ("trav_cost", C.c_float)]
 
@@ -123,7 +127,7 @@ EXPORTS = ["salty_ctx_create", "salty_ctx_destroy", "salty_last_error", "salty_a
            "salty_get_tuning", "salty_set_tuning", "salty_autotune", "salty_mesh_load_smd", "salty_mesh_free",
            "salty_mesh_transform", "salty_autotune_trace", "salty_denoise_unet_ensemble", "salty_film_checkpoint",
            "salty_film_restore", "salty_unet_get_adam", "salty_unet_set_adam", "salty_unet_set_conv_kernel",
-           "salty_scene_set_instances"]
+           "salty_scene_set_instances", "salty_scene_set_spheres"]
 
 _lib = None
 
@@ -149,6 +153,7 @@ def lib() -> C.CDLL:
         "salty_scene_destroy": (None, [vp, vp]),
         "salty_scene_set_camera": (i32, [vp, vp, C.POINTER(Camera)]),
         "salty_scene_set_instances": (i32, [vp, vp, vp, C.c_int32]),
+        "salty_scene_set_spheres": (i32, [vp, vp, vp, C.c_int32]),
         "salty_bvh_build": (i32, [vp, vp, C.POINTER(BuildOpts), C.POINTER(BvhInfo)]),
         "salty_trace": (i32, [vp, vp, vp, i64, u32, vp]),
         "salty_last_trace_stats": (i32, [vp, C.POINTER(TraceStats)]),
@@ -571,6 +576,18 @@ class Scene:
             arr[i].object_to_world = (C.c_float * 12)(*np.asarray(m, np.float32).reshape(12).tolist())
         self.ctx.check(lib().salty_scene_set_instances(self.ctx.h, self.h, C.byref(arr), len(instances)),
                        "scene_set_instances")
+
+    def set_spheres(self, spheres) -> None:
+        """salty_scene_set_spheres: sphere shapes, each a dict with center, radius, material
+        and optionally light (a light of the scene); build afterwards."""
+        arr = (Sphere * max(1, len(spheres)))()
+        for i, sp in enumerate(spheres):
+            arr[i].center = _f3(sp["center"])
+            arr[i].radius = float(sp["radius"])
+            arr[i].material = int(sp.get("material", 0))
+            arr[i].light = int(bool(sp.get("light", False)))
+        self.ctx.check(lib().salty_scene_set_spheres(self.ctx.h, self.h, C.byref(arr), len(spheres)),
+                       "scene_set_spheres")
 
     def aov(self, width: int, height: int) -> dict:
         """Mean first-hit features of the film: albedo, normal (H, W, 3), depth = 1/(1+t) (H, W)."""

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "lib", "obj")
 LIB = os.path.join(HERE, "lib", "libsalty_gpu.so")
 
-SOURCES = ["capi.cu", "bvh_build.cu", "instance.cu", "trace.cu", "render.cu", "post.cu", "unet.cu", "conv_tc.cu",
+SOURCES = ["capi.cu", "bvh_build.cu", "instance.cu", "sphere.cu", "trace.cu", "render.cu", "post.cu", "unet.cu", "conv_tc.cu",
            "smd.cpp"]
 HEADERS = ["internal.h", "traverse.cuh", "unet_src.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

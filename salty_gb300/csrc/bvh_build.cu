@@ -677,6 +677,7 @@ inline unsigned grid_for(long long n, int block) { return (unsigned)((n + block 
 
 salty_status build_bvh(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& opts) {
     if (sc->n_inst > 0) return build_instanced(ctx, sc, opts);
+    if (sc->n_sph > 0) return build_with_spheres(ctx, sc, opts);
     if (sc->n_tris <= 0) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "scene has no triangles");
     if (sc->n_tris > (int64_t)0x3fffffff)
         return ctx->err.fail(SALTY_ERR_CAPACITY, "too many triangles (%lld)", (long long)sc->n_tris);

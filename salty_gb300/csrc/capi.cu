@@ -231,6 +231,8 @@ salty_status salty_scene_upload(salty_ctx* ctx, const salty_scene_desc* d, salty
     SceneConsts& k = sc->consts;
     std::memset(&k, 0, sizeof(k));
     k.light_tri0 = -1;
+    k.sph_base = kNoSpheres;
+    k.n_lights = d->has_light ? 1 : 0;
     if (d->has_light) {
         // the light: a black Lambert emitter (two-sided in the compat profile)
         GpuMaterial lm{};

@@ -511,35 +511,45 @@ EncodeTiledFn tensor_map_encoder() {
 }
 
 // ---------------------------------------------------------------- weight gradient
-// dW[tap][co][ci] = sum over pixels p of dY[p][co] * X[p + d(tap)][ci], as a GEMM on the
-// tensor cores with the pixels as its K dimension:
-//   M = rows (tap, ci) of an implicit im2col of X, tap-major (row = tap * cin + ci), in
-//       tiles of 128 rows; a CTA owns `mt` (1 or 2) consecutive tiles (its group)
-//   N = output channels, padded to 16 (mt * cpad <= 512 TMEM columns)
-//   K = pixels, a strip of 64 consecutive pixels of one image row per stage (4 MMAs of 16)
-// Both operands are staged as "planes" of 64 pixels x 8 channels (one 16-byte row per
-// pixel, 1 KB), which is the tensor core's MN-major layout without swizzle: core matrices
-// of 8 pixels (K) x 8 channels (M or N), K-blocks 128 bytes apart (leading byte offset),
-// M/N blocks one plane apart (stride byte offset).  A plane is one TMA box of 8 channels x
-// 64 pixels x 1 row: for A, channels 8o..8o+7 of X at the strip's pixels shifted by the
-// plane's tap (the copy engine fills the image border with zeros), for B, channels
-// 8o..8o+7 of dY.  CTAs of a group split the strips between them (K-split): each writes
-// its partial sums to its own slice of a workspace, and k_wgrad_reduce adds the slices in
-// order -- the result does not depend on scheduling, unlike atomics.
+// dW[tap][co][ci] = sum over pixels p of dY[p][co] * X[p + d(tap)][ci]: per tap a GEMM on
+// the tensor cores with the pixels as its K dimension,
+//   M = output channels (dY transposed; 128 rows, of which cout are real),
+//   N = a chunk of up to 48 input channels (a CTA group's share), one accumulator of N
+//       TMEM columns per tap (9 x 48 <= 512),
+//   K = pixels: a strip of kWgRows image rows x 64 pixels per stage, 16 per MMA.
+// A stage holds the strip's dY (boxes of 16 channels x 64 pixels x kWgRows rows) and the
+// input's halo (boxes of 16 channels x 66 pixels x kWgRows + 2 rows), both copied by TMA in
+// the 32-byte swizzle, which is the tensor core's MN-major layout: one 32-byte row (16
+// channels) per pixel, 8-pixel groups 256 bytes apart (stride byte offset), the next 16
+// channels one box further (leading byte offset).  A tap's B operand is the same halo with
+// its start moved to row r + ky, pixel kx -- the copy engine has zero-filled the image
+// border -- so the input is read once per strip, not once per tap.  CTAs of a group split
+// the strips between them (K-split): each writes its partial sums to its own slice of a
+// workspace, and k_wgrad_reduce adds the slices in order -- the result does not depend on
+// scheduling, unlike atomics.
 //
-// Warp roles: one lane of warp 0 issues the TMA copies of a strip into a ring of kWgStages
-// buffers (a "full" barrier per buffer counts the bytes), one lane of warp 1 issues the
-// MMAs of a stage and commits them to the buffer's "empty" barrier, and after the last
-// stage to the accumulator barrier; then all four warps move the accumulators from TMEM
-// to this CTA's slice of partial sums.  Every wait is bounded.
+// Warp roles: one lane of warp 0 issues the TMA copies of each strip into a ring of
+// kWgStages buffers (a "full" barrier per buffer counts the bytes), one lane of warp 1
+// issues the MMAs and commits them to the buffer's "empty" barrier, and after the last
+// strip to the accumulator barrier; then all four warps move the accumulators from TMEM to
+// this CTA's slice.  Every wait is bounded.
 constexpr int kWgStrip = 64;
-constexpr int kWgPlane = kWgStrip * 16;
-constexpr int kWgMaxTiles = 2;
-constexpr int kWgStages = 4;
+constexpr int kWgRows = 2;
+constexpr int kWgHaloW = kWgStrip + 2;
+constexpr int kWgChunk = 48;
+constexpr int kWgStages = 3;
 constexpr int kWgThreads = 128;
-constexpr int kWgHeader = 256;  // barriers, TMEM address, abort flag, plane table
+constexpr int kWgHeader = 1024;
+constexpr int kWgDyBox = kWgRows * kWgStrip * 32;                                   // 16 channels
+constexpr int kWgXBox = ((kWgRows + 2) * kWgHaloW * 32 + 1023) / 1024 * 1024;  // 16 channels, padded
+constexpr int kWgStage = 8 * kWgDyBox + (kWgChunk / 16) * kWgXBox;  // dY sized for M = 128 rows
 
-__host__ __device__ constexpr int wg_stage_bytes(int mt, int cpad) { return (mt * 16 + cpad / 8) * kWgPlane; }
+// Descriptor of an MN-major operand in the 32-byte swizzle: 16-element atoms `lbo` bytes
+// apart, 8-row groups 256 bytes apart, layout type 6.
+__device__ __forceinline__ uint64_t sdesc_sw32_mn(uint32_t addr, uint32_t lbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)(256u >> 4) << 32) | (1ull << 46) | (6ull << 61);
+}
 
 // Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both MN-major
 // (transpose bits 15 and 16), N >> 3 at bit 17, M >> 4 at bit 24.
@@ -549,11 +559,9 @@ __device__ __forceinline__ uint32_t idesc_bf16_mn(int m, int n) {
 }
 
 struct WgradArgs {
-    int cpad, cin, N, H, W;
-    int rows;     // 9 * cin
-    int mt;       // M-tiles per group
-    int strips;   // N * H * ceil(W / kWgStrip)
-    float* part;  // [gridDim.x slices][rows][cpad]
+    int cpad, cout, cin, N, H, W;
+    int strips;   // N * ceil(H / kWgRows) * ceil(W / kWgStrip)
+    float* part;  // [gridDim.x slices][9][cpad][cin]
     int* status;
 };
 
@@ -563,21 +571,18 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUt
     uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kWgStages]
     uint64_t* empty = full + kWgStages;                  // [kWgStages]
     uint64_t* acc = empty + kWgStages;                   // [1]
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 96);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 100);
-    unsigned short* pinfo = reinterpret_cast<unsigned short*>(smem + 128);  // [32] plane -> tap, octet
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 128);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 132);
     unsigned char* stage0 = smem + kWgHeader;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    if (saddr(smem) & 1023u) {  // the descriptors below assume 1 KB aligned planes
+    if (saddr(smem) & 1023u) {  // the swizzled boxes need 1 KB aligned destinations
         if (tid == 0) atomicOr(a.status, 2);
         return;
     }
-    const int mt = a.mt, cpad = a.cpad;
-    const int sbytes = wg_stage_bytes(mt, cpad);
-    const int nplanes_a = mt * 16, nplanes_b = cpad / 8;
-    const int row0 = blockIdx.y * mt * 128;           // this group's first (tap, ci) row
-    const int oct = a.cin / 8;                         // channel octets of X
-    const int spr = (a.W + kWgStrip - 1) / kWgStrip;  // strips per image row
+    const int c0 = blockIdx.y * kWgChunk;                    // this group's input channels
+    const int ch = min(kWgChunk, a.cin - c0);               // 16, 32 or 48
+    const int ndy = a.cpad / 16, nx = ch / 16;
+    const int sx = (a.W + kWgStrip - 1) / kWgStrip, sy = (a.H + kWgRows - 1) / kWgRows;
     const int first = blockIdx.x;
     const int count = first < a.strips ? (a.strips - 1 - first) / (int)gridDim.x + 1 : 0;
 
@@ -589,10 +594,6 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUt
         mbar_init(saddr(acc), 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    if (tid < nplanes_a) {  // plane p of this group: ky | kx << 2 | octet << 4, or none
-        const int r8 = row0 / 8 + tid, tap = r8 / oct, o = r8 - tap * oct;
-        pinfo[tid] = tap < 9 ? (unsigned short)((tap / 3) | ((tap % 3) << 2) | (o << 4)) : (unsigned short)0xffffu;
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" :: "r"(saddr(tmem_slot)) : "memory");
@@ -607,9 +608,7 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUt
     if (warp == 0 && lane == 0) {
         asm volatile("prefetch.tensormap [%0];" :: "l"(reinterpret_cast<uint64_t>(&tm_x)) : "memory");
         asm volatile("prefetch.tensormap [%0];" :: "l"(reinterpret_cast<uint64_t>(&tm_dy)) : "memory");
-        int valid = 0;
-        for (int p = 0; p < nplanes_a; ++p) valid += pinfo[p] != 0xffffu;
-        const uint32_t tx = (uint32_t)(valid + nplanes_b) * kWgPlane;
+        const uint32_t tx = (uint32_t)ndy * kWgDyBox + (uint32_t)nx * ((kWgRows + 2) * kWgHaloW * 32);
         for (int it = 0; it < count; ++it) {
             const int b = it % kWgStages;
             if (!wait_or_abort(saddr(empty + b), ((uint32_t)(it / kWgStages) & 1u) ^ 1u, abort_flag, a.status)) {
@@ -617,22 +616,17 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUt
                 break;
             }
             const int s = first + it * (int)gridDim.x;
-            const int xs = s % spr, t = s / spr;
-            const int y = t % a.H, n = t / a.H;
+            const int xs = s % sx, t = s / sx;
+            const int y0 = (t % sy) * kWgRows, n = t / sy;
             const int x0 = xs * kWgStrip;
             const uint32_t bar = saddr(full + b);
             mbar_expect_tx(bar, tx);
-            const uint32_t as = saddr(stage0 + b * sbytes), bs = as + nplanes_a * kWgPlane;
-            for (int p = 0; p < nplanes_a; ++p) {
-                const unsigned info = pinfo[p];
-                if (info == 0xffffu) continue;
-                const int ky = info & 3, kx = (info >> 2) & 3, o = (int)(info >> 4) & 0xff;
-                tma_load_4d(as + p * kWgPlane, &tm_x, o * 8, x0 - 1 + kx, y - 1 + ky, n, bar);
-            }
-            for (int o = 0; o < nplanes_b; ++o) tma_load_4d(bs + o * kWgPlane, &tm_dy, o * 8, x0, y, n, bar);
+            const uint32_t dyb = saddr(stage0 + b * kWgStage), xb = dyb + 8 * kWgDyBox;
+            for (int k = 0; k < ndy; ++k) tma_load_4d(dyb + k * kWgDyBox, &tm_dy, k * 16, x0, y0, n, bar);
+            for (int k = 0; k < nx; ++k) tma_load_4d(xb + k * kWgXBox, &tm_x, c0 + k * 16, x0 - 1, y0 - 1, n, bar);
         }
     } else if (warp == 1 && lane == 0) {
-        const uint32_t idesc = idesc_bf16_mn(128, cpad);
+        const uint32_t idesc = idesc_bf16_mn(128, ch);
         for (int it = 0; it < count; ++it) {
             const int b = it % kWgStages;
             if (!wait_or_abort(saddr(full + b), (uint32_t)(it / kWgStages) & 1u, abort_flag, a.status)) {
@@ -640,38 +634,39 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUt
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t as = saddr(stage0 + b * sbytes), bs = as + nplanes_a * kWgPlane;
-            for (int k = 0; k < kWgStrip / 16; ++k) {
-                const uint64_t bd = sdesc(bs + k * 256, 128, kWgPlane);
-                for (int t = 0; t < mt; ++t) {
-                    const uint64_t ad = sdesc(as + t * 16 * kWgPlane + k * 256, 128, kWgPlane);
-                    umma_bf16(tmem + t * cpad, ad, bd, idesc, (it > 0 || k > 0) ? 1u : 0u);
+            const uint32_t dyb = saddr(stage0 + b * kWgStage), xb = dyb + 8 * kWgDyBox;
+            for (int r = 0; r < kWgRows; ++r)
+                for (int k = 0; k < kWgStrip / 16; ++k) {
+                    const uint64_t ad = sdesc_sw32_mn(dyb + (r * kWgStrip + 16 * k) * 32, kWgDyBox);
+                    for (int tap = 0; tap < 9; ++tap) {
+                        const int ky = tap / 3, kx = tap - ky * 3;
+                        const uint64_t bd = sdesc_sw32_mn(xb + ((r + ky) * kWgHaloW + kx + 16 * k) * 32, kWgXBox);
+                        umma_bf16(tmem + tap * ch, ad, bd, idesc, (it > 0 || r > 0 || k > 0) ? 1u : 0u);
+                    }
                 }
-            }
             umma_commit(saddr(empty + b));
         }
         if (ok && count > 0) umma_commit(saddr(acc));
     }
     __syncwarp();
-    // epilogue: this warp's TMEM lane quarter of every tile
+    // epilogue: TMEM lane (warp * 32 + lane) holds output channel co for every tap
     const bool got = count == 0 || wait_or_abort(saddr(acc), 0u, abort_flag, a.status);
     if (__all_sync(0xffffffffu, got && !*abort_flag)) {  // warp-uniform: tcgen05.ld is .aligned
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        float* part = a.part + (size_t)blockIdx.x * a.rows * cpad;
-        for (int t = 0; t < mt; ++t) {
-            const int row = row0 + t * 128 + warp * 32 + lane;
-            for (int j = 0; j < cpad / 16; ++j) {
+        const int co = warp * 32 + lane;
+        float* part = a.part + (size_t)blockIdx.x * 9 * a.cpad * a.cin;
+        for (int tap = 0; tap < 9; ++tap)
+            for (int j = 0; j < nx; ++j) {
                 uint32_t v[16];
-                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + t * cpad + j * 16, v);
-                if (row >= a.rows) continue;
-                float4* dst = reinterpret_cast<float4*>(part + (size_t)row * cpad + j * 16);
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + tap * ch + j * 16, v);
+                if (co >= a.cout) continue;
+                float4* dst = reinterpret_cast<float4*>(part + ((size_t)tap * a.cpad + co) * a.cin + c0 + j * 16);
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
                     dst[q] = count > 0 ? make_float4(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1]),
                                                      __uint_as_float(v[4 * q + 2]), __uint_as_float(v[4 * q + 3]))
                                        : make_float4(0.f, 0.f, 0.f, 0.f);
             }
-        }
     } else if (lane == 0) {
         atomicOr(a.status, 1);
     }
@@ -695,18 +690,19 @@ __global__ void k_concat_src(const ConvSrc x, int cin, int N, int H, int W, bf16
     }
 }
 
-// dw[tap][co][ci] += sum over slices s (in order) of part[s][tap * cin + ci][co]
-__global__ void k_wgrad_reduce(const float* __restrict__ part, int slices, int rows, int cpad, int cin, int cout,
+// dw[tap][co][ci] += sum over slices s (in order) of part[s][tap][co][ci]
+__global__ void k_wgrad_reduce(const float* __restrict__ part, int slices, int cpad, int cin, int cout,
                                float* __restrict__ dw) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;  // (row, co), co fastest
-    if (i >= (long long)rows * cout) return;
-    const int co = (int)(i % cout), row = (int)(i / cout);
-    const int tap = row / cin, ci = row - tap * cin;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;  // (tap, co, ci), ci fastest
+    if (i >= 9LL * cout * cin) return;
+    const int ci = (int)(i % cin);
+    const long long r = i / cin;
+    const int co = (int)(r % cout), tap = (int)(r / cout);
     float s = 0.0f;
-    const size_t stride = (size_t)rows * cpad;
-    const float* p = part + (size_t)row * cpad + co;
+    const size_t stride = (size_t)9 * cpad * cin;
+    const float* p = part + ((size_t)tap * cpad + co) * cin + ci;
     for (int k = 0; k < slices; ++k) s += p[k * stride];
-    dw[((size_t)tap * cout + co) * cin + ci] += s;
+    dw[i] += s;
 }
 
 }  // namespace
@@ -780,25 +776,21 @@ salty_status conv3x3_tma(salty_ctx* ctx, const bf16* in, int in_cs, int cin, con
     return SALTY_OK;
 }
 
-// Groups of M-tiles and strip slices for a layer: about one CTA per SM in all.
-static void wgrad_plan(int num_sms, int cin, int cpad, int N, int H, int W, int* mt, int* groups, int* slices) {
-    const int rows = 9 * cin, tiles = (rows + 127) / 128;
-    int m = 512 / cpad;
-    if (m > kWgMaxTiles) m = kWgMaxTiles;
-    if (m > tiles) m = tiles;
-    *mt = m;
-    *groups = (tiles + m - 1) / m;
-    const long long strips = (long long)N * H * ((W + kWgStrip - 1) / kWgStrip);
+// Input-channel groups and strip slices for a layer: about one CTA per SM in all.
+static void wgrad_plan(int num_sms, int cin, int N, int H, int W, int* groups, int* slices, int* strips) {
+    *groups = (cin + kWgChunk - 1) / kWgChunk;
+    const long long st = (long long)N * ((H + kWgRows - 1) / kWgRows) * ((W + kWgStrip - 1) / kWgStrip);
     long long s = num_sms / *groups;
     if (s < 1) s = 1;
-    if (s > strips) s = strips;
+    if (s > st) s = st;
     *slices = (int)s;
+    *strips = (int)st;
 }
 
 size_t conv_wgrad_tc_workspace(int num_sms, int cin, int cpad, int N, int H, int W) {
-    int mt, groups, slices;
-    wgrad_plan(num_sms, cin, cpad, N, H, W, &mt, &groups, &slices);
-    return (size_t)slices * 9 * cin * cpad;
+    int groups, slices, strips;
+    wgrad_plan(num_sms, cin, N, H, W, &groups, &slices, &strips);
+    return (size_t)slices * 9 * cpad * cin;
 }
 
 salty_status conv_wgrad_tc(salty_ctx* ctx, const bf16* dy, int cpad, int cout, const ConvSrc& x, int cin, float* dw,
@@ -809,10 +801,9 @@ salty_status conv_wgrad_tc(salty_ctx* ctx, const bf16* dy, int cpad, int cout, c
         return ctx->err.fail(SALTY_ERR_INVALID_ARG, "conv_wgrad_tc: unsupported shape (cin %d, cout %d)", cin, cout);
     EncodeTiledFn enc = tensor_map_encoder();
     if (!enc) return ctx->err.fail(SALTY_ERR_CUDA, "conv_wgrad_tc: cuTensorMapEncodeTiled is not available");
-    int mt, groups, slices;
-    wgrad_plan(ctx->num_sms, cin, cpad, N, H, W, &mt, &groups, &slices);
-    const int rows = 9 * cin;
-    if ((size_t)slices * rows * cpad > ws_floats)
+    int groups, slices, strips;
+    wgrad_plan(ctx->num_sms, cin, N, H, W, &groups, &slices, &strips);
+    if ((size_t)slices * 9 * cpad * cin > ws_floats)
         return ctx->err.fail(SALTY_ERR_CAPACITY, "conv_wgrad_tc: workspace too small");
     // the input as one NHWC tensor: as given, or the decoder's concatenation written out
     const bf16* xin = x.a;
@@ -827,30 +818,30 @@ salty_status conv_wgrad_tc(salty_ctx* ctx, const bf16* dy, int cpad, int cout, c
         xin = cat_ws;
         xcs = cin;
     }
-    if (reinterpret_cast<uintptr_t>(xin) % 16 || xcs % 8)
+    if (reinterpret_cast<uintptr_t>(xin) % 16 || xcs % 16)
         return ctx->err.fail(SALTY_ERR_INVALID_ARG, "conv_wgrad_tc: input not 16-byte aligned");
     CUtensorMap tm_x, tm_dy;
-    const cuuint32_t box[4] = {8, (cuuint32_t)kWgStrip, 1, 1};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const cuuint32_t xbox[4] = {16, (cuuint32_t)kWgHaloW, (cuuint32_t)(kWgRows + 2), 1};
     const cuuint64_t xdim[4] = {(cuuint64_t)cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
     const cuuint64_t xstr[3] = {(cuuint64_t)xcs * 2, (cuuint64_t)W * xcs * 2, (cuuint64_t)H * W * xcs * 2};
-    if (enc(&tm_x, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(xin), xdim, xstr, box, estr,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+    if (enc(&tm_x, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(xin), xdim, xstr, xbox, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return ctx->err.fail(SALTY_ERR_CUDA, "conv_wgrad_tc: input tensor map");
+    const cuuint32_t dbox[4] = {16, (cuuint32_t)kWgStrip, (cuuint32_t)kWgRows, 1};
     const cuuint64_t ddim[4] = {(cuuint64_t)cpad, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
     const cuuint64_t dstr[3] = {(cuuint64_t)cpad * 2, (cuuint64_t)W * cpad * 2, (cuuint64_t)H * W * cpad * 2};
-    if (enc(&tm_dy, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(dy), ddim, dstr, box, estr,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+    if (enc(&tm_dy, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(dy), ddim, dstr, dbox, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return ctx->err.fail(SALTY_ERR_CUDA, "conv_wgrad_tc: gradient tensor map");
-    const size_t smem = (size_t)kWgHeader + kWgStages * (size_t)wg_stage_bytes(mt, cpad);
+    const size_t smem = (size_t)kWgHeader + (size_t)kWgStages * kWgStage;
     SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    WgradArgs a{cpad, cin, N, H, W, rows, mt, (int)((long long)N * H * ((W + kWgStrip - 1) / kWgStrip)), ws,
-                d_status};
+    WgradArgs a{cpad, cout, cin, N, H, W, strips, ws, d_status};
     k_wgrad_tc<<<dim3(slices, groups), kWgThreads, smem, ctx->stream>>>(tm_x, tm_dy, a);
-    const long long outs = (long long)rows * cout;
-    k_wgrad_reduce<<<(unsigned)((outs + 255) / 256), 256, 0, ctx->stream>>>(ws, slices, rows, cpad, cin, cout, dw);
+    const long long outs = 9LL * cout * cin;
+    k_wgrad_reduce<<<(unsigned)((outs + 255) / 256), 256, 0, ctx->stream>>>(ws, slices, cpad, cin, cout, dw);
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;
 }

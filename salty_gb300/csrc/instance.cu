@@ -197,6 +197,7 @@ extern "C" salty_status salty_scene_set_instances(salty_ctx* ctx, salty_scene* s
     auto& E = ctx->err;
     if (!scene) return E.fail(SALTY_ERR_INVALID_ARG, "null scene");
     if (n < 0 || (n > 0 && !inst)) return E.fail(SALTY_ERR_INVALID_ARG, "bad instance list");
+    if (n > 0 && scene->n_sph > 0) return E.fail(SALTY_ERR_INVALID_ARG, "instances are not combined with spheres");
     const int64_t n_mesh_tris = scene->n_input;
     std::vector<salty_instance> v;
     int64_t total = 0;

@@ -139,6 +139,8 @@ struct SceneConsts {
     float cam_lens, cam_focal;  // thin lens radius (0: pinhole), focal distance
     int ibl_map;                // environment texture, -1: constant sky
     float ibl_scale;
+    int n_lights;               // has_light + sphere lights (Scene::GetLight's list)
+    int sph_base;               // id of the first sphere (kNoSpheres: none)
 };
 
 struct Film {
@@ -184,12 +186,16 @@ struct alignas(16) InstShade {
 // What one traversal launch walks: a BVH (or a batch arena of concatenated BVHs) and, per
 // ray, the node it starts at.  With `inst`, node 0 starts a top-level BVH whose leaf
 // entries are instances (two levels).
+constexpr int kNoSpheres = 0x7fffffff;
+constexpr int kSphLight = 1 << 30;  // flag in a sphere's material word: the sphere is a light
+
 struct TraceTarget {
     const Bvh8Node* nodes = nullptr;
     const float4* tris = nullptr;
     int depth = 0;
     const int* roots = nullptr;  // per-ray root node, or null (node 0)
     const InstRec* inst = nullptr;
+    int sph_base = kNoSpheres;   // first sphere id (leaf entries from it on are spheres)
 };
 
 // Launch shape of the traversal kernel, chosen by salty_autotune.
@@ -226,17 +232,26 @@ struct salty_scene {
     salty::DevBuf<int> inst_vbase;  // n_inst + 1 prefix sums of triangle counts
     int n_inst = 0;
     int64_t n_virtual = 0;          // triangles of all instances
+    // Sphere shapes (src/s3d_sphere.cpp:22-115): ids n_tris + k, in the same BVH
+    std::vector<salty_sphere> sph_host;
+    salty::DevBuf<float4> sph;      // centre, radius
+    salty::DevBuf<int> sph_mat;     // material index
+    salty::DevBuf<int> sph_lights;  // the spheres that are lights, in input order
+    int n_sph = 0;
+    int n_sph_lights = 0;
 };
 
 namespace salty {
 // Launch shapes of the renderer, chosen by salty_autotune (include/salty_gpu.h).
 struct Tuning {
     TraceTuning trace;
-    // Paths in flight per wave (queue capacity).  Each depth level of a wave ends with a
-    // tail of a few long walks; a large wave spreads that tail over more samples (1080p
-    // heightfield, 64 spp: 717 Mrays/s at 2^22, 1,274 at 2^24, 1,573 at 2^26).  352 bytes of
-    // path state per path: 23.6 GB at 2^26.
-    long long wave_paths = 1ll << 26;
+    // Paths in flight (queue capacity).  Every traversal launch ends with a tail of a few
+    // long walks; freed queue slots are refilled with new samples each iteration, so the
+    // launches stay full and a moderate queue already amortises the tails (1080p
+    // heightfield, 64 spp: 1,360 Mrays/s at 2^22, 1,567 at 2^24, 1,633 at 2^26).  352 bytes
+    // of path state per path plus 48 bytes per sample of the per-sample buffers: about 11 GB
+    // at 2^24 for a depth-12 render.
+    long long wave_paths = 1ll << 24;
     int shade_block = 256;             // threads per block of the shading kernels
 };
 
@@ -245,8 +260,8 @@ struct WaveStore {
     DevBuf<float4> rays[2], W[2], L[2], hits, nee, srays, shits, lbuf, abuf;
     DevBuf<uint4> meta[2];
     DevBuf<int> roots[2], sroots;
-    DevBuf<int> counts;
-    DevBuf<long long> wave;
+    DevBuf<int> counts, done;
+    DevBuf<long long> ctl;
     DevBuf<unsigned long long> stats, tc0, tc1;
 };
 
@@ -296,6 +311,7 @@ salty_status build_bvh_tris(salty_ctx* ctx, const float* d_pos, int n, const sal
                             float root_box[6]);
 // instance.cu
 salty_status build_instanced(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& opts);
+salty_status build_with_spheres(salty_ctx* ctx, salty_scene* sc, const salty_build_opts& opts);
 // trace.cu
 salty_status trace_launch(salty_ctx* ctx, salty_scene* sc, const float4* d_rays, long long n,
                           const int* n_dev, uint32_t flags, float4* d_hits,

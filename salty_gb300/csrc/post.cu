@@ -94,15 +94,29 @@ __device__ __forceinline__ float aces_curve(float x) {
     return saturate(__fdiv_rn(num, den));
 }
 
+// 8-bit code of a tonemapped value: clamp to [0, 1], the OETF (the reference's
+// 1.055^(1/2.4)-scaled variant or the standard one), then x * 255 + 0.5 truncated.  The power
+// is first taken with the hardware approximation (__powf); only when the scaled value lies
+// within 2^-10 of a code boundary is it recomputed with powf, so the code always equals
+// the all-powf formula's: the approximation moves x * 255 + 0.5 by less than 1e-4 (from
+// the documented errors of the hardware log2 and exp2 on [0.0031308, 1.055]), a tenth of
+// the margin.  Most values skip powf entirely.
+__device__ __forceinline__ float oetf_scaled(float x, int ref_oetf, bool exact) {
+    const float b = ref_oetf ? __fmul_rn(1.055f, x) : x;
+    const float p = exact ? powf(b, 1.0f / 2.4f) : __powf(b, 1.0f / 2.4f);
+    const float v = ref_oetf ? __fsub_rn(p, 0.055f) : __fsub_rn(__fmul_rn(1.055f, p), 0.055f);
+    return __fadd_rn(__fmul_rn(v, 255.0f), 0.5f);
+}
+
 __device__ __forceinline__ unsigned char to_srgb8(float x, int ref_oetf) {
     if (x > 1.0f) x = 1.0f;
     if (x < 0.0f) x = 0.0f;
     if (x != x) x = 0.0f;
-    if (ref_oetf)
-        x = (x <= 0.0031308f) ? __fmul_rn(12.92f, x) : __fsub_rn(powf(__fmul_rn(1.055f, x), 1.0f / 2.4f), 0.055f);
-    else
-        x = (x <= 0.0031308f) ? __fmul_rn(12.92f, x) : __fsub_rn(__fmul_rn(1.055f, powf(x, 1.0f / 2.4f)), 0.055f);
-    return (unsigned char)__fadd_rn(__fmul_rn(x, 255.0f), 0.5f);
+    if (x <= 0.0031308f) return (unsigned char)__fadd_rn(__fmul_rn(__fmul_rn(12.92f, x), 255.0f), 0.5f);
+    float t = oetf_scaled(x, ref_oetf, false);
+    const float fr = t - floorf(t);
+    if (fr < 0x1p-10f || fr > 1.0f - 0x1p-10f) t = oetf_scaled(x, ref_oetf, true);
+    return (unsigned char)t;
 }
 
 struct TmParams {

@@ -32,6 +32,7 @@
 #include <cfloat>
 #include <cmath>
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "internal.h"
@@ -161,9 +162,17 @@ struct WaveParams {
     const InstRec* irec;          // instances (two-level scenes, one slot), or null
     const InstShade* ishade;
     const int* ivbase;            // n_inst + 1 first virtual ids
+    const float4* sph;            // spheres (one scene): centre, radius
+    const int* sph_mat;           // material | kSphLight when the sphere is a light
+    const int* sph_lights;        // the light spheres, in light-list order
     int n_inst;
     int n_slots;
-    int capacity;
+    int capacity;                 // paths in flight (queue length)
+    int chunk;                    // samples per accumulation chunk
+    long long ring;               // per-sample buffer entries: ring_chunks * chunk
+    int ring_chunks;
+    int launch_iters;             // iterations per graph launch
+    long long iter_limit;         // iterations after which the render is declared stuck
     long long total_samples;
 };
 
@@ -185,9 +194,27 @@ struct WaveBuffers {
     float4* shits;
     float4* lbuf;      // per wave-local sample: radiance xyz
     float4* abuf;      // per wave-local sample, first hit: 2 x float4 (albedo, 1/(1+t)) (normal, 0)
-    int* counts;       // [0] queue A len, [1] queue B len, [2] shadow len, [3] finished
-    long long* wave;   // [0] first global sample of the current wave
+    int* counts;       // [0] queue A len, [1] queue B len, [2] shadow len
+    long long* ctl;    // the sample stream, see enum Ctl
+    int* done;         // per ring chunk: its samples whose paths have ended
     unsigned long long* stats;  // [0] rays traced, [1] paths
+};
+
+constexpr long long kMaxRingChunks = 16;  // per-sample buffers: at most 16 chunks of half a queue
+constexpr int kLaunchIters = 256;          // iterations per graph launch (cancellation granularity)
+
+// Control words of the regenerating wavefront (ctl[]).
+enum Ctl : int {
+    kNext = 0,      // next global sample to start
+    kAccBase = 1,   // samples below this are in the films
+    kAccN = 2,      // samples [kAccBase, kAccBase + kAccN) are ready to accumulate
+    kIters = 3,     // iterations run
+    kLaunchEnd = 4, // this graph launch stops after iteration kLaunchEnd
+    kGenFirst = 5,  // the pending generation: first sample,
+    kGenCount = 6,  //   count,
+    kGenSlot = 7,   //   and first queue slot
+    kStuck = 8,     // set when kIters passed the iteration limit
+    kCtlWords = 9
 };
 
 // the last slot whose offset is <= g (slots with no samples or pixels are skipped)
@@ -201,22 +228,17 @@ __device__ __forceinline__ int find_slot(const long long* off, int lo, int hi, l
 }
 
 // ---------------------------------------------------------------- kernels
-// Camera rays for samples [g0, g0 + n) of the batch; sample g of slot S -> (sample s,
-// film pixel fp) = divmod(g - S.sample_off, S.npx).  PinholeCamera::GetRay
-// (include/s3d_camera.h:95-100) with separately rounded operations.
-__global__ void k_generate(WaveParams P, WaveBuffers B) {
-    const long long g0 = B.wave[0];
-    const long long remain = P.total_samples - g0;
-    const int n = (int)(remain < P.capacity ? remain : P.capacity);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        B.counts[0] = n;
-        B.counts[1] = 0;
-        B.counts[2] = 0;
-        atomicAdd(&B.stats[1], (unsigned long long)n);
-        atomicAdd(&B.stats[0], (unsigned long long)n);
-    }
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const long long g = g0 + i;
+// Camera rays for the pending samples [g0, g0 + n) of the batch, appended to queue q at
+// slots [slot0, slot0 + n); sample g of slot S -> (sample s, film pixel fp) = divmod(g -
+// S.sample_off, S.npx).  PinholeCamera::GetRay (include/s3d_camera.h:95-100) with
+// separately rounded operations.
+__global__ void k_generate(WaveParams P, WaveBuffers B, int q) {
+    const long long g0 = B.ctl[kGenFirst];
+    const int n = (int)B.ctl[kGenCount], slot0 = (int)B.ctl[kGenSlot];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const long long g = g0 + j;
+        const int i = slot0 + j;                          // queue slot
+        const unsigned r = (unsigned)(g % P.ring);        // per-sample buffer entry
         const int sid = P.n_slots == 1 ? 0 : find_slot(P.sample_off, 0, P.n_slots - 1, g);
         const SceneSlot& S = P.slots[sid];
         const long long gl = g - P.sample_off[sid];
@@ -233,10 +255,10 @@ __global__ void k_generate(WaveParams P, WaveBuffers B) {
             fx = __fsub_rn(__fdiv_rn(__fadd_rn(jx, (float)px), (float)S.width), 0.5f);
             fy = __fsub_rn(__fdiv_rn(__fadd_rn(jy, (float)py), (float)S.height), 0.5f);
         }
-        float q[3], d[3];
+        float sp[3], d[3];  // screen point, direction
         for (int a = 0; a < 3; ++a) {
-            q[a] = __fadd_rn(__fadd_rn(__fmul_rn(S.cam.cx[a], fx), __fmul_rn(S.cam.cy[a], fy)), S.cam.cz[a]);
-            d[a] = __fsub_rn(q[a], S.cam.pos[a]);
+            sp[a] = __fadd_rn(__fadd_rn(__fmul_rn(S.cam.cx[a], fx), __fmul_rn(S.cam.cy[a], fy)), S.cam.cz[a]);
+            d[a] = __fsub_rn(sp[a], S.cam.pos[a]);
         }
         const float mag = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
         const float tmin = S.profile == SALTY_PROFILE_COMPAT ? kFHitMin : kEps;
@@ -262,15 +284,14 @@ __global__ void k_generate(WaveParams P, WaveBuffers B) {
             }
             dir = safe_unit(focus - org);
         }
-        B.rays[0][2 * i] = make_float4(org.x, org.y, org.z, tmin);
-        B.rays[0][2 * i + 1] = make_float4(dir.x, dir.y, dir.z, tmax);
-        if (B.roots[0]) B.roots[0][i] = S.root;
-        B.path[0].W[i] = make_float4(1.f, 1.f, 1.f, 0.f);
-        B.path[0].L[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        B.path[0].meta[i] = make_uint4((unsigned)rng.s, (unsigned)(rng.s >> 32), (unsigned)i, pack_w(0, true, sid));
-        B.lbuf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        B.abuf[2 * i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        B.abuf[2 * i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        B.rays[q][2 * i] = make_float4(org.x, org.y, org.z, tmin);
+        B.rays[q][2 * i + 1] = make_float4(dir.x, dir.y, dir.z, tmax);
+        if (B.roots[q]) B.roots[q][i] = S.root;
+        B.path[q].W[i] = make_float4(1.f, 1.f, 1.f, 0.f);
+        B.path[q].L[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        B.path[q].meta[i] = make_uint4((unsigned)rng.s, (unsigned)(rng.s >> 32), r, pack_w(0, true, sid));
+        B.abuf[2 * r] = make_float4(0.f, 0.f, 0.f, 0.f);
+        B.abuf[2 * r + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
@@ -379,6 +400,77 @@ __device__ __forceinline__ bool is_light(const SceneConsts& k, int id) {
     return k.light_tri0 >= 0 && id >= k.light_tri0 && id < k.light_tri0 + 2;
 }
 
+// ---------------------------------------------------------------- hits on spheres
+// What shading needs to find behind a hit id: the material and either the mesh triangle
+// (with its instance) or the sphere.
+struct HitRef {
+    int mat;
+    int mtri;  // mesh triangle, -1 on a sphere
+    int inst;  // instance of the triangle, -1 when none
+    int sph;   // sphere index, -1 on a triangle
+};
+__device__ __forceinline__ HitRef hit_ref(const WaveParams& P, const SceneConsts& K, int id) {
+    HitRef r;
+    if (id >= K.sph_base) {
+        r.sph = id - K.sph_base;
+        r.mtri = -1;
+        r.inst = -1;
+        r.mat = P.sph_mat[r.sph] & (kSphLight - 1);
+    } else {
+        r.sph = -1;
+        r.mtri = mesh_tri(P, id, r.inst);
+        r.mat = P.mat[r.mtri];
+    }
+    return r;
+}
+__device__ __forceinline__ V sph_center(const WaveParams& P, int k) { return xyz(P.sph[k]); }
+// Sphere::CalcParam (src/s3d_sphere.cpp:94-104): the outward normal at p ...
+__device__ __forceinline__ V sph_normal(const WaveParams& P, int k, V p) { return safe_unit(p - sph_center(P, k)); }
+// ... and the texture coordinate (phi / 2 pi, (pi - theta) / pi), phi = atan2(n.x, n.z)
+// in [0, 2 pi), theta = acos(n.y)
+__device__ __forceinline__ V sph_color_map(const WaveParams& P, const GpuMaterial& m, V n) {
+    const float theta = acosf(fminf(1.0f, fmaxf(-1.0f, n.y)));
+    float phi = atan2f(n.x, n.z);
+    if (phi < 0.0f) phi += k2Pi;
+    return tex_sample(P, m.color_map, phi * (1.0f / k2Pi), (kPi - theta) * (1.0f / kPi));
+}
+// the material's colour map at the hit point p (barycentrics b1, b2 on a triangle), or 1
+__device__ __forceinline__ V hit_color_map(const WaveParams& P, const GpuMaterial& m, const HitRef& r, float b1,
+                                           float b2, V p) {
+    if (m.color_map < 0) return mk(1.0f, 1.0f, 1.0f);
+    if (r.sph >= 0) return sph_color_map(P, m, sph_normal(P, r.sph, p));
+    return color_map(P, m, r.mtri, b1, b2);
+}
+// unit shading normal, not oriented
+__device__ __forceinline__ V hit_normal(const WaveParams& P, const HitRef& r, float b1, float b2, V p) {
+    if (r.sph >= 0) return sph_normal(P, r.sph, p);
+    return safe_unit(interp_normal(P, r.mtri, r.inst, b1, b2));
+}
+__device__ __forceinline__ Surf hit_surface(const WaveParams& P, const HitRef& r, float t, float b1, float b2, V o,
+                                            V d) {
+    if (r.sph < 0) return surface(P, r.mtri, r.inst, t, b1, b2, o, d);
+    Surf s;
+    s.p = o + d * t;
+    s.ng = sph_normal(P, r.sph, s.p);
+    s.into = dot(s.ng, d) < 0.0f;
+    s.ngf = s.into ? s.ng : -s.ng;
+    s.ns = s.ng;
+    s.nsf = s.ngf;
+    return s;
+}
+
+// Solid angle pdf of sampling sphere light k uniformly in the cone it subtends from x (0
+// when x is inside): 1 / (2 pi (1 - cos theta_max)), 1 - cos = sin^2 / (1 + cos).
+__device__ __forceinline__ float sph_cone_pdf(const WaveParams& P, int k, V x, float& cos_max) {
+    const float4 sp = P.sph[k];
+    const V w = xyz(sp) - x;
+    const float d2 = dot(w, w), r2 = sp.w * sp.w;
+    if (!(d2 > r2)) { cos_max = 1.0f; return 0.0f; }
+    const float s2 = r2 / d2;
+    cos_max = sqrtf(fmaxf(0.0f, 1.0f - s2));
+    return 1.0f / (k2Pi * (s2 / (1.0f + cos_max)));
+}
+
 __device__ __forceinline__ float ggx_d(float nh, float a2) {
     float k = nh * nh * (a2 - 1.0f) + 1.0f;
     return a2 / (kPi * k * k);
@@ -470,68 +562,142 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
         bool want_l = false, want_s = false;
         float4 ray_l0, ray_l1, ray_s0, ray_s1;
         V cl = mk(0, 0, 0), cs = mk(0, 0, 0);
+        float4 e1x = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // compat sphere light: dist^2, pdf, index + 1
         const uint4 mt = live ? B.path[q].meta[i] : make_uint4(0, 0, 0, 0);
         const int slot = (int)(mt.w >> kSlotShift);
         const SceneSlot& S = P.slots[slot];
         const SceneConsts& K = S.k;
         if (live && id >= 0 && !is_light(K, id)) {
-            int inst;
-            const int mtri = mesh_tri(P, id, inst);
-            GpuMaterial m = P.mats[P.mat[mtri]];
+            const HitRef hr = hit_ref(P, K, id);
+            GpuMaterial m = P.mats[hr.mat];
+            const float4 r0 = B.rays[q][2 * i], r1 = B.rays[q][2 * i + 1];
+            V o = xyz(r0), d = xyz(r1);
+            const V hp = mk(__fadd_rn(o.x, __fmul_rn(d.x, h.x)), __fadd_rn(o.y, __fmul_rn(d.y, h.x)),
+                            __fadd_rn(o.z, __fmul_rn(d.z, h.x)));
             // TexturedMaterial::GetBaseColor: the colour map multiplies the base colour
-            const V tx = color_map(P, m, mtri, h.z, h.w);
+            const V tx = hit_color_map(P, m, hr, h.z, h.w, hp);
             m.color[0] *= tx.x; m.color[1] *= tx.y; m.color[2] *= tx.z;
             const bool delta = (m.type == SALTY_MIRROR || m.type == SALTY_GLASS);
             Rng rng;
             rng.s = (unsigned long long)mt.x | ((unsigned long long)mt.y << 32);
-            const float4 r0 = B.rays[q][2 * i], r1 = B.rays[q][2 * i + 1];
-            V o = xyz(r0), d = xyz(r1);
             if (S.profile == SALTY_PROFILE_COMPAT) {
-                if (!delta && K.has_light) {
-                    Surf s;
-                    s.p = mk(__fadd_rn(o.x, __fmul_rn(d.x, h.x)), __fadd_rn(o.y, __fmul_rn(d.y, h.x)),
-                             __fadd_rn(o.z, __fmul_rn(d.z, h.x)));
-                    V n = safe_unit(interp_normal(P, mtri, inst, h.z, h.w));
-                    (void)rng.u32();  // Scene::GetLight (include/s3d_scene.h:84-90), one light
-                    float u = rng.f32(), w = rng.f32();
-                    V lp = ld3(K.lc) + ld3(K.la) * u + ld3(K.lb) * w;
-                    float pdf = 1.0f / K.larea;
-                    V ld = lp - s.p;
-                    float dist2 = dot(ld, ld);
-                    ld = safe_unit(ld);
-                    float cos_s = fabsf(dot(n, ld));
-                    float cos_l = fabsf(dot(ld3(K.ln), -ld));
-                    V fs = ld3(m.color) * (1.0f / kPi);
-                    float G = cos_s * cos_l / dist2;
-                    float brdf_pdf = fabsf(ld.z / kPi) * cos_l / dist2;
-                    float mis = pdf / (brdf_pdf + pdf);
-                    cl = ld3(K.le) * fs * mis * (G / pdf);
-                    want_l = true;
-                    ray_l0 = make_float4(s.p.x, s.p.y, s.p.z, kFHitMin);
-                    ray_l1 = make_float4(ld.x, ld.y, ld.z, kFHitMax);
+                if (!delta && K.n_lights > 0) {
+                    const V p = hp;
+                    const V nrm = hit_normal(P, hr, h.z, h.w, p);
+                    // Scene::GetLight (include/s3d_scene.h:84-90): one light, uniformly
+                    const int li = (int)(rng.u32() % (unsigned)K.n_lights);
+                    const V fs = ld3(m.color) * (1.0f / kPi);
+                    if (li < K.has_light) {
+                        float u = rng.f32(), w = rng.f32();
+                        V lp = ld3(K.lc) + ld3(K.la) * u + ld3(K.lb) * w;
+                        float pdf = 1.0f / K.larea;
+                        V ld = lp - p;
+                        float dist2 = dot(ld, ld);
+                        ld = safe_unit(ld);
+                        float cos_s = fabsf(dot(nrm, ld));
+                        float cos_l = fabsf(dot(ld3(K.ln), -ld));
+                        float G = cos_s * cos_l / dist2;
+                        float brdf_pdf = fabsf(ld.z / kPi) * cos_l / dist2;
+                        float mis = pdf / (brdf_pdf + pdf);
+                        cl = ld3(K.le) * fs * mis * (G / pdf);
+                        want_l = true;
+                        ray_l0 = make_float4(p.x, p.y, p.z, kFHitMin);
+                        ray_l1 = make_float4(ld.x, ld.y, ld.z, kFHitMax);
+                    } else {
+                        // Sphere::Sample (src/s3d_sphere.cpp:106-115): a point on the sphere
+                        // of radius r + 0.1, pdf 1 / (4 pi r^2); the light's normal and the
+                        // rest of the estimate wait for the shadow ray's hit (k_shade2)
+                        const int k = P.sph_lights[li - K.has_light];
+                        const float4 sp = P.sph[k];
+                        const float a1 = k2Pi * rng.f32();
+                        const float z = 1.0f - 2.0f * rng.f32();
+                        const float rr = sqrtf(1.0f - z * z);
+                        const V lp = xyz(sp) + safe_unit(mk(rr * cosf(a1), rr * sinf(a1), z)) * (sp.w + 1e-1f);
+                        const float pdf = 1.0f / (4.0f * kPi * sp.w * sp.w);
+                        V ld = lp - p;
+                        const float dist2 = dot(ld, ld);
+                        ld = safe_unit(ld);
+                        cl = fs * fabsf(dot(nrm, ld));
+                        e1x = make_float4(dist2, pdf, __int_as_float(k + 1), 0.0f);
+                        want_l = true;
+                        ray_l0 = make_float4(p.x, p.y, p.z, kFHitMin);
+                        ray_l1 = make_float4(ld.x, ld.y, ld.z, kFHitMax);
+                    }
                 }
             } else {
                 if (!delta) {
-                    Surf s = surface(P, mtri, inst, h.x, h.z, h.w, o, d);
+                    Surf s = hit_surface(P, hr, h.x, h.z, h.w, o, d);
                     V wo = -d;
-                    if (K.has_light) {
-                        float u1 = rng.f32(), u2 = rng.f32();
-                        V lp = ld3(K.lc) + ld3(K.la) * u1 + ld3(K.lb) * u2;
-                        V wi = lp - s.p;
-                        float dist2 = dot(wi, wi), dist = sqrtf(dist2);
-                        wi = wi * (1.0f / dist);
-                        float cos_l = dot(ld3(K.ln), -wi);
-                        float cos_s = dot(s.nsf, wi), cos_g = dot(s.ngf, wi);
-                        if (cos_l > 0.0f && cos_s > 0.0f && cos_g > 0.0f) {
-                            float pdf_b;
-                            V f = phys_eval(m, s.nsf, wo, wi, pdf_b);
-                            float pdf_l = dist2 / (cos_l * K.larea);
-                            float mis = pdf_l / (pdf_l + pdf_b);
-                            cl = f * ld3(K.le) * (cos_s * mis / pdf_l);
-                            want_l = true;
-                            const V so = spawn(s.p, s.ng, wi);
-                            ray_l0 = make_float4(so.x, so.y, so.z, 0.0f);
-                            ray_l1 = make_float4(wi.x, wi.y, wi.z, dist * (1.0f - 1e-4f));
+                    if (K.n_lights > 0) {
+                        // one light of the list, uniformly (the draw only with two or more)
+                        int li = 0;
+                        if (K.n_lights > 1) li = min((int)(rng.f32() * (float)K.n_lights), K.n_lights - 1);
+                        const float psel = 1.0f / (float)K.n_lights;
+                        if (li < K.has_light) {
+                            float u1 = rng.f32(), u2 = rng.f32();
+                            V lp = ld3(K.lc) + ld3(K.la) * u1 + ld3(K.lb) * u2;
+                            V wi = lp - s.p;
+                            float dist2 = dot(wi, wi), dist = sqrtf(dist2);
+                            wi = wi * (1.0f / dist);
+                            float cos_l = dot(ld3(K.ln), -wi);
+                            float cos_s = dot(s.nsf, wi), cos_g = dot(s.ngf, wi);
+                            if (cos_l > 0.0f && cos_s > 0.0f && cos_g > 0.0f) {
+                                float pdf_b;
+                                V f = phys_eval(m, s.nsf, wo, wi, pdf_b);
+                                float pdf_l = psel * dist2 / (cos_l * K.larea);
+                                float mis = pdf_l / (pdf_l + pdf_b);
+                                cl = f * ld3(K.le) * (cos_s * mis / pdf_l);
+                                want_l = true;
+                                const V so = spawn(s.p, s.ng, wi);
+                                ray_l0 = make_float4(so.x, so.y, so.z, 0.0f);
+                                ray_l1 = make_float4(wi.x, wi.y, wi.z, dist * (1.0f - 1e-4f));
+                            }
+                        } else {
+                            // a direction uniform in the cone the sphere subtends
+                            const int k = P.sph_lights[li - K.has_light];
+                            const float u1 = rng.f32(), u2 = rng.f32();
+                            float cos_max;
+                            const float pdf_c = sph_cone_pdf(P, k, s.p, cos_max);
+                            if (pdf_c > 0.0f) {
+                                const float4 sp = P.sph[k];
+                                const V w = xyz(sp) - s.p;
+                                const float dc = sqrtf(dot(w, w));
+                                const V wz = w * (1.0f / dc);
+                                const float one_m = (1.0f - cos_max) * u1;  // 1 - cos theta
+                                const float ct = 1.0f - one_m;
+                                const float st = sqrtf(fmaxf(0.0f, one_m * (2.0f - one_m)));
+                                float sp_, cp_;
+                                sincosf(k2Pi * u2, &sp_, &cp_);
+                                V tx_, ty_;
+                                tangent_space(wz, tx_, ty_);
+                                const V wi = safe_unit(tx_ * (st * cp_) + ty_ * (st * sp_) + wz * ct);
+                                // distance to the near side, (dc^2 - r^2) / (dc cos + sqrt(r^2 -
+                                // dc^2 sin^2)): no cancellation at the cone's edge
+                                const float hs = sp.w * sp.w - dc * dc * st * st;
+                                const float dist = (dc * dc - sp.w * sp.w) / (dc * ct + sqrtf(fmaxf(0.0f, hs)));
+                                const float cos_s = dot(s.nsf, wi), cos_g = dot(s.ngf, wi);
+                                if (cos_s > 0.0f && cos_g > 0.0f && dist > 0.0f) {
+                                    float pdf_b;
+                                    V f = phys_eval(m, s.nsf, wo, wi, pdf_b);
+                                    const float pdf_l = psel * pdf_c;
+                                    const float mis = pdf_l / (pdf_l + pdf_b);
+                                    const V le = ld3(P.mats[P.sph_mat[k] & (kSphLight - 1)].emission);
+                                    cl = f * le * (cos_s * mis / pdf_l);
+                                    want_l = true;
+                                    // the shadow ray runs from the light point back to the
+                                    // surface: from just outside the sphere it cannot meet
+                                    // the sphere itself, which a ray towards a grazing point
+                                    // on its silhouette could, by rounding
+                                    const V lq = s.p + wi * dist;
+                                    const V qs = spawn(lq, safe_unit(lq - xyz(sp)), -wi);
+                                    const V ps = spawn(s.p, s.ng, wi);
+                                    V back = ps - qs;
+                                    const float blen = sqrtf(dot(back, back));
+                                    back = back * (1.0f / blen);
+                                    ray_l0 = make_float4(qs.x, qs.y, qs.z, 0.0f);
+                                    ray_l1 = make_float4(back.x, back.y, back.z, blen * (1.0f - 1e-4f));
+                                }
+                            }
                         }
                     }
                     if (K.has_sun) {
@@ -579,13 +745,14 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
         }
         if (live) {
             B.nee[2 * i] = make_float4(cl.x, cl.y, cl.z, __int_as_float(want_l ? ql : -1));
-            B.nee[2 * i + 1] = make_float4(cs.x, cs.y, cs.z, __int_as_float(want_s ? qs : -1));
+            B.nee[2 * i + 1] = make_float4(want_s ? cs.x : e1x.x, want_s ? cs.y : e1x.y, want_s ? cs.z : e1x.z,
+                                           __int_as_float(want_s ? qs : -1));
         }
     }
 }
 
 // BSDF sampling, Russian roulette, compaction of queue q into queue q^1.
-__global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
+__global__ void k_shade2(WaveParams P, WaveBuffers B, int q) {
     const int n = B.counts[q];
     const int stride = gridDim.x * blockDim.x;
     const int lim = (n + 31) & ~31;
@@ -594,13 +761,14 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
         bool cont = false;
         float4 nr0, nr1, nW, nL;
         uint4 nmeta;
-        int root = 0;
+        int root = 0, ended = -1;
         if (live) {
             const float4 h = B.hits[i];
             const int id = __float_as_int(h.y);
             float4 W4 = B.path[q].W[i], L4 = B.path[q].L[i];
             uint4 mt = B.path[q].meta[i];
             const int slot = (int)(mt.w >> kSlotShift);
+            const int depth = (int)(mt.w & 0xffffu);
             const SceneSlot& S = P.slots[slot];
             const SceneConsts& K = S.k;
             const bool compat = S.profile == SALTY_PROFILE_COMPAT;
@@ -615,7 +783,23 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
             // unoccluded light
             const float4 e0 = B.nee[2 * i], e1 = B.nee[2 * i + 1];
             const int q0 = __float_as_int(e0.w), q1 = __float_as_int(e1.w);
-            if (q0 >= 0) {
+            const int sk = compat ? __float_as_int(e1.z) - 1 : -1;  // compat: sampled light sphere
+            if (q0 >= 0 && sk >= 0) {
+                // NextEventEstimation with a sphere light (src/s3d_pt.cpp:274-288): accepted
+                // when the shadow ray's first hit is that sphere; the light's normal is taken
+                // where the ray hit it, the distance is the sampled point's
+                const float4 sh = B.shits[q0];
+                if (__float_as_int(sh.y) == K.sph_base + sk) {
+                    const V sd = xyz(B.srays[2 * q0 + 1]);
+                    const V hp = xyz(B.srays[2 * q0]) + sd * sh.x;
+                    const float cos_l = fabsf(dot(sph_normal(P, sk, hp), -sd));
+                    const float dist2 = e1.x, pdf = e1.y;
+                    const float brdf_pdf = fabsf(sd.z / kPi) * cos_l / dist2;
+                    const float mis = pdf / (brdf_pdf + pdf);
+                    const V le = ld3(P.mats[P.sph_mat[sk] & (kSphLight - 1)].emission);
+                    L = L + W * le * xyz(e0) * (mis * (cos_l / dist2) / pdf);
+                }
+            } else if (q0 >= 0) {
                 const int sid = __float_as_int(B.shits[q0].y);
                 bool vis = compat ? (sid >= 0 && is_light(K, sid)) : (sid < 0);
                 if (vis) L = L + W * xyz(e0);
@@ -627,13 +811,13 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
             if (depth == 0 && id >= 0) {
                 // first-hit features of the sample (denoiser inputs): albedo, 1/(1+t),
                 // shading normal facing the camera
-                int inst;
-                const int mtri = mesh_tri(P, id, inst);
-                const GpuMaterial am = P.mats[P.mat[mtri]];
-                V n = safe_unit(interp_normal(P, mtri, inst, h.z, h.w));
+                const HitRef ar = hit_ref(P, K, id);
+                const GpuMaterial am = P.mats[ar.mat];
+                const V ap = o + d * h.x;
+                V n = hit_normal(P, ar, h.z, h.w, ap);
                 if (dot(n, d) > 0.0f) n = -n;
                 const bool emitter = is_light(K, id);
-                const V atx = color_map(P, am, mtri, h.z, h.w);
+                const V atx = hit_color_map(P, am, ar, h.z, h.w, ap);
                 B.abuf[2 * mt.z] = make_float4(emitter ? 1.0f : am.color[0] * atx.x, emitter ? 1.0f : am.color[1] * atx.y,
                                                emitter ? 1.0f : am.color[2] * atx.z, 1.0f / (1.0f + h.x));
                 B.abuf[2 * mt.z + 1] = make_float4(n.x, n.y, n.z, 0.0f);
@@ -646,14 +830,13 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                     L = L + W * ld3(K.sun_L) * w;
                 }
             } else if (compat) {
-                int inst;
-                const int mtri = mesh_tri(P, id, inst);
-                const GpuMaterial m = P.mats[P.mat[mtri]];
-                const V tx = color_map(P, m, mtri, h.z, h.w);  // TexturedMaterial::Shade scales the weight
+                const HitRef hr = hit_ref(P, K, id);
+                const GpuMaterial m = P.mats[hr.mat];
                 V pos = mk(__fadd_rn(o.x, __fmul_rn(d.x, h.x)), __fadd_rn(o.y, __fmul_rn(d.y, h.x)),
                            __fadd_rn(o.z, __fmul_rn(d.z, h.x)));
+                const V tx = hit_color_map(P, m, hr, h.z, h.w, pos);  // TexturedMaterial::Shade scales the weight
                 L = L + W * ld3(m.emission);
-                V normal = safe_unit(interp_normal(P, mtri, inst, h.z, h.w));
+                V normal = hit_normal(P, hr, h.z, h.w, pos);
                 V nm = dot(normal, d) < 0.0f ? normal : -normal;
                 V col = ld3(m.color), out, wgt;
                 bool dice = false;
@@ -739,19 +922,26 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
                 if (cos_l > 0.0f) {
                     if (prev_delta) L = L + W * ld3(K.le);
                     else {
-                        float pdf_l = h.x * h.x / (cos_l * K.larea);
+                        float pdf_l = h.x * h.x / (cos_l * K.larea * (float)K.n_lights);
                         float mis = prev_pdf / (prev_pdf + pdf_l);
                         L = L + W * ld3(K.le) * mis;
                     }
                 }
             } else {
-                int inst;
-                const int mtri = mesh_tri(P, id, inst);
-                GpuMaterial m = P.mats[P.mat[mtri]];
-                const V tx = color_map(P, m, mtri, h.z, h.w);
+                const HitRef hr = hit_ref(P, K, id);
+                GpuMaterial m = P.mats[hr.mat];
+                Surf s = hit_surface(P, hr, h.x, h.z, h.w, o, d);
+                const V tx = hit_color_map(P, m, hr, h.z, h.w, s.p);
                 m.color[0] *= tx.x; m.color[1] *= tx.y; m.color[2] *= tx.z;
-                Surf s = surface(P, mtri, inst, h.x, h.z, h.w, o, d);
-                L = L + W * ld3(m.emission);
+                if (hr.sph >= 0 && (P.sph_mat[hr.sph] & kSphLight) && !prev_delta) {
+                    // a light sphere reached by BSDF sampling: MIS against the cone sampling
+                    // of next-event estimation from the previous vertex (the ray's origin)
+                    float cos_max;
+                    const float pdf_l = sph_cone_pdf(P, hr.sph, o, cos_max) / (float)K.n_lights;
+                    L = L + W * ld3(m.emission) * (prev_pdf / (prev_pdf + pdf_l));
+                } else {
+                    L = L + W * ld3(m.emission);
+                }
                 V col = ld3(m.color), wi, wgt;
                 float pdf = 0.0f;
                 bool is_delta = false, dead = false;
@@ -862,8 +1052,14 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
             nL = make_float4(L.x, L.y, L.z, 0.0f);
             nmeta = make_uint4((unsigned)rng.s, (unsigned)(rng.s >> 32), mt.z,
                                compat ? pack_w(depth + 1, false, slot) : mt.w);
-            if (!cont) B.lbuf[mt.z] = nL;
+            if (!cont) {
+                B.lbuf[mt.z] = nL;
+                ended = (int)(mt.z / (unsigned)P.chunk);
+            }
         }
+        // the ended sample's chunk: one atomic per distinct chunk of the warp
+        const unsigned peers = __match_any_sync(0xffffffffu, ended);
+        if (ended >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&B.done[ended], __popc(peers));
         const int qi = warp_append(cont, &B.counts[q ^ 1]);
         if (cont) {
             B.rays[q ^ 1][2 * qi] = nr0;
@@ -876,21 +1072,73 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q, int depth) {
     }
 }
 
-__global__ void k_count_rays(WaveBuffers B, int q) {
-    atomicAdd(&B.stats[0], (unsigned long long)(B.counts[q ^ 1] + B.counts[2]));
-}
-
-__global__ void k_reset_queue(WaveBuffers B, int q) {
+// After the shading of queue q: counts its rays, empties it and the shadow queue, and
+// finds the samples ready for the films -- the longest run of whole chunks, from the first
+// sample not yet accumulated, whose paths have all ended.
+__global__ void k_iter_end(WaveParams P, WaveBuffers B, int q) {
+    B.stats[0] += (unsigned long long)(B.counts[q] + B.counts[2]);
     B.counts[q] = 0;
     B.counts[2] = 0;
+    const long long base = B.ctl[kAccBase];
+    long long n = 0;
+    for (int k = 0; k < P.ring_chunks; ++k) {
+        const long long c0 = base + n;
+        if (c0 >= P.total_samples) break;
+        const long long size = min((long long)P.chunk, P.total_samples - c0);
+        if (B.done[(c0 / P.chunk) % P.ring_chunks] != (int)size) break;
+        n += size;
+    }
+    B.ctl[kAccN] = n;
 }
+
+// After the accumulation: frees the accumulated chunks, plans the next generation (queue
+// q ^ 1 filled up to capacity with new samples, as far as free per-sample entries allow)
+// and decides whether the graph launch runs another iteration.
+__global__ void k_iter_next(WaveParams P, WaveBuffers B, int q, cudaGraphConditionalHandle more, int last) {
+    long long* c = B.ctl;
+    const long long n = c[kAccN];
+    for (long long g = c[kAccBase]; g < c[kAccBase] + n; g += P.chunk) B.done[(g / P.chunk) % P.ring_chunks] = 0;
+    c[kAccBase] += n;
+    c[kAccN] = 0;
+    const int have = B.counts[q ^ 1];
+    const long long limit = min(P.total_samples, c[kAccBase] + P.ring);
+    const long long add = max(0LL, min((long long)(P.capacity - have), limit - c[kNext]));
+    c[kGenFirst] = c[kNext];
+    c[kGenCount] = add;
+    c[kGenSlot] = have;
+    c[kNext] += add;
+    B.counts[q ^ 1] = have + (int)add;
+    B.stats[1] += (unsigned long long)add;
+    c[kIters] += 1;
+    if (c[kIters] > P.iter_limit) c[kStuck] = 1;
+    if (last) {
+        const bool go = c[kAccBase] < P.total_samples && c[kIters] < c[kLaunchEnd] && !c[kStuck];
+        cudaGraphSetConditional(more, go ? 1u : 0u);
+    }
+}
+
+// Start of a render: nothing accumulated, the first samples pending for queue 0.
+__global__ void k_render_init(WaveParams P, WaveBuffers B) {
+    for (int k = 0; k < kCtlWords; ++k) B.ctl[k] = 0;
+    for (int k = 0; k < P.ring_chunks; ++k) B.done[k] = 0;
+    const long long add = min((long long)P.capacity, min(P.total_samples, P.ring));
+    B.ctl[kGenCount] = add;
+    B.ctl[kNext] = add;
+    B.counts[0] = (int)add;
+    B.counts[1] = 0;
+    B.counts[2] = 0;
+    B.stats[0] = 0;
+    B.stats[1] = (unsigned long long)add;
+}
+
+// Start of a graph launch: run at most launch_iters iterations.
+__global__ void k_launch_begin(WaveParams P, WaveBuffers B) { B.ctl[kLaunchEnd] = B.ctl[kIters] + P.launch_iters; }
 
 // Adds the wave's samples to the films: one thread per film pixel of the slots the wave
 // touches, that pixel's samples in index order.
 __global__ void k_accumulate(WaveParams P, WaveBuffers B) {
-    const long long g0 = B.wave[0];
-    const long long remain = P.total_samples - g0;
-    const long long n = remain < P.capacity ? remain : P.capacity;
+    const long long g0 = B.ctl[kAccBase];
+    const long long n = B.ctl[kAccN];
     if (n <= 0) return;
     const int s0 = P.n_slots == 1 ? 0 : find_slot(P.sample_off, 0, P.n_slots - 1, g0);
     const int s1 = P.n_slots == 1 ? 0 : find_slot(P.sample_off, s0, P.n_slots - 1, g0 + n - 1);
@@ -911,12 +1159,12 @@ __global__ void k_accumulate(WaveParams P, WaveBuffers B) {
         const long long s_lo = lo <= 0 ? 0 : (lo + npx - 1) / npx;
         const long long s_hi = hi / npx;
         if (s_lo > s_hi) continue;
-        const long long w0 = base - g0;  // wave index of slot-local sample 0
+        // per-sample entry of slot-local sample index j: (base + j) % ring
         if (S.sum64) {
             double a0 = S.sum64[3 * p], a1 = S.sum64[3 * p + 1], a2 = S.sum64[3 * p + 2];
             double b0 = S.sumsq64[3 * p], b1 = S.sumsq64[3 * p + 1], b2 = S.sumsq64[3 * p + 2];
             for (long long sm = s_lo; sm <= s_hi; ++sm) {
-                float4 l = B.lbuf[w0 + sm * npx + p];
+                float4 l = B.lbuf[(base + sm * npx + p) % P.ring];
                 a0 += l.x; a1 += l.y; a2 += l.z;
                 b0 += (double)l.x * l.x; b1 += (double)l.y * l.y; b2 += (double)l.z * l.z;
             }
@@ -926,7 +1174,7 @@ __global__ void k_accumulate(WaveParams P, WaveBuffers B) {
             float sm3[3], c[3], q2[3];
             for (int k = 0; k < 3; ++k) { sm3[k] = S.sum[3 * p + k]; c[k] = S.comp[3 * p + k]; q2[k] = S.sumsq[3 * p + k]; }
             for (long long sm = s_lo; sm <= s_hi; ++sm) {
-                float4 l = B.lbuf[w0 + sm * npx + p];
+                float4 l = B.lbuf[(base + sm * npx + p) % P.ring];
                 float v[3] = {l.x, l.y, l.z};
                 for (int k = 0; k < 3; ++k) {
                     // Kahan-compensated sum
@@ -943,7 +1191,7 @@ __global__ void k_accumulate(WaveParams P, WaveBuffers B) {
         float f[7];
         for (int k = 0; k < 7; ++k) f[k] = S.aov[7 * p + k];
         for (long long sm = s_lo; sm <= s_hi; ++sm) {
-            const long long wi = w0 + sm * npx + p;
+            const long long wi = (base + sm * npx + p) % P.ring;
             const float4 f0 = B.abuf[2 * wi], f1 = B.abuf[2 * wi + 1];
             f[0] += f0.x; f[1] += f0.y; f[2] += f0.z; f[6] += f0.w;
             f[3] += f1.x; f[4] += f1.y; f[5] += f1.z;
@@ -952,7 +1200,6 @@ __global__ void k_accumulate(WaveParams P, WaveBuffers B) {
     }
 }
 
-__global__ void k_next_wave(WaveParams P, WaveBuffers B) { B.wave[0] += P.capacity; }
 
 // Mean first-hit features of the film: albedo W*H*3, normal W*H*3, 1/(1+t) W*H.
 __global__ void k_aov_out(const float* __restrict__ aov, long long npx, double count, float* albedo, float* normal,
@@ -1200,14 +1447,15 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     const float4* texels;
     if (n > 1)
         for (int i = 0; i < n; ++i)
-            if (scenes[i]->n_inst > 0)
-                return E.fail(SALTY_ERR_INVALID_ARG, "scene %d of the batch holds instances: render it with salty_render",
-                              i);
+            if (scenes[i]->n_inst > 0 || scenes[i]->n_sph > 0)
+                return E.fail(SALTY_ERR_INVALID_ARG,
+                              "scene %d of the batch holds instances or spheres: render it with salty_render", i);
     if (n == 1) {
         tgt.nodes = scenes[0]->bvh.nodes.p;
         tgt.tris = scenes[0]->bvh.tris.p;
         tgt.depth = scenes[0]->bvh.depth;
         tgt.inst = scenes[0]->n_inst > 0 ? scenes[0]->inst_rec.p : nullptr;
+        tgt.sph_base = scenes[0]->n_sph > 0 ? (int)scenes[0]->n_tris : kNoSpheres;
         pos = scenes[0]->pos.p;
         nrm = scenes[0]->nrm.p;
         uv = scenes[0]->uv.p;
@@ -1290,9 +1538,18 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     SALTY_TRY_CUDA(E, cudaMemcpyAsync(dslots, slots.data(), slot_bytes, cudaMemcpyHostToDevice, st));
     SALTY_TRY_CUDA(E, cudaMemcpyAsync(doffs, offs.data(), off_bytes, cudaMemcpyHostToDevice, st));
 
-    // queues
+    // queues: `cap` paths in flight; per-sample buffers (radiance, first-hit features) for
+    // `ring` samples, in chunks of `chunk` that enter the films in sample order
     const Tuning& T = ctx->tune;
     const long long cap = std::min<long long>(samples, T.wave_paths);
+    const long long chunk = std::max<long long>(1, cap / 2);
+    const long long chunks_total = (samples + chunk - 1) / chunk;
+    // enough chunks for the samples started during a path's lifetime (max_depth iterations,
+    // about half a queue each), at most kMaxRingChunks and 2^27 samples (6.4 GB)
+    const int ring_chunks = (int)std::max<long long>(
+        1, std::min<long long>({chunks_total, kMaxRingChunks, (long long)max_depth + 2,
+                                std::max<long long>(2, (1ll << 27) / chunk)}));
+    const long long ring = chunk * ring_chunks;
     WaveStore& S = ctx->waves;
     const bool batch = n > 1;
     for (int i = 0; i < 2; ++i) {
@@ -1307,16 +1564,14 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     SALTY_TRY_CUDA(E, S.nee.ensure(cap * 2));
     SALTY_TRY_CUDA(E, S.srays.ensure(cap * 4));
     SALTY_TRY_CUDA(E, S.shits.ensure(cap * 2));
-    SALTY_TRY_CUDA(E, S.lbuf.ensure(cap));
-    SALTY_TRY_CUDA(E, S.abuf.ensure(cap * 2));
+    SALTY_TRY_CUDA(E, S.lbuf.ensure(ring));
+    SALTY_TRY_CUDA(E, S.abuf.ensure(ring * 2));
     SALTY_TRY_CUDA(E, S.counts.ensure(8));
-    SALTY_TRY_CUDA(E, S.wave.ensure(1));
+    SALTY_TRY_CUDA(E, S.ctl.ensure(kCtlWords));
+    SALTY_TRY_CUDA(E, S.done.ensure(kMaxRingChunks));
     SALTY_TRY_CUDA(E, S.stats.ensure(4));
     SALTY_TRY_CUDA(E, S.tc0.ensure(4));
     SALTY_TRY_CUDA(E, S.tc1.ensure(4));
-    SALTY_TRY_CUDA(E, cudaMemsetAsync(S.counts.p, 0, 8 * sizeof(int), st));
-    SALTY_TRY_CUDA(E, cudaMemsetAsync(S.wave.p, 0, sizeof(long long), st));
-    SALTY_TRY_CUDA(E, cudaMemsetAsync(S.stats.p, 0, 4 * sizeof(unsigned long long), st));
     SALTY_TRY_CUDA(E, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), st));
 
     WaveParams P;
@@ -1334,8 +1589,19 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     P.irec = P.n_inst ? scenes[0]->inst_rec.p : nullptr;
     P.ishade = P.n_inst ? scenes[0]->inst_shade.p : nullptr;
     P.ivbase = P.n_inst ? scenes[0]->inst_vbase.p : nullptr;
+    const bool sph = n == 1 && scenes[0]->n_sph > 0;
+    P.sph = sph ? scenes[0]->sph.p : nullptr;
+    P.sph_mat = sph ? scenes[0]->sph_mat.p : nullptr;
+    P.sph_lights = sph ? scenes[0]->sph_lights.p : nullptr;
     P.n_slots = n;
     P.capacity = (int)cap;
+    P.chunk = (int)chunk;
+    P.ring = ring;
+    P.ring_chunks = ring_chunks;
+    P.launch_iters = kLaunchIters;
+    // every path ends within max_depth iterations of its start, and an iteration that finds
+    // the queue empty starts at least one chunk's samples: a bound with a margin of 2
+    P.iter_limit = 2 * (chunks_total + 2) * (long long)(max_depth + 2);
     P.total_samples = samples;
 
     WaveBuffers B;
@@ -1352,7 +1618,8 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     B.lbuf = S.lbuf.p;
     B.abuf = S.abuf.p;
     B.counts = S.counts.p;
-    B.wave = S.wave.p;
+    B.ctl = S.ctl.p;
+    B.done = S.done.p;
     B.stats = S.stats.p;
 
     const bool compat = opts[0].profile == SALTY_PROFILE_COMPAT;
@@ -1360,58 +1627,106 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     const uint32_t sh_flags = compat ? 0u : (uint32_t)(SALTY_TRACE_WATERTIGHT | SALTY_TRACE_ANY_HIT);
     const int sb = T.shade_block;
     const int sgrid = grid_of(cap, 2048 / sb, ctx->num_sms, sb);
+    const int agrid = grid_of(std::min<long long>(pixels, ring), 2048 / 256, ctx->num_sms);
     TraceTarget ext = tgt, shd = tgt;
-    ext.roots = B.roots[0];
     shd.roots = B.sroots;
+
+    // The render is one CUDA graph: a conditional while-node whose body runs two
+    // iterations (queue 0, then queue 1) of
+    //   generate new samples into the free queue slots -> extension rays -> NEE ->
+    //   shadow rays -> BSDF sampling and compaction into the other queue ->
+    //   accumulate the chunks whose samples have all ended -> plan the next generation,
+    // and repeats while samples remain (at most kLaunchIters iterations per launch, so a
+    // cancellation is seen between launches).  Every path lives in the queue until it
+    // ends, so each launch of the traversal sees a full queue instead of the shrinking
+    // depth levels of a fixed wave.
+    // SALTY_RENDER_HOST_LOOP=1 launches the same iterations from a host loop instead (16 per
+    // step): the kernels inside a conditional graph body are invisible to some profilers.
+    const char* hl = std::getenv("SALTY_RENDER_HOST_LOOP");
+    const bool host_loop = hl && std::atoi(hl) != 0;
+    cudaGraphConditionalHandle more = 0;
+    auto iteration_pair = [&](bool in_graph) -> salty_status {
+        for (int q = 0; q < 2; ++q) {
+            k_generate<<<sgrid, sb, 0, st>>>(P, B, q);
+            ext.roots = B.roots[q];
+            SALTY_TRY(trace_launch(ctx, ext, T.trace, B.rays[q], cap, &B.counts[q], ext_flags, B.hits, S.tc0.p, st,
+                                   ctx->status.p));
+            k_shade1<<<sgrid, sb, 0, st>>>(P, B, q);
+            SALTY_TRY(trace_launch(ctx, shd, T.trace, B.srays, 2 * cap, &B.counts[2], sh_flags, B.shits, S.tc1.p, st,
+                                   ctx->status.p));
+            k_shade2<<<sgrid, sb, 0, st>>>(P, B, q);
+            k_iter_end<<<1, 1, 0, st>>>(P, B, q);
+            k_accumulate<<<agrid, 256, 0, st>>>(P, B);
+            k_iter_next<<<1, 1, 0, st>>>(P, B, q, more, in_graph && q == 1 ? 1 : 0);
+        }
+        return SALTY_OK;
+    };
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    struct GraphGuard {
+        cudaGraph_t& g;
+        cudaGraphExec_t& x;
+        ~GraphGuard() {
+            if (x) cudaGraphExecDestroy(x);
+            if (g) cudaGraphDestroy(g);
+        }
+    } guard{graph, exec};
+    if (!host_loop) {
+        SALTY_TRY_CUDA(E, cudaGraphCreate(&graph, 0));
+        SALTY_TRY_CUDA(E, cudaGraphConditionalHandleCreate(&more, graph, 1, cudaGraphCondAssignDefault));
+        cudaGraphNode_t begin_node, loop_node;
+        {
+            cudaKernelNodeParams kp{};
+            void* args[] = {&P, &B};
+            kp.func = reinterpret_cast<void*>(k_launch_begin);
+            kp.gridDim = dim3(1);
+            kp.blockDim = dim3(1);
+            kp.kernelParams = args;
+            SALTY_TRY_CUDA(E, cudaGraphAddKernelNode(&begin_node, graph, nullptr, 0, &kp));
+        }
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = more;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        SALTY_TRY_CUDA(E, cudaGraphAddNode(&loop_node, graph, &begin_node, nullptr, 1, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        SALTY_TRY_CUDA(E, cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
+                                                        cudaStreamCaptureModeThreadLocal));
+        const salty_status cap_status = iteration_pair(true);
+        cudaGraph_t captured = body;
+        cudaError_t ce = cudaStreamEndCapture(st, &captured);
+        if (cap_status != SALTY_OK) return cap_status;
+        SALTY_TRY_CUDA(E, ce);
+        SALTY_TRY_CUDA(E, cudaGraphInstantiate(&exec, graph, 0));
+    }
 
     cudaEvent_t e0 = ctx->ev[0], e1 = ctx->ev[1];
     SALTY_TRY_CUDA(E, cudaEventRecord(e0, st));
-    // one wave as a CUDA graph
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    SALTY_TRY_CUDA(E, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    salty_status cap_status = SALTY_OK;
-    do {
-        k_generate<<<sgrid, sb, 0, st>>>(P, B);
-        int q = 0;
-        for (int depth = 0; depth < max_depth; ++depth) {
-            ext.roots = B.roots[q];
-            cap_status = trace_launch(ctx, ext, T.trace, B.rays[q], cap, &B.counts[q], ext_flags, B.hits, S.tc0.p, st,
-                                      ctx->status.p);
-            if (cap_status != SALTY_OK) break;
-            k_shade1<<<sgrid, sb, 0, st>>>(P, B, q);
-            cap_status = trace_launch(ctx, shd, T.trace, B.srays, 2 * cap, &B.counts[2], sh_flags, B.shits, S.tc1.p,
-                                      st, ctx->status.p);
-            if (cap_status != SALTY_OK) break;
-            k_shade2<<<sgrid, sb, 0, st>>>(P, B, q, depth);
-            k_count_rays<<<1, 1, 0, st>>>(B, q);
-            k_reset_queue<<<1, 1, 0, st>>>(B, q);
-            q ^= 1;
-        }
-        if (cap_status != SALTY_OK) break;
-        k_accumulate<<<grid_of(std::min<long long>(pixels, cap), 2048 / 256, ctx->num_sms), 256, 0, st>>>(P, B);
-        k_next_wave<<<1, 1, 0, st>>>(P, B);
-    } while (0);
-    cudaError_t ce = cudaStreamEndCapture(st, &graph);
-    if (cap_status != SALTY_OK) {
-        if (graph) cudaGraphDestroy(graph);
-        return cap_status;
-    }
-    SALTY_TRY_CUDA(E, ce);
-    SALTY_TRY_CUDA(E, cudaGraphInstantiate(&exec, graph, 0));
-    const long long waves = (samples + cap - 1) / cap;
+    k_render_init<<<1, 1, 0, st>>>(P, B);
     salty_status rs = SALTY_OK;
-    for (long long w = 0; w < waves; ++w) {
+    long long hc[kCtlWords];
+    const int pairs_per_step = 8;
+    const long long max_launches = P.iter_limit / (host_loop ? 2 * pairs_per_step : kLaunchIters) + 2;
+    for (long long launch = 0;; ++launch) {
+        if (launch > max_launches) { rs = E.fail(SALTY_ERR_TIMEOUT, "render made no progress"); break; }
+        if (host_loop) {
+            k_launch_begin<<<1, 1, 0, st>>>(P, B);
+            for (int k = 0; k < pairs_per_step && rs == SALTY_OK; ++k) rs = iteration_pair(false);
+            if (rs != SALTY_OK) break;
+        } else {
+            cudaError_t le = cudaGraphLaunch(exec, st);
+            if (le != cudaSuccess) { rs = E.fail(SALTY_ERR_CUDA, "graph launch: %s", cudaGetErrorString(le)); break; }
+        }
+        cudaError_t re = cudaMemcpyAsync(hc, B.ctl, sizeof hc, cudaMemcpyDeviceToHost, st);
+        if (re == cudaSuccess) re = cudaStreamSynchronize(st);
+        if (re != cudaSuccess) { rs = E.fail(SALTY_ERR_CUDA, "render: %s", cudaGetErrorString(re)); break; }
+        if (hc[kStuck]) { rs = E.fail(SALTY_ERR_TIMEOUT, "render made no progress in %lld iterations", hc[kIters]); break; }
+        if (hc[kAccBase] >= samples) break;
         if (ctx->cancel) { rs = E.fail(SALTY_ERR_CANCELLED, "render cancelled"); break; }
-        cudaError_t le = cudaGraphLaunch(exec, st);
-        if (le != cudaSuccess) { rs = E.fail(SALTY_ERR_CUDA, "graph launch: %s", cudaGetErrorString(le)); break; }
-        if ((w & 7) == 7) cudaStreamSynchronize(st);
     }
     SALTY_TRY_CUDA(E, cudaEventRecord(e1, st));
-    cudaError_t se = cudaEventSynchronize(e1);
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
-    SALTY_TRY_CUDA(E, se);
+    SALTY_TRY_CUDA(E, cudaEventSynchronize(e1));
     SALTY_TRY_CUDA(E, cudaGetLastError());
     if (rs != SALTY_OK) return rs;
     int status = 0;

@@ -28,12 +28,13 @@ constexpr int kMaxStack = 63;  // stack entries per thread: BVHs up to 31 levels
 // Stack entry (.y) that marks where a ray entered an instance.
 constexpr unsigned kInstMarker = 0x40000000u;
 
-template <bool ANY, bool WT, bool COUNT, int TB, bool CAP, bool INST>
+// SPH: leaf entries with ids from sph_base on are spheres (sphere.cu).
+template <bool ANY, bool WT, bool COUNT, int TB, bool CAP, bool INST, bool SPH>
 __global__ void __launch_bounds__(TB, CAP ? 1280 / TB : 1024 / TB)
 k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, const float4* __restrict__ rays,
         const int* __restrict__ roots, long long n_arg, const int* __restrict__ n_dev, float4* __restrict__ hits,
         unsigned long long* __restrict__ counters, float cull_slack, int pool, int postpone, int depth,
-        int* __restrict__ status, const InstRec* __restrict__ inst) {
+        int* __restrict__ status, const InstRec* __restrict__ inst, int sph_base) {
     extern __shared__ uint2 sstack[];
     TravStack st{sstack + threadIdx.x, TB, depth};
     const int lane = threadIdx.x & 31;
@@ -120,7 +121,7 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
             run = false;
         }
         bool done = false;
-        if (run) done = trav_tri_step<ANY, WT, COUNT>(s, tris, r, cull_slack, cnt, vbase);
+        if (run) done = trav_tri_step<ANY, WT, COUNT, SPH>(s, tris, r, cull_slack, cnt, vbase, sph_base);
         bool more = true;
         if (INST && active && !done && !s.ng_hits && !s.tg_hits && s.sp > 0 &&
             st.at(s.sp - 1).y == kInstMarker) {
@@ -165,9 +166,9 @@ struct Launch {
     int* status;
 };
 
-template <bool ANY, bool WT, bool COUNT, int TB, bool CAP, bool INST>
+template <bool ANY, bool WT, bool COUNT, int TB, bool CAP, bool INST, bool SPH = false>
 salty_status launch(salty_ctx* ctx, const Launch& L) {
-    auto kern = k_trace<ANY, WT, COUNT, TB, CAP, INST>;
+    auto kern = k_trace<ANY, WT, COUNT, TB, CAP, INST, SPH>;
     const size_t smem = (size_t)L.depth * TB * sizeof(uint2);
     if (smem > 48 * 1024)
         SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -180,7 +181,7 @@ salty_status launch(salty_ctx* ctx, const Launch& L) {
     if (grid < 1) grid = 1;
     kern<<<(unsigned)grid, TB, smem, L.st>>>(L.tgt.nodes, L.tgt.tris, L.rays, L.tgt.roots, L.n, L.n_dev, L.hits,
                                              L.counters, L.slack, L.pool, L.postpone, L.depth, L.status,
-                                             L.tgt.inst);
+                                             L.tgt.inst, L.tgt.sph_base);
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;
 }
@@ -206,9 +207,26 @@ salty_status dispatch_inst(salty_ctx* ctx, const Launch& L, uint32_t flags) {
     return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad trace flags");
 }
 
+// Scenes with spheres, at the register budget of 64.
+template <int TB>
+salty_status dispatch_sph(salty_ctx* ctx, const Launch& L, uint32_t flags) {
+    const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT;
+#define SALTY_L(A, W) \
+    if (any == A && wt == W) return launch<A, W, false, TB, false, false, true>(ctx, L)
+    SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
+#undef SALTY_L
+    return ctx->err.fail(SALTY_ERR_INVALID_ARG, "bad trace flags");
+}
+
 // Counting walks (node and triangle fetches) use the default launch shape.
 salty_status dispatch_count(salty_ctx* ctx, const Launch& L, uint32_t flags) {
     const bool any = flags & SALTY_TRACE_ANY_HIT, wt = flags & SALTY_TRACE_WATERTIGHT;
+    if (L.tgt.sph_base != kNoSpheres) {
+#define SALTY_L(A, W) \
+    if (any == A && wt == W) return launch<A, W, true, 128, false, false, true>(ctx, L)
+        SALTY_L(false, false); SALTY_L(false, true); SALTY_L(true, false); SALTY_L(true, true);
+#undef SALTY_L
+    }
     if (L.tgt.inst) {
 #define SALTY_L(A, W) \
     if (any == A && wt == W) return launch<A, W, true, 128, false, true>(ctx, L)
@@ -239,6 +257,11 @@ salty_status trace_launch(salty_ctx* ctx, const TraceTarget& tgt, const TraceTun
     Launch L{tgt, d_rays, n, n_dev, d_hits, d_counters, st, wt ? (1.0f / 65536.0f) : 1e-3f,
              tune.pool >= 32 ? tune.pool : 32, tune.postpone, need, d_status};
     if (flags & SALTY_TRACE_COUNTERS) return dispatch_count(ctx, L, flags);
+    if (tgt.sph_base != kNoSpheres) {
+        if (tune.block == 64) return dispatch_sph<64>(ctx, L, flags);
+        if (tune.block == 256) return dispatch_sph<256>(ctx, L, flags);
+        return dispatch_sph<128>(ctx, L, flags);
+    }
     if (tgt.inst) {
         if (tune.block == 64) return dispatch_inst<64>(ctx, L, flags);
         if (tune.block == 256) return dispatch_inst<256>(ctx, L, flags);
@@ -260,6 +283,7 @@ salty_status trace_launch(salty_ctx* ctx, salty_scene* sc, const float4* d_rays,
     t.tris = sc->bvh.tris.p;
     t.depth = sc->bvh.depth;
     t.inst = sc->n_inst > 0 ? sc->inst_rec.p : nullptr;
+    t.sph_base = sc->n_sph > 0 ? (int)sc->n_tris : kNoSpheres;
     return trace_launch(ctx, t, ctx->tune.trace, d_rays, n, n_dev, flags, d_hits, d_counters, st, d_status);
 }
 

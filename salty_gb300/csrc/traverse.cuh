@@ -155,6 +155,46 @@ __device__ __forceinline__ bool tri_watertight(const TravRay& r, float4 a, float
     return true;
 }
 
+// ---------------------------------------------------------------- sphere tests
+// Sphere::IsHit (src/s3d_sphere.cpp:66-92) operation for operation: po = c - o,
+// b = po.d, D4 = b^2 - po.po + r^2, roots b -/+ sqrt(D4); the nearer root above tmin,
+// else the farther (the direction is taken as unit, as the reference does).
+__device__ __forceinline__ bool sph_ref(const TravRay& r, float4 c, float rad, float tmin, float tmax, float& t) {
+    const float px = __fsub_rn(c.x, r.ox), py = __fsub_rn(c.y, r.oy), pz = __fsub_rn(c.z, r.oz);
+    const float b = __fadd_rn(__fadd_rn(__fmul_rn(px, r.dx), __fmul_rn(py, r.dy)), __fmul_rn(pz, r.dz));
+    const float pp = __fadd_rn(__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)), __fmul_rn(pz, pz));
+    const float D4 = __fadd_rn(__fsub_rn(__fmul_rn(b, b), pp), __fmul_rn(rad, rad));
+    if (D4 < 0.0f) return false;
+    const float sq = __fsqrt_rn(D4);
+    const float t1 = __fsub_rn(b, sq), t2 = __fadd_rn(b, sq);
+    if (t1 < tmin && t2 < tmin) return false;
+    t = t1 > tmin ? t1 : t2;
+    return t <= tmax;
+}
+
+// The same intersection without the cancellation of b^2 - po.po for small or distant
+// spheres (Haines, Guenther, Akenine-Moller, "Precision Improvements for Ray/Sphere
+// Intersection", Ray Tracing Gems, 2019): the discriminant from the distance between the
+// centre and the ray's closest point, the roots from the stable quadratic formula; any
+// direction length.
+__device__ __forceinline__ bool sph_robust(const TravRay& r, float4 c, float rad, float tmin, float tmax, float& t) {
+    const float fx = r.ox - c.x, fy = r.oy - c.y, fz = r.oz - c.z;
+    const float a = r.dx * r.dx + r.dy * r.dy + r.dz * r.dz;
+    const float b = -(fx * r.dx + fy * r.dy + fz * r.dz);  // half of -B
+    const float k = b / a;
+    const float lx = fx + k * r.dx, ly = fy + k * r.dy, lz = fz + k * r.dz;
+    const float disc = a * (rad * rad - (lx * lx + ly * ly + lz * lz));
+    if (disc < 0.0f) return false;
+    // roots (b +- sqrt(disc)) / a: the one without cancellation first, the other from
+    // their product cc / a
+    const float cc = fx * fx + fy * fy + fz * fz - rad * rad;
+    const float q = b + copysignf(sqrtf(disc), b);
+    float t0 = q / a, t1 = q != 0.0f ? cc / q : t0;
+    if (t0 > t1) { const float x = t0; t0 = t1; t1 = x; }
+    t = t0 >= tmin ? t0 : t1;
+    return t >= tmin && t <= tmax;
+}
+
 // Byte k of w as a float: the byte is placed under the exponent of 2^23 (one byte
 // permute) and 2^23 is subtracted (one add) -- exact for 0..255.
 __device__ __forceinline__ float u8f(unsigned w, int k) {
@@ -286,9 +326,11 @@ __device__ __forceinline__ void trav_node_step(TravState& s, const Bvh8Node* __r
 // lowest id; boxes are then culled beyond t * (1 + cull_slack), a relative margin over
 // the triangle test's rounding so the answer never depends on what was culled.
 // Returns true when an any-hit query has its answer.
-template <bool ANY, bool WATERTIGHT, bool COUNT>
+// SPH: leaf entries with ids from sph_base on are spheres, (centre, id) (radius, 0, 0, 0).
+template <bool ANY, bool WATERTIGHT, bool COUNT, bool SPH = false>
 __device__ __forceinline__ bool trav_tri_step(TravState& s, const float4* __restrict__ tris, const TravRay& r,
-                                              float cull_slack, TravCount& cnt, int id_off = 0) {
+                                              float cull_slack, TravCount& cnt, int id_off = 0,
+                                              int sph_base = 0x7fffffff) {
     while (s.tg_hits) {
         const unsigned k = __ffs(s.tg_hits) - 1;
         s.tg_hits &= s.tg_hits - 1;
@@ -297,8 +339,15 @@ __device__ __forceinline__ bool trav_tri_step(TravState& s, const float4* __rest
         if (COUNT) ++cnt.tris;
         float t, u, v;
         const float tlim = ANY ? r.tmax : fminf(r.tmax, s.hit.t);
-        const bool h = WATERTIGHT ? tri_watertight(r, a, b, c, r.tmin, tlim, t, u, v)
-                                  : tri_ref(r, a, b, c, r.tmin, r.tmax, tlim, t, u, v);
+        bool h;
+        if (SPH && __float_as_int(a.w) >= sph_base) {
+            h = WATERTIGHT ? sph_robust(r, a, b.x, r.tmin, tlim, t) : sph_ref(r, a, b.x, r.tmin, tlim, t);
+            u = 0.0f;
+            v = 0.0f;
+        } else {
+            h = WATERTIGHT ? tri_watertight(r, a, b, c, r.tmin, tlim, t, u, v)
+                           : tri_ref(r, a, b, c, r.tmin, r.tmax, tlim, t, u, v);
+        }
         if (h) {
             const int id = __float_as_int(a.w) + id_off;  // an instance's first virtual id
             if (t < s.hit.t || (t == s.hit.t && id < s.hit.id)) {

@@ -20,11 +20,13 @@
 //                 of the shifted input into fragments with pixels along K; a CTA covers all
 //                 nine taps of a 16-channel input slice (one dY fragment serves nine taps),
 //                 sums its pixel tiles in registers and adds the partial into FP32 gradients.
-// The forward and backward-data convolutions run by default on tcgen05 (conv_tc.cu: TMEM
-// accumulators, 128-pixel strips; inputs in one tensor staged by TMA in a persistent
-// warp-specialised kernel, the decoder's two-source inputs by cp.async); the mma.sync kernel
-// below stays selectable (salty_unet_set_conv_kernel) and is the reference the tcgen05
-// kernels are tested against.
+// All three convolutions run by default on tcgen05 (conv_tc.cu: TMEM accumulators; the
+// forward and backward-data ones over 128-pixel strips, inputs in one tensor staged by TMA
+// in a persistent warp-specialised kernel, the decoder's two-source inputs by cp.async; the
+// weight gradient over strips of 2 rows x 64 pixels with dY transposed as the MMA's A, the
+// input's halo as B and the taps as descriptor offsets, summed over CTAs in a fixed order);
+// the mma.sync kernels below stay selectable (salty_unet_set_conv_kernel) and are the
+// reference the tcgen05 kernels are tested against.
 #include <cuda_bf16.h>
 
 #include <algorithm>

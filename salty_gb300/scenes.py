@@ -58,7 +58,10 @@ def cornell(variant: str = "baseline") -> dict:
     power 120), back wall Phong (power 8).  "thinlens": the baseline box seen through a thin
     lens of radius 0.06 focused on the tall box (target z = 0.6, focal distance 2.0).
     "textured": a checkerboard colour map on the floor and back wall (TexturedMaterial) and
-    an environment map in place of the black sky, seen through the open front."""
+    an environment map in place of the black sky, seen through the open front.  "spheres":
+    the room without its boxes, holding analytic spheres (Sphere) instead -- a Lambert, a
+    mirror and a glass one and an emitting light sphere that joins the quad light in the
+    light list."""
     W, R, G = (0.75, 0.75, 0.75), (0.75, 0.25, 0.25), (0.25, 0.75, 0.25)
     mats = [{"type": LAMBERT, "color": W}, {"type": LAMBERT, "color": R}, {"type": LAMBERT, "color": G}]
     tall_m = short_m = back_m = 0
@@ -74,6 +77,10 @@ def cornell(variant: str = "baseline") -> dict:
     elif variant == "textured":
         mats += [{"type": LAMBERT, "color": (0.9, 0.9, 0.9), "texture": 0}]
         back_m = 3
+    elif variant == "spheres":
+        mats += [{"type": MIRROR, "color": (0.9, 0.9, 0.9)},
+                 {"type": GLASS, "color": (1.0, 1.0, 1.0), "ior": 1.5},
+                 {"type": LAMBERT, "color": (0.0, 0.0, 0.0), "emission": (6.0, 7.0, 9.0)}]
     elif variant == "glossy":
         mats += [{"type": PHONG, "color": (0.8, 0.8, 0.8), "power": 40.0},
                  {"type": PLASTIC, "color": (0.2, 0.4, 0.7), "specular": (0.6, 0.6, 0.6), "power": 120.0},
@@ -90,11 +97,12 @@ def cornell(variant: str = "baseline") -> dict:
     add(_quad((0, 0, 1), (0, 1, 1), (1, 1, 1), (1, 0, 1)), back_m)  # back wall, normal -z
     add(_quad((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0)), 1)      # x = 1 (image left), red
     add(_quad((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1)), 2)      # x = 0 (image right), green
-    add(_box((0.3, 0.6, 0.3), 15.0, (0.33, 0.0, 0.6)), tall_m)
-    # the specular variant lifts the glass box 2 mm off the floor: rays inside it would
-    # otherwise meet its bottom face and the floor at the same distance, a tie that floating
-    # point rounding decides differently on every machine
-    add(_box((0.3, 0.3, 0.3), -18.0, (0.66, 0.002 if variant == "specular" else 0.0, 0.35)), short_m)
+    if variant != "spheres":
+        add(_box((0.3, 0.6, 0.3), 15.0, (0.33, 0.0, 0.6)), tall_m)
+        # the specular variant lifts the glass box 2 mm off the floor: rays inside it would
+        # otherwise meet its bottom face and the floor at the same distance, a tie that
+        # floating point rounding decides differently on every machine
+        add(_box((0.3, 0.3, 0.3), -18.0, (0.66, 0.002 if variant == "specular" else 0.0, 0.35)), short_m)
     pos = np.stack(tris).reshape(-1, 9).astype(np.float32)
     g = np.cross(pos[:, 3:6] - pos[:, 0:3], pos[:, 6:9] - pos[:, 0:3])
     g /= np.linalg.norm(g, axis=1, keepdims=True)
@@ -114,6 +122,11 @@ def cornell(variant: str = "baseline") -> dict:
         ev, eu = np.mgrid[0:16, 0:32]
         env = np.stack([0.02 + 0.03 * eu / 31, 0.04 * (1 - ev / 15), 0.05 + 0.0 * eu], -1).astype(np.float32)
         extra = {"tri_uv": uv, "textures": [tex, env], "ibl": 1}
+    if variant == "spheres":
+        extra = {"spheres": [{"center": (0.7, 0.19, 0.62), "radius": 0.18, "material": 0},
+                             {"center": (0.28, 0.2, 0.55), "radius": 0.19, "material": 3},
+                             {"center": (0.52, 0.16, 0.22), "radius": 0.15, "material": 4},
+                             {"center": (0.3, 0.78, 0.35), "radius": 0.07, "material": 5, "light": True}]}
     return {
         "name": f"cornell-{variant}",
         "tri_pos": pos, "tri_nrm": nrm, "tri_mat": np.array(mid, np.int32), "materials": mats,
@@ -254,9 +267,12 @@ def heightfield(grid: int = 2048, n_spheres: int = 4096, seed: int = 2026, heigh
 
 
 def upload(ctx, scene: dict):
-    """Context.upload_scene with a scene dict from this module."""
-    kw = {k: v for k, v in scene.items() if k != "name"}
-    return ctx.upload_scene(**kw)
+    """Context.upload_scene with a scene dict from this module (and its spheres)."""
+    kw = {k: v for k, v in scene.items() if k not in ("name", "spheres")}
+    s = ctx.upload_scene(**kw)
+    if scene.get("spheres"):
+        s.set_spheres(scene["spheres"])
+    return s
 
 
 def batch_scene(seed: int) -> tuple[dict, dict]:

@@ -86,12 +86,13 @@ def icosphere_tris(subdiv: int = 3, radius: float = 1.0):
     return (_icosphere(subdiv) * radius).astype(np.float32).reshape(-1, 9)
 
 
-def scene(tris, mats, mat_ids=None, *, camera, sky=(0, 0, 0), sun=None, light=None, textures=(), ibl=None):
+def scene(tris, mats, mat_ids=None, *, camera, sky=(0, 0, 0), sun=None, light=None, textures=(), ibl=None,
+          spheres=()):
     n = tris.shape[0]
     return {"tri_pos": np.ascontiguousarray(tris, np.float32), "tri_nrm": None,
             "tri_mat": np.zeros(n, np.int32) if mat_ids is None else np.asarray(mat_ids, np.int32),
             "materials": mats, "light": light, "sun": sun, "sky": tuple(sky), "camera": camera,
-            "textures": list(textures), "ibl": ibl, "ibl_scale": 1.0}
+            "textures": list(textures), "ibl": ibl, "ibl_scale": 1.0, "spheres": list(spheres)}
 
 
 LOOK_DOWN = {"pos": (0.0, 1.0, -2.0), "target": (0.0, 0.0, 0.0), "up": (0.0, 1.0, 0.0),
@@ -145,6 +146,38 @@ def area_light_plane(albedo, le, width, height, sub=6):
     # no camera ray may reach the light's plane (y = 1) before the floor
     assert np.all(dirs[..., 1] < 0)
     e = polygon_irradiance(plane_hits(pos, dirs), verts).mean(-1)
+    return sc, (np.asarray(albedo, float) * np.asarray(le, float) / math.pi)[None, None, :] * e[..., None]
+
+
+def sphere_light_plane(albedo, le, width, height, with_quad=False, sub=6):
+    """A Lambert plane under a light sphere of radiance le (and, with_quad, also under the
+    quad light of area_light_plane, the two sharing the light list).  A sphere of radius R
+    whose centre is at distance d and angle theta from the normal, wholly above the horizon,
+    gives the irradiance E = pi le (R / d)^2 cos theta; reflected radiance albedo E / pi."""
+    c, R = np.array([0.85, 0.9, 0.5]), 0.2  # clear of the quad light and its light paths
+    mats = [{"type": LAMBERT, "color": albedo},
+            {"type": LAMBERT, "color": (0.0, 0.0, 0.0), "emission": tuple(le)}]
+    light = None
+    if with_quad:
+        light = {"corner": (-0.3, 1.0, -0.2), "edge_a": (0.6, 0.0, 0.0), "edge_b": (0.0, 0.0, 0.5),
+                 "emission": tuple(le)}
+    cam = {"pos": (0.0, 0.6, -2.5), "target": (0.0, 0.0, 0.2), "up": (0.0, 1.0, 0.0),
+           "fov": 2.0 * math.tan(math.radians(12.0)), "near": 1.0}
+    sc = scene(plane_tris(), mats, camera=cam, light=light,
+               spheres=[{"center": tuple(c), "radius": R, "material": 1, "light": True}])
+    pos, dirs = pixel_dirs(cam, width, height, sub)
+    assert np.all(dirs[..., 1] < 0) and c[1] - R > cam["pos"][1]  # the camera sees only the floor
+    x = plane_hits(pos, dirs)
+    w = c - x
+    d2 = np.sum(w * w, -1)
+    cos_t = w[..., 1] / np.sqrt(d2)
+    assert np.all(cos_t > R / np.sqrt(d2))  # the whole sphere above the horizon
+    e = (math.pi * R * R / d2 * cos_t).mean(-1)
+    if with_quad:
+        verts = np.stack([np.asarray(light["corner"]), np.asarray(light["corner"]) + np.asarray(light["edge_a"]),
+                          np.asarray(light["corner"]) + np.asarray(light["edge_a"]) + np.asarray(light["edge_b"]),
+                          np.asarray(light["corner"]) + np.asarray(light["edge_b"])])
+        e = e + polygon_irradiance(x, verts).mean(-1)
     return sc, (np.asarray(albedo, float) * np.asarray(le, float) / math.pi)[None, None, :] * e[..., None]
 
 

@@ -83,7 +83,7 @@ def cornell_scene(variant: str = "baseline") -> SceneData:
     sc = scenes.cornell(variant)
     return SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], None,
                      sc["sky"], sc["camera"], tri_uv=sc.get("tri_uv"), textures=sc.get("textures", []),
-                     ibl=sc.get("ibl"))
+                     ibl=sc.get("ibl"), spheres=sc.get("spheres", []))
 
 
 def hdr_image(seed: int, w: int, h: int) -> np.ndarray:
@@ -148,11 +148,42 @@ def specular_fixture(r) -> None:
     print(f"specular cornell reference render: {secs:.2f} s")
 
 
+def spheres_fixture(r) -> None:
+    """Analytic spheres (Sphere::IsHit/CalcParam/Sample): Lambert, mirror and glass spheres
+    and a light sphere sharing the light list with the quad light."""
+    sc = cornell_scene("spheres")
+    W = H = 48
+    spp, depth = 4096, 8
+    total, sq, secs = r.render(sc, W, H, spp, depth, seed=7171)
+    mean = total / spp
+    var = (sq / spp - mean * mean) * spp / (spp - 1) / spp
+    np.savez_compressed(os.path.join(HERE, "cornell_spheres_ref_48.npz"), mean=mean.astype(np.float32),
+                        var=np.maximum(var, 0).astype(np.float32), spp=spp, max_bounce=depth, width=W, height=H)
+    print(f"sphere cornell reference render: {secs:.2f} s")
+
+
+def c1_fixture(r) -> None:
+    """The Cornell frame as configured for the CPU-runnable benchmark case: 256x256, max
+    depth 8, the reference's estimator; 1024 samples per pixel (64 of the configured 16-spp
+    frames) so that a per-pixel comparison has power.  Mean and standard error of the mean
+    stored as float16 (relative precision 5e-4, far below the noise)."""
+    sc = cornell_scene()
+    W = H = 256
+    spp, depth = 1024, 8
+    total, sq, secs = r.render(sc, W, H, spp, depth, seed=16016)
+    mean = total / spp
+    var = (sq / spp - mean * mean) * spp / (spp - 1) / spp
+    np.savez_compressed(os.path.join(HERE, "cornell_c1_ref_256.npz"), mean=mean.astype(np.float16),
+                        sem=np.sqrt(np.maximum(var, 0)).astype(np.float16), spp=spp, max_bounce=depth,
+                        width=W, height=H)
+    print(f"configured cornell frame: {secs:.2f} s")
+
+
 def main() -> None:
     build(with_reference=True)
     o, r = Oracle(), Reference()
     only = {"glossy": glossy_fixture, "thinlens": thinlens_fixture, "textured": textured_fixture,
-            "specular": specular_fixture}
+            "specular": specular_fixture, "c1": c1_fixture, "spheres": spheres_fixture}
     if sys.argv[1:] and all(a in only for a in sys.argv[1:]):
         for a in sys.argv[1:]:
             only[a](r)
@@ -192,6 +223,8 @@ def main() -> None:
     thinlens_fixture(r)
     textured_fixture(r)
     specular_fixture(r)
+    c1_fixture(r)
+    spheres_fixture(r)
 
     # 4. tonemapping and the sRGB8 capture
     img = hdr_image(99, 48, 32)

@@ -120,3 +120,15 @@ def test_batch_rejects_bad_input(ctx, batch):
         ctx.render_batch(ss[:2], [opts[0], dict(opts[1], profile=salty_gb300.PROFILE_COMPAT)])
     with pytest.raises(salty_gb300.SaltyError):
         ctx.tuning = {"trace_block": 100}
+
+
+def test_host_loop_renders_the_same_films(ctx, batch, monkeypatch):
+    """SALTY_RENDER_HOST_LOOP=1 launches the path loop's iterations from the host instead of
+    one conditional CUDA graph (for profilers that cannot see into graph bodies): the same
+    kernels in the same order, so the films are identical."""
+    ss, opts = batch
+    ctx.render_batch(ss, opts)
+    ref = _films(ss, opts)
+    monkeypatch.setenv("SALTY_RENDER_HOST_LOOP", "1")
+    ctx.render_batch(ss, opts)
+    _same(_films(ss, opts), ref)

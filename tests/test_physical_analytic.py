@@ -5,8 +5,9 @@ principles: white furnaces (energy conservation with and without Russian roulett
 Lambert, mirror and glass), a Lambert plane under sky and sun (delta and disk, the disk
 combined with BSDF sampling by MIS), a Lambert plane under the quad light (next-event
 estimation and BSDF hits of the light, MIS), the exact Fresnel reflectance of a glass plane
-under a half sky, and GGX planes whose BSDF is integrated by quadrature (under the sky, and
-under a disk sun through MIS).  Every pixel must agree with its expectation within the
+under a half sky, GGX planes whose BSDF is integrated by quadrature (under the sky, and
+under a disk sun through MIS), and a Lambert plane under a light sphere (cone sampling and
+BSDF hits combined by MIS), alone and sharing the light list with the quad light.  Every pixel must agree with its expectation within the
 3-sigma Monte Carlo bound of tests/analytic.check.
 
 The oracle's physical path is checked here on the CPU at a small size; the CUDA path
@@ -33,6 +34,9 @@ CASES = {
                                                       (2.0, 1.5, 1.0), 0.08), 4, 4),
     "lambert-area-light": (lambda w, h: A.area_light_plane((0.6, 0.5, 0.4), (4.0, 3.0, 2.0), w, h), 4, 4),
     "glass-fresnel": (lambda w, h: A.glass_plane(1.5, w, h), 4, 4),
+    "lambert-sphere-light": (lambda w, h: A.sphere_light_plane((0.6, 0.5, 0.4), (4.0, 3.0, 2.0), w, h), 4, 4),
+    "lambert-sphere-and-quad-lights": (lambda w, h: A.sphere_light_plane((0.6, 0.5, 0.4), (4.0, 3.0, 2.0), w, h,
+                                                                         with_quad=True), 4, 4),
     "ggx-sky-r05": (lambda w, h: A.ggx_plane((0.9, 0.7, 0.5), 0.5, w, h), 4, 4),
     "ggx-sky-r035": (lambda w, h: A.ggx_plane((0.95, 0.8, 0.6), 0.35, w, h), 4, 4),
     "ggx-disk-sun": (lambda w, h: A.ggx_plane((0.9, 0.7, 0.5), 0.5, w, h, sky=(0.0, 0.0, 0.0),
@@ -43,7 +47,8 @@ CASES = {
 def _oracle_scene(sc):
     from oracle.oracle import SceneData
     return SceneData(sc["tri_pos"], sc["tri_nrm"], sc["tri_mat"], sc["materials"], sc["light"], sc["sun"],
-                     sc["sky"], sc["camera"], textures=sc["textures"], ibl=sc["ibl"], ibl_scale=sc["ibl_scale"])
+                     sc["sky"], sc["camera"], textures=sc["textures"], ibl=sc["ibl"], ibl_scale=sc["ibl_scale"],
+                     spheres=sc.get("spheres", []))
 
 
 @pytest.mark.parametrize("name", list(CASES))

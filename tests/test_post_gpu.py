@@ -59,3 +59,27 @@ def test_variance_nlm_matches_oracle(ctx, oracle):
     ref = oracle.nlm_var(noisy, var, 10, 3, 0.45)
     np.testing.assert_allclose(out, ref, rtol=1e-4, atol=1e-5)
     assert np.mean((out - clean) ** 2) < 0.5 * np.mean((noisy - clean) ** 2)
+
+
+@pytest.mark.parametrize("ref_oetf", [True, False])
+def test_srgb8_equals_the_exact_oetf_of_the_linear_output(ctx, ref_oetf):
+    """The sRGB8 encode takes the power from the hardware approximation and falls back to
+    powf only near a code boundary: every code must equal the all-powf formula applied to
+    the linear output (torch's CUDA pow is powf; the same IEEE operations in the same
+    order), here on 12.6M values covering every code the curve reaches (the reference's OETF
+    tops out at 1.055^(1/2.4) - 0.055, code 247)."""
+    import torch
+    rng = np.random.default_rng(21)
+    img = np.exp(rng.normal(0.0, 2.0, size=(1024, 4096, 3))).astype(np.float32)
+    out, s8, _, _ = ctx.tonemap(img, 0, srgb=True, ref_oetf=ref_oetf)
+    y = torch.from_numpy(out).cuda().clamp(0.0, 1.0)
+    e = torch.tensor(np.float32(1.0) / np.float32(2.4), device="cuda")
+    lin = y <= np.float32(0.0031308)
+    if ref_oetf:
+        v = torch.pow(y * np.float32(1.055), e) - np.float32(0.055)
+    else:
+        v = torch.pow(y, e) * np.float32(1.055) - np.float32(0.055)
+    v = torch.where(lin, y * np.float32(12.92), v)
+    want = (v * np.float32(255.0) + np.float32(0.5)).to(torch.uint8).cpu().numpy()
+    assert len(np.unique(want)) == (248 if ref_oetf else 256)
+    np.testing.assert_array_equal(s8, want)

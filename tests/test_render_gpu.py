@@ -244,7 +244,7 @@ def test_checkpoint_resume_continues_exactly(ctx, fp64):
 
 
 def test_cancel_stops_a_render_and_the_context_recovers(ctx):
-    """salty_ctx_cancel from another thread: the render stops between waves with
+    """salty_ctx_cancel from another thread: the render stops between graph launches with
     ERR_CANCELLED (a host-side stop, nothing waits on the device), and the next render works."""
     import threading
     import time
@@ -252,12 +252,12 @@ def test_cancel_stops_a_render_and_the_context_recovers(ctx):
     from salty_gb300 import scenes
     s = _gpu_scene(ctx, scenes.cornell("baseline"))
     default = ctx.tuning
-    ctx.tuning = {"wave_paths": 1 << 16}  # many waves: ~4,000 for this render
+    ctx.tuning = {"wave_paths": 1 << 16}  # 2^16 paths in flight: tens of thousands of iterations
     err = {}
 
     def run():
         try:
-            s.render(512, 512, 1024, 8, seed=1, want=())
+            s.render(512, 512, 4096, 8, seed=1, want=())
         except salty_gb300.SaltyError as e:
             err["status"] = e.status
 
