@@ -59,11 +59,11 @@ TMIN = 1e-4
 METRIC = "Mrays/s"
 CPU_SAMPLE = 2_097_152      # rays of the same stream timed on the host cores (~10 s of CPU work)
 # DRAM bytes (read + write) per ray of the closest-hit k_trace launch, from one ncu capture
-# of that kernel at the launch shape salty_autotune_trace picks here (256 threads, 64
-# registers, pool 64, postpone 7) on the same soup at 4,194,304 rays; the traffic (rays in,
-# hits out, L2 misses) scales with the ray count, so traffic per launch is this figure times
-# the rays of the launch.
-NCU_DRAM_BYTES_PER_RAY = (530.681856e6 + 69.582848e6) / 4_194_304
+# of that kernel at a launch shape salty_autotune_trace picks here (128 threads, 64
+# registers, pool 128, no triangle postponing) on the same soup at 4,194,304 rays; the
+# traffic (rays in, hits out, L2 misses) scales with the ray count, so traffic per launch is
+# this figure times the rays of the launch.
+NCU_DRAM_BYTES_PER_RAY = (366.647552e6 + 65.853440e6) / 4_194_304
 
 
 def measured_peaks_tensor() -> dict:
