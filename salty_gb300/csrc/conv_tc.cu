@@ -513,7 +513,8 @@ EncodeTiledFn tensor_map_encoder() {
 // ---------------------------------------------------------------- weight gradient
 // dW[tap][co][ci] = sum over pixels p of dY[p][co] * X[p + d(tap)][ci]: per tap a GEMM on
 // the tensor cores with the pixels as its K dimension,
-//   M = output channels (dY transposed; 128 rows, of which cout are real),
+//   M = output channels (dY transposed; 64 rows when they fit, else 128, of which cout
+//       are real),
 //   N = a chunk of up to 48 input channels (a CTA group's share), one accumulator of N
 //       TMEM columns per tap (9 x 48 <= 512),
 //   K = pixels: a strip of kWgRows image rows x 64 pixels per stage, 16 per MMA.
@@ -559,6 +560,7 @@ __device__ __forceinline__ uint32_t idesc_bf16_mn(int m, int n) {
 }
 
 struct WgradArgs {
+    int m;        // MMA rows: 128, or 64 when the output channels (cpad) fit
     int cpad, cout, cin, N, H, W;
     int strips;   // N * ceil(H / kWgRows) * ceil(W / kWgStrip)
     float* part;  // [gridDim.x slices][9][cpad][cin]
@@ -626,7 +628,7 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUt
             for (int k = 0; k < nx; ++k) tma_load_4d(xb + k * kWgXBox, &tm_x, c0 + k * 16, x0 - 1, y0 - 1, n, bar);
         }
     } else if (warp == 1 && lane == 0) {
-        const uint32_t idesc = idesc_bf16_mn(128, ch);
+        const uint32_t idesc = idesc_bf16_mn(a.m, ch);
         for (int it = 0; it < count; ++it) {
             const int b = it % kWgStages;
             if (!wait_or_abort(saddr(full + b), (uint32_t)(it / kWgStages) & 1u, abort_flag, a.status)) {
@@ -653,7 +655,9 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUt
     const bool got = count == 0 || wait_or_abort(saddr(acc), 0u, abort_flag, a.status);
     if (__all_sync(0xffffffffu, got && !*abort_flag)) {  // warp-uniform: tcgen05.ld is .aligned
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int co = warp * 32 + lane;
+        // M = 128: row i in TMEM lane i.  M = 64: rows 16w..16w+15 in lanes 32w..32w+15 of
+        // warp w's quarter (the upper 16 lanes of each quarter are unused)
+        const int co = a.m == 128 ? warp * 32 + lane : (lane < 16 ? warp * 16 + lane : a.cpad);
         float* part = a.part + (size_t)blockIdx.x * 9 * a.cpad * a.cin;
         for (int tap = 0; tap < 9; ++tap)
             for (int j = 0; j < nx; ++j) {
@@ -838,7 +842,7 @@ salty_status conv_wgrad_tc(salty_ctx* ctx, const bf16* dy, int cpad, int cout, c
         return ctx->err.fail(SALTY_ERR_CUDA, "conv_wgrad_tc: gradient tensor map");
     const size_t smem = (size_t)kWgHeader + (size_t)kWgStages * kWgStage;
     SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    WgradArgs a{cpad, cout, cin, N, H, W, strips, ws, d_status};
+    WgradArgs a{cpad <= 64 ? 64 : 128, cpad, cout, cin, N, H, W, strips, ws, d_status};
     k_wgrad_tc<<<dim3(slices, groups), kWgThreads, smem, ctx->stream>>>(tm_x, tm_dy, a);
     const long long outs = 9LL * cout * cin;
     k_wgrad_reduce<<<(unsigned)((outs + 255) / 256), 256, 0, ctx->stream>>>(ws, slices, cpad, cin, cout, dw);

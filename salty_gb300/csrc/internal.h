@@ -201,8 +201,8 @@ struct TraceTarget {
 // Launch shape of the traversal kernel, chosen by salty_autotune.
 struct TraceTuning {
     int block = 128;     // threads per block: 64, 128 or 256
-    int pool = 128;      // rays a warp takes from the global cursor per refill
-    int postpone = 7;    // fewest lanes that test a triangle group together
+    int pool = 64;       // rays a warp takes from the global cursor per refill
+    int postpone = 1;    // fewest lanes that test a triangle group together (1: never postpone)
     int regs = 64;       // register budget per thread: 64 (as compiled) or 48 (more resident warps)
 };
 
