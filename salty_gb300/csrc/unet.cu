@@ -456,52 +456,55 @@ __global__ void k_output(const bf16* __restrict__ out, const bf16* __restrict__ 
                 fmaxf(expm1f(__bfloat162float(out[p * 8 + c]) + __bfloat162float(x[p * 16 + c])), 0.0f);
 }
 
-// ReLU backward on a layer's output y: g = dy * (y > 0) in BF16 (the next GEMMs' operand),
-// with g_cs >= C channels per pixel, the extra ones zero.  One thread per pixel and 8
-// channels (C, y_cs, g_cs multiples of 8).
-__global__ void k_relu_bwd(const bf16* __restrict__ y, int y_cs, const float* __restrict__ dy, int C, int relu,
-                           long long npx, bf16* __restrict__ g, int g_cs) {
-    const int G = g_cs / 8;
-    const long long total = npx * G;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const long long p = i / G;
-        const int c = (int)(i % G) * 8;
-        float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        if (c < C) {
-            const float4* d = reinterpret_cast<const float4*>(dy + p * C + c);
-            const float4 a = __ldg(d), b = __ldg(d + 1);
-            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-            if (relu) {
-                float yv[8];
-                unpack_bf16x8(__ldg(reinterpret_cast<const uint4*>(y + p * y_cs + c)), yv);
-#pragma unroll
-                for (int k = 0; k < 8; ++k)
-                    if (!(yv[k] > 0.0f)) v[k] = 0.0f;
-            }
-        }
-        *reinterpret_cast<uint4*>(g + p * g_cs + c) = pack_bf16x8(v);
-    }
-}
-
-// bias gradient, in a fixed summation order (no atomics): a block of 256 threads takes
-// 8-channel groups j = threadIdx.x % G of the pixels r = threadIdx.x / G, r + 256 / G, ...
-// of its pixel range (threads beyond a multiple of G idle) and sums them in registers; the
-// per-thread sums are added in shared memory in thread order into the block's partial
+// ReLU backward and the bias gradient in one pass over a layer's output gradient dy:
+// g = dy * (y > 0) in BF16 (the next GEMMs' operand, channels C..g_cs-1 zero), and per block
+// the sums of g's BF16 values per channel in a fixed order (no atomics).  Thread t of a
+// block takes 8-channel group j = t % G (G = g_cs / 8) of the pixels r = t / G, r + per,
+// ... of the block's grid stride (per = blockDim / G; threads beyond per * G idle) and sums
+// in registers; the per-thread sums are added in shared memory in thread order into
 // part[blockIdx.x][c], and k_bias_reduce adds the blocks' partials in block order.
-__global__ void k_bias_grad(const bf16* __restrict__ g, int g_cs, int C, long long npx, float* __restrict__ part) {
-    extern __shared__ float sb[];  // [256 / G][C]
-    const int G = C / 8, lanes = (blockDim.x / G) * G, per = blockDim.x / G;
+// dy is FP32 [npx][C], or, when dy16 is given, BF16 with dy16_cs channels per pixel (a
+// backward-data GEMM's output read directly; widening it to FP32 first would be exact).
+// (C, y_cs, g_cs, dy16_cs multiples of 8.)
+__global__ void k_relu_bwd_bias(const bf16* __restrict__ y, int y_cs, const float* __restrict__ dy,
+                                const bf16* __restrict__ dy16, int dy16_cs, int C, int relu, long long npx,
+                                bf16* __restrict__ g, int g_cs, float* __restrict__ part) {
+    extern __shared__ float sb[];  // [per][C]
+    const int G = g_cs / 8, per = blockDim.x / G, lanes = per * G;
     if ((int)threadIdx.x < lanes) {
-        const int j = threadIdx.x % G, r = threadIdx.x / G;
+        const int j = threadIdx.x % G, r = threadIdx.x / G, c = j * 8;
         float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (long long p = (long long)blockIdx.x * per + r; p < npx; p += (long long)gridDim.x * per) {
-            float v[8];
-            unpack_bf16x8(__ldg(reinterpret_cast<const uint4*>(g + p * g_cs + j * 8)), v);
+            float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (c < C) {
+                if (dy16) {
+                    unpack_bf16x8(__ldg(reinterpret_cast<const uint4*>(dy16 + p * dy16_cs + c)), v);
+                } else {
+                    const float4* d = reinterpret_cast<const float4*>(dy + p * C + c);
+                    const float4 a = __ldg(d), b = __ldg(d + 1);
+                    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+                }
+                if (relu) {
+                    float yv[8];
+                    unpack_bf16x8(__ldg(reinterpret_cast<const uint4*>(y + p * y_cs + c)), yv);
 #pragma unroll
-            for (int k = 0; k < 8; ++k) s[k] += v[k];
+                    for (int k = 0; k < 8; ++k)
+                        if (!(yv[k] > 0.0f)) v[k] = 0.0f;
+                }
+            }
+            const uint4 pk = pack_bf16x8(v);
+            *reinterpret_cast<uint4*>(g + p * g_cs + c) = pk;
+            if (c < C) {
+                float w[8];
+                unpack_bf16x8(pk, w);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) s[k] += w[k];
+            }
         }
+        if (c < C) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) sb[r * C + j * 8 + k] = s[k];
+            for (int k = 0; k < 8; ++k) sb[r * C + c + k] = s[k];
+        }
     }
     __syncthreads();
     for (int c = threadIdx.x; c < C; c += blockDim.x) {
@@ -798,9 +801,9 @@ salty_status ensure_workspace(salty_ctx* ctx, Unet& u, int N, int H, int W) {
         const int lv = kLayerLevel[i];
         ws = std::max(ws, conv_wgrad_tc_workspace(ctx->num_sms, L.cin, L.cout_pad, N, H >> lv, W >> lv));
     }
-    // the bias gradients' per-block partials use the same workspace: up to 2 blocks per SM
+    // the bias gradients' per-block partials use the same workspace: up to 4 blocks per SM
     // x 128 channels
-    ws = std::max(ws, (size_t)ctx->num_sms * 2 * 128);
+    ws = std::max(ws, (size_t)ctx->num_sms * 4 * 128);
     SALTY_TRY_CUDA(ctx->err, u.wg_ws.ensure(ws));
     size_t cat = 0;
     for (int i = 0; i < kNumLayers; ++i)
@@ -867,16 +870,17 @@ salty_status forward(salty_ctx* ctx, Unet& u, const float* d_feat, int N, int H,
 // weight and bias gradients; leaves dL/d(input) in BF16 in F.t[T_G2] ([npx][cin]) when
 // want_dx.
 salty_status conv_backward(salty_ctx* ctx, Unet& u, Fwd& F, int li, const ConvSrc& x, int y, const float* dy, int N,
-                           int h, int w, bool want_dx) {
+                           int h, int w, bool want_dx, const bf16* dy16 = nullptr, int dy16_cs = 0) {
     const UnetLayer& L = u.layers[li];
     const long long npx = (long long)N * h * w;
     cudaStream_t st = ctx->stream;
     bf16* g = F.t[T_G];
-    k_relu_bwd<<<gsz(npx * L.cout_pad / 8), 256, 0, st>>>(F.t[y], L.cout, dy, L.cout, L.relu, npx, g, L.cout_pad);
-    // few blocks: each adds its partial sums into the C gradient words once
-    const int bias_blocks = (int)std::min<long long>((long long)ctx->num_sms * 2, (npx + 255) / 256);
-    k_bias_grad<<<bias_blocks, 256, 256 / (L.cout / 8) * L.cout * sizeof(float), st>>>(g, L.cout_pad, L.cout, npx,
-                                                                                       u.wg_ws.p);
+    // ReLU backward and the bias gradient's per-block partial sums in one pass (4 blocks per
+    // SM), then the partials added in block order
+    const int per = 256 / (L.cout_pad / 8);
+    const int bias_blocks = (int)std::min<long long>((long long)ctx->num_sms * 4, (npx + per - 1) / per);
+    k_relu_bwd_bias<<<bias_blocks, 256, (size_t)per * L.cout * sizeof(float), st>>>(
+        F.t[y], L.cout, dy, dy16, dy16_cs, L.cout, L.relu, npx, g, L.cout_pad, u.wg_ws.p);
     k_bias_reduce<<<(L.cout + 127) / 128, 128, 0, st>>>(u.wg_ws.p, bias_blocks, L.cout, u.grads.p + L.b_off);
     SALTY_TRY(launch_wgrad(ctx, u, g, L.cout_pad, L.cout, x, L.cin, u.grads.p + L.w_off, N, h, w));
     if (want_dx)
@@ -910,8 +914,7 @@ salty_status backward(salty_ctx* ctx, Unet& u, Fwd& F, const float* d_target, in
         to_f32(cc + cs, cc, cs, np, g_skip, 0);
     };
     SALTY_TRY(conv_backward(ctx, u, F, 13, x(T_D0, 32), T_OUT, G[G_OUT], N, H, W, true));
-    to_f32(32, 0, 32, P0, G[G_D0], 0);
-    SALTY_TRY(conv_backward(ctx, u, F, 12, cat(T_D1, 48, T_E0, 32), T_D0, G[G_D0], N, H, W, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 12, cat(T_D1, 48, T_E0, 32), T_D0, nullptr, N, H, W, true, F.t[T_G2], 32));
     split(48, 32, H, W, G[G_D1], G[G_E0]);
     SALTY_TRY(conv_backward(ctx, u, F, 11, cat(T_D2, 64, T_E1, 48), T_D1, G[G_D1], N, H1, W1, true));
     split(64, 48, H1, W1, G[G_D2], G[G_E1]);
@@ -923,23 +926,19 @@ salty_status backward(salty_ctx* ctx, Unet& u, Fwd& F, const float* d_target, in
     to_f32(80, 0, 80, P4, G[G_P3], 0);
     k_pool_bwd<<<gsz(P4 * 80 / 8), 256, 0, st>>>(F.t[T_E3], G[G_P3], G[G_E3], N, H3, W3, 80);
     SALTY_TRY(conv_backward(ctx, u, F, 7, x(T_A3, 80), T_E3, G[G_E3], N, H3, W3, true));
-    to_f32(80, 0, 80, P3, G[G_A3], 0);
-    SALTY_TRY(conv_backward(ctx, u, F, 6, x(T_P2, 64), T_A3, G[G_A3], N, H3, W3, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 6, x(T_P2, 64), T_A3, nullptr, N, H3, W3, true, F.t[T_G2], 80));
     to_f32(64, 0, 64, P3, G[G_P2], 0);
     k_pool_bwd<<<gsz(P3 * 64 / 8), 256, 0, st>>>(F.t[T_E2], G[G_P2], G[G_E2], N, H2, W2, 64);
     SALTY_TRY(conv_backward(ctx, u, F, 5, x(T_A2, 64), T_E2, G[G_E2], N, H2, W2, true));
-    to_f32(64, 0, 64, P2, G[G_A2], 0);
-    SALTY_TRY(conv_backward(ctx, u, F, 4, x(T_P1, 48), T_A2, G[G_A2], N, H2, W2, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 4, x(T_P1, 48), T_A2, nullptr, N, H2, W2, true, F.t[T_G2], 64));
     to_f32(48, 0, 48, P2, G[G_P1], 0);
     k_pool_bwd<<<gsz(P2 * 48 / 8), 256, 0, st>>>(F.t[T_E1], G[G_P1], G[G_E1], N, H1, W1, 48);
     SALTY_TRY(conv_backward(ctx, u, F, 3, x(T_A1, 48), T_E1, G[G_E1], N, H1, W1, true));
-    to_f32(48, 0, 48, P1, G[G_A1], 0);
-    SALTY_TRY(conv_backward(ctx, u, F, 2, x(T_P0, 32), T_A1, G[G_A1], N, H1, W1, true));
+    SALTY_TRY(conv_backward(ctx, u, F, 2, x(T_P0, 32), T_A1, nullptr, N, H1, W1, true, F.t[T_G2], 48));
     to_f32(32, 0, 32, P1, G[G_P0], 0);
     k_pool_bwd<<<gsz(P1 * 32 / 8), 256, 0, st>>>(F.t[T_E0], G[G_P0], G[G_E0], N, H, W, 32);
     SALTY_TRY(conv_backward(ctx, u, F, 1, x(T_A0, 32), T_E0, G[G_E0], N, H, W, true));
-    to_f32(32, 0, 32, P0, G[G_A0], 0);
-    SALTY_TRY(conv_backward(ctx, u, F, 0, x(T_X, 16), T_A0, G[G_A0], N, H, W, false));
+    SALTY_TRY(conv_backward(ctx, u, F, 0, x(T_X, 16), T_A0, nullptr, N, H, W, false, F.t[T_G2], 32));
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     double l = 0.0;
     SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(&l, u.loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
