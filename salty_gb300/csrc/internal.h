@@ -262,7 +262,7 @@ struct WaveStore {
     DevBuf<int> roots[2], sroots;
     DevBuf<int> counts, done;
     DevBuf<long long> ctl;
-    DevBuf<unsigned long long> stats, tc0, tc1;
+    DevBuf<unsigned long long> stats, tc0, tc1, tc2, tc3;  // tc*: traversal cursors of the two halves
 };
 
 // Scenes of a batch render concatenated: nodes and leaf triangles of every BVH back to
@@ -286,6 +286,8 @@ struct salty_ctx {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;
+    cudaStream_t aux_stream = nullptr;            // the render's second queue half
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     cudaEvent_t ev[8] = {};
     salty::ErrorSink err;
     salty_trace_stats last_trace{};

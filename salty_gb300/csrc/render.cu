@@ -1,16 +1,19 @@
 // render.cu -- wavefront path tracer.
 //
 // Replaces PathTracer::TracePath / Radiance / NextEventEstimation (src/s3d_pt.cpp:182-353),
-// which walk one path at a time per OpenMP thread.  Here the camera samples of a frame are
-// processed in waves of up to `capacity` paths; each bounce of a wave is
+// which walk one path at a time per OpenMP thread.  Here the paths in flight live in queues
+// on the device, split into two halves that run concurrently, and each iteration is, per half,
+//   generate new camera paths into the queue's free slots
 //   extend   closest-hit traversal of every live path         (trace.cu kernel)
 //   shade1   next-event estimation: builds the shadow-ray queue
 //   shadow   traversal of the shadow queue                     (trace.cu kernel)
 //   shade2   adds unoccluded light, samples the BSDF, Russian roulette, and compacts the
 //            surviving paths into the next queue (warp ballot + one atomic per warp)
-// and a final accumulate pass adds each sample's radiance to the film (Kahan-compensated
-// FP32, or FP64).  Queue lengths stay in device memory, so one wave is a fixed sequence of
-// launches, captured once as a CUDA graph and replayed for every wave of the frame.
+// then, for both halves together, accumulate the samples whose paths have all ended to the
+// film in sample order (Kahan-compensated FP32, or FP64) and plan the next iteration's new
+// samples.  Queue lengths stay in device memory, so the whole frame is one CUDA graph whose
+// conditional while-node repeats the iterations; each half's launches fill the SMs the
+// other half's traversal tail leaves idle.
 //
 // Two estimators:
 //   SALTY_PROFILE_COMPAT reproduces the reference's estimator: pixel-centre rays, uniform
@@ -167,7 +170,8 @@ struct WaveParams {
     const int* sph_lights;        // the light spheres, in light-list order
     int n_inst;
     int n_slots;
-    int capacity;                 // paths in flight (queue length)
+    int capacity;                 // paths in flight (queue length), cap_a + cap_b
+    int cap_a, cap_b;             // the two halves' queue lengths
     int chunk;                    // samples per accumulation chunk
     long long ring;               // per-sample buffer entries: ring_chunks * chunk
     int ring_chunks;
@@ -195,12 +199,14 @@ struct WaveBuffers {
     float4* lbuf;      // per wave-local sample: radiance xyz
     float4* abuf;      // per wave-local sample, first hit: 2 x float4 (albedo, 1/(1+t)) (normal, 0)
     int* counts;       // [0] queue A len, [1] queue B len, [2] shadow len
-    long long* ctl;    // the sample stream, see enum Ctl
+    long long* ctl;    // the sample stream, see enum Ctl (shared by the halves)
+    long long* gen;    // this half's pending generation: first sample, count, first queue slot
     int* done;         // per ring chunk: its samples whose paths have ended
     unsigned long long* stats;  // [0] rays traced, [1] paths
 };
 
 constexpr long long kMaxRingChunks = 16;  // per-sample buffers: at most 16 chunks of half a queue
+constexpr long long kMinSplit = 1 << 16;  // queues of at least this many paths run as two halves
 constexpr int kLaunchIters = 256;          // iterations per graph launch (cancellation granularity)
 
 // Control words of the regenerating wavefront (ctl[]).
@@ -210,11 +216,10 @@ enum Ctl : int {
     kAccN = 2,      // samples [kAccBase, kAccBase + kAccN) are ready to accumulate
     kIters = 3,     // iterations run
     kLaunchEnd = 4, // this graph launch stops after iteration kLaunchEnd
-    kGenFirst = 5,  // the pending generation: first sample,
-    kGenCount = 6,  //   count,
-    kGenSlot = 7,   //   and first queue slot
+    kGenA = 5,      // half A's pending generation (3 words, WaveBuffers::gen)
     kStuck = 8,     // set when kIters passed the iteration limit
-    kCtlWords = 9
+    kGenB = 9,      // half B's pending generation (3 words)
+    kCtlWords = 12
 };
 
 // the last slot whose offset is <= g (slots with no samples or pixels are skipped)
@@ -233,8 +238,8 @@ __device__ __forceinline__ int find_slot(const long long* off, int lo, int hi, l
 // S.sample_off, S.npx).  PinholeCamera::GetRay (include/s3d_camera.h:95-100) with
 // separately rounded operations.
 __global__ void k_generate(WaveParams P, WaveBuffers B, int q) {
-    const long long g0 = B.ctl[kGenFirst];
-    const int n = (int)B.ctl[kGenCount], slot0 = (int)B.ctl[kGenSlot];
+    const long long g0 = B.gen[0];
+    const int n = (int)B.gen[1], slot0 = (int)B.gen[2];
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         const long long g = g0 + j;
         const int i = slot0 + j;                          // queue slot
@@ -1072,43 +1077,58 @@ __global__ void k_shade2(WaveParams P, WaveBuffers B, int q) {
     }
 }
 
-// After the shading of queue q: counts its rays, empties it and the shadow queue, and
-// finds the samples ready for the films -- the longest run of whole chunks, from the first
-// sample not yet accumulated, whose paths have all ended.
-__global__ void k_iter_end(WaveParams P, WaveBuffers B, int q) {
-    B.stats[0] += (unsigned long long)(B.counts[q] + B.counts[2]);
+// After the shading of queue q in both halves: counts their rays, empties those queues and
+// the shadow queues, and finds the samples ready for the films -- the longest run of whole
+// chunks, from the first sample not yet accumulated, whose paths have all ended.
+__global__ void k_iter_end(WaveParams P, WaveBuffers A, WaveBuffers B, int q) {
+    A.stats[0] += (unsigned long long)(A.counts[q] + A.counts[2] + B.counts[q] + B.counts[2]);
+    A.counts[q] = 0;
+    A.counts[2] = 0;
     B.counts[q] = 0;
     B.counts[2] = 0;
-    const long long base = B.ctl[kAccBase];
+    const long long base = A.ctl[kAccBase];
     long long n = 0;
     for (int k = 0; k < P.ring_chunks; ++k) {
         const long long c0 = base + n;
         if (c0 >= P.total_samples) break;
         const long long size = min((long long)P.chunk, P.total_samples - c0);
-        if (B.done[(c0 / P.chunk) % P.ring_chunks] != (int)size) break;
+        if (A.done[(c0 / P.chunk) % P.ring_chunks] != (int)size) break;
         n += size;
     }
-    B.ctl[kAccN] = n;
+    A.ctl[kAccN] = n;
 }
 
-// After the accumulation: frees the accumulated chunks, plans the next generation (queue
-// q ^ 1 filled up to capacity with new samples, as far as free per-sample entries allow)
-// and decides whether the graph launch runs another iteration.
-__global__ void k_iter_next(WaveParams P, WaveBuffers B, int q, cudaGraphConditionalHandle more, int last) {
-    long long* c = B.ctl;
+// New samples for the halves' queues q: up to the free slots of half A, then of half B, as
+// far as free per-sample entries allow (samples below kAccBase + ring).
+__device__ void plan_generation(const WaveParams& P, WaveBuffers& A, WaveBuffers& B, int q) {
+    long long* c = A.ctl;
+    const int have_a = A.counts[q], have_b = B.counts[q];
+    const long long limit = min(P.total_samples, c[kAccBase] + P.ring);
+    const long long avail = max(0LL, limit - c[kNext]);
+    const long long add_a = min((long long)(P.cap_a - have_a), avail);
+    const long long add_b = min((long long)(P.cap_b - have_b), avail - add_a);
+    A.gen[0] = c[kNext];
+    A.gen[1] = add_a;
+    A.gen[2] = have_a;
+    B.gen[0] = c[kNext] + add_a;
+    B.gen[1] = add_b;
+    B.gen[2] = have_b;
+    c[kNext] += add_a + add_b;
+    A.counts[q] = have_a + (int)add_a;
+    B.counts[q] = have_b + (int)add_b;
+    A.stats[1] += (unsigned long long)(add_a + add_b);
+}
+
+// After the accumulation: frees the accumulated chunks, plans the next generation (queues
+// q ^ 1) and decides whether the graph launch runs another iteration.
+__global__ void k_iter_next(WaveParams P, WaveBuffers A, WaveBuffers B, int q, cudaGraphConditionalHandle more,
+                            int last) {
+    long long* c = A.ctl;
     const long long n = c[kAccN];
-    for (long long g = c[kAccBase]; g < c[kAccBase] + n; g += P.chunk) B.done[(g / P.chunk) % P.ring_chunks] = 0;
+    for (long long g = c[kAccBase]; g < c[kAccBase] + n; g += P.chunk) A.done[(g / P.chunk) % P.ring_chunks] = 0;
     c[kAccBase] += n;
     c[kAccN] = 0;
-    const int have = B.counts[q ^ 1];
-    const long long limit = min(P.total_samples, c[kAccBase] + P.ring);
-    const long long add = max(0LL, min((long long)(P.capacity - have), limit - c[kNext]));
-    c[kGenFirst] = c[kNext];
-    c[kGenCount] = add;
-    c[kGenSlot] = have;
-    c[kNext] += add;
-    B.counts[q ^ 1] = have + (int)add;
-    B.stats[1] += (unsigned long long)add;
+    plan_generation(P, A, B, q ^ 1);
     c[kIters] += 1;
     if (c[kIters] > P.iter_limit) c[kStuck] = 1;
     if (last) {
@@ -1117,18 +1137,17 @@ __global__ void k_iter_next(WaveParams P, WaveBuffers B, int q, cudaGraphConditi
     }
 }
 
-// Start of a render: nothing accumulated, the first samples pending for queue 0.
-__global__ void k_render_init(WaveParams P, WaveBuffers B) {
-    for (int k = 0; k < kCtlWords; ++k) B.ctl[k] = 0;
-    for (int k = 0; k < P.ring_chunks; ++k) B.done[k] = 0;
-    const long long add = min((long long)P.capacity, min(P.total_samples, P.ring));
-    B.ctl[kGenCount] = add;
-    B.ctl[kNext] = add;
-    B.counts[0] = (int)add;
-    B.counts[1] = 0;
-    B.counts[2] = 0;
-    B.stats[0] = 0;
-    B.stats[1] = (unsigned long long)add;
+// Start of a render: nothing accumulated, the first samples pending for queues 0.
+__global__ void k_render_init(WaveParams P, WaveBuffers A, WaveBuffers B) {
+    for (int k = 0; k < kCtlWords; ++k) A.ctl[k] = 0;
+    for (int k = 0; k < P.ring_chunks; ++k) A.done[k] = 0;
+    for (int k = 0; k < 3; ++k) {
+        A.counts[k] = 0;
+        B.counts[k] = 0;
+    }
+    A.stats[0] = 0;
+    A.stats[1] = 0;
+    plan_generation(P, A, B, 0);
 }
 
 // Start of a graph launch: run at most launch_iters iterations.
@@ -1566,12 +1585,11 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     SALTY_TRY_CUDA(E, S.shits.ensure(cap * 2));
     SALTY_TRY_CUDA(E, S.lbuf.ensure(ring));
     SALTY_TRY_CUDA(E, S.abuf.ensure(ring * 2));
-    SALTY_TRY_CUDA(E, S.counts.ensure(8));
+    SALTY_TRY_CUDA(E, S.counts.ensure(16));
     SALTY_TRY_CUDA(E, S.ctl.ensure(kCtlWords));
     SALTY_TRY_CUDA(E, S.done.ensure(kMaxRingChunks));
     SALTY_TRY_CUDA(E, S.stats.ensure(4));
-    SALTY_TRY_CUDA(E, S.tc0.ensure(4));
-    SALTY_TRY_CUDA(E, S.tc1.ensure(4));
+    for (auto* tc : {&S.tc0, &S.tc1, &S.tc2, &S.tc3}) SALTY_TRY_CUDA(E, tc->ensure(4));
     SALTY_TRY_CUDA(E, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), st));
 
     WaveParams P;
@@ -1595,6 +1613,9 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     P.sph_lights = sph ? scenes[0]->sph_lights.p : nullptr;
     P.n_slots = n;
     P.capacity = (int)cap;
+    // two halves of the queue run concurrently (a render of fewer paths uses half A alone)
+    P.cap_a = (int)(cap >= kMinSplit ? cap / 2 : cap);
+    P.cap_b = (int)cap - P.cap_a;
     P.chunk = (int)chunk;
     P.ring = ring;
     P.ring_chunks = ring_chunks;
@@ -1604,60 +1625,89 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     P.iter_limit = 2 * (chunks_total + 2) * (long long)(max_depth + 2);
     P.total_samples = samples;
 
-    WaveBuffers B;
-    for (int i = 0; i < 2; ++i) {
-        B.rays[i] = S.rays[i].p;
-        B.path[i] = PathSoA{S.W[i].p, S.L[i].p, S.meta[i].p};
-        B.roots[i] = batch ? S.roots[i].p : nullptr;
-    }
-    B.sroots = batch ? S.sroots.p : nullptr;
-    B.hits = S.hits.p;
-    B.nee = S.nee.p;
-    B.srays = S.srays.p;
-    B.shits = S.shits.p;
-    B.lbuf = S.lbuf.p;
-    B.abuf = S.abuf.p;
-    B.counts = S.counts.p;
-    B.ctl = S.ctl.p;
-    B.done = S.done.p;
-    B.stats = S.stats.p;
+    // the halves' views of the queues: half B starts cap_a paths in (2 rays and 2 shadow
+    // rays per path), with its own queue lengths and generation plan
+    auto half = [&](long long off, int counts_off, int gen_word) {
+        WaveBuffers h;
+        for (int i = 0; i < 2; ++i) {
+            h.rays[i] = S.rays[i].p + 2 * off;
+            h.path[i] = PathSoA{S.W[i].p + off, S.L[i].p + off, S.meta[i].p + off};
+            h.roots[i] = batch ? S.roots[i].p + off : nullptr;
+        }
+        h.sroots = batch ? S.sroots.p + 2 * off : nullptr;
+        h.hits = S.hits.p + off;
+        h.nee = S.nee.p + 2 * off;
+        h.srays = S.srays.p + 4 * off;
+        h.shits = S.shits.p + 2 * off;
+        h.lbuf = S.lbuf.p;
+        h.abuf = S.abuf.p;
+        h.counts = S.counts.p + counts_off;
+        h.ctl = S.ctl.p;
+        h.gen = S.ctl.p + gen_word;
+        h.done = S.done.p;
+        h.stats = S.stats.p;
+        return h;
+    };
+    WaveBuffers BA = half(0, 0, kGenA), BB = half(P.cap_a, 8, kGenB);
 
     const bool compat = opts[0].profile == SALTY_PROFILE_COMPAT;
     const uint32_t ext_flags = compat ? 0u : (uint32_t)SALTY_TRACE_WATERTIGHT;
     const uint32_t sh_flags = compat ? 0u : (uint32_t)(SALTY_TRACE_WATERTIGHT | SALTY_TRACE_ANY_HIT);
     const int sb = T.shade_block;
-    const int sgrid = grid_of(cap, 2048 / sb, ctx->num_sms, sb);
     const int agrid = grid_of(std::min<long long>(pixels, ring), 2048 / 256, ctx->num_sms);
-    TraceTarget ext = tgt, shd = tgt;
-    shd.roots = B.sroots;
 
     // The render is one CUDA graph: a conditional while-node whose body runs two
     // iterations (queue 0, then queue 1) of
-    //   generate new samples into the free queue slots -> extension rays -> NEE ->
-    //   shadow rays -> BSDF sampling and compaction into the other queue ->
-    //   accumulate the chunks whose samples have all ended -> plan the next generation,
+    //   for each half, on its own stream: generate new samples into the free queue slots ->
+    //   extension rays -> NEE -> shadow rays -> BSDF sampling and compaction into the
+    //   other queue;
+    //   joined: accumulate the chunks whose samples have all ended -> plan the next
+    //   generation,
     // and repeats while samples remain (at most kLaunchIters iterations per launch, so a
     // cancellation is seen between launches).  Every path lives in the queue until it
     // ends, so each launch of the traversal sees a full queue instead of the shrinking
-    // depth levels of a fixed wave.
+    // depth levels of a fixed wave, and while one half's traversal finishes its longest
+    // walks the other half's launches take the idle SMs.
     // SALTY_RENDER_HOST_LOOP=1 launches the same iterations from a host loop instead (16 per
     // step): the kernels inside a conditional graph body are invisible to some profilers.
     const char* hl = std::getenv("SALTY_RENDER_HOST_LOOP");
     const bool host_loop = hl && std::atoi(hl) != 0;
     cudaGraphConditionalHandle more = 0;
+    // one half's shading and traversal for queue q, on stream hs
+    auto run_half = [&](const WaveBuffers& H, long long hcap, unsigned long long* tc_ext, unsigned long long* tc_sh,
+                        cudaStream_t hs, int q) -> salty_status {
+        const int hgrid = grid_of(hcap, 2048 / sb, ctx->num_sms, sb);
+        TraceTarget ext = tgt, shd = tgt;
+        ext.roots = H.roots[q];
+        shd.roots = H.sroots;
+        k_generate<<<hgrid, sb, 0, hs>>>(P, H, q);
+        SALTY_TRY(trace_launch(ctx, ext, T.trace, H.rays[q], hcap, &H.counts[q], ext_flags, H.hits, tc_ext, hs,
+                               ctx->status.p));
+        k_shade1<<<hgrid, sb, 0, hs>>>(P, H, q);
+        SALTY_TRY(trace_launch(ctx, shd, T.trace, H.srays, 2 * hcap, &H.counts[2], sh_flags, H.shits, tc_sh, hs,
+                               ctx->status.p));
+        k_shade2<<<hgrid, sb, 0, hs>>>(P, H, q);
+        return SALTY_OK;
+    };
+    const bool split = P.cap_b > 0;
     auto iteration_pair = [&](bool in_graph) -> salty_status {
         for (int q = 0; q < 2; ++q) {
-            k_generate<<<sgrid, sb, 0, st>>>(P, B, q);
-            ext.roots = B.roots[q];
-            SALTY_TRY(trace_launch(ctx, ext, T.trace, B.rays[q], cap, &B.counts[q], ext_flags, B.hits, S.tc0.p, st,
-                                   ctx->status.p));
-            k_shade1<<<sgrid, sb, 0, st>>>(P, B, q);
-            SALTY_TRY(trace_launch(ctx, shd, T.trace, B.srays, 2 * cap, &B.counts[2], sh_flags, B.shits, S.tc1.p, st,
-                                   ctx->status.p));
-            k_shade2<<<sgrid, sb, 0, st>>>(P, B, q);
-            k_iter_end<<<1, 1, 0, st>>>(P, B, q);
-            k_accumulate<<<agrid, 256, 0, st>>>(P, B);
-            k_iter_next<<<1, 1, 0, st>>>(P, B, q, more, in_graph && q == 1 ? 1 : 0);
+            // half B on the auxiliary stream, forked from and joined back into st (in the
+            // host loop both halves run on st, one after the other)
+            const cudaStream_t sb_stream = in_graph && split ? ctx->aux_stream : st;
+            if (in_graph && split) {
+                SALTY_TRY_CUDA(E, cudaEventRecord(ctx->fork_ev, st));
+                SALTY_TRY_CUDA(E, cudaStreamWaitEvent(sb_stream, ctx->fork_ev, 0));
+            }
+            SALTY_TRY(run_half(BA, P.cap_a, S.tc0.p, S.tc1.p, st, q));
+            if (split) SALTY_TRY(run_half(BB, P.cap_b, S.tc2.p, S.tc3.p, sb_stream, q));
+            if (in_graph && split) {
+                SALTY_TRY_CUDA(E, cudaEventRecord(ctx->join_ev, sb_stream));
+                SALTY_TRY_CUDA(E, cudaStreamWaitEvent(st, ctx->join_ev, 0));
+            }
+            k_iter_end<<<1, 1, 0, st>>>(P, BA, BB, q);
+            k_accumulate<<<agrid, 256, 0, st>>>(P, BA);
+            k_iter_next<<<1, 1, 0, st>>>(P, BA, BB, q, more, in_graph && q == 1 ? 1 : 0);
         }
         return SALTY_OK;
     };
@@ -1677,7 +1727,7 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
         cudaGraphNode_t begin_node, loop_node;
         {
             cudaKernelNodeParams kp{};
-            void* args[] = {&P, &B};
+            void* args[] = {&P, &BA};
             kp.func = reinterpret_cast<void*>(k_launch_begin);
             kp.gridDim = dim3(1);
             kp.blockDim = dim3(1);
@@ -1703,7 +1753,7 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
 
     cudaEvent_t e0 = ctx->ev[0], e1 = ctx->ev[1];
     SALTY_TRY_CUDA(E, cudaEventRecord(e0, st));
-    k_render_init<<<1, 1, 0, st>>>(P, B);
+    k_render_init<<<1, 1, 0, st>>>(P, BA, BB);
     salty_status rs = SALTY_OK;
     long long hc[kCtlWords];
     const int pairs_per_step = 8;
@@ -1711,14 +1761,14 @@ salty_status render_batch(salty_ctx* ctx, salty_scene* const* scenes, const salt
     for (long long launch = 0;; ++launch) {
         if (launch > max_launches) { rs = E.fail(SALTY_ERR_TIMEOUT, "render made no progress"); break; }
         if (host_loop) {
-            k_launch_begin<<<1, 1, 0, st>>>(P, B);
+            k_launch_begin<<<1, 1, 0, st>>>(P, BA);
             for (int k = 0; k < pairs_per_step && rs == SALTY_OK; ++k) rs = iteration_pair(false);
             if (rs != SALTY_OK) break;
         } else {
             cudaError_t le = cudaGraphLaunch(exec, st);
             if (le != cudaSuccess) { rs = E.fail(SALTY_ERR_CUDA, "graph launch: %s", cudaGetErrorString(le)); break; }
         }
-        cudaError_t re = cudaMemcpyAsync(hc, B.ctl, sizeof hc, cudaMemcpyDeviceToHost, st);
+        cudaError_t re = cudaMemcpyAsync(hc, S.ctl.p, sizeof hc, cudaMemcpyDeviceToHost, st);
         if (re == cudaSuccess) re = cudaStreamSynchronize(st);
         if (re != cudaSuccess) { rs = E.fail(SALTY_ERR_CUDA, "render: %s", cudaGetErrorString(re)); break; }
         if (hc[kStuck]) { rs = E.fail(SALTY_ERR_TIMEOUT, "render made no progress in %lld iterations", hc[kIters]); break; }

@@ -74,10 +74,15 @@ def _pad16(a: np.ndarray) -> np.ndarray:
 class Denoiser:
     """denoise(mean, var, aov, spp) -> image.  Uses the U-Net when weights are available and
     NLM (salty_denoise_nlm, 21x21 search, 7x7 patch) otherwise, or when method="nlm".  With
-    high-spp weights too, films of at least hq_from_spp samples per pixel use those."""
+    high-spp weights too, films of at least hq_from_spp samples per pixel use those.
+
+    The default pair was chosen on a validation heightfield (seed 3001, in neither the
+    training set nor the benchmark): the general network (16 scenes x 6 views, 7 levels
+    4-16384 spp, directional suns) had the lower error from 64 to 8192 spp, the high-spp
+    network (levels 1024-16384) at 16384 spp, hence hq_from_spp = 16384."""
 
     def __init__(self, ctx: Context, weights: str | None = DEFAULT_WEIGHTS, method: str = "auto",
-                 nlm_k: float = 0.45, hq_weights: str | None = DEFAULT_HQ_WEIGHTS, hq_from_spp: int = 1024,
+                 nlm_k: float = 0.45, hq_weights: str | None = DEFAULT_HQ_WEIGHTS, hq_from_spp: int = 16384,
                  mirrors: int = 8):
         self.ctx = ctx
         # film denoising averages the network over this many symmetries of the pixel grid
@@ -96,8 +101,6 @@ class Denoiser:
             if hq_weights and os.path.exists(hq_weights):
                 self.hq = Unet(ctx)
                 self.hq_meta = load_weights(self.hq, hq_weights)
-                # from the lowest sample count it was trained on
-                self.hq_from_spp = int(min(self.hq_meta.get("levels", [hq_from_spp])))
         elif method == "unet":
             raise FileNotFoundError(f"no U-Net weights at {weights}")
         self.method = "unet" if self.net is not None else "nlm"
