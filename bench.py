@@ -59,11 +59,11 @@ TMIN = 1e-4
 METRIC = "Mrays/s"
 CPU_SAMPLE = 2_097_152      # rays of the same stream timed on the host cores (~10 s of CPU work)
 # DRAM bytes (read + write) per ray of the closest-hit k_trace launch, from one ncu capture
-# of that kernel at a launch shape salty_autotune_trace picks here (128 threads, 64
-# registers, pool 128, no triangle postponing) on the same soup at 4,194,304 rays; the
-# traffic (rays in, hits out, L2 misses) scales with the ray count, so traffic per launch is
-# this figure times the rays of the launch.
-NCU_DRAM_BYTES_PER_RAY = (366.647552e6 + 65.853440e6) / 4_194_304
+# of that kernel at the default launch shape (128 threads, 56 registers, pool 64, no
+# triangle postponing) on the same soup at 4,194,304 rays; the traffic (rays in, hits out,
+# L2 misses) scales with the ray count, so traffic per launch is this figure times the rays
+# of the launch.
+NCU_DRAM_BYTES_PER_RAY = (388.030208e6 + 69.070336e6) / 4_194_304
 
 
 def measured_peaks_tensor() -> dict:
@@ -711,7 +711,7 @@ def prof_trace_sweep() -> dict:
     rays = torch.from_numpy(microbench_rays(20260002, n, 1e-4)).cuda()
     hits = torch.empty((n, 4), device="cuda")
     ref, res = None, []
-    for blk, regs, pool, post in itertools.product((64, 128, 256), (64, 48), (64, 128, 256), (1, 4, 7, 10)):
+    for blk, regs, pool, post in itertools.product((64, 128, 256), (64, 56), (64, 128, 256), (1, 4, 7, 10)):
         ctx.tuning = {"trace_block": blk, "trace_regs": regs, "trace_pool": pool, "trace_postpone": post}
         for _ in range(2):
             sc.trace_raw(rays, hits)

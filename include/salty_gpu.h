@@ -325,7 +325,7 @@ typedef struct salty_tuning {
     int32_t trace_pool;      /* rays a warp takes from the queue per refill, 32..4096 */
     int32_t trace_postpone;  /* fewest lanes that test a triangle group together, 1..32 */
     int32_t shade_block;     /* shading threads per block, a multiple of 32 in 64..1024 */
-    int32_t trace_regs;      /* traversal registers per thread: 64, or 48 (more resident warps) */
+    int32_t trace_regs;      /* traversal registers per thread: 64, or 56 (more resident warps) */
     int64_t wave_paths;      /* paths in flight (queue capacity), 2^16..2^27; default 2^24
                               * (352 bytes of path state per path plus per-sample buffers of
                               * up to 7x as many samples at 48 bytes: about 11 GB for a

@@ -31,17 +31,28 @@ PROFILE_COMPAT, PROFILE_PHYSICAL = 0, 1
 TM_REINHARD, TM_UNCHARTED2, TM_ACES = 0, 1, 2
 
 
+# Where the reference checkout is mounted in the container that builds the fixtures; any
+# other checkout is named by $SALTY_REF_SRC.
+_REF_MOUNT = "/root/reference/src"
+
+
 def reference_dir() -> str | None:
-    """The reference project's source root as oracle/Makefile knows it, if present here."""
-    r = subprocess.run(["make", "-s", "-C", HERE, "ref-dir"], capture_output=True, text=True)
-    d = r.stdout.strip()
-    return d if r.returncode == 0 and d and os.path.isdir(d) else None
+    """The reference project's source root ($SALTY_REF_SRC, else the fixture container's
+    mount), if its sources are present here."""
+    for d in (os.environ.get("SALTY_REF_SRC"), _REF_MOUNT):
+        if d and os.path.isfile(os.path.join(d, "src", "s3d_pt.cpp")):
+            return d
+    return None
 
 
 def build(with_reference: bool | None = None) -> None:
     """Runs oracle/Makefile (the restatement always; the reference when its sources exist)."""
     target = ["all"] if with_reference is None else (["oracle", "ref"] if with_reference else ["oracle"])
-    subprocess.run(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}", *target], check=True)
+    ref = reference_dir()
+    if with_reference and not ref:
+        raise RuntimeError("the reference sources are not present (set SALTY_REF_SRC)")
+    extra = [f"REF={ref}"] if ref else []
+    subprocess.run(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}", *extra, *target], check=True)
 
 
 class _Mat(C.Structure):

@@ -600,7 +600,7 @@ salty_status salty_set_tuning(salty_ctx* ctx, const salty_tuning* t) {
         return E.fail(SALTY_ERR_INVALID_ARG, "trace_postpone must be 1..32");
     if (t->shade_block < 64 || t->shade_block > 1024 || t->shade_block % 32)
         return E.fail(SALTY_ERR_INVALID_ARG, "shade_block must be a multiple of 32 in 64..1024");
-    if (t->trace_regs != 64 && t->trace_regs != 48) return E.fail(SALTY_ERR_INVALID_ARG, "trace_regs must be 64 or 48");
+    if (t->trace_regs != 64 && t->trace_regs != 56) return E.fail(SALTY_ERR_INVALID_ARG, "trace_regs must be 64 or 56");
     if (t->wave_paths < (1 << 16) || t->wave_paths > (1 << 27))
         return E.fail(SALTY_ERR_INVALID_ARG, "wave_paths must be 2^16..2^27");
     ctx->tune.trace.block = t->trace_block;
@@ -652,7 +652,7 @@ salty_status salty_autotune_trace(salty_ctx* ctx, salty_scene* sc, const salty_r
     TraceTuning best = start;
     float best_t = 0;
     salty_status s = time_of(&best_t);
-    const int block_regs[][2] = {{64, 64}, {128, 64}, {256, 64}, {64, 48}, {128, 48}, {256, 48}};
+    const int block_regs[][2] = {{64, 64}, {128, 64}, {256, 64}, {64, 56}, {128, 56}};
     const int pool[] = {64, 128, 256};
     const int postpone[] = {1, 4, 7, 10};
     auto consider = [&](TraceTuning t) -> salty_status {
@@ -731,7 +731,7 @@ salty_status salty_autotune(salty_ctx* ctx, salty_scene* const* scenes, const sa
     const int shade[] = {128, 256, 512};
     // traversal block size and register budget interact (registers x threads x blocks per
     // SM against the shared stack), so they are searched as pairs
-    const int block_regs[][2] = {{64, 64}, {128, 64}, {256, 64}, {64, 48}, {128, 48}, {256, 48}};
+    const int block_regs[][2] = {{64, 64}, {128, 64}, {256, 64}, {64, 56}, {128, 56}};
     const int pool[] = {64, 128, 256};
     const int postpone[] = {1, 4, 7, 10};
     auto try_knob = [&](auto set, const auto& values) -> salty_status {

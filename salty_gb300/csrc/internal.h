@@ -203,7 +203,7 @@ struct TraceTuning {
     int block = 128;     // threads per block: 64, 128 or 256
     int pool = 64;       // rays a warp takes from the global cursor per refill
     int postpone = 1;    // fewest lanes that test a triangle group together (1: never postpone)
-    int regs = 64;       // register budget per thread: 64 (as compiled) or 48 (more resident warps)
+    int regs = 56;       // register budget per thread: 64, or 56 (more resident warps: 9 blocks of 128)
 };
 
 }  // namespace salty

@@ -11,6 +11,8 @@
 // level's leaf entries are instances, and a ray reaching one is transformed into the
 // instance's object space and walks the instance's mesh BVH, above a marker on its stack;
 // popping the marker brings back the world ray and the top-level walk (instance.cu).
+#include <algorithm>
+
 #include "internal.h"
 #include "traverse.cuh"
 
@@ -19,18 +21,23 @@ namespace {
 
 constexpr int kMaxStack = 63;  // stack entries per thread: BVHs up to 31 levels
 
+// Rays per launch: ray indices are 32-bit in the kernel (three registers fewer than 64-bit
+// ones); longer arrays are traced in consecutive launches of at most this many rays.
+constexpr long long kMaxLaunchRays = 1ll << 30;
+
 // counters: [0] ray cursor, [1] node fetches, [2] triangle fetches.  The register budget
 // is set through the resident blocks asked for: 1024 / TB caps registers at 64 per thread,
-// CAP's 1280 / TB at 48 (more warps per SM to hide fetch latency, at the price of a few
-// spilled values).
+// CAP's 1152 / TB at 56 for blocks of up to 128 threads (36 instead of 32 warps per SM to
+// hide fetch latency, at the price of a few spilled values; 256-thread blocks stay at 64).
 // The short stack lives in dynamic shared memory, `depth` entries per thread (two per BVH
-// level plus one), so shallow trees leave room for more resident blocks.
+// level plus one) and one more for the best hit's (u, v), so shallow trees leave room for
+// more resident blocks.
 // Stack entry (.y) that marks where a ray entered an instance.
 constexpr unsigned kInstMarker = 0x40000000u;
 
 // SPH: leaf entries with ids from sph_base on are spheres (sphere.cu).
 template <bool ANY, bool WT, bool COUNT, int TB, bool CAP, bool INST, bool SPH>
-__global__ void __launch_bounds__(TB, CAP ? 1280 / TB : 1024 / TB)
+__global__ void __launch_bounds__(TB, CAP ? 1152 / TB : 1024 / TB)
 k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, const float4* __restrict__ rays,
         const int* __restrict__ roots, long long n_arg, const int* __restrict__ n_dev, float4* __restrict__ hits,
         unsigned long long* __restrict__ counters, float cull_slack, int pool, int postpone, int depth,
@@ -39,16 +46,17 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
     TravStack st{sstack + threadIdx.x, TB, depth};
     const int lane = threadIdx.x & 31;
     // queue length from device memory when given (wavefront queues), else the argument
-    const long long n = n_dev ? (long long)*n_dev : n_arg;
-    const unsigned lt_mask = (1u << lane) - 1u;
+    // (at most kMaxLaunchRays either way)
+    const int n = n_dev ? *n_dev : (int)n_arg;
     TravCount cnt{0, 0};
     int overflow = 0;
     // Warp-uniform pool of ray indices [pool_next, pool_end), refilled `pool` at a time
     // from the global cursor; each lane holds one ray and takes a new one from the pool
-    // as soon as its walk ends.
-    long long pool_next = 0, pool_end = 0;
+    // as soon as its walk ends.  The cursor is 64-bit: warps that find the rays drained
+    // may push it past 2^31.
+    int pool_next = 0, pool_end = 0;
     bool drained = false;
-    long long rid = -1;
+    int rid = -1;
     TravRay r;
     TravState s;
     bool in_mesh = false;  // INST: walking an instance's mesh (else the top level)
@@ -61,16 +69,19 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
                 unsigned long long base = 0;
                 if (lane == 0) base = atomicAdd(&counters[0], (unsigned long long)pool);
                 base = __shfl_sync(0xffffffffu, base, 0);
-                pool_next = (long long)base;
-                pool_end = min((long long)base + pool, n);
-                if ((long long)base + pool >= n) drained = true;
+                const long long end = (long long)base + pool;
+                pool_next = (int)min((long long)base, (long long)n);
+                pool_end = (int)min(end, (long long)n);
+                if (end >= n) drained = true;
             }
-            const long long mine = pool_next + __popc(idle_mask & lt_mask);
+            unsigned lt_mask;
+            asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt_mask));
+            const int mine = pool_next + __popc(idle_mask & lt_mask);
             if (idle && mine < pool_end) {
                 rid = mine;
                 const float4 ra = __ldcs(rays + 2 * rid), rb = __ldcs(rays + 2 * rid + 1);
-                make_trav_ray(r, ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w);
-                trav_init(s, r, roots ? (unsigned)__ldcs(roots + rid) : 0u);
+                make_trav_ray(r, ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z);
+                trav_init(s, r, rb.w, roots ? (unsigned)__ldcs(roots + rid) : 0u);
                 in_mesh = false;
                 vbase = 0;
             }
@@ -78,7 +89,7 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
         }
         const bool active = rid >= 0;
         if (__ballot_sync(0xffffffffu, active) == 0) break;
-        if (active && s.ng_hits) trav_node_step<COUNT>(s, nodes, r, st, cnt, overflow);
+        if (active && s.ng_hits) trav_node_step<COUNT>(s, nodes, r, st, cnt, overflow, cull_slack);
         // INST: a top-level leaf group holds instances; enter the first one, leaving the rest
         // of the group, the pending node group and a return marker on the stack
         if (INST && active && !in_mesh && s.tg_hits) {
@@ -98,7 +109,7 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
                 const float dx = fmaf(m[0], r.dx, fmaf(m[1], r.dy, m[2] * r.dz));
                 const float dy = fmaf(m[4], r.dx, fmaf(m[5], r.dy, m[6] * r.dz));
                 const float dz = fmaf(m[8], r.dx, fmaf(m[9], r.dy, m[10] * r.dz));
-                make_trav_ray(r, ox, oy, oz, r.tmin, dx, dy, dz, r.tmax);
+                make_trav_ray(r, ox, oy, oz, r.tmin, dx, dy, dz);
                 s.ng_base = R.root;
                 s.ng_hits = 1u << r.oct;
                 s.ng_imask = 1u;
@@ -112,30 +123,38 @@ k_trace(const Bvh8Node* __restrict__ nodes, const float4* __restrict__ tris, con
         }
         // Triangle postponing: with too few lanes holding triangles, set the group aside
         // and keep walking nodes with the rest of the warp.
+        // (postpone <= 1 never postpones: the warp-wide count is skipped)
         const bool want = active && s.tg_hits != 0 && (!INST || in_mesh);
-        const unsigned want_mask = __ballot_sync(0xffffffffu, want);
         bool run = want;
-        if (want && __popc(want_mask) < postpone && s.ng_hits != 0 && s.sp < depth) {
-            st.at(s.sp++) = make_uint2(s.tg_base, s.tg_hits | kTriGroupFlag);
-            s.tg_hits = 0;
-            run = false;
+        if (postpone > 1) {
+            const unsigned want_mask = __ballot_sync(0xffffffffu, want);
+            if (want && __popc(want_mask) < postpone && s.ng_hits != 0 && s.sp < depth) {
+                st.at(s.sp++) = make_uint2(s.tg_base, s.tg_hits | kTriGroupFlag);
+                s.tg_hits = 0;
+                run = false;
+            }
         }
         bool done = false;
-        if (run) done = trav_tri_step<ANY, WT, COUNT, SPH>(s, tris, r, cull_slack, cnt, vbase, sph_base);
+        if (run) done = trav_tri_step<ANY, WT, COUNT, SPH>(s, tris, r, st, cnt, vbase, sph_base);
         bool more = true;
         if (INST && active && !done && !s.ng_hits && !s.tg_hits && s.sp > 0 &&
             st.at(s.sp - 1).y == kInstMarker) {
             // the instance's walk is over: back to the world ray and the top level
             --s.sp;
             const float4 ra = __ldcs(rays + 2 * rid), rb = __ldcs(rays + 2 * rid + 1);
-            make_trav_ray(r, ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w);
+            make_trav_ray(r, ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z);
             in_mesh = false;
             vbase = 0;
         } else if (active && !done) {
             more = trav_pop(s, st);
         }
         if (active && (done || !more)) {
-            __stcs(hits + rid, make_float4(s.hit.t, __int_as_float(s.hit.id), s.hit.u, s.hit.v));
+            float4 h = make_float4(INFINITY, __int_as_float(-1), 0.0f, 0.0f);
+            if (s.hit.id >= 0) {
+                const uint2 uv = st.uv();
+                h = make_float4(s.hit.t, __int_as_float(s.hit.id), __uint_as_float(uv.x), __uint_as_float(uv.y));
+            }
+            __stcs(hits + rid, h);
             rid = -1;
         }
     }
@@ -169,20 +188,28 @@ struct Launch {
 template <bool ANY, bool WT, bool COUNT, int TB, bool CAP, bool INST, bool SPH = false>
 salty_status launch(salty_ctx* ctx, const Launch& L) {
     auto kern = k_trace<ANY, WT, COUNT, TB, CAP, INST, SPH>;
-    const size_t smem = (size_t)L.depth * TB * sizeof(uint2);
+    const size_t smem = (size_t)(L.depth + 1) * TB * sizeof(uint2);  // the stack and (u, v)
     if (smem > 48 * 1024)
         SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     SALTY_TRY_CUDA(ctx->err, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TB, smem));
     if (per_sm < 1) per_sm = 1;
-    long long want = (L.n + TB - 1) / TB;
-    long long grid = (long long)ctx->num_sms * per_sm;
-    if (grid > want) grid = want;
-    if (grid < 1) grid = 1;
-    kern<<<(unsigned)grid, TB, smem, L.st>>>(L.tgt.nodes, L.tgt.tris, L.rays, L.tgt.roots, L.n, L.n_dev, L.hits,
-                                             L.counters, L.slack, L.pool, L.postpone, L.depth, L.status,
-                                             L.tgt.inst, L.tgt.sph_base);
-    SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    if (L.n_dev && L.n > kMaxLaunchRays)
+        return ctx->err.fail(SALTY_ERR_CAPACITY, "ray queue capacity %lld exceeds %lld", L.n, kMaxLaunchRays);
+    // consecutive launches of at most kMaxLaunchRays rays; each restarts the ray cursor
+    for (long long off = 0; off == 0 || off < L.n; off += kMaxLaunchRays) {
+        const long long n = std::min(L.n - off, kMaxLaunchRays);
+        if (off > 0) SALTY_TRY_CUDA(ctx->err, cudaMemsetAsync(L.counters, 0, sizeof(unsigned long long), L.st));
+        long long want = (n + TB - 1) / TB;
+        long long grid = (long long)ctx->num_sms * per_sm;
+        if (grid > want) grid = want;
+        if (grid < 1) grid = 1;
+        kern<<<(unsigned)grid, TB, smem, L.st>>>(L.tgt.nodes, L.tgt.tris, L.rays + 2 * off,
+                                                 L.tgt.roots ? L.tgt.roots + off : nullptr, n, L.n_dev,
+                                                 L.hits + off, L.counters, L.slack, L.pool, L.postpone, L.depth,
+                                                 L.status, L.tgt.inst, L.tgt.sph_base);
+        SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
+    }
     return SALTY_OK;
 }
 
@@ -249,11 +276,15 @@ salty_status trace_launch(salty_ctx* ctx, const TraceTarget& tgt, const TraceTun
                           unsigned long long* d_counters, cudaStream_t st, int* d_status) {
     SALTY_TRY_CUDA(ctx->err, cudaMemsetAsync(d_counters, 0, 3 * sizeof(unsigned long long), st));
     const bool wt = flags & SALTY_TRACE_WATERTIGHT;
-    // Each BVH level can hold one pending node group and one postponed triangle group.
-    const int need = 2 * tgt.depth + 1;
+    // Without postponing, the walk keeps at most one pending node group per BVH level
+    // (it pushes the rest of a group before descending into one of its children, and puts
+    // back what is left of a group it pops); postponing adds a triangle group per level, and
+    // instances their return markers.  A full stack is reported, never overrun.
+    const bool two = tune.postpone > 1 || tgt.inst != nullptr;
+    const int need = two ? 2 * tgt.depth + 1 : tgt.depth + 1;
     if (need > kMaxStack)
-        return ctx->err.fail(SALTY_ERR_CAPACITY, "BVH depth %d exceeds the traversal stack (%d levels)", tgt.depth,
-                             (kMaxStack - 1) / 2);
+        return ctx->err.fail(SALTY_ERR_CAPACITY, "BVH depth %d needs %d traversal stack entries (at most %d)",
+                             tgt.depth, need, kMaxStack);
     Launch L{tgt, d_rays, n, n_dev, d_hits, d_counters, st, wt ? (1.0f / 65536.0f) : 1e-3f,
              tune.pool >= 32 ? tune.pool : 32, tune.postpone, need, d_status};
     if (flags & SALTY_TRACE_COUNTERS) return dispatch_count(ctx, L, flags);
@@ -267,7 +298,7 @@ salty_status trace_launch(salty_ctx* ctx, const TraceTarget& tgt, const TraceTun
         if (tune.block == 256) return dispatch_inst<256>(ctx, L, flags);
         return dispatch_inst<128>(ctx, L, flags);
     }
-    const bool cap = tune.regs == 48;
+    const bool cap = tune.regs == 56;
 #define SALTY_D(B) return cap ? dispatch_flags<B, true>(ctx, L, flags) : dispatch_flags<B, false>(ctx, L, flags)
     if (tune.block == 64) SALTY_D(64);
     if (tune.block == 256) SALTY_D(256);

@@ -17,25 +17,34 @@
 namespace salty {
 
 // Group stack entry: x = child base index, y = (hit bits in key order << 8) | imask.
+// One more entry per thread, after the stack, holds the best hit's (u, v), which is
+// written only when the best hit changes and read once at the end of the walk: two
+// registers fewer for the whole walk.
 struct TravStack {
-    uint2* base;    // shared memory, [depth][blockDim]
+    uint2* base;    // shared memory, [depth + 1][blockDim]
     int stride;     // blockDim.x
-    int depth;      // entries per thread
+    int depth;      // stack entries per thread
     __device__ __forceinline__ uint2& at(int i) const { return base[i * stride]; }
+    __device__ __forceinline__ uint2& uv() const { return base[depth * stride]; }
 };
 
+// The ray's tmax is not kept here: the walk starts with the best distance at tmax
+// (TravHit::t) and only ever lowers it.
 struct TravRay {
     float ox, oy, oz, dx, dy, dz;
     float ix, iy, iz;        // 1/d with zero components replaced by tiny values
-    float tmin, tmax;
+    float tmin;
     unsigned oct;            // bit a set when d[a] < 0
     // watertight shear constants
     int kx, ky, kz;
     float Sx, Sy, Sz;
 };
 
+// Best hit so far: t starts at tmax (or +inf when tmax is NaN, which bounds nothing) and
+// id at -1, which compares as the largest unsigned id, so a triangle at exactly tmax is
+// still taken.  (u, v) live in TravStack::uv().
 struct TravHit {
-    float t, u, v;
+    float t;
     int id;
 };
 
@@ -50,10 +59,9 @@ __device__ __forceinline__ float safe_rcp(float d) {
 }
 
 __device__ __forceinline__ void make_trav_ray(TravRay& r, float ox, float oy, float oz, float tmin, float dx,
-                                              float dy, float dz, float tmax) {
+                                              float dy, float dz) {
     r.ox = ox; r.oy = oy; r.oz = oz; r.dx = dx; r.dy = dy; r.dz = dz;
     r.tmin = fmaxf(tmin, 0.0f);  // a negative tmin is treated as 0
-    r.tmax = tmax;
     r.ix = safe_rcp(dx); r.iy = safe_rcp(dy); r.iz = safe_rcp(dz);
     r.oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
     float ad[3] = {fabsf(dx), fabsf(dy), fabsf(dz)};
@@ -195,12 +203,6 @@ __device__ __forceinline__ bool sph_robust(const TravRay& r, float4 c, float rad
     return t >= tmin && t <= tmax;
 }
 
-// Byte k of w as a float: the byte is placed under the exponent of 2^23 (one byte
-// permute) and 2^23 is subtracted (one add) -- exact for 0..255.
-__device__ __forceinline__ float u8f(unsigned w, int k) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + k)) - 8388608.0f;
-}
-
 __device__ __forceinline__ float fmax4(float a, float b, float c, float d) {
     float m;
     asm("max.f32 %0, %1, %2, %3;" : "=f"(m) : "f"(a), "f"(b), "f"(c));
@@ -216,6 +218,25 @@ __device__ __forceinline__ float fmin4(float a, float b, float c, float d) {
 // planes, of 1/d and of the fused plane evaluation, so the quantised-box test never
 // rejects a box the exact ray segment meets.
 constexpr float kBoxSlackMul = 1.0f + 1.0f / (1 << 17);
+
+// Two FP32 values in one 64-bit register pair, for the packed FP32 instructions of sm_100
+// and later (add/fma .f32x2: one issue slot for two values).
+__device__ __forceinline__ unsigned long long f2_pack(unsigned lo, unsigned hi) {
+    unsigned long long v;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(v) : "r"(lo), "r"(hi));
+    return v;
+}
+
+// A child's near and far plane bytes along one axis as exact floats: each byte placed under
+// the exponent of 2^23 (one byte permute each), then 2^23 taken off both with one packed
+// subtraction (exact for 0..255) -- two issue slots fewer per child and axis than two
+// separate subtractions.
+__device__ __forceinline__ void q2(unsigned wn, unsigned wf, int k, unsigned long long off, float& qn, float& qf) {
+    unsigned long long q = f2_pack(__byte_perm(wn, 0x4B000000u, 0x7540u + k),
+                                   __byte_perm(wf, 0x4B000000u, 0x7540u + k));
+    asm("sub.rn.f32x2 %0, %0, %1;" : "+l"(q) : "l"(off));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(qn), "=f"(qf) : "l"(q));
+}
 
 // Intersects the 8 children of node `idx`.  Returns inner-child hits in key order
 // (bit slot^oct) and triangle hits relative to tri_base.
@@ -245,6 +266,7 @@ __device__ __forceinline__ void intersect_node(const Bvh8Node* __restrict__ node
     // 24..31 (key order) and leaf triangles in bits 0..23.
     const unsigned spread_lo = (((imask & 0x0fu) * 0x00204081u) & 0x01010101u) * r.oct;
     const unsigned spread_hi = ((((imask >> 4) & 0x0fu) * 0x00204081u) & 0x01010101u) * r.oct;
+    const unsigned long long off = f2_pack(0x4B000000u, 0x4B000000u);  // 2^23, twice
     unsigned hits = 0;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
@@ -254,14 +276,20 @@ __device__ __forceinline__ void intersect_node(const Bvh8Node* __restrict__ node
         const unsigned meta = half ? (w1.w ^ spread_hi) : (w1.z ^ spread_lo);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const float tnx = fmaf(u8f(lx, k), ax, bx), tfx = fmaf(u8f(hx, k), ax, bx);
-            const float tny = fmaf(u8f(ly, k), ay, by), tfy = fmaf(u8f(hy, k), ay, by);
-            const float tnz = fmaf(u8f(lz, k), az, bz), tfz = fmaf(u8f(hz, k), az, bz);
+            float qnx, qfx, qny, qfy, qnz, qfz;
+            q2(lx, hx, k, off, qnx, qfx);
+            q2(ly, hy, k, off, qny, qfy);
+            q2(lz, hz, k, off, qnz, qfz);
+            const float tnx = fmaf(qnx, ax, bx), tfx = fmaf(qfx, ax, bx);
+            const float tny = fmaf(qny, ay, by), tfy = fmaf(qfy, ay, by);
+            const float tnz = fmaf(qnz, az, bz), tfz = fmaf(qfz, az, bz);
             const float tn = fmax4(tnx, tny, tnz, r.tmin);
             const float tf = fmin4(tfx, tfy, tfz, tcull);
             if (tn <= tf * kBoxSlackMul) {
+                // the slot's bit pattern shifted into place; the funnel shift takes its
+                // amount modulo 32, so the meta byte needs no masking
                 const unsigned m = __byte_perm(meta, 0u, 0x4440u + k);
-                hits |= (m >> 5) << (m & 31u);
+                hits |= __funnelshift_l(0u, m >> 5, m);
             }
         }
     }
@@ -278,7 +306,6 @@ struct TravState {
     unsigned ng_base, ng_hits, ng_imask;  // current node group (hits in key order)
     unsigned tg_base, tg_hits;            // current triangle group
     int sp;
-    float tcull;                          // far limit for boxes: best t * (1 + slack), or tmax
     TravHit hit;
 };
 
@@ -286,24 +313,24 @@ struct TravState {
 constexpr unsigned kTriGroupFlag = 0x80000000u;
 
 // root: index of the BVH's root node (0 for one scene; a scene's offset in a batch arena)
-__device__ __forceinline__ void trav_init(TravState& s, const TravRay& r, unsigned root = 0) {
+__device__ __forceinline__ void trav_init(TravState& s, const TravRay& r, float tmax, unsigned root = 0) {
     s.ng_base = root;
     s.ng_hits = 1u << r.oct;  // a group holding only the root, in slot 0
     s.ng_imask = 1u;
     s.tg_base = 0;
     s.tg_hits = 0;
     s.sp = 0;
-    s.tcull = r.tmax;
-    s.hit.t = INFINITY;
+    s.hit.t = tmax == tmax ? tmax : INFINITY;
     s.hit.id = -1;
-    s.hit.u = s.hit.v = 0.0f;
 }
 
 // Visits the nearest pending child of the current node group.  A full stack drops the
 // remaining group and raises `overflow` (reported to the caller as an error).
+// Boxes are culled beyond the best distance times (1 + cull_slack): a relative margin
+// over the triangle test's rounding, so the answer never depends on what was culled.
 template <bool COUNT>
 __device__ __forceinline__ void trav_node_step(TravState& s, const Bvh8Node* __restrict__ nodes, const TravRay& r,
-                                               TravStack st, TravCount& cnt, int& overflow) {
+                                               TravStack st, TravCount& cnt, int& overflow, float cull_slack) {
     const unsigned key = __ffs(s.ng_hits) - 1;
     s.ng_hits &= s.ng_hits - 1;
     const unsigned slot = key ^ r.oct;
@@ -313,7 +340,7 @@ __device__ __forceinline__ void trav_node_step(TravState& s, const Bvh8Node* __r
         else overflow = 1;
     }
     unsigned cb, im, ih, tb, th;
-    intersect_node(nodes, idx, r, s.tcull, cb, im, ih, tb, th);
+    intersect_node(nodes, idx, r, fmaf(cull_slack, s.hit.t, s.hit.t), cb, im, ih, tb, th);
     if (COUNT) ++cnt.nodes;
     s.ng_base = cb;
     s.ng_imask = im;
@@ -323,13 +350,12 @@ __device__ __forceinline__ void trav_node_step(TravState& s, const Bvh8Node* __r
 }
 
 // Tests the triangles of the current group.  Closest hit: smallest t, equal t to the
-// lowest id; boxes are then culled beyond t * (1 + cull_slack), a relative margin over
-// the triangle test's rounding so the answer never depends on what was culled.
+// lowest id, every candidate bounded by the best distance so far (tmax at first).
 // Returns true when an any-hit query has its answer.
 // SPH: leaf entries with ids from sph_base on are spheres, (centre, id) (radius, 0, 0, 0).
 template <bool ANY, bool WATERTIGHT, bool COUNT, bool SPH = false>
 __device__ __forceinline__ bool trav_tri_step(TravState& s, const float4* __restrict__ tris, const TravRay& r,
-                                              float cull_slack, TravCount& cnt, int id_off = 0,
+                                              TravStack st, TravCount& cnt, int id_off = 0,
                                               int sph_base = 0x7fffffff) {
     while (s.tg_hits) {
         const unsigned k = __ffs(s.tg_hits) - 1;
@@ -338,7 +364,7 @@ __device__ __forceinline__ bool trav_tri_step(TravState& s, const float4* __rest
         const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
         if (COUNT) ++cnt.tris;
         float t, u, v;
-        const float tlim = ANY ? r.tmax : fminf(r.tmax, s.hit.t);
+        const float tlim = s.hit.t;
         bool h;
         if (SPH && __float_as_int(a.w) >= sph_base) {
             h = WATERTIGHT ? sph_robust(r, a, b.x, r.tmin, tlim, t) : sph_ref(r, a, b.x, r.tmin, tlim, t);
@@ -346,17 +372,15 @@ __device__ __forceinline__ bool trav_tri_step(TravState& s, const float4* __rest
             v = 0.0f;
         } else {
             h = WATERTIGHT ? tri_watertight(r, a, b, c, r.tmin, tlim, t, u, v)
-                           : tri_ref(r, a, b, c, r.tmin, r.tmax, tlim, t, u, v);
+                           : tri_ref(r, a, b, c, r.tmin, tlim, tlim, t, u, v);
         }
         if (h) {
             const int id = __float_as_int(a.w) + id_off;  // an instance's first virtual id
-            if (t < s.hit.t || (t == s.hit.t && id < s.hit.id)) {
+            if (t < s.hit.t || (t == s.hit.t && (unsigned)id < (unsigned)s.hit.id)) {
                 s.hit.t = t;
-                s.hit.u = u;
-                s.hit.v = v;
                 s.hit.id = id;
+                st.uv() = make_uint2(__float_as_uint(u), __float_as_uint(v));
                 if (ANY) return true;
-                s.tcull = fminf(r.tmax, fmaf(cull_slack, t, t));
             }
         }
     }

@@ -87,7 +87,7 @@ def test_tuning_does_not_change_results(ctx, batch):
     default = ctx.tuning
     ctx.render_batch(ss, opts)
     ref = _films(ss, opts)
-    for t in ({"trace_block": 64, "trace_pool": 32, "trace_postpone": 1, "shade_block": 128, "trace_regs": 48,
+    for t in ({"trace_block": 64, "trace_pool": 32, "trace_postpone": 1, "shade_block": 128, "trace_regs": 56,
                "wave_paths": 1 << 16},
               {"trace_block": 256, "trace_pool": 256, "trace_postpone": 10, "shade_block": 512, "trace_regs": 64,
                "wave_paths": 1 << 20}):

@@ -222,7 +222,7 @@ def test_autotune_trace_keeps_results(ctx, gpu_soup_1m):
     gpu_soup_1m.trace_raw(rays, hits)
     ref = hits.cpu().numpy().view(np.int32).copy()
     t, ms = gpu_soup_1m.autotune_trace(rays)
-    assert ms > 0 and t == ctx.tuning and t["trace_block"] in (64, 128, 256) and t["trace_regs"] in (48, 64)
+    assert ms > 0 and t == ctx.tuning and t["trace_block"] in (64, 128, 256) and t["trace_regs"] in (56, 64)
     gpu_soup_1m.trace_raw(rays, hits)
     np.testing.assert_array_equal(hits.cpu().numpy().view(np.int32), ref)
     ctx.tuning = default

@@ -86,3 +86,39 @@ def test_noalloc_rejects_host_arrays(noalloc_ctx):
     out = np.empty_like(img)
     st = salty_gb300.lib().salty_tonemap_noalloc(ctx.h, None, 0, 8, 8, img.ctypes.data, out.ctypes.data, None, 1)
     assert st == salty_gb300.ERR_INVALID_ARG
+
+
+def test_noalloc_on_the_callers_stream_allocates_nothing(noalloc_ctx):
+    """The pattern such a caller uses: the image produced on its own stream, the call
+    enqueued on that same stream (no extra synchronisation), and device memory unchanged
+    across the calls once the first call has looked up the scratch array."""
+    import torch
+    import salty_gb300
+    ctx = noalloc_ctx
+    h, w = 540, 960
+    img = _image(7, h, w)
+    ref_out, ref_s8, _, _ = ctx.tonemap(img, 0, srgb=True, ref_oetf=True)
+    s = torch.cuda.Stream()
+    host = torch.from_numpy(img).pin_memory()
+    with torch.cuda.stream(s):
+        d_img = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
+        d_out = torch.empty_like(d_img)
+        d_s8 = torch.empty((h, w, 3), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    L = salty_gb300.lib()
+    ctx.check(L.salty_tonemap_noalloc(ctx.h, s.cuda_stream, 0, w, h, d_img.data_ptr(), d_out.data_ptr(),
+                                      d_s8.data_ptr(), 1), "tonemap_noalloc")  # warm call
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(2):
+        with torch.cuda.stream(s):
+            d_out.zero_()
+            d_img.copy_(host, non_blocking=True)
+        ctx.check(L.salty_tonemap_noalloc(ctx.h, s.cuda_stream, 0, w, h, d_img.data_ptr(), d_out.data_ptr(),
+                                          d_s8.data_ptr(), 1), "tonemap_noalloc")
+        s.synchronize()
+        np.testing.assert_allclose(d_out.cpu().numpy(), ref_out, rtol=2e-5, atol=1e-7)
+        d = np.abs(d_s8.cpu().numpy().astype(int) - ref_s8.astype(int))
+        assert d.max() <= 1 and (d > 0).mean() < 0.01
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
