@@ -867,7 +867,7 @@ def main():
     for _ in range(args.steps):
         s = scene.trace_raw(rays_h, hits_h, any_hit=any_hit)
         h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
-        e2e_kernels += math.ceil(n_rays / (1 << 21))
+        e2e_kernels += s["launches"]
     e3.record()
     torch.cuda.synchronize()
     barrier(pg)

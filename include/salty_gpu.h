@@ -267,6 +267,7 @@ typedef struct salty_trace_stats {
     int64_t node_fetches;    /* SALTY_TRACE_COUNTERS only */
     int64_t tri_fetches;     /* SALTY_TRACE_COUNTERS only */
     int64_t h2d_bytes, d2h_bytes;
+    int64_t launches;        /* traversal kernel launches of the call */
 } salty_trace_stats;
 /* Statistics of the last salty_trace on this context. */
 salty_status salty_last_trace_stats(const salty_ctx* ctx, salty_trace_stats* out);

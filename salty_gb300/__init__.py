@@ -87,7 +87,7 @@ class BvhInfo(C.Structure):
 class TraceStats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("total_ms", C.c_double), ("rays", C.c_int64),
                 ("node_fetches", C.c_int64), ("tri_fetches", C.c_int64), ("h2d_bytes", C.c_int64),
-                ("d2h_bytes", C.c_int64)]
+                ("d2h_bytes", C.c_int64), ("launches", C.c_int64)]
 
 
 class RenderOpts(C.Structure):

@@ -455,6 +455,7 @@ salty_status salty_trace(salty_ctx* ctx, salty_scene* sc, const salty_ray* rays,
         SALTY_TRY_CUDA(E, cudaEventRecord(k0, st));
         SALTY_TRY(trace_launch(ctx, sc, (const float4*)rays, n, nullptr, flags, (float4*)hits, ctx->counters.p, st,
                                ctx->status.p));
+        stats.launches = 1;
         SALTY_TRY_CUDA(E, cudaEventRecord(k1, st));
         SALTY_TRY_CUDA(E, cudaMemcpyAsync(counts, ctx->counters.p, sizeof counts, cudaMemcpyDeviceToHost, st));
         SALTY_TRY_CUDA(E, cudaEventRecord(t1, st));
@@ -486,6 +487,7 @@ salty_status salty_trace(salty_ctx* ctx, salty_scene* sc, const salty_ray* rays,
                 stats.h2d_bytes += m * (int64_t)sizeof(salty_ray);
             }
             SALTY_TRY(trace_launch(ctx, sc, rin, m, nullptr, flags, hout, ctx->counters.p + 4 * s, ss[s], ctx->status.p));
+            ++stats.launches;
             if (!dout) {
                 SALTY_TRY_CUDA(E, cudaMemcpyAsync(hits + b, hb, (size_t)m * sizeof(salty_hit), cudaMemcpyDefault, ss[s]));
                 stats.d2h_bytes += m * (int64_t)sizeof(salty_hit);

@@ -5,16 +5,17 @@ estimator) against the reference's own render of it (tests/golden/cornell_c1_ref
 Bar: the frame is cut into 8x8-pixel blocks; a block's mean has a near-normal error
 (64 pixels' worth of samples), so its z-score z = (a - b) / sqrt(va + vb) follows the
 normal law closely, unlike a single pixel's at a few hundred samples (a pixel's variance
-estimate is itself noisy and its error heavy-tailed).  Required: at most 1% of block
-channels beyond 3 sigma (a normal variable: 0.27%), none beyond 5.5 sigma, and the whole
-frame's mean within 4 standard errors.
+estimate is itself noisy and its error heavy-tailed).  Required: the count of block
+channels beyond 3 sigma within the binomial bound of a normal variable (0.27 %, plus four
+standard deviations of that count: conftest.beyond3_bound), none beyond 5.5 sigma, and
+the whole frame's mean within 4 standard errors.
 """
 import os
 
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, beyond3_bound
 
 BLOCK = 8
 
@@ -35,8 +36,8 @@ def check_against_reference(mean, var):
     g, gm, gv = _fixture()
     n = BLOCK * BLOCK
     zb = (_blocks(mean) - _blocks(gm)) / np.sqrt((_blocks(var) + _blocks(gv)) / n + 1e-30)
-    frac, zmax = np.mean(np.abs(zb) > 3), np.max(np.abs(zb))
-    assert frac < 0.01 and zmax < 5.5, (frac, zmax)
+    k, zmax = int(np.count_nonzero(np.abs(zb) > 3)), float(np.max(np.abs(zb)))
+    assert k <= beyond3_bound(zb.size) and zmax < 5.5, (k, zb.size, zmax)
     se = np.sqrt(var.sum() + gv.sum()) / mean.size
     assert abs(mean.mean() - gm.mean()) < 4 * se, (mean.mean(), gm.mean(), se)
 

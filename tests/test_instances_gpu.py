@@ -13,7 +13,7 @@ import math
 import numpy as np
 import pytest
 
-from test_render_gpu import zstats
+from test_render_gpu import zcheck
 
 pytestmark = pytest.mark.gpu
 
@@ -140,8 +140,7 @@ def test_instanced_render_matches_flattened(scenes_pair, profile):
     W, H, spp = 48, 32, 512
     ra = a.render(W, H, spp, 6, rr_depth=3, profile=profile, seed=31)
     rb = b.render(W, H, spp, 6, rr_depth=3, profile=profile, seed=32)
-    frac, zmax = zstats(ra["mean"], ra["var"], rb["mean"], rb["var"])
-    assert frac < 0.01 and zmax < 6, (frac, zmax)
+    zcheck(ra["mean"], ra["var"], rb["mean"], rb["var"])
     assert abs(ra["mean"].mean() / rb["mean"].mean() - 1) < 0.01
 
 

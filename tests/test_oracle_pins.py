@@ -11,17 +11,13 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, assert_agree
 
 SOUP_SEED, RAY_SEED = 20260001, 20260002
 
 
 def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
-
-
-def zscores(mean_a, var_a, mean_b, var_b):
-    return (mean_a - mean_b) / np.sqrt(np.maximum(var_a + var_b, 1e-30))
 
 
 def test_generators_reproduce_fixture_inputs(oracle):
@@ -130,10 +126,8 @@ def test_oracle_compat_render_matches_reference_fixture(oracle):
                             profile=PROFILE_COMPAT, seed=777)
     m = tot / spp
     v = np.maximum((sq / spp - m * m) * spp / (spp - 1) / spp, 0)
-    z = zscores(m, v, g["mean"], g["var"])
-    # 3-sigma per pixel: at most ~1% of pixel-channels outside, none beyond 6 sigma
-    assert np.mean(np.abs(z) > 3) < 0.01
-    assert np.max(np.abs(z)) < 6
+    # 3-sigma per pixel (conftest.assert_within_3_sigma), none beyond 6 sigma
+    assert_agree(m, v, g["mean"], g["var"])
     assert abs(m.mean() / g["mean"].mean() - 1) < 0.01
 
 
@@ -159,9 +153,7 @@ def test_oracle_compat_variants_match_reference_fixtures(oracle, variant, fixtur
                             profile=PROFILE_COMPAT, seed=seed)
     m = tot / spp
     v = np.maximum((sq / spp - m * m) * spp / (spp - 1) / spp, 0)
-    z = zscores(m, v, g["mean"], g["var"])
-    assert np.mean(np.abs(z) > 3) < 0.01
-    assert np.max(np.abs(z)) < 6
+    assert_agree(m, v, g["mean"], g["var"])
     assert abs(m.mean() / g["mean"].mean() - 1) < 0.01
 
 
@@ -179,8 +171,7 @@ def test_oracle_physical_glossy_is_consistent(oracle):
         m = tot / 256
         res.append((m, np.maximum((sq / 256 - m * m) * 256 / 255 / 256, 0)))
     assert all(np.all(np.isfinite(m)) for m, _ in res)
-    z = zscores(res[0][0], res[0][1], res[1][0], res[1][1])
-    assert np.mean(np.abs(z) > 3) < 0.015 and np.max(np.abs(z)) < 6
+    assert_agree(res[0][0], res[0][1], res[1][0], res[1][1])
 
 
 def test_oracle_tonemap_matches_reference_fixture(oracle):
@@ -217,5 +208,4 @@ def test_oracle_physical_render_is_consistent(oracle):
         tot, sq = oracle.render(sd, 32, 32, 256, 8, profile=PROFILE_PHYSICAL, seed=seed)
         m = tot / 256
         res.append((m, np.maximum((sq / 256 - m * m) * 256 / 255 / 256, 0)))
-    z = zscores(res[0][0], res[0][1], res[1][0], res[1][1])
-    assert np.mean(np.abs(z) > 3) < 0.02
+    assert_agree(res[0][0], res[0][1], res[1][0], res[1][1])

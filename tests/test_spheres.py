@@ -15,7 +15,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, assert_within_3_sigma
 
 
 def _oracle_scene(sc):
@@ -25,10 +25,12 @@ def _oracle_scene(sc):
                      ibl=sc.get("ibl"), spheres=sc.get("spheres", []))
 
 
-def _zstats(ma, va, mb, vb):
+def _zcheck(ma, va, mb, vb):
+    """Per pixel-channel z-scores and the image means against the 3-sigma bounds."""
+    ma, va, mb, vb = (np.asarray(x, float) for x in (ma, va, mb, vb))
     floor = (1e-5 * np.maximum(np.abs(ma), np.abs(mb))) ** 2
-    z = (ma - mb) / np.sqrt(np.maximum(va + vb + floor, 1e-30))
-    return np.mean(np.abs(z) > 3), np.max(np.abs(z))
+    v = np.maximum(va + vb + floor, 1e-30)
+    assert_within_3_sigma((ma - mb) / np.sqrt(v), zsum=float((ma - mb).sum() / np.sqrt(v.sum())))
 
 
 def test_oracle_compat_spheres_match_reference_fixture(oracle):
@@ -39,8 +41,7 @@ def test_oracle_compat_spheres_match_reference_fixture(oracle):
     tot, sq = oracle.render(_oracle_scene(scenes.cornell("spheres")), int(g["width"]), int(g["height"]), spp,
                             int(g["max_bounce"]), profile=PROFILE_COMPAT, seed=99)
     m = tot / spp
-    frac, zmax = _zstats(m, np.maximum((sq / spp - m * m) / (spp - 1), 0), g["mean"], g["var"])
-    assert frac < 0.01 and zmax < 6, (frac, zmax)
+    _zcheck(m, np.maximum((sq / spp - m * m) / (spp - 1), 0), g["mean"], g["var"])
 
 
 # ---------------------------------------------------------------- GPU
@@ -142,8 +143,7 @@ def test_compat_spheres_match_reference_fixture(ctx):
     r = s.render(int(g["width"]), int(g["height"]), int(g["spp"]), int(g["max_bounce"]),
                  profile=salty_gb300.PROFILE_COMPAT, seed=4545)
     s.close()
-    frac, zmax = _zstats(r["mean"], r["var"], g["mean"], g["var"])
-    assert frac < 0.01 and zmax < 6, (frac, zmax)
+    _zcheck(r["mean"], r["var"], g["mean"], g["var"])
     assert abs(r["mean"].mean() / g["mean"].mean() - 1) < 0.01
 
 
@@ -161,8 +161,7 @@ def test_physical_spheres_match_oracle(ctx, oracle):
     s.close()
     tot, sq = oracle.render(_oracle_scene(sc), W, H, spp, 8, rr_depth=3, profile=PROFILE_PHYSICAL, seed=1235)
     m = tot / spp
-    frac, zmax = _zstats(r["mean"], r["var"], m, np.maximum((sq / spp - m * m) / (spp - 1), 0))
-    assert frac < 0.01 and zmax < 6, (frac, zmax)
+    _zcheck(r["mean"], r["var"], m, np.maximum((sq / spp - m * m) / (spp - 1), 0))
 
 
 @pytest.mark.gpu
