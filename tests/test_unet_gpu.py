@@ -3,8 +3,11 @@ rounding at the same points (oracle/unet_oracle.py).
 
 Tolerances: the two differ only by FP32 (tensor-core) vs FP64 accumulation order, which
 now and then moves a BF16 rounding by one step (2^-8 relative); those differences
-propagate, so outputs are compared at 2% relative L2 and gradients per layer at 5%
-relative L2 with a cosine similarity above 0.998.
+propagate.  Outputs are compared at 0.5 % relative L2 (measured on the GB300: at most
+0.09 %); per-layer gradients of a 1 x 48 x 272 batch at 2.5 % relative L2 with a cosine
+similarity above 0.9995 (measured: at most 1.7 %, at least 0.99986), and of the tiny
+2 x 32 x 32 batch, whose small gradients carry relatively more rounding, at 5 % and 0.999
+(measured: at most 3.4 %, at least 0.99945).
 """
 import numpy as np
 import pytest
@@ -48,7 +51,7 @@ def test_forward_matches_oracle(net):
     out = net.forward(f)
     want, _ = UnetOracle(net.params()).forward(f)
     assert out.shape == (2, 32, 32, 3)
-    assert _rel(out, want) < 0.02, _rel(out, want)
+    assert _rel(out, want) < 0.005, _rel(out, want)
 
 
 def test_gradients_match_oracle(net):
@@ -65,7 +68,7 @@ def test_gradients_match_oracle(net):
         n = 9 * ci * co + co
         a, b = g[o:o + n], go[o:o + n]
         cos = a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
-        assert _rel(a, b) < 0.05 and cos > 0.998, (i, _rel(a, b), cos)
+        assert _rel(a, b) < 0.05 and cos > 0.999, (i, _rel(a, b), cos)
         o += n
 
 
@@ -202,7 +205,7 @@ def test_conv_kernels_match_oracle_on_ragged_strips(ctx, kind):
     orc = UnetOracle(p0)
     out = net.forward(f)
     want, _ = orc.forward(f)
-    assert _rel(out, want) < 0.02, _rel(out, want)
+    assert _rel(out, want) < 0.005, _rel(out, want)
     loss = net.train_step(f, t, lr=0.0)
     lo, go = orc.loss_and_grads(f, t)
     assert abs(loss / lo - 1) < 1e-2, (loss, lo)
@@ -212,7 +215,7 @@ def test_conv_kernels_match_oracle_on_ragged_strips(ctx, kind):
         n = 9 * ci * co + co
         a, b = g[o:o + n], go[o:o + n]
         cos = a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
-        assert _rel(a, b) < 0.05 and cos > 0.998, (i, _rel(a, b), cos)
+        assert _rel(a, b) < 0.025 and cos > 0.9995, (i, _rel(a, b), cos)
         o += n
     net.close()
 
