@@ -29,9 +29,10 @@ constexpr long long kMaxLaunchRays = 1ll << 30;
 // is set through the resident blocks asked for: 1024 / TB caps registers at 64 per thread,
 // CAP's 1152 / TB at 56 for blocks of up to 128 threads (36 instead of 32 warps per SM to
 // hide fetch latency, at the price of a few spilled values; 256-thread blocks stay at 64).
-// The short stack lives in dynamic shared memory, `depth` entries per thread (two per BVH
-// level plus one) and one more for the best hit's (u, v), so shallow trees leave room for
-// more resident blocks.
+// The short stack lives in dynamic shared memory, `depth` entries per thread (one per BVH
+// level plus one, or two per level plus one with postponing or instances; trace_launch
+// sizes it) and one more for the best hit's (u, v), so shallow trees leave room for more
+// resident blocks.
 // Stack entry (.y) that marks where a ray entered an instance.
 constexpr unsigned kInstMarker = 0x40000000u;
 
