@@ -1165,26 +1165,37 @@ salty_status salty_denoise_unet_ensemble(salty_ctx* ctx, salty_unet* net, salty_
     const int Wp = (W + 15) / 16 * 16, Hp = (H + 15) / 16 * 16;
     SALTY_TRY(check_shape(ctx, 1, Hp, Wp));
     const long long npx = (long long)W * H, npp = (long long)Wp * Hp;
+    // The symmetries run as batches of images of one shape: the mirror images (up to 4) in
+    // one forward pass, their transposes in a second -- each convolution launch then has
+    // that many times more strips to spread over the SMs.  An image's outputs do not depend
+    // on the batch it runs in (tests/test_unet_gpu.py), and the images are added to the
+    // result in the order k = 0..mirrors-1, as one pass per image would add them.
+    const int per = mirrors < 4 ? mirrors : 4;
+    SALTY_TRY(check_shape(ctx, per, Hp, Wp));
     // [mean 3 | var 3 | albedo 3 | normal 3 | depth 1] per film pixel, then features, then the image
-    SALTY_TRY_CUDA(ctx->err, u.film_ws.ensure((size_t)(npx * 16 + npp * kFeatures)));
+    SALTY_TRY_CUDA(ctx->err, u.film_ws.ensure((size_t)(npx * 16 + per * npp * kFeatures)));
     float* mean = u.film_ws.p;
     float* var = mean + npx * 3;
     float* alb = var + npx * 3;
     float* nrm = alb + npx * 3;
     float* dep = nrm + npx * 3;
     float* feat = dep + npx;
-    float* img = feat + npp * kFeatures;
+    float* img = feat + per * npp * kFeatures;
     SALTY_TRY(film_features(ctx, scene, mean, var, alb, nrm, dep));
     SALTY_TRY(conv_status_reset(ctx));
-    for (int k = 0; k < mirrors; ++k) {
-        k_pack_features<<<gsz(npp), 256, 0, ctx->stream>>>(mean, var, alb, nrm, dep, W, H, Wp, Hp, k, feat);
+    for (int k0 = 0; k0 < mirrors; k0 += per) {
+        for (int j = 0; j < per; ++j)
+            k_pack_features<<<gsz(npp), 256, 0, ctx->stream>>>(mean, var, alb, nrm, dep, W, H, Wp, Hp, k0 + j,
+                                                               feat + j * npp * kFeatures);
         Fwd F;
-        if (k & 4)
-            SALTY_TRY(forward(ctx, u, feat, 1, Wp, Hp, F));  // the transposed frame: Hp wide, Wp tall
+        if (k0 & 4)
+            SALTY_TRY(forward(ctx, u, feat, per, Wp, Hp, F));  // the transposed frames: Hp wide, Wp tall
         else
-            SALTY_TRY(forward(ctx, u, feat, 1, Hp, Wp, F));
-        k_output_flipped<<<gsz(npx), 256, 0, ctx->stream>>>(F.t[T_OUT], F.t[T_X], W, H, Wp, Hp, k,
-                                                           1.0f / (float)mirrors, k == 0, img);
+            SALTY_TRY(forward(ctx, u, feat, per, Hp, Wp, F));
+        for (int j = 0; j < per; ++j)
+            k_output_flipped<<<gsz(npx), 256, 0, ctx->stream>>>(F.t[T_OUT] + j * npp * 8, F.t[T_X] + j * npp * 16, W,
+                                                               H, Wp, Hp, k0 + j, 1.0f / (float)mirrors,
+                                                               k0 + j == 0, img);
     }
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     SALTY_TRY_CUDA(ctx->err, cudaMemcpyAsync(out_rgb, img, (size_t)npx * 3 * sizeof(float), cudaMemcpyDefault,

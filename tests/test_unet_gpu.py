@@ -72,6 +72,22 @@ def test_gradients_match_oracle(net):
         o += n
 
 
+@pytest.mark.parametrize("kind", ["tcgen05", "tcgen05_cp_async", "mma_sync"])
+def test_an_image_gives_the_same_output_in_any_batch(ctx, kind):
+    """Each image of a batch goes through its own strips, borders and pooling windows, so
+    its output is the same bit for bit alone or in a batch -- the film ensemble runs its
+    mirror images as one batch on that ground."""
+    import salty_gb300
+    net = salty_gb300.Unet(ctx, seed=15)
+    net.set_conv_kernel({"tcgen05": salty_gb300.CONV_TCGEN05, "tcgen05_cp_async": salty_gb300.CONV_TCGEN05_CP_ASYNC,
+                         "mma_sync": salty_gb300.CONV_MMA_SYNC}[kind])
+    f, _ = _batch(16, n=3, h=48, w=272)
+    both = net.forward(f)
+    for i in range(3):
+        np.testing.assert_array_equal(net.forward(f[i:i + 1])[0], both[i])
+    net.close()
+
+
 def test_weight_gradient_kernels_agree(ctx):
     """The tensor-core weight gradient (tcgen05, partial sums per CTA added in a fixed
     order) against the mma.sync one, layer by layer: the two differ only by FP32 summation
