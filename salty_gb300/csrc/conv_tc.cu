@@ -30,7 +30,9 @@
 //             chunk the halo (a box of 16 channels x 130 pixels x R+2 rows, the image
 //             border zero-filled by the copy engine) and the weights (16 channels x Npad
 //             rows x 9 taps) into a ring of up to 4 stages, each guarded by a "full"
-//             (transaction bytes) and an "empty" (MMAs done) mbarrier.  Both land in the
+//             (transaction bytes) and an "empty" (MMAs done) mbarrier.  A layer whose
+//             weights fit in 48 KB has them copied once, before the first strip, into a
+//             region of their own (its own mbarrier), and its stages hold only halos.  Both land in the
 //             tensor core's 32-byte-swizzled K-major layout: one 32-byte row per pixel (or
 //             weight row), the two 16-byte halves of a row exchanged where address bit 7 is
 //             set.  The MMA unit undoes the exchange from the absolute shared-memory
@@ -288,6 +290,7 @@ constexpr int kMaxStages = 4;
 constexpr int kTmaMmaWarps = 8;
 constexpr int kTmaHeader = 2048;   // barriers, TMEM address, abort flag, bias
 constexpr int kTmaMinSmem = 120 * 1024;  // above half an SM's shared memory: one CTA per SM owns all 512 TMEM columns
+constexpr int kResidentMaxBytes = 48 * 1024;  // weights kept resident up to this size
 
 __host__ __device__ constexpr int tma_halo(int R) { return ((R + 2) * kHaloW * 32 + 1023) / 1024 * 1024; }
 __host__ __device__ constexpr int tma_wts(int npad) { return (9 * npad * 32 + 1023) / 1024 * 1024; }
@@ -303,6 +306,7 @@ __device__ __forceinline__ uint64_t sdesc_sw32(uint32_t addr) {
 struct TmaConvArgs {
     int cin, npad, R, cout, relu, out_cs, out_co;
     int N, H, W, tiles, stages;
+    int resident, wres;  // weights staged once for the whole kernel; bytes reserved for them
     const float* bias;
     bf16* out;
     int* status;
@@ -352,10 +356,12 @@ k_conv3x3_tma(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__
     uint64_t* empty = full + kMaxStages;                 // [kMaxStages]
     uint64_t* acc_full = empty + kMaxStages;             // [2]
     uint64_t* acc_empty = acc_full + 2;                  // [2]
+    uint64_t* wbar = acc_empty + 2;                      // resident weights landed
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 128);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 132);
     float* sbias = reinterpret_cast<float*>(smem + 256);  // [npad]
-    unsigned char* ring = smem + kTmaHeader;
+    unsigned char* wres = smem + kTmaHeader;
+    unsigned char* ring = smem + kTmaHeader + a.wres;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // TMA destinations and the descriptors below assume a 1024-byte aligned base
     if (saddr(smem) & 1023u) {
@@ -363,8 +369,8 @@ k_conv3x3_tma(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__
         return;
     }
     const int R = a.R, npad = a.npad, S = a.stages;
-    const int hbytes = tma_halo(R), sbytes = tma_stage(R, npad);
-    const uint32_t tx_bytes = (uint32_t)(R + 2) * kHaloW * 32u + 9u * npad * 32u;
+    const int hbytes = tma_halo(R), sbytes = a.resident ? tma_halo(R) : tma_stage(R, npad);
+    const uint32_t tx_bytes = (uint32_t)(R + 2) * kHaloW * 32u + (a.resident ? 0u : 9u * npad * 32u);
     const int nchunks = a.cin / 16;
     const int strips_x = (a.W + kStrip - 1) / kStrip, strips_y = (a.H + R - 1) / R;
     if (tid == 0) {
@@ -376,6 +382,7 @@ k_conv3x3_tma(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__
             mbar_init(saddr(acc_full + b), MW);
             mbar_init(saddr(acc_empty + b), 4);  // one arrival per epilogue warp
         }
+        mbar_init(saddr(wbar), 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -393,6 +400,12 @@ k_conv3x3_tma(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__
         if (lane == 0) {
             asm volatile("prefetch.tensormap [%0];" :: "l"(reinterpret_cast<uint64_t>(&tm_in)) : "memory");
             asm volatile("prefetch.tensormap [%0];" :: "l"(reinterpret_cast<uint64_t>(&tm_w)) : "memory");
+            // resident weights: every chunk's nine taps once, before the first strip
+            if (a.resident) {
+                mbar_expect_tx(saddr(wbar), (uint32_t)nchunks * 9u * npad * 32u);
+                for (int c = 0; c < nchunks; ++c)
+                    tma_load_3d(saddr(wres) + c * 9 * npad * 32, &tm_w, c * 16, 0, 0, saddr(wbar));
+            }
             int k = 0;
             for (int t = blockIdx.x; t < a.tiles; t += gridDim.x) {
                 int tt = t;
@@ -410,14 +423,14 @@ k_conv3x3_tma(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__
                     mbar_expect_tx(bar, tx_bytes);
                     const uint32_t dst = saddr(ring + s * sbytes);
                     tma_load_4d(dst, &tm_in, c * 16, x0 - 1, y0 - 1, n, bar);
-                    tma_load_3d(dst + hbytes, &tm_w, c * 16, 0, 0, bar);
+                    if (!a.resident) tma_load_3d(dst + hbytes, &tm_w, c * 16, 0, 0, bar);
                 }
                 if (!ok) break;
             }
         }
     } else if (warp <= MW) {
         const int m = warp - 1;
-        if (lane == 0) {
+        if (lane == 0 && (!a.resident || wait_or_abort(saddr(wbar), 0u, abort_flag, a.status))) {
             const uint32_t idesc = idesc_bf16(kStrip, npad);
             int k = 0, i = 0;
             for (int t = blockIdx.x; t < a.tiles; t += gridDim.x, ++i) {
@@ -430,7 +443,8 @@ k_conv3x3_tma(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__
                     const int s = k % S;
                     if (!wait_or_abort(saddr(full + s), (uint32_t)(k / S) & 1u, abort_flag, a.status)) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t hs = saddr(ring + s * sbytes), ws = hs + hbytes;
+                    const uint32_t hs = saddr(ring + s * sbytes);
+                    const uint32_t ws = a.resident ? saddr(wres) + c * 9 * npad * 32 : hs + hbytes;
                     for (int tap = 0; tap < 9; ++tap) {
                         const int ky = tap / 3, kx = tap - ky * 3;
                         const uint64_t bd = sdesc_sw32(ws + tap * npad * 32);
@@ -746,11 +760,15 @@ salty_status conv3x3_tma(salty_ctx* ctx, const bf16* in, int in_cs, int cin, con
     EncodeTiledFn enc = tensor_map_encoder();
     if (!enc) return ctx->err.fail(SALTY_ERR_CUDA, "conv3x3_tma: cuTensorMapEncodeTiled is not available");
     const int R = conv_tc_rows(cout);
-    const int sbytes = tma_stage(R, npad);
-    int S = (int)((227 * 1024 - kTmaHeader) / sbytes);
+    // the layer's weights stay in shared memory for the whole kernel when they are small
+    const int wbytes = (cin / 16) * 9 * npad * 32;
+    const bool resident = wbytes <= kResidentMaxBytes;
+    const int wres = resident ? (wbytes + 1023) / 1024 * 1024 : 0;
+    const int sbytes = resident ? tma_halo(R) : tma_stage(R, npad);
+    int S = (int)((227 * 1024 - kTmaHeader - wres) / sbytes);
     if (S > kMaxStages) S = kMaxStages;
     if (S < 2) return ctx->err.fail(SALTY_ERR_INVALID_ARG, "conv3x3_tma: stage too large");
-    size_t smem = (size_t)kTmaHeader + (size_t)S * sbytes;
+    size_t smem = (size_t)kTmaHeader + wres + (size_t)S * sbytes;
     if (smem < (size_t)kTmaMinSmem) smem = kTmaMinSmem;
     // input: 4-D (channels, x, y, image), boxes of 16 channels x 130 pixels x R + 2 rows
     CUtensorMap tm_in, tm_w;
@@ -774,7 +792,8 @@ salty_status conv3x3_tma(salty_ctx* ctx, const bf16* in, int in_cs, int cin, con
     SALTY_TRY_CUDA(ctx->err, cudaFuncSetAttribute(k_conv3x3_tma<MW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long tiles = (long long)N * ((H + R - 1) / R) * ((W + kStrip - 1) / kStrip);
     const int grid = (int)(tiles < ctx->num_sms ? tiles : ctx->num_sms);
-    TmaConvArgs a{cin, npad, R, cout, relu, out_cs, out_co, N, H, W, (int)tiles, S, bias, out, d_status};
+    TmaConvArgs a{cin, npad, R, cout, relu, out_cs, out_co, N, H, W, (int)tiles, S, resident ? 1 : 0, wres, bias, out,
+                  d_status};
     k_conv3x3_tma<MW><<<grid, tma_threads(MW), smem, ctx->stream>>>(tm_in, tm_w, a);
     SALTY_TRY_CUDA(ctx->err, cudaGetLastError());
     return SALTY_OK;

@@ -30,7 +30,7 @@ def _const(src, name):
 def k():
     s = _src("conv_tc.cu")
     c = {n: _const(s, n) for n in ("kTcThreads", "kStrip", "kTmemCols", "kBarBytes", "kMaxStages", "kTmaMmaWarps",
-                                   "kTmaHeader", "kTmaMinSmem")}
+                                   "kTmaHeader", "kTmaMinSmem", "kResidentMaxBytes")}
     c["kHaloW"] = c["kStrip"] + 2
     return c
 
@@ -100,10 +100,15 @@ def test_tma_kernel_layout(k, launches):
         R, npad = rows(k, cout)
         halo = ((R + 2) * k["kHaloW"] * 32 + 1023) // 1024 * 1024
         wts = (9 * npad * 32 + 1023) // 1024 * 1024
-        stage = halo + wts
-        S = min(k["kMaxStages"], (SMEM_MAX - k["kTmaHeader"]) // stage)
+        # weights resident for the whole kernel when they fit, then the stages hold halos only
+        wbytes = cin // 16 * 9 * npad * 32
+        resident = wbytes <= k["kResidentMaxBytes"]
+        wres = (wbytes + 1023) // 1024 * 1024 if resident else 0
+        stage = halo if resident else halo + wts
+        S = min(k["kMaxStages"], (SMEM_MAX - k["kTmaHeader"] - wres) // stage)
         assert S >= 2, (kind, cin, cout)
-        smem = max(k["kTmaHeader"] + S * stage, k["kTmaMinSmem"])
+        smem = max(k["kTmaHeader"] + wres + S * stage, k["kTmaMinSmem"])
+        assert wres % 1024 == 0 and wbytes < 1 << 20  # TMA destination alignment, transaction count
         assert smem <= SMEM_MAX and smem > SMEM_SM // 2  # one CTA per SM
         assert stage % 1024 == 0 and k["kTmaHeader"] % 1024 == 0  # swizzle-pattern alignment of every TMA destination
         # TMA boxes: halo 16 ch x 130 px x (R + 2) rows, weights 16 ch x npad rows x 9 taps
@@ -114,8 +119,12 @@ def test_tma_kernel_layout(k, launches):
         # A rows in 32-byte steps: the last tap of the last row stays in the halo tile
         assert ((R - 1 + 2) * k["kHaloW"] + 2) * 32 + k["kStrip"] * 32 <= (R + 2) * k["kHaloW"] * 32
         assert 8 * npad * 32 + npad * 32 <= wts
-        # two accumulators and the bias table
+        # a resident chunk's nine taps at c * 9 * npad * 32, within the resident region
+        assert not resident or (cin // 16) * 9 * npad * 32 <= wres
+        # two accumulators and the bias table; nine mbarriers (full, empty x 4 stages, the
+        # accumulators' pairs, the resident weights) before the TMEM address at byte 128
         assert 2 * R * npad <= 512 and 256 + 4 * npad <= k["kTmaHeader"]
+        assert (2 * k["kMaxStages"] + 4 + 1) * 8 <= 128
         # every strip row has an issuing warp (rows r = m, m + MW, ...)
         assert k["kTmaMmaWarps"] >= 1 and 32 * (k["kTmaMmaWarps"] + 5) <= 1024
 
