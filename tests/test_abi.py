@@ -86,3 +86,39 @@ def test_header_is_plain_c99_and_links(salty_lib, tmp_path):
                         f"-Wl,-rpath,{libdir}", "-o", exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert subprocess.run([exe]).returncode == 0
+
+
+def test_python_structs_match_the_header_layout(salty_lib, tmp_path):
+    """Every ctypes mirror of a header struct has the C struct's size and each field its
+    offset, as a C compiler lays them out (a field added on one side only would make the
+    library read past the caller's struct)."""
+    import ctypes
+    import shutil
+    import salty_gb300 as S
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    pairs = [("salty_material", S.Material), ("salty_camera", S.Camera), ("salty_scene_desc", S.SceneDesc),
+             ("salty_texture", S.Texture), ("salty_instance", S.Instance), ("salty_sphere", S.Sphere),
+             ("salty_build_opts", S.BuildOpts), ("salty_bvh_info", S.BvhInfo),
+             ("salty_trace_stats", S.TraceStats), ("salty_render_opts", S.RenderOpts),
+             ("salty_render_stats", S.RenderStats), ("salty_mesh", S.Mesh), ("salty_tuning", S.Tuning)]
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "salty_gpu.h"', "int main(void) {"]
+    for cname, cls in pairs:
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'    printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "layout")
+    r = subprocess.run(["gcc", "-std=c99", f"-I{os.path.join(ROOT, 'include')}", str(src), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = {}
+    for line in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.splitlines():
+        name, field, value = line.split()
+        got[(name, field)] = int(value)
+    for cname, cls in pairs:
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
