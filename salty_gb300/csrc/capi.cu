@@ -15,9 +15,7 @@ struct V3 {
     float x, y, z;
 };
 inline V3 v3(const float* p) { return {p[0], p[1], p[2]}; }
-inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 inline V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-inline V3 scl(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
 inline V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
 // Vector3::UnitVector (include/s3d_math.h:830-842)
 inline V3 unit(V3 v) {
